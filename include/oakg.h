@@ -1,0 +1,151 @@
+/*
+ * oakg.h -- C ABI of the GB300 (sm_103a) local ensemble square-root analysis.
+ *
+ * Drop-in boundary for OAK's analysis path (gher-uliege/OAK 1.7). Two groups of entry points:
+ *
+ *  1. OAK's existing C interface, same names and signatures
+ *     (assimilation.F90:4911-4933, compiled there under CINTERFACE, bind(C)):
+ *        void oak_init(const char* fname);            assimilation.F90:4911-4916
+ *        void oak_assim(int ntime, int n, int r,      assimilation.F90:4919-4927
+ *                       double* Ef, double* Ea);
+ *        void oak_done(void);                         assimilation.F90:4929-4933
+ *     The reference stops the process on error (ERROR_STOP, ppdef.h:22); these return
+ *     nothing either, but record the failure for oakg_last_error()/oakg_last_status()
+ *     instead of exiting.
+ *
+ *  2. Kernel-level entry points replacing the Fortran routines the reference calls
+ *     directly (test/test_rrsqrt.F90:65,144,154,174; assimilation.F90:3235,3288):
+ *        oakg_analysis      <- analysis(xf,Hxf,yo,Sf,HSf,R,xa,Sa,amplitudes)
+ *                              rrsqrt.F90:196-208 (R = DiagCovar, covariance.F90:70-79)
+ *        oakg_locanalysis   <- locAnalysis(zoneSize,selectObservations,xf,Hxf,yo,Sf,HSf,
+ *                              R,xa,Sa,amplitudes,localise_obs) rrsqrt.F90:433-466, with
+ *                              selectObservations (assimilation.F90:3683-3771) replaced by
+ *                              zone/observation geometry and a built-in weight kind.
+ *
+ * Conventions (all entry points):
+ *  - Arrays are Fortran column-major, as in the reference: Sf/Sa are (n, N) with leading
+ *    dimension ldS >= n; HSf is (m, N) with leading dimension ldH >= m; amplitudes is
+ *    (N, nzones). Values are double precision (real(c_double)).
+ *  - All pointers are borrowed for the duration of the call only. They are host pointers
+ *    (mem = OAKG_MEM_HOST; copies to and from the GPU happen inside the call) or device
+ *    pointers of the current CUDA device (mem = OAKG_MEM_DEVICE).
+ *  - Outputs Sa and amplitudes may be NULL (the reference's optional arguments).
+ *  - Return value: OAKG_OK (0) or one of the OAKG_ERR_* codes; oakg_last_error() gives a
+ *    message. Calls are serialised by an internal lock (one call at a time per process).
+ *  - The library keeps per-device buffers between calls; oakg_release() frees them.
+ */
+#ifndef OAKG_H
+#define OAKG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define OAKG_OK 0
+#define OAKG_ERR_ARGS 1     /* invalid sizes, pointers or options                        */
+#define OAKG_ERR_CUDA 2     /* CUDA runtime error (no device, launch failure, ...)       */
+#define OAKG_ERR_NAN 3      /* NaN analysis amplitudes (rrsqrt.F90:145-149)              */
+#define OAKG_ERR_EIG 4      /* symmetric eigensolver did not converge                    */
+#define OAKG_ERR_NOMEM 5    /* device allocation failed                                  */
+#define OAKG_ERR_TIMEOUT 6  /* a bounded device-side wait ran out                        */
+#define OAKG_ERR_INIT 7     /* init file / configuration error (oak_init, oak_assim)     */
+#define OAKG_ERR_NOTIMPL 8  /* option not supported by this build                        */
+
+/* where array pointers live */
+#define OAKG_MEM_HOST 0
+#define OAKG_MEM_DEVICE 1
+
+/* observation weight kinds */
+#define OAKG_WEIGHT_GAUSS_CUTOFF 0 /* w = exp(-(d/L)^2), d <= maxLength (assimilation.F90:3756-3767) */
+#define OAKG_WEIGHT_GASPARI_COHN 1 /* w = locfun(d/L), d <= maxLength, w /= 0 (covariance.F90:645-667) */
+
+/* metrics (metrictype, assimilation.F90:108-112, 3635-3672) */
+#define OAKG_METRIC_CARTESIAN 0
+#define OAKG_METRIC_SPHERICAL 1
+#define OAKG_METRIC_SPHERICAL_APPROX 2
+
+/* precision of the local analysis */
+#define OAKG_PREC_FP64 0  /* every product in FP64 (the plain form)                     */
+
+/* oakg_loc.flags */
+#define OAKG_FLAG_AMPL_ALWAYS 1 /* write amplitudes for every analysed zone (the reference
+                                   writes them only when localise_obs is false, :375-384) */
+#define OAKG_FLAG_BRUTE_SEARCH 2 /* test every observation for every zone (the reference's
+                                    O(Z m) loop, assimilation.F90:3745-3757) instead of the
+                                    cell-grid search; same results, for validation         */
+
+typedef struct {
+  int64_t n;        /* state vector size                                        */
+  int32_t N;        /* ensemble size / error-space dimension (columns of Sf)    */
+  int32_t pad0;
+  int64_t m;        /* number of observations                                   */
+  int64_t ldS;      /* leading dimension of Sf and Sa (>= n)                    */
+  int64_t ldH;      /* leading dimension of HSf (>= m)                          */
+  int32_t mem;      /* OAKG_MEM_HOST or OAKG_MEM_DEVICE                         */
+  int32_t pad1;
+} oakg_dims;
+
+typedef struct {
+  int32_t weight;       /* OAKG_WEIGHT_*                                          */
+  int32_t metric;       /* OAKG_METRIC_* (metrictype)                             */
+  int32_t loctype;      /* 1 horizontal (x,y), 2 |dz|, 3 |dt| (assimilation.F90:3748-3754) */
+  int32_t localise_obs; /* localise_obs argument (default true, rrsqrt.F90:318-320) */
+  int32_t rotate;       /* ROTATE_ENSEMBLE (rrsqrt.F90:24): 1 = rotate (reference default) */
+  int32_t precision;    /* OAKG_PREC_*                                            */
+  int32_t flags;        /* OAKG_FLAG_*                                            */
+  int32_t pad0;
+  double cell_size;     /* search-cell edge in coordinate units; <= 0 picks one   */
+} oakg_loc;
+
+/* analysis (rrsqrt.F90:196-208) with diagonal R = diag(r_diag):
+ *   xf(n), Hxf(m), yo(m), Sf(n,N), HSf(m,N), r_diag(m) -> xa(n), Sa(n,N), ampl(N). */
+int oakg_analysis(const oakg_dims* dims, const double* xf, const double* Hxf,
+                  const double* yo, const double* Sf, const double* HSf,
+                  const double* r_diag, double* xa, double* Sa, double* ampl);
+
+/* locAnalysis (rrsqrt.F90:433-466): zones are consecutive blocks of the state vector,
+ * zone_size(nzones) long (rrsqrt.F90:291-300). selectObservations (assimilation.F90:
+ * 3683-3771) is evaluated on the device from:
+ *   zone_xyzt(4, nzones)  column-major: x,y,z,t of each zone's first element (:3713-3740)
+ *   obs_x, obs_y, obs_z, obs_t (m)      obsGridX/Y/Z/T (assimilation.F90:228);
+ *                                        unused coordinates may be NULL
+ *   corr_len, max_len (nzones)          hCorrLengthToObs / hMaxCorrLengthToObs at the
+ *                                        zone's first element (assimilation.F90:229)
+ * Outputs: xa(n), Sa(n,N) (may be NULL), ampl(N,nzones) (may be NULL), nobs(nzones)
+ * (may be NULL; the number of relevant observations of each zone). */
+int oakg_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                     const int32_t* zone_size, const double* xf, const double* Hxf,
+                     const double* yo, const double* Sf, const double* HSf,
+                     const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                     const double* obs_y, const double* obs_z, const double* obs_t,
+                     const double* corr_len, const double* max_len, double* xa, double* Sa,
+                     double* ampl, int32_t* nobs);
+
+/* Message of the last failed call on this thread (empty if none); returns its length. */
+size_t oakg_last_error(char* buf, size_t len);
+
+/* Status of the last call of any entry point (oak_* entry points return void). */
+int oakg_last_status(void);
+
+/* Device buffers kept between calls are freed. */
+int oakg_release(void);
+
+/* Per-stage device times of the last oakg_locanalysis call, in milliseconds, measured with
+ * CUDA events on the library's stream: [0] observation preparation, [1] selection + Gram,
+ * [2] eigensolve + transform, [3] ensemble update, [4] whole call (device). Returns the
+ * number of values written (<= n). */
+int oakg_last_timings(double* ms, int n);
+
+/* OAK's C interface (assimilation.F90:4885-4935). */
+void oak_init(const char* fname);
+void oak_assim(int ntime, int n, int r, double* Ef, double* Ea);
+void oak_done(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OAKG_H */

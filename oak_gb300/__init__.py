@@ -1,0 +1,292 @@
+"""GB300-native local ensemble square-root analysis (the analysis path of gher-uliege/OAK).
+
+Python host binding over the C ABI of ``liboakg.so`` (``include/oakg.h``). The functions keep
+the argument meaning and order of the reference routines they replace:
+
+* :func:`analysis`      <- ``analysis(xf,Hxf,yo,Sf,HSf,R,xa,Sa,amplitudes)`` (rrsqrt.F90:196-208)
+* :func:`loc_analysis`  <- ``locAnalysis(zoneSize,selectObservations,xf,Hxf,yo,Sf,HSf,R,xa,Sa,
+  amplitudes,localise_obs)`` (rrsqrt.F90:433-466), with ``selectObservations``
+  (assimilation.F90:3683-3771) given as geometry: zone and observation coordinates, the
+  per-zone correlation and maximum lengths, a metric and a weight kind.
+
+Arrays are NumPy arrays (host memory; the call copies to and from the GPU) or CUDA
+``torch.Tensor`` objects (device memory; nothing is copied). Ensemble matrices are the
+reference's Fortran column-major ``(n, N)`` arrays: NumPy arrays are passed in Fortran order,
+torch tensors must have strides ``(1, ld)``.
+
+Errors are raised as :class:`OakError` carrying the C status code, where the reference would
+stop the program (ERROR_STOP, ppdef.h:22).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["analysis", "loc_analysis", "OakError", "lib", "last_timings", "release",
+           "GAUSS_CUTOFF", "GASPARI_COHN", "CARTESIAN", "SPHERICAL", "SPHERICAL_APPROX",
+           "zone_positions"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liboakg.so")
+
+# constants of include/oakg.h
+OK = 0
+ERR_ARGS, ERR_CUDA, ERR_NAN, ERR_EIG, ERR_NOMEM, ERR_TIMEOUT, ERR_INIT, ERR_NOTIMPL = range(1, 9)
+MEM_HOST, MEM_DEVICE = 0, 1
+GAUSS_CUTOFF, GASPARI_COHN = 0, 1
+CARTESIAN, SPHERICAL, SPHERICAL_APPROX = 0, 1, 2
+PREC_FP64 = 0
+FLAG_AMPL_ALWAYS, FLAG_BRUTE_SEARCH = 1, 2
+
+
+class OakError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[oakg status {code}] {msg}")
+        self.code = code
+
+
+class Dims(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("N", ctypes.c_int32), ("pad0", ctypes.c_int32),
+                ("m", ctypes.c_int64), ("ldS", ctypes.c_int64), ("ldH", ctypes.c_int64),
+                ("mem", ctypes.c_int32), ("pad1", ctypes.c_int32)]
+
+
+class Loc(ctypes.Structure):
+    _fields_ = [("weight", ctypes.c_int32), ("metric", ctypes.c_int32),
+                ("loctype", ctypes.c_int32), ("localise_obs", ctypes.c_int32),
+                ("rotate", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("flags", ctypes.c_int32), ("pad0", ctypes.c_int32),
+                ("cell_size", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded ``liboakg.so``; raises if it has not been built (no fallback path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OakError(ERR_CUDA, f"{LIB_PATH} is missing: build it with "
+                                 "`python -m oak_gb300.build` (there is no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    L.oakg_analysis.argtypes = [ctypes.POINTER(Dims)] + [P] * 9
+    L.oakg_analysis.restype = ctypes.c_int
+    L.oakg_locanalysis.argtypes = [ctypes.POINTER(Dims), ctypes.POINTER(Loc), ctypes.c_int32] + [P] * 18
+    L.oakg_locanalysis.restype = ctypes.c_int
+    L.oakg_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.oakg_last_error.restype = ctypes.c_size_t
+    L.oakg_last_status.argtypes = []
+    L.oakg_last_status.restype = ctypes.c_int
+    L.oakg_release.argtypes = []
+    L.oakg_release.restype = ctypes.c_int
+    L.oakg_last_timings.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    L.oakg_last_timings.restype = ctypes.c_int
+    L.oak_init.argtypes = [ctypes.c_char_p]
+    L.oak_init.restype = None
+    L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
+    L.oak_assim.restype = None
+    L.oak_done.argtypes = []
+    L.oak_done.restype = None
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != OK:
+        buf = ctypes.create_string_buffer(1024)
+        lib().oakg_last_error(buf, len(buf))
+        raise OakError(rc, buf.value.decode(errors="replace"))
+
+
+def last_timings() -> dict:
+    """Device time per stage of the last call (CUDA events on the library stream), in ms."""
+    arr = (ctypes.c_double * 5)()
+    k = lib().oakg_last_timings(arr, 5)
+    names = ["obs_prep", "gram", "eig", "update", "total"]
+    return {names[i]: arr[i] for i in range(k)}
+
+
+def release() -> None:
+    """Free the device buffers the library keeps between calls."""
+    lib().oakg_release()
+
+
+# ---------------------------------------------------------------------------- array helpers
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+class _Args:
+    """Collects pointers, keeping the backing arrays alive; all host or all device."""
+
+    def __init__(self, device: bool):
+        self.device = device
+        self.keep = []
+
+    def vec(self, a, dtype=np.float64, name="array", n=None):
+        if a is None:
+            return None
+        if self.device:
+            import torch
+            tdt = torch.float64 if dtype == np.float64 else torch.int32
+            if not (_is_torch(a) and a.is_cuda):
+                raise OakError(ERR_ARGS, f"{name}: expected a CUDA tensor")
+            if a.dtype != tdt or not a.is_contiguous():
+                raise OakError(ERR_ARGS, f"{name}: expected a contiguous {tdt} tensor")
+            if n is not None and a.numel() < n:
+                raise OakError(ERR_ARGS, f"{name}: needs {n} elements, has {a.numel()}")
+            self.keep.append(a)
+            return ctypes.c_void_p(a.data_ptr())
+        arr = np.ascontiguousarray(np.asarray(a, dtype=dtype)).reshape(-1)
+        if n is not None and arr.size < n:
+            raise OakError(ERR_ARGS, f"{name}: needs {n} elements, has {arr.size}")
+        self.keep.append(arr)
+        return ctypes.c_void_p(arr.ctypes.data)
+
+    def mat(self, a, rows, cols, name):
+        """Column-major (rows, cols) matrix; returns (pointer, leading dimension)."""
+        if self.device:
+            if not (_is_torch(a) and a.is_cuda):
+                raise OakError(ERR_ARGS, f"{name}: expected a CUDA tensor")
+            import torch
+            if a.dtype != torch.float64 or tuple(a.shape) != (rows, cols):
+                raise OakError(ERR_ARGS, f"{name}: expected float64 of shape ({rows}, {cols})")
+            if a.stride(0) != 1 or (cols > 1 and a.stride(1) < rows):
+                raise OakError(ERR_ARGS, f"{name}: expected column-major strides (1, ld>=rows)")
+            self.keep.append(a)
+            return ctypes.c_void_p(a.data_ptr()), (a.stride(1) if cols > 1 else rows)
+        arr = np.asfortranarray(np.asarray(a, dtype=np.float64))
+        if arr.shape != (rows, cols):
+            raise OakError(ERR_ARGS, f"{name}: expected shape ({rows}, {cols}), got {arr.shape}")
+        self.keep.append(arr)
+        return ctypes.c_void_p(arr.ctypes.data), rows
+
+
+def _device_mode(*arrays) -> bool:
+    dev = [_is_torch(a) and a.is_cuda for a in arrays if a is not None]
+    if any(dev) and not all(dev):
+        raise OakError(ERR_ARGS, "mix of host and device arrays")
+    return bool(dev) and all(dev)
+
+
+def _empty_like_mode(device: bool, shape, dtype=np.float64, order="C", like=None):
+    if device:
+        import torch
+        tdt = torch.float64 if dtype == np.float64 else torch.int32
+        if order == "F" and len(shape) == 2:
+            return torch.empty((shape[1], shape[0]), dtype=tdt, device=like.device).t()
+        return torch.empty(shape, dtype=tdt, device=like.device)
+    return np.empty(shape, dtype=dtype, order=order)
+
+
+def _sync_torch(device: bool, ref) -> None:
+    if device:
+        import torch
+        torch.cuda.synchronize(ref.device)
+
+
+# ----------------------------------------------------------------------------- entry points
+
+def analysis(xf, Hxf, yo, Sf, HSf, r_diag, *, want_sa=True, out=None):
+    """Global analysis (rrsqrt.F90:196-208) with diagonal R = diag(r_diag).
+
+    Returns ``(xa, Sa, amplitudes)``.
+    """
+    n = int(xf.shape[0])
+    m = int(yo.shape[0])
+    N = int(Sf.shape[1])
+    device = _device_mode(xf, Hxf, yo, Sf, HSf, r_diag)
+    A = _Args(device)
+    pSf, ldS = A.mat(Sf, n, N, "Sf")
+    pHS, ldH = A.mat(HSf, m, N, "HSf")
+    dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
+    like = Sf
+    xa = _empty_like_mode(device, (n,), like=like)
+    Sa = None
+    if want_sa:
+        Sa = _empty_like_mode(device, (n, N), order="F", like=like)
+        if device and ldS != n:
+            raise OakError(ERR_ARGS, "device Sf with ld != n: pass out arrays explicitly")
+    ampl = _empty_like_mode(device, (N,), like=like)
+    _sync_torch(device, like)
+    rc = lib().oakg_analysis(ctypes.byref(dims), A.vec(xf, n=n, name="xf"),
+                             A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"), pSf, pHS,
+                             A.vec(r_diag, n=m, name="r_diag"), A.vec(xa, name="xa"),
+                             None if Sa is None else A.mat(Sa, n, N, "Sa")[0],
+                             A.vec(ampl, name="ampl"))
+    _check(rc)
+    return xa, Sa, ampl
+
+
+def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, corr_len,
+                 max_len, *, weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1,
+                 localise_obs=True, rotate=True, want_sa=True, want_ampl=True,
+                 ampl_always=False, brute_search=False, cell_size=0.0):
+    """Local analysis (rrsqrt.F90:433-466) with geometric observation selection.
+
+    ``zone_pos``: (Z, 4) x, y, z, t of each zone's first state element
+    (assimilation.F90:3713-3740); ``obs_pos``: (x, y, z, t) observation coordinate arrays
+    (obsGridX/Y/Z/T; unused ones may be None); ``corr_len``, ``max_len``: (Z,) lengths
+    (hCorrLengthToObs / hMaxCorrLengthToObs at each zone's first element).
+
+    Returns ``(xa, Sa, amplitudes (N, Z), nobs (Z,))``. As in the reference, amplitudes are
+    only written for the non-localised branch unless ``ampl_always`` is set.
+    """
+    Z = int(zone_size.shape[0])
+    n = int(xf.shape[0])
+    m = int(yo.shape[0])
+    N = int(Sf.shape[1])
+    ox, oy, oz, ot = (tuple(obs_pos) + (None,) * 4)[:4]
+    device = _device_mode(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, corr_len, max_len,
+                          ox, oy, oz, ot)
+    A = _Args(device)
+    pSf, ldS = A.mat(Sf, n, N, "Sf")
+    pHS, ldH = A.mat(HSf, m, N, "HSf")
+    dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
+    flags = (FLAG_AMPL_ALWAYS if ampl_always else 0) | (FLAG_BRUTE_SEARCH if brute_search else 0)
+    loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
+              rotate=int(bool(rotate)), precision=PREC_FP64, flags=flags,
+              cell_size=float(cell_size))
+    like = Sf
+    if device:
+        zp = zone_pos.reshape(-1)
+    else:
+        zp = np.ascontiguousarray(np.asarray(zone_pos, dtype=np.float64).reshape(Z, 4))
+    xa = _empty_like_mode(device, (n,), like=like)
+    Sa = _empty_like_mode(device, (n, N), order="F", like=like) if want_sa else None
+    if device and want_sa and ldS != n:
+        raise OakError(ERR_ARGS, "device Sf with ld != n is not supported by this wrapper")
+    ampl = _empty_like_mode(device, (N, Z), order="F", like=like) if want_ampl else None
+    nobs = _empty_like_mode(device, (Z,), dtype=np.int32, like=like)
+    _sync_torch(device, like)
+    rc = lib().oakg_locanalysis(
+        ctypes.byref(dims), ctypes.byref(loc), Z, A.vec(zone_size, np.int32, "zone_size", Z),
+        A.vec(xf, n=n, name="xf"), A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"),
+        pSf, pHS, A.vec(r_diag, n=m, name="r_diag"), A.vec(zp, n=4 * Z, name="zone_pos"),
+        A.vec(ox, n=m, name="obs_x"), A.vec(oy, n=m, name="obs_y"), A.vec(oz, n=m, name="obs_z"),
+        A.vec(ot, n=m, name="obs_t"), A.vec(corr_len, n=Z, name="corr_len"),
+        A.vec(max_len, n=Z, name="max_len"), A.vec(xa, name="xa"),
+        None if Sa is None else A.mat(Sa, n, N, "Sa")[0],
+        None if ampl is None else A.mat(ampl, N, Z, "ampl")[0],
+        A.vec(nobs, np.int32, "nobs"))
+    _check(rc)
+    return xa, Sa, ampl, nobs
+
+
+def zone_positions(zone_size, x, y=None, z=None, t=None):
+    """(Z, 4) coordinates of each zone's first element, from per-element coordinate arrays
+    of the (zone-permuted) state vector -- what selectObservations reads through
+    zoneIndex/ind2submv/getCoord (assimilation.F90:3710-3740)."""
+    zs = np.asarray(zone_size, dtype=np.int64)
+    first = np.concatenate([[0], np.cumsum(zs)[:-1]])
+    out = np.zeros((zs.size, 4))
+    for k, c in enumerate((x, y, z, t)):
+        if c is not None:
+            out[:, k] = np.asarray(c, dtype=np.float64)[first]
+    return out

@@ -1,0 +1,612 @@
+// C ABI of liboakg.so (declared in include/oakg.h): argument checking, the per-device
+// context (stream, events, buffers kept between calls), host<->device staging and the
+// stage sequence K0 -> (K1+K2) -> (K3+K4) -> K5 over chunks of zones.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "oakg_internal.cuh"
+
+namespace oakg {
+
+namespace {
+
+thread_local std::string t_last_error;
+int g_last_status = OAKG_OK;
+std::mutex g_mutex;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_last_error = buf;
+  g_last_status = code;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  int code = (e == cudaErrorMemoryAllocation) ? OAKG_ERR_NOMEM : OAKG_ERR_CUDA;
+  return fail(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// A device buffer that only grows.
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+enum BufId {
+  B_ZONE_SIZE, B_XF, B_HXF, B_YO, B_R, B_SF, B_HSF, B_ZXYZT, B_OX, B_OY, B_OZ, B_OT, B_CORR,
+  B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
+  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_COUNT_
+};
+
+struct Ctx {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  Buf buf[B_COUNT_];
+  double timings[5] = {0, 0, 0, 0, 0};
+};
+
+Ctx* g_ctx[64] = {};
+
+int get_ctx(Ctx** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(OAKG_ERR_CUDA, "device index %d out of range", dev);
+  if (!g_ctx[dev]) {
+    Ctx* c = new Ctx();
+    c->device = dev;
+    // blocking stream: ordered after work the caller queued on the legacy default stream
+    e = cudaStreamCreate(&c->stream);
+    if (e != cudaSuccess) {
+      delete c;
+      return cuda_fail(e, "cudaStreamCreate");
+    }
+    for (auto& ev : c->ev) cudaEventCreate(&ev);
+    g_ctx[dev] = c;
+  }
+  *out = g_ctx[dev];
+  return OAKG_OK;
+}
+
+// Device view of an input: the caller's pointer (device memory) or a staged copy.
+template <typename T>
+int stage_in(Ctx* c, BufId id, const T* src, size_t count, int mem, const T** out,
+             const char* name) {
+  if (!src) {
+    *out = nullptr;
+    return OAKG_OK;
+  }
+  if (mem == OAKG_MEM_DEVICE) {
+    *out = src;
+    return OAKG_OK;
+  }
+  cudaError_t e = c->buf[id].ensure(count * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_fail(e, name);
+  e = cudaMemcpyAsync(c->buf[id].p, src, count * sizeof(T), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, name);
+  *out = c->buf[id].as<T>();
+  return OAKG_OK;
+}
+
+template <typename T>
+int stage_out(Ctx* c, BufId id, T* dst, size_t count, int mem, T** out, const char* name) {
+  if (!dst) {
+    *out = nullptr;
+    return OAKG_OK;
+  }
+  if (mem == OAKG_MEM_DEVICE) {
+    *out = dst;
+    return OAKG_OK;
+  }
+  cudaError_t e = c->buf[id].ensure(count * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_fail(e, name);
+  *out = c->buf[id].as<T>();
+  return OAKG_OK;
+}
+
+template <typename T>
+int scratch(Ctx* c, BufId id, size_t count, T** out, const char* name) {
+  cudaError_t e = c->buf[id].ensure(count * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_fail(e, name);
+  *out = c->buf[id].as<T>();
+  return OAKG_OK;
+}
+
+int check_dims(const oakg_dims* d) {
+  if (!d) return fail(OAKG_ERR_ARGS, "dims is NULL");
+  if (d->n <= 0) return fail(OAKG_ERR_ARGS, "n must be positive (got %lld)", (long long)d->n);
+  if (d->N < 2 || d->N > max_fp64_ensemble())
+    return fail(OAKG_ERR_ARGS, "ensemble size N=%d outside [2, %d]", d->N, max_fp64_ensemble());
+  if (d->m < 0) return fail(OAKG_ERR_ARGS, "m must be >= 0");
+  if (d->m > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "m above 2^31-2");
+  if (d->ldS < d->n) return fail(OAKG_ERR_ARGS, "ldS < n");
+  if (d->ldH < d->m) return fail(OAKG_ERR_ARGS, "ldH < m");
+  if (d->mem != OAKG_MEM_HOST && d->mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  return OAKG_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+__global__ void k_or_status(const int32_t* __restrict__ st, int32_t n, int32_t* __restrict__ out) {
+  int32_t acc = 0;
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    acc |= st[i];
+  for (int o = 16; o > 0; o >>= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicOr(out, acc);
+}
+
+__global__ void k_set_int(int32_t* p, int32_t v) { *p = v; }
+
+int status_code(int32_t bits) {
+  if (bits & ZST_NAN) return fail(OAKG_ERR_NAN, "NaN in analysis amplitudes (rrsqrt.F90:145-149)");
+  if (bits & ZST_EIG) return fail(OAKG_ERR_EIG, "symmetric eigensolver did not converge");
+  if (bits) return fail(OAKG_ERR_CUDA, "device status 0x%x", bits);
+  return OAKG_OK;
+}
+
+// Scratch budget for the per-zone G/T matrices of one chunk.
+size_t chunk_budget_bytes() {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return (size_t)4 << 30;
+  size_t b = free_b / 4;
+  const size_t cap = (size_t)16 << 30;
+  return b > cap ? cap : b;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
+                     const int32_t* zone_size, const double* xf, const double* Hxf,
+                     const double* yo, const double* Sf, const double* HSf,
+                     const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                     const double* obs_y, const double* obs_z, const double* obs_t,
+                     const double* corr_len, const double* max_len, double* xa, double* Sa,
+                     double* ampl, int32_t* nobs_out) {
+  int rc = check_dims(dims);
+  if (rc) return rc;
+  if (!loc) return fail(OAKG_ERR_ARGS, "loc is NULL");
+  if (Z < 1) return fail(OAKG_ERR_ARGS, "nzones must be >= 1");
+  if (loc->weight != OAKG_WEIGHT_GAUSS_CUTOFF && loc->weight != OAKG_WEIGHT_GASPARI_COHN)
+    return fail(OAKG_ERR_ARGS, "unknown weight kind %d", loc->weight);
+  if (loc->metric < 0 || loc->metric > 2)
+    return fail(OAKG_ERR_ARGS, "Unsupported metric: %d (assimilation.F90:3664-3668)",
+                loc->metric);
+  if (loc->loctype < 1 || loc->loctype > 3)
+    return fail(OAKG_ERR_ARGS, "loctype must be 1, 2 or 3 (got %d)", loc->loctype);
+  if (loc->precision != OAKG_PREC_FP64)
+    return fail(OAKG_ERR_NOTIMPL, "precision mode %d not available", loc->precision);
+  const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
+  const int N = dims->N, mem = dims->mem;
+  if (!zone_size || !xf || !xa || !zone_xyzt || !corr_len || !max_len)
+    return fail(OAKG_ERR_ARGS, "zone_size, xf, zone_xyzt, corr_len, max_len and xa are required");
+  if (!Sf) return fail(OAKG_ERR_ARGS, "Sf is required");
+  if (m > 0 && (!Hxf || !yo || !HSf || !r_diag))
+    return fail(OAKG_ERR_ARGS, "Hxf, yo, HSf and r_diag are required when m > 0");
+  const double* u_src_h = (loc->loctype == 1) ? obs_x : (loc->loctype == 2 ? obs_z : obs_t);
+  const double* v_src_h = (loc->loctype == 1) ? obs_y : nullptr;
+  if (m > 0 && (!u_src_h || (loc->loctype == 1 && !v_src_h)))
+    return fail(OAKG_ERR_ARGS, "observation coordinates required by loctype %d are NULL",
+                loc->loctype);
+
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  cudaEventRecord(c->ev[0], st);
+
+  const int32_t* d_zsize;
+  const double *d_xf, *d_Hxf = nullptr, *d_yo = nullptr, *d_r = nullptr, *d_Sf,
+                      *d_HSf = nullptr, *d_zxyzt, *d_u = nullptr, *d_v = nullptr, *d_corr,
+                      *d_maxl;
+  if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &d_zsize, "zone_size"))) return rc;
+  if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &d_xf, "xf"))) return rc;
+  if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &d_Sf, "Sf"))) return rc;
+  if ((rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &d_zxyzt, "zone_xyzt"))) return rc;
+  if ((rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &d_corr, "corr_len"))) return rc;
+  if ((rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &d_maxl, "max_len"))) return rc;
+  if (m > 0) {
+    if ((rc = stage_in(c, B_HXF, Hxf, (size_t)m, mem, &d_Hxf, "Hxf"))) return rc;
+    if ((rc = stage_in(c, B_YO, yo, (size_t)m, mem, &d_yo, "yo"))) return rc;
+    if ((rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &d_r, "r_diag"))) return rc;
+    if ((rc = stage_in(c, B_HSF, HSf, (size_t)ldH * N, mem, &d_HSf, "HSf"))) return rc;
+    if ((rc = stage_in(c, B_OX, u_src_h, (size_t)m, mem, &d_u, "obs coordinate u"))) return rc;
+    if (v_src_h && (rc = stage_in(c, B_OY, v_src_h, (size_t)m, mem, &d_v, "obs coordinate v")))
+      return rc;
+  }
+  double *d_xa, *d_Sa, *d_ampl;
+  int32_t* d_nobs;
+  if ((rc = stage_out(c, B_XA, xa, (size_t)n, mem, &d_xa, "xa"))) return rc;
+  if ((rc = stage_out(c, B_SA, Sa, (size_t)ldS * N, mem, &d_Sa, "Sa"))) return rc;
+  if ((rc = stage_out(c, B_AMPL, ampl, (size_t)N * Z, mem, &d_ampl, "amplitudes"))) return rc;
+  if (mem == OAKG_MEM_DEVICE && nobs_out) {
+    d_nobs = nobs_out;
+  } else if ((rc = scratch(c, B_NOBS, (size_t)Z, &d_nobs, "nobs"))) {
+    return rc;
+  }
+  if (mem == OAKG_MEM_HOST && Sa) {
+    // rows beyond n (ldS > n) are returned unchanged
+    e = cudaMemcpyAsync(d_Sa, d_Sf, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                        st);
+    if (e != cudaSuccess) return cuda_fail(e, "Sa init");
+  }
+
+  // zone offsets and sizes
+  int64_t* d_zstart;
+  double* d_small;
+  if ((rc = scratch(c, B_ZSTART, (size_t)Z + 1, &d_zstart, "zone offsets"))) return rc;
+  if ((rc = scratch(c, B_SMALL, 16, &d_small, "small"))) return rc;
+  int32_t* d_zmax = reinterpret_cast<int32_t*>(d_small + 8);
+  if ((e = zone_offsets(d_zsize, Z, d_zstart, d_zmax, st)) != cudaSuccess)
+    return cuda_fail(e, "zone offsets");
+  int brute = (loc->flags & OAKG_FLAG_BRUTE_SEARCH) || !loc->localise_obs;
+  if (m > 0) {
+    if ((e = obs_bounds(d_u, d_v, m, d_small, st)) != cudaSuccess) return cuda_fail(e, "bounds");
+    if ((e = obs_bounds(d_maxl, nullptr, Z, d_small + 4, st)) != cudaSuccess)
+      return cuda_fail(e, "bounds");
+  }
+  double hsmall[9] = {0};
+  int64_t htotal = 0;
+  if ((e = cudaMemcpyAsync(hsmall, d_small, 9 * sizeof(double), cudaMemcpyDeviceToHost, st)) !=
+      cudaSuccess)
+    return cuda_fail(e, "D2H");
+  if ((e = cudaMemcpyAsync(&htotal, d_zstart + Z, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) !=
+      cudaSuccess)
+    return cuda_fail(e, "D2H");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "synchronize");
+  int32_t zone_max = 0;
+  std::memcpy(&zone_max, &hsmall[8], sizeof(int32_t));
+  if (htotal != n)
+    return fail(OAKG_ERR_ARGS, "sum(zone_size) = %lld differs from n = %lld", (long long)htotal,
+                (long long)n);
+
+  // cell grid over the observation coordinates
+  CellGrid g{};
+  g.nu = g.nv = 1;
+  g.csu = g.csv = 1.0;
+  const int spherical = (loc->loctype == 1 && loc->metric != OAKG_METRIC_CARTESIAN);
+  if (m > 0 && !brute) {
+    double umin = hsmall[0], umax = hsmall[1], vmin = hsmall[2], vmax = hsmall[3];
+    double Rmax = hsmall[5];
+    if (!(std::isfinite(umin) && std::isfinite(umax) && std::isfinite(vmin) && std::isfinite(vmax)))
+      return fail(OAKG_ERR_ARGS, "non-finite observation coordinates");
+    double reach = Rmax;  // maxLength in coordinate units
+    if (spherical) reach = Rmax / (3.141592653589793 * 6378137.0 / 180.0);  // metres -> degrees
+    double cs = (loc->cell_size > 0) ? loc->cell_size : 0.5 * reach;
+    const double max_cells = 4.0e6;
+    g.periodic_u = (loc->metric == OAKG_METRIC_SPHERICAL && loc->loctype == 1);
+    if (g.periodic_u) {
+      umin = 0.0;
+      umax = 360.0;
+    }
+    double spanu = std::max(umax - umin, 0.0), spanv = std::max(vmax - vmin, 0.0);
+    if (!(cs > 0) || !std::isfinite(cs)) cs = std::max(std::max(spanu, spanv), 1.0);
+    while ((std::floor(spanu / cs) + 1.0) * (std::floor(spanv / cs) + 1.0) > max_cells) cs *= 2.0;
+    g.u0 = umin;
+    g.v0 = vmin;
+    g.csu = cs;
+    g.csv = cs;
+    g.nu = (int32_t)std::floor(spanu / cs) + 1;
+    g.nv = (loc->loctype == 1) ? (int32_t)std::floor(spanv / cs) + 1 : 1;
+    if (g.periodic_u) g.nu = std::max(1, (int32_t)std::ceil(360.0 / cs));
+  }
+  const int64_t ncells = (int64_t)g.nu * g.nv;
+
+  SortedObs so{};
+  if (m > 0) {
+    int32_t *d_cell, *d_count, *d_cstart, *d_pos, *d_perm;
+    double *d_su, *d_sv, *d_sinnov, *d_sr, *d_hst;
+    if ((rc = scratch(c, B_CELL, (size_t)m, &d_cell, "cells"))) return rc;
+    if ((rc = scratch(c, B_COUNT, (size_t)ncells + 1, &d_count, "cells"))) return rc;
+    if ((rc = scratch(c, B_CSTART, (size_t)ncells + 1, &d_cstart, "cells"))) return rc;
+    if ((rc = scratch(c, B_POS, (size_t)m, &d_pos, "obs"))) return rc;
+    if ((rc = scratch(c, B_PERM, (size_t)m, &d_perm, "obs"))) return rc;
+    if ((rc = scratch(c, B_SU, (size_t)m, &d_su, "obs"))) return rc;
+    if ((rc = scratch(c, B_SV, (size_t)m, &d_sv, "obs"))) return rc;
+    if ((rc = scratch(c, B_SINNOV, (size_t)m, &d_sinnov, "obs"))) return rc;
+    if ((rc = scratch(c, B_SR, (size_t)m, &d_sr, "obs"))) return rc;
+    if ((rc = scratch(c, B_HST, (size_t)m * N, &d_hst, "obs rows"))) return rc;
+    e = obs_bin_and_sort(g, m, N, d_u, d_v, d_yo, d_Hxf, d_r, d_HSf, ldH, d_cell, d_count,
+                         d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr, d_hst, st);
+    if (e != cudaSuccess) return cuda_fail(e, "observation binning");
+    so.u = d_su;
+    so.v = d_sv;
+    so.innov = d_sinnov;
+    so.r = d_sr;
+    so.HSt = d_hst;
+    so.cell_start = d_cstart;
+    so.perm = d_perm;
+  } else {
+    int32_t* d_cstart;
+    if ((rc = scratch(c, B_CSTART, 2, &d_cstart, "cells"))) return rc;
+    cudaMemsetAsync(d_cstart, 0, 2 * sizeof(int32_t), st);
+    so.cell_start = d_cstart;
+  }
+  cudaEventRecord(c->ev[1], st);
+
+  // zone chunks
+  const size_t per_zone = (size_t)N * N * 8 + (size_t)N * 16 + 8;
+  int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
+  if (chunk < 1) chunk = 1;
+  if (chunk > Z) chunk = Z;
+  double *d_G, *d_gv, *d_za;
+  int32_t *d_status, *d_work;
+  if ((rc = scratch(c, B_G, (size_t)chunk * N * N, &d_G, "zone matrices"))) return rc;
+  if ((rc = scratch(c, B_GV, (size_t)chunk * N, &d_gv, "zone vectors"))) return rc;
+  if ((rc = scratch(c, B_ZAMPL, (size_t)chunk * N, &d_za, "zone amplitudes"))) return rc;
+  if ((rc = scratch(c, B_STATUS, (size_t)chunk + 1, &d_status, "zone status"))) return rc;
+  if ((rc = scratch(c, B_WORK, 4, &d_work, "work counters"))) return rc;
+  int32_t* d_status_all = d_work + 2;
+  k_set_int<<<1, 1, 0, st>>>(d_status_all, 0);
+  LocParams lp{loc->weight, loc->metric, loc->loctype, loc->localise_obs ? 1 : 0,
+               loc->rotate ? 1 : 0, loc->flags};
+  const int all_ampl = (!loc->localise_obs) || (loc->flags & OAKG_FLAG_AMPL_ALWAYS);
+  double t_gram = 0, t_eig = 0, t_upd = 0;
+  for (int64_t z0 = 0; z0 < Z; z0 += chunk) {
+    const int32_t nzc = (int32_t)std::min<int64_t>(chunk, Z - z0);
+    cudaEventRecord(c->ev[2], st);
+    e = zone_gram_fp64(g, so, N, lp, (int32_t)z0, nzc, d_zxyzt, d_corr, d_maxl, d_G, d_gv,
+                       d_nobs, brute, d_work, st);
+    if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
+    cudaEventRecord(c->ev[3], st);
+    e = zone_eig_fp64(N, nzc, d_G, d_gv, d_nobs + z0, lp.rotate, d_za, d_status, d_work + 1, st);
+    if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
+    cudaEventRecord(c->ev[4], st);
+    e = zone_update_fp64(N, (int32_t)z0, nzc, d_zstart, zone_max, d_xf, d_Sf, ldS, d_G, d_za,
+                         d_nobs + z0, d_xa, d_Sa, st);
+    if (e != cudaSuccess) return cuda_fail(e, "update kernel");
+    cudaEventRecord(c->ev[5], st);
+    if (d_ampl) {
+      e = write_amplitudes(N, (int32_t)z0, nzc, d_za, d_nobs + z0, all_ampl, d_ampl, st);
+      if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
+    }
+    k_or_status<<<64, 256, 0, st>>>(d_status, nzc, d_status_all);
+    if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
+    t_gram += elapsed(c->ev[2], c->ev[3]);
+    t_eig += elapsed(c->ev[3], c->ev[4]);
+    t_upd += elapsed(c->ev[4], c->ev[5]);
+  }
+  cudaEventRecord(c->ev[6], st);
+  int32_t hstatus = 0;
+  if ((e = cudaMemcpyAsync(&hstatus, d_status_all, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) !=
+      cudaSuccess)
+    return cuda_fail(e, "D2H");
+  if (mem == OAKG_MEM_HOST) {
+    if ((e = cudaMemcpyAsync(xa, d_xa, n * sizeof(double), cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H xa");
+    if (Sa && (e = cudaMemcpyAsync(Sa, d_Sa, (size_t)ldS * N * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H Sa");
+    if (ampl && (e = cudaMemcpyAsync(ampl, d_ampl, (size_t)N * Z * sizeof(double),
+                                     cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H amplitudes");
+    if (nobs_out && (e = cudaMemcpyAsync(nobs_out, d_nobs, (size_t)Z * sizeof(int32_t),
+                                         cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H nobs");
+  }
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "synchronize");
+  c->timings[0] = elapsed(c->ev[0], c->ev[1]);
+  c->timings[1] = t_gram;
+  c->timings[2] = t_eig;
+  c->timings[3] = t_upd;
+  c->timings[4] = elapsed(c->ev[0], c->ev[6]);
+  return status_code(hstatus);
+}
+
+int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
+                  const double* yo, const double* Sf, const double* HSf, const double* r_diag,
+                  double* xa, double* Sa, double* ampl) {
+  int rc = check_dims(dims);
+  if (rc) return rc;
+  const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
+  const int N = dims->N, mem = dims->mem;
+  if (!xf || !Sf || !xa) return fail(OAKG_ERR_ARGS, "xf, Sf and xa are required");
+  if (m > 0 && (!Hxf || !yo || !HSf || !r_diag))
+    return fail(OAKG_ERR_ARGS, "Hxf, yo, HSf and r_diag are required when m > 0");
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  cudaEventRecord(c->ev[0], st);
+  const double *d_xf, *d_Hxf = nullptr, *d_yo = nullptr, *d_r = nullptr, *d_Sf, *d_HSf = nullptr;
+  if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &d_xf, "xf"))) return rc;
+  if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &d_Sf, "Sf"))) return rc;
+  if (m > 0) {
+    if ((rc = stage_in(c, B_HXF, Hxf, (size_t)m, mem, &d_Hxf, "Hxf"))) return rc;
+    if ((rc = stage_in(c, B_YO, yo, (size_t)m, mem, &d_yo, "yo"))) return rc;
+    if ((rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &d_r, "r_diag"))) return rc;
+    if ((rc = stage_in(c, B_HSF, HSf, (size_t)ldH * N, mem, &d_HSf, "HSf"))) return rc;
+  }
+  double *d_xa, *d_Sa, *d_ampl;
+  if ((rc = stage_out(c, B_XA, xa, (size_t)n, mem, &d_xa, "xa"))) return rc;
+  if ((rc = stage_out(c, B_SA, Sa, (size_t)ldS * N, mem, &d_Sa, "Sa"))) return rc;
+  if ((rc = stage_out(c, B_AMPL, ampl, (size_t)N, mem, &d_ampl, "amplitudes"))) return rc;
+  if (mem == OAKG_MEM_HOST && Sa) {
+    e = cudaMemcpyAsync(d_Sa, d_Sf, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                        st);
+    if (e != cudaSuccess) return cuda_fail(e, "Sa init");
+  }
+  double *d_G, *d_gv, *d_za;
+  int32_t *d_status, *d_work, *d_nobs;
+  int64_t* d_zstart;
+  if ((rc = scratch(c, B_G, (size_t)N * N, &d_G, "Gram"))) return rc;
+  if ((rc = scratch(c, B_GV, (size_t)N, &d_gv, "Gram"))) return rc;
+  if ((rc = scratch(c, B_ZAMPL, (size_t)N, &d_za, "amplitudes"))) return rc;
+  if ((rc = scratch(c, B_STATUS, 2, &d_status, "status"))) return rc;
+  if ((rc = scratch(c, B_WORK, 4, &d_work, "work"))) return rc;
+  if ((rc = scratch(c, B_NOBS, 2, &d_nobs, "nobs"))) return rc;
+  if ((rc = scratch(c, B_ZSTART, 2, &d_zstart, "zone offsets"))) return rc;
+  int64_t hz[2] = {0, n};
+  e = cudaMemcpyAsync(d_zstart, hz, sizeof(hz), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "H2D");
+  // The reference runs analysisIncrement even without observations; the result is then
+  // xa = xf, Sa = Sf (G = 0 -> T = I, v = w -> Omega = I), which the copy path gives.
+  k_set_int<<<1, 1, 0, st>>>(d_nobs, m > 0 ? 1 : 0);
+  if (m > 0) {
+    e = global_gram_fp64(m, N, d_HSf, ldH, d_yo, d_Hxf, d_r, d_G, d_gv, st);
+    if (e != cudaSuccess) return cuda_fail(e, "Gram kernel");
+  }
+  cudaEventRecord(c->ev[2], st);
+  e = zone_eig_fp64(N, 1, d_G, d_gv, d_nobs, 1, d_za, d_status, d_work + 1, st);
+  if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
+  cudaEventRecord(c->ev[3], st);
+  if (m == 0) cudaMemsetAsync(d_za, 0, N * sizeof(double), st);
+  int32_t zone_max = (int32_t)std::min<int64_t>(n, INT32_MAX);
+  e = zone_update_fp64(N, 0, 1, d_zstart, zone_max, d_xf, d_Sf, ldS, d_G, d_za, d_nobs, d_xa,
+                       d_Sa, st);
+  if (e != cudaSuccess) return cuda_fail(e, "update kernel");
+  cudaEventRecord(c->ev[4], st);
+  if (d_ampl) {
+    e = cudaMemcpyAsync(d_ampl, d_za, N * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
+  }
+  int32_t hstatus = 0;
+  e = cudaMemcpyAsync(&hstatus, d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "D2H");
+  if (mem == OAKG_MEM_HOST) {
+    if ((e = cudaMemcpyAsync(xa, d_xa, n * sizeof(double), cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H xa");
+    if (Sa && (e = cudaMemcpyAsync(Sa, d_Sa, (size_t)ldS * N * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H Sa");
+    if (ampl && (e = cudaMemcpyAsync(ampl, d_ampl, (size_t)N * sizeof(double),
+                                     cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H amplitudes");
+  }
+  cudaEventRecord(c->ev[6], st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "synchronize");
+  c->timings[0] = 0;
+  c->timings[1] = elapsed(c->ev[0], c->ev[2]);
+  c->timings[2] = elapsed(c->ev[2], c->ev[3]);
+  c->timings[3] = elapsed(c->ev[3], c->ev[4]);
+  c->timings[4] = elapsed(c->ev[0], c->ev[6]);
+  return status_code(hstatus);
+}
+
+int release_impl() {
+  for (auto& cp : g_ctx) {
+    if (!cp) continue;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(cp->device);
+    cudaStreamSynchronize(cp->stream);
+    for (auto& b : cp->buf) b.release();
+    for (auto& ev : cp->ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(cp->stream);
+    cudaSetDevice(prev);
+    delete cp;
+    cp = nullptr;
+  }
+  return OAKG_OK;
+}
+
+int timings_impl(double* ms, int n) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || !g_ctx[dev]) return 0;
+  int k = std::min(n, 5);
+  for (int i = 0; i < k; i++) ms[i] = g_ctx[dev]->timings[i];
+  return k;
+}
+
+void set_ok() {
+  g_last_status = OAKG_OK;
+  t_last_error.clear();
+}
+
+std::mutex& api_mutex() { return g_mutex; }
+int& last_status() { return g_last_status; }
+std::string& last_error() { return t_last_error; }
+int record_failure(int code, const char* msg) { return fail(code, "%s", msg); }
+
+}  // namespace oakg
+
+// ------------------------------------------------------------------------------------------
+extern "C" {
+
+int oakg_analysis(const oakg_dims* dims, const double* xf, const double* Hxf, const double* yo,
+                  const double* Sf, const double* HSf, const double* r_diag, double* xa,
+                  double* Sa, double* ampl) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::analysis_impl(dims, xf, Hxf, yo, Sf, HSf, r_diag, xa, Sa, ampl);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                     const int32_t* zone_size, const double* xf, const double* Hxf,
+                     const double* yo, const double* Sf, const double* HSf,
+                     const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                     const double* obs_y, const double* obs_z, const double* obs_t,
+                     const double* corr_len, const double* max_len, double* xa, double* Sa,
+                     double* ampl, int32_t* nobs) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::locanalysis_impl(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf, r_diag,
+                                  zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, xa,
+                                  Sa, ampl, nobs);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+size_t oakg_last_error(char* buf, size_t len) {
+  const std::string& s = oakg::last_error();
+  if (buf && len > 0) {
+    size_t k = std::min(len - 1, s.size());
+    std::memcpy(buf, s.data(), k);
+    buf[k] = '\0';
+  }
+  return s.size();
+}
+
+int oakg_last_status(void) { return oakg::last_status(); }
+
+int oakg_release(void) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  return oakg::release_impl();
+}
+
+int oakg_last_timings(double* ms, int n) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  if (!ms || n <= 0) return 0;
+  return oakg::timings_impl(ms, n);
+}
+
+}  // extern "C"

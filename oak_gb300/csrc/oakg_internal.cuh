@@ -1,0 +1,90 @@
+// Internal declarations shared by the CUDA translation units of liboakg.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/oakg.h"
+
+namespace oakg {
+
+// Per-zone status bits written by the device (host folds them into one OAKG_ERR_* code).
+enum : int32_t {
+  ZST_NAN = 1,       // NaN/Inf amplitudes (rrsqrt.F90:145-149)
+  ZST_EIG = 2,       // QL iterations did not converge
+  ZST_CAPACITY = 4,  // zone larger than the kernel's row tile (cannot happen: tiles split)
+};
+
+// Cell grid over observation coordinates (u, v): cells are cs_u x cs_v, nu x nv of them,
+// origin (u0, v0). For longitudes on the sphere (metric 1), u is periodic with period 360.
+struct CellGrid {
+  double u0, v0;     // origin
+  double csu, csv;   // cell edge
+  int32_t nu, nv;    // cells per axis
+  int32_t periodic_u;
+  int32_t pad;
+};
+
+// Observation arrays in cell-sorted order (index q), produced by obs_prep.
+struct SortedObs {
+  const double* u;      // coordinate used by the metric (x, z or t)          [m]
+  const double* v;      // second horizontal coordinate (y) or 0              [m]
+  const double* innov;  // yo - Hxf                                            [m]
+  const double* r;      // observation error variance (R diagonal)            [m]
+  const double* HSt;    // HSf rows, row-major [m][N]
+  const int32_t* cell_start;  // [ncells + 1]
+  const int32_t* perm;  // sorted position -> original index                [m]
+};
+
+struct LocParams {
+  int32_t weight, metric, loctype, localise, rotate, flags;
+};
+
+// ---- obs_prep.cu
+// Fills the sorted-observation arrays and the cell offsets; returns a CUDA error code.
+// u_src/v_src are the coordinate arrays for the metric (v_src may be null: v = 0).
+cudaError_t obs_bounds(const double* u, const double* v, int64_t m, double* d_out4,
+                       cudaStream_t st);
+cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* u_src,
+                             const double* v_src, const double* yo, const double* Hxf,
+                             const double* r, const double* HSf, int64_t ldH,
+                             int32_t* d_cell, int32_t* d_count, int32_t* d_cell_start,
+                             int32_t* d_pos, int32_t* d_perm, double* d_u, double* d_v,
+                             double* d_innov, double* d_r, double* d_HSt, cudaStream_t st);
+cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_start,
+                         int32_t* d_zone_max, cudaStream_t st);
+
+// ---- zone_gram_fp64.cu
+// Selection + Gram + innovation projection for zones [z0, z0 + nzc); writes G (N x N, both
+// triangles, row-major per zone), gvec (N), nobs per zone.
+cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                           int32_t z0, int32_t nzc, const double* zone_xyzt,
+                           const double* corr_len, const double* max_len, double* d_G,
+                           double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                           cudaStream_t st);
+// Global analysis Gram over all m observations (weights 1): G, g accumulated atomically.
+cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,
+                             const double* yo, const double* Hxf, const double* r, double* d_G,
+                             double* d_g, cudaStream_t st);
+
+// ---- zone_eig_fp64.cu
+// For zones [0, nzc) of a chunk with nobs > 0: eigen-decomposition of G (d_GT, N x N per
+// zone), T = U (I+L)^-1/2 U^T Omega written over G, ampl (N per zone), status per zone.
+// d_nobs/d_ampl/d_status are chunk-relative.
+cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
+                          const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
+                          int32_t* d_work, cudaStream_t st);
+size_t zone_eig_fp64_smem(int N);
+
+// ---- zone_update_fp64.cu
+// xa = xf + Sf ampl, Sa = Sf T per zone; zones with nobs == 0 copy (xa = xf, Sa = Sf).
+cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const double* xf, const double* Sf,
+                             int64_t ldS, const double* d_T, const double* d_ampl,
+                             const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st);
+cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_ampl,
+                             const int32_t* d_nobs, int all_zones, double* ampl_out,
+                             cudaStream_t st);
+
+int max_fp64_ensemble();  // largest N the FP64 kernels accept
+
+}  // namespace oakg

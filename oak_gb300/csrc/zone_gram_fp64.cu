@@ -1,0 +1,521 @@
+// K1 + K2 (FP64) -- per-zone observation selection and the Gram / innovation products.
+//
+// For zone z (one CTA at a time, zones handed out by an atomic work counter):
+//   selection  (assimilation.F90:3683-3771): d = distance(obs, zone) for loctype 1 (metric
+//              0/1/2, assimilation.F90:3635-3672), |dz| (loctype 2) or |dt| (loctype 3);
+//              relevant = d <= maxLength;  w = exp(-(d/L)^2)            (Gaussian, :3767)
+//              or w = locfun(d/L), relevant also needs w /= 0        (Gaspari-Cohn,
+//              covariance.F90:645-667, the rule of test/test_rrsqrt.F90:268-269)
+//   R^-1_eff   DCDCovar with D = w over DiagCovar R (rrsqrt.F90:395, covariance.F90:612-619,
+//              :425-432): c_q = w_q (w_q / r_q)
+//   Gram       G = HS_sel^T diag(c) HS_sel      (rrsqrt.F90:135, N x N, lower triangle
+//              accumulated, both triangles stored)
+//   innovation g = HS_sel^T diag(c) (yo - Hxf)_sel   (the inner product of :142)
+//
+// Only the cells of the observation grid that can contain observations within maxLength are
+// visited (cell rows are contiguous ranges of the cell-sorted arrays); with
+// OAKG_FLAG_BRUTE_SEARCH or localise_obs = false every observation is visited, which is the
+// reference's own loop. Work per zone: 2 p N^2/2 + 2 p N FP64 flops; the FP64 pipe bounds it.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "oakg_internal.cuh"
+
+namespace oakg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kListCap = 512;   // selected-observation staging list (flushed at >= 256)
+constexpr int kFlushAt = 256;
+constexpr double kPi = 3.141592653589793238462643383279502884197;
+constexpr double kEarthRadius = 6378137.0;
+
+// Gaspari-Cohn (covariance.F90:645-667), evaluated in the reference's Horner order.
+__device__ __forceinline__ double locfun(double r) {
+  if (r <= 1.0) return (((-r / 4.0 + 1.0 / 2.0) * r + 5.0 / 8.0) * r - 5.0 / 3.0) * (r * r) + 1.0;
+  if (r <= 2.0)
+    return ((((r / 12.0 - 1.0 / 2.0) * r + 5.0 / 8.0) * r + 5.0 / 3.0) * r - 5.0) * r + 4.0 -
+           2.0 / (3.0 * r);
+  return 0.0;
+}
+
+// distance(p0 = observation, p1 = zone) (assimilation.F90:3635-3672). Products and sums are
+// rounded one by one (no FMA contraction), so the Cartesian value is the correctly rounded
+// result of the reference expression and the d <= maxLength test matches a CPU evaluation.
+__device__ __forceinline__ double distance(double x0, double y0, double x1, double y1,
+                                           int metric) {
+  if (metric == OAKG_METRIC_CARTESIAN) {
+    double dx = __dsub_rn(x1, x0), dy = __dsub_rn(y1, y0);
+    return sqrt(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  } else if (metric == OAKG_METRIC_SPHERICAL_APPROX) {
+    const double coeff = kPi * kEarthRadius / 180.0;
+    double a = __dmul_rn(__dmul_rn(coeff, cos(__dmul_rn(__dadd_rn(y0, y1), kPi / 360.0))),
+                         __dsub_rn(x1, x0));
+    double b = __dmul_rn(coeff, __dsub_rn(y1, y0));
+    return sqrt(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)));
+  } else {
+    const double d2r = kPi / 180.0;
+    double a = __dmul_rn(y0, d2r), b = __dmul_rn(y1, d2r), C = __dmul_rn(__dsub_rn(x1, x0), d2r);
+    double coeff = __dadd_rn(__dmul_rn(sin(b), sin(a)),
+                             __dmul_rn(__dmul_rn(cos(b), cos(a)), cos(C)));
+    coeff = fmax(fmin(coeff, 1.0), -1.0);
+    return __dmul_rn(kEarthRadius, acos(coeff));
+  }
+}
+
+// Cell-index ranges a zone has to visit. Rows are v cells [cv0, cv1]; in each row the u cells
+// [cu0, cu1] (unclamped for a periodic axis; iterate modulo nu). all_u: visit every u cell.
+struct ScanRange {
+  int cu0, cu1, cv0, cv1, all_u;
+};
+
+__device__ ScanRange zone_scan_range(const CellGrid& g, int metric, int loctype, double zu,
+                                     double zv, double R) {
+  ScanRange s;
+  double du, dv;
+  int all_u = 0;
+  if (loctype != 1 || metric == OAKG_METRIC_CARTESIAN) {
+    du = R;
+    dv = (loctype == 1) ? R : 0.0;
+  } else if (metric == OAKG_METRIC_SPHERICAL_APPROX) {
+    const double coeff = kPi * kEarthRadius / 180.0;
+    dv = R / coeff;  // |dlat| bound, degrees
+    double a = (zv - 0.5 * dv) * (kPi / 180.0), b = (zv + 0.5 * dv) * (kPi / 180.0);
+    double cmin = fmin(fabs(cos(a)), fabs(cos(b)));
+    if ((zv - 0.5 * dv) <= 0.0 && (zv + 0.5 * dv) >= 0.0) cmin = fmin(cmin, 1.0);
+    if (fabs(zv) + 0.5 * dv >= 90.0 || cmin < 1e-12) {
+      all_u = 1;
+      du = 0.0;
+    } else {
+      du = R / (coeff * cmin);
+    }
+  } else {
+    double rho = R / kEarthRadius;  // angular radius, radians
+    dv = rho * (180.0 / kPi);
+    if (rho >= kPi || fabs(zv) + dv >= 90.0) {
+      all_u = 1;
+      du = 0.0;
+    } else {
+      double sl = sin(rho) / cos(zv * (kPi / 180.0));
+      du = (sl >= 1.0) ? 180.0 : asin(sl) * (180.0 / kPi);
+      if (du >= 180.0) all_u = 1;
+    }
+  }
+  // relative + absolute safety margins: candidates are a superset, the exact test decides
+  du = du * (1.0 + 1e-9) + 1e-9 * (fabs(zu) + du + g.csu);
+  dv = dv * (1.0 + 1e-9) + 1e-9 * (fabs(zv) + dv + g.csv);
+  double zuu = zu;
+  if (g.periodic_u) zuu = zu - 360.0 * floor(zu / 360.0);
+  double fu0 = floor((zuu - du - g.u0) / g.csu), fu1 = floor((zuu + du - g.u0) / g.csu);
+  double fv0 = floor((zv - dv - g.v0) / g.csv), fv1 = floor((zv + dv - g.v0) / g.csv);
+  fv0 = fmax(fv0, 0.0);
+  fv1 = fmin(fv1, (double)(g.nv - 1));
+  s.cv0 = (int)fv0;
+  s.cv1 = (int)fv1;
+  if (fv0 > fv1) {
+    s.cv0 = 0;
+    s.cv1 = -1;
+  }
+  if (g.periodic_u) {
+    if (all_u || fu1 - fu0 + 1.0 >= (double)g.nu) {
+      all_u = 1;
+    } else {
+      s.cu0 = (int)fu0;
+      s.cu1 = (int)fu1;
+    }
+  } else {
+    fu0 = fmax(fu0, 0.0);
+    fu1 = fmin(fu1, (double)(g.nu - 1));
+    s.cu0 = (int)fu0;
+    s.cu1 = (int)fu1;
+    if (fu0 > fu1) {
+      s.cv0 = 0;
+      s.cv1 = -1;
+    }
+  }
+  if (all_u) {
+    s.cu0 = 0;
+    s.cu1 = g.nu - 1;
+  }
+  s.all_u = all_u;
+  return s;
+}
+
+struct ZoneShared {
+  int32_t list_q[kListCap];
+  double list_c[kListCap];
+  int32_t warp_cnt[kThreads / 32];
+  int32_t list_len;
+  int32_t nrel;
+  int32_t zone;
+};
+
+// Accumulate the staged observations list[0..len) into the per-thread Gram entries.
+template <int MAXE>
+__device__ __forceinline__ void flush_list(ZoneShared& zs, int len, const SortedObs& so, int N,
+                                           int CH, double* sh, double* st, double* sinn,
+                                           const int32_t (&ea)[MAXE], const int32_t (&eb)[MAXE],
+                                           double (&acc)[MAXE], int E, int nent) {
+  for (int c0 = 0; c0 < len; c0 += CH) {
+    int rows = min(CH, len - c0);
+    __syncthreads();  // previous chunk fully consumed
+    for (int idx = threadIdx.x; idx < rows * N; idx += kThreads) {
+      int i = idx / N, k = idx - i * N;
+      int32_t q = zs.list_q[c0 + i];
+      double h = so.HSt[(int64_t)q * N + k];
+      sh[i * N + k] = h;
+      st[i * N + k] = zs.list_c[c0 + i] * h;
+    }
+    for (int i = threadIdx.x; i < rows; i += kThreads) {
+      int32_t q = zs.list_q[c0 + i];
+      sinn[i] = zs.list_c[c0 + i] * so.innov[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < MAXE; s++) {
+      int e = threadIdx.x + s * kThreads;
+      if (e < nent) {
+        double a = acc[s];
+        const int ia = ea[s], ib = eb[s];
+        if (e < E) {
+          for (int i = 0; i < rows; i++) a = fma(sh[i * N + ia], st[i * N + ib], a);
+        } else {
+          for (int i = 0; i < rows; i++) a = fma(sh[i * N + ia], sinn[i], a);
+        }
+        acc[s] = a;
+      }
+    }
+  }
+}
+
+template <int MAXE>
+__global__ void __launch_bounds__(kThreads)
+    k_zone_gram_fp64(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
+                     const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
+                     const double* __restrict__ max_len, double* __restrict__ G,
+                     double* __restrict__ gv, int32_t* __restrict__ nobs, int brute, int CH,
+                     int32_t* __restrict__ work) {
+  extern __shared__ double dyn[];
+  double* sh = dyn;            // [CH][N]
+  double* st = sh + CH * N;    // [CH][N]
+  double* sinn = st + CH * N;  // [CH]
+  __shared__ ZoneShared zs;
+
+  const int E = N * (N + 1) / 2;
+  const int nent = E + N;
+  int32_t ea[MAXE], eb[MAXE];
+#pragma unroll
+  for (int s = 0; s < MAXE; s++) {
+    int e = threadIdx.x + s * kThreads;
+    if (e < E) {
+      int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+      while ((a + 1) * (a + 2) / 2 <= e) a++;
+      while (a * (a + 1) / 2 > e) a--;
+      ea[s] = a;
+      eb[s] = e - a * (a + 1) / 2;
+    } else {
+      ea[s] = (e < nent) ? e - E : 0;
+      eb[s] = 0;
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t ncells = (int64_t)g.nu * g.nv;
+  const int full_scan = brute || !lp.localise;
+
+  for (;;) {
+    if (threadIdx.x == 0) zs.zone = atomicAdd(work, 1);
+    __syncthreads();
+    const int32_t zl = zs.zone;
+    if (zl >= nzc) break;
+    const int32_t z = z0 + zl;
+    const double zx = zone_xyzt[4 * (int64_t)z + 0], zy = zone_xyzt[4 * (int64_t)z + 1];
+    const double zzc = zone_xyzt[4 * (int64_t)z + 2], ztc = zone_xyzt[4 * (int64_t)z + 3];
+    const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
+    const double zv = (lp.loctype == 1) ? zy : 0.0;
+    const double L = corr_len[z], R = max_len[z];
+    if (threadIdx.x == 0) {
+      zs.list_len = 0;
+      zs.nrel = 0;
+    }
+    double acc[MAXE];
+#pragma unroll
+    for (int s = 0; s < MAXE; s++) acc[s] = 0.0;
+
+    ScanRange sr;
+    if (full_scan) {
+      sr.cu0 = 0;
+      sr.cu1 = g.nu - 1;
+      sr.cv0 = 0;
+      sr.cv1 = g.nv - 1;
+      sr.all_u = 1;
+    } else {
+      sr = zone_scan_range(g, lp.metric, lp.loctype, zu, zv, R);
+    }
+    __syncthreads();
+    int nrel_local = 0;
+    // Segments: one per cell row (two when a periodic range wraps).
+    for (int cv = sr.cv0; cv <= sr.cv1; cv++) {
+      for (int part = 0; part < 2; part++) {
+        int cu_a, cu_b;
+        if (sr.all_u) {
+          if (part) break;
+          cu_a = 0;
+          cu_b = g.nu - 1;
+        } else if (!g.periodic_u) {
+          if (part) break;
+          cu_a = sr.cu0;
+          cu_b = sr.cu1;
+        } else {
+          // periodic: [cu0, cu1] may extend below 0 or above nu-1
+          int a0 = sr.cu0, b0 = sr.cu1;
+          if (a0 < 0) {
+            if (part == 0) { cu_a = a0 + g.nu; cu_b = g.nu - 1; }
+            else { cu_a = 0; cu_b = b0; }
+          } else if (b0 >= g.nu) {
+            if (part == 0) { cu_a = a0; cu_b = g.nu - 1; }
+            else { cu_a = 0; cu_b = b0 - g.nu; }
+          } else {
+            if (part) break;
+            cu_a = a0;
+            cu_b = b0;
+          }
+        }
+        const int64_t c_lo = (int64_t)cu_a + (int64_t)g.nu * cv;
+        const int64_t c_hi = (int64_t)cu_b + (int64_t)g.nu * cv;
+        if (c_lo > c_hi || c_lo < 0 || c_hi >= ncells) continue;
+        const int32_t q_lo = so.cell_start[c_lo], q_hi = so.cell_start[c_hi + 1];
+        for (int32_t qb = q_lo; qb < q_hi; qb += kThreads) {
+          const int32_t q = qb + threadIdx.x;
+          int sel = 0, rel = 0;
+          double c = 0.0;
+          if (q < q_hi) {
+            double d;
+            if (lp.loctype == 1)
+              d = distance(so.u[q], so.v[q], zu, zv, lp.metric);
+            else
+              d = fabs(__dsub_rn(so.u[q], zu));
+            double w;
+            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+              rel = (d <= R);
+              double t = d / L;
+              w = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
+            } else {
+              w = locfun(d / L);
+              rel = (d <= R) && (w != 0.0);
+            }
+            sel = rel || !lp.localise;
+            if (sel) c = w * (w / so.r[q]);
+          }
+          nrel_local += rel;
+          unsigned ball = __ballot_sync(0xffffffffu, sel);
+          if (lane == 0) zs.warp_cnt[warp] = __popc(ball);
+          __syncthreads();
+          int base = zs.list_len, before = 0, total = 0;
+          for (int w2 = 0; w2 < kThreads / 32; w2++) {
+            int cnt = zs.warp_cnt[w2];
+            before += (w2 < warp) ? cnt : 0;
+            total += cnt;
+          }
+          if (sel) {
+            int slot = base + before + __popc(ball & ((1u << lane) - 1u));
+            zs.list_q[slot] = q;
+            zs.list_c[slot] = c;
+          }
+          __syncthreads();
+          if (threadIdx.x == 0) zs.list_len = base + total;
+          __syncthreads();
+          if (zs.list_len >= kFlushAt) {
+            int len = zs.list_len;
+            flush_list<MAXE>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, E, nent);
+            __syncthreads();
+            if (threadIdx.x == 0) zs.list_len = 0;
+            __syncthreads();
+          }
+        }
+      }
+    }
+    if (zs.list_len > 0) {
+      int len = zs.list_len;
+      flush_list<MAXE>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, E, nent);
+    }
+    // relevant-observation count of the zone
+    for (int o = 16; o > 0; o >>= 1) nrel_local += __shfl_xor_sync(0xffffffffu, nrel_local, o);
+    if (lane == 0) atomicAdd(&zs.nrel, nrel_local);
+    __syncthreads();
+    const int nrel = zs.nrel;
+    if (threadIdx.x == 0) nobs[z] = nrel;
+    if (nrel > 0) {
+      double* Gz = G + (int64_t)zl * N * N;
+#pragma unroll
+      for (int s = 0; s < MAXE; s++) {
+        int e = threadIdx.x + s * kThreads;
+        if (e < E) {
+          Gz[ea[s] * N + eb[s]] = acc[s];
+          Gz[eb[s] * N + ea[s]] = acc[s];
+        } else if (e < nent) {
+          gv[(int64_t)zl * N + ea[s]] = acc[s];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Global analysis (rrsqrt.F90:196-208): every observation, D = 1 (DiagCovar): c_j = 1/r_j.
+// Observations in chunks of CH; partial sums per CTA added atomically into G (zeroed).
+template <int MAXE>
+__global__ void __launch_bounds__(kThreads)
+    k_global_gram_fp64(int64_t m, int N, const double* __restrict__ HSf, int64_t ldH,
+                       const double* __restrict__ yo, const double* __restrict__ Hxf,
+                       const double* __restrict__ r, double* __restrict__ G,
+                       double* __restrict__ gv, int CH) {
+  extern __shared__ double dyn[];
+  double* sh = dyn;
+  double* st = sh + CH * N;
+  double* sinn = st + CH * N;
+  const int E = N * (N + 1) / 2;
+  const int nent = E + N;
+  int32_t ea[MAXE], eb[MAXE];
+  double acc[MAXE];
+#pragma unroll
+  for (int s = 0; s < MAXE; s++) {
+    int e = threadIdx.x + s * kThreads;
+    acc[s] = 0.0;
+    if (e < E) {
+      int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+      while ((a + 1) * (a + 2) / 2 <= e) a++;
+      while (a * (a + 1) / 2 > e) a--;
+      ea[s] = a;
+      eb[s] = e - a * (a + 1) / 2;
+    } else {
+      ea[s] = (e < nent) ? e - E : 0;
+      eb[s] = 0;
+    }
+  }
+  for (int64_t j0 = (int64_t)blockIdx.x * CH; j0 < m; j0 += (int64_t)gridDim.x * CH) {
+    int rows = (int)((m - j0 < CH) ? (m - j0) : CH);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < rows * N; idx += kThreads) {
+      int k = idx / rows, i = idx - k * rows;  // coalesced along observations
+      double h = HSf[j0 + i + (int64_t)k * ldH];
+      double c = 1.0 / r[j0 + i];
+      sh[i * N + k] = h;
+      st[i * N + k] = c * h;
+    }
+    for (int i = threadIdx.x; i < rows; i += kThreads)
+      sinn[i] = (1.0 / r[j0 + i]) * (yo[j0 + i] - Hxf[j0 + i]);
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < MAXE; s++) {
+      int e = threadIdx.x + s * kThreads;
+      if (e < nent) {
+        double a = acc[s];
+        const int ia = ea[s], ib = eb[s];
+        if (e < E) {
+          for (int i = 0; i < rows; i++) a = fma(sh[i * N + ia], st[i * N + ib], a);
+        } else {
+          for (int i = 0; i < rows; i++) a = fma(sh[i * N + ia], sinn[i], a);
+        }
+        acc[s] = a;
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < MAXE; s++) {
+    int e = threadIdx.x + s * kThreads;
+    if (e < E) {
+      atomicAdd(&G[ea[s] * N + eb[s]], acc[s]);
+      if (ea[s] != eb[s]) atomicAdd(&G[eb[s] * N + ea[s]], acc[s]);
+    } else if (e < nent) {
+      atomicAdd(&gv[ea[s]], acc[s]);
+    }
+  }
+}
+
+inline int chunk_rows(int N) {
+  int ch = 4096 / N;
+  if (ch > 128) ch = 128;
+  if (ch < 8) ch = 8;
+  return ch;
+}
+
+template <int MAXE>
+cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
+                        int32_t nzc, const double* zone_xyzt, const double* corr_len,
+                        const double* max_len, double* d_G, double* d_g, int32_t* d_nobs,
+                        int brute, int32_t* d_work, cudaStream_t st) {
+  int CH = chunk_rows(N);
+  size_t smem = (size_t)(2 * CH * N + CH) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_zone_gram_fp64<MAXE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int blocks_per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zone_gram_fp64<MAXE>,
+                                                    kThreads, smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = sms * (blocks_per_sm > 0 ? blocks_per_sm : 1);
+  if (grid > nzc) grid = nzc > 0 ? nzc : 1;
+  e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  k_zone_gram_fp64<MAXE><<<grid, kThreads, smem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt,
+                                                        corr_len, max_len, d_G, d_g, d_nobs,
+                                                        brute, CH, d_work);
+  return cudaGetLastError();
+}
+
+template <int MAXE>
+cudaError_t launch_global(int64_t m, int N, const double* HSf, int64_t ldH, const double* yo,
+                          const double* Hxf, const double* r, double* d_G, double* d_g,
+                          cudaStream_t st) {
+  int CH = chunk_rows(N);
+  size_t smem = (size_t)(2 * CH * N + CH) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_global_gram_fp64<MAXE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int64_t chunks = (m + CH - 1) / CH;
+  int grid = (int)(chunks < 152 * 2 ? (chunks < 1 ? 1 : chunks) : 152 * 2);
+  e = cudaMemsetAsync(d_G, 0, sizeof(double) * N * N, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(d_g, 0, sizeof(double) * N, st);
+  if (e != cudaSuccess) return e;
+  k_global_gram_fp64<MAXE><<<grid, kThreads, smem, st>>>(m, N, HSf, ldH, yo, Hxf, r, d_G, d_g,
+                                                          CH);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int max_fp64_ensemble() { return 112; }
+
+// Per-thread entry count classes: ceil((N(N+1)/2 + N) / 256).
+#define OAKG_GRAM_DISPATCH(FN, ...)                                         \
+  do {                                                                      \
+    int ent_ = N * (N + 1) / 2 + N;                                         \
+    int per_ = (ent_ + kThreads - 1) / kThreads;                            \
+    if (per_ <= 3) return FN<3>(__VA_ARGS__);                               \
+    if (per_ <= 9) return FN<9>(__VA_ARGS__);                               \
+    if (per_ <= 19) return FN<19>(__VA_ARGS__);                             \
+    if (per_ <= 26) return FN<26>(__VA_ARGS__);                             \
+    return cudaErrorInvalidValue;                                           \
+  } while (0)
+
+cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                           int32_t z0, int32_t nzc, const double* zone_xyzt,
+                           const double* corr_len, const double* max_len, double* d_G,
+                           double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                           cudaStream_t st) {
+  OAKG_GRAM_DISPATCH(launch_zone, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len, d_G, d_g,
+                     d_nobs, brute, d_work, st);
+}
+
+cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,
+                             const double* yo, const double* Hxf, const double* r, double* d_G,
+                             double* d_g, cudaStream_t st) {
+  OAKG_GRAM_DISPATCH(launch_global, m, N, HSf, ldH, yo, Hxf, r, d_G, d_g, st);
+}
+
+}  // namespace oakg

@@ -1,0 +1,197 @@
+"""Seeded synthetic workloads with the shapes and value distributions of the benchmark
+configurations (the reference publishes no dataset for this path; these stand in for it).
+
+* ``global_case``  -- one 2-D field 100 x 80, N = 30 members, m = 500 observations at distinct
+  uniform cells, y = x_true + N(0, 0.1^2), R = 0.01 I (global analysis, rrsqrt.F90:196-208).
+* ``local_case``   -- 3-D grid 360 x 180 x 20, one variable, N = 64 members (Gaussian
+  random fields, horizontal length 8 cells, vertical 3 levels), m = 50,000 observations
+  (70 % on 40 great-circle-like tracks, 30 % uniform, noise sd 0.1), zones = the 64,800
+  vertical columns, Gaspari-Cohn localisation with support radius 12 cells
+  (locfun(d/6), maxLength = 12), Cartesian cell-index coordinates (metrictype = 0).
+  ``scale`` shrinks the horizontal grid and observation count for tests.
+
+Random fields: white N(0,1) noise convolved (FFT, periodic) with g(r) = exp(-(r/l)^2)
+per axis, renormalised to sample standard deviation 1. Seeds are 1000*config + role
+(0 truth, 1..N members, 900 positions, 901 noise, 902 tracks).
+
+State layout: zones are vertical columns, so the state vector is ordered column by column
+(the partition-sorted order the reference builds with initPartition/zoneIndex,
+assimilation.F90:578-641): element (i, j, k) sits at ((j*nx + i) * nz + k).
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    xf: np.ndarray          # (n,)
+    Hxf: np.ndarray         # (m,)
+    yo: np.ndarray          # (m,)
+    Sf: np.ndarray          # (n, N) Fortran order
+    HSf: np.ndarray         # (m, N) Fortran order
+    r_diag: np.ndarray      # (m,)
+    x_true: np.ndarray      # (n,)
+    zone_size: np.ndarray | None = None   # (Z,) int32
+    zone_pos: np.ndarray | None = None    # (Z, 4)
+    obs_pos: tuple | None = None          # (x, y, z, t)
+    corr_len: np.ndarray | None = None    # (Z,)
+    max_len: np.ndarray | None = None     # (Z,)
+    weight: int = 1                       # Gaspari-Cohn
+    metric: int = 0
+    loctype: int = 1
+    obs_index: np.ndarray | None = None   # (m,) state index observed (nearest cell H)
+    Ef: np.ndarray | None = None          # (n, N) ensemble, when kept
+    HEf: np.ndarray | None = None
+
+    @property
+    def n(self):
+        return self.xf.size
+
+    @property
+    def N(self):
+        return self.Sf.shape[1]
+
+    @property
+    def m(self):
+        return self.yo.size
+
+    @property
+    def Z(self):
+        return 0 if self.zone_size is None else self.zone_size.size
+
+
+def gaussian_field(shape, lengths, rng, dtype=np.float64):
+    """White noise convolved with exp(-(r/l)^2) per axis (periodic FFT), sd renormalised to 1."""
+    noise = rng.standard_normal(shape)
+    F = np.fft.rfftn(noise)
+    for ax, (nax, l) in enumerate(zip(shape, lengths)):
+        if l <= 0:
+            continue
+        if ax == len(shape) - 1:
+            k = np.fft.rfftfreq(nax)
+        else:
+            k = np.fft.fftfreq(nax)
+        # Fourier transform of exp(-(x/l)^2) (up to a constant): exp(-(pi l k)^2)
+        tf = np.exp(-((np.pi * l * k) ** 2))
+        sh = [1] * len(shape)
+        sh[ax] = tf.size
+        F = F * tf.reshape(sh)
+    f = np.fft.irfftn(F, s=shape, axes=tuple(range(len(shape))))
+    f = f / f.std()
+    return f.astype(dtype, copy=False)
+
+
+def _anomalies(Ef, HEf):
+    N = Ef.shape[1]
+    xf = Ef.mean(axis=1)
+    Hxf = HEf.mean(axis=1)
+    s = np.sqrt(N - 1.0)
+    Sf = np.asfortranarray((Ef - xf[:, None]) / s)
+    HSf = np.asfortranarray((HEf - Hxf[:, None]) / s)
+    return xf, Hxf, Sf, HSf
+
+
+def global_case(keep_ensemble=False) -> Case:
+    """Config: global analysis, 100 x 80 field, N = 30, m = 500, R = 0.01 I."""
+    cfg = 0
+    nx, ny, N, m, ell = 100, 80, 30, 500, 10.0
+    truth = gaussian_field((ny, nx), (ell, ell), np.random.default_rng(1000 * cfg + 0)).reshape(-1)
+    Ef = np.empty((nx * ny, N), order="F")
+    for k in range(N):
+        Ef[:, k] = gaussian_field((ny, nx), (ell, ell),
+                                  np.random.default_rng(1000 * cfg + 1 + k)).reshape(-1)
+    idx = np.random.default_rng(1000 * cfg + 900).choice(nx * ny, size=m, replace=False)
+    noise = np.random.default_rng(1000 * cfg + 901).standard_normal(m) * 0.1
+    yo = truth[idx] + noise
+    HEf = Ef[idx, :]
+    xf, Hxf, Sf, HSf = _anomalies(Ef, HEf)
+    c = Case("global 100x80 N=30 m=500", xf, Hxf, yo, Sf, HSf, np.full(m, 0.01), truth,
+             obs_index=idx)
+    if keep_ensemble:
+        c.Ef, c.HEf = Ef, HEf
+    return c
+
+
+def _track_obs(nx, ny, m_track, ntracks, rng):
+    """Observation (i, j) cells on great-circle-like tracks
+    j = ny/2 + (ny/2) atan(tan(a) sin(2 pi (i - i0)/nx)) / (pi/2)."""
+    per = np.full(ntracks, m_track // ntracks)
+    per[: m_track - per.sum()] += 1
+    ii, jj = [], []
+    for t in range(ntracks):
+        a = np.deg2rad(rng.uniform(10.0, 80.0))
+        i0 = rng.uniform(0.0, nx)
+        i = rng.uniform(0.0, nx, per[t])
+        j = ny / 2 + (ny / 2) * np.arctan(np.tan(a) * np.sin(2 * np.pi * (i - i0) / nx)) / (np.pi / 2)
+        ii.append(np.clip(np.rint(i), 0, nx - 1).astype(np.int64))
+        jj.append(np.clip(np.rint(j), 0, ny - 1).astype(np.int64))
+    return np.concatenate(ii), np.concatenate(jj)
+
+
+def local_case(scale=1.0, N=64, nz=20, m=50_000, radius=12.0, seed_cfg=1, track_frac=0.7,
+               ntracks=40, dtype=np.float64, keep_ensemble=False) -> Case:
+    """Config: local analysis 360 x 180 x 20, N = 64, m = 50,000, GC radius 12 cells.
+
+    ``scale`` < 1 shrinks nx, ny by ``scale`` and m by ``scale**2`` (observation density kept).
+    """
+    nx = max(4, int(round(360 * scale)))
+    ny = max(4, int(round(180 * scale)))
+    if scale != 1.0:
+        m = max(1, int(round(m * scale * scale)))
+    cfg = seed_cfg
+    shape = (ny, nx, nz)
+    lengths = (8.0, 8.0, 3.0)
+    n = nx * ny * nz
+    truth = gaussian_field(shape, lengths, np.random.default_rng(1000 * cfg + 0)).reshape(-1)
+    Ef = np.empty((n, N), order="F", dtype=np.float64)
+    for k in range(N):
+        Ef[:, k] = gaussian_field(shape, lengths,
+                                  np.random.default_rng(1000 * cfg + 1 + k)).reshape(-1)
+    # observations: track part + uniform part, nearest cell, random level
+    rng_pos = np.random.default_rng(1000 * cfg + 900)
+    m_track = int(round(track_frac * m))
+    ti, tj = _track_obs(nx, ny, m_track, ntracks, np.random.default_rng(1000 * cfg + 902))
+    ui = rng_pos.integers(0, nx, m - m_track)
+    uj = rng_pos.integers(0, ny, m - m_track)
+    oi = np.concatenate([ti, ui])
+    oj = np.concatenate([tj, uj])
+    ok = rng_pos.integers(0, nz, m)
+    idx = (oj * nx + oi) * nz + ok   # state index (column-ordered layout)
+    noise = np.random.default_rng(1000 * cfg + 901).standard_normal(m) * 0.1
+    yo = truth[idx] + noise
+    HEf = Ef[idx, :]
+    xf, Hxf, Sf, HSf = _anomalies(Ef, HEf)
+    Z = nx * ny
+    zone_size = np.full(Z, nz, dtype=np.int32)
+    zc = np.arange(Z)
+    zone_pos = np.zeros((Z, 4))
+    zone_pos[:, 0] = zc % nx   # x = i
+    zone_pos[:, 1] = zc // nx  # y = j
+    obs_pos = (oi.astype(np.float64), oj.astype(np.float64), ok.astype(np.float64),
+               np.zeros(m))
+    corr = np.full(Z, radius / 2.0)
+    maxl = np.full(Z, radius)
+    c = Case(f"local {nx}x{ny}x{nz} N={N} m={m} GC radius {radius:g}", xf, Hxf, yo,
+             Sf.astype(dtype, copy=False), HSf.astype(dtype, copy=False), np.full(m, 0.01),
+             truth, zone_size, zone_pos, obs_pos, corr, maxl, weight=1, metric=0, loctype=1,
+             obs_index=idx)
+    if keep_ensemble:
+        c.Ef, c.HEf = Ef, HEf
+    return c
+
+
+def rrsqrt_test_case():
+    """The known-answer case of test/test_rrsqrt.F90:277-322: n = 10, m = 5, N = 12,
+    Ef(i) = sin(3 i^2) (column-major fill), H = reshape(1..50, [5, 10]), y = 1..5, R = 2 I."""
+    n, m, N = 10, 5, 12
+    i = np.arange(1, n * N + 1, dtype=np.float64)
+    Ef = np.sin(3.0 * i * i).reshape(N, n).T.copy()
+    H = np.arange(1, m * n + 1, dtype=np.float64).reshape(n, m).T.copy()
+    y = np.arange(1, m + 1, dtype=np.float64)
+    xf = Ef.sum(axis=1) / N
+    Sf = (Ef - xf[:, None]) / np.sqrt(N - 1.0)
+    return xf, Sf, H, y, np.full(m, 2.0)

@@ -1,0 +1,267 @@
+"""NumPy restatement of OAK's local ensemble square-root analysis (test oracle).
+
+This module is TEST INFRASTRUCTURE. Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import it, and only as the checker: the product path
+(``oak_gb300`` + ``liboakg.so``) never calls into it.
+
+Every function restates one routine of the reference (gher-uliege/OAK 1.7, Fortran), in the
+reference's own argument order, with 0-based indices where the reference is 1-based.
+Arrays follow the reference layout: state/observation vectors are 1-D, ensembles are
+``(n, N)`` matrices (members are columns).
+
+Pinned against the reference's own known-answer tests (``test/test_rrsqrt.F90`` Kalman-formula
+identities, ``test/test_covariance.F90:612-617`` ``locfun`` values) by
+``tests/test_oracle_golden.py``.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# Metric codes (assimilation.F90:108-112)
+CARTESIAN = 0
+SPHERICAL = 1
+SPHERICAL_APPROX = 2
+
+# Weight kinds: the reference Gaussian with cut-off (assimilation.F90:3756-3767) and the
+# Gaspari-Cohn function (covariance.F90:645-667) as used by test/test_rrsqrt.F90:254-271.
+GAUSS_CUTOFF = 0
+GASPARI_COHN = 1
+
+EARTH_RADIUS = 6378137.0  # m, assimilation.F90:3643
+PI = 3.141592653589793238462643383279502884197
+
+
+def locfun(r):
+    """Gaspari-Cohn 5th-order piecewise rational function (covariance.F90:645-667)."""
+    r = np.asarray(r, dtype=np.float64)
+    out = np.zeros_like(r)
+    a = r <= 1.0
+    b = (r > 1.0) & (r <= 2.0)
+    ra = r[a]
+    out[a] = (((-ra / 4.0 + 1.0 / 2.0) * ra + 5.0 / 8.0) * ra - 5.0 / 3.0) * ra**2 + 1.0
+    rb = r[b]
+    out[b] = ((((rb / 12.0 - 1.0 / 2.0) * rb + 5.0 / 8.0) * rb + 5.0 / 3.0) * rb - 5.0) * rb \
+        + 4.0 - 2.0 / (3.0 * rb)
+    return out
+
+
+def distance(x0, y0, x1, y1, metric):
+    """Distance between p0 = (x0, y0) and p1 = (x1, y1) (assimilation.F90:3635-3672),
+    elementwise with NumPy broadcasting."""
+    x0 = np.asarray(x0, dtype=np.float64)
+    y0 = np.asarray(y0, dtype=np.float64)
+    x1 = np.asarray(x1, dtype=np.float64)
+    y1 = np.asarray(y1, dtype=np.float64)
+    if metric == CARTESIAN:
+        dx = x1 - x0
+        dy = y1 - y0
+        return np.sqrt(dx * dx + dy * dy)
+    if metric == SPHERICAL_APPROX:
+        coeff = PI * EARTH_RADIUS / 180.0
+        a = coeff * np.cos((y0 + y1) * (PI / 360.0)) * (x1 - x0)
+        b = coeff * (y1 - y0)
+        return np.sqrt(a * a + b * b)
+    if metric == SPHERICAL:
+        d2r = PI / 180.0
+        a = y0 * d2r
+        b = y1 * d2r
+        c = (x1 - x0) * d2r
+        coeff = np.sin(b) * np.sin(a) + np.cos(b) * np.cos(a) * np.cos(c)
+        coeff = np.clip(coeff, -1.0, 1.0)
+        return EARTH_RADIUS * np.arccos(coeff)
+    raise ValueError(f"unsupported metric {metric}")
+
+
+def select_observations(zone_pos, obs_pos, corr_len, max_len, metric=CARTESIAN,
+                        loctype=1, kind=GAUSS_CUTOFF):
+    """Per-zone observation selection (assimilation.F90:3683-3771).
+
+    ``zone_pos`` = (x, y, z, t) of the zone's first element (assimilation.F90:3713-3740);
+    ``obs_pos`` = (obsGridX, obsGridY, obsGridZ, obsGridT) arrays.
+    Returns ``(weight, relevant)`` over all m observations.
+
+    GAUSS_CUTOFF: relevant = d <= maxLength (:3756), weight = exp(-(d/L)^2) (:3767).
+    GASPARI_COHN: weight = locfun(d/L) (covariance.F90:645), relevant = d <= maxLength and
+    weight /= 0 (the selection rule of test/test_rrsqrt.F90:268-269).
+    """
+    if loctype == 1:
+        # p0 = observation, p1 = zone position, as in assimilation.F90:3749
+        d = distance(obs_pos[0], obs_pos[1], zone_pos[0], zone_pos[1], metric)
+    elif loctype == 2:
+        d = np.abs(np.asarray(obs_pos[2], dtype=np.float64) - zone_pos[2])
+    else:
+        d = np.abs(np.asarray(obs_pos[3], dtype=np.float64) - zone_pos[3])
+    if kind == GAUSS_CUTOFF:
+        relevant = d <= max_len
+        if relevant.any():
+            weight = np.exp(-((d / corr_len) ** 2))
+        else:
+            weight = d
+    else:
+        weight = locfun(d / corr_len)
+        relevant = (d <= max_len) & (weight != 0)
+    return weight, relevant
+
+
+def perp_space(w):
+    """n-1 orthonormal vectors perpendicular to w (matoper.F90:509-535, Hoteit et al. 2002)."""
+    w = np.asarray(w, dtype=np.float64)
+    n = w.size
+    alpha = -1.0 / (abs(w[n - 1]) + 1.0)
+    H = np.zeros((n, n - 1))
+    H[: n - 1, :] = alpha * np.outer(w[: n - 1], w[: n - 1]) + np.eye(n - 1)
+    sgn = 1.0 if w[n - 1] >= 0 else -1.0  # Fortran sign(1., x) with x = +0 or -0 -> +1 for +0
+    if w[n - 1] == 0.0 and math.copysign(1.0, w[n - 1]) < 0:
+        sgn = -1.0
+    H[n - 1, :] = alpha * (w[n - 1] + sgn) * w[: n - 1]
+    return H
+
+
+def normate(v):
+    """v / ||v|| (rrsqrt.F90:748-756)."""
+    v = np.asarray(v, dtype=np.float64)
+    return v / np.sqrt(np.sum(v**2))
+
+
+def rotate_vector(w, v):
+    """Orthogonal matrix Omega with Omega w = v (rrsqrt.F90:737-742)."""
+    return np.outer(v, w) + perp_space(v) @ perp_space(w).T
+
+
+def analysis_increment(Hxf, yo, Sf, HSf, rinv_eff, rotate=True):
+    """Analysis increment and anomalies (rrsqrt.F90:100-190).
+
+    ``rinv_eff`` is the diagonal of the (localised) inverse observation error covariance,
+    i.e. ``R%mldivide`` for DiagCovar (covariance.F90:425-432) or DCDCovar with D = w
+    (covariance.F90:612-619): ``w**2 / r``.
+    Returns ``(xa_xf, Sa, ampl)``.
+    """
+    HSf = np.asarray(HSf, dtype=np.float64)
+    Sf = np.asarray(Sf, dtype=np.float64)
+    N = Sf.shape[1]
+    temp = HSf.T @ (rinv_eff[:, None] * HSf)  # :135 (HSf .tx. R%mldivide(HSf))
+    lam, U = np.linalg.eigh(temp, UPLO="L")  # :136 symeig -> dsyev('V','L')
+    lam = np.where(lam < 0, 0.0, lam)  # :137
+    lam = 1.0 / (1.0 + lam)  # :140
+    ampl = U @ (lam * (U.T @ (HSf.T @ (rinv_eff * (yo - Hxf)))))  # :142
+    if np.any(ampl != ampl):  # :145-149
+        raise FloatingPointError("NaN in analysis amplitudes")
+    xa_xf = Sf @ ampl  # :151
+    sqrt_lam = np.sqrt(lam)  # :162
+    if rotate:  # ROTATE_ENSEMBLE (:24, :165-185)
+        w = np.full(N, 1.0 / np.sqrt(1.0 * N))
+        v = U @ (np.sum(U, axis=0) / sqrt_lam)
+        v = normate(v)
+        Sa = Sf @ (U @ (sqrt_lam[:, None] * (U.T @ rotate_vector(w, v))))
+    else:
+        Sa = Sf @ (U @ (sqrt_lam[:, None] * U.T))
+    return xa_xf, Sa, ampl
+
+
+def analysis(xf, Hxf, yo, Sf, HSf, r_diag, rotate=True):
+    """Global analysis with diagonal R (rrsqrt.F90:196-208). Returns ``(xa, Sa, ampl)``."""
+    rinv = 1.0 / np.asarray(r_diag, dtype=np.float64)
+    xa_xf, Sa, ampl = analysis_increment(Hxf, yo, Sf, HSf, rinv, rotate)
+    return xf + xa_xf, Sa, ampl
+
+
+def loc_analysis(zone_size, select, xf, Hxf, yo, Sf, HSf, r_diag, localise_obs=True,
+                 rotate=True):
+    """Local analysis (rrsqrt.F90:258-466) with a selection callback.
+
+    ``select(zi, start_index) -> (weight(m), relevant(m))`` plays the role of
+    ``selectObservations`` (called with the zone's first state index, :368).
+    Returns ``(xa, Sa, amplitudes(N, Z), nobs(Z))``. As in the reference, ``amplitudes`` is
+    only filled in the non-localised branch (:375-384); zones without relevant
+    observations keep ``xa_xf = 0`` and ``Sa = Sf`` (:322-326, :371).
+    """
+    xf = np.asarray(xf, dtype=np.float64)
+    Sf = np.asarray(Sf, dtype=np.float64)
+    HSf = np.asarray(HSf, dtype=np.float64)
+    yo = np.asarray(yo, dtype=np.float64)
+    Hxf = np.asarray(Hxf, dtype=np.float64)
+    r_diag = np.asarray(r_diag, dtype=np.float64)
+    m = yo.size
+    N = Sf.shape[1]
+    Z = len(zone_size)
+    xa_xf = np.zeros_like(xf)
+    Sa = Sf.copy()
+    amplitudes = np.zeros((N, Z))
+    nobs = np.zeros(Z, dtype=np.int64)
+    ends = np.cumsum(zone_size)
+    starts = ends - np.asarray(zone_size)
+    for zi in range(Z):
+        i1, i2 = int(starts[zi]), int(ends[zi])
+        weight, relevant = select(zi, i1)
+        nb = int(np.count_nonzero(relevant))
+        nobs[zi] = nb
+        if nb == 0:
+            continue
+        if not localise_obs:
+            rinv = weight**2 / r_diag
+            dxa, dSa, ampl = analysis_increment(Hxf, yo, Sf[i1:i2], HSf, rinv, rotate)
+            amplitudes[:, zi] = ampl
+        elif nb == m:
+            rinv = weight**2 / r_diag
+            dxa, dSa, _ = analysis_increment(Hxf, yo, Sf[i1:i2], HSf, rinv, rotate)
+        else:
+            sel = np.nonzero(relevant)[0]
+            rinv = weight[sel] ** 2 / r_diag[sel]
+            dxa, dSa, _ = analysis_increment(Hxf[sel], yo[sel], Sf[i1:i2], HSf[sel], rinv,
+                                             rotate)
+        xa_xf[i1:i2] = dxa
+        Sa[i1:i2] = dSa
+    return xf + xa_xf, Sa, amplitudes, nobs
+
+
+def geometric_selector(zone_pos, obs_pos, corr_len, max_len, metric=CARTESIAN, loctype=1,
+                       kind=GAUSS_CUTOFF):
+    """Selection callback built from zone/observation geometry, as the C ABI takes it.
+
+    ``zone_pos`` is ``(Z, 4)``; ``corr_len``/``max_len`` are per-zone ``(Z,)`` arrays
+    (hCorrLengthToObs / hMaxCorrLengthToObs at the zone's first element,
+    assimilation.F90:3756-3767).
+    """
+    def select(zi, _start):
+        return select_observations(zone_pos[zi], obs_pos, corr_len[zi], max_len[zi],
+                                   metric, loctype, kind)
+    return select
+
+
+def ensemble_prologue(Ef, HEf):
+    """Mean and scaled anomalies of an ensemble (assimilation.F90:3127-3134, ASSIM_SCALING=1).
+
+    Returns ``(xf, Hxf, Sf, HSf)`` with ``Sf = (Ef - xf) / sqrt(N-1)``.
+    """
+    N = Ef.shape[1]
+    scaling = math.sqrt(N - 1.0)
+    xf = Ef.sum(axis=1) / N
+    Hxf = HEf.sum(axis=1) / N
+    Sf = (Ef - xf[:, None]) / scaling
+    HSf = (HEf - Hxf[:, None]) / scaling
+    return xf, Hxf, Sf, HSf
+
+
+def ensemble_epilogue(xf, xa, Sa, inflation=1.0, max_correction=None):
+    """Inflation, correction clip and ensemble reconstruction (assimilation.F90:3299-3312,
+    3558-3565). Returns ``Ea``."""
+    N = Sa.shape[1]
+    if inflation != 1:
+        Sa = inflation * Sa
+    xa = xa.copy()
+    if max_correction is not None:
+        mc = np.asarray(max_correction, dtype=np.float64)
+        xa = np.where(xa - mc > xf, xf + mc, xa)
+        xa = np.where(xa < xf - mc, xf - mc, xa)
+    return xa[:, None] + Sa * math.sqrt(N - 1.0)
+
+
+def kalman_reference(xf, Sf, H, yo, R):
+    """Explicit Kalman formulas of test/test_rrsqrt.F90:49-56 (the reference's check)."""
+    Pf = Sf @ Sf.T
+    K = (Pf @ H.T) @ np.linalg.inv(H @ Pf @ H.T + R)
+    Pa = Pf - K @ (H @ Pf)
+    xa = xf + K @ (yo - H @ xf)
+    return xa, Pa

@@ -1,0 +1,38 @@
+"""The C ABI library builds for sm_103a, loads, and exports every function include/oakg.h
+declares. No compute call is made here (no GPU in the CPU suite)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from oak_gb300 import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "oakg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:int|void|size_t)\s+\**\s*(\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_reference_entry_points():
+    names = declared_functions()
+    for ref in ("oak_init", "oak_assim", "oak_done", "oakg_analysis", "oakg_locanalysis"):
+        assert ref in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib_path = build.build()
+    lib = ctypes.CDLL(lib_path)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_python_binding_loads():
+    build.build()
+    import oak_gb300
+    L = oak_gb300.lib()
+    assert L.oakg_last_status() == 0
