@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark of the local ensemble square-root analysis (OAK locAnalysis) on GB300.
+
+Workload (default): the local FP64 configuration -- 360 x 180 x 20 grid, one variable,
+N = 64 members, m = 50,000 observations (70 % on tracks), 64,800 column zones, Gaspari-Cohn
+localisation radius 12 cells. Synthetic seeded inputs of those shapes (oak_gb300.workloads).
+
+One step = one oakg_locanalysis call over all zones (observation binning, selection + Gram,
+eigensolve + transform, ensemble update). The metric is local analyses (zones) per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference algorithm on the host cores: the C/OpenMP restatement
+of rrsqrt.F90 / assimilation.F90 (oracle/oakref.c with LAPACK dsyev), a port because the
+Fortran reference cannot be compiled here (no Fortran compiler).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")  # BLAS inside each OpenMP thread (CPU leg)
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = ("local analyses/s: mixed-prec vs FP64 on GB300 at ≤1e-4 rel err; adjoint cost")
+UNIT = "local analyses/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--scale", type=float, default=1.0, help="horizontal scale of the workload")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="target CPU time of the cpu_baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_config(c, scale):
+    return {"workload": c.name, "zones": int(c.Z), "n": int(c.n), "N": int(c.N), "m": int(c.m),
+            "localisation": "Gaspari-Cohn locfun(d/6), maxLength 12 cells",
+            "precision": "fp64 (plain form)", "horizontal_scale": scale,
+            "l2": "inputs larger than L2 (Sf and Sa 664 MB each at full scale)"}
+
+
+# --------------------------------------------------------------------------- CPU baseline
+
+def cpu_sample(c, target_zones):
+    """A bounded sample of the workload: every k-th zone, all observations (the reference's
+    brute-force selection over all m observations stays in the sample's cost)."""
+    k = max(1, c.Z // max(1, target_zones))
+    zsel = np.arange(0, c.Z, k)
+    starts = np.concatenate([[0], np.cumsum(c.zone_size)[:-1]])
+    rows = np.concatenate([np.arange(starts[z], starts[z] + c.zone_size[z]) for z in zsel])
+    return zsel, rows
+
+
+def run_cpu_oracle(c, zsel, rows, threads):
+    from oracle import cref
+    t0 = time.perf_counter()
+    cref.locanalysis(c.zone_size[zsel], c.xf[rows], c.Hxf, c.yo, c.Sf[rows], c.HSf, c.r_diag,
+                     c.zone_pos[zsel], c.obs_pos, c.corr_len[zsel], c.max_len[zsel],
+                     kind=c.weight, metric=c.metric, loctype=c.loctype, nthreads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(c, seconds, threads):
+    """Times the C/OpenMP oracle on a zone sample sized for ~`seconds` of CPU work."""
+    zsel, rows = cpu_sample(c, 256)
+    dt = run_cpu_oracle(c, zsel, rows, threads)          # calibration
+    per_zone = dt / len(zsel)
+    target = int(min(c.Z, max(256, seconds / max(per_zone, 1e-9))))
+    zsel, rows = cpu_sample(c, target)
+    dt = run_cpu_oracle(c, zsel, rows, threads)
+    return {"value": len(zsel) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(zsel)} of {c.Z} zones (every {c.Z // len(zsel)}-th), all {c.m} "
+                      f"observations, brute-force selection as assimilation.F90:3745-3757, "
+                      f"LAPACK dsyev via SciPy, OpenMP dynamic schedule, {dt:.2f} s"}
+
+
+# --------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- GPU arm
+
+def algorithmic_work(c, nobs, stage):
+    """Algorithmic FP64 flops of one launch of a stage (per-zone counts x zones):
+    gram: p N (N+1) + 2 p N   (lower-triangular HS^T diag(c) HS plus HS^T diag(c) d)
+    eig:  9 N^3 (Householder tridiagonalisation + QR with vectors) + 2 N^3 + 4 N^2 (T, ampl)
+    update: 2 nz N^2 + 2 nz N (Sf T and Sf ampl), zones with observations."""
+    N = c.N
+    act = nobs > 0
+    p = nobs[act].astype(np.float64)
+    nz = c.zone_size[act].astype(np.float64)
+    if stage == "gram":
+        return float(np.sum(p * N * (N + 1) + 2 * p * N))
+    if stage == "eig":
+        return float(act.sum() * (11.0 * N ** 3 + 4.0 * N ** 2))
+    return float(np.sum(2 * nz * N * N + 2 * nz * N))
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+
+    import torch
+    import oak_gb300
+    from oak_gb300 import build as _build
+    from oak_gb300.workloads import local_case
+
+    # workload first (numpy), CPU baseline before any CUDA work
+    c = local_case(scale=args.scale)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(c, args.cpu_seconds, os.cpu_count() or 1)
+
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _build.build()
+    L = oak_gb300.lib()
+
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    F = lambda a: torch.as_tensor(np.ascontiguousarray(np.asarray(a).T), device=dev).t()
+    d_args = (T(c.zone_size), T(c.xf), T(c.Hxf), T(c.yo), F(c.Sf), F(c.HSf), T(c.r_diag),
+              T(c.zone_pos), tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
+    stream = torch.cuda.current_stream(dev)
+    L.oakg_set_stream(ctypes_ptr(stream.cuda_stream))
+
+    def step():
+        return oak_gb300.loc_analysis(*d_args, weight=c.weight, metric=c.metric,
+                                      loctype=c.loctype, want_ampl=False)
+
+    out = None
+    for _ in range(args.warmup):
+        out = step()
+    nobs = out[3].cpu().numpy()
+    peak_fp64 = ctypes_double()
+    L.oakg_fp64_peak(ctypes_ref(peak_fp64))
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    stage_ms = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = L.oakg_launch_count()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        for k, v in oak_gb300.last_timings().items():
+            stage_ms[k] += v
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    clk = clocks.stop()
+    launches = L.oakg_launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * c.Z / (ms / 1e3)
+
+    # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        def pinned(a, fortran=False):
+            a = np.asarray(a)
+            if fortran:
+                t = torch.empty((a.shape[1], a.shape[0]), dtype=torch.float64, pin_memory=True)
+                t.numpy()[...] = a.T
+                return t.numpy().T
+            t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0].copy()).dtype, pin_memory=True)
+            t.numpy()[...] = a
+            return t.numpy()
+        h = (pinned(c.zone_size), pinned(c.xf), pinned(c.Hxf), pinned(c.yo),
+             pinned(c.Sf, True), pinned(c.HSf, True), pinned(c.r_diag), pinned(c.zone_pos),
+             tuple(pinned(x) for x in c.obs_pos[:2]), pinned(c.corr_len), pinned(c.max_len))
+        h2d = sum(x.nbytes for x in h[:8]) + sum(x.nbytes for x in h[8]) + h[9].nbytes + h[10].nbytes
+        d2h = c.xf.nbytes + c.Sf.nbytes + c.Z * 4
+        outs = (pinned(np.zeros(c.n)), pinned(np.zeros((c.n, c.N)), True))
+
+        def hstep():
+            return oak_gb300.loc_analysis(*h, weight=c.weight, metric=c.metric,
+                                          loctype=c.loctype, want_ampl=False, out=outs)
+        hstep()
+        ksteps = max(1, min(args.steps, 3))
+        barrier()
+        torch.cuda.synchronize(dev)
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(ksteps):
+            hstep()
+        g1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        ems = g0.elapsed_time(g1) / ksteps
+        e2e = {"value": ws * c.Z / (ems / 1e3), "unit": UNIT, "ms_per_step": ems,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "host_buffers": "pinned"}
+    L.oakg_set_stream(None)
+
+    if rank != 0:
+        return
+    per_step = {k: v / args.steps for k, v in stage_ms.items()}
+    dom = max(("gram", "eig", "update"), key=lambda k: per_step[k])
+    kernel = {"gram": "k_zone_gram_fp64", "eig": "k_zone_eig_fp64",
+              "update": "k_zone_update_fp64"}[dom]
+    work = algorithmic_work(c, nobs, dom)
+    achieved = work / (per_step[dom] / 1e3) / 1e12
+    peak = peak_fp64.value
+    traffic = read_traffic(kernel)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, BASELINE shapes)",
+        "config": workload_config(c, args.scale) | {"parallelism": f"zones sharded, {ws} GPU(s)",
+                                                     "zones_with_obs": int((nobs > 0).sum())},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "stage_ms_per_step": per_step,
+        "roofline": {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak if peak > 0 else None,
+                     "peak_source": "measured FP64 FMA loop (oakg_fp64_peak) on this GPU",
+                     "traffic": traffic,
+                     "algorithmic_flops_per_launch": work},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        parts = ln.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args, ws, rank):
+    """The reference algorithm on the host cores (C/OpenMP port of rrsqrt.F90), rank 0 only."""
+    if rank != 0:
+        return
+    from oak_gb300.workloads import local_case
+    c = local_case(scale=args.scale)
+    threads = os.cpu_count() or 1
+    # size each step's sample for a few seconds of CPU work
+    zsel, rows = cpu_sample(c, 256)
+    per_zone = run_cpu_oracle(c, zsel, rows, threads) / len(zsel)
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    target = int(min(c.Z, max(256, budget / max(per_zone, 1e-9))))
+    zsel, rows = cpu_sample(c, target)
+    for _ in range(args.warmup):
+        run_cpu_oracle(c, zsel, rows, threads)
+    t = 0.0
+    for _ in range(args.steps):
+        t += run_cpu_oracle(c, zsel, rows, threads)
+    v = args.steps * len(zsel) / t
+    sample = (f"{len(zsel)} of {c.Z} zones per step (every {c.Z // len(zsel)}-th), all {c.m} "
+              f"observations, brute-force selection, LAPACK dsyev via SciPy, OpenMP dynamic")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded, BASELINE shapes)",
+        "config": workload_config(c, args.scale),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ctypes helpers (kept local so the module imports without the library)
+def ctypes_ptr(x):
+    import ctypes
+    return ctypes.c_void_p(x)
+
+
+def ctypes_double():
+    import ctypes
+    return ctypes.c_double(0.0)
+
+
+def ctypes_ref(x):
+    import ctypes
+    return ctypes.byref(x)
+
+
+if __name__ == "__main__":
+    main()

@@ -140,6 +140,20 @@ int oakg_release(void);
  * number of values written (<= n). */
 int oakg_last_timings(double* ms, int n);
 
+/* CUDA stream (a cudaStream_t) the library launches on for the current device; NULL
+ * restores the library's own stream. Calls still return only after their work is done.
+ * No reference counterpart (the reference has no device). */
+int oakg_set_stream(void* stream);
+
+/* Number of kernel launches the library has made in this process (all devices).
+ * No reference counterpart; used to account for device work in benchmarks. */
+int64_t oakg_launch_count(void);
+
+/* Diagnostic: measured FP64 FMA throughput of the current device in TFLOP/s (a
+ * dependent-FMA loop over all SMs, ~0.1 s). No reference counterpart; it is the roofline
+ * denominator of the FP64 kernels. */
+int oakg_fp64_peak(double* tflops);
+
 /* OAK's C interface (assimilation.F90:4885-4935). */
 void oak_init(const char* fname);
 void oak_assim(int ntime, int n, int r, double* Ef, double* Ea);

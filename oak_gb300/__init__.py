@@ -86,6 +86,12 @@ def lib() -> ctypes.CDLL:
     L.oakg_release.restype = ctypes.c_int
     L.oakg_last_timings.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
     L.oakg_last_timings.restype = ctypes.c_int
+    L.oakg_set_stream.argtypes = [P]
+    L.oakg_set_stream.restype = ctypes.c_int
+    L.oakg_launch_count.argtypes = []
+    L.oakg_launch_count.restype = ctypes.c_int64
+    L.oakg_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.oakg_fp64_peak.restype = ctypes.c_int
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -227,7 +233,7 @@ def analysis(xf, Hxf, yo, Sf, HSf, r_diag, *, want_sa=True, out=None):
 def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, corr_len,
                  max_len, *, weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1,
                  localise_obs=True, rotate=True, want_sa=True, want_ampl=True,
-                 ampl_always=False, brute_search=False, cell_size=0.0):
+                 ampl_always=False, brute_search=False, cell_size=0.0, out=None):
     """Local analysis (rrsqrt.F90:433-466) with geometric observation selection.
 
     ``zone_pos``: (Z, 4) x, y, z, t of each zone's first state element
@@ -236,7 +242,9 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     (hCorrLengthToObs / hMaxCorrLengthToObs at each zone's first element).
 
     Returns ``(xa, Sa, amplitudes (N, Z), nobs (Z,))``. As in the reference, amplitudes are
-    only written for the non-localised branch unless ``ampl_always`` is set.
+    only written for the non-localised branch unless ``ampl_always`` is set. ``out`` may give
+    preallocated ``(xa, Sa)`` arrays of the same memory kind as the inputs (e.g. pinned host
+    arrays).
     """
     Z = int(zone_size.shape[0])
     n = int(xf.shape[0])
@@ -258,8 +266,11 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
         zp = zone_pos.reshape(-1)
     else:
         zp = np.ascontiguousarray(np.asarray(zone_pos, dtype=np.float64).reshape(Z, 4))
-    xa = _empty_like_mode(device, (n,), like=like)
-    Sa = _empty_like_mode(device, (n, N), order="F", like=like) if want_sa else None
+    if out is not None:
+        xa, Sa = out
+    else:
+        xa = _empty_like_mode(device, (n,), like=like)
+        Sa = _empty_like_mode(device, (n, N), order="F", like=like) if want_sa else None
     if device and want_sa and ldS != n:
         raise OakError(ERR_ARGS, "device Sf with ld != n is not supported by this wrapper")
     ampl = _empty_like_mode(device, (N, Z), order="F", like=like) if want_ampl else None

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -21,6 +22,7 @@ namespace {
 thread_local std::string t_last_error;
 int g_last_status = OAKG_OK;
 std::mutex g_mutex;
+std::atomic<int64_t> g_launches{0};
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -66,12 +68,14 @@ struct Buf {
 enum BufId {
   B_ZONE_SIZE, B_XF, B_HXF, B_YO, B_R, B_SF, B_HSF, B_ZXYZT, B_OX, B_OY, B_OZ, B_OT, B_CORR,
   B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
-  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_COUNT_
+  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
+  B_COUNT_
 };
 
 struct Ctx {
   int device = -1;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;       // the stream launches go to (own or the caller's)
+  cudaStream_t own_stream = nullptr;
   cudaEvent_t ev[8] = {};
   Buf buf[B_COUNT_];
   double timings[5] = {0, 0, 0, 0, 0};
@@ -88,11 +92,12 @@ int get_ctx(Ctx** out) {
     Ctx* c = new Ctx();
     c->device = dev;
     // blocking stream: ordered after work the caller queued on the legacy default stream
-    e = cudaStreamCreate(&c->stream);
+    e = cudaStreamCreate(&c->own_stream);
     if (e != cudaSuccess) {
       delete c;
       return cuda_fail(e, "cudaStreamCreate");
     }
+    c->stream = c->own_stream;
     for (auto& ev : c->ev) cudaEventCreate(&ev);
     g_ctx[dev] = c;
   }
@@ -325,7 +330,12 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     g.csv = cs;
     g.nu = (int32_t)std::floor(spanu / cs) + 1;
     g.nv = (loc->loctype == 1) ? (int32_t)std::floor(spanv / cs) + 1 : 1;
-    if (g.periodic_u) g.nu = std::max(1, (int32_t)std::ceil(360.0 / cs));
+    if (g.periodic_u) {
+      // the periodic axis is cut into exactly nu cells of 360/nu degrees, so that cell
+      // index + nu is the same longitude one period later
+      g.nu = std::max(1, (int32_t)std::ceil(360.0 / cs));
+      g.csu = 360.0 / g.nu;
+    }
   }
   const int64_t ncells = (int64_t)g.nu * g.nv;
 
@@ -362,7 +372,7 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   cudaEventRecord(c->ev[1], st);
 
   // zone chunks
-  const size_t per_zone = (size_t)N * N * 8 + (size_t)N * 16 + 8;
+  const size_t per_zone = (size_t)N * N * 16 + (size_t)N * 16 + zone_eig_fp64_aux(N) * 8 + 8;
   int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
   if (chunk < 1) chunk = 1;
   if (chunk > Z) chunk = Z;
@@ -372,9 +382,13 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   if ((rc = scratch(c, B_GV, (size_t)chunk * N, &d_gv, "zone vectors"))) return rc;
   if ((rc = scratch(c, B_ZAMPL, (size_t)chunk * N, &d_za, "zone amplitudes"))) return rc;
   if ((rc = scratch(c, B_STATUS, (size_t)chunk + 1, &d_status, "zone status"))) return rc;
-  if ((rc = scratch(c, B_WORK, 4, &d_work, "work counters"))) return rc;
+  if ((rc = scratch(c, B_WORK, 8, &d_work, "work counters"))) return rc;
+  double *d_aux, *d_zvec;
+  if ((rc = scratch(c, B_AUX, (size_t)chunk * zone_eig_fp64_aux(N), &d_aux, "zone aux"))) return rc;
+  if ((rc = scratch(c, B_ZVEC, (size_t)chunk * N * N, &d_zvec, "zone eigenvectors"))) return rc;
   int32_t* d_status_all = d_work + 2;
   k_set_int<<<1, 1, 0, st>>>(d_status_all, 0);
+  count_launches(1);
   LocParams lp{loc->weight, loc->metric, loc->loctype, loc->localise_obs ? 1 : 0,
                loc->rotate ? 1 : 0, loc->flags};
   const int all_ampl = (!loc->localise_obs) || (loc->flags & OAKG_FLAG_AMPL_ALWAYS);
@@ -386,7 +400,8 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
                        d_nobs, brute, d_work, st);
     if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
     cudaEventRecord(c->ev[3], st);
-    e = zone_eig_fp64(N, nzc, d_G, d_gv, d_nobs + z0, lp.rotate, d_za, d_status, d_work + 1, st);
+    e = zone_eig_fp64(N, nzc, d_G, d_gv, d_nobs + z0, lp.rotate, d_za, d_status, d_aux, d_zvec,
+                      d_work + 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
     cudaEventRecord(c->ev[4], st);
     e = zone_update_fp64(N, (int32_t)z0, nzc, d_zstart, zone_max, d_xf, d_Sf, ldS, d_G, d_za,
@@ -398,6 +413,7 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
       if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
     }
     k_or_status<<<64, 256, 0, st>>>(d_status, nzc, d_status_all);
+    count_launches(1);
     if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
     t_gram += elapsed(c->ev[2], c->ev[3]);
     t_eig += elapsed(c->ev[3], c->ev[4]);
@@ -470,7 +486,10 @@ int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
   if ((rc = scratch(c, B_GV, (size_t)N, &d_gv, "Gram"))) return rc;
   if ((rc = scratch(c, B_ZAMPL, (size_t)N, &d_za, "amplitudes"))) return rc;
   if ((rc = scratch(c, B_STATUS, 2, &d_status, "status"))) return rc;
-  if ((rc = scratch(c, B_WORK, 4, &d_work, "work"))) return rc;
+  if ((rc = scratch(c, B_WORK, 8, &d_work, "work"))) return rc;
+  double *d_aux, *d_zvec;
+  if ((rc = scratch(c, B_AUX, zone_eig_fp64_aux(N), &d_aux, "zone aux"))) return rc;
+  if ((rc = scratch(c, B_ZVEC, (size_t)N * N, &d_zvec, "zone eigenvectors"))) return rc;
   if ((rc = scratch(c, B_NOBS, 2, &d_nobs, "nobs"))) return rc;
   if ((rc = scratch(c, B_ZSTART, 2, &d_zstart, "zone offsets"))) return rc;
   int64_t hz[2] = {0, n};
@@ -479,12 +498,13 @@ int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
   // The reference runs analysisIncrement even without observations; the result is then
   // xa = xf, Sa = Sf (G = 0 -> T = I, v = w -> Omega = I), which the copy path gives.
   k_set_int<<<1, 1, 0, st>>>(d_nobs, m > 0 ? 1 : 0);
+  count_launches(1);
   if (m > 0) {
     e = global_gram_fp64(m, N, d_HSf, ldH, d_yo, d_Hxf, d_r, d_G, d_gv, st);
     if (e != cudaSuccess) return cuda_fail(e, "Gram kernel");
   }
   cudaEventRecord(c->ev[2], st);
-  e = zone_eig_fp64(N, 1, d_G, d_gv, d_nobs, 1, d_za, d_status, d_work + 1, st);
+  e = zone_eig_fp64(N, 1, d_G, d_gv, d_nobs, 1, d_za, d_status, d_aux, d_zvec, d_work + 4, st);
   if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
   cudaEventRecord(c->ev[3], st);
   if (m == 0) cudaMemsetAsync(d_za, 0, N * sizeof(double), st);
@@ -529,7 +549,7 @@ int release_impl() {
     cudaStreamSynchronize(cp->stream);
     for (auto& b : cp->buf) b.release();
     for (auto& ev : cp->ev) cudaEventDestroy(ev);
-    cudaStreamDestroy(cp->stream);
+    cudaStreamDestroy(cp->own_stream);
     cudaSetDevice(prev);
     delete cp;
     cp = nullptr;
@@ -543,6 +563,24 @@ int timings_impl(double* ms, int n) {
   int k = std::min(n, 5);
   for (int i = 0; i < k; i++) ms[i] = g_ctx[dev]->timings[i];
   return k;
+}
+
+void count_launches(int k) { g_launches += k; }
+int64_t launch_total() { return g_launches.load(); }
+
+cudaStream_t current_stream() {
+  Ctx* c = nullptr;
+  if (get_ctx(&c) != OAKG_OK) return nullptr;
+  return c->stream;
+}
+
+int set_stream_impl(void* stream) {
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  cudaStreamSynchronize(c->stream);
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  return OAKG_OK;
 }
 
 void set_ok() {
@@ -602,6 +640,13 @@ int oakg_release(void) {
   std::lock_guard<std::mutex> lk(oakg::api_mutex());
   return oakg::release_impl();
 }
+
+int oakg_set_stream(void* stream) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  return oakg::set_stream_impl(stream);
+}
+
+int64_t oakg_launch_count(void) { return oakg::launch_total(); }
 
 int oakg_last_timings(double* ms, int n) {
   std::lock_guard<std::mutex> lk(oakg::api_mutex());

@@ -70,10 +70,12 @@ cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,
 // For zones [0, nzc) of a chunk with nobs > 0: eigen-decomposition of G (d_GT, N x N per
 // zone), T = U (I+L)^-1/2 U^T Omega written over G, ampl (N per zone), status per zone.
 // d_nobs/d_ampl/d_status are chunk-relative.
+// d_aux holds zone_eig_fp64_aux(N) doubles per zone, d_Z N*N doubles per zone;
+// d_work two counters.
 cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
                           const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
-                          int32_t* d_work, cudaStream_t st);
-size_t zone_eig_fp64_smem(int N);
+                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st);
+size_t zone_eig_fp64_aux(int N);
 
 // ---- zone_update_fp64.cu
 // xa = xf + Sf ampl, Sa = Sf T per zone; zones with nobs == 0 copy (xa = xf, Sa = Sf).
@@ -86,5 +88,10 @@ cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_amp
                              cudaStream_t st);
 
 int max_fp64_ensemble();  // largest N the FP64 kernels accept
+
+// ---- oakg_api.cu
+void count_launches(int k);       // kernel-launch accounting (oakg_launch_count)
+int64_t launch_total();
+cudaStream_t current_stream();    // stream of the current device's context
 
 }  // namespace oakg

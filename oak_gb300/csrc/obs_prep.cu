@@ -259,6 +259,7 @@ inline int grid_for(int64_t n, int threads) {
 cudaError_t obs_bounds(const double* u, const double* v, int64_t m, double* d_out4,
                        cudaStream_t st) {
   k_bounds<<<1, 1024, 0, st>>>(u, v, m, d_out4);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -290,6 +291,7 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
     dim3 tb(32, 8), tg((unsigned)((m + 31) / 32), (unsigned)((N + 31) / 32));
     k_transpose_rows<<<tg, tb, 0, st>>>(m, N, HSf, ldH, d_pos, d_HSt);
   }
+  count_launches(m > 0 ? 7 : 1);
   return cudaGetLastError();
 }
 
@@ -297,6 +299,7 @@ cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_st
                          int32_t* d_zone_max, cudaStream_t st) {
   k_scan_single<int32_t, int64_t><<<1, kScanThreads, 0, st>>>(zone_size, Z, d_zone_start,
                                                               d_zone_max);
+  count_launches(1);
   return cudaGetLastError();
 }
 

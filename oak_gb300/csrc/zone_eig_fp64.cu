@@ -10,17 +10,20 @@
 //       w = 1/sqrt(N),  v = normate(U (colsum(U) / sqrt(lambda)))
 // T (N x N, row-major, T[k][c]) overwrites G's slot; Sa = Sf T is formed by K5.
 //
-// Algorithm (one CTA per zone, matrix in shared memory, all FP64):
-//  1. Householder tridiagonalisation A = Q_h Tri Q_h^T (Golub & Van Loan, Matrix
-//     Computations 4th ed., 8.3.1), reflector vectors kept below the sub-diagonal.
-//  2. Q_h formed explicitly by backward accumulation (GvL 5.1.6).
-//  3. Implicit symmetric QR sweeps with Wilkinson shift (GvL 8.3.3-8.3.5) on (d, e): one warp
-//     runs the bulge chase and records the Givens rotations of a sweep, then the CTA applies
-//     them to the rows of Q.
-//  4. With Q = U: ampl, v, T_sym = U diag(sqrt(lambda)) U^T (lower triangle + mirror), then
-//     T = T_sym Omega applied in O(N^2): with P_x = I - u_x u_x^T / (1 + |x_N|),
-//     u_x = x + sign(x_N) e_N (the reflector whose first N-1 columns are perpSpace(x),
-//     matoper.F90:509-535), Omega = P_v P_w + (1 - s_v s_w) v w^T.
+// GB300 executes one FP64 warp instruction per 16 SM cycles whatever its active-lane mask,
+// so FP64 work is arranged to keep all 32 lanes busy:
+//  E1 (one CTA per zone): Householder tridiagonalisation A = Q_h Tri Q_h^T (Golub & Van Loan,
+//     Matrix Computations 4th ed., 8.3.1) in shared memory, lower triangle only; the
+//     reflector vectors stay below the sub-diagonal of G's slot.
+//  E2 (one thread per zone, 32 zones per warp): eigenvalues of Tri by implicit symmetric QR
+//     sweeps with Wilkinson shift (GvL 8.3.3-8.3.5), then the eigenvectors of Tri by inverse
+//     iteration with a partial-pivoting LU of Tri - lambda I, re-orthogonalised inside
+//     clusters |lambda_i - lambda_{i-1}| <= 1e-3 ||Tri|| (the convention of LAPACK dstein).
+//  E3 (one CTA per zone): U = Q_h Z (reflectors applied backwards), then ampl, v,
+//     T_sym = U diag(sqrt(lambda)) U^T and T = T_sym Omega, Omega applied in O(N^2) through
+//     its reflector form: with P_x = I - u_x u_x^T / (1 + |x_N|), u_x = x + sign(x_N) e_N
+//     (the reflector whose first N-1 columns are perpSpace(x), matoper.F90:509-535),
+//     Omega = P_v P_w + (1 - s_v s_w) v w^T.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -32,14 +35,18 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr int kNMax = 112;               // largest N (matches max_fp64_ensemble)
 constexpr int kMaxSweepsPerN = 30;
+constexpr double kEps = 1.1102230246251565e-16;
+
+// per-zone auxiliary layout (doubles): d[N] e[N] beta[N] lambda[N] | anorm
+__host__ __device__ inline int aux_stride(int N) { return 4 * N + 2; }
 
 __device__ __forceinline__ double warp_sum(double x) {
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
 }
 
-// Block-wide sum; red must hold kWarps doubles. All threads receive the result.
 __device__ __forceinline__ double block_sum(double x, double* red) {
   x = warp_sum(x);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -52,113 +59,111 @@ __device__ __forceinline__ double block_sum(double x, double* red) {
   return t;
 }
 
-struct EigShared {
-  double red[kWarps];
-  double beta_k;
-  double scal[8];
-  int32_t ctl[4];
-};
+__device__ __forceinline__ void lower_index(int e2, int& a, int& b) {
+  a = (int)((sqrt(8.0 * e2 + 1.0) - 1.0) * 0.5);
+  while ((a + 1) * (a + 2) / 2 <= e2) a++;
+  while (a * (a + 1) / 2 > e2) a--;
+  b = e2 - a * (a + 1) / 2;
+}
 
+// ------------------------------------------------------------------------------------ E1
 __global__ void __launch_bounds__(kThreads)
-    k_zone_eig_fp64(int N, int32_t nzc, double* __restrict__ GT, const double* __restrict__ gv,
-                    const int32_t* __restrict__ nobs, int rotate, double* __restrict__ ampl_out,
-                    int32_t* __restrict__ status, int32_t* __restrict__ work) {
+    k_eig_tridiag(int N, int32_t nzc, double* __restrict__ GT, double* __restrict__ aux,
+                  const int32_t* __restrict__ nobs, int32_t* __restrict__ work) {
   extern __shared__ double dyn[];
   const int ld = N + 1;
-  double* A = dyn;            // [N][ld]  matrix, then T_sym
-  double* Q = A + N * ld;     // [N][ld]  Q_h, then U
-  double* d = Q + N * ld;     // [N] diagonal / eigenvalues
-  double* e = d + N;          // [N] off-diagonal
-  double* beta = e + N;       // [N] Householder scalars
-  double* vec0 = beta + N;    // [N] work vectors
-  double* vec1 = vec0 + N;    // [N]
-  double* vec2 = vec1 + N;    // [N]
-  double* rc = vec2 + N;      // [N] rotation cosines of one sweep
-  double* rs = rc + N;        // [N] rotation sines
-  __shared__ EigShared es;
+  double* A = dyn;          // [N][ld], lower triangle valid
+  double* v = A + N * ld;   // [N]
+  double* w = v + N;        // [N]
+  __shared__ double red[kWarps];
+  __shared__ double s_beta;
+  __shared__ int32_t s_zone;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
   for (;;) {
-    if (tid == 0) es.ctl[0] = atomicAdd(work, 1);
+    if (tid == 0) s_zone = atomicAdd(work, 1);
     __syncthreads();
-    const int32_t zl = es.ctl[0];
+    const int32_t zl = s_zone;
     if (zl >= nzc) break;
     if (nobs[zl] == 0) {
       __syncthreads();
       continue;
     }
     double* Gz = GT + (int64_t)zl * N * N;
-    for (int idx = tid; idx < N * N; idx += kThreads) {
-      int i = idx / N, j = idx - i * N;
-      A[i * ld + j] = Gz[idx];
-    }
-    for (int i = tid; i < N; i += kThreads) vec2[i] = gv[(int64_t)zl * N + i];  // g
-    __syncthreads();
-    // ||A||_max for the deflation threshold
+    double* ax = aux + (int64_t)zl * aux_stride(N);
     double amax = 0.0;
     for (int idx = tid; idx < N * N; idx += kThreads) {
       int i = idx / N, j = idx - i * N;
-      amax = fmax(amax, fabs(A[i * ld + j]));
+      double g = Gz[idx];
+      if (j <= i) A[i * ld + j] = g;
+      amax = fmax(amax, fabs(g));
     }
     for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    if (lane == 0) es.red[warp] = amax;
+    __syncthreads();
+    if (lane == 0) red[warp] = amax;
     __syncthreads();
     if (tid == 0) {
       double t = 0.0;
-      for (int w = 0; w < kWarps; w++) t = fmax(t, es.red[w]);
-      es.scal[7] = t;
+      for (int k = 0; k < kWarps; k++) t = fmax(t, red[k]);
+      ax[4 * N] = t * N;  // ||G|| bound used for deflation / pivot floors
     }
-    __syncthreads();
-    const double anorm = es.scal[7] * N;
-
-    // ---- 1. tridiagonalisation
+    double* d = ax;
+    double* e = ax + N;
+    double* beta = ax + 2 * N;
     for (int k = 0; k < N - 2; k++) {
       const int L = N - k - 1;
-      double* col = A + (k + 1) * ld + k;  // x_i = A[k+1+i][k] = col[i*ld]
+      // column k below the diagonal: x_i = A[k+1+i][k]
       double sig = 0.0;
-      for (int i = 1 + tid; i < L; i += kThreads) sig += col[i * ld] * col[i * ld];
-      sig = block_sum(sig, es.red);
+      for (int i = 1 + tid; i < L; i += kThreads) {
+        double x = A[(k + 1 + i) * ld + k];
+        sig = fma(x, x, sig);
+      }
+      sig = block_sum(sig, red);
       if (tid == 0) {
-        double x0 = col[0];
+        double x0 = A[(k + 1) * ld + k];
+        double bk = 0.0;
         if (sig == 0.0) {
           e[k] = x0;
-          beta[k] = 0.0;
         } else {
           double mu = sqrt(x0 * x0 + sig);
           double v0 = (x0 <= 0.0) ? x0 - mu : x0 + mu;  // v0 = x0 + sign(x0) mu
           e[k] = (x0 <= 0.0) ? mu : -mu;               // alpha = -sign(x0) ||x||
-          beta[k] = 2.0 / (v0 * v0 + sig);
-          col[0] = v0;
+          bk = 2.0 / (v0 * v0 + sig);
+          A[(k + 1) * ld + k] = v0;
         }
         d[k] = A[k * ld + k];
-        es.beta_k = beta[k];
+        beta[k] = bk;
+        s_beta = bk;
       }
       __syncthreads();
-      const double bk = es.beta_k;
+      const double bk = s_beta;
       if (bk == 0.0) continue;
-      // v (length L) is col[i*ld]; copy to vec0 for contiguous access
-      for (int i = tid; i < L; i += kThreads) vec0[i] = col[i * ld];
+      for (int i = tid; i < L; i += kThreads) v[i] = A[(k + 1 + i) * ld + k];
       __syncthreads();
-      // p = beta A22 v   (A22 = A[k+1.., k+1..], full symmetric storage)
+      // p = beta A22 v with A22 symmetric, lower triangle stored
       for (int i = warp; i < L; i += kWarps) {
         const double* row = A + (k + 1 + i) * ld + (k + 1);
         double s = 0.0;
-        for (int j = lane; j < L; j += 32) s = fma(row[j], vec0[j], s);
+        for (int j = lane; j < L; j += 32) {
+          double a = (j <= i) ? row[j] : A[(k + 1 + j) * ld + (k + 1 + i)];
+          s = fma(a, v[j], s);
+        }
         s = warp_sum(s);
-        if (lane == 0) vec1[i] = bk * s;
+        if (lane == 0) w[i] = bk * s;
       }
       __syncthreads();
       double pv = 0.0;
-      for (int i = tid; i < L; i += kThreads) pv = fma(vec1[i], vec0[i], pv);
-      pv = block_sum(pv, es.red);
+      for (int i = tid; i < L; i += kThreads) pv = fma(w[i], v[i], pv);
+      pv = block_sum(pv, red);
       const double Kc = 0.5 * bk * pv;
-      for (int i = tid; i < L; i += kThreads) vec1[i] = vec1[i] - Kc * vec0[i];  // w
+      for (int i = tid; i < L; i += kThreads) w[i] = w[i] - Kc * v[i];
       __syncthreads();
-      // A22 -= v w^T + w v^T
-      for (int idx = tid; idx < L * L; idx += kThreads) {
-        int i = idx / L, j = idx - i * L;
+      // A22 -= v w^T + w v^T on the lower triangle
+      const int E = L * (L + 1) / 2;
+      for (int e2 = tid; e2 < E; e2 += kThreads) {
+        int i, j;
+        lower_index(e2, i, j);
         double* a = A + (k + 1 + i) * ld + (k + 1 + j);
-        *a = *a - vec0[i] * vec1[j] - vec1[i] * vec0[j];
+        *a = fma(-v[i], w[j], fma(-w[i], v[j], *a));
       }
       __syncthreads();
     }
@@ -166,189 +171,316 @@ __global__ void __launch_bounds__(kThreads)
       if (N >= 2) {
         d[N - 2] = A[(N - 2) * ld + (N - 2)];
         e[N - 2] = A[(N - 1) * ld + (N - 2)];
+        beta[N - 2] = 0.0;
       }
       d[N - 1] = A[(N - 1) * ld + (N - 1)];
       e[N - 1] = 0.0;
+      beta[N - 1] = 0.0;
     }
-    // ---- 2. Q_h = H_0 ... H_{N-3} (backward accumulation)
+    // reflector vectors (strictly below the diagonal of each column) back to G's slot
     for (int idx = tid; idx < N * N; idx += kThreads) {
       int i = idx / N, j = idx - i * N;
-      Q[i * ld + j] = (i == j) ? 1.0 : 0.0;
+      if (i > j) Gz[idx] = A[i * ld + j];
     }
     __syncthreads();
-    for (int k = N - 3; k >= 0; k--) {
-      const double bk = beta[k];
-      if (bk == 0.0) continue;
-      const int L = N - k - 1;
-      const double* col = A + (k + 1) * ld + k;
-      // y_j = sum_i v_i Q[k+1+i][k+1+j]
-      for (int j = tid; j < L; j += kThreads) {
-        double s = 0.0;
-        for (int i = 0; i < L; i++) s = fma(col[i * ld], Q[(k + 1 + i) * ld + (k + 1 + j)], s);
-        vec1[j] = bk * s;
-      }
-      __syncthreads();
-      for (int idx = tid; idx < L * L; idx += kThreads) {
-        int i = idx / L, j = idx - i * L;
-        double* q = Q + (k + 1 + i) * ld + (k + 1 + j);
-        *q = fma(-col[i * ld], vec1[j], *q);
-      }
-      __syncthreads();
-    }
-    // ---- 3. implicit QR sweeps on (d, e) with rotations applied to Q's columns
-    const double eps = 1.1102230246251565e-16;
-    int hi = N - 1, sweeps = 0, failed = 0;
+  }
+}
+
+// ------------------------------------------------------------------------------------ E2
+// One thread per zone. Local arrays are per-thread (the hardware interleaves them).
+__global__ void __launch_bounds__(128)
+    k_eig_tridiag_solve(int N, int32_t nzc, double* __restrict__ aux, double* __restrict__ Zg,
+                        const int32_t* __restrict__ nobs, int32_t* __restrict__ status) {
+  const int32_t zl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;
+  double* ax = aux + (int64_t)zl * aux_stride(N);
+  double* Z = Zg + (int64_t)zl * N * N;  // Z[j*N + i] = component i of eigenvector j
+  double d[kNMax], e[kNMax];
+  for (int i = 0; i < N; i++) {
+    d[i] = ax[i];
+    e[i] = ax[N + i];
+  }
+  e[N - 1] = 0.0;
+  const double anorm = ax[4 * N];
+  int st = 0;
+  // ---- eigenvalues: implicit QR sweeps with Wilkinson shift, no vectors
+  {
+    int hi = N - 1, sweeps = 0;
     const int max_sweeps = kMaxSweepsPerN * N;
+    const double abs_tol = kEps * anorm * 1e-3;
     while (hi > 0) {
-      // deflation scan (warp 0 decides, everyone follows)
-      if (tid == 0) {
-        int h = hi;
-        while (h > 0) {
-          double t = fabs(e[h - 1]);
-          if (t <= eps * (fabs(d[h - 1]) + fabs(d[h])) || t <= eps * anorm * 1e-3) {
-            e[h - 1] = 0.0;
-            h--;
-          } else {
-            break;
-          }
+      while (hi > 0) {
+        double t = fabs(e[hi - 1]);
+        if (t <= kEps * (fabs(d[hi - 1]) + fabs(d[hi])) || t <= abs_tol) {
+          e[hi - 1] = 0.0;
+          hi--;
+        } else {
+          break;
         }
-        int lo = h;
-        if (h > 0) {
-          lo = h - 1;
-          while (lo > 0) {
-            double t = fabs(e[lo - 1]);
-            if (t <= eps * (fabs(d[lo - 1]) + fabs(d[lo])) || t <= eps * anorm * 1e-3) {
-              e[lo - 1] = 0.0;
-              break;
-            }
-            lo--;
-          }
-        }
-        es.ctl[1] = h;
-        es.ctl[2] = lo;
       }
-      __syncthreads();
-      hi = es.ctl[1];
-      const int lo = es.ctl[2];
-      if (hi <= 0) break;
+      if (hi == 0) break;
+      int lo = hi - 1;
+      while (lo > 0) {
+        double t = fabs(e[lo - 1]);
+        if (t <= kEps * (fabs(d[lo - 1]) + fabs(d[lo])) || t <= abs_tol) {
+          e[lo - 1] = 0.0;
+          break;
+        }
+        lo--;
+      }
       if (++sweeps > max_sweeps) {
-        failed = 1;
+        st |= ZST_EIG;
         break;
       }
-      // one implicit QR step on [lo, hi], computed by warp 0 (all lanes redundantly)
-      if (warp == 0) {
-        double a = d[hi - 1], b = d[hi], f = e[hi - 1];
-        double del = 0.5 * (a - b);
-        double den = del + copysign(sqrt(del * del + f * f), del == 0.0 ? 1.0 : del);
-        double mu = (den == 0.0) ? b : b - f * f / den;
-        double x = d[lo] - mu, z = e[lo], bulge = 0.0;
-        for (int k = lo; k < hi; k++) {
-          // every lane reads its operands before lane 0 writes this step's results
-          if (k > lo) {
-            x = e[k - 1];
-            z = bulge;
-          }
-          const double dk = d[k], dk1 = d[k + 1], ek = e[k];
-          const double ek1 = (k + 1 < hi) ? e[k + 1] : 0.0;
-          __syncwarp();
-          double r = hypot(x, z);
-          double c = 1.0, s = 0.0;
-          if (r != 0.0) {
-            c = x / r;
-            s = z / r;
-          }
-          double cc = c * c, ss = s * s, cs = c * s;
-          double nd0 = cc * dk + 2.0 * cs * ek + ss * dk1;
-          double nd1 = ss * dk - 2.0 * cs * ek + cc * dk1;
-          double ne = cs * (dk1 - dk) + (cc - ss) * ek;
-          if (lane == 0) {
-            if (k > lo) e[k - 1] = r;
-            d[k] = nd0;
-            d[k + 1] = nd1;
-            e[k] = ne;
-            if (k + 1 < hi) e[k + 1] = c * ek1;
-            rc[k] = c;
-            rs[k] = s;
-          }
-          bulge = s * ek1;
-          __syncwarp();
+      const double a = d[hi - 1], b = d[hi], f = e[hi - 1];
+      const double del = 0.5 * (a - b);
+      const double den = del + copysign(sqrt(del * del + f * f), del == 0.0 ? 1.0 : del);
+      const double mu = (den == 0.0) ? b : b - f * f / den;
+      double x = d[lo] - mu, z = e[lo], bulge = 0.0;
+      for (int k = lo; k < hi; k++) {
+        if (k > lo) {
+          x = e[k - 1];
+          z = bulge;
         }
-      }
-      __syncthreads();
-      // Q <- Q P_k^T for k = lo..hi-1: new col_k = c col_k + s col_{k+1},
-      // new col_{k+1} = -s col_k + c col_{k+1}
-      for (int row = tid; row < N; row += kThreads) {
-        double* qr = Q + row * ld;
-        double qa = qr[lo];
-        for (int k = lo; k < hi; k++) {
-          const double c = rc[k], s = rs[k];
-          const double qb = qr[k + 1];
-          qr[k] = c * qa + s * qb;
-          qa = -s * qa + c * qb;
+        const double r2 = x * x + z * z;
+        double c = 1.0, s = 0.0, r = 0.0;
+        if (r2 > 0.0) {
+          const double ri = rsqrt(r2);
+          c = x * ri;
+          s = z * ri;
+          r = r2 * ri;
         }
-        qr[hi] = qa;
+        if (k > lo) e[k - 1] = r;
+        const double dk = d[k], dk1 = d[k + 1], ek = e[k];
+        const double ek1 = (k + 1 < hi) ? e[k + 1] : 0.0;
+        const double cc = c * c, ss = s * s, cs = c * s;
+        d[k] = cc * dk + 2.0 * cs * ek + ss * dk1;
+        d[k + 1] = ss * dk - 2.0 * cs * ek + cc * dk1;
+        e[k] = cs * (dk1 - dk) + (cc - ss) * ek;
+        if (k + 1 < hi) e[k + 1] = c * ek1;
+        bulge = s * ek1;
       }
-      __syncthreads();
     }
-    // ---- 4. amplitudes, rotation vector, transform
-    // d = eigenvalues; lambda <- 1/(1+max(d,0)), vec0 = lambda, vec1 = sqrt(lambda)
+  }
+  // ascending order (insertion sort)
+  for (int i = 1; i < N; i++) {
+    double t = d[i];
+    int k = i - 1;
+    while (k >= 0 && d[k] > t) {
+      d[k + 1] = d[k];
+      k--;
+    }
+    d[k + 1] = t;
+  }
+  for (int i = 0; i < N; i++) ax[3 * N + i] = d[i];
+  // ---- eigenvectors of Tri by inverse iteration (Tri reloaded into td/te)
+  double td[kNMax], te[kNMax];
+  for (int i = 0; i < N; i++) {
+    td[i] = ax[i];
+    te[i] = ax[N + i];
+  }
+  const double tnorm = fmax(anorm, 1e-300);
+  const double tiny = fmax(kEps * tnorm, 1e-300);
+  const double ortol = 1e-3 * tnorm;
+  double u1[kNMax], u2[kNMax], lm[kNMax], uinv[kNMax], x[kNMax];
+  unsigned char piv[kNMax];
+  int cstart = 0;
+  double lprev = 0.0;
+  for (int j = 0; j < N; j++) {
+    double l = d[j];
+    if (j > 0) {
+      if (d[j] - d[j - 1] > ortol) cstart = j;
+      const double pert = 10.0 * kEps * fabs(l);
+      if (l - lprev < pert) l = lprev + pert;  // separate equal eigenvalues
+    }
+    lprev = l;
+    // LU with partial pivoting of Tri - l I: U has a diagonal and two super-diagonals
+    double cd = td[0] - l, csup = (N > 1) ? te[0] : 0.0;
+    for (int i = 0; i < N - 1; i++) {
+      const double sub = te[i], dg = td[i + 1] - l, sp = (i + 1 < N - 1) ? te[i + 1] : 0.0;
+      double u0, li;
+      if (fabs(cd) >= fabs(sub)) {
+        u0 = cd;
+        if (fabs(u0) < tiny) u0 = copysign(tiny, u0);
+        li = sub / u0;
+        u1[i] = csup;
+        u2[i] = 0.0;
+        piv[i] = 0;
+        cd = dg - li * csup;
+        csup = sp;
+      } else {
+        u0 = sub;
+        li = cd / sub;
+        u1[i] = dg;
+        u2[i] = sp;
+        piv[i] = 1;
+        cd = csup - li * dg;
+        csup = -li * sp;
+      }
+      lm[i] = li;
+      uinv[i] = 1.0 / u0;
+    }
+    {
+      double u0 = cd;
+      if (fabs(u0) < tiny) u0 = copysign(tiny, u0);
+      uinv[N - 1] = 1.0 / u0;
+    }
+    // deterministic pseudo-random start vector
+    for (int i = 0; i < N; i++) {
+      unsigned h = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
+      h ^= h >> 15;
+      h *= 2246822519u;
+      h ^= h >> 13;
+      x[i] = (double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5;
+    }
+    for (int it = 0; it < 2; it++) {
+      // forward: apply the row interchanges and L
+      for (int i = 0; i < N - 1; i++) {
+        if (piv[i]) {
+          double t = x[i];
+          x[i] = x[i + 1];
+          x[i + 1] = t;
+        }
+        x[i + 1] -= lm[i] * x[i];
+      }
+      // back substitution with U
+      x[N - 1] *= uinv[N - 1];
+      if (N > 1) x[N - 2] = (x[N - 2] - u1[N - 2] * x[N - 1]) * uinv[N - 2];
+      for (int i = N - 3; i >= 0; i--)
+        x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * uinv[i];
+      // normalise, re-orthogonalise against the cluster, normalise
+      double nrm = 0.0;
+      for (int i = 0; i < N; i++) nrm = fma(x[i], x[i], nrm);
+      double sc = rsqrt(nrm);
+      for (int i = 0; i < N; i++) x[i] *= sc;
+      for (int k = cstart; k < j; k++) {
+        const double* zk = Z + (int64_t)k * N;
+        double dot = 0.0;
+        for (int i = 0; i < N; i++) dot = fma(zk[i], x[i], dot);
+        for (int i = 0; i < N; i++) x[i] = fma(-dot, zk[i], x[i]);
+      }
+      nrm = 0.0;
+      for (int i = 0; i < N; i++) nrm = fma(x[i], x[i], nrm);
+      sc = 1.0 / sqrt(nrm);
+      for (int i = 0; i < N; i++) x[i] *= sc;
+    }
+    double* zj = Z + (int64_t)j * N;
+    for (int i = 0; i < N; i++) zj[i] = x[i];
+  }
+  if (st) status[zl] |= st;
+}
+
+// ------------------------------------------------------------------------------------ E3
+__global__ void __launch_bounds__(kThreads)
+    k_eig_transform(int N, int32_t nzc, double* __restrict__ GT, const double* __restrict__ aux,
+                    const double* __restrict__ Zg, const double* __restrict__ gv,
+                    const int32_t* __restrict__ nobs, int rotate, double* __restrict__ ampl_out,
+                    int32_t* __restrict__ status, int32_t* __restrict__ work) {
+  extern __shared__ double dyn[];
+  const int ld = N + 1;
+  double* A = dyn;           // [N][ld] reflectors, then T_sym
+  double* U = A + N * ld;    // [N][ld] Z, then U
+  double* lam = U + N * ld;  // [N] 1/(1+lambda)
+  double* sq = lam + N;      // [N] sqrt(1/(1+lambda))
+  double* g = sq + N;        // [N]
+  double* beta = g + N;      // [N]
+  double* t0 = beta + N;     // [N]
+  double* t1 = t0 + N;       // [N]
+  double* vv = t1 + N;       // [N]
+  __shared__ double red[kWarps];
+  __shared__ int32_t s_zone;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_zone = atomicAdd(work, 1);
+    __syncthreads();
+    const int32_t zl = s_zone;
+    if (zl >= nzc) break;
+    if (nobs[zl] == 0) {
+      __syncthreads();
+      continue;
+    }
+    double* Gz = GT + (int64_t)zl * N * N;
+    const double* ax = aux + (int64_t)zl * aux_stride(N);
+    const double* Z = Zg + (int64_t)zl * N * N;
+    for (int idx = tid; idx < N * N; idx += kThreads) {
+      int i = idx / N, j = idx - i * N;
+      A[i * ld + j] = (i > j) ? Gz[idx] : 0.0;
+      U[j * ld + i] = Z[idx];  // Z[i*N + j] = component j of eigenvector i -> U[j][i]
+    }
     for (int i = tid; i < N; i += kThreads) {
-      double l = d[i];
+      double l = ax[3 * N + i];
       if (l < 0.0) l = 0.0;
-      double lam = 1.0 / (1.0 + l);
-      vec0[i] = lam;
-      vec1[i] = sqrt(lam);
+      const double li = 1.0 / (1.0 + l);
+      lam[i] = li;
+      sq[i] = sqrt(li);
+      g[i] = gv[(int64_t)zl * N + i];
+      beta[i] = ax[2 * N + i];
     }
     __syncthreads();
-    // y = lambda .* (U^T g) -> beta[] (free now)
+    // U = Q_h Z = H_0 H_1 ... H_{N-3} Z: apply H_k for k = N-3 .. 0
+    for (int k = N - 3; k >= 0; k--) {
+      const double bk = beta[k];
+      if (bk == 0.0) continue;  // uniform across the block
+      const int L = N - k - 1;
+      for (int j = tid; j < N; j += kThreads) {
+        double s = 0.0;
+        for (int i = 0; i < L; i++) s = fma(A[(k + 1 + i) * ld + k], U[(k + 1 + i) * ld + j], s);
+        t0[j] = bk * s;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < L * N; idx += kThreads) {
+        int i = idx / N, j = idx - i * N;
+        double* u = U + (k + 1 + i) * ld + j;
+        *u = fma(-A[(k + 1 + i) * ld + k], t0[j], *u);
+      }
+      __syncthreads();
+    }
+    // ampl = U (lambda .* (U^T g))
     for (int i = tid; i < N; i += kThreads) {
       double s = 0.0;
-      for (int j = 0; j < N; j++) s = fma(Q[j * ld + i], vec2[j], s);
-      beta[i] = vec0[i] * s;
+      for (int r = 0; r < N; r++) s = fma(U[r * ld + i], g[r], s);
+      t0[i] = lam[i] * s;
     }
     __syncthreads();
     int nan_flag = 0;
-    for (int j = tid; j < N; j += kThreads) {
+    for (int r = tid; r < N; r += kThreads) {
       double s = 0.0;
-      for (int i = 0; i < N; i++) s = fma(Q[j * ld + i], beta[i], s);
-      ampl_out[(int64_t)zl * N + j] = s;
+      for (int i = 0; i < N; i++) s = fma(U[r * ld + i], t0[i], s);
+      ampl_out[(int64_t)zl * N + r] = s;
       if (!(s == s) || isinf(s)) nan_flag = 1;
     }
     nan_flag = __syncthreads_or(nan_flag);
     if (rotate) {
-      // t_i = colsum(U)_i / sqrt(lambda_i) -> rc[]
+      // v = normate(U (colsum(U) / sqrt(lambda)))
       for (int i = tid; i < N; i += kThreads) {
         double s = 0.0;
-        for (int j = 0; j < N; j++) s += Q[j * ld + i];
-        rc[i] = s / vec1[i];
+        for (int r = 0; r < N; r++) s += U[r * ld + i];
+        t1[i] = s / sq[i];
       }
       __syncthreads();
       double nrm = 0.0;
-      for (int j = tid; j < N; j += kThreads) {
+      for (int r = tid; r < N; r += kThreads) {
         double s = 0.0;
-        for (int i = 0; i < N; i++) s = fma(Q[j * ld + i], rc[i], s);
-        rs[j] = s;  // v (unnormalised)
+        for (int i = 0; i < N; i++) s = fma(U[r * ld + i], t1[i], s);
+        vv[r] = s;
         nrm = fma(s, s, nrm);
       }
-      nrm = block_sum(nrm, es.red);
+      nrm = block_sum(nrm, red);
       const double inv = 1.0 / sqrt(nrm);
-      for (int j = tid; j < N; j += kThreads) rs[j] = rs[j] * inv;  // v = normate(v)
-      __syncthreads();
+      for (int r = tid; r < N; r += kThreads) vv[r] *= inv;
     }
-    // T_sym = U diag(sqrt(lambda)) U^T: scale U's columns by lambda^(1/4), then U U^T
+    // T_sym = U diag(sqrt(lambda)) U^T: U's columns scaled by lambda^(1/4), then U U^T
     for (int idx = tid; idx < N * N; idx += kThreads) {
-      int i = idx / N, k = idx - i * N;
-      Q[i * ld + k] *= sqrt(vec1[k]);
+      int r = idx / N, i = idx - r * N;
+      U[r * ld + i] *= sqrt(sq[i]);
     }
     __syncthreads();
     const int E = N * (N + 1) / 2;
     for (int e2 = tid; e2 < E; e2 += kThreads) {
-      int a = (int)((sqrt(8.0 * e2 + 1.0) - 1.0) * 0.5);
-      while ((a + 1) * (a + 2) / 2 <= e2) a++;
-      while (a * (a + 1) / 2 > e2) a--;
-      int b = e2 - a * (a + 1) / 2;
-      const double* qa = Q + a * ld;
-      const double* qb = Q + b * ld;
+      int a, b;
+      lower_index(e2, a, b);
+      const double* qa = U + a * ld;
+      const double* qb = U + b * ld;
       double s = 0.0;
       for (int k = 0; k < N; k++) s = fma(qa[k], qb[k], s);
       A[a * ld + b] = s;
@@ -356,47 +488,45 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     if (rotate) {
-      // v in rs[], w = 1/sqrt(N). u_v = v + s_v e_N, c_v = 1 + |v_N|; same for w.
-      const double vN = rs[N - 1];
+      const double vN = vv[N - 1];
       const double sv = signbit(vN) ? -1.0 : 1.0;
       const double cv = 1.0 + fabs(vN);
       const double wv = 1.0 / sqrt((double)N);
       const double cw = 1.0 + wv;
-      // a = T_sym u_v -> vec0 ; tv = T_sym v -> vec2 (g is no longer needed)
+      // t0 = T_sym u_v, t1 = T_sym v
       for (int i = tid; i < N; i += kThreads) {
         const double* ti = A + i * ld;
         double sa = 0.0, sb = 0.0;
         for (int j = 0; j < N; j++) {
-          double uj = rs[j] + ((j == N - 1) ? sv : 0.0);
-          sa = fma(ti[j], uj, sa);
-          sb = fma(ti[j], rs[j], sb);
+          sa = fma(ti[j], vv[j] + ((j == N - 1) ? sv : 0.0), sa);
+          sb = fma(ti[j], vv[j], sb);
         }
-        vec0[i] = sa;
-        vec2[i] = sb;
+        t0[i] = sa;
+        t1[i] = sb;
       }
       __syncthreads();
-      // T1 = T_sym - a u_v^T / c_v
+      // T1 = T_sym - t0 u_v^T / c_v
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
-        double uj = rs[j] + ((j == N - 1) ? sv : 0.0);
-        A[i * ld + j] -= vec0[i] * uj / cv;
+        double uj = vv[j] + ((j == N - 1) ? sv : 0.0);
+        A[i * ld + j] -= t0[i] * uj / cv;
       }
       __syncthreads();
-      // b = T1 u_w -> vec1
+      // g <- T1 u_w (g is no longer needed)
       for (int i = tid; i < N; i += kThreads) {
         const double* ti = A + i * ld;
         double s = 0.0;
         for (int j = 0; j < N; j++) s = fma(ti[j], wv + ((j == N - 1) ? 1.0 : 0.0), s);
-        vec1[i] = s;
+        g[i] = s;
       }
       __syncthreads();
-      // T = T1 - b u_w^T / c_w + (1 - s_v s_w) (T_sym v) w^T   (s_w = +1)
+      // T = T1 - (T1 u_w) u_w^T / c_w + (1 - s_v s_w) (T_sym v) w^T   (s_w = +1)
       const double extra = 1.0 - sv;
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
         double uj = wv + ((j == N - 1) ? 1.0 : 0.0);
-        double t = A[i * ld + j] - vec1[i] * uj / cw;
-        if (extra != 0.0) t = fma(extra * vec2[i], wv, t);
+        double t = A[i * ld + j] - g[i] * uj / cw;
+        if (extra != 0.0) t = fma(extra * t1[i], wv, t);
         Gz[idx] = t;
       }
     } else {
@@ -405,36 +535,51 @@ __global__ void __launch_bounds__(kThreads)
         Gz[idx] = A[i * ld + j];
       }
     }
-    if (tid == 0) status[zl] = (failed ? ZST_EIG : 0) | (nan_flag ? ZST_NAN : 0);
+    if (tid == 0 && nan_flag) status[zl] |= ZST_NAN;
     __syncthreads();
   }
 }
 
-}  // namespace
-
-size_t zone_eig_fp64_smem(int N) { return (size_t)(2 * N * (N + 1) + 8 * N) * sizeof(double); }
-
-cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
-                          const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
-                          int32_t* d_work, cudaStream_t st) {
-  size_t smem = zone_eig_fp64_smem(N);
-  cudaError_t e = cudaFuncSetAttribute(k_zone_eig_fp64,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+int grid_for_smem(const void* fn, size_t smem, int32_t nzc) {
   int bps = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_eig_fp64, kThreads, smem);
-  if (e != cudaSuccess) return e;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, kThreads, smem);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int grid = sms * (bps > 0 ? bps : 1);
   if (grid > nzc) grid = nzc > 0 ? nzc : 1;
-  e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
+  return grid;
+}
+
+}  // namespace
+
+size_t zone_eig_fp64_aux(int N) { return (size_t)aux_stride(N); }
+
+cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
+                          const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
+                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st) {
+  if (N < 2 || N > kNMax) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int32_t) * (nzc > 0 ? nzc : 1), st);
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(d_status, 0, sizeof(int32_t) * (nzc > 0 ? nzc : 1), st);
+  e = cudaMemsetAsync(d_work, 0, 2 * sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
-  k_zone_eig_fp64<<<grid, kThreads, smem, st>>>(N, nzc, d_GT, d_g, d_nobs, rotate, d_ampl,
-                                                 d_status, d_work);
+  // E1
+  size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(double);
+  e = cudaFuncSetAttribute(k_eig_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  if (e != cudaSuccess) return e;
+  k_eig_tridiag<<<grid_for_smem((const void*)k_eig_tridiag, smem1, nzc), kThreads, smem1, st>>>(
+      N, nzc, d_GT, d_aux, d_nobs, d_work);
+  // E2
+  k_eig_tridiag_solve<<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_Z, d_nobs, d_status);
+  // E3
+  size_t smem3 = (size_t)(2 * N * (N + 1) + 7 * N) * sizeof(double);
+  e = cudaFuncSetAttribute(k_eig_transform, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem3);
+  if (e != cudaSuccess) return e;
+  k_eig_transform<<<grid_for_smem((const void*)k_eig_transform, smem3, nzc), kThreads, smem3,
+                    st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
+                          d_work + 1);
+  count_launches(3);
   return cudaGetLastError();
 }
 

@@ -31,12 +31,25 @@ constexpr int kFlushAt = 256;
 constexpr double kPi = 3.141592653589793238462643383279502884197;
 constexpr double kEarthRadius = 6378137.0;
 
-// Gaspari-Cohn (covariance.F90:645-667), evaluated in the reference's Horner order.
+// Gaspari-Cohn (covariance.F90:645-667), evaluated in the reference's Horner order with every
+// product and sum rounded separately (no FMA contraction). Near r = 2 the value is a
+// cancellation of order (2-r)^3, so the `w /= 0` relevance test is only reproducible when the
+// operations round exactly as a plain IEEE evaluation does.
 __device__ __forceinline__ double locfun(double r) {
-  if (r <= 1.0) return (((-r / 4.0 + 1.0 / 2.0) * r + 5.0 / 8.0) * r - 5.0 / 3.0) * (r * r) + 1.0;
-  if (r <= 2.0)
-    return ((((r / 12.0 - 1.0 / 2.0) * r + 5.0 / 8.0) * r + 5.0 / 3.0) * r - 5.0) * r + 4.0 -
-           2.0 / (3.0 * r);
+  if (r <= 1.0) {
+    double t = __dadd_rn(__ddiv_rn(-r, 4.0), 0.5);
+    t = __dadd_rn(__dmul_rn(t, r), 5.0 / 8.0);
+    t = __dsub_rn(__dmul_rn(t, r), 5.0 / 3.0);
+    return __dadd_rn(__dmul_rn(t, __dmul_rn(r, r)), 1.0);
+  }
+  if (r <= 2.0) {
+    double t = __dsub_rn(__ddiv_rn(r, 12.0), 0.5);
+    t = __dadd_rn(__dmul_rn(t, r), 5.0 / 8.0);
+    t = __dadd_rn(__dmul_rn(t, r), 5.0 / 3.0);
+    t = __dsub_rn(__dmul_rn(t, r), 5.0);
+    t = __dadd_rn(__dmul_rn(t, r), 4.0);
+    return __dsub_rn(t, __ddiv_rn(2.0, __dmul_rn(3.0, r)));
+  }
   return 0.0;
 }
 
@@ -108,6 +121,10 @@ __device__ ScanRange zone_scan_range(const CellGrid& g, int metric, int loctype,
   double zuu = zu;
   if (g.periodic_u) zuu = zu - 360.0 * floor(zu / 360.0);
   double fu0 = floor((zuu - du - g.u0) / g.csu), fu1 = floor((zuu + du - g.u0) / g.csu);
+  if (g.periodic_u) {  // one extra cell each side absorbs rounding of the wrap-around
+    fu0 -= 1.0;
+    fu1 += 1.0;
+  }
   double fv0 = floor((zv - dv - g.v0) / g.csv), fv1 = floor((zv + dv - g.v0) / g.csv);
   fv0 = fmax(fv0, 0.0);
   fv1 = fmin(fv1, (double)(g.nv - 1));
@@ -464,6 +481,7 @@ cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams
   k_zone_gram_fp64<MAXE><<<grid, kThreads, smem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt,
                                                         corr_len, max_len, d_G, d_g, d_nobs,
                                                         brute, CH, d_work);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -484,6 +502,7 @@ cudaError_t launch_global(int64_t m, int N, const double* HSf, int64_t ldH, cons
   if (e != cudaSuccess) return e;
   k_global_gram_fp64<MAXE><<<grid, kThreads, smem, st>>>(m, N, HSf, ldH, yo, Hxf, r, d_G, d_g,
                                                           CH);
+  count_launches(1);
   return cudaGetLastError();
 }
 

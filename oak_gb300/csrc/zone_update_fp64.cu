@@ -105,6 +105,7 @@ cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zo
   int grid = (int)(ntasks < 152 * 16 ? (ntasks < 1 ? 1 : ntasks) : 152 * 16);
   k_zone_update_fp64<<<grid, kThreads, smem, st>>>(N, z0, nzc, d_zone_start, tiles, xf, Sf, ldS,
                                                     d_T, d_ampl, d_nobs, xa, Sa);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -115,6 +116,7 @@ cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_amp
   int grid = (int)((total + 255) / 256 < 152 * 8 ? (total + 255) / 256 : 152 * 8);
   if (grid < 1) grid = 1;
   k_write_amplitudes<<<grid, 256, 0, st>>>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
