@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kThreads)
   for (int s = 0; s < MAXE; s++) {
     int e = threadIdx.x + s * kThreads;
     if (e < E) {
-      int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+      int a = (int)((__fsqrt_rn((float)(8 * e + 1)) - 1.0f) * 0.5f);
       while ((a + 1) * (a + 2) / 2 <= e) a++;
       while (a * (a + 1) / 2 > e) a--;
       ea[s] = a;
@@ -400,7 +400,7 @@ __global__ void __launch_bounds__(kThreads)
     int e = threadIdx.x + s * kThreads;
     acc[s] = 0.0;
     if (e < E) {
-      int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+      int a = (int)((__fsqrt_rn((float)(8 * e + 1)) - 1.0f) * 0.5f);
       while ((a + 1) * (a + 2) / 2 <= e) a++;
       while (a * (a + 1) / 2 > e) a--;
       ea[s] = a;

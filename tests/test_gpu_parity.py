@@ -257,3 +257,19 @@ def test_local_config_scaled_matches_oracle(oakg):
                                              c.max_len, kind=c.weight)
     assert np.array_equal(nobs, nobs_o)
     check_local(xa, Sa, xa_o, Sa_o, c.xf)
+
+
+def test_zero_weight_zone_keeps_forecast(oakg):
+    """Gaussian weights that underflow to 0 (d >> L but d <= maxLength) give G = 0: the
+    reference then returns xa = xf, Sa = Sf for the zone (lambda = 0, T = I, Omega = I)."""
+    P = _random_local(15, nzones=12, m=40)
+    corr = np.full(12, 1e-3)       # exp(-(d/L)^2) underflows for every d > ~0.03
+    maxl = np.full(12, 1e9)        # every observation relevant
+    xa, Sa, _, nobs = oakg.loc_analysis(P["zs"], P["xf"], P["Hxf"], P["yo"], P["Sf"],
+                                        P["HSf"], P["r"], P["zone_pos"], P["obs_pos"], corr,
+                                        maxl, weight=oakg.GAUSS_CUTOFF)
+    assert np.all(nobs == 40)
+    xa_o, Sa_o, _, _ = cref.locanalysis(P["zs"], P["xf"], P["Hxf"], P["yo"], P["Sf"], P["HSf"],
+                                        P["r"], P["zone_pos"], P["obs_pos"], corr, maxl, kind=0)
+    assert np.allclose(xa, P["xf"], atol=1e-14) and np.allclose(Sa, P["Sf"], atol=1e-14)
+    assert np.allclose(xa_o, P["xf"], atol=1e-14) and np.allclose(Sa_o, P["Sf"], atol=1e-14)
