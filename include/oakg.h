@@ -125,6 +125,23 @@ int oakg_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
                      const double* corr_len, const double* max_len, double* xa, double* Sa,
                      double* ampl, int32_t* nobs);
 
+/* oakg_analysis for callers that cannot allocate device memory -- no counterpart in the
+ * reference. Host programs that reserve all GPU memory for their own pool before loading this
+ * library (model couplers often do), or that must not call cudaMalloc/cudaFree inside a
+ * forecast-analysis cycle because those calls can synchronise the device, use this entry:
+ * it calls no allocating routine. All temporaries live in one static device array of 256 KiB
+ * that every GPU loading the library holds until the process exits.
+ *   - Same arguments and results as oakg_analysis, plus the CUDA stream (cudaStream_t, NULL
+ *     for the legacy default stream) the work is queued on; returns after it completed.
+ *   - dims->mem must be OAKG_MEM_DEVICE; N (dims->N) must be <= 112, else OAKG_ERR_ARGS.
+ *   - Calls share the array: calls that overlap on the GPU race, so serialise them.
+ *   - The first call on a device also looks up the array's device address; make that first
+ *     call before any stream capture. */
+int oakg_analysis_noalloc(const oakg_dims* dims, const double* xf, const double* Hxf,
+                          const double* yo, const double* Sf, const double* HSf,
+                          const double* r_diag, double* xa, double* Sa, double* ampl,
+                          void* stream);
+
 /* Message of the last failed call on this thread (empty if none); returns its length. */
 size_t oakg_last_error(char* buf, size_t len);
 
