@@ -48,6 +48,7 @@ def parse():
                    help="target CPU time of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mixed", action="store_true")
     return p.parse_args()
 
 
@@ -248,6 +249,42 @@ def main():
         ms = float(t.item())
     value = ws * c.Z / (ms / 1e3)
 
+    # mixed-precision form on the same device inputs; errors against the FP64 form's outputs
+    mixed = None
+    if not args.no_mixed:
+        ref_xa, ref_Sa = out[0].clone(), out[1].clone()
+
+        def mstep():
+            return oak_gb300.loc_analysis(*d_args, weight=c.weight, metric=c.metric,
+                                          loctype=c.loctype, want_ampl=False,
+                                          precision=oak_gb300.PREC_MIXED)
+        for _ in range(args.warmup):
+            mout = mstep()
+        mstage = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
+        barrier()
+        torch.cuda.synchronize(dev)
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for _ in range(args.steps):
+            mout = mstep()
+            for k, v in oak_gb300.last_timings().items():
+                mstage[k] += v
+        m1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        mms = m0.elapsed_time(m1) / args.steps
+        xf_d = d_args[1]
+        e_mean = float(torch.linalg.norm(mout[0] - ref_xa) / torch.linalg.norm(ref_xa - xf_d))
+        e_anom = float(torch.linalg.norm(mout[1] - ref_Sa) / torch.linalg.norm(ref_Sa))
+        mixed = {"value": ws * c.Z / (mms / 1e3), "unit": UNIT, "ms_per_step": mms,
+                 "speedup_vs_fp64": ms / mms, "rel_err_mean_increment": e_mean,
+                 "rel_err_anomalies": e_anom,
+                 "precision": "FP64 selection and (1+lambda)^-1/2 scaling; FP32 Gram, "
+                              "eigensolve and update; compensated FP32 innovation sums",
+                 "stage_ms_per_step": {k: v / args.steps for k, v in mstage.items()}}
+        del ref_xa, ref_Sa, mout
+
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
     if not args.no_e2e:
@@ -305,6 +342,7 @@ def main():
         "config": workload_config(c, args.scale) | {"parallelism": f"zones sharded, {ws} GPU(s)",
                                                      "zones_with_obs": int((nobs > 0).sum())},
         "e2e": e2e,
+        "mixed": mixed,
         "gpu_launches": int(launches),
         "stage_ms_per_step": per_step,
         "roofline": {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,

@@ -25,6 +25,7 @@ import os
 import numpy as np
 
 __all__ = ["analysis", "loc_analysis", "OakError", "lib", "last_timings", "release",
+           "PREC_FP64", "PREC_MIXED",
            "GAUSS_CUTOFF", "GASPARI_COHN", "CARTESIAN", "SPHERICAL", "SPHERICAL_APPROX",
            "zone_positions"]
 
@@ -37,7 +38,7 @@ ERR_ARGS, ERR_CUDA, ERR_NAN, ERR_EIG, ERR_NOMEM, ERR_TIMEOUT, ERR_INIT, ERR_NOTI
 MEM_HOST, MEM_DEVICE = 0, 1
 GAUSS_CUTOFF, GASPARI_COHN = 0, 1
 CARTESIAN, SPHERICAL, SPHERICAL_APPROX = 0, 1, 2
-PREC_FP64 = 0
+PREC_FP64, PREC_MIXED = 0, 1
 FLAG_AMPL_ALWAYS, FLAG_BRUTE_SEARCH = 1, 2
 
 
@@ -233,7 +234,8 @@ def analysis(xf, Hxf, yo, Sf, HSf, r_diag, *, want_sa=True, out=None):
 def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, corr_len,
                  max_len, *, weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1,
                  localise_obs=True, rotate=True, want_sa=True, want_ampl=True,
-                 ampl_always=False, brute_search=False, cell_size=0.0, out=None):
+                 ampl_always=False, brute_search=False, cell_size=0.0, out=None,
+                 precision=PREC_FP64):
     """Local analysis (rrsqrt.F90:433-466) with geometric observation selection.
 
     ``zone_pos``: (Z, 4) x, y, z, t of each zone's first state element
@@ -244,7 +246,8 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     Returns ``(xa, Sa, amplitudes (N, Z), nobs (Z,))``. As in the reference, amplitudes are
     only written for the non-localised branch unless ``ampl_always`` is set. ``out`` may give
     preallocated ``(xa, Sa)`` arrays of the same memory kind as the inputs (e.g. pinned host
-    arrays).
+    arrays). ``precision``: PREC_FP64 (plain form) or PREC_MIXED (FP32 Gram, eigensolve and
+    update; FP64 selection and eigenvalue scalings).
     """
     Z = int(zone_size.shape[0])
     n = int(xf.shape[0])
@@ -259,7 +262,7 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
     flags = (FLAG_AMPL_ALWAYS if ampl_always else 0) | (FLAG_BRUTE_SEARCH if brute_search else 0)
     loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
-              rotate=int(bool(rotate)), precision=PREC_FP64, flags=flags,
+              rotate=int(bool(rotate)), precision=int(precision), flags=flags,
               cell_size=float(cell_size))
     like = Sf
     if device:

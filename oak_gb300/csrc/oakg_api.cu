@@ -197,6 +197,104 @@ size_t chunk_budget_bytes() {
 
 }  // namespace
 
+// Per-precision kernel sets (R = double: plain form; R = float: mixed form).
+template <typename R>
+struct ZoneKernels;
+template <>
+struct ZoneKernels<double> {
+  template <typename... A>
+  static cudaError_t gram(A... a) { return zone_gram_fp64(a...); }
+  template <typename... A>
+  static cudaError_t eig(A... a) { return zone_eig_fp64(a...); }
+  template <typename... A>
+  static cudaError_t update(A... a) { return zone_update_fp64(a...); }
+  template <typename... A>
+  static cudaError_t ampl(A... a) { return write_amplitudes(a...); }
+};
+template <>
+struct ZoneKernels<float> {
+  template <typename... A>
+  static cudaError_t gram(A... a) { return zone_gram_fp32(a...); }
+  template <typename... A>
+  static cudaError_t eig(A... a) { return zone_eig_fp32(a...); }
+  template <typename... A>
+  static cudaError_t update(A... a) { return zone_update_fp32(a...); }
+  template <typename... A>
+  static cudaError_t ampl(A... a) { return write_amplitudes_fp32(a...); }
+};
+
+struct ChunkArgs {
+  CellGrid g;
+  SortedObs so;
+  LocParams lp;
+  int32_t Z;
+  int N;
+  int64_t ldS;
+  int32_t zone_max;
+  int brute, all_ampl;
+  const double *zxyzt, *corr, *maxl;
+  const int64_t* zstart;
+  const double *xf, *Sf;
+  double *xa, *Sa, *ampl;
+  int32_t* nobs;
+};
+
+// Runs the zone stages over chunks of zones sized to the scratch budget.
+template <typename R>
+int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram, double* t_eig,
+               double* t_upd) {
+  using K = ZoneKernels<R>;
+  const int N = a.N;
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  int rc;
+  const size_t per_zone =
+      ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) * sizeof(R) + 2 * sizeof(int32_t);
+  int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
+  if (chunk < 1) chunk = 1;
+  if (chunk > a.Z) chunk = a.Z;
+  R *d_G, *d_gv, *d_za, *d_aux, *d_zvec;
+  int32_t *d_status, *d_work;
+  if ((rc = scratch(c, B_G, (size_t)chunk * N * N, &d_G, "zone matrices"))) return rc;
+  if ((rc = scratch(c, B_GV, (size_t)chunk * N, &d_gv, "zone vectors"))) return rc;
+  if ((rc = scratch(c, B_ZAMPL, (size_t)chunk * N, &d_za, "zone amplitudes"))) return rc;
+  if ((rc = scratch(c, B_STATUS, (size_t)chunk + 1, &d_status, "zone status"))) return rc;
+  if ((rc = scratch(c, B_WORK, 8, &d_work, "work counters"))) return rc;
+  if ((rc = scratch(c, B_AUX, (size_t)chunk * zone_eig_aux(N), &d_aux, "zone aux"))) return rc;
+  if ((rc = scratch(c, B_ZVEC, (size_t)chunk * N * N, &d_zvec, "zone eigenvectors"))) return rc;
+  *status_all = d_work + 2;
+  k_set_int<<<1, 1, 0, st>>>(*status_all, 0);
+  count_launches(1);
+  for (int64_t z0 = 0; z0 < a.Z; z0 += chunk) {
+    const int32_t nzc = (int32_t)std::min<int64_t>(chunk, a.Z - z0);
+    cudaEventRecord(c->ev[2], st);
+    e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv, a.nobs,
+                a.brute, d_work, st);
+    if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
+    cudaEventRecord(c->ev[3], st);
+    e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate, d_za,
+               d_status, d_aux, d_zvec, d_work + 4, st);
+    if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
+    cudaEventRecord(c->ev[4], st);
+    e = K::update(N, (int32_t)z0, nzc, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, (const R*)d_G,
+                  (const R*)d_za, (const int32_t*)(a.nobs + z0), a.xa, a.Sa, st);
+    if (e != cudaSuccess) return cuda_fail(e, "update kernel");
+    cudaEventRecord(c->ev[5], st);
+    if (a.ampl) {
+      e = K::ampl(N, (int32_t)z0, nzc, (const R*)d_za, (const int32_t*)(a.nobs + z0), a.all_ampl,
+                  a.ampl, st);
+      if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
+    }
+    k_or_status<<<64, 256, 0, st>>>(d_status, nzc, *status_all);
+    count_launches(1);
+    if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
+    *t_gram += elapsed(c->ev[2], c->ev[3]);
+    *t_eig += elapsed(c->ev[3], c->ev[4]);
+    *t_upd += elapsed(c->ev[4], c->ev[5]);
+  }
+  return OAKG_OK;
+}
+
 // ------------------------------------------------------------------------------------------
 int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
                      const int32_t* zone_size, const double* xf, const double* Hxf,
@@ -216,8 +314,8 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
                 loc->metric);
   if (loc->loctype < 1 || loc->loctype > 3)
     return fail(OAKG_ERR_ARGS, "loctype must be 1, 2 or 3 (got %d)", loc->loctype);
-  if (loc->precision != OAKG_PREC_FP64)
-    return fail(OAKG_ERR_NOTIMPL, "precision mode %d not available", loc->precision);
+  if (loc->precision != OAKG_PREC_FP64 && loc->precision != OAKG_PREC_MIXED)
+    return fail(OAKG_ERR_ARGS, "unknown precision mode %d", loc->precision);
   const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
   const int N = dims->N, mem = dims->mem;
   if (!zone_size || !xf || !xa || !zone_xyzt || !corr_len || !max_len)
@@ -371,54 +469,18 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   }
   cudaEventRecord(c->ev[1], st);
 
-  // zone chunks
-  const size_t per_zone = (size_t)N * N * 16 + (size_t)N * 16 + zone_eig_fp64_aux(N) * 8 + 8;
-  int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
-  if (chunk < 1) chunk = 1;
-  if (chunk > Z) chunk = Z;
-  double *d_G, *d_gv, *d_za;
-  int32_t *d_status, *d_work;
-  if ((rc = scratch(c, B_G, (size_t)chunk * N * N, &d_G, "zone matrices"))) return rc;
-  if ((rc = scratch(c, B_GV, (size_t)chunk * N, &d_gv, "zone vectors"))) return rc;
-  if ((rc = scratch(c, B_ZAMPL, (size_t)chunk * N, &d_za, "zone amplitudes"))) return rc;
-  if ((rc = scratch(c, B_STATUS, (size_t)chunk + 1, &d_status, "zone status"))) return rc;
-  if ((rc = scratch(c, B_WORK, 8, &d_work, "work counters"))) return rc;
-  double *d_aux, *d_zvec;
-  if ((rc = scratch(c, B_AUX, (size_t)chunk * zone_eig_fp64_aux(N), &d_aux, "zone aux"))) return rc;
-  if ((rc = scratch(c, B_ZVEC, (size_t)chunk * N * N, &d_zvec, "zone eigenvectors"))) return rc;
-  int32_t* d_status_all = d_work + 2;
-  k_set_int<<<1, 1, 0, st>>>(d_status_all, 0);
-  count_launches(1);
+  // zone chunks: selection + Gram, eigensolve + transform, update
   LocParams lp{loc->weight, loc->metric, loc->loctype, loc->localise_obs ? 1 : 0,
                loc->rotate ? 1 : 0, loc->flags};
   const int all_ampl = (!loc->localise_obs) || (loc->flags & OAKG_FLAG_AMPL_ALWAYS);
+  int32_t* d_status_all = nullptr;
+  ChunkArgs ca{g, so, lp, Z, N, ldS, zone_max, brute, all_ampl, d_zxyzt, d_corr, d_maxl,
+               d_zstart, d_xf, d_Sf, d_xa, d_Sa, d_ampl, d_nobs};
   double t_gram = 0, t_eig = 0, t_upd = 0;
-  for (int64_t z0 = 0; z0 < Z; z0 += chunk) {
-    const int32_t nzc = (int32_t)std::min<int64_t>(chunk, Z - z0);
-    cudaEventRecord(c->ev[2], st);
-    e = zone_gram_fp64(g, so, N, lp, (int32_t)z0, nzc, d_zxyzt, d_corr, d_maxl, d_G, d_gv,
-                       d_nobs, brute, d_work, st);
-    if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
-    cudaEventRecord(c->ev[3], st);
-    e = zone_eig_fp64(N, nzc, d_G, d_gv, d_nobs + z0, lp.rotate, d_za, d_status, d_aux, d_zvec,
-                      d_work + 4, st);
-    if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
-    cudaEventRecord(c->ev[4], st);
-    e = zone_update_fp64(N, (int32_t)z0, nzc, d_zstart, zone_max, d_xf, d_Sf, ldS, d_G, d_za,
-                         d_nobs + z0, d_xa, d_Sa, st);
-    if (e != cudaSuccess) return cuda_fail(e, "update kernel");
-    cudaEventRecord(c->ev[5], st);
-    if (d_ampl) {
-      e = write_amplitudes(N, (int32_t)z0, nzc, d_za, d_nobs + z0, all_ampl, d_ampl, st);
-      if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
-    }
-    k_or_status<<<64, 256, 0, st>>>(d_status, nzc, d_status_all);
-    count_launches(1);
-    if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
-    t_gram += elapsed(c->ev[2], c->ev[3]);
-    t_eig += elapsed(c->ev[3], c->ev[4]);
-    t_upd += elapsed(c->ev[4], c->ev[5]);
-  }
+  rc = (loc->precision == OAKG_PREC_MIXED)
+           ? run_chunks<float>(c, ca, &d_status_all, &t_gram, &t_eig, &t_upd)
+           : run_chunks<double>(c, ca, &d_status_all, &t_gram, &t_eig, &t_upd);
+  if (rc) return rc;
   cudaEventRecord(c->ev[6], st);
   int32_t hstatus = 0;
   if ((e = cudaMemcpyAsync(&hstatus, d_status_all, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) !=
@@ -488,7 +550,7 @@ int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
   if ((rc = scratch(c, B_STATUS, 2, &d_status, "status"))) return rc;
   if ((rc = scratch(c, B_WORK, 8, &d_work, "work"))) return rc;
   double *d_aux, *d_zvec;
-  if ((rc = scratch(c, B_AUX, zone_eig_fp64_aux(N), &d_aux, "zone aux"))) return rc;
+  if ((rc = scratch(c, B_AUX, zone_eig_aux(N), &d_aux, "zone aux"))) return rc;
   if ((rc = scratch(c, B_ZVEC, (size_t)N * N, &d_zvec, "zone eigenvectors"))) return rc;
   if ((rc = scratch(c, B_NOBS, 2, &d_nobs, "nobs"))) return rc;
   if ((rc = scratch(c, B_ZSTART, 2, &d_zstart, "zone offsets"))) return rc;

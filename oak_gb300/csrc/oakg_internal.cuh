@@ -53,7 +53,7 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
 cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_start,
                          int32_t* d_zone_max, cudaStream_t st);
 
-// ---- zone_gram_fp64.cu
+// ---- zone_gram.cu
 // Selection + Gram + innovation projection for zones [z0, z0 + nzc); writes G (N x N, both
 // triangles, row-major per zone), gvec (N), nobs per zone.
 cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
@@ -61,23 +61,32 @@ cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocPar
                            const double* corr_len, const double* max_len, double* d_G,
                            double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
                            cudaStream_t st);
+// Mixed precision: same selection, products accumulated in FP32 (G, g in float).
+cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                           int32_t z0, int32_t nzc, const double* zone_xyzt,
+                           const double* corr_len, const double* max_len, float* d_G,
+                           float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                           cudaStream_t st);
 // Global analysis Gram over all m observations (weights 1): G, g accumulated atomically.
 cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,
                              const double* yo, const double* Hxf, const double* r, double* d_G,
                              double* d_g, cudaStream_t st);
 
-// ---- zone_eig_fp64.cu
+// ---- zone_eig.cu
 // For zones [0, nzc) of a chunk with nobs > 0: eigen-decomposition of G (d_GT, N x N per
 // zone), T = U (I+L)^-1/2 U^T Omega written over G, ampl (N per zone), status per zone.
 // d_nobs/d_ampl/d_status are chunk-relative.
-// d_aux holds zone_eig_fp64_aux(N) doubles per zone, d_Z N*N doubles per zone;
+// d_aux holds zone_eig_aux(N) elements per zone, d_Z N*N elements per zone;
 // d_work two counters.
 cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
                           const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
                           double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st);
-size_t zone_eig_fp64_aux(int N);
+cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,
+                          const int32_t* d_nobs, int rotate, float* d_ampl, int32_t* d_status,
+                          float* d_aux, float* d_Z, int32_t* d_work, cudaStream_t st);
+size_t zone_eig_aux(int N);
 
-// ---- zone_update_fp64.cu
+// ---- zone_update.cu
 // xa = xf + Sf ampl, Sa = Sf T per zone; zones with nobs == 0 copy (xa = xf, Sa = Sf).
 cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
                              int32_t zone_max, const double* xf, const double* Sf,
@@ -86,6 +95,13 @@ cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zo
 cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_ampl,
                              const int32_t* d_nobs, int all_zones, double* ampl_out,
                              cudaStream_t st);
+cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const double* xf, const double* Sf,
+                             int64_t ldS, const float* d_T, const float* d_ampl,
+                             const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st);
+cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d_ampl,
+                                  const int32_t* d_nobs, int all_zones, double* ampl_out,
+                                  cudaStream_t st);
 
 int max_fp64_ensemble();  // largest N the FP64 kernels accept
 

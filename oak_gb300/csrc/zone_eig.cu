@@ -1,4 +1,6 @@
-// K3 + K4 (FP64) -- per-zone symmetric eigensolve and the square-root transform.
+// K3 + K4 -- per-zone symmetric eigensolve and the square-root transform, templated on the
+// arithmetic type R: double for the plain form, float for the mixed-precision form (where the
+// (1 + lambda)^-1/2 and (1 + lambda)^-1 scalings are still evaluated in FP64).
 //
 // For each zone with relevant observations (G = HS^T R^-1_eff HS and g = HS^T R^-1_eff d
 // from K2), this computes what rrsqrt.F90:136-185 computes:
@@ -11,7 +13,7 @@
 // T (N x N, row-major, T[k][c]) overwrites G's slot; Sa = Sf T is formed by K5.
 //
 // GB300 executes one FP64 warp instruction per ~16 SM cycles whatever its active-lane mask,
-// so the work is split into kernels whose FP64 instructions keep all 32 lanes busy:
+// so the work is split into kernels whose arithmetic keeps all 32 lanes busy:
 //  E1  (one CTA per zone): Householder tridiagonalisation A = Q_h Tri Q_h^T (Golub & Van
 //      Loan, Matrix Computations 4th ed., 8.3.1) in shared memory on the lower triangle; the
 //      reflector vectors stay below the diagonal of G's slot.
@@ -39,19 +41,40 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNMax = 112;               // largest N (matches max_fp64_ensemble)
 constexpr int kMaxSweepsPerN = 30;
-constexpr double kEps = 1.1102230246251565e-16;
 
-// per-zone auxiliary layout (doubles):
-//   d[N] e[N] beta[N] lambda[N] shift[N] | anorm onenrm
+template <typename R>
+struct Prec;
+template <>
+struct Prec<double> {
+  static __device__ __forceinline__ double eps() { return 1.1102230246251565e-16; }
+  static __device__ __forceinline__ double tiny() { return 1e-300; }
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  static __device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
+};
+template <>
+struct Prec<float> {
+  static __device__ __forceinline__ float eps() { return 5.9604645e-8f; }
+  static __device__ __forceinline__ float tiny() { return 1e-36f; }
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
+};
+
+// per-zone auxiliary layout (elements of R). The eigensolve works on G / scale with
+// scale = max|G_ij| (LAPACK-style scaling: keeps FP32 squares away from underflow):
+//   d[N] e[N] beta[N]      tridiagonal of G/scale and the Householder scalars
+//   lambda[N]              eigenvalues of G (unscaled, ascending)
+//   shift[N]               inverse-iteration shifts (scaled units)
+//   scale ||Tri||_1        (||Tri||_1 in scaled units)
 __host__ __device__ inline int aux_stride(int N) { return 5 * N + 2; }
 
-__device__ __forceinline__ double warp_sum(double x) {
+template <typename R>
+__device__ __forceinline__ R warp_sum(R x) {
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
 }
 
 // (row, col) of the e2-th lower-triangle entry. The estimate uses an FP32 square root (the
-// FP64 pipe is the bottleneck of every kernel here) and integer fix-ups make it exact.
+// FP64 pipe is the bottleneck of the FP64 kernels) and integer fix-ups make it exact.
 __device__ __forceinline__ void lower_index(int e2, int& a, int& b) {
   a = (int)((__fsqrt_rn((float)(8 * e2 + 1)) - 1.0f) * 0.5f);
   while ((a + 1) * (a + 2) / 2 <= e2) a++;
@@ -60,16 +83,18 @@ __device__ __forceinline__ void lower_index(int e2, int& a, int& b) {
 }
 
 // ------------------------------------------------------------------------------------ E1
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-    k_eig_tridiag(int N, int32_t nzc, double* __restrict__ GT, double* __restrict__ aux,
+    k_eig_tridiag(int N, int32_t nzc, R* __restrict__ GT, R* __restrict__ aux,
                   const int32_t* __restrict__ nobs, int32_t* __restrict__ work) {
-  extern __shared__ double dyn[];
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  R* dyn = reinterpret_cast<R*>(dyn_raw);
   const int ld = N + 1;
-  double* A = dyn;          // [N][ld], lower triangle valid
-  double* v = A + N * ld;   // [N]
-  double* w = v + N;        // [N]
-  __shared__ double red[kWarps];
-  __shared__ double s_beta, s_kc;
+  R* A = dyn;          // [N][ld], lower triangle valid
+  R* v = A + N * ld;   // [N]
+  R* w = v + N;        // [N]
+  __shared__ R red[kWarps];
+  __shared__ R s_beta, s_kc;
   __shared__ int32_t s_zone;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (;;) {
@@ -81,46 +106,47 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
       continue;
     }
-    double* Gz = GT + (int64_t)zl * N * N;
-    double* ax = aux + (int64_t)zl * aux_stride(N);
-    double amax = 0.0;
-    for (int idx = tid; idx < N * N; idx += kThreads) {
-      int i = idx / N, j = idx - i * N;
-      double g = Gz[idx];
-      if (j <= i) A[i * ld + j] = g;
-      amax = fmax(amax, fabs(g));
-    }
+    R* Gz = GT + (int64_t)zl * N * N;
+    R* ax = aux + (int64_t)zl * aux_stride(N);
+    R amax = 0;
+    for (int idx = tid; idx < N * N; idx += kThreads) amax = fmax(amax, fabs(Gz[idx]));
     for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     if (lane == 0) red[warp] = amax;
     __syncthreads();
-    if (tid == 0) {
-      double t = 0.0;
-      for (int k = 0; k < kWarps; k++) t = fmax(t, red[k]);
-      ax[5 * N] = t * N;  // bound on ||G||, deflation floor
+    R scale = 0;
+    for (int k = 0; k < kWarps; k++) scale = fmax(scale, red[k]);
+    if (!(scale > R(0)) || isinf(scale)) scale = R(1);
+    const R iscale = R(1) / scale;
+    for (int idx = tid; idx < N * N; idx += kThreads) {
+      int i = idx / N, j = idx - i * N;
+      if (j <= i) A[i * ld + j] = Gz[idx] * iscale;
     }
-    double* d = ax;
-    double* e = ax + N;
-    double* beta = ax + 2 * N;
+    if (tid == 0) ax[5 * N] = scale;
+    __syncthreads();
+    R* d = ax;
+    R* e = ax + N;
+    R* beta = ax + 2 * N;
     for (int k = 0; k < N - 2; k++) {
       const int L = N - k - 1;
       if (warp == 0) {
         // column k below the diagonal: x_i = A[k+1+i][k]
-        double sig = 0.0;
+        R sig = 0;
         for (int i = 1 + lane; i < L; i += 32) {
-          double x = A[(k + 1 + i) * ld + k];
+          R x = A[(k + 1 + i) * ld + k];
           sig = fma(x, x, sig);
         }
         sig = warp_sum(sig);
         if (lane == 0) {
-          double x0 = A[(k + 1) * ld + k];
-          double bk = 0.0;
-          if (sig == 0.0) {
+          R x0 = A[(k + 1) * ld + k];
+          R bk = 0;
+          const R mu = Prec<R>::sqrt_(x0 * x0 + sig);
+          const R v0 = (x0 <= R(0)) ? x0 - mu : x0 + mu;  // v0 = x0 + sign(x0) mu
+          const R vv = v0 * v0 + sig;
+          if (sig == R(0) || !(vv > R(0)) || isinf(vv)) {  // nothing to annihilate
             e[k] = x0;
           } else {
-            double mu = sqrt(x0 * x0 + sig);
-            double v0 = (x0 <= 0.0) ? x0 - mu : x0 + mu;  // v0 = x0 + sign(x0) mu
-            e[k] = (x0 <= 0.0) ? mu : -mu;               // alpha = -sign(x0) ||x||
-            bk = 2.0 / (v0 * v0 + sig);
+            e[k] = (x0 <= R(0)) ? mu : -mu;               // alpha = -sign(x0) ||x||
+            bk = R(2) / vv;
             A[(k + 1) * ld + k] = v0;
           }
           d[k] = A[k * ld + k];
@@ -129,27 +155,27 @@ __global__ void __launch_bounds__(kThreads)
         }
       }
       __syncthreads();
-      const double bk = s_beta;
-      if (bk == 0.0) continue;  // uniform across the block
+      const R bk = s_beta;
+      if (bk == R(0)) continue;  // uniform across the block
       for (int i = tid; i < L; i += kThreads) v[i] = A[(k + 1 + i) * ld + k];
       __syncthreads();
       // p = beta A22 v, one thread per row, A22 symmetric with its lower triangle stored
       for (int i = tid; i < L; i += kThreads) {
-        const double* row = A + (k + 1 + i) * ld + (k + 1);
-        const double* col = A + (k + 1) * ld + (k + 1 + i);
-        double s = 0.0;
+        const R* row = A + (k + 1 + i) * ld + (k + 1);
+        const R* col = A + (k + 1) * ld + (k + 1 + i);
+        R s = 0;
         for (int j = 0; j < L; j++) s = fma((j <= i) ? row[j] : col[j * ld], v[j], s);
         w[i] = bk * s;
       }
       __syncthreads();
       if (warp == 0) {
-        double pv = 0.0;
+        R pv = 0;
         for (int i = lane; i < L; i += 32) pv = fma(w[i], v[i], pv);
         pv = warp_sum(pv);
-        if (lane == 0) s_kc = 0.5 * bk * pv;
+        if (lane == 0) s_kc = R(0.5) * bk * pv;
       }
       __syncthreads();
-      const double Kc = s_kc;
+      const R Kc = s_kc;
       for (int i = tid; i < L; i += kThreads) w[i] = fma(-Kc, v[i], w[i]);
       __syncthreads();
       // A22 -= v w^T + w v^T on the lower triangle
@@ -157,7 +183,7 @@ __global__ void __launch_bounds__(kThreads)
       for (int e2 = tid; e2 < E; e2 += kThreads) {
         int i, j;
         lower_index(e2, i, j);
-        double* a = A + (k + 1 + i) * ld + (k + 1 + j);
+        R* a = A + (k + 1 + i) * ld + (k + 1 + j);
         *a = fma(-v[i], w[j], fma(-w[i], v[j], *a));
       }
       __syncthreads();
@@ -166,11 +192,11 @@ __global__ void __launch_bounds__(kThreads)
       if (N >= 2) {
         d[N - 2] = A[(N - 2) * ld + (N - 2)];
         e[N - 2] = A[(N - 1) * ld + (N - 2)];
-        beta[N - 2] = 0.0;
+        beta[N - 2] = 0;
       }
       d[N - 1] = A[(N - 1) * ld + (N - 1)];
-      e[N - 1] = 0.0;
-      beta[N - 1] = 0.0;
+      e[N - 1] = 0;
+      beta[N - 1] = 0;
     }
     // reflector vectors (strictly below the diagonal of each column) back to G's slot
     for (int idx = tid; idx < N * N; idx += kThreads) {
@@ -183,32 +209,34 @@ __global__ void __launch_bounds__(kThreads)
 
 // ------------------------------------------------------------------------------------ E2a
 // One thread per zone: eigenvalues of Tri (sorted) and the inverse-iteration shifts.
+template <typename R>
 __global__ void __launch_bounds__(128)
-    k_eig_tridiag_values(int N, int32_t nzc, double* __restrict__ aux,
+    k_eig_tridiag_values(int N, int32_t nzc, R* __restrict__ aux,
                          const int32_t* __restrict__ nobs, int32_t* __restrict__ status) {
   const int32_t zl = blockIdx.x * blockDim.x + threadIdx.x;
   if (zl >= nzc || nobs[zl] == 0) return;
-  double* ax = aux + (int64_t)zl * aux_stride(N);
-  double d[kNMax], e[kNMax];
-  double onenrm = 0.0;
+  const R eps = Prec<R>::eps();
+  R* ax = aux + (int64_t)zl * aux_stride(N);
+  R d[kNMax], e[kNMax];
+  R onenrm = 0;
   for (int i = 0; i < N; i++) {
     d[i] = ax[i];
-    e[i] = (i < N - 1) ? ax[N + i] : 0.0;
+    e[i] = (i < N - 1) ? ax[N + i] : R(0);
   }
   for (int i = 0; i < N; i++) {
-    double s = fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0);
+    R s = fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : R(0));
     onenrm = fmax(onenrm, s);
   }
-  const double anorm = ax[5 * N];
+  const R scale = ax[5 * N];
   int st = 0;
   int hi = N - 1, sweeps = 0;
   const int max_sweeps = kMaxSweepsPerN * N;
-  const double abs_tol = kEps * anorm * 1e-3;
+  const R abs_tol = eps * onenrm;  // deflation floor: the rounding level of Tri
   while (hi > 0) {
     while (hi > 0) {
-      double t = fabs(e[hi - 1]);
-      if (t <= kEps * (fabs(d[hi - 1]) + fabs(d[hi])) || t <= abs_tol) {
-        e[hi - 1] = 0.0;
+      R t = fabs(e[hi - 1]);
+      if (t <= eps * (fabs(d[hi - 1]) + fabs(d[hi])) || t <= abs_tol) {
+        e[hi - 1] = 0;
         hi--;
       } else {
         break;
@@ -217,9 +245,9 @@ __global__ void __launch_bounds__(128)
     if (hi == 0) break;
     int lo = hi - 1;
     while (lo > 0) {
-      double t = fabs(e[lo - 1]);
-      if (t <= kEps * (fabs(d[lo - 1]) + fabs(d[lo])) || t <= abs_tol) {
-        e[lo - 1] = 0.0;
+      R t = fabs(e[lo - 1]);
+      if (t <= eps * (fabs(d[lo - 1]) + fabs(d[lo])) || t <= abs_tol) {
+        e[lo - 1] = 0;
         break;
       }
       lo--;
@@ -228,30 +256,30 @@ __global__ void __launch_bounds__(128)
       st |= ZST_EIG;
       break;
     }
-    const double a = d[hi - 1], b = d[hi], f = e[hi - 1];
-    const double del = 0.5 * (a - b);
-    const double den = del + copysign(sqrt(del * del + f * f), del == 0.0 ? 1.0 : del);
-    const double mu = (den == 0.0) ? b : b - f * f / den;
-    double x = d[lo] - mu, z = e[lo], bulge = 0.0;
+    const R a = d[hi - 1], b = d[hi], f = e[hi - 1];
+    const R del = R(0.5) * (a - b);
+    const R den = del + copysign(Prec<R>::sqrt_(del * del + f * f), del == R(0) ? R(1) : del);
+    const R mu = (den == R(0)) ? b : b - f * f / den;
+    R x = d[lo] - mu, z = e[lo], bulge = 0;
     for (int k = lo; k < hi; k++) {
       if (k > lo) {
         x = e[k - 1];
         z = bulge;
       }
-      const double r2 = x * x + z * z;
-      double c = 1.0, s = 0.0, r = 0.0;
-      if (r2 > 0.0) {
-        const double ri = rsqrt(r2);
+      const R r2 = x * x + z * z;
+      R c = 1, s = 0, r = 0;
+      if (r2 > R(0)) {
+        const R ri = Prec<R>::rsqrt_(r2);
         c = x * ri;
         s = z * ri;
         r = r2 * ri;
       }
       if (k > lo) e[k - 1] = r;
-      const double dk = d[k], dk1 = d[k + 1], ek = e[k];
-      const double ek1 = (k + 1 < hi) ? e[k + 1] : 0.0;
-      const double cc = c * c, ss = s * s, cs = c * s;
-      d[k] = cc * dk + 2.0 * cs * ek + ss * dk1;
-      d[k + 1] = ss * dk - 2.0 * cs * ek + cc * dk1;
+      const R dk = d[k], dk1 = d[k + 1], ek = e[k];
+      const R ek1 = (k + 1 < hi) ? e[k + 1] : R(0);
+      const R cc = c * c, ss = s * s, cs = c * s;
+      d[k] = cc * dk + R(2) * cs * ek + ss * dk1;
+      d[k + 1] = ss * dk - R(2) * cs * ek + cc * dk1;
       e[k] = cs * (dk1 - dk) + (cc - ss) * ek;
       if (k + 1 < hi) e[k + 1] = c * ek1;
       bulge = s * ek1;
@@ -259,7 +287,7 @@ __global__ void __launch_bounds__(128)
   }
   // ascending order (insertion sort)
   for (int i = 1; i < N; i++) {
-    double t = d[i];
+    R t = d[i];
     int k = i - 1;
     while (k >= 0 && d[k] > t) {
       d[k + 1] = d[k];
@@ -267,12 +295,12 @@ __global__ void __launch_bounds__(128)
     }
     d[k + 1] = t;
   }
-  double prev = 0.0;
+  R prev = 0;
   for (int j = 0; j < N; j++) {
-    ax[3 * N + j] = d[j];
-    double s = d[j];
+    ax[3 * N + j] = d[j] * scale;
+    R s = d[j];
     if (j > 0) {
-      const double pert = 10.0 * kEps * fabs(s);
+      const R pert = R(10) * eps * fabs(s);
       if (s - prev < pert) s = prev + pert;
     }
     ax[4 * N + j] = s;
@@ -284,49 +312,50 @@ __global__ void __launch_bounds__(128)
 
 // ------------------------------------------------------------------------------------ E2b
 // One thread per eigenpair (zone zl, eigenvalue j): inverse iteration on Tri.
+template <typename R>
 __global__ void __launch_bounds__(128)
-    k_eig_tridiag_vectors(int N, int32_t nzc, const double* __restrict__ aux,
-                          double* __restrict__ Zg, const int32_t* __restrict__ nobs) {
+    k_eig_tridiag_vectors(int N, int32_t nzc, const R* __restrict__ aux, R* __restrict__ Zg,
+                          const int32_t* __restrict__ nobs) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int32_t zl = (int32_t)(t / N);
   const int j = (int)(t - (int64_t)zl * N);
   if (zl >= nzc || nobs[zl] == 0) return;
-  const double* ax = aux + (int64_t)zl * aux_stride(N);
-  const double* td = ax;
-  const double* te = ax + N;
-  const double l = ax[4 * N + j];
-  const double onenrm = ax[5 * N + 1];
-  double* zj = Zg + (int64_t)zl * N * N + (int64_t)j * N;
-  if (!(onenrm > 1e-290)) {  // Tri = 0: every vector is an eigenvector
-    for (int i = 0; i < N; i++) zj[i] = (i == j) ? 1.0 : 0.0;
+  const R* ax = aux + (int64_t)zl * aux_stride(N);
+  const R* td = ax;
+  const R* te = ax + N;
+  const R l = ax[4 * N + j];
+  const R onenrm = ax[5 * N + 1];
+  R* zj = Zg + (int64_t)zl * N * N + (int64_t)j * N;
+  if (!(onenrm > R(1e4) * Prec<R>::tiny())) {  // Tri = 0: every vector is an eigenvector
+    for (int i = 0; i < N; i++) zj[i] = (i == j) ? R(1) : R(0);
     return;
   }
-  const double tiny = kEps * onenrm;
-  double u1[kNMax], u2[kNMax], lm[kNMax], uinv[kNMax], x[kNMax];
+  const R tiny = Prec<R>::eps() * onenrm;
+  R u1[kNMax], u2[kNMax], lm[kNMax], uinv[kNMax], x[kNMax];
   unsigned char piv[kNMax];
   // LU with partial pivoting of Tri - l I (U: diagonal + two super-diagonals), branch-free
-  double cd = td[0] - l, csup = (N > 1) ? te[0] : 0.0;
+  R cd = td[0] - l, csup = (N > 1) ? te[0] : R(0);
   for (int i = 0; i < N - 1; i++) {
-    const double sub = te[i], dg = td[i + 1] - l, sp = (i + 1 < N - 1) ? te[i + 1] : 0.0;
+    const R sub = te[i], dg = td[i + 1] - l, sp = (i + 1 < N - 1) ? te[i + 1] : R(0);
     const bool swap = fabs(cd) < fabs(sub);
-    double pivot = swap ? sub : cd;
+    R pivot = swap ? sub : cd;
     if (!swap && fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
-    const double ui = 1.0 / pivot;
-    const double li = (swap ? cd : sub) * ui;
+    const R ui = R(1) / pivot;
+    const R li = (swap ? cd : sub) * ui;
     u1[i] = swap ? dg : csup;
-    u2[i] = swap ? sp : 0.0;
+    u2[i] = swap ? sp : R(0);
     piv[i] = swap ? 1 : 0;
     lm[i] = li;
     uinv[i] = ui;
-    const double a = swap ? csup : dg, b = swap ? dg : csup;
+    const R a = swap ? csup : dg, b = swap ? dg : csup;
     cd = fma(-li, b, a);
-    const double nls = -li * sp;
+    const R nls = -li * sp;
     csup = swap ? nls : sp;
   }
   {
-    double pivot = cd;
+    R pivot = cd;
     if (fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
-    uinv[N - 1] = 1.0 / pivot;
+    uinv[N - 1] = R(1) / pivot;
   }
   // deterministic pseudo-random start vector
   for (int i = 0; i < N; i++) {
@@ -334,12 +363,12 @@ __global__ void __launch_bounds__(128)
     h ^= h >> 15;
     h *= 2246822519u;
     h ^= h >> 13;
-    x[i] = (double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5;
+    x[i] = (R)((double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5);
   }
   for (int it = 0; it < 2; it++) {
     for (int i = 0; i < N - 1; i++) {
-      const double a = x[i], b = x[i + 1];
-      const double xi = piv[i] ? b : a, xn = piv[i] ? a : b;
+      const R a = x[i], b = x[i + 1];
+      const R xi = piv[i] ? b : a, xn = piv[i] ? a : b;
       x[i] = xi;
       x[i + 1] = fma(-lm[i], xi, xn);
     }
@@ -348,40 +377,42 @@ __global__ void __launch_bounds__(128)
     for (int i = N - 3; i >= 0; i--)
       x[i] = fma(-u2[i], x[i + 2], fma(-u1[i], x[i + 1], x[i])) * uinv[i];
     // scale by the largest entry first, so the sum of squares cannot overflow
-    double mx = 0.0;
+    R mx = 0;
     for (int i = 0; i < N; i++) mx = fmax(mx, fabs(x[i]));
-    const double im = 1.0 / mx;
-    double nrm = 0.0;
+    const R im = R(1) / mx;
+    R nrm = 0;
     for (int i = 0; i < N; i++) {
       x[i] *= im;
       nrm = fma(x[i], x[i], nrm);
     }
-    const double sc = rsqrt(nrm);
+    const R sc = Prec<R>::rsqrt_(nrm);
     for (int i = 0; i < N; i++) x[i] *= sc;
   }
   for (int i = 0; i < N; i++) zj[i] = x[i];
 }
 
 // ------------------------------------------------------------------------------------ E3
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-    k_eig_transform(int N, int32_t nzc, double* __restrict__ GT, const double* __restrict__ aux,
-                    const double* __restrict__ Zg, const double* __restrict__ gv,
-                    const int32_t* __restrict__ nobs, int rotate, double* __restrict__ ampl_out,
+    k_eig_transform(int N, int32_t nzc, R* __restrict__ GT, const R* __restrict__ aux,
+                    const R* __restrict__ Zg, const R* __restrict__ gv,
+                    const int32_t* __restrict__ nobs, int rotate, R* __restrict__ ampl_out,
                     int32_t* __restrict__ status, int32_t* __restrict__ work) {
-  extern __shared__ double dyn[];
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  R* dyn = reinterpret_cast<R*>(dyn_raw);
   const int ld = N + 1;
-  double* A = dyn;           // [N][ld] reflectors, then T_sym
-  double* U = A + N * ld;    // [N][ld] Z, then U
-  double* lam = U + N * ld;  // [N] 1/(1+lambda)
-  double* sq = lam + N;      // [N] sqrt(1/(1+lambda))
-  double* g = sq + N;        // [N]
-  double* beta = g + N;      // [N]
-  double* t0 = beta + N;     // [N]
-  double* t1 = t0 + N;       // [N]
-  double* vv = t1 + N;       // [N]
-  double* qs = vv + N;       // [N] lambda^(1/4)
+  R* A = dyn;           // [N][ld] reflectors, then T_sym
+  R* U = A + N * ld;    // [N][ld] Z, then U
+  R* lam = U + N * ld;  // [N] 1/(1+lambda)         (evaluated in FP64)
+  R* sq = lam + N;      // [N] sqrt(1/(1+lambda))   (evaluated in FP64)
+  R* g = sq + N;        // [N]
+  R* beta = g + N;      // [N]
+  R* t0 = beta + N;     // [N]
+  R* t1 = t0 + N;       // [N]
+  R* vv = t1 + N;       // [N]
+  R* qs = vv + N;       // [N] lambda^(1/4)        (evaluated in FP64)
   int* cst = reinterpret_cast<int*>(qs + N);  // [N] cluster start of each eigenvector
-  __shared__ double red[kWarps];
+  __shared__ R red[kWarps];
   __shared__ int32_t s_zone;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (;;) {
@@ -393,26 +424,27 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
       continue;
     }
-    double* Gz = GT + (int64_t)zl * N * N;
-    const double* ax = aux + (int64_t)zl * aux_stride(N);
-    const double* Z = Zg + (int64_t)zl * N * N;
+    R* Gz = GT + (int64_t)zl * N * N;
+    const R* ax = aux + (int64_t)zl * aux_stride(N);
+    const R* Z = Zg + (int64_t)zl * N * N;
     for (int idx = tid; idx < N * N; idx += kThreads) {
       int i = idx / N, j = idx - i * N;
-      A[i * ld + j] = (i > j) ? Gz[idx] : 0.0;
+      A[i * ld + j] = (i > j) ? Gz[idx] : R(0);
       U[j * ld + i] = Z[idx];  // Z[i*N + j] = component j of eigenvector i -> U[j][i]
     }
     for (int i = tid; i < N; i += kThreads) {
-      double l = ax[3 * N + i];
+      double l = (double)ax[3 * N + i];
       if (l < 0.0) l = 0.0;
       const double li = 1.0 / (1.0 + l);
-      lam[i] = li;
-      sq[i] = sqrt(li);
-      qs[i] = sqrt(sq[i]);
+      const double s = sqrt(li);
+      lam[i] = (R)li;
+      sq[i] = (R)s;
+      qs[i] = (R)sqrt(s);
       g[i] = gv[(int64_t)zl * N + i];
       beta[i] = ax[2 * N + i];
     }
     if (tid == 0) {
-      const double ortol = 1e-3 * ax[5 * N + 1];
+      const R ortol = R(1e-3) * ax[5 * N + 1] * ax[5 * N];
       int c0 = 0;
       cst[0] = 0;
       for (int j = 1; j < N; j++) {
@@ -421,64 +453,116 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
     __syncthreads();
-    // clusters: two classical Gram-Schmidt passes of column j against columns [cst[j], j)
-    for (int j = 1; j < N; j++) {
-      const int k0 = cst[j], nk = j - k0;
+    // FP64: two classical Gram-Schmidt passes of column j against its cluster [cst[j], j).
+    // FP32 (larger relative rounding, gaps between clusters less reliable): every column
+    // against all columns of larger eigenvalue, largest first.
+    const bool full = sizeof(R) < sizeof(double);
+    for (int jj = 1; jj < N; jj++) {
+      const int j = full ? N - 1 - jj : jj;
+      const int k0 = full ? j + 1 : cst[j], nk = full ? N - 1 - j : j - k0;
       if (nk == 0) continue;  // uniform
       for (int pass = 0; pass < 2; pass++) {
-        // one thread per dot product (no cross-lane reductions on the FP64 pipe)
+        // one thread per dot product (no cross-lane reductions)
         for (int kk = tid; kk < nk; kk += kThreads) {
-          double s = 0.0;
+          R s = 0;
           for (int i = 0; i < N; i++) s = fma(U[i * ld + k0 + kk], U[i * ld + j], s);
           t0[kk] = s;
         }
         __syncthreads();
         for (int i = tid; i < N; i += kThreads) {
-          double s = U[i * ld + j];
+          R s = U[i * ld + j];
           for (int kk = 0; kk < nk; kk++) s = fma(-t0[kk], U[i * ld + k0 + kk], s);
           U[i * ld + j] = s;
         }
         __syncthreads();
       }
       if (warp == 0) {
-        double s = 0.0;
+        R s = 0;
         for (int i = lane; i < N; i += 32) s = fma(U[i * ld + j], U[i * ld + j], s);
         s = warp_sum(s);
-        if (lane == 0) red[0] = rsqrt(s);
+        // a unit vector that kept less than half its norm lay (almost) in the span of the
+        // cluster's earlier vectors: mark it for the complement fill below
+        if (lane == 0) {
+          red[0] = (s > R(0)) ? Prec<R>::rsqrt_(s) : R(0);
+          if (s < R(0.5)) cst[j] = -1;
+        }
       }
       __syncthreads();
-      const double sc = red[0];
+      const R sc = red[0];
+      for (int i = tid; i < N; i += kThreads) U[i * ld + j] *= sc;
+      __syncthreads();
+    }
+    // complement fill: a collapsed vector is replaced by a pseudo-random vector made
+    // orthogonal (two classical Gram-Schmidt passes) to every accepted eigenvector. When the
+    // accepted vectors are accurate, the complement is the missing part of the degenerate
+    // cluster's invariant subspace, so any unit vector in it is an eigenvector.
+    for (int j = 0; j < N; j++) {
+      if (cst[j] >= 0) continue;  // uniform
+      for (int i = tid; i < N; i += kThreads) {
+        unsigned h = (unsigned)i * 2246822519u ^ ((unsigned)j * 3266489917u + 0x27d4eb2fu);
+        h ^= h >> 15;
+        h *= 2654435761u;
+        h ^= h >> 13;
+        U[i * ld + j] = (R)((double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5);
+      }
+      __syncthreads();
+      for (int pass = 0; pass < 2; pass++) {
+        for (int k = tid; k < N; k += kThreads) {
+          R s = 0;
+          if (k != j && cst[k] >= 0)
+            for (int i = 0; i < N; i++) s = fma(U[i * ld + k], U[i * ld + j], s);
+          t0[k] = s;
+        }
+        __syncthreads();
+        for (int i = tid; i < N; i += kThreads) {
+          R s = U[i * ld + j];
+          for (int k = 0; k < N; k++) s = fma(-t0[k], U[i * ld + k], s);
+          U[i * ld + j] = s;
+        }
+        __syncthreads();
+      }
+      if (warp == 0) {
+        R s = 0;
+        for (int i = lane; i < N; i += 32) s = fma(U[i * ld + j], U[i * ld + j], s);
+        s = warp_sum(s);
+        if (lane == 0) {
+          red[0] = (s > R(0)) ? Prec<R>::rsqrt_(s) : R(0);
+          cst[j] = j;  // accepted
+        }
+      }
+      __syncthreads();
+      const R sc = red[0];
       for (int i = tid; i < N; i += kThreads) U[i * ld + j] *= sc;
       __syncthreads();
     }
     // U = Q_h Z = H_0 H_1 ... H_{N-3} Z: apply H_k for k = N-3 .. 0
     for (int k = N - 3; k >= 0; k--) {
-      const double bk = beta[k];
-      if (bk == 0.0) continue;  // uniform across the block
+      const R bk = beta[k];
+      if (bk == R(0)) continue;  // uniform across the block
       const int L = N - k - 1;
       for (int j = tid; j < N; j += kThreads) {
-        double s = 0.0;
+        R s = 0;
         for (int i = 0; i < L; i++) s = fma(A[(k + 1 + i) * ld + k], U[(k + 1 + i) * ld + j], s);
         t0[j] = bk * s;
       }
       __syncthreads();
       for (int idx = tid; idx < L * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
-        double* u = U + (k + 1 + i) * ld + j;
+        R* u = U + (k + 1 + i) * ld + j;
         *u = fma(-A[(k + 1 + i) * ld + k], t0[j], *u);
       }
       __syncthreads();
     }
     // ampl = U (lambda .* (U^T g))
     for (int i = tid; i < N; i += kThreads) {
-      double s = 0.0;
+      R s = 0;
       for (int r = 0; r < N; r++) s = fma(U[r * ld + i], g[r], s);
       t0[i] = lam[i] * s;
     }
     __syncthreads();
     int nan_flag = 0;
     for (int r = tid; r < N; r += kThreads) {
-      double s = 0.0;
+      R s = 0;
       for (int i = 0; i < N; i++) s = fma(U[r * ld + i], t0[i], s);
       ampl_out[(int64_t)zl * N + r] = s;
       if (!(s == s) || isinf(s)) nan_flag = 1;
@@ -487,25 +571,25 @@ __global__ void __launch_bounds__(kThreads)
     if (rotate) {
       // v = normate(U (colsum(U) / sqrt(lambda)))
       for (int i = tid; i < N; i += kThreads) {
-        double s = 0.0;
+        R s = 0;
         for (int r = 0; r < N; r++) s += U[r * ld + i];
         t1[i] = s / sq[i];
       }
       __syncthreads();
       for (int r = tid; r < N; r += kThreads) {
-        double s = 0.0;
+        R s = 0;
         for (int i = 0; i < N; i++) s = fma(U[r * ld + i], t1[i], s);
         vv[r] = s;
       }
       __syncthreads();
       if (warp == 0) {
-        double s = 0.0;
+        R s = 0;
         for (int r = lane; r < N; r += 32) s = fma(vv[r], vv[r], s);
         s = warp_sum(s);
-        if (lane == 0) red[0] = 1.0 / sqrt(s);
+        if (lane == 0) red[0] = R(1) / Prec<R>::sqrt_(s);
       }
       __syncthreads();
-      const double inv = red[0];
+      const R inv = red[0];
       for (int r = tid; r < N; r += kThreads) vv[r] *= inv;
     }
     // T_sym = U diag(sqrt(lambda)) U^T: U's columns scaled by lambda^(1/4), then U U^T
@@ -518,26 +602,26 @@ __global__ void __launch_bounds__(kThreads)
     for (int e2 = tid; e2 < E; e2 += kThreads) {
       int a, b;
       lower_index(e2, a, b);
-      const double* qa = U + a * ld;
-      const double* qb = U + b * ld;
-      double s = 0.0;
+      const R* qa = U + a * ld;
+      const R* qb = U + b * ld;
+      R s = 0;
       for (int k = 0; k < N; k++) s = fma(qa[k], qb[k], s);
       A[a * ld + b] = s;
       A[b * ld + a] = s;
     }
     __syncthreads();
     if (rotate) {
-      const double vN = vv[N - 1];
-      const double sv = signbit(vN) ? -1.0 : 1.0;
-      const double cv = 1.0 + fabs(vN);
-      const double wv = 1.0 / sqrt((double)N);
-      const double cw = 1.0 + wv;
+      const R vN = vv[N - 1];
+      const R sv = signbit(vN) ? R(-1) : R(1);
+      const R cv = R(1) + fabs(vN);
+      const R wv = (R)(1.0 / sqrt((double)N));
+      const R cw = R(1) + wv;
       // t0 = T_sym u_v, t1 = T_sym v
       for (int i = tid; i < N; i += kThreads) {
-        const double* ti = A + i * ld;
-        double sa = 0.0, sb = 0.0;
+        const R* ti = A + i * ld;
+        R sa = 0, sb = 0;
         for (int j = 0; j < N; j++) {
-          sa = fma(ti[j], vv[j] + ((j == N - 1) ? sv : 0.0), sa);
+          sa = fma(ti[j], vv[j] + ((j == N - 1) ? sv : R(0)), sa);
           sb = fma(ti[j], vv[j], sb);
         }
         t0[i] = sa;
@@ -545,28 +629,28 @@ __global__ void __launch_bounds__(kThreads)
       }
       __syncthreads();
       // T1 = T_sym - t0 u_v^T / c_v
-      const double icv = 1.0 / cv, icw = 1.0 / cw;
+      const R icv = R(1) / cv, icw = R(1) / cw;
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
-        double uj = vv[j] + ((j == N - 1) ? sv : 0.0);
+        R uj = vv[j] + ((j == N - 1) ? sv : R(0));
         A[i * ld + j] = fma(-t0[i] * icv, uj, A[i * ld + j]);
       }
       __syncthreads();
       // g <- T1 u_w (g is no longer needed)
       for (int i = tid; i < N; i += kThreads) {
-        const double* ti = A + i * ld;
-        double s = 0.0;
-        for (int j = 0; j < N; j++) s = fma(ti[j], wv + ((j == N - 1) ? 1.0 : 0.0), s);
+        const R* ti = A + i * ld;
+        R s = 0;
+        for (int j = 0; j < N; j++) s = fma(ti[j], wv + ((j == N - 1) ? R(1) : R(0)), s);
         g[i] = s * icw;
       }
       __syncthreads();
       // T = T1 - (T1 u_w) u_w^T / c_w + (1 - s_v s_w) (T_sym v) w^T   (s_w = +1)
-      const double extra = 1.0 - sv;
+      const R extra = R(1) - sv;
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
-        double uj = wv + ((j == N - 1) ? 1.0 : 0.0);
-        double t = fma(-g[i], uj, A[i * ld + j]);
-        if (extra != 0.0) t = fma(extra * t1[i], wv, t);
+        R uj = wv + ((j == N - 1) ? R(1) : R(0));
+        R t = fma(-g[i], uj, A[i * ld + j]);
+        if (extra != R(0)) t = fma(extra * t1[i], wv, t);
         Gz[idx] = t;
       }
     } else {
@@ -591,39 +675,55 @@ int grid_for_smem(const void* fn, size_t smem, int32_t nzc) {
   return grid;
 }
 
-}  // namespace
-
-size_t zone_eig_fp64_aux(int N) { return (size_t)aux_stride(N); }
-
-cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
-                          const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
-                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st) {
+template <typename R>
+cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32_t* d_nobs,
+                          int rotate, R* d_ampl, int32_t* d_status, R* d_aux, R* d_Z,
+                          int32_t* d_work, cudaStream_t st) {
   if (N < 2 || N > kNMax) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int32_t) * (nzc > 0 ? nzc : 1), st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(d_work, 0, 2 * sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
   // E1
-  size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(double);
-  e = cudaFuncSetAttribute(k_eig_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(R);
+  e = cudaFuncSetAttribute(k_eig_tridiag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem1);
   if (e != cudaSuccess) return e;
-  k_eig_tridiag<<<grid_for_smem((const void*)k_eig_tridiag, smem1, nzc), kThreads, smem1, st>>>(
-      N, nzc, d_GT, d_aux, d_nobs, d_work);
+  k_eig_tridiag<R><<<grid_for_smem((const void*)k_eig_tridiag<R>, smem1, nzc), kThreads, smem1,
+                     st>>>(N, nzc, d_GT, d_aux, d_nobs, d_work);
   // E2a, E2b
-  k_eig_tridiag_values<<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   const int64_t pairs = (int64_t)nzc * N;
-  k_eig_tridiag_vectors<<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
-                                                                          d_nobs);
+  k_eig_tridiag_vectors<R><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
+                                                                             d_nobs);
   // E3
-  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(double);
-  e = cudaFuncSetAttribute(k_eig_transform, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
+  e = cudaFuncSetAttribute(k_eig_transform<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem3);
   if (e != cudaSuccess) return e;
-  k_eig_transform<<<grid_for_smem((const void*)k_eig_transform, smem3, nzc), kThreads, smem3,
-                    st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
-                          d_work + 1);
+  k_eig_transform<R><<<grid_for_smem((const void*)k_eig_transform<R>, smem3, nzc), kThreads,
+                       smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl,
+                                    d_status, d_work + 1);
   count_launches(4);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t zone_eig_aux(int N) { return (size_t)aux_stride(N); }
+
+cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
+                          const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
+                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st) {
+  return zone_eig_impl<double>(N, nzc, d_GT, d_g, d_nobs, rotate, d_ampl, d_status, d_aux, d_Z,
+                               d_work, st);
+}
+
+cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,
+                          const int32_t* d_nobs, int rotate, float* d_ampl, int32_t* d_status,
+                          float* d_aux, float* d_Z, int32_t* d_work, cudaStream_t st) {
+  return zone_eig_impl<float>(N, nzc, d_GT, d_g, d_nobs, rotate, d_ampl, d_status, d_aux, d_Z,
+                              d_work, st);
 }
 
 }  // namespace oakg

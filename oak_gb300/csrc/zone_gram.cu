@@ -1,4 +1,7 @@
-// K1 + K2 (FP64) -- per-zone observation selection and the Gram / innovation products.
+// K1 + K2 -- per-zone observation selection and the Gram / innovation products. Selection is
+// always FP64 (the same decisions as a CPU evaluation of the reference); the products are
+// accumulated in R: double for the plain form, float for the mixed-precision form (with
+// compensated (Kahan) sums for the innovation projection).
 //
 // For zone z (one CTA at a time, zones handed out by an atomic work counter):
 //   selection  (assimilation.F90:3683-3771): d = distance(obs, zone) for loctype 1 (metric
@@ -169,11 +172,11 @@ struct ZoneShared {
 };
 
 // Accumulate the staged observations list[0..len) into the per-thread Gram entries.
-template <int MAXE>
+template <int MAXE, typename R>
 __device__ __forceinline__ void flush_list(ZoneShared& zs, int len, const SortedObs& so, int N,
-                                           int CH, double* sh, double* st, double* sinn,
+                                           int CH, R* sh, R* st, R* sinn,
                                            const int32_t (&ea)[MAXE], const int32_t (&eb)[MAXE],
-                                           double (&acc)[MAXE], int E, int nent) {
+                                           R (&acc)[MAXE], R (&cmp)[MAXE], int E, int nent) {
   for (int c0 = 0; c0 < len; c0 += CH) {
     int rows = min(CH, len - c0);
     __syncthreads();  // previous chunk fully consumed
@@ -181,24 +184,34 @@ __device__ __forceinline__ void flush_list(ZoneShared& zs, int len, const Sorted
       int i = idx / N, k = idx - i * N;
       int32_t q = zs.list_q[c0 + i];
       double h = so.HSt[(int64_t)q * N + k];
-      sh[i * N + k] = h;
-      st[i * N + k] = zs.list_c[c0 + i] * h;
+      sh[i * N + k] = (R)h;
+      st[i * N + k] = (R)(zs.list_c[c0 + i] * h);
     }
     for (int i = threadIdx.x; i < rows; i += kThreads) {
       int32_t q = zs.list_q[c0 + i];
-      sinn[i] = zs.list_c[c0 + i] * so.innov[q];
+      sinn[i] = (R)(zs.list_c[c0 + i] * so.innov[q]);
     }
     __syncthreads();
 #pragma unroll
     for (int s = 0; s < MAXE; s++) {
       int e = threadIdx.x + s * kThreads;
       if (e < nent) {
-        double a = acc[s];
+        R a = acc[s];
         const int ia = ea[s], ib = eb[s];
         if (e < E) {
           for (int i = 0; i < rows; i++) a = fma(sh[i * N + ia], st[i * N + ib], a);
-        } else {
+        } else if (sizeof(R) == sizeof(double)) {
           for (int i = 0; i < rows; i++) a = fma(sh[i * N + ia], sinn[i], a);
+        } else {
+          // compensated (Kahan) sum of the innovation projection in FP32
+          R c = cmp[s];
+          for (int i = 0; i < rows; i++) {
+            const R y = sh[i * N + ia] * sinn[i] - c;
+            const R t = a + y;
+            c = (t - a) - y;
+            a = t;
+          }
+          cmp[s] = c;
         }
         acc[s] = a;
       }
@@ -206,17 +219,17 @@ __device__ __forceinline__ void flush_list(ZoneShared& zs, int len, const Sorted
   }
 }
 
-template <int MAXE>
+template <int MAXE, typename R>
 __global__ void __launch_bounds__(kThreads)
-    k_zone_gram_fp64(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
-                     const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
-                     const double* __restrict__ max_len, double* __restrict__ G,
-                     double* __restrict__ gv, int32_t* __restrict__ nobs, int brute, int CH,
-                     int32_t* __restrict__ work) {
-  extern __shared__ double dyn[];
-  double* sh = dyn;            // [CH][N]
-  double* st = sh + CH * N;    // [CH][N]
-  double* sinn = st + CH * N;  // [CH]
+    k_zone_gram(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
+                const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
+                const double* __restrict__ max_len, R* __restrict__ G, R* __restrict__ gv,
+                int32_t* __restrict__ nobs, int brute, int CH, int32_t* __restrict__ work) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  R* dyn = reinterpret_cast<R*>(dyn_raw);
+  R* sh = dyn;            // [CH][N]
+  R* st = sh + CH * N;    // [CH][N]
+  R* sinn = st + CH * N;  // [CH]
   __shared__ ZoneShared zs;
 
   const int E = N * (N + 1) / 2;
@@ -250,14 +263,14 @@ __global__ void __launch_bounds__(kThreads)
     const double zzc = zone_xyzt[4 * (int64_t)z + 2], ztc = zone_xyzt[4 * (int64_t)z + 3];
     const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
     const double zv = (lp.loctype == 1) ? zy : 0.0;
-    const double L = corr_len[z], R = max_len[z];
+    const double L = corr_len[z], Rmax = max_len[z];
     if (threadIdx.x == 0) {
       zs.list_len = 0;
       zs.nrel = 0;
     }
-    double acc[MAXE];
+    R acc[MAXE], cmp[MAXE];
 #pragma unroll
-    for (int s = 0; s < MAXE; s++) acc[s] = 0.0;
+    for (int s = 0; s < MAXE; s++) acc[s] = cmp[s] = R(0);
 
     ScanRange sr;
     if (full_scan) {
@@ -267,7 +280,7 @@ __global__ void __launch_bounds__(kThreads)
       sr.cv1 = g.nv - 1;
       sr.all_u = 1;
     } else {
-      sr = zone_scan_range(g, lp.metric, lp.loctype, zu, zv, R);
+      sr = zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
     }
     __syncthreads();
     int nrel_local = 0;
@@ -314,12 +327,12 @@ __global__ void __launch_bounds__(kThreads)
               d = fabs(__dsub_rn(so.u[q], zu));
             double w;
             if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-              rel = (d <= R);
+              rel = (d <= Rmax);
               double t = d / L;
               w = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
             } else {
               w = locfun(d / L);
-              rel = (d <= R) && (w != 0.0);
+              rel = (d <= Rmax) && (w != 0.0);
             }
             sel = rel || !lp.localise;
             if (sel) c = w * (w / so.r[q]);
@@ -344,7 +357,7 @@ __global__ void __launch_bounds__(kThreads)
           __syncthreads();
           if (zs.list_len >= kFlushAt) {
             int len = zs.list_len;
-            flush_list<MAXE>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, E, nent);
+            flush_list<MAXE, R>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, cmp, E, nent);
             __syncthreads();
             if (threadIdx.x == 0) zs.list_len = 0;
             __syncthreads();
@@ -354,7 +367,7 @@ __global__ void __launch_bounds__(kThreads)
     }
     if (zs.list_len > 0) {
       int len = zs.list_len;
-      flush_list<MAXE>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, E, nent);
+      flush_list<MAXE, R>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, cmp, E, nent);
     }
     // relevant-observation count of the zone
     for (int o = 16; o > 0; o >>= 1) nrel_local += __shfl_xor_sync(0xffffffffu, nrel_local, o);
@@ -363,7 +376,7 @@ __global__ void __launch_bounds__(kThreads)
     const int nrel = zs.nrel;
     if (threadIdx.x == 0) nobs[z] = nrel;
     if (nrel > 0) {
-      double* Gz = G + (int64_t)zl * N * N;
+      R* Gz = G + (int64_t)zl * N * N;
 #pragma unroll
       for (int s = 0; s < MAXE; s++) {
         int e = threadIdx.x + s * kThreads;
@@ -457,18 +470,18 @@ inline int chunk_rows(int N) {
   return ch;
 }
 
-template <int MAXE>
+template <int MAXE, typename R>
 cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                         int32_t nzc, const double* zone_xyzt, const double* corr_len,
-                        const double* max_len, double* d_G, double* d_g, int32_t* d_nobs,
+                        const double* max_len, R* d_G, R* d_g, int32_t* d_nobs,
                         int brute, int32_t* d_work, cudaStream_t st) {
   int CH = chunk_rows(N);
-  size_t smem = (size_t)(2 * CH * N + CH) * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(k_zone_gram_fp64<MAXE>,
+  size_t smem = (size_t)(2 * CH * N + CH) * sizeof(R);
+  cudaError_t e = cudaFuncSetAttribute(k_zone_gram<MAXE, R>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int blocks_per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zone_gram_fp64<MAXE>,
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zone_gram<MAXE, R>,
                                                     kThreads, smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
@@ -478,9 +491,9 @@ cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams
   if (grid > nzc) grid = nzc > 0 ? nzc : 1;
   e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
-  k_zone_gram_fp64<MAXE><<<grid, kThreads, smem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt,
-                                                        corr_len, max_len, d_G, d_g, d_nobs,
-                                                        brute, CH, d_work);
+  k_zone_gram<MAXE, R><<<grid, kThreads, smem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
+                                                      max_len, d_G, d_g, d_nobs, brute, CH,
+                                                      d_work);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -521,14 +534,33 @@ int max_fp64_ensemble() { return 112; }
     if (per_ <= 26) return FN<26>(__VA_ARGS__);                             \
     return cudaErrorInvalidValue;                                           \
   } while (0)
+#define OAKG_GRAM_DISPATCH_T(FN, R, ...)                                    \
+  do {                                                                      \
+    int ent_ = N * (N + 1) / 2 + N;                                         \
+    int per_ = (ent_ + kThreads - 1) / kThreads;                            \
+    if (per_ <= 3) return FN<3, R>(__VA_ARGS__);                            \
+    if (per_ <= 9) return FN<9, R>(__VA_ARGS__);                            \
+    if (per_ <= 19) return FN<19, R>(__VA_ARGS__);                          \
+    if (per_ <= 26) return FN<26, R>(__VA_ARGS__);                          \
+    return cudaErrorInvalidValue;                                           \
+  } while (0)
 
 cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
                            int32_t z0, int32_t nzc, const double* zone_xyzt,
                            const double* corr_len, const double* max_len, double* d_G,
                            double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
                            cudaStream_t st) {
-  OAKG_GRAM_DISPATCH(launch_zone, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len, d_G, d_g,
-                     d_nobs, brute, d_work, st);
+  OAKG_GRAM_DISPATCH_T(launch_zone, double, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len,
+                       d_G, d_g, d_nobs, brute, d_work, st);
+}
+
+cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                           int32_t z0, int32_t nzc, const double* zone_xyzt,
+                           const double* corr_len, const double* max_len, float* d_G,
+                           float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                           cudaStream_t st) {
+  OAKG_GRAM_DISPATCH_T(launch_zone, float, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len,
+                       d_G, d_g, d_nobs, brute, d_work, st);
 }
 
 cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,

@@ -1,0 +1,157 @@
+// K5 -- ensemble update per zone (T and the amplitudes in R: double for the plain form, float
+// for the mixed-precision form; Sf, Sa, xf, xa stay double at the boundary):
+//   xa(i1:i2) = xf(i1:i2) + Sf(i1:i2,:) ampl          (rrsqrt.F90:151 and :462-464)
+//   Sa(i1:i2,:) = Sf(i1:i2,:) T                       (rrsqrt.F90:165-185 with T from K4)
+// Zones without relevant observations keep xa = xf and Sa = Sf (rrsqrt.F90:322-326, :371).
+//
+// Sf/Sa are the reference's column-major (n, N) arrays (leading dimension ldS). A task is a
+// tile of up to kRows consecutive rows of one zone; the tile of Sf is staged column by column
+// into shared memory (coalesced along rows), T (N x N) next to it, and Sa is written column by
+// column. Reads and writes are in place safe (Sa may alias Sf, xa may alias xf).
+// Work per zone: 2 nz N^2 FP64 flops, 2 nz N 8-byte reads/writes + N^2 8-byte T read.
+#include <cuda_runtime.h>
+
+#include "oakg_internal.cuh"
+
+namespace oakg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRows = 64;
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+    k_zone_update(int N, int32_t z0, int32_t nzc, const int64_t* __restrict__ zone_start,
+                  int tiles_per_zone, const double* __restrict__ xf,
+                  const double* __restrict__ Sf, int64_t ldS, const R* __restrict__ T,
+                  const R* __restrict__ ampl, const int32_t* __restrict__ nobs,
+                  double* __restrict__ xa, double* __restrict__ Sa) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  R* dyn = reinterpret_cast<R*>(dyn_raw);
+  R* Ts = dyn;                // [N][N]
+  R* Ss = Ts + N * N;         // [N][kRows]  (column k of the tile at Ss + k*kRows)
+  R* as = Ss + N * kRows;     // [N]
+  const int64_t ntasks = (int64_t)nzc * tiles_per_zone;
+  for (int64_t task = blockIdx.x; task < ntasks; task += gridDim.x) {
+    const int32_t zl = (int32_t)(task / tiles_per_zone);
+    const int tile = (int)(task - (int64_t)zl * tiles_per_zone);
+    const int32_t z = z0 + zl;
+    const int64_t i1 = zone_start[z], i2 = zone_start[z + 1];
+    const int64_t r0 = i1 + (int64_t)tile * kRows;
+    if (r0 >= i2) continue;  // uniform across the block
+    const int R_ = (int)((i2 - r0) < kRows ? (i2 - r0) : kRows);
+    if (nobs[zl] == 0) {
+      for (int idx = threadIdx.x; idx < R_; idx += kThreads) xa[r0 + idx] = xf[r0 + idx];
+      if (Sa && Sa != Sf) {
+        for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
+          int k = idx / R_, r = idx - k * R_;
+          Sa[r0 + r + (int64_t)k * ldS] = Sf[r0 + r + (int64_t)k * ldS];
+        }
+      }
+      continue;
+    }
+    __syncthreads();  // previous task's shared data consumed
+    const R* Tz = T + (int64_t)zl * N * N;
+    if (Sa) {
+      for (int idx = threadIdx.x; idx < N * N; idx += kThreads) Ts[idx] = Tz[idx];
+    }
+    for (int idx = threadIdx.x; idx < N; idx += kThreads) as[idx] = ampl[(int64_t)zl * N + idx];
+    for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
+      int k = idx / R_, r = idx - k * R_;
+      Ss[k * kRows + r] = (R)Sf[r0 + r + (int64_t)k * ldS];
+    }
+    __syncthreads();
+    // xa = xf + Sf ampl
+    for (int r = threadIdx.x; r < R_; r += kThreads) {
+      R s = 0;
+      for (int k = 0; k < N; k++) s = fma(Ss[k * kRows + r], as[k], s);
+      xa[r0 + r] = xf[r0 + r] + (double)s;
+    }
+    if (Sa) {
+      // Sa(r, c) = sum_k Sf(r, k) T(k, c); consecutive threads -> consecutive rows
+      for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
+        int c = idx / R_, r = idx - c * R_;
+        R s = 0;
+        for (int k = 0; k < N; k++) s = fma(Ss[k * kRows + r], Ts[k * N + c], s);
+        Sa[r0 + r + (int64_t)c * ldS] = (double)s;
+      }
+    }
+  }
+}
+
+template <typename R>
+__global__ void k_write_amplitudes(int N, int32_t z0, int32_t nzc, const R* __restrict__ za,
+                                   const int32_t* __restrict__ nobs, int all_zones,
+                                   double* __restrict__ out) {
+  const int64_t total = (int64_t)nzc * N;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int32_t zl = (int32_t)(idx / N);
+    double v = (all_zones && nobs[zl] > 0) ? (double)za[idx] : 0.0;
+    out[(int64_t)z0 * N + idx] = v;
+  }
+}
+
+}  // namespace
+
+template <typename R>
+cudaError_t zone_update_impl(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const double* xf, const double* Sf,
+                             int64_t ldS, const R* d_T, const R* d_ampl,
+                             const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
+  size_t smem = (size_t)(N * N + N * kRows + N) * sizeof(R);
+  cudaError_t e = cudaFuncSetAttribute(k_zone_update<R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int tiles = (zone_max + kRows - 1) / kRows;
+  if (tiles < 1) tiles = 1;
+  int64_t ntasks = (int64_t)nzc * tiles;
+  int grid = (int)(ntasks < 152 * 16 ? (ntasks < 1 ? 1 : ntasks) : 152 * 16);
+  k_zone_update<R><<<grid, kThreads, smem, st>>>(N, z0, nzc, d_zone_start, tiles, xf, Sf, ldS,
+                                                 d_T, d_ampl, d_nobs, xa, Sa);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t write_amplitudes_impl(int N, int32_t z0, int32_t nzc, const R* d_ampl,
+                                  const int32_t* d_nobs, int all_zones, double* ampl_out,
+                                  cudaStream_t st) {
+  int64_t total = (int64_t)nzc * N;
+  int grid = (int)((total + 255) / 256 < 152 * 8 ? (total + 255) / 256 : 152 * 8);
+  if (grid < 1) grid = 1;
+  k_write_amplitudes<R><<<grid, 256, 0, st>>>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const double* xf, const double* Sf,
+                             int64_t ldS, const double* d_T, const double* d_ampl,
+                             const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
+  return zone_update_impl<double>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T, d_ampl,
+                                  d_nobs, xa, Sa, st);
+}
+
+cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const double* xf, const double* Sf,
+                             int64_t ldS, const float* d_T, const float* d_ampl,
+                             const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
+  return zone_update_impl<float>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T, d_ampl,
+                                 d_nobs, xa, Sa, st);
+}
+
+cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_ampl,
+                             const int32_t* d_nobs, int all_zones, double* ampl_out,
+                             cudaStream_t st) {
+  return write_amplitudes_impl<double>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out, st);
+}
+
+cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d_ampl,
+                                  const int32_t* d_nobs, int all_zones, double* ampl_out,
+                                  cudaStream_t st) {
+  return write_amplitudes_impl<float>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out, st);
+}
+
+}  // namespace oakg

@@ -1,0 +1,71 @@
+"""Mixed-precision form (OAKG_PREC_MIXED) against the FP64 oracle.
+
+Tolerance: 1e-4 relative analysis error (the spec bar): increment-relative for the mean,
+Frobenius-relative for the anomalies. The observation selection is FP64 in both forms, so the
+relevant-observation counts must be identical.
+"""
+import numpy as np
+import pytest
+
+from oak_gb300.workloads import local_case
+from oracle import cref
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def _errs(xa, Sa, xa_o, Sa_o, xf):
+    return (np.linalg.norm(xa - xa_o) / np.linalg.norm(xa_o - xf),
+            np.linalg.norm(Sa - Sa_o) / np.linalg.norm(Sa_o))
+
+
+@pytest.mark.parametrize("N,scale", [(64, 1 / 6), (32, 1 / 8), (100, 1 / 10)])
+def test_mixed_local_matches_fp64_oracle(oakg, N, scale):
+    c = local_case(scale=scale, N=N)
+    xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        weight=c.weight, precision=oakg.PREC_MIXED)
+    xa_o, Sa_o, _, nobs_o = cref.locanalysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                             c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                             c.max_len, kind=c.weight)
+    assert np.array_equal(nobs, nobs_o)
+    e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
+    assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)
+
+
+def test_mixed_gaussian_weights_and_amplitudes(oakg):
+    c = local_case(scale=1 / 8, N=48)
+    kw = dict(weight=oakg.GAUSS_CUTOFF, ampl_always=True)
+    xa, Sa, ampl, _ = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        precision=oakg.PREC_MIXED, **kw)
+    xa6, Sa6, ampl6, _ = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                           c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                           c.max_len, **kw)
+    e_mean, e_anom = _errs(xa, Sa, xa6, Sa6, c.xf)
+    assert e_mean < TOL and e_anom < TOL
+    assert np.linalg.norm(ampl - ampl6) / np.linalg.norm(ampl6) < TOL
+
+
+def test_mixed_empty_zones_copy_forecast(oakg):
+    c = local_case(scale=1 / 8, N=16, m=400)
+    xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        weight=c.weight, precision=oakg.PREC_MIXED)
+    empty = np.repeat(nobs == 0, c.zone_size)
+    assert empty.any()
+    assert np.array_equal(xa[empty], c.xf[empty]) and np.array_equal(Sa[empty], c.Sf[empty])
+
+
+def test_mixed_rank_deficient_zones(oakg):
+    c = local_case(scale=1 / 8, N=64, m=2000)
+    xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        weight=c.weight, precision=oakg.PREC_MIXED)
+    xa_o, Sa_o, _, _ = cref.locanalysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        kind=c.weight)
+    assert (nobs[nobs > 0] < 64).any()
+    e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
+    assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)

@@ -273,3 +273,14 @@ def test_zero_weight_zone_keeps_forecast(oakg):
                                         P["r"], P["zone_pos"], P["obs_pos"], corr, maxl, kind=0)
     assert np.allclose(xa, P["xf"], atol=1e-14) and np.allclose(Sa, P["Sf"], atol=1e-14)
     assert np.allclose(xa_o, P["xf"], atol=1e-14) and np.allclose(Sa_o, P["Sf"], atol=1e-14)
+
+
+@pytest.mark.parametrize("N", [16, 64])
+def test_rank_deficient_zones(oakg, N):
+    """Few observations per zone (p < N): G has a large cluster of zero eigenvalues, which the
+    eigensolver must still turn into an orthonormal basis (complement fill)."""
+    P = _random_local(31 + N, N=N, nzones=60, m=12, dom=20.0, radius=10.0)
+    (xa, Sa, _, nobs), (xa_o, Sa_o, nobs_o) = _run_both(oakg, P)
+    assert np.array_equal(nobs, nobs_o)
+    assert nobs.max() < N
+    check_local(xa, Sa, xa_o, Sa_o, P["xf"])
