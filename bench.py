@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true")
     return p.parse_args()
 
 
@@ -285,6 +286,43 @@ def main():
                  "stage_ms_per_step": {k: v / args.steps for k, v in mstage.items()}}
         del ref_xa, ref_Sa, mout
 
+    # adjoint cost: J = mean over a 60 x 40 column sub-region (all levels) of (xa - x_true)^2,
+    # gradients w.r.t. yo, r, the localisation length factor and the prior inflation (1.05)
+    adjoint = None
+    if not args.no_adjoint:
+        nx = int(round(360 * args.scale))
+        zc = np.arange(c.Z)
+        subz = ((zc % nx) >= nx // 3) & ((zc % nx) < nx // 3 + max(1, round(60 * args.scale))) & \
+               ((zc // nx) >= 60 * args.scale) & ((zc // nx) < 60 * args.scale + max(1, round(40 * args.scale)))
+        sub = np.repeat(subz, c.zone_size)
+        xt_d = T(c.x_true)
+        sub_d = T(sub.astype(np.float64))
+        xa_fwd = step()[0]
+        seed = 2.0 * (xa_fwd - xt_d) * sub_d / float(sub.sum())
+        a_args = (d_args[0], d_args[2], d_args[3], d_args[4], d_args[5], d_args[6], d_args[7],
+                  d_args[8], d_args[9], d_args[10])
+
+        def astep():
+            return oak_gb300.loc_analysis_adjoint(*a_args, seed, inflation=1.05, weight=c.weight,
+                                                  metric=c.metric, loctype=c.loctype)
+        for _ in range(args.warmup):
+            astep()
+        torch.cuda.synchronize(dev)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(args.steps):
+            ga = astep()
+        a1.record(stream)
+        torch.cuda.synchronize(dev)
+        ams = a0.elapsed_time(a1) / args.steps
+        adjoint = {"ms_per_call": ams, "cost_vs_forward_fp64": ams / ms,
+                   "cost_vs_forward_mixed": (ams / mixed["ms_per_step"]) if mixed else None,
+                   "cost": "J = mean over a 60x40 column sub-region (all levels) of "
+                           "(xa - x_true)^2; gradients w.r.t. all yo, r, the localisation "
+                           "length factor and the prior inflation 1.05",
+                   "zones_seeded": int(subz.sum()), "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
+
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
     if not args.no_e2e:
@@ -343,6 +381,7 @@ def main():
                                                      "zones_with_obs": int((nobs > 0).sum())},
         "e2e": e2e,
         "mixed": mixed,
+        "adjoint": adjoint,
         "gpu_launches": int(launches),
         "stage_ms_per_step": per_step,
         "roofline": {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,

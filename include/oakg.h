@@ -128,6 +128,26 @@ int oakg_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
                      const double* corr_len, const double* max_len, double* xa, double* Sa,
                      double* ampl, int32_t* nobs);
 
+/* Adjoint of the local analysis mean -- no counterpart in the reference (it has no derivative
+ * code). For a scalar cost J(xa) given by its gradient dJ_dxa(n) at the analysis of
+ * oakg_locanalysis with the same inputs, where the prior anomalies are inflated by
+ * `inflation` (Sf and HSf multiplied by it, the ErrorSpace.scale of assimilation.F90:1201):
+ *   dJ_dyo(m), dJ_dr(m)   gradients w.r.t. the observations and their error variances
+ *                          (original order; memory kind per dims->mem; may be NULL)
+ *   *dJ_dlen              derivative w.r.t. a common factor on corr_len and max_len, at 1
+ *                          (host pointer; the set of selected observations is held fixed,
+ *                          exact for Gaspari-Cohn weights which vanish at the cut-off)
+ *   *dJ_dinfl             derivative w.r.t. `inflation` (host pointer)
+ * Only zones where dJ_dxa is non-zero are recomputed (Cholesky of I + G per zone, no stored
+ * eigensystem). FP64. Sf and HSf are the anomalies before inflation. */
+int oakg_locanalysis_adjoint(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                             const int32_t* zone_size, const double* Hxf, const double* yo,
+                             const double* Sf, const double* HSf, const double* r_diag,
+                             const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                             const double* obs_z, const double* obs_t, const double* corr_len,
+                             const double* max_len, double inflation, const double* dJ_dxa,
+                             double* dJ_dyo, double* dJ_dr, double* dJ_dlen, double* dJ_dinfl);
+
 /* oakg_analysis for callers that cannot allocate device memory -- no counterpart in the
  * reference. Host programs that reserve all GPU memory for their own pool before loading this
  * library (model couplers often do), or that must not call cudaMalloc/cudaFree inside a

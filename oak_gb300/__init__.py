@@ -24,7 +24,7 @@ import os
 
 import numpy as np
 
-__all__ = ["analysis", "loc_analysis", "OakError", "lib", "last_timings", "release",
+__all__ = ["analysis", "loc_analysis", "loc_analysis_adjoint", "OakError", "lib", "last_timings", "release",
            "PREC_FP64", "PREC_MIXED",
            "GAUSS_CUTOFF", "GASPARI_COHN", "CARTESIAN", "SPHERICAL", "SPHERICAL_APPROX",
            "zone_positions"]
@@ -93,6 +93,11 @@ def lib() -> ctypes.CDLL:
     L.oakg_launch_count.restype = ctypes.c_int64
     L.oakg_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
     L.oakg_fp64_peak.restype = ctypes.c_int
+    L.oakg_locanalysis_adjoint.argtypes = ([ctypes.POINTER(Dims), ctypes.POINTER(Loc), ctypes.c_int32]
+                                           + [P] * 13 + [ctypes.c_double, P, P, P,
+                                                          ctypes.POINTER(ctypes.c_double),
+                                                          ctypes.POINTER(ctypes.c_double)])
+    L.oakg_locanalysis_adjoint.restype = ctypes.c_int
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -304,3 +309,49 @@ def zone_positions(zone_size, x, y=None, z=None, t=None):
         if c is not None:
             out[:, k] = np.asarray(c, dtype=np.float64)[first]
     return out
+
+
+def loc_analysis_adjoint(zone_size, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, corr_len,
+                         max_len, dJ_dxa, *, inflation=1.0, weight=GAUSS_CUTOFF,
+                         metric=CARTESIAN, loctype=1, localise_obs=True, brute_search=False,
+                         cell_size=0.0):
+    """Gradients of a scalar cost J(xa) of the local analysis mean (oakg_locanalysis_adjoint).
+
+    ``dJ_dxa`` is dJ/dxa (n,). The analysis is the one of :func:`loc_analysis` with the prior
+    anomalies ``inflation * Sf`` and ``inflation * HSf``. Returns ``(dJ_dyo (m,), dJ_dr (m,),
+    dJ_dlen, dJ_dinfl)``; ``dJ_dlen`` is the derivative w.r.t. a common factor on
+    ``corr_len`` and ``max_len`` at 1, with the selected observations held fixed.
+    """
+    Z = int(zone_size.shape[0])
+    n = int(dJ_dxa.shape[0])
+    m = int(yo.shape[0])
+    N = int(Sf.shape[1])
+    ox, oy, oz, ot = (tuple(obs_pos) + (None,) * 4)[:4]
+    device = _device_mode(zone_size, Hxf, yo, Sf, HSf, r_diag, zone_pos, corr_len, max_len,
+                          dJ_dxa, ox, oy, oz, ot)
+    A = _Args(device)
+    pSf, ldS = A.mat(Sf, n, N, "Sf")
+    pHS, ldH = A.mat(HSf, m, N, "HSf")
+    dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
+    loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
+              rotate=1, precision=PREC_FP64, flags=FLAG_BRUTE_SEARCH if brute_search else 0,
+              cell_size=float(cell_size))
+    zp = zone_pos.reshape(-1) if device else np.ascontiguousarray(
+        np.asarray(zone_pos, dtype=np.float64).reshape(Z, 4))
+    like = Sf
+    dyo = _empty_like_mode(device, (m,), like=like)
+    dr = _empty_like_mode(device, (m,), like=like)
+    dlen = ctypes.c_double(0.0)
+    dinfl = ctypes.c_double(0.0)
+    _sync_torch(device, like)
+    rc = lib().oakg_locanalysis_adjoint(
+        ctypes.byref(dims), ctypes.byref(loc), Z, A.vec(zone_size, np.int32, "zone_size", Z),
+        A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"), pSf, pHS,
+        A.vec(r_diag, n=m, name="r_diag"), A.vec(zp, n=4 * Z, name="zone_pos"),
+        A.vec(ox, n=m, name="obs_x"), A.vec(oy, n=m, name="obs_y"), A.vec(oz, n=m, name="obs_z"),
+        A.vec(ot, n=m, name="obs_t"), A.vec(corr_len, n=Z, name="corr_len"),
+        A.vec(max_len, n=Z, name="max_len"), float(inflation), A.vec(dJ_dxa, n=n, name="dJ_dxa"),
+        A.vec(dyo, name="dJ_dyo"), A.vec(dr, name="dJ_dr"), ctypes.byref(dlen),
+        ctypes.byref(dinfl))
+    _check(rc)
+    return dyo, dr, dlen.value, dinfl.value

@@ -295,14 +295,19 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   return OAKG_OK;
 }
 
-// ------------------------------------------------------------------------------------------
-int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
-                     const int32_t* zone_size, const double* xf, const double* Hxf,
-                     const double* yo, const double* Sf, const double* HSf,
-                     const double* r_diag, const double* zone_xyzt, const double* obs_x,
-                     const double* obs_y, const double* obs_z, const double* obs_t,
-                     const double* corr_len, const double* max_len, double* xa, double* Sa,
-                     double* ampl, int32_t* nobs_out) {
+// Inputs of a local analysis on the device: staged arrays, zone offsets, the observation
+// cell grid and the cell-sorted observations.
+struct Prep {
+  const int32_t* zsize;
+  const double *xf, *Hxf, *yo, *r, *Sf, *HSf, *zxyzt, *u, *v, *corr, *maxl;
+  int64_t* zstart;
+  int32_t zone_max;
+  int brute;
+  CellGrid g;
+  SortedObs so;
+};
+
+int check_loc(const oakg_dims* dims, const oakg_loc* loc, int32_t Z) {
   int rc = check_dims(dims);
   if (rc) return rc;
   if (!loc) return fail(OAKG_ERR_ARGS, "loc is NULL");
@@ -316,11 +321,20 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     return fail(OAKG_ERR_ARGS, "loctype must be 1, 2 or 3 (got %d)", loc->loctype);
   if (loc->precision != OAKG_PREC_FP64 && loc->precision != OAKG_PREC_MIXED)
     return fail(OAKG_ERR_ARGS, "unknown precision mode %d", loc->precision);
+  return OAKG_OK;
+}
+
+int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
+                const int32_t* zone_size, const double* xf, const double* Hxf,
+                const double* yo, const double* Sf, const double* HSf, const double* r_diag,
+                const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                const double* obs_z, const double* obs_t, const double* corr_len,
+                const double* max_len, Prep* P) {
   const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
   const int N = dims->N, mem = dims->mem;
-  if (!zone_size || !xf || !xa || !zone_xyzt || !corr_len || !max_len)
-    return fail(OAKG_ERR_ARGS, "zone_size, xf, zone_xyzt, corr_len, max_len and xa are required");
-  if (!Sf) return fail(OAKG_ERR_ARGS, "Sf is required");
+  int rc;
+  if (!zone_size || !zone_xyzt || !corr_len || !max_len || !Sf)
+    return fail(OAKG_ERR_ARGS, "zone_size, zone_xyzt, corr_len, max_len and Sf are required");
   if (m > 0 && (!Hxf || !yo || !HSf || !r_diag))
     return fail(OAKG_ERR_ARGS, "Hxf, yo, HSf and r_diag are required when m > 0");
   const double* u_src_h = (loc->loctype == 1) ? obs_x : (loc->loctype == 2 ? obs_z : obs_t);
@@ -328,61 +342,35 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   if (m > 0 && (!u_src_h || (loc->loctype == 1 && !v_src_h)))
     return fail(OAKG_ERR_ARGS, "observation coordinates required by loctype %d are NULL",
                 loc->loctype);
-
-  Ctx* c = nullptr;
-  if ((rc = get_ctx(&c))) return rc;
   cudaStream_t st = c->stream;
   cudaError_t e;
-  cudaEventRecord(c->ev[0], st);
-
-  const int32_t* d_zsize;
-  const double *d_xf, *d_Hxf = nullptr, *d_yo = nullptr, *d_r = nullptr, *d_Sf,
-                      *d_HSf = nullptr, *d_zxyzt, *d_u = nullptr, *d_v = nullptr, *d_corr,
-                      *d_maxl;
-  if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &d_zsize, "zone_size"))) return rc;
-  if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &d_xf, "xf"))) return rc;
-  if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &d_Sf, "Sf"))) return rc;
-  if ((rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &d_zxyzt, "zone_xyzt"))) return rc;
-  if ((rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &d_corr, "corr_len"))) return rc;
-  if ((rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &d_maxl, "max_len"))) return rc;
+  *P = Prep{};
+  if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &P->zsize, "zone_size"))) return rc;
+  if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &P->xf, "xf"))) return rc;
+  if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &P->Sf, "Sf"))) return rc;
+  if ((rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &P->zxyzt, "zone_xyzt"))) return rc;
+  if ((rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &P->corr, "corr_len"))) return rc;
+  if ((rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &P->maxl, "max_len"))) return rc;
   if (m > 0) {
-    if ((rc = stage_in(c, B_HXF, Hxf, (size_t)m, mem, &d_Hxf, "Hxf"))) return rc;
-    if ((rc = stage_in(c, B_YO, yo, (size_t)m, mem, &d_yo, "yo"))) return rc;
-    if ((rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &d_r, "r_diag"))) return rc;
-    if ((rc = stage_in(c, B_HSF, HSf, (size_t)ldH * N, mem, &d_HSf, "HSf"))) return rc;
-    if ((rc = stage_in(c, B_OX, u_src_h, (size_t)m, mem, &d_u, "obs coordinate u"))) return rc;
-    if (v_src_h && (rc = stage_in(c, B_OY, v_src_h, (size_t)m, mem, &d_v, "obs coordinate v")))
+    if ((rc = stage_in(c, B_HXF, Hxf, (size_t)m, mem, &P->Hxf, "Hxf"))) return rc;
+    if ((rc = stage_in(c, B_YO, yo, (size_t)m, mem, &P->yo, "yo"))) return rc;
+    if ((rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &P->r, "r_diag"))) return rc;
+    if ((rc = stage_in(c, B_HSF, HSf, (size_t)ldH * N, mem, &P->HSf, "HSf"))) return rc;
+    if ((rc = stage_in(c, B_OX, u_src_h, (size_t)m, mem, &P->u, "obs coordinate u"))) return rc;
+    if (v_src_h && (rc = stage_in(c, B_OY, v_src_h, (size_t)m, mem, &P->v, "obs coordinate v")))
       return rc;
   }
-  double *d_xa, *d_Sa, *d_ampl;
-  int32_t* d_nobs;
-  if ((rc = stage_out(c, B_XA, xa, (size_t)n, mem, &d_xa, "xa"))) return rc;
-  if ((rc = stage_out(c, B_SA, Sa, (size_t)ldS * N, mem, &d_Sa, "Sa"))) return rc;
-  if ((rc = stage_out(c, B_AMPL, ampl, (size_t)N * Z, mem, &d_ampl, "amplitudes"))) return rc;
-  if (mem == OAKG_MEM_DEVICE && nobs_out) {
-    d_nobs = nobs_out;
-  } else if ((rc = scratch(c, B_NOBS, (size_t)Z, &d_nobs, "nobs"))) {
-    return rc;
-  }
-  if (mem == OAKG_MEM_HOST && Sa) {
-    // rows beyond n (ldS > n) are returned unchanged
-    e = cudaMemcpyAsync(d_Sa, d_Sf, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToDevice,
-                        st);
-    if (e != cudaSuccess) return cuda_fail(e, "Sa init");
-  }
-
   // zone offsets and sizes
-  int64_t* d_zstart;
   double* d_small;
-  if ((rc = scratch(c, B_ZSTART, (size_t)Z + 1, &d_zstart, "zone offsets"))) return rc;
+  if ((rc = scratch(c, B_ZSTART, (size_t)Z + 1, &P->zstart, "zone offsets"))) return rc;
   if ((rc = scratch(c, B_SMALL, 16, &d_small, "small"))) return rc;
   int32_t* d_zmax = reinterpret_cast<int32_t*>(d_small + 8);
-  if ((e = zone_offsets(d_zsize, Z, d_zstart, d_zmax, st)) != cudaSuccess)
+  if ((e = zone_offsets(P->zsize, Z, P->zstart, d_zmax, st)) != cudaSuccess)
     return cuda_fail(e, "zone offsets");
-  int brute = (loc->flags & OAKG_FLAG_BRUTE_SEARCH) || !loc->localise_obs;
+  P->brute = (loc->flags & OAKG_FLAG_BRUTE_SEARCH) || !loc->localise_obs;
   if (m > 0) {
-    if ((e = obs_bounds(d_u, d_v, m, d_small, st)) != cudaSuccess) return cuda_fail(e, "bounds");
-    if ((e = obs_bounds(d_maxl, nullptr, Z, d_small + 4, st)) != cudaSuccess)
+    if ((e = obs_bounds(P->u, P->v, m, d_small, st)) != cudaSuccess) return cuda_fail(e, "bounds");
+    if ((e = obs_bounds(P->maxl, nullptr, Z, d_small + 4, st)) != cudaSuccess)
       return cuda_fail(e, "bounds");
   }
   double hsmall[9] = {0};
@@ -390,22 +378,21 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   if ((e = cudaMemcpyAsync(hsmall, d_small, 9 * sizeof(double), cudaMemcpyDeviceToHost, st)) !=
       cudaSuccess)
     return cuda_fail(e, "D2H");
-  if ((e = cudaMemcpyAsync(&htotal, d_zstart + Z, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) !=
+  if ((e = cudaMemcpyAsync(&htotal, P->zstart + Z, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) !=
       cudaSuccess)
     return cuda_fail(e, "D2H");
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "synchronize");
-  int32_t zone_max = 0;
-  std::memcpy(&zone_max, &hsmall[8], sizeof(int32_t));
+  std::memcpy(&P->zone_max, &hsmall[8], sizeof(int32_t));
   if (htotal != n)
     return fail(OAKG_ERR_ARGS, "sum(zone_size) = %lld differs from n = %lld", (long long)htotal,
                 (long long)n);
-
   // cell grid over the observation coordinates
-  CellGrid g{};
+  CellGrid& g = P->g;
+  g = CellGrid{};
   g.nu = g.nv = 1;
   g.csu = g.csv = 1.0;
   const int spherical = (loc->loctype == 1 && loc->metric != OAKG_METRIC_CARTESIAN);
-  if (m > 0 && !brute) {
+  if (m > 0 && !P->brute) {
     double umin = hsmall[0], umax = hsmall[1], vmin = hsmall[2], vmax = hsmall[3];
     double Rmax = hsmall[5];
     if (!(std::isfinite(umin) && std::isfinite(umax) && std::isfinite(vmin) && std::isfinite(vmax)))
@@ -436,8 +423,8 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     }
   }
   const int64_t ncells = (int64_t)g.nu * g.nv;
-
-  SortedObs so{};
+  SortedObs& so = P->so;
+  so = SortedObs{};
   if (m > 0) {
     int32_t *d_cell, *d_count, *d_cstart, *d_pos, *d_perm;
     double *d_su, *d_sv, *d_sinnov, *d_sr, *d_hst;
@@ -451,7 +438,7 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     if ((rc = scratch(c, B_SINNOV, (size_t)m, &d_sinnov, "obs"))) return rc;
     if ((rc = scratch(c, B_SR, (size_t)m, &d_sr, "obs"))) return rc;
     if ((rc = scratch(c, B_HST, (size_t)m * N, &d_hst, "obs rows"))) return rc;
-    e = obs_bin_and_sort(g, m, N, d_u, d_v, d_yo, d_Hxf, d_r, d_HSf, ldH, d_cell, d_count,
+    e = obs_bin_and_sort(g, m, N, P->u, P->v, P->yo, P->Hxf, P->r, P->HSf, ldH, d_cell, d_count,
                          d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr, d_hst, st);
     if (e != cudaSuccess) return cuda_fail(e, "observation binning");
     so.u = d_su;
@@ -467,6 +454,47 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     cudaMemsetAsync(d_cstart, 0, 2 * sizeof(int32_t), st);
     so.cell_start = d_cstart;
   }
+  return OAKG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
+                     const int32_t* zone_size, const double* xf, const double* Hxf,
+                     const double* yo, const double* Sf, const double* HSf,
+                     const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                     const double* obs_y, const double* obs_z, const double* obs_t,
+                     const double* corr_len, const double* max_len, double* xa, double* Sa,
+                     double* ampl, int32_t* nobs_out) {
+  int rc = check_loc(dims, loc, Z);
+  if (rc) return rc;
+  if (!xf || !xa) return fail(OAKG_ERR_ARGS, "xf and xa are required");
+  const int64_t n = dims->n, ldS = dims->ldS;
+  const int N = dims->N, mem = dims->mem;
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  cudaEventRecord(c->ev[0], st);
+  Prep P;
+  if ((rc = prepare_loc(c, dims, loc, Z, zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
+                        obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &P)))
+    return rc;
+  double *d_xa, *d_Sa, *d_ampl;
+  int32_t* d_nobs;
+  if ((rc = stage_out(c, B_XA, xa, (size_t)n, mem, &d_xa, "xa"))) return rc;
+  if ((rc = stage_out(c, B_SA, Sa, (size_t)ldS * N, mem, &d_Sa, "Sa"))) return rc;
+  if ((rc = stage_out(c, B_AMPL, ampl, (size_t)N * Z, mem, &d_ampl, "amplitudes"))) return rc;
+  if (mem == OAKG_MEM_DEVICE && nobs_out) {
+    d_nobs = nobs_out;
+  } else if ((rc = scratch(c, B_NOBS, (size_t)Z, &d_nobs, "nobs"))) {
+    return rc;
+  }
+  if (mem == OAKG_MEM_HOST && Sa) {
+    // rows beyond n (ldS > n) are returned unchanged
+    e = cudaMemcpyAsync(d_Sa, P.Sf, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                        st);
+    if (e != cudaSuccess) return cuda_fail(e, "Sa init");
+  }
   cudaEventRecord(c->ev[1], st);
 
   // zone chunks: selection + Gram, eigensolve + transform, update
@@ -474,8 +502,8 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
                loc->rotate ? 1 : 0, loc->flags};
   const int all_ampl = (!loc->localise_obs) || (loc->flags & OAKG_FLAG_AMPL_ALWAYS);
   int32_t* d_status_all = nullptr;
-  ChunkArgs ca{g, so, lp, Z, N, ldS, zone_max, brute, all_ampl, d_zxyzt, d_corr, d_maxl,
-               d_zstart, d_xf, d_Sf, d_xa, d_Sa, d_ampl, d_nobs};
+  ChunkArgs ca{P.g, P.so, lp, Z, N, ldS, P.zone_max, P.brute, all_ampl, P.zxyzt, P.corr, P.maxl,
+               P.zstart, P.xf, P.Sf, d_xa, d_Sa, d_ampl, d_nobs};
   double t_gram = 0, t_eig = 0, t_upd = 0;
   rc = (loc->precision == OAKG_PREC_MIXED)
            ? run_chunks<float>(c, ca, &d_status_all, &t_gram, &t_eig, &t_upd)
@@ -506,6 +534,103 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   c->timings[3] = t_upd;
   c->timings[4] = elapsed(c->ev[0], c->ev[6]);
   return status_code(hstatus);
+}
+
+// Adjoint of the local analysis mean (zone_adjoint.cu): gradients of J(xa) given dJ/dxa.
+int adjoint_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z, const int32_t* zone_size,
+                 const double* Hxf, const double* yo, const double* Sf, const double* HSf,
+                 const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                 const double* obs_y, const double* obs_z, const double* obs_t,
+                 const double* corr_len, const double* max_len, double inflation,
+                 const double* dJ_dxa, double* dJ_dyo, double* dJ_dr, double* dJ_dlen,
+                 double* dJ_dinfl) {
+  int rc = check_loc(dims, loc, Z);
+  if (rc) return rc;
+  if (!dJ_dxa) return fail(OAKG_ERR_ARGS, "dJ_dxa is required");
+  if (!(inflation > 0.0)) return fail(OAKG_ERR_ARGS, "inflation must be positive");
+  const int64_t n = dims->n, m = dims->m, ldS = dims->ldS;
+  const int N = dims->N, mem = dims->mem;
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  cudaEventRecord(c->ev[0], st);
+  Prep P;
+  if ((rc = prepare_loc(c, dims, loc, Z, zone_size, nullptr, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
+                        obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &P)))
+    return rc;
+  const double* d_seed;
+  if ((rc = stage_in(c, B_XA, dJ_dxa, (size_t)n, mem, &d_seed, "dJ_dxa"))) return rc;
+  double *d_dyo, *d_dr, *d_scal;
+  const size_t mm = (size_t)(m > 0 ? m : 1);
+  if ((rc = stage_out(c, B_AMPL, dJ_dyo, mm, OAKG_MEM_HOST, &d_dyo, "dJ_dyo"))) return rc;
+  if (mem == OAKG_MEM_DEVICE && dJ_dyo) d_dyo = dJ_dyo;
+  double* d_dr_buf;
+  if ((rc = scratch(c, B_SA, mm + 8, &d_dr_buf, "dJ_dr"))) return rc;
+  d_dr = (mem == OAKG_MEM_DEVICE && dJ_dr) ? dJ_dr : d_dr_buf;
+  d_scal = d_dr_buf + mm;
+  if (!d_dyo) {
+    if ((rc = scratch(c, B_AMPL, mm, &d_dyo, "dJ_dyo"))) return rc;
+  }
+  cudaMemsetAsync(d_dyo, 0, mm * sizeof(double), st);
+  cudaMemsetAsync(d_dr, 0, mm * sizeof(double), st);
+  cudaMemsetAsync(d_scal, 0, 2 * sizeof(double), st);
+  // seeded zones
+  int32_t *d_flag, *d_pos, *d_list, *d_nobs, *d_work;
+  if ((rc = scratch(c, B_CELL, (size_t)Z + 1, &d_flag, "zone flags"))) return rc;
+  if ((rc = scratch(c, B_STATUS, (size_t)Z + 1, &d_pos, "zone positions"))) return rc;
+  if ((rc = scratch(c, B_POS, (size_t)Z + 1, &d_list, "zone list"))) return rc;
+  if ((rc = scratch(c, B_NOBS, (size_t)Z, &d_nobs, "nobs"))) return rc;
+  if ((rc = scratch(c, B_WORK, 8, &d_work, "work counters"))) return rc;
+  // the obs-prep buffers B_CELL/B_POS are free once binning is done (binning ran above)
+  if ((e = zone_active_list(d_seed, P.zstart, Z, d_flag, d_pos, d_list, st)) != cudaSuccess)
+    return cuda_fail(e, "seeded zones");
+  int32_t nact = 0;
+  if ((e = cudaMemcpyAsync(&nact, d_pos + Z, sizeof(int32_t), cudaMemcpyDeviceToHost, st)))
+    return cuda_fail(e, "D2H");
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "synchronize");
+  LocParams lp{loc->weight, loc->metric, loc->loctype, loc->localise_obs ? 1 : 0,
+               loc->rotate ? 1 : 0, loc->flags};
+  const size_t per_zone = (size_t)N * N * 8 + (size_t)N * 8;
+  int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
+  if (chunk < 1) chunk = 1;
+  if (chunk > nact) chunk = nact;
+  double *d_G, *d_gv;
+  if (nact > 0) {
+    if ((rc = scratch(c, B_G, (size_t)chunk * N * N, &d_G, "zone matrices"))) return rc;
+    if ((rc = scratch(c, B_GV, (size_t)chunk * N, &d_gv, "zone vectors"))) return rc;
+  }
+  cudaEventRecord(c->ev[1], st);
+  for (int64_t k0 = 0; k0 < nact; k0 += chunk) {
+    const int32_t nk = (int32_t)std::min<int64_t>(chunk, nact - k0);
+    e = zone_gram_fp64_list(P.g, P.so, N, lp, d_list + k0, nk, P.zxyzt, P.corr, P.maxl, d_G, d_gv,
+                            d_nobs, P.brute, d_work, st);
+    if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
+    e = zone_adjoint_fp64(P.g, P.so, N, lp, d_list + k0, nk, P.zxyzt, P.corr, P.maxl, P.zstart,
+                          P.Sf, ldS, d_seed, inflation, d_G, d_gv, d_nobs, d_dyo, d_dr, d_scal,
+                          P.brute, d_work + 1, st);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel");
+  }
+  cudaEventRecord(c->ev[6], st);
+  double hs[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(hs, d_scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, st)))
+    return cuda_fail(e, "D2H");
+  if (mem == OAKG_MEM_HOST && m > 0) {
+    if (dJ_dyo && (e = cudaMemcpyAsync(dJ_dyo, d_dyo, m * sizeof(double), cudaMemcpyDeviceToHost,
+                                       st)))
+      return cuda_fail(e, "D2H dJ_dyo");
+    if (dJ_dr &&
+        (e = cudaMemcpyAsync(dJ_dr, d_dr, m * sizeof(double), cudaMemcpyDeviceToHost, st)))
+      return cuda_fail(e, "D2H dJ_dr");
+  }
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "synchronize");
+  if (dJ_dlen) *dJ_dlen = hs[0];
+  if (dJ_dinfl) *dJ_dinfl = hs[1];
+  c->timings[0] = elapsed(c->ev[0], c->ev[1]);
+  c->timings[1] = elapsed(c->ev[1], c->ev[6]);
+  c->timings[2] = c->timings[3] = 0.0;
+  c->timings[4] = elapsed(c->ev[0], c->ev[6]);
+  return OAKG_OK;
 }
 
 int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
@@ -666,6 +791,22 @@ int oakg_analysis(const oakg_dims* dims, const double* xf, const double* Hxf, co
   std::lock_guard<std::mutex> lk(oakg::api_mutex());
   oakg::set_ok();
   int rc = oakg::analysis_impl(dims, xf, Hxf, yo, Sf, HSf, r_diag, xa, Sa, ampl);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_locanalysis_adjoint(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                             const int32_t* zone_size, const double* Hxf, const double* yo,
+                             const double* Sf, const double* HSf, const double* r_diag,
+                             const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                             const double* obs_z, const double* obs_t, const double* corr_len,
+                             const double* max_len, double inflation, const double* dJ_dxa,
+                             double* dJ_dyo, double* dJ_dr, double* dJ_dlen, double* dJ_dinfl) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::adjoint_impl(dims, loc, nzones, zone_size, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
+                              obs_x, obs_y, obs_z, obs_t, corr_len, max_len, inflation, dJ_dxa,
+                              dJ_dyo, dJ_dr, dJ_dlen, dJ_dinfl);
   oakg::last_status() = rc;
   return rc;
 }

@@ -67,6 +67,23 @@ cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocPar
                            const double* corr_len, const double* max_len, float* d_G,
                            float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
                            cudaStream_t st);
+// Same as zone_gram_fp64 for the zones listed in zlist[0..nzc) (G, g slots in list order).
+cudaError_t zone_gram_fp64_list(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                                const int32_t* zlist, int32_t nzc, const double* zone_xyzt,
+                                const double* corr_len, const double* max_len, double* d_G,
+                                double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                                cudaStream_t st);
+// Adjoint of the analysis mean for the zones in zlist (see zone_adjoint.cu).
+cudaError_t zone_adjoint_fp64(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                              const int32_t* zlist, int32_t nzc, const double* zone_xyzt,
+                              const double* corr_len, const double* max_len,
+                              const int64_t* zone_start, const double* Sf, int64_t ldS,
+                              const double* seed, double infl, const double* d_G,
+                              const double* d_g, const int32_t* d_nobs, double* dyo, double* dr,
+                              double* dscal, int brute, int32_t* d_work, cudaStream_t st);
+cudaError_t zone_active_list(const double* seed, const int64_t* zone_start, int32_t Z,
+                             int32_t* d_flag, int32_t* d_pos, int32_t* d_list,
+                             cudaStream_t st);
 // Global analysis Gram over all m observations (weights 1): G, g accumulated atomically.
 cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,
                              const double* yo, const double* Hxf, const double* r, double* d_G,

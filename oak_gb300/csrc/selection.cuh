@@ -1,0 +1,155 @@
+// Device-side observation selection shared by the forward (zone_gram.cu) and adjoint
+// (zone_adjoint.cu) kernels: the reference's distance() and Gaspari-Cohn locfun() with
+// explicit rounding, and the cell ranges a zone has to visit.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "oakg_internal.cuh"
+
+namespace oakg {
+namespace sel {
+
+constexpr double kPi = 3.141592653589793238462643383279502884197;
+constexpr double kEarthRadius = 6378137.0;
+
+// Gaspari-Cohn (covariance.F90:645-667), evaluated in the reference's Horner order with every
+// product and sum rounded separately (no FMA contraction). Near r = 2 the value is a
+// cancellation of order (2-r)^3, so the `w /= 0` relevance test is only reproducible when the
+// operations round exactly as a plain IEEE evaluation does.
+static __device__ __forceinline__ double locfun(double r) {
+  if (r <= 1.0) {
+    double t = __dadd_rn(__ddiv_rn(-r, 4.0), 0.5);
+    t = __dadd_rn(__dmul_rn(t, r), 5.0 / 8.0);
+    t = __dsub_rn(__dmul_rn(t, r), 5.0 / 3.0);
+    return __dadd_rn(__dmul_rn(t, __dmul_rn(r, r)), 1.0);
+  }
+  if (r <= 2.0) {
+    double t = __dsub_rn(__ddiv_rn(r, 12.0), 0.5);
+    t = __dadd_rn(__dmul_rn(t, r), 5.0 / 8.0);
+    t = __dadd_rn(__dmul_rn(t, r), 5.0 / 3.0);
+    t = __dsub_rn(__dmul_rn(t, r), 5.0);
+    t = __dadd_rn(__dmul_rn(t, r), 4.0);
+    return __dsub_rn(t, __ddiv_rn(2.0, __dmul_rn(3.0, r)));
+  }
+  return 0.0;
+}
+
+// distance(p0 = observation, p1 = zone) (assimilation.F90:3635-3672). Products and sums are
+// rounded one by one (no FMA contraction), so the Cartesian value is the correctly rounded
+// result of the reference expression and the d <= maxLength test matches a CPU evaluation.
+static __device__ __forceinline__ double distance(double x0, double y0, double x1, double y1,
+                                           int metric) {
+  if (metric == OAKG_METRIC_CARTESIAN) {
+    double dx = __dsub_rn(x1, x0), dy = __dsub_rn(y1, y0);
+    return sqrt(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  } else if (metric == OAKG_METRIC_SPHERICAL_APPROX) {
+    const double coeff = kPi * kEarthRadius / 180.0;
+    double a = __dmul_rn(__dmul_rn(coeff, cos(__dmul_rn(__dadd_rn(y0, y1), kPi / 360.0))),
+                         __dsub_rn(x1, x0));
+    double b = __dmul_rn(coeff, __dsub_rn(y1, y0));
+    return sqrt(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)));
+  } else {
+    const double d2r = kPi / 180.0;
+    double a = __dmul_rn(y0, d2r), b = __dmul_rn(y1, d2r), C = __dmul_rn(__dsub_rn(x1, x0), d2r);
+    double coeff = __dadd_rn(__dmul_rn(sin(b), sin(a)),
+                             __dmul_rn(__dmul_rn(cos(b), cos(a)), cos(C)));
+    coeff = fmax(fmin(coeff, 1.0), -1.0);
+    return __dmul_rn(kEarthRadius, acos(coeff));
+  }
+}
+
+// Cell-index ranges a zone has to visit. Rows are v cells [cv0, cv1]; in each row the u cells
+// [cu0, cu1] (unclamped for a periodic axis; iterate modulo nu). all_u: visit every u cell.
+struct ScanRange {
+  int cu0, cu1, cv0, cv1, all_u;
+};
+
+static __device__ ScanRange zone_scan_range(const CellGrid& g, int metric, int loctype, double zu,
+                                     double zv, double R) {
+  ScanRange s;
+  double du, dv;
+  int all_u = 0;
+  if (loctype != 1 || metric == OAKG_METRIC_CARTESIAN) {
+    du = R;
+    dv = (loctype == 1) ? R : 0.0;
+  } else if (metric == OAKG_METRIC_SPHERICAL_APPROX) {
+    const double coeff = kPi * kEarthRadius / 180.0;
+    dv = R / coeff;  // |dlat| bound, degrees
+    double a = (zv - 0.5 * dv) * (kPi / 180.0), b = (zv + 0.5 * dv) * (kPi / 180.0);
+    double cmin = fmin(fabs(cos(a)), fabs(cos(b)));
+    if ((zv - 0.5 * dv) <= 0.0 && (zv + 0.5 * dv) >= 0.0) cmin = fmin(cmin, 1.0);
+    if (fabs(zv) + 0.5 * dv >= 90.0 || cmin < 1e-12) {
+      all_u = 1;
+      du = 0.0;
+    } else {
+      du = R / (coeff * cmin);
+    }
+  } else {
+    double rho = R / kEarthRadius;  // angular radius, radians
+    dv = rho * (180.0 / kPi);
+    if (rho >= kPi || fabs(zv) + dv >= 90.0) {
+      all_u = 1;
+      du = 0.0;
+    } else {
+      double sl = sin(rho) / cos(zv * (kPi / 180.0));
+      du = (sl >= 1.0) ? 180.0 : asin(sl) * (180.0 / kPi);
+      if (du >= 180.0) all_u = 1;
+    }
+  }
+  // relative + absolute safety margins: candidates are a superset, the exact test decides
+  du = du * (1.0 + 1e-9) + 1e-9 * (fabs(zu) + du + g.csu);
+  dv = dv * (1.0 + 1e-9) + 1e-9 * (fabs(zv) + dv + g.csv);
+  double zuu = zu;
+  if (g.periodic_u) zuu = zu - 360.0 * floor(zu / 360.0);
+  double fu0 = floor((zuu - du - g.u0) / g.csu), fu1 = floor((zuu + du - g.u0) / g.csu);
+  if (g.periodic_u) {  // one extra cell each side absorbs rounding of the wrap-around
+    fu0 -= 1.0;
+    fu1 += 1.0;
+  }
+  double fv0 = floor((zv - dv - g.v0) / g.csv), fv1 = floor((zv + dv - g.v0) / g.csv);
+  fv0 = fmax(fv0, 0.0);
+  fv1 = fmin(fv1, (double)(g.nv - 1));
+  s.cv0 = (int)fv0;
+  s.cv1 = (int)fv1;
+  if (fv0 > fv1) {
+    s.cv0 = 0;
+    s.cv1 = -1;
+  }
+  if (g.periodic_u) {
+    if (all_u || fu1 - fu0 + 1.0 >= (double)g.nu) {
+      all_u = 1;
+    } else {
+      s.cu0 = (int)fu0;
+      s.cu1 = (int)fu1;
+    }
+  } else {
+    fu0 = fmax(fu0, 0.0);
+    fu1 = fmin(fu1, (double)(g.nu - 1));
+    s.cu0 = (int)fu0;
+    s.cu1 = (int)fu1;
+    if (fu0 > fu1) {
+      s.cv0 = 0;
+      s.cv1 = -1;
+    }
+  }
+  if (all_u) {
+    s.cu0 = 0;
+    s.cu1 = g.nu - 1;
+  }
+  s.all_u = all_u;
+  return s;
+}
+
+
+// d locfun / dr (the derivative of the Gaspari-Cohn polynomial pieces, covariance.F90:645-667).
+static __device__ __forceinline__ double locfun_deriv(double r) {
+  if (r <= 1.0) return (((-5.0 / 4.0 * r + 2.0) * r + 15.0 / 8.0) * r - 10.0 / 3.0) * r;
+  if (r <= 2.0)
+    return (((5.0 / 12.0 * r - 2.0) * r + 15.0 / 8.0) * r + 10.0 / 3.0) * r - 5.0 +
+           2.0 / (3.0 * r * r);
+  return 0.0;
+}
+
+}  // namespace sel
+}  // namespace oakg

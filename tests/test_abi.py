@@ -36,3 +36,26 @@ def test_python_binding_loads():
     import oak_gb300
     L = oak_gb300.lib()
     assert L.oakg_last_status() == 0
+
+
+def declared_arities():
+    src = open(os.path.join(ROOT, "include", "oakg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for name, params in re.findall(r"^\s*(?:int|void|size_t)\s+\**\s*(\w+)\s*\(([^)]*)\)",
+                                   src, flags=re.M):
+        p = params.strip()
+        out[name] = 0 if p in ("", "void") else p.count(",") + 1
+    return out
+
+
+def test_python_argtypes_match_header():
+    build.build()
+    import oak_gb300
+    L = oak_gb300.lib()
+    bad = {}
+    for name, k in declared_arities().items():
+        at = getattr(L, name).argtypes
+        if at is not None and len(at) != k:
+            bad[name] = (len(at), k)
+    assert not bad, f"argtypes length != header parameter count: {bad}"
