@@ -1,0 +1,51 @@
+"""Command-line runner for the synthetic local-analysis workload.
+
+  python -m oak_gb300 local [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--m M]
+
+Builds the seeded local case (360 x 180 x 20 columns scaled horizontally by S, Gaspari-Cohn
+radius 12 cells), moves it to cuda:0 and calls :func:`oak_gb300.loc_analysis` K times, printing
+the device time of each stage of the last call. Used to run one precision's kernels in
+isolation (profiling, quick timing); the full benchmark is bench.py.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(prog="python -m oak_gb300")
+    sub = p.add_subparsers(dest="cmd", required=True)
+    lp = sub.add_parser("local", help="run the local analysis workload on cuda:0")
+    lp.add_argument("--scale", type=float, default=0.5)
+    lp.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    lp.add_argument("--calls", type=int, default=2)
+    lp.add_argument("--N", type=int, default=64)
+    lp.add_argument("--m", type=int, default=50000,
+                    help="observations at scale 1 (the case scales them by S^2)")
+    a = p.parse_args(argv)
+
+    import torch
+    import oak_gb300
+    from oak_gb300.workloads import local_case
+
+    c = local_case(scale=a.scale, N=a.N, m=a.m)
+    dev = torch.device("cuda", 0)
+    T = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=dev)
+    F = lambda x: torch.as_tensor(np.ascontiguousarray(np.asarray(x).T), device=dev).t()
+    args = (T(c.zone_size), T(c.xf), T(c.Hxf), T(c.yo), F(c.Sf), F(c.HSf), T(c.r_diag),
+            T(c.zone_pos), tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
+    prec = oak_gb300.PREC_FP64 if a.precision == "fp64" else oak_gb300.PREC_MIXED
+    for _ in range(a.calls):
+        oak_gb300.loc_analysis(*args, weight=c.weight, metric=c.metric, loctype=c.loctype,
+                               want_ampl=False, precision=prec)
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"workload": c.name, "zones": int(c.Z), "N": int(c.N), "m": int(c.m),
+                      "precision": a.precision, "calls": a.calls,
+                      "stage_ms_last_call": oak_gb300.last_timings()}))
+
+
+if __name__ == "__main__":
+    main()

@@ -675,6 +675,67 @@ int grid_for_smem(const void* fn, size_t smem, int32_t nzc) {
   return grid;
 }
 
+// E1 and E3 of the generic path
+template <typename R>
+cudaError_t launch_e1(int N, int32_t nzc, R* d_GT, R* d_aux, const int32_t* d_nobs,
+                      int32_t* d_work, cudaStream_t st) {
+  size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(R);
+  cudaError_t e = cudaFuncSetAttribute(k_eig_tridiag<R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  if (e != cudaSuccess) return e;
+  k_eig_tridiag<R><<<grid_for_smem((const void*)k_eig_tridiag<R>, smem1, nzc), kThreads, smem1,
+                     st>>>(N, nzc, d_GT, d_aux, d_nobs, d_work);
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z, const R* d_g,
+                      const int32_t* d_nobs, int rotate, R* d_ampl, int32_t* d_status,
+                      int32_t* d_work, cudaStream_t st) {
+  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
+  cudaError_t e = cudaFuncSetAttribute(k_eig_transform<R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
+  if (e != cudaSuccess) return e;
+  k_eig_transform<R><<<grid_for_smem((const void*)k_eig_transform<R>, smem3, nzc), kThreads,
+                       smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl,
+                                    d_status, d_work);
+  return cudaSuccess;
+}
+
+// FP32 with at most 64 members: the register-blocked E1/E3 of zone_eig32.cu (they share the
+// aux layout and the inverse-iteration output with E2a/E2b, and store the reflectors
+// vector-major, so both are used together)
+template <>
+cudaError_t launch_e1<float>(int N, int32_t nzc, float* d_GT, float* d_aux,
+                             const int32_t* d_nobs, int32_t* d_work, cudaStream_t st) {
+  if (N <= eig32_max_n()) return eig32_tridiag(N, nzc, d_GT, d_aux, d_nobs, d_work, st);
+  size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_eig_tridiag<float>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  if (e != cudaSuccess) return e;
+  k_eig_tridiag<float><<<grid_for_smem((const void*)k_eig_tridiag<float>, smem1, nzc), kThreads,
+                         smem1, st>>>(N, nzc, d_GT, d_aux, d_nobs, d_work);
+  return cudaSuccess;
+}
+
+template <>
+cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux,
+                             const float* d_Z, const float* d_g, const int32_t* d_nobs,
+                             int rotate, float* d_ampl, int32_t* d_status, int32_t* d_work,
+                             cudaStream_t st) {
+  if (N <= eig32_max_n())
+    return eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
+                           d_work, st);
+  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(float) + (size_t)N * sizeof(int);
+  cudaError_t e = cudaFuncSetAttribute(k_eig_transform<float>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
+  if (e != cudaSuccess) return e;
+  k_eig_transform<float><<<grid_for_smem((const void*)k_eig_transform<float>, smem3, nzc),
+                           kThreads, smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate,
+                                                  d_ampl, d_status, d_work);
+  return cudaSuccess;
+}
+
 template <typename R>
 cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32_t* d_nobs,
                           int rotate, R* d_ampl, int32_t* d_status, R* d_aux, R* d_Z,
@@ -684,26 +745,16 @@ cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(d_work, 0, 2 * sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
-  // E1
-  size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(R);
-  e = cudaFuncSetAttribute(k_eig_tridiag<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem1);
+  e = launch_e1<R>(N, nzc, d_GT, d_aux, d_nobs, d_work, st);
   if (e != cudaSuccess) return e;
-  k_eig_tridiag<R><<<grid_for_smem((const void*)k_eig_tridiag<R>, smem1, nzc), kThreads, smem1,
-                     st>>>(N, nzc, d_GT, d_aux, d_nobs, d_work);
   // E2a, E2b
   k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   const int64_t pairs = (int64_t)nzc * N;
   k_eig_tridiag_vectors<R><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
                                                                              d_nobs);
-  // E3
-  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
-  e = cudaFuncSetAttribute(k_eig_transform<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem3);
+  e = launch_e3<R>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, d_work + 1,
+                   st);
   if (e != cudaSuccess) return e;
-  k_eig_transform<R><<<grid_for_smem((const void*)k_eig_transform<R>, smem3, nzc), kThreads,
-                       smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl,
-                                    d_status, d_work + 1);
   count_launches(4);
   return cudaGetLastError();
 }
