@@ -68,7 +68,7 @@ struct Buf {
 enum BufId {
   B_ZONE_SIZE, B_XF, B_HXF, B_YO, B_R, B_SF, B_HSF, B_ZXYZT, B_OX, B_OY, B_OZ, B_OT, B_CORR,
   B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
-  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
+  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
   B_COUNT_
 };
 
@@ -182,6 +182,7 @@ __global__ void k_set_int(int32_t* p, int32_t v) { *p = v; }
 int status_code(int32_t bits) {
   if (bits & ZST_NAN) return fail(OAKG_ERR_NAN, "NaN in analysis amplitudes (rrsqrt.F90:145-149)");
   if (bits & ZST_EIG) return fail(OAKG_ERR_EIG, "symmetric eigensolver did not converge");
+  if (bits & ZST_TIMEOUT) return fail(OAKG_ERR_TIMEOUT, "a bounded device wait expired");
   if (bits) return fail(OAKG_ERR_CUDA, "device status 0x%x", bits);
   return OAKG_OK;
 }
@@ -202,8 +203,13 @@ template <typename R>
 struct ZoneKernels;
 template <>
 struct ZoneKernels<double> {
-  template <typename... A>
-  static cudaError_t gram(A... a) { return zone_gram_fp64(a...); }
+  static cudaError_t gram(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
+                          int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
+                          double* d_G, double* d_g, int32_t* nobs, int brute, int32_t* work,
+                          int32_t* /*err*/, cudaStream_t st) {
+    return zone_gram_fp64(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
+                          st);
+  }
   template <typename... A>
   static cudaError_t eig(A... a) { return zone_eig_fp64(a...); }
   template <typename... A>
@@ -213,8 +219,17 @@ struct ZoneKernels<double> {
 };
 template <>
 struct ZoneKernels<float> {
-  template <typename... A>
-  static cudaError_t gram(A... a) { return zone_gram_fp32(a...); }
+  // tensor-core Gram for ensembles of up to gram_tc_max_n() members, else the CUDA-core one
+  static cudaError_t gram(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
+                          int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
+                          float* d_G, float* d_g, int32_t* nobs, int brute, int32_t* work,
+                          int32_t* err, cudaStream_t st) {
+    if (N <= gram_tc_max_n() && so.HSt32)
+      return zone_gram_tc(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
+                          err, st);
+    return zone_gram_fp32(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
+                          st);
+  }
   template <typename... A>
   static cudaError_t eig(A... a) { return zone_eig_fp32(a...); }
   template <typename... A>
@@ -269,7 +284,7 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     const int32_t nzc = (int32_t)std::min<int64_t>(chunk, a.Z - z0);
     cudaEventRecord(c->ev[2], st);
     e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv, a.nobs,
-                a.brute, d_work, st);
+                a.brute, d_work, *status_all, st);
     if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
     cudaEventRecord(c->ev[3], st);
     e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate, d_za,
@@ -448,6 +463,13 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     so.HSt = d_hst;
     so.cell_start = d_cstart;
     so.perm = d_perm;
+    if (loc->precision == OAKG_PREC_MIXED) {
+      float* d_hst32;
+      if ((rc = scratch(c, B_HST32, (size_t)m * N, &d_hst32, "obs rows (FP32)"))) return rc;
+      if ((e = rows_to_fp32(d_hst, d_hst32, m * N, st)) != cudaSuccess)
+        return cuda_fail(e, "FP32 observation rows");
+      so.HSt32 = d_hst32;
+    }
   } else {
     int32_t* d_cstart;
     if ((rc = scratch(c, B_CSTART, 2, &d_cstart, "cells"))) return rc;

@@ -12,6 +12,7 @@ enum : int32_t {
   ZST_NAN = 1,       // NaN/Inf amplitudes (rrsqrt.F90:145-149)
   ZST_EIG = 2,       // QL iterations did not converge
   ZST_CAPACITY = 4,  // zone larger than the kernel's row tile (cannot happen: tiles split)
+  ZST_TIMEOUT = 8,   // a bounded device wait expired (tensor-core pipeline)
 };
 
 // Cell grid over observation coordinates (u, v): cells are cs_u x cs_v, nu x nv of them,
@@ -31,6 +32,7 @@ struct SortedObs {
   const double* innov;  // yo - Hxf                                            [m]
   const double* r;      // observation error variance (R diagonal)            [m]
   const double* HSt;    // HSf rows, row-major [m][N]
+  const float* HSt32;   // the same rows in FP32 (mixed precision only, else null)
   const int32_t* cell_start;  // [ncells + 1]
   const int32_t* perm;  // sorted position -> original index                [m]
 };
@@ -67,6 +69,15 @@ cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocPar
                            const double* corr_len, const double* max_len, float* d_G,
                            float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
                            cudaStream_t st);
+// Mixed precision on the tensor cores (zone_gram_tc.cu), N <= gram_tc_max_n(); needs
+// so.HSt32. d_err receives ZST_TIMEOUT (OR) if a bounded device wait expired.
+int gram_tc_max_n();
+cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
+                         int32_t nzc, const double* zone_xyzt, const double* corr_len,
+                         const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
+                         int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st);
+// FP32 copy of count doubles (HS rows for the mixed form).
+cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st);
 // Same as zone_gram_fp64 for the zones listed in zlist[0..nzc) (G, g slots in list order).
 cudaError_t zone_gram_fp64_list(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
                                 const int32_t* zlist, int32_t nzc, const double* zone_xyzt,

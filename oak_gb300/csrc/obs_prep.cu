@@ -295,6 +295,19 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
   return cudaGetLastError();
 }
 
+__global__ void k_to_fp32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_to_fp32<<<grid_for(count, 256), 256, 0, st>>>(src, dst, count);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_start,
                          int32_t* d_zone_max, cudaStream_t st) {
   k_scan_single<int32_t, int64_t><<<1, kScanThreads, 0, st>>>(zone_size, Z, d_zone_start,

@@ -1,0 +1,471 @@
+// K1 + K2, mixed-precision form on the tensor cores (ensembles of up to 64 members).
+//
+// Selection is the FP64 selection of zone_gram.cu (assimilation.F90:3683-3771 with the
+// reference distance and weight functions), so the selected set is identical to the plain
+// form's. The Gram matrix G = HS_sel^T diag(c) HS_sel (rrsqrt.F90:135, c = w^2 / r from the
+// DCDCovar of rrsqrt.F90:395) is written as G = X^T X with X = diag(sqrt(c)) HS_sel and
+// computed by tcgen05.mma kind::tf32 with FP32 accumulation in tensor memory:
+//
+//   X (FP32) is split into two TF32 parts, X = X_hi + X_lo (X_lo = tf32(X - X_hi)), leaving a
+//   residual of ~2^-22 |X|. A K-tile of 32 selected observations is staged in shared memory as
+//   one 128-row operand S = [X_hi^T ; X_lo^T] (rows 0-63: hi parts of members 0-63, rows
+//   64-127: lo parts; K-major, 128-byte swizzle). One M=128, N=128 MMA chain with S as both A
+//   and B accumulates D = S S^T, whose four 64 x 64 blocks are X_hi^T X_hi, X_hi^T X_lo,
+//   X_lo^T X_hi and X_lo^T X_lo; G is their sum (symmetrised from the lower triangle).
+//
+// The innovation projection g = X^T (sqrt(c) d) (rrsqrt.F90:142) is accumulated on the CUDA
+// cores by the staging threads with compensated (Kahan) FP32 sums.
+//
+// Pipeline per CTA (one zone at a time): candidates are tested 256 at a time; selected
+// observations go to a ring of (index, sqrt(c), sqrt(c) d); every full K-tile is staged into
+// one of two shared buffers and handed to the tensor core by one thread (4 MMAs of K = 8 and a
+// commit to the buffer's mbarrier), so staging of the next tile overlaps the MMAs. At the end
+// of the zone the accumulator is read with tcgen05.ld. Every mbarrier wait is bounded; on
+// expiry the kernel records ZST_TIMEOUT, stops taking zones, waits (bounded) for its MMAs and
+// frees its tensor memory.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "oakg_internal.cuh"
+#include "selection.cuh"
+
+namespace oakg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int NB = 64;            // padded ensemble size
+constexpr int KT = 32;            // observations per K-tile (128 bytes of TF32 per row)
+constexpr int kRing = 512;        // selected-observation ring (power of two)
+constexpr uint32_t kTileBytes = 128u * 128u;
+constexpr uint32_t kTmemCols = 128;
+constexpr int kWaitPolls = 1 << 22;
+constexpr int GLD = NB + 1;       // row stride of the shared G staging (floats)
+// dynamic shared memory: 1 KB alignment slack, two tiles (also reused for G at the end of a
+// zone), compensated innovation partials; padded so that at most 4 CTAs share an SM (4 x 128
+// tensor-memory columns = all 512)
+constexpr size_t kDynSmem = 1024 + 2 * kTileBytes + 2 * 4 * NB * sizeof(float) + 12 * 1024;
+static_assert(NB * GLD * sizeof(float) <= 2 * kTileBytes, "G staging must fit in the tiles");
+
+struct TcShared {
+  int32_t ring_q[kRing];
+  float ring_s[kRing];  // sqrt(c_q)
+  float ring_y[kRing];  // sqrt(c_q) (yo - Hxf)_q
+  unsigned long long mbar[2];
+  int32_t warp_cnt[kThreads / 32];
+  uint32_t tmem_base;
+  int32_t zone;
+  int32_t nrel;
+  int32_t flag;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused: K fits one swizzle row)
+  d |= (uint64_t)(1024u >> 4) << 32;        // stride byte offset
+  d |= (uint64_t)1 << 46;                   // descriptor version
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: D F32, A and B TF32, both K-major, N = 128, M = 128
+constexpr uint32_t kIdesc =
+    (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t desc, uint32_t accum) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %3, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %4, p;\n}\n" ::"r"(tmem_d),
+      "l"(desc), "l"(desc), "r"(accum), "r"(kIdesc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (int i = 0; i < kWaitPolls; i++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 16 consecutive accumulator columns of this warp's 32 tensor-memory lanes
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of the 16-byte chunk `chunk` (4 observations) of operand row `row` in a tile
+__device__ __forceinline__ uint32_t tile_off(int row, int chunk) {
+  return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
+}
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float term) {
+  const float y = term - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+__global__ void __launch_bounds__(kThreads, 4)
+    k_zone_gram_tc(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
+                   const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
+                   const double* __restrict__ max_len, float* __restrict__ G,
+                   float* __restrict__ gv, int32_t* __restrict__ nobs, int brute,
+                   int32_t* __restrict__ work, int32_t* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  __shared__ __align__(16) TcShared ts;
+  const uint32_t raw_addr = smem_u32(dyn_raw);
+  const uint32_t pad = ((raw_addr + 1023u) & ~1023u) - raw_addr;
+  unsigned char* tiles = dyn_raw + pad;                 // 2 x kTileBytes, 1024-aligned
+  const uint32_t tile_addr = raw_addr + pad;
+  float* gps = reinterpret_cast<float*>(tiles + 2 * kTileBytes);  // [4][NB] partial sums
+  float* gpc = gps + 4 * NB;                                       // [4][NB] compensations
+  float* Gs = reinterpret_cast<float*>(tiles);                     // [NB][GLD] (end of zone)
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int a = tid & (NB - 1), kq = tid >> 6;  // staging: member a, observation quads kq, kq+4
+  const uint32_t mbar0 = smem_u32(&ts.mbar[0]);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ts.flag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ts.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = ts.tmem_base;
+
+  const int64_t ncells = (int64_t)g.nu * g.nv;
+  const int full_scan = brute || !lp.localise;
+  int pend0 = 0, pend1 = 0;     // buffer has MMAs not yet waited for (uniform)
+  uint32_t ph0 = 0, ph1 = 0;    // parity of the buffer's next completion (uniform)
+  bool abort = false;
+
+  // wait for buffer b's outstanding MMAs (thread 0, bounded); result published in ts.flag
+  auto drain = [&](int b) {
+    if (tid == 0) {
+      const uint32_t ph = b ? ph1 : ph0;
+      if (!mbar_wait(mbar0 + 8 * b, ph)) ts.flag = 1;
+    }
+    if (b) {
+      ph1 ^= 1u;
+      pend1 = 0;
+    } else {
+      ph0 ^= 1u;
+      pend0 = 0;
+    }
+  };
+
+  for (;;) {
+    if (tid == 0) ts.zone = atomicAdd(work, 1);
+    __syncthreads();
+    const int32_t zl = ts.zone;
+    if (zl >= nzc || ts.flag) break;
+    const int32_t z = z0 + zl;
+    const double zx = zone_xyzt[4 * (int64_t)z + 0], zy = zone_xyzt[4 * (int64_t)z + 1];
+    const double zzc = zone_xyzt[4 * (int64_t)z + 2], ztc = zone_xyzt[4 * (int64_t)z + 3];
+    const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
+    const double zv = (lp.loctype == 1) ? zy : 0.0;
+    const double L = corr_len[z], Rmax = max_len[z];
+    if (tid == 0) ts.nrel = 0;
+    int head = 0, tail = 0, ntile = 0, nrel_local = 0;
+    float gsum = 0.f, gcmp = 0.f;
+
+    // stage ring entries [head, head + rows) as one K-tile and issue its MMAs
+    auto do_tile = [&](int rows) {
+      const int b = ntile & 1;
+      if (b ? pend1 : pend0) drain(b);
+      __syncthreads();  // buffer free (flag published), ring entries visible
+      if (ts.flag) {
+        abort = true;
+        return;
+      }
+      unsigned char* tb = tiles + b * kTileBytes;
+#pragma unroll
+      for (int pass = 0; pass < 2; pass++) {
+        const int quad = kq + 4 * pass;
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int k = 4 * quad + i;
+          float X = 0.f, y = 0.f;
+          if (k < rows) {
+            const int idx = (head + k) & (kRing - 1);
+            const int32_t q = ts.ring_q[idx];
+            const float h = (a < N) ? so.HSt32[(int64_t)q * N + a] : 0.f;
+            X = ts.ring_s[idx] * h;
+            y = ts.ring_y[idx];
+          }
+          hi[i] = to_tf32(X);
+          lo[i] = to_tf32(X - __uint_as_float(hi[i]));
+          kahan_add(gsum, gcmp, X * y);
+        }
+        *reinterpret_cast<uint4*>(tb + tile_off(a, quad)) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(tb + tile_off(a + NB, quad)) =
+            make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();  // tile complete
+      if (tid == 0) {
+        fence_after();
+        const uint32_t base = tile_addr + b * kTileBytes;
+#pragma unroll
+        for (int kk = 0; kk < KT / 8; kk++)
+          mma_tf32(tmem, make_desc(base + kk * 32), (ntile > 0 || kk > 0) ? 1u : 0u);
+        mma_commit(mbar0 + 8 * b);
+      }
+      if (b)
+        pend1 = 1;
+      else
+        pend0 = 1;
+      ntile++;
+      head += rows;
+    };
+
+    sel::ScanRange sr;
+    if (full_scan) {
+      sr.cu0 = 0;
+      sr.cu1 = g.nu - 1;
+      sr.cv0 = 0;
+      sr.cv1 = g.nv - 1;
+      sr.all_u = 1;
+    } else {
+      sr = sel::zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
+    }
+    for (int cv = sr.cv0; cv <= sr.cv1 && !abort; cv++) {
+      for (int part = 0; part < 2 && !abort; part++) {
+        int cu_a, cu_b;
+        if (sr.all_u) {
+          if (part) break;
+          cu_a = 0;
+          cu_b = g.nu - 1;
+        } else if (!g.periodic_u) {
+          if (part) break;
+          cu_a = sr.cu0;
+          cu_b = sr.cu1;
+        } else {
+          const int a0 = sr.cu0, b0 = sr.cu1;
+          if (a0 < 0) {
+            cu_a = part ? 0 : a0 + g.nu;
+            cu_b = part ? b0 : g.nu - 1;
+          } else if (b0 >= g.nu) {
+            cu_a = part ? 0 : a0;
+            cu_b = part ? b0 - g.nu : g.nu - 1;
+          } else {
+            if (part) break;
+            cu_a = a0;
+            cu_b = b0;
+          }
+        }
+        const int64_t c_lo = (int64_t)cu_a + (int64_t)g.nu * cv;
+        const int64_t c_hi = (int64_t)cu_b + (int64_t)g.nu * cv;
+        if (c_lo > c_hi || c_lo < 0 || c_hi >= ncells) continue;
+        const int32_t q_lo = so.cell_start[c_lo], q_hi = so.cell_start[c_hi + 1];
+        for (int32_t qb = q_lo; qb < q_hi && !abort; qb += kThreads) {
+          const int32_t q = qb + tid;
+          int sel = 0, rel = 0;
+          double w = 0.0, rq = 1.0, dq = 0.0;
+          if (q < q_hi) {
+            double d;
+            if (lp.loctype == 1)
+              d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
+            else
+              d = fabs(__dsub_rn(so.u[q], zu));
+            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+              rel = (d <= Rmax);
+              const double t = d / L;
+              w = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
+            } else {
+              w = sel::locfun(d / L);
+              rel = (d <= Rmax) && (w != 0.0);
+            }
+            sel = rel || !lp.localise;
+            if (sel) {
+              rq = so.r[q];
+              dq = so.innov[q];
+            }
+          }
+          nrel_local += rel;
+          const unsigned ball = __ballot_sync(0xffffffffu, sel);
+          if (lane == 0) ts.warp_cnt[warp] = __popc(ball);
+          __syncthreads();
+          int before = 0, total = 0;
+#pragma unroll
+          for (int w2 = 0; w2 < kThreads / 32; w2++) {
+            const int cnt = ts.warp_cnt[w2];
+            before += (w2 < warp) ? cnt : 0;
+            total += cnt;
+          }
+          if (sel) {
+            // c = w (w / r) (DCDCovar, covariance.F90:612-619); sqrt(c) = |w| / sqrt(r)
+            const double sc = sqrt(w * (w / rq));
+            const int slot = (tail + before + __popc(ball & ((1u << lane) - 1u))) & (kRing - 1);
+            ts.ring_q[slot] = q;
+            ts.ring_s[slot] = (float)sc;
+            ts.ring_y[slot] = (float)(sc * dq);
+          }
+          __syncthreads();
+          tail += total;
+          while (tail - head >= KT && !abort) do_tile(KT);
+        }
+      }
+    }
+    if (!abort && tail > head) do_tile(tail - head);
+    if (abort) break;
+    // relevant-observation count of the zone
+    for (int o = 16; o > 0; o >>= 1) nrel_local += __shfl_xor_sync(0xffffffffu, nrel_local, o);
+    if (lane == 0) atomicAdd(&ts.nrel, nrel_local);
+    gps[kq * NB + a] = gsum;
+    gpc[kq * NB + a] = gcmp;
+    if (ntile > 0) {
+      if (pend0) drain(0);
+      if (pend1) drain(1);
+    }
+    __syncthreads();  // nrel, partials and the MMA completion published
+    if (ts.flag) break;
+    const int nrel = ts.nrel;
+    if (tid == 0) nobs[z] = nrel;
+    if (nrel > 0 && ntile > 0) {
+      fence_after();
+      // G = sum of the four 64 x 64 blocks of D; warps 2-3 hold rows 64-127 (lo parts),
+      // warps 0-1 rows 0-63 (hi parts); each adds its two column halves
+      if (warp == 2 || warp == 3) {
+        const int r = lane + 32 * (warp - 2);
+        const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+          float v0[16], v1[16];
+          tmem_ld16(ta + 16 * h, v0);
+          tmem_ld16(ta + 64 + 16 * h, v1);
+#pragma unroll
+          for (int i = 0; i < 16; i++) Gs[r * GLD + 16 * h + i] = v0[i] + v1[i];
+        }
+      }
+      __syncthreads();
+      if (warp == 0 || warp == 1) {
+        const int r = lane + 32 * warp;
+        const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+          float v0[16], v1[16];
+          tmem_ld16(ta + 16 * h, v0);
+          tmem_ld16(ta + 64 + 16 * h, v1);
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            float* p = Gs + r * GLD + 16 * h + i;
+            *p = (v0[i] + v1[i]) + *p;
+          }
+        }
+      }
+      fence_before();
+      __syncthreads();
+      float* Gz = G + (int64_t)zl * N * N;
+      for (int idx = tid; idx < N * N; idx += kThreads) {
+        const int i = idx / N, j = idx - i * N;
+        Gz[idx] = (j <= i) ? Gs[i * GLD + j] : Gs[j * GLD + i];
+      }
+      if (tid < N) {
+        // compensated combination of the four partial sums of member tid
+        float s = 0.f, cmp = 0.f;
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+          kahan_add(s, cmp, gps[p * NB + tid]);
+          kahan_add(s, cmp, -gpc[p * NB + tid]);
+        }
+        gv[(int64_t)zl * N + tid] = s;
+      }
+    }
+    __syncthreads();  // G staging and partials consumed before the next zone's tiles
+  }
+  // teardown: no MMA may still write tensor memory when it is freed
+  if (pend0) drain(0);
+  if (pend1) drain(1);
+  if (tid == 0 && ts.flag) atomicOr(err, ZST_TIMEOUT);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+}
+
+}  // namespace
+
+int gram_tc_max_n() { return NB; }
+
+cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
+                         int32_t nzc, const double* zone_xyzt, const double* corr_len,
+                         const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
+                         int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st) {
+  if (N < 1 || N > NB || !so.HSt32) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_zone_gram_tc,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kDynSmem);
+  if (e != cudaSuccess) return e;
+  int bps = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_gram_tc, kThreads, kDynSmem);
+  if (e != cudaSuccess) return e;
+  if (bps > 4) bps = 4;  // 4 x 128 tensor-memory columns per SM
+  if (bps < 1) bps = 1;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = sms * bps;
+  if (grid > nzc) grid = nzc > 0 ? nzc : 1;
+  e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  k_zone_gram_tc<<<grid, kThreads, kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
+                                                   max_len, d_G, d_g, d_nobs, brute, d_work,
+                                                   d_err);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace oakg
