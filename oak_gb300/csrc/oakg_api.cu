@@ -68,7 +68,7 @@ struct Buf {
 enum BufId {
   B_ZONE_SIZE, B_XF, B_HXF, B_YO, B_R, B_SF, B_HSF, B_ZXYZT, B_OX, B_OY, B_OZ, B_OT, B_CORR,
   B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
-  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
+  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_OBS32, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
   B_COUNT_
 };
 
@@ -224,7 +224,7 @@ struct ZoneKernels<float> {
                           int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
                           float* d_G, float* d_g, int32_t* nobs, int brute, int32_t* work,
                           int32_t* err, cudaStream_t st) {
-    if (N <= gram_tc_max_n() && so.HSt32)
+    if (N <= gram_tc_max_n() && so.HSt32 && so.r32)
       return zone_gram_tc(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
                           err, st);
     return zone_gram_fp32(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
@@ -469,6 +469,13 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
       if ((e = rows_to_fp32(d_hst, d_hst32, m * N, st)) != cudaSuccess)
         return cuda_fail(e, "FP32 observation rows");
       so.HSt32 = d_hst32;
+      float* d_obs32;
+      if ((rc = scratch(c, B_OBS32, (size_t)2 * m, &d_obs32, "obs (FP32)"))) return rc;
+      if ((e = rows_to_fp32(d_sr, d_obs32, m, st)) != cudaSuccess ||
+          (e = rows_to_fp32(d_sinnov, d_obs32 + m, m, st)) != cudaSuccess)
+        return cuda_fail(e, "FP32 observation values");
+      so.r32 = d_obs32;
+      so.innov32 = d_obs32 + m;
     }
   } else {
     int32_t* d_cstart;

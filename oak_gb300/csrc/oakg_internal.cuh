@@ -33,6 +33,8 @@ struct SortedObs {
   const double* r;      // observation error variance (R diagonal)            [m]
   const double* HSt;    // HSf rows, row-major [m][N]
   const float* HSt32;   // the same rows in FP32 (mixed precision only, else null)
+  const float* r32;     // r in FP32 (mixed precision only)
+  const float* innov32; // yo - Hxf in FP32 (mixed precision only)
   const int32_t* cell_start;  // [ncells + 1]
   const int32_t* perm;  // sorted position -> original index                [m]
 };

@@ -1,8 +1,12 @@
 // K1 + K2, mixed-precision form on the tensor cores (ensembles of up to 64 members).
 //
-// Selection is the FP64 selection of zone_gram.cu (assimilation.F90:3683-3771 with the
-// reference distance and weight functions), so the selected set is identical to the plain
-// form's. The Gram matrix G = HS_sel^T diag(c) HS_sel (rrsqrt.F90:135, c = w^2 / r from the
+// Selection makes the decisions of zone_gram.cu (assimilation.F90:3683-3771): d <= maxLength
+// and, for Gaspari-Cohn, locfun(d/L) /= 0. For Cartesian and 1-D distances they are taken from
+// an FP32 distance (relative error < 2e-7, from an FP64 squared distance) when it is farther
+// than a relative 1e-6 from maxLength and r = d/L is below 2 - 1e-3 or above 2 + 1e-5; inside
+// those margins the reference's FP64 distance and locfun with IEEE rounding decide, as they do
+// for the spherical metrics. The selected set is therefore identical to the plain form's. The
+// weights themselves are FP32 (locfun or exp of the FP32 ratio). The Gram matrix G = HS_sel^T diag(c) HS_sel (rrsqrt.F90:135, c = w^2 / r from the
 // DCDCovar of rrsqrt.F90:395) is written as G = X^T X with X = diag(sqrt(c)) HS_sel and
 // computed by tcgen05.mma kind::tf32 with FP32 accumulation in tensor memory:
 //
@@ -138,6 +142,17 @@ __device__ __forceinline__ uint32_t tile_off(int row, int chunk) {
   return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
+// Gaspari-Cohn weight in FP32 (covariance.F90:645-667); used for weight values only, never for
+// the relevance decision
+__device__ __forceinline__ float locfun32(float r) {
+  if (r <= 1.f) return fmaf(fmaf(fmaf(fmaf(-0.25f, r, 0.5f), r, 0.625f), r, -5.f / 3.f), r * r, 1.f);
+  if (r <= 2.f)
+    return fmaf(fmaf(fmaf(fmaf(fmaf(r, 1.f / 12.f, -0.5f), r, 0.625f), r, 5.f / 3.f), r, -5.f), r,
+                4.f) -
+           2.f / (3.f * r);
+  return 0.f;
+}
+
 __device__ __forceinline__ void kahan_add(float& s, float& c, float term) {
   const float y = term - c;
   const float t = s + y;
@@ -184,6 +199,7 @@ __global__ void __launch_bounds__(kThreads, 4)
 
   const int64_t ncells = (int64_t)g.nu * g.nv;
   const int full_scan = brute || !lp.localise;
+  const bool fast = (lp.loctype != 1) || (lp.metric == OAKG_METRIC_CARTESIAN);
   int pend0 = 0, pend1 = 0;     // buffer has MMAs not yet waited for (uniform)
   uint32_t ph0 = 0, ph1 = 0;    // parity of the buffer's next completion (uniform)
   bool abort = false;
@@ -214,6 +230,8 @@ __global__ void __launch_bounds__(kThreads, 4)
     const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
     const double zv = (lp.loctype == 1) ? zy : 0.0;
     const double L = corr_len[z], Rmax = max_len[z];
+    const float iL32 = (float)(1.0 / L);
+    const float r_lo = (float)Rmax * (1.f - 1e-6f), r_hi = (float)Rmax * (1.f + 1e-6f);
     if (tid == 0) ts.nrel = 0;
     int head = 0, tail = 0, ntile = 0, nrel_local = 0;
     float gsum = 0.f, gcmp = 0.f;
@@ -311,26 +329,53 @@ __global__ void __launch_bounds__(kThreads, 4)
         for (int32_t qb = q_lo; qb < q_hi && !abort; qb += kThreads) {
           const int32_t q = qb + tid;
           int sel = 0, rel = 0;
-          double w = 0.0, rq = 1.0, dq = 0.0;
+          float w32 = 0.f;
           if (q < q_hi) {
-            double d;
-            if (lp.loctype == 1)
-              d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
-            else
-              d = fabs(__dsub_rn(so.u[q], zu));
-            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-              rel = (d <= Rmax);
-              const double t = d / L;
-              w = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
-            } else {
-              w = sel::locfun(d / L);
-              rel = (d <= Rmax) && (w != 0.0);
+            // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
+            bool done = false;
+            if (fast) {
+              const double du = so.u[q] - zu;
+              double D2 = du * du;
+              if (lp.loctype == 1) {
+                const double dv = so.v[q] - zv;
+                D2 = fma(dv, dv, D2);
+              }
+              const float d32 = sqrtf((float)D2);  // relative error < 2e-7
+              const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
+              if (inside >= 0) {
+                const float r32 = d32 * iL32;
+                if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+                  rel = inside;
+                  w32 = (rel || !lp.localise) ? expf(-(r32 * r32)) : 0.f;
+                  done = true;
+                } else if (r32 >= 2.f + 1e-5f) {  // locfun = 0
+                  rel = 0;
+                  done = true;
+                } else if (r32 <= 2.f - 1e-3f) {  // locfun > 3e-13, far above its FP64 rounding (1e-15)
+                  rel = inside;
+                  w32 = locfun32(r32);
+                  done = true;
+                }
+              }
+            }
+            if (!done) {
+              double d;
+              if (lp.loctype == 1)
+                d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
+              else
+                d = fabs(__dsub_rn(so.u[q], zu));
+              double w;
+              if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+                rel = (d <= Rmax);
+                const double t = d / L;
+                w = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
+              } else {
+                w = sel::locfun(d / L);
+                rel = (d <= Rmax) && (w != 0.0);
+              }
+              w32 = (float)w;
             }
             sel = rel || !lp.localise;
-            if (sel) {
-              rq = so.r[q];
-              dq = so.innov[q];
-            }
           }
           nrel_local += rel;
           const unsigned ball = __ballot_sync(0xffffffffu, sel);
@@ -345,11 +390,11 @@ __global__ void __launch_bounds__(kThreads, 4)
           }
           if (sel) {
             // c = w (w / r) (DCDCovar, covariance.F90:612-619); sqrt(c) = |w| / sqrt(r)
-            const double sc = sqrt(w * (w / rq));
+            const float sc = fabsf(w32) * rsqrtf(so.r32[q]);
             const int slot = (tail + before + __popc(ball & ((1u << lane) - 1u))) & (kRing - 1);
             ts.ring_q[slot] = q;
-            ts.ring_s[slot] = (float)sc;
-            ts.ring_y[slot] = (float)(sc * dq);
+            ts.ring_s[slot] = sc;
+            ts.ring_y[slot] = sc * so.innov32[q];
           }
           __syncthreads();
           tail += total;
@@ -444,16 +489,15 @@ cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParam
                          int32_t nzc, const double* zone_xyzt, const double* corr_len,
                          const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
                          int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st) {
-  if (N < 1 || N > NB || !so.HSt32) return cudaErrorInvalidValue;
+  if (N < 1 || N > NB || !so.HSt32 || !so.r32 || !so.innov32) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_zone_gram_tc,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kDynSmem);
   if (e != cudaSuccess) return e;
-  int bps = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_gram_tc, kThreads, kDynSmem);
+  e = cudaFuncSetAttribute(k_zone_gram_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
-  if (bps > 4) bps = 4;  // 4 x 128 tensor-memory columns per SM
-  if (bps < 1) bps = 1;
+  const int bps = 4;  // the shared-memory size admits at most 4 CTAs (4 x 128 TMEM columns)
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
