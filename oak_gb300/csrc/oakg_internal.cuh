@@ -121,6 +121,10 @@ size_t zone_eig_aux(int N);
 int eig32_max_n();
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
                           int32_t* d_work, cudaStream_t st);
+cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs,
+                         int32_t* d_status, cudaStream_t st);
+cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
+                          const int32_t* d_nobs, cudaStream_t st);
 cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
                             float* d_ampl, int32_t* d_status, int32_t* d_work, cudaStream_t st);

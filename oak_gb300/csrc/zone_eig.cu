@@ -737,6 +737,31 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
 }
 
 template <typename R>
+cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nobs,
+                      int32_t* d_status, cudaStream_t st) {
+  k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  const int64_t pairs = (int64_t)nzc * N;
+  k_eig_tridiag_vectors<R><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
+                                                                             d_nobs);
+  return cudaSuccess;
+}
+
+template <>
+cudaError_t launch_e2<float>(int N, int32_t nzc, float* d_aux, float* d_Z, const int32_t* d_nobs,
+                             int32_t* d_status, cudaStream_t st) {
+  if (N <= eig32_max_n()) {
+    cudaError_t e = eig32_values(N, nzc, d_aux, d_nobs, d_status, st);
+    if (e != cudaSuccess) return e;
+    return eig32_vectors(N, nzc, d_aux, d_Z, d_nobs, st);
+  }
+  k_eig_tridiag_values<float><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  const int64_t pairs = (int64_t)nzc * N;
+  k_eig_tridiag_vectors<float><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux,
+                                                                                 d_Z, d_nobs);
+  return cudaSuccess;
+}
+
+template <typename R>
 cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32_t* d_nobs,
                           int rotate, R* d_ampl, int32_t* d_status, R* d_aux, R* d_Z,
                           int32_t* d_work, cudaStream_t st) {
@@ -748,10 +773,8 @@ cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32
   e = launch_e1<R>(N, nzc, d_GT, d_aux, d_nobs, d_work, st);
   if (e != cudaSuccess) return e;
   // E2a, E2b
-  k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
-  const int64_t pairs = (int64_t)nzc * N;
-  k_eig_tridiag_vectors<R><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
-                                                                             d_nobs);
+  e = launch_e2<R>(N, nzc, d_aux, d_Z, d_nobs, d_status, st);
+  if (e != cudaSuccess) return e;
   e = launch_e3<R>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, d_work + 1,
                    st);
   if (e != cudaSuccess) return e;

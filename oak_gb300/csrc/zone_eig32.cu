@@ -543,6 +543,228 @@ __global__ void __launch_bounds__(kT, 4)
   }
 }
 
+// ------------------------------------------------------------------------------------ E2a
+// One thread per zone: eigenvalues of Tri by implicit symmetric QR sweeps with Wilkinson shift
+// (the arithmetic of the generic E2a in zone_eig.cu), with d and e in shared memory and the
+// chase's running values in registers; ascending sort; inverse-iteration shifts.
+constexpr int kT2 = 64;
+
+__global__ void __launch_bounds__(kT2)
+    k_eig_values32(int N, int32_t nzc, float* __restrict__ aux, const int32_t* __restrict__ nobs,
+                   int32_t* __restrict__ status) {
+  __shared__ float sd[NB * kT2], se[NB * kT2];  // element i of thread t at [i * kT2 + t]
+  const int t = threadIdx.x;
+  const int32_t zl = blockIdx.x * kT2 + t;
+  if (zl >= nzc || nobs[zl] == 0) return;  // no barrier below
+  const float eps = 5.9604645e-8f;
+  float* ax = aux + (int64_t)zl * aux_stride32(N);
+  float* d = sd + t;
+  float* e = se + t;
+  float onenrm = 0.f;
+  for (int i = 0; i < N; i++) {
+    d[i * kT2] = ax[i];
+    e[i * kT2] = (i < N - 1) ? ax[N + i] : 0.f;
+  }
+  for (int i = 0; i < N; i++) {
+    const float sabs = fabsf(d[i * kT2]) + fabsf(e[i * kT2]) + (i > 0 ? fabsf(e[(i - 1) * kT2]) : 0.f);
+    onenrm = fmaxf(onenrm, sabs);
+  }
+  const float scale = ax[5 * N];
+  const float abs_tol = eps * onenrm;
+  int st = 0, hi = N - 1, sweeps = 0;
+  const int max_sweeps = 30 * N;
+  while (hi > 0) {
+    while (hi > 0) {
+      const float tt = fabsf(e[(hi - 1) * kT2]);
+      if (tt <= eps * (fabsf(d[(hi - 1) * kT2]) + fabsf(d[hi * kT2])) || tt <= abs_tol) {
+        e[(hi - 1) * kT2] = 0.f;
+        hi--;
+      } else {
+        break;
+      }
+    }
+    if (hi == 0) break;
+    int lo = hi - 1;
+    while (lo > 0) {
+      const float tt = fabsf(e[(lo - 1) * kT2]);
+      if (tt <= eps * (fabsf(d[(lo - 1) * kT2]) + fabsf(d[lo * kT2])) || tt <= abs_tol) {
+        e[(lo - 1) * kT2] = 0.f;
+        break;
+      }
+      lo--;
+    }
+    if (++sweeps > max_sweeps) {
+      st |= ZST_EIG;
+      break;
+    }
+    const float a = d[(hi - 1) * kT2], b = d[hi * kT2], f = e[(hi - 1) * kT2];
+    const float del = 0.5f * (a - b);
+    const float den = del + copysignf(sqrtf(del * del + f * f), del == 0.f ? 1.f : del);
+    const float mu = (den == 0.f) ? b : b - f * f / den;
+    float dk = d[lo * kT2], ek = e[lo * kT2], ep = 0.f;  // d[k], e[k], e[k-1] (running)
+    float x = dk - mu, z = ek, bulge = 0.f;
+    for (int k = lo; k < hi; k++) {
+      const float dk1 = d[(k + 1) * kT2];
+      const float ek1 = (k + 1 < hi) ? e[(k + 1) * kT2] : 0.f;
+      if (k > lo) {
+        x = ep;
+        z = bulge;
+      }
+      const float r2 = x * x + z * z;
+      float c = 1.f, s = 0.f, r = 0.f;
+      if (r2 > 0.f) {
+        const float ri = rsqrtf(r2);
+        c = x * ri;
+        s = z * ri;
+        r = r2 * ri;
+      }
+      if (k > lo) e[(k - 1) * kT2] = r;
+      const float cc = c * c, ss = s * s, cs = c * s;
+      d[k * kT2] = cc * dk + 2.f * cs * ek + ss * dk1;
+      const float nd1 = ss * dk - 2.f * cs * ek + cc * dk1;
+      ep = cs * (dk1 - dk) + (cc - ss) * ek;
+      dk = nd1;
+      ek = c * ek1;
+      bulge = s * ek1;
+    }
+    d[hi * kT2] = dk;
+    e[(hi - 1) * kT2] = ep;
+  }
+  for (int i = 1; i < N; i++) {  // ascending (insertion sort)
+    const float v = d[i * kT2];
+    int k = i - 1;
+    while (k >= 0 && d[k * kT2] > v) {
+      d[(k + 1) * kT2] = d[k * kT2];
+      k--;
+    }
+    d[(k + 1) * kT2] = v;
+  }
+  float prev = 0.f;
+  for (int j = 0; j < N; j++) {
+    const float v = d[j * kT2];
+    ax[3 * N + j] = v * scale;
+    float sh = v;
+    if (j > 0) {
+      const float pert = 10.f * eps * fabsf(sh);
+      if (sh - prev < pert) sh = prev + pert;
+    }
+    ax[4 * N + j] = sh;
+    prev = sh;
+  }
+  ax[5 * N + 1] = onenrm;
+  if (st) status[zl] |= st;
+}
+
+// ------------------------------------------------------------------------------------ E2b
+// One block of 64 threads per zone, thread j = eigenpair j: inverse iteration on Tri - shift_j I
+// (two solves from a fixed pseudo-random start, as the generic E2b). The partial-pivoting LU
+// is recomputed in each forward sweep (fused with the elimination), its upper factor kept in
+// shared memory; the iterate lives in registers (loops unrolled to 64).
+__global__ void __launch_bounds__(kT2)
+    k_eig_vectors32(int N, int32_t nzc, const float* __restrict__ aux, float* __restrict__ Zg,
+                    const int32_t* __restrict__ nobs) {
+  __shared__ float sfac[3 * NB * kT2];  // upper factor u1, u2, 1/diag: [i][j] each
+  __shared__ float sd[NB], se[NB];
+  float* su1 = sfac;
+  float* su2 = sfac + NB * kT2;
+  float* sui = sfac + 2 * NB * kT2;
+  const int j = threadIdx.x;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  const float* ax = aux + (int64_t)zl * aux_stride32(N);
+  if (j < N) {
+    sd[j] = ax[j];
+    se[j] = (j < N - 1) ? ax[N + j] : 0.f;
+  }
+  __syncthreads();
+  const float onenrm = ax[5 * N + 1];
+  float* Zz = Zg + (int64_t)zl * N * N;
+  float* tr = sfac;  // [i][NB + 1] transpose staging, used at the end
+  float x[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) x[i] = 0.f;
+  if (!(onenrm > 1e4f * 1e-36f)) {  // Tri = 0: every vector is an eigenvector
+#pragma unroll
+    for (int i = 0; i < NB; i++) x[i] = (i == j) ? 1.f : 0.f;
+  } else if (j < N) {
+    const float l = ax[4 * N + j];
+    const float tiny = 5.9604645e-8f * onenrm;
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+      unsigned h = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
+      h ^= h >> 15;
+      h *= 2246822519u;
+      h ^= h >> 13;
+      x[i] = (i < N) ? (float)(h & 0xffffff) * (1.f / 16777216.f) - 0.5f : 0.f;
+    }
+#pragma unroll 1
+    for (int it = 0; it < 2; it++) {
+      float cd = sd[0] - l, csup = (N > 1) ? se[0] : 0.f;
+#pragma unroll
+      for (int i = 0; i < NB - 1; i++) {
+        if (i < N - 1) {
+          const float sub = se[i], dg = sd[i + 1] - l, sp = (i + 1 < N - 1) ? se[i + 1] : 0.f;
+          const bool swap = fabsf(cd) < fabsf(sub);
+          float pivot = swap ? sub : cd;
+          if (!swap && fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
+          const float ui = 1.f / pivot;
+          const float li = (swap ? cd : sub) * ui;
+          if (it == 0) {
+            su1[i * kT2 + j] = swap ? dg : csup;
+            su2[i * kT2 + j] = swap ? sp : 0.f;
+            sui[i * kT2 + j] = ui;
+          }
+          const float aa = swap ? csup : dg, bb = swap ? dg : csup;
+          cd = fmaf(-li, bb, aa);
+          csup = swap ? -li * sp : sp;
+          const float xi = swap ? x[i + 1] : x[i], xn = swap ? x[i] : x[i + 1];
+          x[i] = xi;
+          x[i + 1] = fmaf(-li, xi, xn);
+        }
+      }
+      if (it == 0) {
+        float pivot = cd;
+        if (fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
+        sui[(N - 1) * kT2 + j] = 1.f / pivot;
+        su1[(N - 1) * kT2 + j] = 0.f;
+        su2[(N - 1) * kT2 + j] = 0.f;
+        if (N >= 2) su2[(N - 2) * kT2 + j] = 0.f;
+      }
+      // back substitution with the upper factor (diagonal + two super-diagonals)
+#pragma unroll
+      for (int i = NB - 1; i >= 0; i--) {
+        if (i < N) {
+          float v = x[i];
+          if (i + 1 < NB) v = fmaf(-su1[i * kT2 + j], x[i + 1], v);
+          if (i + 2 < NB) v = fmaf(-su2[i * kT2 + j], x[i + 2], v);
+          x[i] = v * sui[i * kT2 + j];
+        }
+      }
+      float mx = 0.f;
+#pragma unroll
+      for (int i = 0; i < NB; i++) mx = fmaxf(mx, fabsf(x[i]));
+      const float im = 1.f / mx;
+      float nrm = 0.f;
+#pragma unroll
+      for (int i = 0; i < NB; i++) {
+        x[i] *= im;
+        nrm = fmaf(x[i], x[i], nrm);
+      }
+      const float sc = rsqrtf(nrm);
+#pragma unroll
+      for (int i = 0; i < NB; i++) x[i] *= sc;
+    }
+  }
+  __syncthreads();  // factors no longer read: reuse su1/su2 as the transpose buffer
+#pragma unroll
+  for (int i = 0; i < NB; i++) tr[i * (NB + 1) + j] = x[i];
+  __syncthreads();
+  for (int idx = j; idx < N * N; idx += kT2) {
+    const int jj = idx / N, i = idx - jj * N;
+    Zz[idx] = tr[i * (NB + 1) + jj];
+  }
+}
+
 int grid32(const void* fn, size_t smem, int32_t nzc) {
   int bps = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, kT, smem);
@@ -557,6 +779,20 @@ int grid32(const void* fn, size_t smem, int32_t nzc) {
 }  // namespace
 
 int eig32_max_n() { return NB; }
+
+cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs,
+                         int32_t* d_status, cudaStream_t st) {
+  if (N < 2 || N > NB) return cudaErrorInvalidValue;
+  k_eig_values32<<<(nzc + kT2 - 1) / kT2, kT2, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  return cudaGetLastError();
+}
+
+cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
+                          const int32_t* d_nobs, cudaStream_t st) {
+  if (N < 2 || N > NB) return cudaErrorInvalidValue;
+  k_eig_vectors32<<<nzc > 0 ? nzc : 1, kT2, 0, st>>>(N, nzc, d_aux, d_Z, d_nobs);
+  return cudaGetLastError();
+}
 
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
                           int32_t* d_work, cudaStream_t st) {
