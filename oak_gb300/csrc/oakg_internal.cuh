@@ -116,18 +116,18 @@ cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,
                           float* d_aux, float* d_Z, int32_t* d_work, cudaStream_t st);
 size_t zone_eig_aux(int N);
 
-// ---- zone_eig32.cu: register-blocked FP32 E1 / E3 for N <= eig32_max_n(), used by
-// zone_eig_fp32 (same arguments as the stages of zone_eig_fp32; d_work one counter each)
+// ---- zone_eig32.cu: FP32 stages for N <= eig32_max_n() (one block per zone), used by
+// zone_eig_fp32 (same arguments as its stages)
 int eig32_max_n();
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
-                          int32_t* d_work, cudaStream_t st);
+                          cudaStream_t st);
 cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs,
                          int32_t* d_status, cudaStream_t st);
 cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
                           const int32_t* d_nobs, cudaStream_t st);
 cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
-                            float* d_ampl, int32_t* d_status, int32_t* d_work, cudaStream_t st);
+                            float* d_ampl, int32_t* d_status, cudaStream_t st);
 
 // ---- zone_update.cu
 // xa = xf + Sf ampl, Sa = Sf T per zone; zones with nobs == 0 copy (xa = xf, Sa = Sf).

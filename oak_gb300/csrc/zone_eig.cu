@@ -708,7 +708,7 @@ cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z,
 template <>
 cudaError_t launch_e1<float>(int N, int32_t nzc, float* d_GT, float* d_aux,
                              const int32_t* d_nobs, int32_t* d_work, cudaStream_t st) {
-  if (N <= eig32_max_n()) return eig32_tridiag(N, nzc, d_GT, d_aux, d_nobs, d_work, st);
+  if (N <= eig32_max_n()) return eig32_tridiag(N, nzc, d_GT, d_aux, d_nobs, st);
   size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_eig_tridiag<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
@@ -725,7 +725,7 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
                              cudaStream_t st) {
   if (N <= eig32_max_n())
     return eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
-                           d_work, st);
+                           st);
   size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(float) + (size_t)N * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);

@@ -1,28 +1,29 @@
-// Mixed-precision eigensolve kernels for ensembles of up to 64 members: E1 (Householder
-// tridiagonalisation) and E3 (eigenvector orthogonalisation, back-transform, amplitudes and the
-// square-root transform) in FP32, built around register blocking instead of the shared-memory
-// loops of the generic kernels in zone_eig.cu. E2a/E2b (tridiagonal eigenvalues and inverse
-// iteration) are shared with the generic path.
+// Mixed-precision eigensolve kernels for ensembles of up to 64 members, in FP32: E1
+// (Householder tridiagonalisation), E2a (tridiagonal eigenvalues), E2b (inverse iteration) and
+// E3 (back-transform, orthogonalisation, amplitudes and the square-root transform). They replace
+// the generic FP32 kernels of zone_eig.cu for these sizes.
 //
 // The arithmetic follows rrsqrt.F90:136-185 as the generic kernels do (the comment block at the
 // top of zone_eig.cu lists the reference lines); the matrix is padded to 64 x 64 with zeros,
 // which adds decoupled zero rows that no output reads.
 //
-// E1 (one CTA of 256 threads per zone): thread (bi, bj), bi, bj in [0,16), holds the 16
-// elements A[bi + 16a][bj + 16b], a, b in [0,4) of the scaled symmetric matrix in registers.
-//   Column k lives in one half-warp (bj = k mod 16), so the reflector's norm is a half-warp
-//   reduction; p = beta A v is formed as column sums (A is symmetric) reduced over the
-//   half-warp; two CTA barriers per step. Reflector k is stored vector-major, zero padded,
-//   in row k of the zone's matrix slot: slot[k*N + r] = v_k[r] (v_k[r] = 0 for r <= k).
+// Every stage runs one block of 64 threads per zone and keeps a row (E1) or an eigenvector
+// (E3, E2b) of 64 elements per thread in registers, so matrix-vector products need no
+// cross-thread reductions: the shared operand is broadcast with 128-bit shared loads.
 //
-// E3 (one CTA of 256 threads per zone): thread t works on eigenvector j = t/4, components
-//   16 (t mod 4) .. +15, held in registers.
-//   back-transform U = H_0 ... H_{N-3} Z: per reflector a 4-lane dot and an axpy, no barrier;
+// E1: thread r holds row r of the scaled symmetric matrix. Row k equals column k, so thread k
+//   forms reflector k; p = beta A v is one register dot per thread; two barriers per step.
+//   Reflector k is stored vector-major, zero padded, in row k of the zone's matrix slot:
+//   slot[k*N + r] = v_k[r] (v_k[r] = 0 for r <= k).
+// E2a: one thread per zone, implicit QR sweeps (working arrays in shared memory).
+// E2b: thread j = eigenpair j, inverse iteration (LU factor in shared memory).
+// E3: thread j holds eigenvector j.
+//   back-transform U = H_0 ... H_{N-3} Z: per reflector a register dot and axpy, no barrier;
 //   orthogonalisation: right-looking modified Gram-Schmidt, two sweeps, largest eigenvalue
 //     first (a vector is final when every larger-eigenvalue vector has been projected out of
 //     it); a vector that keeps less than half its norm is marked collapsed and replaced, after
 //     the sweeps, by a pseudo-random vector orthogonalised against every accepted one;
-//   T_sym = (U Q)(U Q)^T with Q = diag((1+lambda)^-1/4): 4 x 4 register blocks, 128-bit
+//   T_sym = (U Q)(U Q)^T with Q = diag((1+lambda)^-1/4): 4 x 16 register blocks, 128-bit
 //     shared loads; Omega = RotateVector(w, v) applied to the register blocks in its
 //     reflector form (rank-one updates, matoper.F90:509-535).
 #include <cuda_runtime.h>
@@ -35,512 +36,478 @@ namespace oakg {
 namespace {
 
 constexpr int NB = 64;        // padded ensemble size
-constexpr int kT = 256;       // threads per CTA
 constexpr int LDV = NB + 4;   // row stride of vector-major shared matrices (16-byte rows,
                               // 8 consecutive rows fall in 8 different 16-byte bank groups)
 
 __host__ __device__ inline int aux_stride32(int N) { return 5 * N + 2; }
 
-__device__ __forceinline__ float hsum16(float x) {  // sum over the 16 lanes of a half-warp
-  x += __shfl_xor_sync(0xffffffffu, x, 1);
-  x += __shfl_xor_sync(0xffffffffu, x, 2);
-  x += __shfl_xor_sync(0xffffffffu, x, 4);
-  x += __shfl_xor_sync(0xffffffffu, x, 8);
-  return x;
+__device__ __forceinline__ void vload(float (&x)[NB], const float* p) {
+#pragma unroll
+  for (int c = 0; c < NB; c += 4) {
+    const float4 v = *reinterpret_cast<const float4*>(p + c);
+    x[c] = v.x;
+    x[c + 1] = v.y;
+    x[c + 2] = v.z;
+    x[c + 3] = v.w;
+  }
 }
 
-// sum over the 4 lanes of one vector; only those 4 lanes need to be converged
-__device__ __forceinline__ float qsum4(float x) {
+__device__ __forceinline__ void vstore(const float (&x)[NB], float* p) {
+#pragma unroll
+  for (int c = 0; c < NB; c += 4)
+    *reinterpret_cast<float4*>(p + c) = make_float4(x[c], x[c + 1], x[c + 2], x[c + 3]);
+}
+
+// ------------------------------------------------------------------------------------ E1
+// One block of 64 threads per zone; thread r holds row r of the scaled symmetric matrix in
+// registers (a[c] = A[r][c]). Row k equals column k, so the owner of step k is thread k.
+// Columns at or left of k are not read after step k, so 16-column groups lying entirely there
+// are skipped (the same groups for every thread).
+constexpr int kT1 = 64;
+
+__global__ void __launch_bounds__(kT1, 6)
+    k_eig_tridiag32(int N, int32_t nzc, float* __restrict__ GT, float* __restrict__ aux,
+                    const int32_t* __restrict__ nobs) {
+  // v, p, the partial dots and beta are double-buffered by step parity: the update of step k
+  // re-reads v and p after the second barrier while the owner of step k+1 already writes
+  __shared__ __align__(16) float vbuf2[2][NB];
+  __shared__ __align__(16) float pbuf2[2][NB];
+  __shared__ float red[2][2];
+  __shared__ float s_beta[2];
+  const int r = threadIdx.x, lane = r & 31, warp = r >> 5;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  float* Gz = GT + (int64_t)zl * N * N;
+  float* ax = aux + (int64_t)zl * aux_stride32(N);
+  float a[NB];
+#pragma unroll
+  for (int c = 0; c < NB; c++) a[c] = (r < N && c < N) ? Gz[r * N + c] : 0.f;
+  float amax = 0.f;
+#pragma unroll
+  for (int c = 0; c < NB; c++) amax = fmaxf(amax, fabsf(a[c]));
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if (lane == 0) red[0][warp] = amax;
+  __syncthreads();
+  float scale = fmaxf(red[0][0], red[0][1]);
+  if (!(scale > 0.f) || isinf(scale)) scale = 1.f;
+  const float iscale = 1.f / scale;
+#pragma unroll
+  for (int c = 0; c < NB; c++) a[c] *= iscale;
+  if (r == 0) ax[5 * N] = scale;
+  __syncthreads();  // every row read before reflectors overwrite the slot; red reused
+  for (int k = 0; k < N - 2; k++) {
+    float* vbuf = vbuf2[k & 1];
+    float* pbuf = pbuf2[k & 1];
+    if (r == k) {
+      // reflector of x = A[k+1:, k] = A[k][k+1:]. Single entries are read back through
+      // shared memory: an equality-selected register element would become a dynamic index
+      // and move the whole row to local memory.
+      vstore(a, vbuf);
+      const float x0 = vbuf[k + 1], dk = vbuf[k];
+      float sig = 0.f;
+#pragma unroll
+      for (int c = 0; c < NB; c++)
+        if (c > k + 1) sig = fmaf(a[c], a[c], sig);
+      const float mu = sqrtf(fmaf(x0, x0, sig));
+      const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
+      const float vv = fmaf(v0, v0, sig);
+      const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
+      const float bk = skip ? 0.f : 2.f / vv;
+#pragma unroll
+      for (int c = 0; c < NB; c += 4) {
+        float4 q4;
+        q4.x = (c + 0 > k + 1) ? a[c + 0] : 0.f;
+        q4.y = (c + 1 > k + 1) ? a[c + 1] : 0.f;
+        q4.z = (c + 2 > k + 1) ? a[c + 2] : 0.f;
+        q4.w = (c + 3 > k + 1) ? a[c + 3] : 0.f;
+        *reinterpret_cast<float4*>(vbuf + c) = q4;
+      }
+      vbuf[k + 1] = skip ? x0 : v0;
+      ax[k] = dk;                                          // d_k
+      ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);    // e_k
+      ax[2 * N + k] = bk;                                  // beta_k
+      s_beta[k & 1] = bk;
+    }
+    __syncthreads();  // S1: v and beta published (beta double-buffered by step parity)
+    const float bk = s_beta[k & 1];
+    if (r < N) Gz[(int64_t)k * N + r] = vbuf[r];  // reflector k, vector-major, zero padded
+    if (bk == 0.f) continue;                       // uniform: identity reflector
+    const float vr = vbuf[r];
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      if (16 * g + 15 > k) {  // v vanishes on columns <= k
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          const int c = 16 * g + 4 * m;
+          const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
+          p0 = fmaf(a[c + 0], v4.x, p0);
+          p1 = fmaf(a[c + 1], v4.y, p1);
+          p2 = fmaf(a[c + 2], v4.z, p2);
+          p3 = fmaf(a[c + 3], v4.w, p3);
+        }
+      }
+    }
+    const float p = bk * ((p0 + p1) + (p2 + p3));
+    pbuf[r] = p;
+    float pv = p * vr;
+    for (int o = 16; o > 0; o >>= 1) pv += __shfl_xor_sync(0xffffffffu, pv, o);
+    if (lane == 0) red[k & 1][warp] = pv;
+    __syncthreads();  // S2: p and the partial dots published
+    const float kc = 0.5f * bk * (red[k & 1][0] + red[k & 1][1]);
+    const float wr = fmaf(-kc, vr, p);
+    // A -= v w^T + w v^T, w = p - kc v
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      if (16 * g + 15 > k) {
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          const int c = 16 * g + 4 * m;
+          const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
+          const float4 p4 = *reinterpret_cast<const float4*>(pbuf + c);
+          const float vc[4] = {v4.x, v4.y, v4.z, v4.w};
+          const float pc[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+          for (int t = 0; t < 4; t++) {
+            const float wc = fmaf(-kc, vc[t], pc[t]);
+            a[c + t] = fmaf(-vr, wc, fmaf(-wr, vc[t], a[c + t]));
+          }
+        }
+      }
+    }
+  }
+  // trailing 2 x 2 block (rows read back through shared memory, see above)
+  __syncthreads();  // last step's reads of the buffers done
+  if (r == N - 2) vstore(a, vbuf2[0]);
+  if (r == N - 1) vstore(a, vbuf2[1]);
+  if (r == N - 2) {
+    ax[N - 2] = vbuf2[0][N - 2];
+    ax[2 * N + N - 2] = 0.f;
+  } else if (r == N - 1) {
+    ax[N + N - 2] = vbuf2[1][N - 2];
+    ax[N - 1] = vbuf2[1][N - 1];
+    ax[N + N - 1] = 0.f;
+    ax[2 * N + N - 1] = 0.f;
+  }
+}
+
+// ------------------------------------------------------------------------------------ E3
+// One block of 64 threads per zone; thread j holds eigenvector j (64 components) in
+// registers. Shared matrices are vector-major with 16-byte rows.
+constexpr int kT3 = 64;
+constexpr size_t kSmem3 = (size_t)(2 * NB * LDV + 12 * NB) * sizeof(float);
+
+// u . x over the 16-component groups g >= g0 (the others are zero in u)
+__device__ __forceinline__ float vdot(const float (&x)[NB], const float* u, int g0) {
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+    if (g >= g0) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const int c = 16 * g + 4 * m;
+        const float4 v = *reinterpret_cast<const float4*>(u + c);
+        s0 = fmaf(x[c], v.x, s0);
+        s1 = fmaf(x[c + 1], v.y, s1);
+        s2 = fmaf(x[c + 2], v.z, s2);
+        s3 = fmaf(x[c + 3], v.w, s3);
+      }
+    }
+  }
+  return (s0 + s1) + (s2 + s3);
+}
+
+// x -= f u over the groups g >= g0
+__device__ __forceinline__ void vaxpy(float (&x)[NB], float f, const float* u, int g0) {
+#pragma unroll
+  for (int g = 0; g < 4; g++) {
+    if (g >= g0) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const int c = 16 * g + 4 * m;
+        const float4 v = *reinterpret_cast<const float4*>(u + c);
+        x[c] = fmaf(-f, v.x, x[c]);
+        x[c + 1] = fmaf(-f, v.y, x[c + 1]);
+        x[c + 2] = fmaf(-f, v.z, x[c + 2]);
+        x[c + 3] = fmaf(-f, v.w, x[c + 3]);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ float qsum4(float x) {  // the 4 lanes of one row of T blocks
   const unsigned m = 0xFu << (threadIdx.x & 28);
   x += __shfl_xor_sync(m, x, 1);
   x += __shfl_xor_sync(m, x, 2);
   return x;
 }
 
-// ------------------------------------------------------------------------------------ E1
-template <int KB>
-__device__ __forceinline__ void tridiag_step(int k, int N, float (&A)[4][4], float* vbuf,
-                                             float* pbuf, float* red, float* s_beta, float* Gz,
-                                             float* ax, int tid, int bi, int bj, int warp) {
-  const int kk = k & 15;
-  // (1) reflector of column k (owned by half-warp bj == kk of warp kk/2)
-  if (warp == (kk >> 1)) {
-    const bool mine = (bj == kk);
-    float sig = 0.f, x0 = 0.f;
-    if (mine) {
-#pragma unroll
-      for (int a = 0; a < 4; a++) {
-        const int r = bi + 16 * a;
-        const float x = A[a][KB];
-        if (r > k + 1) sig = fmaf(x, x, sig);
-        if (r == k + 1) x0 = x;
-      }
-    }
-    sig = hsum16(sig);
-    x0 = hsum16(x0);
-    const float mu = sqrtf(fmaf(x0, x0, sig));
-    const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
-    const float vv = fmaf(v0, v0, sig);
-    const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
-    const float bk = skip ? 0.f : 2.f / vv;
-    if (mine) {
-#pragma unroll
-      for (int a = 0; a < 4; a++) {
-        const int r = bi + 16 * a;
-        const float val = (r > k + 1) ? A[a][KB] : ((r == k + 1) ? (skip ? x0 : v0) : 0.f);
-        vbuf[r] = val;
-        if (r < N) Gz[(int64_t)k * N + r] = val;
-        if (r == k) ax[k] = A[a][KB];  // d_k
-      }
-      if (bi == 0) {
-        ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);  // e_k
-        ax[2 * N + k] = bk;                                 // beta_k
-        s_beta[k & 1] = bk;
-      }
-    }
-  }
-  __syncthreads();  // S1: v and beta published
-  // beta is double-buffered by step parity: after an identity step (no S2) the next step's
-  // owner may already write its beta while slower warps still read this one
-  const float bk = s_beta[k & 1];
-  if (bk == 0.f) return;  // uniform: identity reflector
-  float vr[4], vc[4];
-#pragma unroll
-  for (int a = 0; a < 4; a++) vr[a] = vbuf[bi + 16 * a];
-#pragma unroll
-  for (int b = 0; b < 4; b++) vc[b] = vbuf[bj + 16 * b];
-  // p_c = beta sum_r A[r][c] v_r (column sums; A symmetric), reduced over the half-warp
-  float q[4];
-#pragma unroll
-  for (int b = 0; b < 4; b++) {
-    float s = A[0][b] * vr[0];
-    s = fmaf(A[1][b], vr[1], s);
-    s = fmaf(A[2][b], vr[2], s);
-    s = fmaf(A[3][b], vr[3], s);
-    q[b] = hsum16(s) * bk;
-  }
-  float pv = 0.f;
-  if (bi == 0) {
-#pragma unroll
-    for (int b = 0; b < 4; b++) {
-      pbuf[bj + 16 * b] = q[b];
-      pv = fmaf(q[b], vc[b], pv);
-    }
-  }
-  pv += __shfl_xor_sync(0xffffffffu, pv, 16);
-  if ((tid & 31) == 0) red[warp] = pv;
-  __syncthreads();  // S2: p and the partial dots published
-  float kc = 0.f;
-#pragma unroll
-  for (int w = 0; w < kT / 32; w++) kc += red[w];
-  kc *= 0.5f * bk;
-  float wr[4], wc[4];
-#pragma unroll
-  for (int a = 0; a < 4; a++) wr[a] = fmaf(-kc, vr[a], pbuf[bi + 16 * a]);
-#pragma unroll
-  for (int b = 0; b < 4; b++) wc[b] = fmaf(-kc, vc[b], pbuf[bj + 16 * b]);
-  // A -= v w^T + w v^T
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int b = 0; b < 4; b++) A[a][b] = fmaf(-vr[a], wc[b], fmaf(-wr[a], vc[b], A[a][b]));
-}
-
-__global__ void __launch_bounds__(kT, 4)
-    k_eig_tridiag32(int N, int32_t nzc, float* __restrict__ GT, float* __restrict__ aux,
-                    const int32_t* __restrict__ nobs, int32_t* __restrict__ work) {
-  __shared__ __align__(16) float vbuf[NB];
-  __shared__ __align__(16) float pbuf[NB];
-  __shared__ float red[kT / 32];
-  __shared__ float s_beta[2];
-  __shared__ int32_t s_zone;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int bi = tid & 15, bj = tid >> 4;
-  for (;;) {
-    if (tid == 0) s_zone = atomicAdd(work, 1);
-    __syncthreads();
-    const int32_t zl = s_zone;
-    if (zl >= nzc) break;
-    if (nobs[zl] == 0) {
-      __syncthreads();
-      continue;
-    }
-    float* Gz = GT + (int64_t)zl * N * N;
-    float* ax = aux + (int64_t)zl * aux_stride32(N);
-    float A[4][4];
-    float amax = 0.f;
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int b = 0; b < 4; b++) {
-        const int r = bi + 16 * a, c = bj + 16 * b;
-        const float gval = (r < N && c < N) ? Gz[r * N + c] : 0.f;
-        A[a][b] = gval;
-        amax = fmaxf(amax, fabsf(gval));
-      }
-    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    if ((tid & 31) == 0) red[warp] = amax;
-    __syncthreads();
-    float scale = 0.f;
-#pragma unroll
-    for (int w = 0; w < kT / 32; w++) scale = fmaxf(scale, red[w]);
-    if (!(scale > 0.f) || isinf(scale)) scale = 1.f;
-    const float iscale = 1.f / scale;
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int b = 0; b < 4; b++) A[a][b] *= iscale;
-    if (tid == 0) ax[5 * N] = scale;
-    __syncthreads();  // red reused below; the slot is overwritten by reflectors from here on
-    const int ksteps = N - 2;
-#pragma unroll 1
-    for (int k = 0; k < ksteps && k < 16; k++)
-      tridiag_step<0>(k, N, A, vbuf, pbuf, red, s_beta, Gz, ax, tid, bi, bj, warp);
-#pragma unroll 1
-    for (int k = 16; k < ksteps && k < 32; k++)
-      tridiag_step<1>(k, N, A, vbuf, pbuf, red, s_beta, Gz, ax, tid, bi, bj, warp);
-#pragma unroll 1
-    for (int k = 32; k < ksteps && k < 48; k++)
-      tridiag_step<2>(k, N, A, vbuf, pbuf, red, s_beta, Gz, ax, tid, bi, bj, warp);
-#pragma unroll 1
-    for (int k = 48; k < ksteps; k++)
-      tridiag_step<3>(k, N, A, vbuf, pbuf, red, s_beta, Gz, ax, tid, bi, bj, warp);
-    // trailing 2 x 2 block
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int b = 0; b < 4; b++) {
-        const int r = bi + 16 * a, c = bj + 16 * b;
-        if (c == N - 2 && r == N - 2) ax[N - 2] = A[a][b];
-        if (c == N - 2 && r == N - 1) ax[N + N - 2] = A[a][b];
-        if (c == N - 1 && r == N - 1) ax[N - 1] = A[a][b];
-      }
-    if (tid == 0) {
-      ax[N + N - 1] = 0.f;
-      ax[2 * N + N - 2] = 0.f;
-      ax[2 * N + N - 1] = 0.f;
-    }
-    __syncthreads();
-  }
-}
-
-// ------------------------------------------------------------------------------------ E3
-__device__ __forceinline__ float dot16(const float (&x)[16], const float* p) {
-  const float4* p4 = reinterpret_cast<const float4*>(p);
-  float s[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    const float4 v = p4[m];
-    s[m] = fmaf(x[4 * m + 0], v.x, s[m]);
-    s[m] = fmaf(x[4 * m + 1], v.y, s[m]);
-    s[m] = fmaf(x[4 * m + 2], v.z, s[m]);
-    s[m] = fmaf(x[4 * m + 3], v.w, s[m]);
-  }
-  return (s[0] + s[1]) + (s[2] + s[3]);
-}
-
-__device__ __forceinline__ void axpy16(float (&x)[16], float f, const float* p) {
-  const float4* p4 = reinterpret_cast<const float4*>(p);
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    const float4 v = p4[m];
-    x[4 * m + 0] = fmaf(-f, v.x, x[4 * m + 0]);
-    x[4 * m + 1] = fmaf(-f, v.y, x[4 * m + 1]);
-    x[4 * m + 2] = fmaf(-f, v.z, x[4 * m + 2]);
-    x[4 * m + 3] = fmaf(-f, v.w, x[4 * m + 3]);
-  }
-}
-
-__device__ __forceinline__ void store16(const float (&x)[16], float* p) {
-  float4* p4 = reinterpret_cast<float4*>(p);
-#pragma unroll
-  for (int m = 0; m < 4; m++)
-    p4[m] = make_float4(x[4 * m + 0], x[4 * m + 1], x[4 * m + 2], x[4 * m + 3]);
-}
-
-__device__ __forceinline__ void load16(float (&x)[16], const float* p) {
-  const float4* p4 = reinterpret_cast<const float4*>(p);
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    const float4 v = p4[m];
-    x[4 * m + 0] = v.x;
-    x[4 * m + 1] = v.y;
-    x[4 * m + 2] = v.z;
-    x[4 * m + 3] = v.w;
-  }
-}
-
-constexpr size_t kSmem3 = (size_t)(2 * NB * LDV + 12 * NB) * sizeof(float);
-
-__global__ void __launch_bounds__(kT, 4)
+__global__ void __launch_bounds__(kT3, 6)
     k_eig_transform32(int N, int32_t nzc, float* __restrict__ GT, const float* __restrict__ aux,
                       const float* __restrict__ Zg, const float* __restrict__ gv,
                       const int32_t* __restrict__ nobs, int rotate, float* __restrict__ ampl_out,
-                      int32_t* __restrict__ status, int32_t* __restrict__ work) {
+                      int32_t* __restrict__ status) {
   extern __shared__ __align__(16) float sm[];
-  float* Vs = sm;               // [NB][LDV] reflectors, vector-major, zero padded
-  float* Us = Vs + NB * LDV;    // [NB][LDV] eigenvectors (vector-major), later Q-scaled
+  float* Vs = sm;               // [NB][LDV] reflectors (vector-major, zero padded)
+  float* Us = Vs + NB * LDV;    // [NB][LDV] Z, eigenvectors, then W = U diag(lambda'^1/4)
   float* lam = Us + NB * LDV;   // [NB] 1/(1+lambda)            (evaluated in FP64)
   float* sq = lam + NB;         // [NB] (1+lambda)^-1/2         (evaluated in FP64)
   float* qs = sq + NB;          // [NB] (1+lambda)^-1/4         (evaluated in FP64)
   float* gs = qs + NB;          // [NB] g
   float* bet = gs + NB;         // [NB] Householder scalars
-  float* tt = bet + NB;         // [NB] lambda' .* (U^T g)
-  float* cc = tt + NB;          // [NB] colsum(U) / sqrt(lambda')
+  float* tt = bet + NB;         // [NB] lambda' (u_j . g)
+  float* cc = tt + NB;          // [NB] colsum(u_j) / sqrt(lambda')
   float* vv = cc + NB;          // [NB] v (unnormalised)
   float* t0 = vv + NB;          // [NB] scratch
   int* flag = reinterpret_cast<int*>(t0 + NB);  // [NB] 1 accepted, 0 collapsed
-  __shared__ float red[kT / 32];
-  __shared__ int32_t s_zone;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int j = tid >> 2, q = tid & 3;  // eigenvector j, components 16q .. 16q + 15
-  for (;;) {
-    if (tid == 0) s_zone = atomicAdd(work, 1);
-    __syncthreads();
-    const int32_t zl = s_zone;
-    if (zl >= nzc) break;
-    if (nobs[zl] == 0) {
+  __shared__ float red[2];
+  const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  float* Gz = GT + (int64_t)zl * N * N;
+  const float* ax = aux + (int64_t)zl * aux_stride32(N);
+  const float* Zz = Zg + (int64_t)zl * N * N;
+  for (int idx = j; idx < NB * NB; idx += kT3) {
+    const int k = idx >> 6, c = idx & (NB - 1);
+    Vs[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
+    Us[k * LDV + c] = (k < N) ? ((c < N) ? Zz[k * N + c] : 0.f) : ((c == k) ? 1.f : 0.f);
+  }
+  {
+    double l = (j < N) ? (double)ax[3 * N + j] : 0.0;
+    if (l < 0.0) l = 0.0;
+    const double li = 1.0 / (1.0 + l);
+    const double s = sqrt(li);
+    lam[j] = (float)li;
+    sq[j] = (float)s;
+    qs[j] = (float)sqrt(s);
+    gs[j] = (j < N) ? gv[(int64_t)zl * N + j] : 0.f;
+    bet[j] = (j < N - 2) ? ax[2 * N + j] : 0.f;
+    flag[j] = 1;
+  }
+  __syncthreads();
+  float x[NB];
+  vload(x, Us + j * LDV);
+  // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k)
+  for (int k = N - 3; k >= 0; k--) {
+    const float bk = bet[k];
+    if (bk == 0.f) continue;  // uniform
+    const float* vk = Vs + k * LDV;
+    const int g0 = (k + 1) >> 4;
+    const float s = vdot(x, vk, g0);
+    vaxpy(x, bk * s, vk, g0);
+  }
+  // modified Gram-Schmidt, two sweeps, largest eigenvalue first: vector c is final once every
+  // larger-eigenvalue vector has been projected out of it; a vector keeping less than half its
+  // norm is marked collapsed (replaced below)
+  for (int sweep = 0; sweep < 2; sweep++) {
+    for (int c = N - 1; c >= 0; c--) {
+      if (j == c) {
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i < NB; i += 2) {
+          s0 = fmaf(x[i], x[i], s0);
+          s1 = fmaf(x[i + 1], x[i + 1], s1);
+        }
+        const float s = s0 + s1;
+        const bool ok = flag[c] && (s >= 0.5f);
+        const float sc = ok ? rsqrtf(s) : 0.f;
+#pragma unroll
+        for (int i = 0; i < NB; i++) x[i] *= sc;
+        vstore(x, Us + c * LDV);
+        if (!ok) flag[c] = 0;
+      }
       __syncthreads();
-      continue;
-    }
-    float* Gz = GT + (int64_t)zl * N * N;
-    const float* ax = aux + (int64_t)zl * aux_stride32(N);
-    for (int idx = tid; idx < NB * NB; idx += kT) {
-      const int k = idx >> 6, r = idx & (NB - 1);
-      Vs[k * LDV + r] = (k < N - 2 && r < N) ? Gz[k * N + r] : 0.f;
-    }
-    if (tid < NB) {
-      const int i = tid;
-      double l = (i < N) ? (double)ax[3 * N + i] : 0.0;
-      if (l < 0.0) l = 0.0;
-      const double li = 1.0 / (1.0 + l);
-      const double s = sqrt(li);
-      lam[i] = (float)li;
-      sq[i] = (float)s;
-      qs[i] = (float)sqrt(s);
-      gs[i] = (i < N) ? gv[(int64_t)zl * N + i] : 0.f;
-      bet[i] = (i < N - 2) ? ax[2 * N + i] : 0.f;
-      flag[i] = 1;
-    }
-    float x[16];
-    {
-      const float* zj = Zg + (int64_t)zl * N * N + (int64_t)j * N;
-#pragma unroll
-      for (int i = 0; i < 16; i++) {
-        const int r = 16 * q + i;
-        x[i] = (j < N) ? ((r < N) ? zj[r] : 0.f) : ((r == j) ? 1.f : 0.f);
+      if (j < c && flag[c]) {
+        const float* uc = Us + c * LDV;
+        const float d = vdot(x, uc, 0);
+        vaxpy(x, d, uc, 0);
       }
     }
-    __syncthreads();
-    // back-transform: U = H_0 H_1 ... H_{N-3} Z, applied right to left
-    for (int k = N - 3; k >= 0; k--) {
-      const float bk = bet[k];
-      if (bk == 0.f) continue;  // uniform
-      const float* vk = Vs + k * LDV + 16 * q;
-      const float s = qsum4(dot16(x, vk));
-      axpy16(x, bk * s, vk);
-    }
-    // modified Gram-Schmidt, two sweeps, largest eigenvalue first
-    for (int sweep = 0; sweep < 2; sweep++) {
-      for (int c = N - 1; c >= 0; c--) {
-        if (j == c) {
+  }
+  int ncol = 0;
+  if (j < N) ncol = (flag[j] == 0);
+  ncol = __syncthreads_or(ncol);
+  if (ncol) {
+    // complement fill (rare): a collapsed vector is replaced by a pseudo-random vector made
+    // orthogonal (two classical Gram-Schmidt passes) to every accepted eigenvector
+    for (int c = 0; c < N; c++) {
+      if (flag[c]) continue;  // uniform
+      {
+        unsigned h = (unsigned)j * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
+        h ^= h >> 15;
+        h *= 2654435761u;
+        h ^= h >> 13;
+        Us[c * LDV + j] =
+            (j < N) ? (float)((double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5) : 0.f;
+      }
+      __syncthreads();
+      for (int pass = 0; pass < 2; pass++) {
+        {
           float s = 0.f;
-#pragma unroll
-          for (int i = 0; i < 16; i++) s = fmaf(x[i], x[i], s);
-          s = qsum4(s);
-          const bool ok = flag[c] && (s >= 0.5f);
-          const float sc = ok ? rsqrtf(s) : 0.f;
-#pragma unroll
-          for (int i = 0; i < 16; i++) x[i] *= sc;
-          store16(x, Us + c * LDV + 16 * q);
-          if (q == 0 && !ok) flag[c] = 0;
+          if (j < N && j != c && flag[j])
+            for (int i = 0; i < N; i++) s = fmaf(Us[j * LDV + i], Us[c * LDV + i], s);
+          t0[j] = s;
         }
         __syncthreads();
-        if (j < c && flag[c]) {
-          const float* uc = Us + c * LDV + 16 * q;
-          const float d = qsum4(dot16(x, uc));
-          axpy16(x, d, uc);
-        }
-      }
-    }
-    int ncol = 0;
-    for (int i = tid; i < N; i += kT) ncol += (flag[i] == 0);
-    ncol = __syncthreads_or(ncol);
-    if (ncol) {
-      // complement fill (rare): a collapsed vector is replaced by a pseudo-random vector made
-      // orthogonal (two classical Gram-Schmidt passes) to every accepted eigenvector
-      for (int c = 0; c < N; c++) {
-        if (flag[c]) continue;  // uniform
-        for (int r = tid; r < NB; r += kT) {
-          unsigned h = (unsigned)r * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
-          h ^= h >> 15;
-          h *= 2654435761u;
-          h ^= h >> 13;
-          Us[c * LDV + r] = (r < N) ? (float)((double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5)
-                                    : 0.f;
-        }
-        __syncthreads();
-        for (int pass = 0; pass < 2; pass++) {
-          for (int k = tid; k < N; k += kT) {
-            float s = 0.f;
-            if (k != c && flag[k])
-              for (int r = 0; r < N; r++) s = fmaf(Us[k * LDV + r], Us[c * LDV + r], s);
-            t0[k] = s;
-          }
+        {
+          float s = Us[c * LDV + j];
+          for (int k = 0; k < N; k++) s = fmaf(-t0[k], Us[k * LDV + j], s);
           __syncthreads();
-          for (int r = tid; r < N; r += kT) {
-            float s = Us[c * LDV + r];
-            for (int k = 0; k < N; k++) s = fmaf(-t0[k], Us[k * LDV + r], s);
-            Us[c * LDV + r] = s;
-          }
-          __syncthreads();
-        }
-        if (warp == 0) {
-          float s = 0.f;
-          for (int r = lane; r < N; r += 32) s = fmaf(Us[c * LDV + r], Us[c * LDV + r], s);
-          for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-          if (lane == 0) {
-            red[0] = (s > 0.f) ? rsqrtf(s) : 0.f;
-            flag[c] = 1;
-          }
+          Us[c * LDV + j] = s;
         }
         __syncthreads();
-        const float sc = red[0];
-        for (int r = tid; r < NB; r += kT) Us[c * LDV + r] *= sc;
+      }
+      {
+        const float u = Us[c * LDV + j];
+        float s = u * u;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[warp] = s;
+        __syncthreads();
+        const float tot = red[0] + red[1];
+        Us[c * LDV + j] = u * ((tot > 0.f) ? rsqrtf(tot) : 0.f);
+        if (j == 0) flag[c] = 1;
         __syncthreads();
       }
-      if (j < N) load16(x, Us + j * LDV + 16 * q);
     }
-    // per-vector scalars: lambda' (u_j . g) and colsum(u_j) / sqrt(lambda')
-    {
-      float y = dot16(x, gs + 16 * q);
-      float cs = 0.f;
+    vload(x, Us + j * LDV);
+  }
+  // per-vector scalars: lambda' (u_j . g), colsum(u_j) / sqrt(lambda')
+  {
+    const float y = vdot(x, gs, 0);
+    float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-      for (int i = 0; i < 16; i++) cs += x[i];
-      y = qsum4(y);
-      cs = qsum4(cs);
-      if (q == 0) {
-        tt[j] = (j < N) ? lam[j] * y : 0.f;
-        cc[j] = (j < N) ? cs / sq[j] : 0.f;
-      }
+    for (int i = 0; i < NB; i += 2) {
+      s0 += x[i];
+      s1 += x[i + 1];
     }
-    __syncthreads();
-    // ampl = U tt, v = U cc (one thread per component)
-    int nan_flag = 0;
-    if (tid < NB) {
-      const int r = tid;
-      float s = 0.f;
-      for (int jj = 0; jj < N; jj++) s = fmaf(Us[jj * LDV + r], tt[jj], s);
-      if (r < N) {
-        ampl_out[(int64_t)zl * N + r] = s;
-        if (!(s == s) || isinf(s)) nan_flag = 1;
-      }
-    } else if (tid < 2 * NB && rotate) {
-      const int r = tid - NB;
-      float s = 0.f;
-      for (int jj = 0; jj < N; jj++) s = fmaf(Us[jj * LDV + r], cc[jj], s);
-      vv[r] = (r < N) ? s : 0.f;
-    }
-    nan_flag = __syncthreads_or(nan_flag);
-    // W = U Q into Us (every vector, the padding ones included)
-    {
-      const float qj = qs[j];
-#pragma unroll
-      for (int i = 0; i < 16; i++) x[i] *= qj;
-      store16(x, Us + j * LDV + 16 * q);
-    }
-    if (rotate && warp == 0) {
-      float s = 0.f;
-      for (int r = lane; r < N; r += 32) s = fmaf(vv[r], vv[r], s);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) red[0] = 1.f / sqrtf(s);
-    }
-    __syncthreads();
-    // T_sym = W W^T, rows 4ab .. 4ab+3, columns 4bb .. 4bb+3 per thread
-    const int ab = tid >> 4, bb = tid & 15;
-    float T[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) T[i][c] = 0.f;
-#pragma unroll 4
+    tt[j] = (j < N) ? lam[j] * y : 0.f;
+    cc[j] = (j < N) ? (s0 + s1) / sq[j] : 0.f;
+  }
+  __syncthreads();
+  // ampl = U tt, v = U cc (thread j: component j)
+  int nan_flag = 0;
+  {
+    float sa = 0.f, sv = 0.f;
     for (int jj = 0; jj < N; jj++) {
-      const float4 wa = *reinterpret_cast<const float4*>(Us + jj * LDV + 4 * ab);
-      const float4 wb = *reinterpret_cast<const float4*>(Us + jj * LDV + 4 * bb);
-      const float ra[4] = {wa.x, wa.y, wa.z, wa.w};
-      const float rb[4] = {wb.x, wb.y, wb.z, wb.w};
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) T[i][c] = fmaf(ra[i], rb[c], T[i][c]);
+      const float u = Us[jj * LDV + j];
+      sa = fmaf(u, tt[jj], sa);
+      sv = fmaf(u, cc[jj], sv);
     }
+    if (j < N) {
+      ampl_out[(int64_t)zl * N + j] = sa;
+      if (!(sa == sa) || isinf(sa)) nan_flag = 1;
+    }
+    vv[j] = (j < N) ? sv : 0.f;
+  }
+  nan_flag = __syncthreads_or(nan_flag);
+  {
+    const float qj = qs[j];
+#pragma unroll
+    for (int i = 0; i < NB; i++) x[i] *= qj;
+    vstore(x, Us + j * LDV);  // W = U diag(qs); padding vectors stay unit vectors
     if (rotate) {
-      // Omega = P_v P_w + (1 - s_v s_w) v w^T with P_x = I - u_x u_x^T / (1 + |x_N|),
-      // u_x = x + sign(x_N) e_N, w = 1/sqrt(N) (s_w = +1)
-      const float inv = red[0];
-      const float vN = vv[N - 1] * inv;
-      const float sv = signbit(vN) ? -1.f : 1.f;
-      const float icv = 1.f / (1.f + fabsf(vN));
-      const float wv = (float)(1.0 / sqrt((double)N));
-      const float icw = 1.f / (1.f + wv);
-      float uv[4], vn[4], uw[4];
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int col = 4 * bb + c;
-        const bool in = col < N;
-        vn[c] = in ? vv[col] * inv : 0.f;
-        uv[c] = vn[c] + ((col == N - 1) ? sv : 0.f);
-        uw[c] = in ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
-      }
-      float pa[4], pb[4], pg[4];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        float sa = 0.f, sb = 0.f;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          sa = fmaf(T[i][c], uv[c], sa);
-          sb = fmaf(T[i][c], vn[c], sb);
-        }
-        pa[i] = hsum16(sa);  // (T_sym u_v)_row
-        pb[i] = hsum16(sb);  // (T_sym v)_row
-      }
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) T[i][c] = fmaf(-pa[i] * icv, uv[c], T[i][c]);
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        float s = 0.f;
-#pragma unroll
-        for (int c = 0; c < 4; c++) s = fmaf(T[i][c], uw[c], s);
-        pg[i] = hsum16(s) * icw;
-      }
-      const float extra = 1.f - sv;
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          float t = fmaf(-pg[i], uw[c], T[i][c]);
-          if (extra != 0.f && 4 * bb + c < N) t = fmaf(extra * pb[i], wv, t);
-          T[i][c] = t;
-        }
+      float s = (j < N) ? vv[j] * vv[j] : 0.f;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) red[warp] = s;
     }
+  }
+  __syncthreads();
+  // T_sym = W W^T: thread (rb, cb) = (j / 4, j % 4) computes rows 4 rb .. 4 rb + 3 and the
+  // columns of 16-byte chunks cb, cb + 4, cb + 8, cb + 12 (interleaved: conflict-free loads)
+  const int rb = j >> 2, cb = j & 3;
+  float T[4][16];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int c = 0; c < 16; c++) T[i][c] = 0.f;
+#pragma unroll 2
+  for (int jj = 0; jj < N; jj++) {
+    const float* w = Us + jj * LDV;
+    const float4 wa = *reinterpret_cast<const float4*>(w + 4 * rb);
+    const float ra[4] = {wa.x, wa.y, wa.z, wa.w};
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const float4 wb = *reinterpret_cast<const float4*>(w + 4 * (cb + 4 * m));
+      const float rbv[4] = {wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int t = 0; t < 4; t++) T[i][4 * m + t] = fmaf(ra[i], rbv[t], T[i][4 * m + t]);
+    }
+  }
+  if (rotate) {
+    // Omega = P_v P_w + (1 - s_v s_w) v w^T with P_x = I - u_x u_x^T / (1 + |x_N|),
+    // u_x = x + sign(x_N) e_N, w = 1/sqrt(N) (s_w = +1)  (matoper.F90:509-535)
+    const float inv = 1.f / sqrtf(red[0] + red[1]);
+    const float vN = vv[N - 1] * inv;
+    const float sv = signbit(vN) ? -1.f : 1.f;
+    const float icv = 1.f / (1.f + fabsf(vN));
+    const float wv = (float)(1.0 / sqrt((double)N));
+    const float icw = 1.f / (1.f + wv);
+    float pa[4], pb[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-      const int row = 4 * ab + i;
-      if (row >= N) continue;
+      float sa = 0.f, sb = 0.f;
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int col = 4 * (cb + 4 * m) + t;
+          const float vn = (col < N) ? vv[col] * inv : 0.f;
+          const float uv = vn + ((col == N - 1) ? sv : 0.f);
+          sa = fmaf(T[i][4 * m + t], uv, sa);
+          sb = fmaf(T[i][4 * m + t], vn, sb);
+        }
+      pa[i] = qsum4(sa) * icv;  // (T_sym u_v)_row / c_v
+      pb[i] = qsum4(sb);        // (T_sym v)_row
+    }
+    const float extra = 1.f - sv;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      float sg = 0.f;
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int col = 4 * (cb + 4 * m) + t;
+          const float vn = (col < N) ? vv[col] * inv : 0.f;
+          const float uv = vn + ((col == N - 1) ? sv : 0.f);
+          const float uw = (col < N) ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
+          const float t1 = fmaf(-pa[i], uv, T[i][4 * m + t]);  // T1 = T_sym - t0 u_v^T / c_v
+          T[i][4 * m + t] = t1;
+          sg = fmaf(t1, uw, sg);
+        }
+      const float g = qsum4(sg) * icw;  // (T1 u_w)_row / c_w
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int col = 4 * (cb + 4 * m) + t;
+          const float uw = (col < N) ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
+          float tv = fmaf(-g, uw, T[i][4 * m + t]);
+          if (extra != 0.f && col < N) tv = fmaf(extra * pb[i], wv, tv);
+          T[i][4 * m + t] = tv;
+        }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int row = 4 * rb + i;
+    if (row >= N) continue;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const int col = 4 * (cb + 4 * m);
       if (N == NB) {
-        *reinterpret_cast<float4*>(Gz + row * N + 4 * bb) =
-            make_float4(T[i][0], T[i][1], T[i][2], T[i][3]);
+        *reinterpret_cast<float4*>(Gz + row * N + col) =
+            make_float4(T[i][4 * m], T[i][4 * m + 1], T[i][4 * m + 2], T[i][4 * m + 3]);
       } else {
 #pragma unroll
-        for (int c = 0; c < 4; c++)
-          if (4 * bb + c < N) Gz[row * N + 4 * bb + c] = T[i][c];
+        for (int t = 0; t < 4; t++)
+          if (col + t < N) Gz[row * N + col + t] = T[i][4 * m + t];
       }
     }
-    if (tid == 0 && nan_flag) status[zl] |= ZST_NAN;
-    __syncthreads();
   }
+  if (j == 0 && nan_flag) status[zl] |= ZST_NAN;
 }
 
 // ------------------------------------------------------------------------------------ E2a
@@ -765,17 +732,6 @@ __global__ void __launch_bounds__(kT2)
   }
 }
 
-int grid32(const void* fn, size_t smem, int32_t nzc) {
-  int bps = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, kT, smem);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int grid = sms * (bps > 0 ? bps : 1);
-  if (grid > nzc) grid = nzc > 0 ? nzc : 1;
-  return grid;
-}
-
 }  // namespace
 
 int eig32_max_n() { return NB; }
@@ -795,23 +751,21 @@ cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
 }
 
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
-                          int32_t* d_work, cudaStream_t st) {
+                          cudaStream_t st) {
   if (N < 2 || N > NB) return cudaErrorInvalidValue;
-  k_eig_tridiag32<<<grid32((const void*)k_eig_tridiag32, 0, nzc), kT, 0, st>>>(N, nzc, d_GT,
-                                                                               d_aux, d_nobs,
-                                                                               d_work);
+  k_eig_tridiag32<<<nzc > 0 ? nzc : 1, kT1, 0, st>>>(N, nzc, d_GT, d_aux, d_nobs);
   return cudaGetLastError();
 }
 
 cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
-                            float* d_ampl, int32_t* d_status, int32_t* d_work, cudaStream_t st) {
+                            float* d_ampl, int32_t* d_status, cudaStream_t st) {
   if (N < 2 || N > NB) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform32,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem3);
   if (e != cudaSuccess) return e;
-  k_eig_transform32<<<grid32((const void*)k_eig_transform32, kSmem3, nzc), kT, kSmem3, st>>>(
-      N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, d_work);
+  k_eig_transform32<<<nzc > 0 ? nzc : 1, kT3, kSmem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
+                                                            d_nobs, rotate, d_ampl, d_status);
   return cudaGetLastError();
 }
 
