@@ -19,10 +19,11 @@
 // E2b: thread j = eigenpair j, inverse iteration (LU factor in shared memory).
 // E3: thread j holds eigenvector j.
 //   back-transform U = H_0 ... H_{N-3} Z: per reflector a register dot and axpy, no barrier;
-//   orthogonalisation: right-looking modified Gram-Schmidt, two sweeps, largest eigenvalue
-//     first (a vector is final when every larger-eigenvalue vector has been projected out of
-//     it); a vector that keeps less than half its norm is marked collapsed and replaced, after
-//     the sweeps, by a pseudo-random vector orthogonalised against every accepted one;
+//   orthogonalisation: right-looking modified Gram-Schmidt, largest eigenvalue first (a vector
+//     is final when every larger-eigenvalue vector has been projected out of it); a vector that
+//     keeps at least half its squared norm is accepted after this one projection (Kahan-Parlett
+//     "twice is enough"), one that does not is marked collapsed and replaced by a
+//     pseudo-random vector orthogonalised (two passes) against every accepted one;
 //   T_sym = (U Q)(U Q)^T with Q = diag((1+lambda)^-1/4): 4 x 16 register blocks, 128-bit
 //     shared loads; Omega = RotateVector(w, v) applied to the register blocks in its
 //     reflector form (rank-one updates, matoper.F90:509-535).
@@ -267,10 +268,30 @@ __global__ void __launch_bounds__(kT3, 6)
   float* Gz = GT + (int64_t)zl * N * N;
   const float* ax = aux + (int64_t)zl * aux_stride32(N);
   const float* Zz = Zg + (int64_t)zl * N * N;
-  for (int idx = j; idx < NB * NB; idx += kT3) {
-    const int k = idx >> 6, c = idx & (NB - 1);
-    Vs[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
-    Us[k * LDV + c] = (k < N) ? ((c < N) ? Zz[k * N + c] : 0.f) : ((c == k) ? 1.f : 0.f);
+  if (N == NB) {
+    // 16 float4 of each matrix per thread, all loads issued before the stores
+    float4 vq[16], zq[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int idx4 = j + kT3 * i;  // float4 index in the 64 x 64 matrix
+      const int k = idx4 >> 4;
+      vq[i] = (k < N - 2) ? reinterpret_cast<const float4*>(Gz)[idx4] : make_float4(0, 0, 0, 0);
+      zq[i] = reinterpret_cast<const float4*>(Zz)[idx4];
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int idx4 = j + kT3 * i;
+      const int k = idx4 >> 4, c = (idx4 & 15) * 4;
+      *reinterpret_cast<float4*>(Vs + k * LDV + c) = vq[i];
+      *reinterpret_cast<float4*>(Us + k * LDV + c) = zq[i];
+    }
+  } else {
+#pragma unroll 8
+    for (int idx = j; idx < NB * NB; idx += kT3) {
+      const int k = idx >> 6, c = idx & (NB - 1);
+      Vs[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
+      Us[k * LDV + c] = (k < N) ? ((c < N) ? Zz[k * N + c] : 0.f) : ((c == k) ? 1.f : 0.f);
+    }
   }
   {
     double l = (j < N) ? (double)ax[3 * N + j] : 0.0;
@@ -296,10 +317,12 @@ __global__ void __launch_bounds__(kT3, 6)
     const float s = vdot(x, vk, g0);
     vaxpy(x, bk * s, vk, g0);
   }
-  // modified Gram-Schmidt, two sweeps, largest eigenvalue first: vector c is final once every
-  // larger-eigenvalue vector has been projected out of it; a vector keeping less than half its
-  // norm is marked collapsed (replaced below)
-  for (int sweep = 0; sweep < 2; sweep++) {
+  // modified Gram-Schmidt, largest eigenvalue first: vector c is final once every
+  // larger-eigenvalue vector has been projected out of it. A vector that keeps at least half its
+  // squared norm (a norm drop below sqrt(2)) is orthogonal to working precision after this one
+  // projection ("twice is enough", Kahan-Parlett; Parlett, The Symmetric Eigenvalue Problem,
+  // 6-9); one that does not is marked collapsed and replaced below.
+  {
     for (int c = N - 1; c >= 0; c--) {
       if (j == c) {
         float s0 = 0.f, s1 = 0.f;
@@ -570,9 +593,16 @@ __global__ void __launch_bounds__(kT2)
     const float mu = (den == 0.f) ? b : b - f * f / den;
     float dk = d[lo * kT2], ek = e[lo * kT2], ep = 0.f;  // d[k], e[k], e[k-1] (running)
     float x = dk - mu, z = ek, bulge = 0.f;
+    // d[k+1], e[k+1] are loaded one rotation ahead (they are not written before use)
+    float dk1n = d[(lo + 1) * kT2];
+    float ek1n = (lo + 1 < hi) ? e[(lo + 1) * kT2] : 0.f;
     for (int k = lo; k < hi; k++) {
-      const float dk1 = d[(k + 1) * kT2];
-      const float ek1 = (k + 1 < hi) ? e[(k + 1) * kT2] : 0.f;
+      const float dk1 = dk1n;
+      const float ek1 = ek1n;
+      if (k + 2 <= hi) {
+        dk1n = d[(k + 2) * kT2];
+        ek1n = (k + 2 < hi) ? e[(k + 2) * kT2] : 0.f;
+      }
       if (k > lo) {
         x = ep;
         z = bulge;
