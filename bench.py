@@ -316,11 +316,31 @@ def main():
         a1.record(stream)
         torch.cuda.synchronize(dev)
         ams = a0.elapsed_time(a1) / args.steps
+        # worst case: a cost over the whole domain seeds every zone
+        seed_all = 2.0 * (xa_fwd - xt_d) / float(c.n)
+
+        def astep_all():
+            return oak_gb300.loc_analysis_adjoint(*a_args, seed_all, inflation=1.05,
+                                                  weight=c.weight, metric=c.metric,
+                                                  loctype=c.loctype)
+        astep_all()
+        torch.cuda.synchronize(dev)
+        a0.record(stream)
+        for _ in range(args.steps):
+            astep_all()
+        a1.record(stream)
+        torch.cuda.synchronize(dev)
+        ams_all = a0.elapsed_time(a1) / args.steps
         adjoint = {"ms_per_call": ams, "cost_vs_forward_fp64": ams / ms,
+                   "ms_per_call_all_zones": ams_all,
+                   "cost_vs_forward_fp64_all_zones": ams_all / ms,
+                   "dJ_dinfl_posterior_mult": 0.0,
                    "cost_vs_forward_mixed": (ams / mixed["ms_per_step"]) if mixed else None,
                    "cost": "J = mean over a 60x40 column sub-region (all levels) of "
                            "(xa - x_true)^2; gradients w.r.t. all yo, r, the localisation "
-                           "length factor and the prior inflation 1.05",
+                           "length factor and the prior inflation 1.05 (the scaling of Sf and "
+                           "HSf, ErrorSpace.scale); the posterior inflation.mult scales Sa "
+                           "only, so its derivative of a mean-based J is 0",
                    "zones_seeded": int(subz.sum()), "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
 
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
