@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-global", action="store_true")
     return p.parse_args()
 
 
@@ -89,10 +90,22 @@ def run_cpu_oracle(c, zsel, rows, threads):
 
 
 def cpu_baseline(c, seconds, threads):
-    """Times the C/OpenMP oracle on a zone sample sized for ~`seconds` of CPU work."""
-    zsel, rows = cpu_sample(c, 256)
+    """Times the C/OpenMP oracle for ~`seconds` of CPU work: whole passes over the workload
+    while one pass fits the budget, else a zone sample sized from a calibration run."""
+    zsel, rows = cpu_sample(c, 2048)
     dt = run_cpu_oracle(c, zsel, rows, threads)          # calibration
     per_zone = dt / len(zsel)
+    if per_zone * c.Z <= seconds:
+        zsel, rows = np.arange(c.Z), np.arange(c.n)
+        total, passes = 0.0, 0
+        while total < seconds and passes < 8:
+            total += run_cpu_oracle(c, zsel, rows, threads)
+            passes += 1
+        return {"value": passes * c.Z / total, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"{passes} full passes over all {c.Z} zones and {c.m} observations "
+                          f"({total:.1f} s), brute-force selection as "
+                          f"assimilation.F90:3745-3757, LAPACK dsyev via SciPy, OpenMP dynamic "
+                          f"schedule"}
     target = int(min(c.Z, max(256, seconds / max(per_zone, 1e-9))))
     zsel, rows = cpu_sample(c, target)
     dt = run_cpu_oracle(c, zsel, rows, threads)
@@ -343,6 +356,36 @@ def main():
                            "only, so its derivative of a mean-based J is 0",
                    "zones_seeded": int(subz.sum()), "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
 
+    # global analysis (rrsqrt.F90:196-208) of the 100 x 80, N = 30, m = 500 configuration:
+    # device-resident time per analysis, and the CPU port on the host cores beside it
+    glob = None
+    if not args.no_global and rank == 0:
+        from oak_gb300.workloads import global_case
+        g = global_case()
+        gd = (T(g.xf), T(g.Hxf), T(g.yo), F(g.Sf), F(g.HSf), T(g.r_diag))
+        for _ in range(max(3, args.warmup)):
+            oak_gb300.analysis(*gd)
+        torch.cuda.synchronize(dev)
+        kg = 50
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(kg):
+            oak_gb300.analysis(*gd)
+        g1.record(stream)
+        torch.cuda.synchronize(dev)
+        gms = g0.elapsed_time(g1) / kg
+        glob = {"workload": g.name, "ms_per_analysis": gms,
+                "note": "device-resident inputs; each call synchronises (status read-back)"}
+        if not args.no_cpu_baseline:
+            from oracle import cref
+            cref.analysis(g.xf, g.Hxf, g.yo, g.Sf, g.HSf, g.r_diag)
+            t0 = time.perf_counter()
+            for _ in range(10):
+                cref.analysis(g.xf, g.Hxf, g.yo, g.Sf, g.HSf, g.r_diag)
+            glob["cpu_ms_per_analysis"] = (time.perf_counter() - t0) / 10 * 1e3
+            glob["cpu_kind"] = "port (oracle/oakref.c, LAPACK dsyev)"
+
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
     if not args.no_e2e:
@@ -402,6 +445,7 @@ def main():
         "e2e": e2e,
         "mixed": mixed,
         "adjoint": adjoint,
+        "global_analysis": glob,
         "gpu_launches": int(launches),
         "stage_ms_per_step": per_step,
         "roofline": {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,
