@@ -4,7 +4,8 @@
 //   Sa(i1:i2,:) = Sf(i1:i2,:) T                       (rrsqrt.F90:165-185 with T from K4)
 // Zones without relevant observations keep xa = xf and Sa = Sf (rrsqrt.F90:322-326, :371).
 //
-// Sf/Sa are the reference's column-major (n, N) arrays (leading dimension ldS). A task is a
+// Sf/Sa are the reference's column-major (n, N) arrays (leading dimension ldS). In the generic
+// kernel a task is a
 // tile of up to kRows consecutive rows of one zone; the tile of Sf is staged column by column
 // into shared memory (coalesced along rows), T (N x N) next to it, and Sa is written column by
 // column. Reads and writes are in place safe (Sa may alias Sf, xa may alias xf).
@@ -80,6 +81,89 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Mixed form, N <= 64 and N % 8 == 0. A task is a tile of up to kRows rows of one zone, as in
+// k_zone_update, with T, the amplitudes and the Sf tile (converted to FP32) staged in shared
+// memory in one round of coalesced loads. A work item is one row x 8 columns of Sa; the items
+// of a warp share their 8 columns (consecutive threads take consecutive rows), so each k costs
+// the warp one broadcast 128-bit T load pair and one Sf load for 8 FMAs per thread. The FMA
+// order over k is that of k_zone_update<float>.
+constexpr int kColBlk = 8;
+
+__global__ void __launch_bounds__(kThreads)
+    k_zone_update_f32(int N, int32_t z0, int32_t nzc, const int64_t* __restrict__ zone_start,
+                      int tiles_per_zone, const double* __restrict__ xf,
+                      const double* __restrict__ Sf, int64_t ldS, const float* __restrict__ T,
+                      const float* __restrict__ ampl, const int32_t* __restrict__ nobs,
+                      double* __restrict__ xa, double* __restrict__ Sa) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  float* Ts = reinterpret_cast<float*>(dyn_raw);  // [N][N]
+  float* Ss = Ts + N * N;                          // [N][kRows]
+  float* as = Ss + N * kRows;                      // [N]
+  const int64_t ntasks = (int64_t)nzc * tiles_per_zone;
+  const int ncb = N / kColBlk;
+  for (int64_t task = blockIdx.x; task < ntasks; task += gridDim.x) {
+    const int32_t zl = (int32_t)(task / tiles_per_zone);
+    const int tile = (int)(task - (int64_t)zl * tiles_per_zone);
+    const int32_t z = z0 + zl;
+    const int64_t i1 = zone_start[z], i2 = zone_start[z + 1];
+    const int64_t r0 = i1 + (int64_t)tile * kRows;
+    if (r0 >= i2) continue;  // uniform across the block
+    const int R_ = (int)((i2 - r0) < kRows ? (i2 - r0) : kRows);
+    if (nobs[zl] == 0) {
+      for (int idx = threadIdx.x; idx < R_; idx += kThreads) xa[r0 + idx] = xf[r0 + idx];
+      if (Sa && Sa != Sf) {
+        for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
+          const int k = idx / R_, r = idx - k * R_;
+          Sa[r0 + r + (int64_t)k * ldS] = Sf[r0 + r + (int64_t)k * ldS];
+        }
+      }
+      continue;
+    }
+    __syncthreads();  // previous task's shared data consumed
+    const float4* Tz4 = reinterpret_cast<const float4*>(T + (int64_t)zl * N * N);
+    float4* Ts4 = reinterpret_cast<float4*>(Ts);
+    if (Sa) {
+      for (int idx = threadIdx.x; idx < N * N / 4; idx += kThreads) Ts4[idx] = Tz4[idx];
+    }
+    for (int idx = threadIdx.x; idx < N; idx += kThreads) as[idx] = ampl[(int64_t)zl * N + idx];
+    for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
+      const int k = idx / R_, r = idx - k * R_;
+      Ss[k * kRows + r] = (float)Sf[r0 + r + (int64_t)k * ldS];
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < R_; r += kThreads) {  // xa = xf + Sf ampl
+      float sx = 0.f;
+      for (int k = 0; k < N; k++) sx = fmaf(Ss[k * kRows + r], as[k], sx);
+      xa[r0 + r] = xf[r0 + r] + (double)sx;
+    }
+    if (Sa) {
+      for (int it = threadIdx.x; it < R_ * ncb; it += kThreads) {
+        const int cb = it / R_, r = it - cb * R_;
+        const int c0 = kColBlk * cb;
+        float acc[kColBlk];
+#pragma unroll
+        for (int t = 0; t < kColBlk; t++) acc[t] = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < N; k++) {
+          const float sk = Ss[k * kRows + r];
+          const float4 ta = *reinterpret_cast<const float4*>(Ts + k * N + c0);
+          const float4 tb = *reinterpret_cast<const float4*>(Ts + k * N + c0 + 4);
+          acc[0] = fmaf(sk, ta.x, acc[0]);
+          acc[1] = fmaf(sk, ta.y, acc[1]);
+          acc[2] = fmaf(sk, ta.z, acc[2]);
+          acc[3] = fmaf(sk, ta.w, acc[3]);
+          acc[4] = fmaf(sk, tb.x, acc[4]);
+          acc[5] = fmaf(sk, tb.y, acc[5]);
+          acc[6] = fmaf(sk, tb.z, acc[6]);
+          acc[7] = fmaf(sk, tb.w, acc[7]);
+        }
+#pragma unroll
+        for (int t = 0; t < kColBlk; t++) Sa[r0 + r + (int64_t)(c0 + t) * ldS] = (double)acc[t];
+      }
+    }
+  }
+}
+
 template <typename R>
 __global__ void k_write_amplitudes(int N, int32_t z0, int32_t nzc, const R* __restrict__ za,
                                    const int32_t* __restrict__ nobs, int all_zones,
@@ -138,6 +222,26 @@ cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zo
                              int32_t zone_max, const double* xf, const double* Sf,
                              int64_t ldS, const float* d_T, const float* d_ampl,
                              const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
+  if (N % kColBlk == 0) {
+    size_t smem = (size_t)(N * N + N * kRows + N) * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_zone_update_f32,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int tiles = (zone_max + kRows - 1) / kRows;
+    if (tiles < 1) tiles = 1;
+    const int64_t ntasks = (int64_t)nzc * tiles;
+    int bps = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_update_f32, kThreads, smem);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t cap = (int64_t)sms * (bps > 0 ? bps : 1) * 8;
+    const int grid = (int)(ntasks < cap ? (ntasks < 1 ? 1 : ntasks) : cap);
+    k_zone_update_f32<<<grid, kThreads, smem, st>>>(N, z0, nzc, d_zone_start, tiles, xf, Sf, ldS,
+                                                    d_T, d_ampl, d_nobs, xa, Sa);
+    count_launches(1);
+    return cudaGetLastError();
+  }
   return zone_update_impl<float>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T, d_ampl,
                                  d_nobs, xa, Sa, st);
 }
