@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--no-mixed", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-global", action="store_true")
+    p.add_argument("--no-graph", action="store_true")
     return p.parse_args()
 
 
@@ -356,6 +357,38 @@ def main():
                            "only, so its derivative of a mean-based J is 0",
                    "zones_seeded": int(subz.sum()), "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
 
+    # prepared analyses replayed as CUDA graphs (oakg_plan_*): FP64 with the default cell edge,
+    # mixed with the tuned one; each execution waits for its status
+    graph = None
+    if not args.no_graph:
+        def time_plan(pl, k):
+            for _ in range(2):
+                pl.execute(stream)
+            torch.cuda.synchronize(dev)
+            p0 = torch.cuda.Event(enable_timing=True)
+            p1 = torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            for _ in range(k):
+                pl.execute(stream)
+            p1.record(stream)
+            torch.cuda.synchronize(dev)
+            return p0.elapsed_time(p1) / k
+        kw = dict(weight=c.weight, metric=c.metric, loctype=c.loctype)
+        pl = oak_gb300.Plan(*d_args, **kw)
+        g64 = time_plan(pl, args.steps)
+        nodes64 = pl.info["graph_nodes"]
+        pl.close()
+        pl = oak_gb300.Plan(*d_args, precision=oak_gb300.PREC_MIXED, tune=True, **kw)
+        gmx = time_plan(pl, max(args.steps, 5))
+        info = pl.info
+        pl.close()
+        graph = {"fp64_ms_per_step": g64, "fp64_graph_nodes": nodes64,
+                 "mixed_tuned_ms_per_step": gmx,
+                 "mixed_tuned_value": ws * c.Z / (gmx / 1e3),
+                 "mixed_tuned_speedup_vs_fp64": ms / gmx,
+                 "mixed_cell_size": info["cell_size"], "mixed_graph_nodes": info["graph_nodes"],
+                 "tuning_cell_ms": info["tuning"]}
+
     # global analysis (rrsqrt.F90:196-208) of the 100 x 80, N = 30, m = 500 configuration:
     # device-resident time per analysis, and the CPU port on the host cores beside it
     glob = None
@@ -446,6 +479,7 @@ def main():
         "mixed": mixed,
         "adjoint": adjoint,
         "global_analysis": glob,
+        "graph": graph,
         "gpu_launches": int(launches),
         "stage_ms_per_step": per_step,
         "roofline": {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,

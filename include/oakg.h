@@ -165,6 +165,33 @@ int oakg_analysis_noalloc(const oakg_dims* dims, const double* xf, const double*
                           const double* r_diag, double* xa, double* Sa, double* ampl,
                           void* stream);
 
+/* Prepared local analysis -- no counterpart in the reference; for the repeated analyses of a
+ * forecast-analysis cycle whose buffers stay in place (the cycle of assim.F90:71-99 calling
+ * locAnalysis each step). oakg_plan_locanalysis takes the arguments of oakg_locanalysis (device
+ * pointers only: dims->mem must be OAKG_MEM_DEVICE) and runs it once; it keeps the zone
+ * offsets, the observation cell grid and every scratch buffer, and captures the device work
+ * (observation binning, selection + Gram, eigensolve, update, status) as one CUDA graph.
+ * oakg_plan_execute replays it on `stream` (NULL: the plan's own stream) against the current
+ * contents of the same buffers -- new observation values and positions are honoured, the
+ * sizes and pointers are those of the plan -- and waits for it: same status codes as
+ * oakg_locanalysis. With tune != 0 (and loc->cell_size <= 0) the cell edge of the observation
+ * grid is chosen among 0.25, 0.35, 0.5, 0.7 and 1 times the localisation reach by timing the
+ * selection + Gram stage on the data. oakg_plan_info reports the chosen edge, the graph's
+ * node count and up to ntune (edge, ms) tuning samples; it returns the number of samples.
+ * A plan holds the caller's pointers: keep the buffers alive until oakg_plan_destroy. */
+typedef struct oakg_plan oakg_plan;
+int oakg_plan_locanalysis(oakg_plan** plan, const oakg_dims* dims, const oakg_loc* loc,
+                          int32_t nzones, const int32_t* zone_size, const double* xf,
+                          const double* Hxf, const double* yo, const double* Sf,
+                          const double* HSf, const double* r_diag, const double* zone_xyzt,
+                          const double* obs_x, const double* obs_y, const double* obs_z,
+                          const double* obs_t, const double* corr_len, const double* max_len,
+                          double* xa, double* Sa, double* ampl, int32_t* nobs, int32_t tune);
+int oakg_plan_execute(oakg_plan* plan, void* stream);
+int oakg_plan_info(const oakg_plan* plan, double* cell_size, int64_t* graph_nodes,
+                   double* tune_cell, double* tune_ms, int32_t ntune);
+void oakg_plan_destroy(oakg_plan* plan);
+
 /* Message of the last failed call on this thread (empty if none); returns its length. */
 size_t oakg_last_error(char* buf, size_t len);
 

@@ -98,6 +98,18 @@ def lib() -> ctypes.CDLL:
                                                           ctypes.POINTER(ctypes.c_double),
                                                           ctypes.POINTER(ctypes.c_double)])
     L.oakg_locanalysis_adjoint.restype = ctypes.c_int
+    L.oakg_plan_locanalysis.argtypes = ([ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Dims),
+                                         ctypes.POINTER(Loc), ctypes.c_int32] + [P] * 18
+                                        + [ctypes.c_int32])
+    L.oakg_plan_locanalysis.restype = ctypes.c_int
+    L.oakg_plan_execute.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.oakg_plan_execute.restype = ctypes.c_int
+    L.oakg_plan_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
+    L.oakg_plan_info.restype = ctypes.c_int
+    L.oakg_plan_destroy.argtypes = [ctypes.c_void_p]
+    L.oakg_plan_destroy.restype = None
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -296,6 +308,94 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
         A.vec(nobs, np.int32, "nobs"))
     _check(rc)
     return xa, Sa, ampl, nobs
+
+
+class Plan:
+    """A prepared local analysis over device (torch CUDA) tensors (oakg_plan_locanalysis).
+
+    Takes the arguments of :func:`loc_analysis` (all CUDA tensors). The constructor runs the
+    analysis once and captures its device work as one CUDA graph; :meth:`execute` replays it
+    against the current contents of the same tensors (update them in place between calls)
+    and returns ``(xa, Sa, nobs)`` -- tensors owned by the plan, overwritten by each
+    execution. ``tune=True`` picks the observation cell edge by timing candidates on the data
+    (see :attr:`info`). The plan keeps references to every tensor it was given.
+    """
+
+    def __init__(self, zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, corr_len,
+                 max_len, *, weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1,
+                 localise_obs=True, rotate=True, want_sa=True, precision=PREC_FP64, tune=False,
+                 cell_size=0.0):
+        self._h = None
+        Z = int(zone_size.shape[0])
+        n = int(xf.shape[0])
+        m = int(yo.shape[0])
+        N = int(Sf.shape[1])
+        ox, oy, oz, ot = (tuple(obs_pos) + (None,) * 4)[:4]
+        if not _device_mode(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, corr_len,
+                            max_len, ox, oy, oz, ot):
+            raise OakError(ERR_ARGS, "a plan binds CUDA tensors")
+        A = _Args(True)
+        pSf, ldS = A.mat(Sf, n, N, "Sf")
+        pHS, ldH = A.mat(HSf, m, N, "HSf")
+        dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE)
+        loc = Loc(weight=weight, metric=metric, loctype=loctype,
+                  localise_obs=int(bool(localise_obs)), rotate=int(bool(rotate)),
+                  precision=int(precision), flags=0, cell_size=float(cell_size))
+        self.xa = _empty_like_mode(True, (n,), like=Sf)
+        self.Sa = _empty_like_mode(True, (n, N), order="F", like=Sf) if want_sa else None
+        self.nobs = _empty_like_mode(True, (Z,), dtype=np.int32, like=Sf)
+        _sync_torch(True, Sf)
+        h = ctypes.c_void_p()
+        rc = lib().oakg_plan_locanalysis(
+            ctypes.byref(h), ctypes.byref(dims), ctypes.byref(loc), Z,
+            A.vec(zone_size, np.int32, "zone_size", Z), A.vec(xf, n=n, name="xf"),
+            A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"), pSf, pHS,
+            A.vec(r_diag, n=m, name="r_diag"), A.vec(zone_pos.reshape(-1), n=4 * Z,
+                                                      name="zone_pos"),
+            A.vec(ox, n=m, name="obs_x"), A.vec(oy, n=m, name="obs_y"),
+            A.vec(oz, n=m, name="obs_z"), A.vec(ot, n=m, name="obs_t"),
+            A.vec(corr_len, n=Z, name="corr_len"), A.vec(max_len, n=Z, name="max_len"),
+            A.vec(self.xa, name="xa"), None if self.Sa is None else A.mat(self.Sa, n, N, "Sa")[0],
+            None, A.vec(self.nobs, np.int32, "nobs"), int(bool(tune)))
+        _check(rc)
+        self._h = h
+        self._keep = A.keep + [zone_pos]
+
+    def execute(self, stream=None):
+        """Replay the analysis on ``stream`` (a torch stream, a raw handle or None: the plan's
+        own stream, ordered after work on the current torch stream) and wait for it."""
+        if self._h is None:
+            raise OakError(ERR_ARGS, "plan is closed")
+        if stream is None:
+            import torch
+            torch.cuda.current_stream(self.xa.device).synchronize()
+            ptr = None
+        else:
+            ptr = getattr(stream, "cuda_stream", stream)
+        _check(lib().oakg_plan_execute(self._h, None if ptr is None else ctypes.c_void_p(ptr)))
+        return self.xa, self.Sa, self.nobs
+
+    @property
+    def info(self) -> dict:
+        """Chosen cell edge, graph node count and the tuning samples (edge, ms)."""
+        cs = ctypes.c_double(0.0)
+        nodes = ctypes.c_int64(0)
+        tc = (ctypes.c_double * 8)()
+        tm = (ctypes.c_double * 8)()
+        k = lib().oakg_plan_info(self._h, ctypes.byref(cs), ctypes.byref(nodes), tc, tm, 8)
+        return {"cell_size": cs.value, "graph_nodes": nodes.value,
+                "tuning": [(tc[i], tm[i]) for i in range(k)]}
+
+    def close(self):
+        if self._h is not None:
+            lib().oakg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def zone_positions(zone_size, x, y=None, z=None, t=None):

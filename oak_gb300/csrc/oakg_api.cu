@@ -79,6 +79,7 @@ struct Ctx {
   cudaEvent_t ev[8] = {};
   Buf buf[B_COUNT_];
   double timings[5] = {0, 0, 0, 0, 0};
+  int64_t chunk_override = 0;  // > 0: zones per chunk fixed (plans: no memory query in capture)
 };
 
 Ctx* g_ctx[64] = {};
@@ -254,10 +255,15 @@ struct ChunkArgs {
   int32_t* nobs;
 };
 
+// How run_chunks issues its work: timed (events + a host wait per chunk), captured into a CUDA
+// graph (no event, no host wait), or the selection + Gram stage alone (autotuning).
+enum class RunMode { kTimed, kCapture, kGramOnly };
+
 // Runs the zone stages over chunks of zones sized to the scratch budget.
 template <typename R>
 int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram, double* t_eig,
-               double* t_upd) {
+               double* t_upd, RunMode mode = RunMode::kTimed) {
+  const bool timed = (mode != RunMode::kCapture);
   using K = ZoneKernels<R>;
   const int N = a.N;
   cudaStream_t st = c->stream;
@@ -265,7 +271,8 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   int rc;
   const size_t per_zone =
       ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) * sizeof(R) + 2 * sizeof(int32_t);
-  int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
+  int64_t chunk = c->chunk_override > 0 ? c->chunk_override
+                                        : (int64_t)(chunk_budget_bytes() / per_zone);
   if (chunk < 1) chunk = 1;
   if (chunk > a.Z) chunk = a.Z;
   R *d_G, *d_gv, *d_za, *d_aux, *d_zvec;
@@ -282,19 +289,25 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   count_launches(1);
   for (int64_t z0 = 0; z0 < a.Z; z0 += chunk) {
     const int32_t nzc = (int32_t)std::min<int64_t>(chunk, a.Z - z0);
-    cudaEventRecord(c->ev[2], st);
+    if (timed) cudaEventRecord(c->ev[2], st);
     e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv, a.nobs,
                 a.brute, d_work, *status_all, st);
     if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
-    cudaEventRecord(c->ev[3], st);
+    if (mode == RunMode::kGramOnly) {
+      cudaEventRecord(c->ev[3], st);
+      if ((e = cudaEventSynchronize(c->ev[3])) != cudaSuccess) return cuda_fail(e, "kernels");
+      *t_gram += elapsed(c->ev[2], c->ev[3]);
+      continue;
+    }
+    if (timed) cudaEventRecord(c->ev[3], st);
     e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate, d_za,
                d_status, d_aux, d_zvec, d_work + 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
-    cudaEventRecord(c->ev[4], st);
+    if (timed) cudaEventRecord(c->ev[4], st);
     e = K::update(N, (int32_t)z0, nzc, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, (const R*)d_G,
                   (const R*)d_za, (const int32_t*)(a.nobs + z0), a.xa, a.Sa, st);
     if (e != cudaSuccess) return cuda_fail(e, "update kernel");
-    cudaEventRecord(c->ev[5], st);
+    if (timed) cudaEventRecord(c->ev[5], st);
     if (a.ampl) {
       e = K::ampl(N, (int32_t)z0, nzc, (const R*)d_za, (const int32_t*)(a.nobs + z0), a.all_ampl,
                   a.ampl, st);
@@ -302,6 +315,7 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     }
     k_or_status<<<64, 256, 0, st>>>(d_status, nzc, *status_all);
     count_launches(1);
+    if (!timed) continue;
     if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
     *t_gram += elapsed(c->ev[2], c->ev[3]);
     *t_eig += elapsed(c->ev[3], c->ev[4]);
@@ -336,6 +350,62 @@ int check_loc(const oakg_dims* dims, const oakg_loc* loc, int32_t Z) {
     return fail(OAKG_ERR_ARGS, "loctype must be 1, 2 or 3 (got %d)", loc->loctype);
   if (loc->precision != OAKG_PREC_FP64 && loc->precision != OAKG_PREC_MIXED)
     return fail(OAKG_ERR_ARGS, "unknown precision mode %d", loc->precision);
+  return OAKG_OK;
+}
+
+// Bins the observations into P->g (cell-sorted arrays in P->so), plus the FP32 copies of the
+// mixed form. Issues device work only (no host wait), so it can be captured in a graph.
+int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH, Prep* P) {
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  int rc;
+  const CellGrid& g = P->g;
+  const int64_t ncells = (int64_t)g.nu * g.nv;
+  SortedObs& so = P->so;
+  so = SortedObs{};
+  if (m > 0) {
+    int32_t *d_cell, *d_count, *d_cstart, *d_pos, *d_perm;
+    double *d_su, *d_sv, *d_sinnov, *d_sr, *d_hst;
+    if ((rc = scratch(c, B_CELL, (size_t)m, &d_cell, "cells"))) return rc;
+    if ((rc = scratch(c, B_COUNT, (size_t)ncells + 1, &d_count, "cells"))) return rc;
+    if ((rc = scratch(c, B_CSTART, (size_t)ncells + 1, &d_cstart, "cells"))) return rc;
+    if ((rc = scratch(c, B_POS, (size_t)m, &d_pos, "obs"))) return rc;
+    if ((rc = scratch(c, B_PERM, (size_t)m, &d_perm, "obs"))) return rc;
+    if ((rc = scratch(c, B_SU, (size_t)m, &d_su, "obs"))) return rc;
+    if ((rc = scratch(c, B_SV, (size_t)m, &d_sv, "obs"))) return rc;
+    if ((rc = scratch(c, B_SINNOV, (size_t)m, &d_sinnov, "obs"))) return rc;
+    if ((rc = scratch(c, B_SR, (size_t)m, &d_sr, "obs"))) return rc;
+    if ((rc = scratch(c, B_HST, (size_t)m * N, &d_hst, "obs rows"))) return rc;
+    e = obs_bin_and_sort(g, m, N, P->u, P->v, P->yo, P->Hxf, P->r, P->HSf, ldH, d_cell, d_count,
+                         d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr, d_hst, st);
+    if (e != cudaSuccess) return cuda_fail(e, "observation binning");
+    so.u = d_su;
+    so.v = d_sv;
+    so.innov = d_sinnov;
+    so.r = d_sr;
+    so.HSt = d_hst;
+    so.cell_start = d_cstart;
+    so.perm = d_perm;
+    if (loc->precision == OAKG_PREC_MIXED) {
+      float* d_hst32;
+      if ((rc = scratch(c, B_HST32, (size_t)m * N, &d_hst32, "obs rows (FP32)"))) return rc;
+      if ((e = rows_to_fp32(d_hst, d_hst32, m * N, st)) != cudaSuccess)
+        return cuda_fail(e, "FP32 observation rows");
+      so.HSt32 = d_hst32;
+      float* d_obs32;
+      if ((rc = scratch(c, B_OBS32, (size_t)2 * m, &d_obs32, "obs (FP32)"))) return rc;
+      if ((e = rows_to_fp32(d_sr, d_obs32, m, st)) != cudaSuccess ||
+          (e = rows_to_fp32(d_sinnov, d_obs32 + m, m, st)) != cudaSuccess)
+        return cuda_fail(e, "FP32 observation values");
+      so.r32 = d_obs32;
+      so.innov32 = d_obs32 + m;
+    }
+  } else {
+    int32_t* d_cstart;
+    if ((rc = scratch(c, B_CSTART, 2, &d_cstart, "cells"))) return rc;
+    cudaMemsetAsync(d_cstart, 0, 2 * sizeof(int32_t), st);
+    so.cell_start = d_cstart;
+  }
   return OAKG_OK;
 }
 
@@ -437,53 +507,7 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
       g.csu = 360.0 / g.nu;
     }
   }
-  const int64_t ncells = (int64_t)g.nu * g.nv;
-  SortedObs& so = P->so;
-  so = SortedObs{};
-  if (m > 0) {
-    int32_t *d_cell, *d_count, *d_cstart, *d_pos, *d_perm;
-    double *d_su, *d_sv, *d_sinnov, *d_sr, *d_hst;
-    if ((rc = scratch(c, B_CELL, (size_t)m, &d_cell, "cells"))) return rc;
-    if ((rc = scratch(c, B_COUNT, (size_t)ncells + 1, &d_count, "cells"))) return rc;
-    if ((rc = scratch(c, B_CSTART, (size_t)ncells + 1, &d_cstart, "cells"))) return rc;
-    if ((rc = scratch(c, B_POS, (size_t)m, &d_pos, "obs"))) return rc;
-    if ((rc = scratch(c, B_PERM, (size_t)m, &d_perm, "obs"))) return rc;
-    if ((rc = scratch(c, B_SU, (size_t)m, &d_su, "obs"))) return rc;
-    if ((rc = scratch(c, B_SV, (size_t)m, &d_sv, "obs"))) return rc;
-    if ((rc = scratch(c, B_SINNOV, (size_t)m, &d_sinnov, "obs"))) return rc;
-    if ((rc = scratch(c, B_SR, (size_t)m, &d_sr, "obs"))) return rc;
-    if ((rc = scratch(c, B_HST, (size_t)m * N, &d_hst, "obs rows"))) return rc;
-    e = obs_bin_and_sort(g, m, N, P->u, P->v, P->yo, P->Hxf, P->r, P->HSf, ldH, d_cell, d_count,
-                         d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr, d_hst, st);
-    if (e != cudaSuccess) return cuda_fail(e, "observation binning");
-    so.u = d_su;
-    so.v = d_sv;
-    so.innov = d_sinnov;
-    so.r = d_sr;
-    so.HSt = d_hst;
-    so.cell_start = d_cstart;
-    so.perm = d_perm;
-    if (loc->precision == OAKG_PREC_MIXED) {
-      float* d_hst32;
-      if ((rc = scratch(c, B_HST32, (size_t)m * N, &d_hst32, "obs rows (FP32)"))) return rc;
-      if ((e = rows_to_fp32(d_hst, d_hst32, m * N, st)) != cudaSuccess)
-        return cuda_fail(e, "FP32 observation rows");
-      so.HSt32 = d_hst32;
-      float* d_obs32;
-      if ((rc = scratch(c, B_OBS32, (size_t)2 * m, &d_obs32, "obs (FP32)"))) return rc;
-      if ((e = rows_to_fp32(d_sr, d_obs32, m, st)) != cudaSuccess ||
-          (e = rows_to_fp32(d_sinnov, d_obs32 + m, m, st)) != cudaSuccess)
-        return cuda_fail(e, "FP32 observation values");
-      so.r32 = d_obs32;
-      so.innov32 = d_obs32 + m;
-    }
-  } else {
-    int32_t* d_cstart;
-    if ((rc = scratch(c, B_CSTART, 2, &d_cstart, "cells"))) return rc;
-    cudaMemsetAsync(d_cstart, 0, 2 * sizeof(int32_t), st);
-    so.cell_start = d_cstart;
-  }
-  return OAKG_OK;
+  return bin_observations(c, loc, m, N, ldH, P);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -621,7 +645,8 @@ int adjoint_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z, const in
   LocParams lp{loc->weight, loc->metric, loc->loctype, loc->localise_obs ? 1 : 0,
                loc->rotate ? 1 : 0, loc->flags};
   const size_t per_zone = (size_t)N * N * 8 + (size_t)N * 8;
-  int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
+  int64_t chunk = c->chunk_override > 0 ? c->chunk_override
+                                        : (int64_t)(chunk_budget_bytes() / per_zone);
   if (chunk < 1) chunk = 1;
   if (chunk > nact) chunk = nact;
   double *d_G, *d_gv;
@@ -756,6 +781,200 @@ int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
   return status_code(hstatus);
 }
 
+// ------------------------------------------------------------------------------------------
+// Plans: a local analysis over fixed device buffers, prepared once (staging, zone offsets,
+// observation cell grid, scratch) and replayed as one CUDA graph. The graph re-bins the
+// observations, so new values and positions in the same buffers are honoured; the cell grid's
+// geometry is that of the preparation (observations outside it fall in its edge cells, which
+// the zone scans always reach, so results stay exact). With tuning, the cell edge is chosen
+// among multiples of the localisation reach by timing the selection + Gram stage on the data.
+struct Plan {
+  Ctx ctx;  // private buffers, events and the capture stream
+  oakg_dims dims{};
+  oakg_loc loc{};
+  int32_t Z = 0;
+  Prep P{};
+  ChunkArgs ca{};
+  int32_t* d_status_all = nullptr;
+  int32_t* h_status = nullptr;  // pinned
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  size_t nodes = 0;
+  double cell_size = 0.0;
+  double tune_ms[8] = {};
+  double tune_cell[8] = {};
+  int ntune = 0;
+};
+
+void plan_free(Plan* pl) {
+  if (!pl) return;
+  if (pl->ctx.stream) cudaStreamSynchronize(pl->ctx.stream);
+  if (pl->exec) cudaGraphExecDestroy(pl->exec);
+  if (pl->graph) cudaGraphDestroy(pl->graph);
+  if (pl->h_status) cudaFreeHost(pl->h_status);
+  for (auto& b : pl->ctx.buf) b.release();
+  for (auto& ev : pl->ctx.ev)
+    if (ev) cudaEventDestroy(ev);
+  if (pl->ctx.own_stream) cudaStreamDestroy(pl->ctx.own_stream);
+  delete pl;
+}
+
+template <typename R>
+int plan_run(Plan* pl, RunMode mode, double* t_gram) {
+  double tg = 0, te = 0, tu = 0;
+  int rc = run_chunks<R>(&pl->ctx, pl->ca, &pl->d_status_all, &tg, &te, &tu, mode);
+  if (t_gram) *t_gram = tg;
+  return rc;
+}
+
+int plan_run_mode(Plan* pl, RunMode mode, double* t_gram = nullptr) {
+  return (pl->loc.precision == OAKG_PREC_MIXED) ? plan_run<float>(pl, mode, t_gram)
+                                                : plan_run<double>(pl, mode, t_gram);
+}
+
+int plan_create_impl(Plan** out, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
+                     const int32_t* zone_size, const double* xf, const double* Hxf,
+                     const double* yo, const double* Sf, const double* HSf, const double* r_diag,
+                     const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                     const double* obs_z, const double* obs_t, const double* corr_len,
+                     const double* max_len, double* xa, double* Sa, double* ampl,
+                     int32_t* nobs_out, int32_t tune) {
+  if (!out) return fail(OAKG_ERR_ARGS, "plan is NULL");
+  *out = nullptr;
+  int rc = check_loc(dims, loc, Z);
+  if (rc) return rc;
+  if (dims->mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "plans bind device buffers: dims->mem must be OAKG_MEM_DEVICE");
+  if (!xf || !xa) return fail(OAKG_ERR_ARGS, "xf and xa are required");
+  Plan* pl = new Plan();
+  Ctx* c = &pl->ctx;
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "plan stream");
+  }
+  c->stream = c->own_stream;
+  for (auto& ev : c->ev) cudaEventCreate(&ev);
+  pl->dims = *dims;
+  pl->loc = *loc;
+  pl->Z = Z;
+  const int N = dims->N;
+  const int64_t m = dims->m, ldH = dims->ldH;
+  auto setup = [&](const oakg_loc* lc) -> int {
+    int r = prepare_loc(c, dims, lc, Z, zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
+                        obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &pl->P);
+    if (r) return r;
+    int32_t* d_nobs = nobs_out;
+    if (!d_nobs && (r = scratch(c, B_NOBS, (size_t)Z, &d_nobs, "nobs"))) return r;
+    LocParams lp{lc->weight, lc->metric, lc->loctype, lc->localise_obs ? 1 : 0,
+                 lc->rotate ? 1 : 0, lc->flags};
+    const int all_ampl = (!lc->localise_obs) || (lc->flags & OAKG_FLAG_AMPL_ALWAYS);
+    pl->ca = ChunkArgs{pl->P.g, pl->P.so, lp, Z, N, dims->ldS, pl->P.zone_max, pl->P.brute,
+                       all_ampl, pl->P.zxyzt, pl->P.corr, pl->P.maxl, pl->P.zstart, pl->P.xf,
+                       pl->P.Sf, xa, Sa, ampl, d_nobs};
+    return OAKG_OK;
+  };
+  oakg_loc lc = *loc;
+  if ((rc = setup(&lc))) {
+    plan_free(pl);
+    return rc;
+  }
+  if (tune && lc.cell_size <= 0.0 && m > 0 && !pl->P.brute) {
+    // the default edge is half the reach; candidates from a quarter to one reach
+    const double reach = 2.0 * pl->P.g.csv;
+    const double factors[5] = {0.25, 0.35, 0.5, 0.7, 1.0};
+    double best = -1.0, best_ms = 1e300;
+    for (double f : factors) {
+      lc.cell_size = f * reach;
+      double ms = 0.0;
+      if ((rc = setup(&lc)) || (rc = plan_run_mode(pl, RunMode::kGramOnly)) ||
+          (rc = plan_run_mode(pl, RunMode::kGramOnly, &ms))) {
+        plan_free(pl);
+        return rc;
+      }
+      if (pl->ntune < 8) {
+        pl->tune_cell[pl->ntune] = lc.cell_size;
+        pl->tune_ms[pl->ntune++] = ms;
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = lc.cell_size;
+      }
+    }
+    lc.cell_size = best;
+    if ((rc = setup(&lc))) {
+      plan_free(pl);
+      return rc;
+    }
+  }
+  pl->loc = lc;
+  pl->cell_size = pl->P.g.csv;
+  // fix the chunk size so that the captured sequence queries nothing, then one ordinary run
+  // allocates every buffer at that size and sets the kernel attributes
+  {
+    const size_t per_zone =
+        ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) *
+            (lc.precision == OAKG_PREC_MIXED ? sizeof(float) : sizeof(double)) +
+        2 * sizeof(int32_t);
+    const int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
+    c->chunk_override = std::max<int64_t>(1, std::min<int64_t>(chunk, Z));
+  }
+  if ((rc = plan_run_mode(pl, RunMode::kTimed))) {
+    plan_free(pl);
+    return rc;
+  }
+  if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "synchronize");
+  }
+  e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "begin capture");
+  }
+  int rc_cap = bin_observations(c, &lc, m, N, ldH, &pl->P);
+  if (!rc_cap) {
+    pl->ca.so = pl->P.so;
+    rc_cap = plan_run_mode(pl, RunMode::kCapture);
+  }
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(c->stream, &graph);
+  pl->graph = graph;
+  if (rc_cap) {
+    plan_free(pl);
+    return rc_cap;
+  }
+  if (e != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "end capture");
+  }
+  if ((e = cudaGraphInstantiate(&pl->exec, pl->graph, 0)) != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "graph instantiate");
+  }
+  cudaGraphGetNodes(pl->graph, nullptr, &pl->nodes);
+  if ((e = cudaMallocHost(&pl->h_status, sizeof(int32_t))) != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "pinned status");
+  }
+  *out = pl;
+  return OAKG_OK;
+}
+
+int plan_execute_impl(Plan* pl, void* stream) {
+  if (!pl) return fail(OAKG_ERR_ARGS, "plan is NULL");
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : pl->ctx.stream;
+  cudaError_t e = cudaGraphLaunch(pl->exec, st);
+  if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+  count_launches((int)pl->nodes);
+  e = cudaMemcpyAsync(pl->h_status, pl->d_status_all, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                      st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "plan execution");
+  return status_code(*pl->h_status);
+}
+
 int release_impl() {
   for (auto& cp : g_ctx) {
     if (!cp) continue;
@@ -886,4 +1105,62 @@ int oakg_last_timings(double* ms, int n) {
   return oakg::timings_impl(ms, n);
 }
 
+struct oakg_plan {
+  oakg::Plan* p;
+};
+
+int oakg_plan_locanalysis(oakg_plan** plan, const oakg_dims* dims, const oakg_loc* loc,
+                          int32_t nzones, const int32_t* zone_size, const double* xf,
+                          const double* Hxf, const double* yo, const double* Sf,
+                          const double* HSf, const double* r_diag, const double* zone_xyzt,
+                          const double* obs_x, const double* obs_y, const double* obs_z,
+                          const double* obs_t, const double* corr_len, const double* max_len,
+                          double* xa, double* Sa, double* ampl, int32_t* nobs, int32_t tune) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  if (!plan) {
+    int rc = oakg::record_failure(OAKG_ERR_ARGS, "plan is NULL");
+    oakg::last_status() = rc;
+    return rc;
+  }
+  *plan = nullptr;
+  oakg::Plan* p = nullptr;
+  int rc = oakg::plan_create_impl(&p, dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf, r_diag,
+                                  zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, xa, Sa,
+                                  ampl, nobs, tune);
+  if (rc == OAKG_OK) *plan = new oakg_plan{p};
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_plan_execute(oakg_plan* plan, void* stream) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::plan_execute_impl(plan ? plan->p : nullptr, stream);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_plan_info(const oakg_plan* plan, double* cell_size, int64_t* graph_nodes,
+                   double* tune_cell, double* tune_ms, int32_t ntune) {
+  if (!plan || !plan->p) return 0;
+  const oakg::Plan* p = plan->p;
+  if (cell_size) *cell_size = p->cell_size;
+  if (graph_nodes) *graph_nodes = (int64_t)p->nodes;
+  const int k = std::min<int>(p->ntune, ntune > 0 ? ntune : 0);
+  for (int i = 0; i < k; i++) {
+    if (tune_cell) tune_cell[i] = p->tune_cell[i];
+    if (tune_ms) tune_ms[i] = p->tune_ms[i];
+  }
+  return p->ntune;
+}
+
+void oakg_plan_destroy(oakg_plan* plan) {
+  if (!plan) return;
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::plan_free(plan->p);
+  delete plan;
+}
+
 }  // extern "C"
+

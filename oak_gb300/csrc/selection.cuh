@@ -107,15 +107,15 @@ static __device__ ScanRange zone_scan_range(const CellGrid& g, int metric, int l
     fu0 -= 1.0;
     fu1 += 1.0;
   }
+  // Ranges are clamped to the grid, never emptied: observations outside the grid are binned
+  // into its edge cells, so a zone whose window lies beyond an edge still scans that edge
+  // (the exact distance test decides). This keeps a grid valid when observations later move
+  // outside the bounds it was built for.
   double fv0 = floor((zv - dv - g.v0) / g.csv), fv1 = floor((zv + dv - g.v0) / g.csv);
-  fv0 = fmax(fv0, 0.0);
-  fv1 = fmin(fv1, (double)(g.nv - 1));
+  fv0 = fmin(fmax(fv0, 0.0), (double)(g.nv - 1));
+  fv1 = fmin(fmax(fv1, 0.0), (double)(g.nv - 1));
   s.cv0 = (int)fv0;
   s.cv1 = (int)fv1;
-  if (fv0 > fv1) {
-    s.cv0 = 0;
-    s.cv1 = -1;
-  }
   if (g.periodic_u) {
     if (all_u || fu1 - fu0 + 1.0 >= (double)g.nu) {
       all_u = 1;
@@ -124,14 +124,10 @@ static __device__ ScanRange zone_scan_range(const CellGrid& g, int metric, int l
       s.cu1 = (int)fu1;
     }
   } else {
-    fu0 = fmax(fu0, 0.0);
-    fu1 = fmin(fu1, (double)(g.nu - 1));
+    fu0 = fmin(fmax(fu0, 0.0), (double)(g.nu - 1));
+    fu1 = fmin(fmax(fu1, 0.0), (double)(g.nu - 1));
     s.cu0 = (int)fu0;
     s.cu1 = (int)fu1;
-    if (fu0 > fu1) {
-      s.cv0 = 0;
-      s.cv1 = -1;
-    }
   }
   if (all_u) {
     s.cu0 = 0;
