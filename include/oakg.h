@@ -165,6 +165,44 @@ int oakg_analysis_noalloc(const oakg_dims* dims, const double* xf, const double*
                           const double* r_diag, double* xa, double* Sa, double* ampl,
                           void* stream);
 
+/* Sparse observation operator H (m x n) in row form: observation j is
+ *   sum_{t < K} weight[j*K + t] * x[index[j*K + t]] + (shift ? shift[j] : 0),
+ * the reference's obsoper(H, x) + Hshift (assimilation.F90:3110-3114); a negative index
+ * marks an unused pair (rows with fewer than K non-zeros). */
+typedef struct oakg_obsoper {
+  int64_t m;             /* rows (observations); must equal dims->m */
+  int32_t K, pad0;       /* pairs per row */
+  const int64_t* index;  /* [m*K] state rows */
+  const double* weight;  /* [m*K] */
+  const double* shift;   /* [m] Hshift, or NULL */
+} oakg_obsoper;
+
+/* Ensemble prologue of Assim (assimilation.F90:3110-3134, ASSIM_SCALING = 1): from the
+ * ensemble Ef (n x N, leading dimension ldE) and H, the mean xf (n), the scaled anomalies
+ * Sf = (Ef - xf)/sqrt(N-1) (n x N, dims->ldS), and the same for HEf = H Ef + Hshift: Hxf (m),
+ * HSf (m x N, dims->ldH). Host or device arrays per dims->mem. */
+int oakg_ensemble_prologue(const oakg_dims* dims, const double* Ef, int64_t ldE,
+                           const oakg_obsoper* H, double* xf, double* Sf, double* Hxf,
+                           double* HSf);
+
+/* Ensemble epilogue (assimilation.F90:3299-3312, 3558-3565): Sa scaled by the posterior
+ * inflation factor, xa clipped to xf +- max_correction (NULL: no clip), then
+ * Ea(:,k) = xa + sqrt(N-1) Sa(:,k) (n x N, leading dimension ldE). */
+int oakg_ensemble_epilogue(const oakg_dims* dims, const double* xf, const double* xa,
+                           const double* Sa, double inflation, const double* max_correction,
+                           double* Ea, int64_t ldE);
+
+/* The local analysis of an ensemble, all on the device: prologue, oakg_locanalysis (dims->ldS
+ * and dims->ldH are ignored: the anomalies are the library's), epilogue. Ea may alias Ef. The
+ * numerical core of oak_assim for schemetype = 1 without the file I/O. */
+int oakg_ens_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                         const int32_t* zone_size, const double* Ef, int64_t ldE,
+                         const oakg_obsoper* H, const double* yo, const double* r_diag,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, double inflation, const double* max_correction,
+                         double* Ea);
+
 /* Prepared local analysis -- no counterpart in the reference; for the repeated analyses of a
  * forecast-analysis cycle whose buffers stay in place (the cycle of assim.F90:71-99 calling
  * locAnalysis each step). oakg_plan_locanalysis takes the arguments of oakg_locanalysis (device

@@ -62,6 +62,13 @@ class Loc(ctypes.Structure):
                 ("cell_size", ctypes.c_double)]
 
 
+class ObsOper(ctypes.Structure):
+    """oakg_obsoper: sparse observation operator, K (index, weight) pairs per observation."""
+    _fields_ = [("m", ctypes.c_int64), ("K", ctypes.c_int32), ("pad0", ctypes.c_int32),
+                ("index", ctypes.c_void_p), ("weight", ctypes.c_void_p),
+                ("shift", ctypes.c_void_p)]
+
+
 _lib = None
 
 
@@ -110,6 +117,17 @@ def lib() -> ctypes.CDLL:
     L.oakg_plan_info.restype = ctypes.c_int
     L.oakg_plan_destroy.argtypes = [ctypes.c_void_p]
     L.oakg_plan_destroy.restype = None
+    L.oakg_ensemble_prologue.argtypes = [ctypes.POINTER(Dims), P, ctypes.c_int64,
+                                         ctypes.POINTER(ObsOper), P, P, P, P]
+    L.oakg_ensemble_prologue.restype = ctypes.c_int
+    L.oakg_ensemble_epilogue.argtypes = [ctypes.POINTER(Dims), P, P, P, ctypes.c_double, P, P,
+                                         ctypes.c_int64]
+    L.oakg_ensemble_epilogue.restype = ctypes.c_int
+    L.oakg_ens_locanalysis.argtypes = ([ctypes.POINTER(Dims), ctypes.POINTER(Loc),
+                                        ctypes.c_int32, P, P, ctypes.c_int64,
+                                        ctypes.POINTER(ObsOper)] + [P] * 9
+                                       + [ctypes.c_double, P, P])
+    L.oakg_ens_locanalysis.restype = ctypes.c_int
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -308,6 +326,102 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
         A.vec(nobs, np.int32, "nobs"))
     _check(rc)
     return xa, Sa, ampl, nobs
+
+
+def _obsoper(A, H_index, H_weight, H_shift, m):
+    """oakg_obsoper from (m, K) index / weight arrays (host or device, as A)."""
+    if m == 0:
+        return None
+    K = int(H_index.shape[1]) if len(H_index.shape) == 2 else 1
+    if A.device:
+        if H_index.dtype.__str__() != "torch.int64":
+            raise OakError(ERR_ARGS, "H_index: expected an int64 CUDA tensor")
+        A.keep.append(H_index)
+        pidx = ctypes.c_void_p(H_index.contiguous().data_ptr())
+    else:
+        idx = np.ascontiguousarray(np.asarray(H_index, dtype=np.int64)).reshape(-1)
+        A.keep.append(idx)
+        pidx = ctypes.c_void_p(idx.ctypes.data)
+    H = ObsOper(m=m, K=K, index=pidx, weight=A.vec(H_weight, n=m * K, name="H_weight"),
+                shift=A.vec(H_shift, n=m, name="H_shift"))
+    A.keep.append(H)
+    return H
+
+
+def ensemble_prologue(Ef, H_index, H_weight, H_shift=None):
+    """Mean and scaled anomalies of the ensemble and of H Ef + Hshift
+    (assimilation.F90:3110-3134). ``H_index``/``H_weight``: (m, K) sparse rows (index < 0
+    unused). Returns ``(xf, Sf, Hxf, HSf)``."""
+    n, N = int(Ef.shape[0]), int(Ef.shape[1])
+    m = int(H_index.shape[0])
+    device = _device_mode(Ef, H_weight, H_shift)
+    A = _Args(device)
+    pE, ldE = A.mat(Ef, n, N, "Ef")
+    H = _obsoper(A, H_index, H_weight, H_shift, m)
+    xf = _empty_like_mode(device, (n,), like=Ef)
+    Sf = _empty_like_mode(device, (n, N), order="F", like=Ef)
+    Hxf = _empty_like_mode(device, (m,), like=Ef)
+    HSf = _empty_like_mode(device, (m, N), order="F", like=Ef)
+    dims = Dims(n=n, N=N, m=m, ldS=n, ldH=max(m, 1), mem=MEM_DEVICE if device else MEM_HOST)
+    _sync_torch(device, Ef)
+    rc = lib().oakg_ensemble_prologue(ctypes.byref(dims), pE, ldE,
+                                      None if H is None else ctypes.byref(H),
+                                      A.vec(xf, name="xf"), A.mat(Sf, n, N, "Sf")[0],
+                                      A.vec(Hxf, name="Hxf"), A.mat(HSf, m, N, "HSf")[0])
+    _check(rc)
+    return xf, Sf, Hxf, HSf
+
+
+def ensemble_epilogue(xf, xa, Sa, inflation=1.0, max_correction=None):
+    """Posterior inflation, correction clip and reconstruction
+    (assimilation.F90:3299-3312, 3558-3565). Returns ``Ea`` (n, N)."""
+    n, N = int(Sa.shape[0]), int(Sa.shape[1])
+    device = _device_mode(xf, xa, Sa, max_correction)
+    A = _Args(device)
+    pSa, ldS = A.mat(Sa, n, N, "Sa")
+    Ea = _empty_like_mode(device, (n, N), order="F", like=Sa)
+    dims = Dims(n=n, N=N, m=0, ldS=ldS, ldH=1, mem=MEM_DEVICE if device else MEM_HOST)
+    _sync_torch(device, Sa)
+    rc = lib().oakg_ensemble_epilogue(ctypes.byref(dims), A.vec(xf, n=n, name="xf"),
+                                      A.vec(xa, n=n, name="xa"), pSa, float(inflation),
+                                      A.vec(max_correction, n=n, name="max_correction"),
+                                      A.mat(Ea, n, N, "Ea")[0], n)
+    _check(rc)
+    return Ea
+
+
+def ens_loc_analysis(zone_size, Ef, H_index, H_weight, yo, r_diag, zone_pos, obs_pos, corr_len,
+                     max_len, *, H_shift=None, inflation=1.0, max_correction=None,
+                     weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1, localise_obs=True,
+                     rotate=True, precision=PREC_FP64):
+    """Local analysis of an ensemble on the device: prologue, :func:`loc_analysis`, epilogue
+    (oakg_ens_locanalysis). Returns ``Ea`` (n, N)."""
+    Z = int(zone_size.shape[0])
+    n, N = int(Ef.shape[0]), int(Ef.shape[1])
+    m = int(yo.shape[0])
+    ox, oy, oz, ot = (tuple(obs_pos) + (None,) * 4)[:4]
+    device = _device_mode(zone_size, Ef, H_weight, yo, r_diag, zone_pos, corr_len, max_len,
+                          ox, oy, oz, ot)
+    A = _Args(device)
+    pE, ldE = A.mat(Ef, n, N, "Ef")
+    H = _obsoper(A, H_index, H_weight, H_shift, m)
+    dims = Dims(n=n, N=N, m=m, ldS=n, ldH=max(m, 1), mem=MEM_DEVICE if device else MEM_HOST)
+    loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
+              rotate=int(bool(rotate)), precision=int(precision), flags=0, cell_size=0.0)
+    zp = zone_pos.reshape(-1) if device else np.ascontiguousarray(
+        np.asarray(zone_pos, dtype=np.float64).reshape(Z, 4))
+    Ea = _empty_like_mode(device, (n, N), order="F", like=Ef)
+    _sync_torch(device, Ef)
+    rc = lib().oakg_ens_locanalysis(
+        ctypes.byref(dims), ctypes.byref(loc), Z, A.vec(zone_size, np.int32, "zone_size", Z), pE,
+        ldE, None if H is None else ctypes.byref(H), A.vec(yo, n=m, name="yo"),
+        A.vec(r_diag, n=m, name="r_diag"), A.vec(zp, n=4 * Z, name="zone_pos"),
+        A.vec(ox, n=m, name="obs_x"), A.vec(oy, n=m, name="obs_y"), A.vec(oz, n=m, name="obs_z"),
+        A.vec(ot, n=m, name="obs_t"), A.vec(corr_len, n=Z, name="corr_len"),
+        A.vec(max_len, n=Z, name="max_len"), float(inflation),
+        A.vec(max_correction, n=n, name="max_correction"), A.mat(Ea, n, N, "Ea")[0])
+    _check(rc)
+    return Ea
 
 
 class Plan:

@@ -68,7 +68,8 @@ struct Buf {
 enum BufId {
   B_ZONE_SIZE, B_XF, B_HXF, B_YO, B_R, B_SF, B_HSF, B_ZXYZT, B_OX, B_OY, B_OZ, B_OT, B_CORR,
   B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
-  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_OBS32, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
+  B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_OBS32, B_E_EF, B_E_HIDX, B_E_HW, B_E_HSH, B_E_HEF, B_E_XF, B_E_SF,
+  B_E_HXF, B_E_HSF, B_E_XA, B_E_SA, B_E_MC, B_E_EA, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
   B_COUNT_
 };
 
@@ -975,6 +976,192 @@ int plan_execute_impl(Plan* pl, void* stream) {
   return status_code(*pl->h_status);
 }
 
+// ------------------------------------------------------------------------------------------
+// Ensemble prologue / epilogue (ensemble.cu) and the whole-ensemble local analysis.
+int check_obsoper(const oakg_obsoper* H, int64_t m) {
+  if (m == 0) return OAKG_OK;
+  if (!H) return fail(OAKG_ERR_ARGS, "observation operator is NULL with m > 0");
+  if (H->m != m) return fail(OAKG_ERR_ARGS, "operator has %lld rows, m = %lld",
+                             (long long)H->m, (long long)m);
+  if (H->K < 1) return fail(OAKG_ERR_ARGS, "operator K must be >= 1");
+  if (!H->index || !H->weight) return fail(OAKG_ERR_ARGS, "operator index/weight are NULL");
+  return OAKG_OK;
+}
+
+struct EnsDev {
+  const double *Ef = nullptr, *w = nullptr, *shift = nullptr;
+  const int64_t* idx = nullptr;
+  double *xf = nullptr, *Sf = nullptr, *Hxf = nullptr, *HSf = nullptr, *HEf = nullptr;
+};
+
+// device view of Ef and H, device outputs of the prologue (caller's buffers in device mode)
+int prologue_issue(Ctx* c, const oakg_dims* d, const double* Ef, int64_t ldE,
+                   const oakg_obsoper* H, double* xf, double* Sf, double* Hxf, double* HSf,
+                   EnsDev* E) {
+  const int64_t n = d->n, m = d->m;
+  const int N = d->N, mem = d->mem;
+  int rc;
+  if ((rc = stage_in(c, B_E_EF, Ef, (size_t)ldE * N, mem, &E->Ef, "Ef"))) return rc;
+  if (m > 0) {
+    const size_t mk = (size_t)m * H->K;
+    if ((rc = stage_in(c, B_E_HIDX, H->index, mk, mem, &E->idx, "operator index"))) return rc;
+    if ((rc = stage_in(c, B_E_HW, H->weight, mk, mem, &E->w, "operator weight"))) return rc;
+    if ((rc = stage_in(c, B_E_HSH, H->shift, (size_t)m, mem, &E->shift, "Hshift"))) return rc;
+    if ((rc = scratch(c, B_E_HEF, (size_t)m * N, &E->HEf, "HEf"))) return rc;
+  }
+  if ((rc = stage_out(c, B_E_XF, xf, (size_t)n, mem, &E->xf, "xf"))) return rc;
+  if ((rc = stage_out(c, B_E_SF, Sf, (size_t)d->ldS * N, mem, &E->Sf, "Sf"))) return rc;
+  if ((rc = stage_out(c, B_E_HXF, Hxf, (size_t)(m > 0 ? m : 1), mem, &E->Hxf, "Hxf"))) return rc;
+  if ((rc = stage_out(c, B_E_HSF, HSf, (size_t)(m > 0 ? d->ldH : 1) * N, mem, &E->HSf, "HSf")))
+    return rc;
+  cudaError_t e = ensemble_prologue(n, N, E->Ef, ldE, m, m > 0 ? H->K : 1, E->idx, E->w, E->shift,
+                                    E->xf, E->Sf, d->ldS, E->Hxf, E->HSf, d->ldH, E->HEf,
+                                    c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ensemble prologue");
+  return OAKG_OK;
+}
+
+int prologue_impl(const oakg_dims* d, const double* Ef, int64_t ldE, const oakg_obsoper* H,
+                  double* xf, double* Sf, double* Hxf, double* HSf) {
+  int rc = check_dims(d);
+  if (rc) return rc;
+  if (!Ef || !xf || !Sf) return fail(OAKG_ERR_ARGS, "Ef, xf and Sf are required");
+  if (ldE < d->n) return fail(OAKG_ERR_ARGS, "ldE < n");
+  if ((rc = check_obsoper(H, d->m))) return rc;
+  if (d->m > 0 && (!Hxf || !HSf)) return fail(OAKG_ERR_ARGS, "Hxf and HSf are required");
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  EnsDev E;
+  if ((rc = prologue_issue(c, d, Ef, ldE, H, xf, Sf, Hxf, HSf, &E))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (d->mem == OAKG_MEM_HOST) {
+    const int N = d->N;
+    e = cudaMemcpyAsync(xf, E.xf, d->n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(Sf, E.Sf, (size_t)d->ldS * N * sizeof(double), cudaMemcpyDeviceToHost,
+                          st);
+    if (e == cudaSuccess && d->m > 0)
+      e = cudaMemcpyAsync(Hxf, E.Hxf, d->m * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && d->m > 0)
+      e = cudaMemcpyAsync(HSf, E.HSf, (size_t)d->ldH * N * sizeof(double),
+                          cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "prologue results");
+  return OAKG_OK;
+}
+
+int epilogue_impl(const oakg_dims* d, const double* xf, const double* xa, const double* Sa,
+                  double inflation, const double* max_correction, double* Ea, int64_t ldE) {
+  int rc = check_dims(d);
+  if (rc) return rc;
+  if (!xf || !xa || !Sa || !Ea) return fail(OAKG_ERR_ARGS, "xf, xa, Sa and Ea are required");
+  if (ldE < d->n) return fail(OAKG_ERR_ARGS, "ldE < n");
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t n = d->n;
+  const int N = d->N, mem = d->mem;
+  const double *dxf, *dxa, *dSa, *dmc;
+  double* dEa;
+  if ((rc = stage_in(c, B_E_XF, xf, (size_t)n, mem, &dxf, "xf"))) return rc;
+  if ((rc = stage_in(c, B_E_XA, xa, (size_t)n, mem, &dxa, "xa"))) return rc;
+  if ((rc = stage_in(c, B_E_SA, Sa, (size_t)d->ldS * N, mem, &dSa, "Sa"))) return rc;
+  if ((rc = stage_in(c, B_E_MC, max_correction, (size_t)n, mem, &dmc, "maxCorrection")))
+    return rc;
+  if ((rc = stage_out(c, B_E_EA, Ea, (size_t)ldE * N, mem, &dEa, "Ea"))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = ensemble_epilogue(n, N, dxf, dxa, dSa, d->ldS, inflation, dmc, dEa, ldE, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(Ea, dEa, (size_t)ldE * N * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "ensemble epilogue");
+  return OAKG_OK;
+}
+
+int ens_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
+                         const int32_t* zone_size, const double* Ef, int64_t ldE,
+                         const oakg_obsoper* H, const double* yo, const double* r_diag,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, double inflation,
+                         const double* max_correction, double* Ea) {
+  int rc = check_loc(d, loc, Z);
+  if (rc) return rc;
+  if (!Ef || !Ea) return fail(OAKG_ERR_ARGS, "Ef and Ea are required");
+  if (ldE < d->n) return fail(OAKG_ERR_ARGS, "ldE < n");
+  if ((rc = check_obsoper(H, d->m))) return rc;
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t n = d->n, m = d->m;
+  const int N = d->N, mem = d->mem;
+  // device views of every input (the inner analysis runs in device mode)
+  const int32_t* dzs;
+  const double *dyo = nullptr, *dr = nullptr, *dzp, *dox = nullptr, *doy = nullptr,
+               *doz = nullptr, *dot = nullptr, *dcorr, *dmaxl, *dmc;
+  if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &dzs, "zone_size"))) return rc;
+  if ((rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &dzp, "zone_xyzt"))) return rc;
+  if ((rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &dcorr, "corr_len"))) return rc;
+  if ((rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &dmaxl, "max_len"))) return rc;
+  if ((rc = stage_in(c, B_E_MC, max_correction, (size_t)n, mem, &dmc, "maxCorrection")))
+    return rc;
+  if (m > 0) {
+    if ((rc = stage_in(c, B_YO, yo, (size_t)m, mem, &dyo, "yo"))) return rc;
+    if ((rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &dr, "r_diag"))) return rc;
+    if ((rc = stage_in(c, B_OX, obs_x, (size_t)m, mem, &dox, "obs_x"))) return rc;
+    if ((rc = stage_in(c, B_OY, obs_y, (size_t)m, mem, &doy, "obs_y"))) return rc;
+    if ((rc = stage_in(c, B_OZ, obs_z, (size_t)m, mem, &doz, "obs_z"))) return rc;
+    if ((rc = stage_in(c, B_OT, obs_t, (size_t)m, mem, &dot, "obs_t"))) return rc;
+  }
+  oakg_dims dd = *d;
+  dd.mem = OAKG_MEM_DEVICE;
+  dd.ldS = n;
+  dd.ldH = m > 0 ? m : 1;
+  EnsDev E;
+  {
+    // prologue outputs into library buffers (device mode with NULL outputs is not allowed,
+    // so the buffers are claimed here and passed as device pointers)
+    double *xf, *Sf, *Hxf, *HSf;
+    if ((rc = scratch(c, B_E_XF, (size_t)n, &xf, "xf")) ||
+        (rc = scratch(c, B_E_SF, (size_t)n * N, &Sf, "Sf")) ||
+        (rc = scratch(c, B_E_HXF, (size_t)(m > 0 ? m : 1), &Hxf, "Hxf")) ||
+        (rc = scratch(c, B_E_HSF, (size_t)(m > 0 ? m : 1) * N, &HSf, "HSf")))
+      return rc;
+    oakg_dims pd = dd;
+    pd.mem = mem;  // Ef and H are staged from the caller's memory kind
+    const double* Ef_view;
+    if ((rc = stage_in(c, B_E_EF, Ef, (size_t)ldE * N, mem, &Ef_view, "Ef"))) return rc;
+    oakg_obsoper Hd{};
+    if (m > 0) {
+      Hd = *H;
+      const size_t mk = (size_t)m * H->K;
+      if ((rc = stage_in(c, B_E_HIDX, H->index, mk, mem, &Hd.index, "operator index")) ||
+          (rc = stage_in(c, B_E_HW, H->weight, mk, mem, &Hd.weight, "operator weight")) ||
+          (rc = stage_in(c, B_E_HSH, H->shift, (size_t)m, mem, &Hd.shift, "Hshift")))
+        return rc;
+    }
+    pd.mem = OAKG_MEM_DEVICE;
+    if ((rc = prologue_issue(c, &pd, Ef_view, ldE, m > 0 ? &Hd : nullptr, xf, Sf, Hxf, HSf, &E)))
+      return rc;
+  }
+  double *xa, *Sa;
+  if ((rc = scratch(c, B_E_XA, (size_t)n, &xa, "xa")) ||
+      (rc = scratch(c, B_E_SA, (size_t)n * N, &Sa, "Sa")))
+    return rc;
+  rc = locanalysis_impl(&dd, loc, Z, dzs, E.xf, E.Hxf, dyo, E.Sf, E.HSf, dr, dzp, dox, doy, doz,
+                        dot, dcorr, dmaxl, xa, Sa, nullptr, nullptr);
+  if (rc) return rc;
+  double* dEa;
+  if ((rc = stage_out(c, B_E_EA, Ea, (size_t)ldE * N, mem, &dEa, "Ea"))) return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = ensemble_epilogue(n, N, E.xf, xa, Sa, n, inflation, dmc, dEa, ldE, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(Ea, dEa, (size_t)ldE * N * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "ensemble epilogue");
+  return OAKG_OK;
+}
+
 int release_impl() {
   for (auto& cp : g_ctx) {
     if (!cp) continue;
@@ -1162,5 +1349,42 @@ void oakg_plan_destroy(oakg_plan* plan) {
   delete plan;
 }
 
+int oakg_ensemble_prologue(const oakg_dims* dims, const double* Ef, int64_t ldE,
+                           const oakg_obsoper* H, double* xf, double* Sf, double* Hxf,
+                           double* HSf) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::prologue_impl(dims, Ef, ldE, H, xf, Sf, Hxf, HSf);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_ensemble_epilogue(const oakg_dims* dims, const double* xf, const double* xa,
+                           const double* Sa, double inflation, const double* max_correction,
+                           double* Ea, int64_t ldE) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::epilogue_impl(dims, xf, xa, Sa, inflation, max_correction, Ea, ldE);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_ens_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                         const int32_t* zone_size, const double* Ef, int64_t ldE,
+                         const oakg_obsoper* H, const double* yo, const double* r_diag,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, double inflation, const double* max_correction,
+                         double* Ea) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::ens_locanalysis_impl(dims, loc, nzones, zone_size, Ef, ldE, H, yo, r_diag,
+                                      zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len,
+                                      inflation, max_correction, Ea);
+  oakg::last_status() = rc;
+  return rc;
+}
+
 }  // extern "C"
+
 

@@ -129,6 +129,16 @@ cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
                             float* d_ampl, int32_t* d_status, cudaStream_t st);
 
+// ---- ensemble.cu: the ensemble prologue (mean, anomalies, sparse H E + Hshift) and epilogue
+// (inflation, correction clip, reconstruction); HEf_scratch holds m x N values.
+cudaError_t ensemble_prologue(int64_t n, int N, const double* Ef, int64_t ldE, int64_t m, int K,
+                              const int64_t* idx, const double* w, const double* shift,
+                              double* xf, double* Sf, int64_t ldS, double* Hxf, double* HSf,
+                              int64_t ldH, double* HEf_scratch, cudaStream_t st);
+cudaError_t ensemble_epilogue(int64_t n, int N, const double* xf, const double* xa,
+                              const double* Sa, int64_t ldS, double inflation,
+                              const double* maxcorr, double* Ea, int64_t ldE, cudaStream_t st);
+
 // ---- zone_update.cu
 // xa = xf + Sf ampl, Sa = Sf T per zone; zones with nobs == 0 copy (xa = xf, Sa = Sf).
 cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,

@@ -1,0 +1,74 @@
+"""Ensemble prologue / epilogue and the whole-ensemble local analysis on the GPU, against the
+oracle (assimilation.F90:3110-3134, 3299-3312, 3558-3565 restated in oracle/oakref.py)."""
+import numpy as np
+import pytest
+
+from oak_gb300.workloads import local_case
+from oracle import cref, oakref
+
+pytestmark = pytest.mark.gpu
+
+
+def _sparse_operator(c, rng):
+    """Two non-zeros per observation (observed level and its neighbour), some rows with one."""
+    idx2 = np.where(c.obs_index % 20 > 0, c.obs_index - 1, c.obs_index + 1)
+    index = np.stack([c.obs_index, idx2], axis=1).astype(np.int64)
+    w = rng.uniform(0.2, 0.8, c.m)
+    weight = np.stack([w, 1 - w], axis=1)
+    index[::7, 1] = -1  # unused pair
+    shift = 0.01 * rng.standard_normal(c.m)
+    H = np.zeros((c.m, c.n))
+    for t in range(2):
+        ok = index[:, t] >= 0
+        np.add.at(H, (np.nonzero(ok)[0], index[ok, t]), weight[ok, t])
+    return index, weight, shift, H
+
+
+def test_prologue_matches_oracle(oakg):
+    rng = np.random.default_rng(11)
+    c = local_case(scale=1 / 10, N=24, keep_ensemble=True)
+    index, weight, shift, H = _sparse_operator(c, rng)
+    xf, Sf, Hxf, HSf = oakg.ensemble_prologue(c.Ef, index, weight, shift)
+    xf_o, Hxf_o, Sf_o, HSf_o = oakref.ensemble_prologue(c.Ef, H @ c.Ef + shift[:, None])
+    for a, b in ((xf, xf_o), (Sf, Sf_o), (Hxf, Hxf_o), (HSf, HSf_o)):
+        assert np.allclose(a, b, rtol=1e-13, atol=1e-13 * np.abs(b).max())
+
+
+def test_epilogue_matches_oracle(oakg):
+    rng = np.random.default_rng(12)
+    n, N = 5000, 16
+    xf = rng.standard_normal(n)
+    xa = xf + rng.standard_normal(n)
+    Sa = np.asfortranarray(rng.standard_normal((n, N)))
+    mc = np.full(n, 0.8)
+    for infl, m in ((1.0, None), (1.05, mc)):
+        Ea = oakg.ensemble_epilogue(xf, xa, Sa, inflation=infl, max_correction=m)
+        Ea_o = oakref.ensemble_epilogue(xf, xa, Sa, inflation=infl, max_correction=m)
+        assert np.allclose(Ea, Ea_o, rtol=1e-15, atol=1e-15)
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_ensemble_local_analysis_matches_oracle(oakg, device):
+    import torch
+    rng = np.random.default_rng(13)
+    c = local_case(scale=1 / 10, N=24, keep_ensemble=True)
+    index, weight, shift, H = _sparse_operator(c, rng)
+    mc = np.full(c.n, 0.5)
+    args = (c.zone_size, c.Ef, index, weight, c.yo, c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+            c.max_len)
+    kw = dict(H_shift=shift, inflation=1.05, max_correction=mc, weight=c.weight)
+    if device:
+        dev = torch.device("cuda", 0)
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+        F = lambda a: torch.as_tensor(np.ascontiguousarray(np.asarray(a).T), device=dev).t()
+        args = (T(c.zone_size), F(c.Ef), T(index), T(weight), T(c.yo), T(c.r_diag),
+                T(c.zone_pos), tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
+        kw.update(H_shift=T(shift), max_correction=T(mc))
+    Ea = oakg.ens_loc_analysis(*args, **kw)
+    if device:
+        Ea = Ea.cpu().numpy()
+    xf, Hxf, Sf, HSf = oakref.ensemble_prologue(c.Ef, H @ c.Ef + shift[:, None])
+    xa, Sa, _, _ = cref.locanalysis(c.zone_size, xf, Hxf, c.yo, Sf, HSf, c.r_diag, c.zone_pos,
+                                    c.obs_pos, c.corr_len, c.max_len, kind=c.weight)
+    Ea_o = oakref.ensemble_epilogue(xf, xa, Sa, inflation=1.05, max_correction=mc)
+    assert np.linalg.norm(Ea - Ea_o) <= 1e-10 * np.linalg.norm(Ea_o - c.Ef)
