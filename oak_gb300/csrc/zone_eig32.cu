@@ -12,7 +12,8 @@
 // cross-thread reductions: the shared operand is broadcast with 128-bit shared loads.
 //
 // E1: thread r holds row r of the scaled symmetric matrix. Row k equals column k, so thread k
-//   forms reflector k; p = beta A v is one register dot per thread; two barriers per step.
+//   forms reflector k; p = beta A v is one register dot per thread; w = p - kc v is formed
+//   once per row and shared; three barriers per step; warps whose rows are final skip work.
 //   Reflector k is stored vector-major, zero padded, in row k of the zone's matrix slot:
 //   slot[k*N + r] = v_k[r] (v_k[r] = 0 for r <= k).
 // E2a: one thread per zone, implicit QR sweeps (working arrays in shared memory).
@@ -69,10 +70,12 @@ constexpr int kT1 = 64;
 __global__ void __launch_bounds__(kT1, 6)
     k_eig_tridiag32(int N, int32_t nzc, float* __restrict__ GT, float* __restrict__ aux,
                     const int32_t* __restrict__ nobs) {
-  // v, p, the partial dots and beta are double-buffered by step parity: the update of step k
-  // re-reads v and p after the second barrier while the owner of step k+1 already writes
+  // v, the partial dots and beta are double-buffered by step parity: the update of step k
+  // re-reads v after the last barrier while the owner of step k+1 already writes. w needs one
+  // buffer: it is written after the second barrier of a step, when every thread has finished
+  // the previous step's update.
   __shared__ __align__(16) float vbuf2[2][NB];
-  __shared__ __align__(16) float pbuf2[2][NB];
+  __shared__ __align__(16) float wbuf[NB];
   __shared__ float red[2][2];
   __shared__ float s_beta[2];
   const int r = threadIdx.x, lane = r & 31, warp = r >> 5;
@@ -98,7 +101,6 @@ __global__ void __launch_bounds__(kT1, 6)
   __syncthreads();  // every row read before reflectors overwrite the slot; red reused
   for (int k = 0; k < N - 2; k++) {
     float* vbuf = vbuf2[k & 1];
-    float* pbuf = pbuf2[k & 1];
     if (r == k) {
       // reflector of x = A[k+1:, k] = A[k][k+1:]. Single entries are read back through
       // shared memory: an equality-selected register element would become a dynamic index
@@ -134,30 +136,38 @@ __global__ void __launch_bounds__(kT1, 6)
     if (r < N) Gz[(int64_t)k * N + r] = vbuf[r];  // reflector k, vector-major, zero padded
     if (bk == 0.f) continue;                       // uniform: identity reflector
     const float vr = vbuf[r];
-    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+    // rows at or above k are final (their entries right of the band are never read again):
+    // a warp whose rows are all final, or all padding, skips the products; its p and w are 0
+    const bool idle = (32 * warp + 31 <= k) || (32 * warp >= N);
+    float p = 0.f;
+    if (!idle) {
+      float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
 #pragma unroll
-    for (int g = 0; g < 4; g++) {
-      if (16 * g + 15 > k) {  // v vanishes on columns <= k
+      for (int g = 0; g < 4; g++) {
+        if (16 * g + 15 > k) {  // v vanishes on columns <= k
 #pragma unroll
-        for (int m = 0; m < 4; m++) {
-          const int c = 16 * g + 4 * m;
-          const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
-          p0 = fmaf(a[c + 0], v4.x, p0);
-          p1 = fmaf(a[c + 1], v4.y, p1);
-          p2 = fmaf(a[c + 2], v4.z, p2);
-          p3 = fmaf(a[c + 3], v4.w, p3);
+          for (int m = 0; m < 4; m++) {
+            const int c = 16 * g + 4 * m;
+            const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
+            p0 = fmaf(a[c + 0], v4.x, p0);
+            p1 = fmaf(a[c + 1], v4.y, p1);
+            p2 = fmaf(a[c + 2], v4.z, p2);
+            p3 = fmaf(a[c + 3], v4.w, p3);
+          }
         }
       }
+      p = bk * ((p0 + p1) + (p2 + p3));
     }
-    const float p = bk * ((p0 + p1) + (p2 + p3));
-    pbuf[r] = p;
     float pv = p * vr;
     for (int o = 16; o > 0; o >>= 1) pv += __shfl_xor_sync(0xffffffffu, pv, o);
     if (lane == 0) red[k & 1][warp] = pv;
-    __syncthreads();  // S2: p and the partial dots published
+    __syncthreads();  // S2: the partial dots published
     const float kc = 0.5f * bk * (red[k & 1][0] + red[k & 1][1]);
-    const float wr = fmaf(-kc, vr, p);
-    // A -= v w^T + w v^T, w = p - kc v
+    const float wr = fmaf(-kc, vr, p);  // w = p - kc v, once per row
+    wbuf[r] = wr;
+    __syncthreads();  // S3: w published
+    if (idle) continue;
+    // A -= v w^T + w v^T
 #pragma unroll
     for (int g = 0; g < 4; g++) {
       if (16 * g + 15 > k) {
@@ -165,14 +175,11 @@ __global__ void __launch_bounds__(kT1, 6)
         for (int m = 0; m < 4; m++) {
           const int c = 16 * g + 4 * m;
           const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
-          const float4 p4 = *reinterpret_cast<const float4*>(pbuf + c);
+          const float4 w4 = *reinterpret_cast<const float4*>(wbuf + c);
           const float vc[4] = {v4.x, v4.y, v4.z, v4.w};
-          const float pc[4] = {p4.x, p4.y, p4.z, p4.w};
+          const float wc[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
-          for (int t = 0; t < 4; t++) {
-            const float wc = fmaf(-kc, vc[t], pc[t]);
-            a[c + t] = fmaf(-vr, wc, fmaf(-wr, vc[t], a[c + t]));
-          }
+          for (int t = 0; t < 4; t++) a[c + t] = fmaf(-vr, wc[t], fmaf(-wr, vc[t], a[c + t]));
         }
       }
     }
