@@ -7,13 +7,13 @@
 // top of zone_eig.cu lists the reference lines); the matrix is padded to 64 x 64 with zeros,
 // which adds decoupled zero rows that no output reads.
 //
-// Every stage runs one block of 64 threads per zone and keeps a row (E1) or an eigenvector
-// (E3, E2b) of 64 elements per thread in registers, so matrix-vector products need no
+// The stages keep rows (E1: two per lane, one warp per zone) or eigenvectors (E2b, E3: one per
+// thread, 64 threads per zone) of 64 elements in registers, so matrix-vector products need no
 // cross-thread reductions: the shared operand is broadcast with 128-bit shared loads.
 //
-// E1: thread r holds row r of the scaled symmetric matrix. Row k equals column k, so thread k
-//   forms reflector k; p = beta A v is one register dot per thread; w = p - kc v is formed
-//   once per row and shared; three barriers per step; warps whose rows are final skip work.
+// E1: one warp per zone, lane t holding rows t and t + 32 of the scaled symmetric matrix. Row
+//   k equals column k, so the lane holding row k forms reflector k; p = beta A v is a register
+//   dot per row; w = p - kc v is formed once per row and shared; warp-level synchronisation.
 //   Reflector k is stored vector-major, zero padded, in row k of the zone's matrix slot:
 //   slot[k*N + r] = v_k[r] (v_k[r] = 0 for r <= k).
 // E2a: one thread per zone, implicit QR sweeps (working arrays in shared memory).
@@ -61,87 +61,95 @@ __device__ __forceinline__ void vstore(const float (&x)[NB], float* p) {
 }
 
 // ------------------------------------------------------------------------------------ E1
-// One block of 64 threads per zone; thread r holds row r of the scaled symmetric matrix in
-// registers (a[c] = A[r][c]). Row k equals column k, so the owner of step k is thread k.
-// Columns at or left of k are not read after step k, so 16-column groups lying entirely there
-// are skipped (the same groups for every thread).
-constexpr int kT1 = 64;
+// One warp per zone (kZpb zones per block). Lane t holds rows t and t + 32 of the scaled
+// symmetric matrix in registers (a0[c] = A[t][c], a1[c] = A[t+32][c]). Row k equals column k,
+// so the lane holding row k forms reflector k; p = beta A v is a register dot per row; every
+// synchronisation is warp-level. Columns at or left of k are not read after step k, so
+// 16-column groups lying entirely there are skipped, and the first row set is skipped once all
+// its rows are final (k >= 31).
+constexpr int kZpb = 4;
 
-__global__ void __launch_bounds__(kT1, 6)
+template <int SLOT>
+__device__ __forceinline__ void owner_reflector(const float (&row)[NB], int k, int N, float* vbuf,
+                                                float* ax, float* beta_slot) {
+  // single entries are read back through shared memory: an equality-selected register
+  // element would become a dynamic index and move the row to local memory
+  vstore(row, vbuf);
+  const float x0 = vbuf[k + 1], dk = vbuf[k];
+  float sig = 0.f;
+#pragma unroll
+  for (int c = 0; c < NB; c++)
+    if (c > k + 1) sig = fmaf(row[c], row[c], sig);
+  const float mu = sqrtf(fmaf(x0, x0, sig));
+  const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
+  const float vv = fmaf(v0, v0, sig);
+  const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
+  const float bk = skip ? 0.f : 2.f / vv;
+#pragma unroll
+  for (int c = 0; c < NB; c += 4) {
+    float4 q4;
+    q4.x = (c + 0 > k + 1) ? row[c + 0] : 0.f;
+    q4.y = (c + 1 > k + 1) ? row[c + 1] : 0.f;
+    q4.z = (c + 2 > k + 1) ? row[c + 2] : 0.f;
+    q4.w = (c + 3 > k + 1) ? row[c + 3] : 0.f;
+    *reinterpret_cast<float4*>(vbuf + c) = q4;
+  }
+  vbuf[k + 1] = skip ? x0 : v0;
+  ax[k] = dk;                                        // d_k
+  ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);  // e_k
+  ax[2 * N + k] = bk;                                // beta_k
+  *beta_slot = bk;
+}
+
+__global__ void __launch_bounds__(32 * kZpb, 3)
     k_eig_tridiag32(int N, int32_t nzc, float* __restrict__ GT, float* __restrict__ aux,
                     const int32_t* __restrict__ nobs) {
-  // v, the partial dots and beta are double-buffered by step parity: the update of step k
-  // re-reads v after the last barrier while the owner of step k+1 already writes. w needs one
-  // buffer: it is written after the second barrier of a step, when every thread has finished
-  // the previous step's update.
-  __shared__ __align__(16) float vbuf2[2][NB];
-  __shared__ __align__(16) float wbuf[NB];
-  __shared__ float red[2][2];
-  __shared__ float s_beta[2];
-  const int r = threadIdx.x, lane = r & 31, warp = r >> 5;
-  const int32_t zl = blockIdx.x;
-  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  __shared__ __align__(16) float vbuf_s[kZpb][NB];
+  __shared__ __align__(16) float wbuf_s[kZpb][NB];
+  __shared__ float beta_s[kZpb];
+  const int lane = threadIdx.x & 31, wz = threadIdx.x >> 5;
+  const int32_t zl = blockIdx.x * kZpb + wz;
+  if (zl >= nzc || nobs[zl] == 0) return;  // warp-uniform; only warp-level synchronisation
+  float* vbuf = vbuf_s[wz];
+  float* wbuf = wbuf_s[wz];
   float* Gz = GT + (int64_t)zl * N * N;
   float* ax = aux + (int64_t)zl * aux_stride32(N);
-  float a[NB];
+  const int r0 = lane, r1 = lane + 32;
+  float a0[NB], a1[NB];
 #pragma unroll
-  for (int c = 0; c < NB; c++) a[c] = (r < N && c < N) ? Gz[r * N + c] : 0.f;
+  for (int c = 0; c < NB; c++) {
+    a0[c] = (r0 < N && c < N) ? Gz[r0 * N + c] : 0.f;
+    a1[c] = (r1 < N && c < N) ? Gz[r1 * N + c] : 0.f;
+  }
   float amax = 0.f;
 #pragma unroll
-  for (int c = 0; c < NB; c++) amax = fmaxf(amax, fabsf(a[c]));
+  for (int c = 0; c < NB; c++) amax = fmaxf(amax, fmaxf(fabsf(a0[c]), fabsf(a1[c])));
   for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  if (lane == 0) red[0][warp] = amax;
-  __syncthreads();
-  float scale = fmaxf(red[0][0], red[0][1]);
+  float scale = amax;
   if (!(scale > 0.f) || isinf(scale)) scale = 1.f;
   const float iscale = 1.f / scale;
 #pragma unroll
-  for (int c = 0; c < NB; c++) a[c] *= iscale;
-  if (r == 0) ax[5 * N] = scale;
-  __syncthreads();  // every row read before reflectors overwrite the slot; red reused
+  for (int c = 0; c < NB; c++) {
+    a0[c] *= iscale;
+    a1[c] *= iscale;
+  }
+  if (lane == 0) ax[5 * N] = scale;
+  __syncwarp();  // every row read before reflectors overwrite the slot
   for (int k = 0; k < N - 2; k++) {
-    float* vbuf = vbuf2[k & 1];
-    if (r == k) {
-      // reflector of x = A[k+1:, k] = A[k][k+1:]. Single entries are read back through
-      // shared memory: an equality-selected register element would become a dynamic index
-      // and move the whole row to local memory.
-      vstore(a, vbuf);
-      const float x0 = vbuf[k + 1], dk = vbuf[k];
-      float sig = 0.f;
-#pragma unroll
-      for (int c = 0; c < NB; c++)
-        if (c > k + 1) sig = fmaf(a[c], a[c], sig);
-      const float mu = sqrtf(fmaf(x0, x0, sig));
-      const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
-      const float vv = fmaf(v0, v0, sig);
-      const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
-      const float bk = skip ? 0.f : 2.f / vv;
-#pragma unroll
-      for (int c = 0; c < NB; c += 4) {
-        float4 q4;
-        q4.x = (c + 0 > k + 1) ? a[c + 0] : 0.f;
-        q4.y = (c + 1 > k + 1) ? a[c + 1] : 0.f;
-        q4.z = (c + 2 > k + 1) ? a[c + 2] : 0.f;
-        q4.w = (c + 3 > k + 1) ? a[c + 3] : 0.f;
-        *reinterpret_cast<float4*>(vbuf + c) = q4;
-      }
-      vbuf[k + 1] = skip ? x0 : v0;
-      ax[k] = dk;                                          // d_k
-      ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);    // e_k
-      ax[2 * N + k] = bk;                                  // beta_k
-      s_beta[k & 1] = bk;
+    if (lane == (k & 31)) {
+      if (k < 32)
+        owner_reflector<0>(a0, k, N, vbuf, ax, &beta_s[wz]);
+      else
+        owner_reflector<1>(a1, k, N, vbuf, ax, &beta_s[wz]);
     }
-    __syncthreads();  // S1: v and beta published (beta double-buffered by step parity)
-    const float bk = s_beta[k & 1];
-    if (r < N) Gz[(int64_t)k * N + r] = vbuf[r];  // reflector k, vector-major, zero padded
-    if (bk == 0.f) continue;                       // uniform: identity reflector
-    const float vr = vbuf[r];
-    // rows at or above k are final (their entries right of the band are never read again):
-    // a warp whose rows are all final, or all padding, skips the products; its p and w are 0
-    const bool idle = (32 * warp + 31 <= k) || (32 * warp >= N);
-    float p = 0.f;
-    if (!idle) {
-      float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+    __syncwarp();  // v and beta published
+    const float bk = beta_s[wz];
+    const float v0r = vbuf[r0], v1r = vbuf[r1];
+    if (r0 < N) Gz[(int64_t)k * N + r0] = v0r;  // reflector k, vector-major, zero padded
+    if (r1 < N) Gz[(int64_t)k * N + r1] = v1r;
+    if (bk != 0.f) {  // warp-uniform; beta = 0 is an identity reflector
+      const bool act0 = (k < 31);  // rows 0..31 are all final once k >= 31
+      float p00 = 0.f, p01 = 0.f, p10 = 0.f, p11 = 0.f;
 #pragma unroll
       for (int g = 0; g < 4; g++) {
         if (16 * g + 15 > k) {  // v vanishes on columns <= k
@@ -149,53 +157,66 @@ __global__ void __launch_bounds__(kT1, 6)
           for (int m = 0; m < 4; m++) {
             const int c = 16 * g + 4 * m;
             const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
-            p0 = fmaf(a[c + 0], v4.x, p0);
-            p1 = fmaf(a[c + 1], v4.y, p1);
-            p2 = fmaf(a[c + 2], v4.z, p2);
-            p3 = fmaf(a[c + 3], v4.w, p3);
+            if (act0) {
+              p00 = fmaf(a0[c + 0], v4.x, p00);
+              p01 = fmaf(a0[c + 1], v4.y, p01);
+              p00 = fmaf(a0[c + 2], v4.z, p00);
+              p01 = fmaf(a0[c + 3], v4.w, p01);
+            }
+            p10 = fmaf(a1[c + 0], v4.x, p10);
+            p11 = fmaf(a1[c + 1], v4.y, p11);
+            p10 = fmaf(a1[c + 2], v4.z, p10);
+            p11 = fmaf(a1[c + 3], v4.w, p11);
           }
         }
       }
-      p = bk * ((p0 + p1) + (p2 + p3));
-    }
-    float pv = p * vr;
-    for (int o = 16; o > 0; o >>= 1) pv += __shfl_xor_sync(0xffffffffu, pv, o);
-    if (lane == 0) red[k & 1][warp] = pv;
-    __syncthreads();  // S2: the partial dots published
-    const float kc = 0.5f * bk * (red[k & 1][0] + red[k & 1][1]);
-    const float wr = fmaf(-kc, vr, p);  // w = p - kc v, once per row
-    wbuf[r] = wr;
-    __syncthreads();  // S3: w published
-    if (idle) continue;
-    // A -= v w^T + w v^T
+      const float p0 = bk * (p00 + p01), p1 = bk * (p10 + p11);
+      float pv = fmaf(p0, v0r, p1 * v1r);
+      for (int o = 16; o > 0; o >>= 1) pv += __shfl_xor_sync(0xffffffffu, pv, o);
+      const float kc = 0.5f * bk * pv;
+      const float w0 = fmaf(-kc, v0r, p0), w1 = fmaf(-kc, v1r, p1);  // w = p - kc v
+      wbuf[r0] = w0;
+      wbuf[r1] = w1;
+      __syncwarp();  // w published
+      // A -= v w^T + w v^T
 #pragma unroll
-    for (int g = 0; g < 4; g++) {
-      if (16 * g + 15 > k) {
+      for (int g = 0; g < 4; g++) {
+        if (16 * g + 15 > k) {
 #pragma unroll
-        for (int m = 0; m < 4; m++) {
-          const int c = 16 * g + 4 * m;
-          const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
-          const float4 w4 = *reinterpret_cast<const float4*>(wbuf + c);
-          const float vc[4] = {v4.x, v4.y, v4.z, v4.w};
-          const float wc[4] = {w4.x, w4.y, w4.z, w4.w};
+          for (int m = 0; m < 4; m++) {
+            const int c = 16 * g + 4 * m;
+            const float4 v4 = *reinterpret_cast<const float4*>(vbuf + c);
+            const float4 w4 = *reinterpret_cast<const float4*>(wbuf + c);
+            const float vc[4] = {v4.x, v4.y, v4.z, v4.w};
+            const float wc[4] = {w4.x, w4.y, w4.z, w4.w};
 #pragma unroll
-          for (int t = 0; t < 4; t++) a[c + t] = fmaf(-vr, wc[t], fmaf(-wr, vc[t], a[c + t]));
+            for (int t = 0; t < 4; t++) {
+              if (act0) a0[c + t] = fmaf(-v0r, wc[t], fmaf(-w0, vc[t], a0[c + t]));
+              a1[c + t] = fmaf(-v1r, wc[t], fmaf(-w1, vc[t], a1[c + t]));
+            }
+          }
         }
       }
     }
+    __syncwarp();  // v and w consumed before the next owner writes
   }
-  // trailing 2 x 2 block (rows read back through shared memory, see above)
-  __syncthreads();  // last step's reads of the buffers done
-  if (r == N - 2) vstore(a, vbuf2[0]);
-  if (r == N - 1) vstore(a, vbuf2[1]);
-  if (r == N - 2) {
-    ax[N - 2] = vbuf2[0][N - 2];
-    ax[2 * N + N - 2] = 0.f;
-  } else if (r == N - 1) {
-    ax[N + N - 2] = vbuf2[1][N - 2];
-    ax[N - 1] = vbuf2[1][N - 1];
-    ax[N + N - 1] = 0.f;
-    ax[2 * N + N - 1] = 0.f;
+  // trailing 2 x 2 block: rows N-2 and N-1, read back through shared memory
+  if (N >= 2) {
+    if (lane == ((N - 2) & 31)) {
+      if (N - 2 < 32) vstore(a0, vbuf); else vstore(a1, vbuf);
+    }
+    if (lane == ((N - 1) & 31)) {
+      if (N - 1 < 32) vstore(a0, wbuf); else vstore(a1, wbuf);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      ax[N - 2] = vbuf[N - 2];
+      ax[2 * N + N - 2] = 0.f;
+      ax[N + N - 2] = wbuf[N - 2];
+      ax[N - 1] = wbuf[N - 1];
+      ax[N + N - 1] = 0.f;
+      ax[2 * N + N - 1] = 0.f;
+    }
   }
 }
 
@@ -790,7 +811,8 @@ cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
                           cudaStream_t st) {
   if (N < 2 || N > NB) return cudaErrorInvalidValue;
-  k_eig_tridiag32<<<nzc > 0 ? nzc : 1, kT1, 0, st>>>(N, nzc, d_GT, d_aux, d_nobs);
+  const int blocks = (nzc + kZpb - 1) / kZpb;
+  k_eig_tridiag32<<<blocks > 0 ? blocks : 1, 32 * kZpb, 0, st>>>(N, nzc, d_GT, d_aux, d_nobs);
   return cudaGetLastError();
 }
 
