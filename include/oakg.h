@@ -259,7 +259,14 @@ int64_t oakg_launch_count(void);
  * denominator of the FP64 kernels. */
 int oakg_fp64_peak(double* tflops);
 
-/* OAK's C interface (assimilation.F90:4885-4935). */
+/* OAK's C interface (assimilation.F90:4885-4935), same names and signatures. oak_init checks
+ * that the init file is readable (OAKG_ERR_INIT otherwise) and creates the library's device
+ * context (stream, events; buffers grow on use); oak_done frees it (as oakg_release). The
+ * reference's init-file driver behind oak_assim -- model and observation files (NetCDF / GHER),
+ * state packing by masks, observation-operator generation, diagnostics -- is not part of this
+ * library: oak_assim records OAKG_ERR_NOTIMPL. Its numerical core is oakg_ens_locanalysis,
+ * which a driver calls once it has read the files. The reference's functions return nothing;
+ * the status of the last call is oakg_last_status() / oakg_last_error(). */
 void oak_init(const char* fname);
 void oak_assim(int ntime, int n, int r, double* Ef, double* Ea);
 void oak_done(void);

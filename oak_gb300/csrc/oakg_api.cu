@@ -1179,6 +1179,11 @@ int release_impl() {
   return OAKG_OK;
 }
 
+int context_init_impl() {
+  Ctx* c = nullptr;
+  return get_ctx(&c);
+}
+
 int timings_impl(double* ms, int n) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || !g_ctx[dev]) return 0;

@@ -72,3 +72,20 @@ def test_mixed_rank_deficient_zones(oakg):
     assert (nobs[nobs > 0] < 64).any()
     e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
     assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)
+
+
+def test_dense_clusters_fill_many_tiles(oakg):
+    """Observations packed on a few tracks: zones select well over the 512-entry staging ring
+    of the tensor-core Gram (many K-tiles, ring wrap-around); both forms against the oracle."""
+    c = local_case(scale=1 / 8, N=64, m=300000, track_frac=0.95, ntracks=3)
+    xa_o, Sa_o, _, nobs_o = cref.locanalysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                             c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                             c.max_len, kind=c.weight)
+    assert nobs_o.max() > 1500
+    for prec, tol in ((oakg.PREC_FP64, 1e-10), (oakg.PREC_MIXED, TOL)):
+        xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                            c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                            c.max_len, weight=c.weight, precision=prec)
+        assert np.array_equal(nobs, nobs_o)
+        e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
+        assert e_mean < tol and e_anom < tol, (prec, e_mean, e_anom)
