@@ -7,9 +7,10 @@
 // top of zone_eig.cu lists the reference lines); the matrix is padded to 64 x 64 with zeros,
 // which adds decoupled zero rows that no output reads.
 //
-// The stages keep rows (E1: two per lane, one warp per zone) or eigenvectors (E2b, E3: one per
-// thread, 64 threads per zone) of 64 elements in registers, so matrix-vector products need no
-// cross-thread reductions: the shared operand is broadcast with 128-bit shared loads.
+// The stages keep rows (E1: two per lane, one warp per zone) or eigenvectors (E3: two per lane,
+// one warp per zone; E2b: one per thread, 64 threads per zone) of 64 elements in registers, so
+// matrix-vector products need no cross-thread reductions: the shared operand is broadcast
+// with 128-bit shared loads.
 //
 // E1: one warp per zone, lane t holding rows t and t + 32 of the scaled symmetric matrix. Row
 //   k equals column k, so the lane holding row k forms reflector k; p = beta A v is a register
@@ -18,16 +19,16 @@
 //   slot[k*N + r] = v_k[r] (v_k[r] = 0 for r <= k).
 // E2a: one thread per zone, implicit QR sweeps (working arrays in shared memory).
 // E2b: thread j = eigenpair j, inverse iteration (LU factor in shared memory).
-// E3: thread j holds eigenvector j.
+// E3: one warp per zone, lane t holding eigenvectors t and t + 32.
 //   back-transform U = H_0 ... H_{N-3} Z: per reflector a register dot and axpy, no barrier;
 //   orthogonalisation: right-looking modified Gram-Schmidt, largest eigenvalue first (a vector
 //     is final when every larger-eigenvalue vector has been projected out of it); a vector that
 //     keeps at least half its squared norm is accepted after this one projection (Kahan-Parlett
 //     "twice is enough"), one that does not is marked collapsed and replaced by a
 //     pseudo-random vector orthogonalised (two passes) against every accepted one;
-//   T_sym = (U Q)(U Q)^T with Q = diag((1+lambda)^-1/4): 4 x 16 register blocks, 128-bit
-//     shared loads; Omega = RotateVector(w, v) applied to the register blocks in its
-//     reflector form (rank-one updates, matoper.F90:509-535).
+//   T_sym = (U Q)(U Q)^T with Q = diag((1+lambda)^-1/4): each lane computes two full rows
+//     (128-bit broadcast loads of W's rows); Omega = RotateVector(w, v) applied to those rows
+//     in its reflector form (rank-one updates, matoper.F90:509-535).
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -221,14 +222,25 @@ __global__ void __launch_bounds__(32 * kZpb, 3)
 }
 
 // ------------------------------------------------------------------------------------ E3
-// One block of 64 threads per zone; thread j holds eigenvector j (64 components) in
-// registers. Shared matrices are vector-major with 16-byte rows.
-constexpr int kT3 = 64;
-constexpr size_t kSmem3 = (size_t)(2 * NB * LDV + 12 * NB) * sizeof(float);
+// One warp per zone (kZpb3 zones per block). Lane t holds eigenvectors t and t + 32 (64
+// components each) in registers, so every dot product and axpy is lane-local and the 128-bit
+// loads of a shared row (a reflector, a final vector) serve both vectors. One shared 64 x 64
+// matrix per zone (vector-major, 16-byte rows) holds the reflectors during the
+// back-transform, then the eigenvectors, W = U diag(lambda'^1/4) and finally T for the
+// coalesced store.
+constexpr int kZpb3 = 2;
+struct Zone3 {
+  float buf[NB * LDV];
+  float lam[NB], sq[NB], qs[NB], gs[NB], bet[NB], tt[NB], cc[NB], vv[NB], uv[NB], vn[NB];
+  float t0[NB];
+  int flag[NB];
+};
+constexpr size_t kSmem3 = (size_t)kZpb3 * sizeof(Zone3);
 
-// u . x over the 16-component groups g >= g0 (the others are zero in u)
-__device__ __forceinline__ float vdot(const float (&x)[NB], const float* u, int g0) {
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+// (x0 . u, x1 . u) over the 16-component groups g >= g0 (the others are zero in u)
+__device__ __forceinline__ void vdot2(const float (&x0)[NB], const float (&x1)[NB], const float* u,
+                                      int g0, bool use0, float& d0, float& d1) {
+  float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
 #pragma unroll
   for (int g = 0; g < 4; g++) {
     if (g >= g0) {
@@ -236,18 +248,26 @@ __device__ __forceinline__ float vdot(const float (&x)[NB], const float* u, int 
       for (int m = 0; m < 4; m++) {
         const int c = 16 * g + 4 * m;
         const float4 v = *reinterpret_cast<const float4*>(u + c);
-        s0 = fmaf(x[c], v.x, s0);
-        s1 = fmaf(x[c + 1], v.y, s1);
-        s2 = fmaf(x[c + 2], v.z, s2);
-        s3 = fmaf(x[c + 3], v.w, s3);
+        if (use0) {
+          a0 = fmaf(x0[c], v.x, a0);
+          a1 = fmaf(x0[c + 1], v.y, a1);
+          a0 = fmaf(x0[c + 2], v.z, a0);
+          a1 = fmaf(x0[c + 3], v.w, a1);
+        }
+        b0 = fmaf(x1[c], v.x, b0);
+        b1 = fmaf(x1[c + 1], v.y, b1);
+        b0 = fmaf(x1[c + 2], v.z, b0);
+        b1 = fmaf(x1[c + 3], v.w, b1);
       }
     }
   }
-  return (s0 + s1) + (s2 + s3);
+  d0 = a0 + a1;
+  d1 = b0 + b1;
 }
 
-// x -= f u over the groups g >= g0
-__device__ __forceinline__ void vaxpy(float (&x)[NB], float f, const float* u, int g0) {
+// x0 -= f0 u (if use0), x1 -= f1 u (if use1) over the groups g >= g0
+__device__ __forceinline__ void vaxpy2(float (&x0)[NB], float (&x1)[NB], float f0, float f1,
+                                       const float* u, int g0, bool use0, bool use1) {
 #pragma unroll
   for (int g = 0; g < 4; g++) {
     if (g >= g0) {
@@ -255,310 +275,340 @@ __device__ __forceinline__ void vaxpy(float (&x)[NB], float f, const float* u, i
       for (int m = 0; m < 4; m++) {
         const int c = 16 * g + 4 * m;
         const float4 v = *reinterpret_cast<const float4*>(u + c);
-        x[c] = fmaf(-f, v.x, x[c]);
-        x[c + 1] = fmaf(-f, v.y, x[c + 1]);
-        x[c + 2] = fmaf(-f, v.z, x[c + 2]);
-        x[c + 3] = fmaf(-f, v.w, x[c + 3]);
+        if (use0) {
+          x0[c] = fmaf(-f0, v.x, x0[c]);
+          x0[c + 1] = fmaf(-f0, v.y, x0[c + 1]);
+          x0[c + 2] = fmaf(-f0, v.z, x0[c + 2]);
+          x0[c + 3] = fmaf(-f0, v.w, x0[c + 3]);
+        }
+        if (use1) {
+          x1[c] = fmaf(-f1, v.x, x1[c]);
+          x1[c + 1] = fmaf(-f1, v.y, x1[c + 1]);
+          x1[c + 2] = fmaf(-f1, v.z, x1[c + 2]);
+          x1[c + 3] = fmaf(-f1, v.w, x1[c + 3]);
+        }
       }
     }
   }
 }
 
-__device__ __forceinline__ float qsum4(float x) {  // the 4 lanes of one row of T blocks
-  const unsigned m = 0xFu << (threadIdx.x & 28);
-  x += __shfl_xor_sync(m, x, 1);
-  x += __shfl_xor_sync(m, x, 2);
+__device__ __forceinline__ float wsum(float x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
 }
 
-__global__ void __launch_bounds__(kT3, 6)
+// the owner lane normalises its vector (or marks it collapsed) and publishes it in row c
+__device__ __forceinline__ void mgs_owner(float (&x)[NB], int c, Zone3& zs) {
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+  for (int i = 0; i < NB; i += 2) {
+    s0 = fmaf(x[i], x[i], s0);
+    s1 = fmaf(x[i + 1], x[i + 1], s1);
+  }
+  const float s = s0 + s1;
+  const bool ok = zs.flag[c] && (s >= 0.5f);
+  const float sc = ok ? rsqrtf(s) : 0.f;
+#pragma unroll
+  for (int i = 0; i < NB; i++) x[i] *= sc;
+  vstore(x, zs.buf + c * LDV);
+  if (!ok) zs.flag[c] = 0;
+}
+
+__global__ void __launch_bounds__(32 * kZpb3, 4)
     k_eig_transform32(int N, int32_t nzc, float* __restrict__ GT, const float* __restrict__ aux,
                       const float* __restrict__ Zg, const float* __restrict__ gv,
                       const int32_t* __restrict__ nobs, int rotate, float* __restrict__ ampl_out,
                       int32_t* __restrict__ status) {
-  extern __shared__ __align__(16) float sm[];
-  float* Vs = sm;               // [NB][LDV] reflectors (vector-major, zero padded)
-  float* Us = Vs + NB * LDV;    // [NB][LDV] Z, eigenvectors, then W = U diag(lambda'^1/4)
-  float* lam = Us + NB * LDV;   // [NB] 1/(1+lambda)            (evaluated in FP64)
-  float* sq = lam + NB;         // [NB] (1+lambda)^-1/2         (evaluated in FP64)
-  float* qs = sq + NB;          // [NB] (1+lambda)^-1/4         (evaluated in FP64)
-  float* gs = qs + NB;          // [NB] g
-  float* bet = gs + NB;         // [NB] Householder scalars
-  float* tt = bet + NB;         // [NB] lambda' (u_j . g)
-  float* cc = tt + NB;          // [NB] colsum(u_j) / sqrt(lambda')
-  float* vv = cc + NB;          // [NB] v (unnormalised)
-  float* t0 = vv + NB;          // [NB] scratch
-  int* flag = reinterpret_cast<int*>(t0 + NB);  // [NB] 1 accepted, 0 collapsed
-  __shared__ float red[2];
-  const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
-  const int32_t zl = blockIdx.x;
-  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int lane = threadIdx.x & 31, wz = threadIdx.x >> 5;
+  Zone3& zs = reinterpret_cast<Zone3*>(sm_raw)[wz];
+  const int32_t zl = blockIdx.x * kZpb3 + wz;
+  if (zl >= nzc || nobs[zl] == 0) return;  // warp-uniform; warp-level synchronisation only
   float* Gz = GT + (int64_t)zl * N * N;
   const float* ax = aux + (int64_t)zl * aux_stride32(N);
   const float* Zz = Zg + (int64_t)zl * N * N;
+  const int j0 = lane, j1 = lane + 32;
+  float* buf = zs.buf;
+  // reflectors into buf (rows k < N-2, zero padded)
   if (N == NB) {
-    // 16 float4 of each matrix per thread, all loads issued before the stores
-    float4 vq[16], zq[16];
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const int idx4 = j + kT3 * i;  // float4 index in the 64 x 64 matrix
-      const int k = idx4 >> 4;
-      vq[i] = (k < N - 2) ? reinterpret_cast<const float4*>(Gz)[idx4] : make_float4(0, 0, 0, 0);
-      zq[i] = reinterpret_cast<const float4*>(Zz)[idx4];
-    }
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const int idx4 = j + kT3 * i;
+#pragma unroll 4
+    for (int i = 0; i < NB * NB / 4 / 32; i++) {
+      const int idx4 = lane + 32 * i;
       const int k = idx4 >> 4, c = (idx4 & 15) * 4;
-      *reinterpret_cast<float4*>(Vs + k * LDV + c) = vq[i];
-      *reinterpret_cast<float4*>(Us + k * LDV + c) = zq[i];
+      *reinterpret_cast<float4*>(buf + k * LDV + c) =
+          (k < N - 2) ? reinterpret_cast<const float4*>(Gz)[idx4] : make_float4(0, 0, 0, 0);
     }
   } else {
-#pragma unroll 8
-    for (int idx = j; idx < NB * NB; idx += kT3) {
+    for (int idx = lane; idx < NB * NB; idx += 32) {
       const int k = idx >> 6, c = idx & (NB - 1);
-      Vs[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
-      Us[k * LDV + c] = (k < N) ? ((c < N) ? Zz[k * N + c] : 0.f) : ((c == k) ? 1.f : 0.f);
+      buf[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
     }
   }
-  {
-    double l = (j < N) ? (double)ax[3 * N + j] : 0.0;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int i = lane + 32 * h;
+    double l = (i < N) ? (double)ax[3 * N + i] : 0.0;
     if (l < 0.0) l = 0.0;
     const double li = 1.0 / (1.0 + l);
     const double s = sqrt(li);
-    lam[j] = (float)li;
-    sq[j] = (float)s;
-    qs[j] = (float)sqrt(s);
-    gs[j] = (j < N) ? gv[(int64_t)zl * N + j] : 0.f;
-    bet[j] = (j < N - 2) ? ax[2 * N + j] : 0.f;
-    flag[j] = 1;
+    zs.lam[i] = (float)li;
+    zs.sq[i] = (float)s;
+    zs.qs[i] = (float)sqrt(s);
+    zs.gs[i] = (i < N) ? gv[(int64_t)zl * N + i] : 0.f;
+    zs.bet[i] = (i < N - 2) ? ax[2 * N + i] : 0.f;
+    zs.flag[i] = 1;
   }
-  __syncthreads();
-  float x[NB];
-  vload(x, Us + j * LDV);
+  float x0[NB], x1[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    x0[i] = (j0 < N) ? ((i < N) ? Zz[(int64_t)j0 * N + i] : 0.f) : ((i == j0) ? 1.f : 0.f);
+    x1[i] = (j1 < N) ? ((i < N) ? Zz[(int64_t)j1 * N + i] : 0.f) : ((i == j1) ? 1.f : 0.f);
+  }
+  __syncwarp();
   // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k)
   for (int k = N - 3; k >= 0; k--) {
-    const float bk = bet[k];
-    if (bk == 0.f) continue;  // uniform
-    const float* vk = Vs + k * LDV;
+    const float bk = zs.bet[k];
+    if (bk == 0.f) continue;  // warp-uniform
+    const float* vk = buf + k * LDV;
     const int g0 = (k + 1) >> 4;
-    const float s = vdot(x, vk, g0);
-    vaxpy(x, bk * s, vk, g0);
+    float d0, d1;
+    vdot2(x0, x1, vk, g0, true, d0, d1);
+    vaxpy2(x0, x1, bk * d0, bk * d1, vk, g0, true, true);
   }
+  __syncwarp();  // the reflectors are read: buf holds the final vectors from here on
   // modified Gram-Schmidt, largest eigenvalue first: vector c is final once every
-  // larger-eigenvalue vector has been projected out of it. A vector that keeps at least half its
-  // squared norm (a norm drop below sqrt(2)) is orthogonal to working precision after this one
-  // projection ("twice is enough", Kahan-Parlett; Parlett, The Symmetric Eigenvalue Problem,
-  // 6-9); one that does not is marked collapsed and replaced below.
-  {
-    for (int c = N - 1; c >= 0; c--) {
-      if (j == c) {
-        float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-        for (int i = 0; i < NB; i += 2) {
-          s0 = fmaf(x[i], x[i], s0);
-          s1 = fmaf(x[i + 1], x[i + 1], s1);
-        }
-        const float s = s0 + s1;
-        const bool ok = flag[c] && (s >= 0.5f);
-        const float sc = ok ? rsqrtf(s) : 0.f;
-#pragma unroll
-        for (int i = 0; i < NB; i++) x[i] *= sc;
-        vstore(x, Us + c * LDV);
-        if (!ok) flag[c] = 0;
-      }
-      __syncthreads();
-      if (j < c && flag[c]) {
-        const float* uc = Us + c * LDV;
-        const float d = vdot(x, uc, 0);
-        vaxpy(x, d, uc, 0);
+  // larger-eigenvalue vector has been projected out of it. A vector that keeps at least half
+  // its squared norm is orthogonal to working precision after this one projection ("twice is
+  // enough", Kahan-Parlett; Parlett, The Symmetric Eigenvalue Problem, 6-9); one that does not
+  // is marked collapsed and replaced below.
+  for (int c = N - 1; c >= 0; c--) {
+    if (lane == (c & 31)) {
+      if (c >= 32)
+        mgs_owner(x1, c, zs);
+      else
+        mgs_owner(x0, c, zs);
+    }
+    __syncwarp();
+    if (zs.flag[c]) {
+      const float* uc = buf + c * LDV;
+      const bool use0 = j0 < c, use1 = j1 < c;
+      if (use0 || use1) {
+        float d0, d1;
+        vdot2(x0, x1, uc, 0, use0, d0, d1);
+        vaxpy2(x0, x1, d0, d1, uc, 0, use0, use1);
       }
     }
   }
+  __syncwarp();
   int ncol = 0;
-  if (j < N) ncol = (flag[j] == 0);
-  ncol = __syncthreads_or(ncol);
-  if (ncol) {
+  if (j0 < N && !zs.flag[j0]) ncol = 1;
+  if (j1 < N && !zs.flag[j1]) ncol = 1;
+  if (__any_sync(0xffffffffu, ncol)) {
     // complement fill (rare): a collapsed vector is replaced by a pseudo-random vector made
     // orthogonal (two classical Gram-Schmidt passes) to every accepted eigenvector
     for (int c = 0; c < N; c++) {
-      if (flag[c]) continue;  // uniform
-      {
-        unsigned h = (unsigned)j * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
-        h ^= h >> 15;
-        h *= 2654435761u;
-        h ^= h >> 13;
-        Us[c * LDV + j] =
-            (j < N) ? (float)((double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5) : 0.f;
+      if (zs.flag[c]) continue;  // warp-uniform
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int i = lane + 32 * h;
+        unsigned hsh = (unsigned)i * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
+        hsh ^= hsh >> 15;
+        hsh *= 2654435761u;
+        hsh ^= hsh >> 13;
+        buf[c * LDV + i] =
+            (i < N) ? (float)((double)(hsh & 0xffffff) * (1.0 / 16777216.0) - 0.5) : 0.f;
       }
-      __syncthreads();
+      __syncwarp();
       for (int pass = 0; pass < 2; pass++) {
-        {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int k = lane + 32 * h;
           float s = 0.f;
-          if (j < N && j != c && flag[j])
-            for (int i = 0; i < N; i++) s = fmaf(Us[j * LDV + i], Us[c * LDV + i], s);
-          t0[j] = s;
+          if (k < N && k != c && zs.flag[k])
+            for (int i = 0; i < N; i++) s = fmaf(buf[k * LDV + i], buf[c * LDV + i], s);
+          zs.t0[k] = s;
         }
-        __syncthreads();
-        {
-          float s = Us[c * LDV + j];
-          for (int k = 0; k < N; k++) s = fmaf(-t0[k], Us[k * LDV + j], s);
-          __syncthreads();
-          Us[c * LDV + j] = s;
+        __syncwarp();
+        float sv[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int i = lane + 32 * h;
+          float s = buf[c * LDV + i];
+          for (int k = 0; k < N; k++) s = fmaf(-zs.t0[k], buf[k * LDV + i], s);
+          sv[h] = s;
         }
-        __syncthreads();
+        __syncwarp();
+        buf[c * LDV + lane] = sv[0];
+        buf[c * LDV + lane + 32] = sv[1];
+        __syncwarp();
       }
-      {
-        const float u = Us[c * LDV + j];
-        float s = u * u;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) red[warp] = s;
-        __syncthreads();
-        const float tot = red[0] + red[1];
-        Us[c * LDV + j] = u * ((tot > 0.f) ? rsqrtf(tot) : 0.f);
-        if (j == 0) flag[c] = 1;
-        __syncthreads();
-      }
+      const float u0 = buf[c * LDV + lane], u1 = buf[c * LDV + lane + 32];
+      const float tot = wsum(u0 * u0 + u1 * u1);
+      const float sc = (tot > 0.f) ? rsqrtf(tot) : 0.f;
+      __syncwarp();
+      buf[c * LDV + lane] = u0 * sc;
+      buf[c * LDV + lane + 32] = u1 * sc;
+      if (lane == 0) zs.flag[c] = 1;
+      __syncwarp();
     }
-    vload(x, Us + j * LDV);
+    if (j0 < N) vload(x0, buf + j0 * LDV);
+    if (j1 < N) vload(x1, buf + j1 * LDV);
   }
   // per-vector scalars: lambda' (u_j . g), colsum(u_j) / sqrt(lambda')
   {
-    const float y = vdot(x, gs, 0);
-    float s0 = 0.f, s1 = 0.f;
+    float y0, y1;
+    vdot2(x0, x1, zs.gs, 0, true, y0, y1);
+    float c0 = 0.f, c1 = 0.f;
 #pragma unroll
-    for (int i = 0; i < NB; i += 2) {
-      s0 += x[i];
-      s1 += x[i + 1];
+    for (int i = 0; i < NB; i++) {
+      c0 += x0[i];
+      c1 += x1[i];
     }
-    tt[j] = (j < N) ? lam[j] * y : 0.f;
-    cc[j] = (j < N) ? (s0 + s1) / sq[j] : 0.f;
+    zs.tt[j0] = (j0 < N) ? zs.lam[j0] * y0 : 0.f;
+    zs.tt[j1] = (j1 < N) ? zs.lam[j1] * y1 : 0.f;
+    zs.cc[j0] = (j0 < N) ? c0 / zs.sq[j0] : 0.f;
+    zs.cc[j1] = (j1 < N) ? c1 / zs.sq[j1] : 0.f;
   }
-  __syncthreads();
-  // ampl = U tt, v = U cc (thread j: component j)
+  __syncwarp();
+  // ampl = U tt, v = U cc (lane: components lane and lane + 32)
   int nan_flag = 0;
-  {
+  float vsq = 0.f;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int r = lane + 32 * h;
     float sa = 0.f, sv = 0.f;
     for (int jj = 0; jj < N; jj++) {
-      const float u = Us[jj * LDV + j];
-      sa = fmaf(u, tt[jj], sa);
-      sv = fmaf(u, cc[jj], sv);
+      const float u = buf[jj * LDV + r];
+      sa = fmaf(u, zs.tt[jj], sa);
+      sv = fmaf(u, zs.cc[jj], sv);
     }
-    if (j < N) {
-      ampl_out[(int64_t)zl * N + j] = sa;
+    if (r < N) {
+      ampl_out[(int64_t)zl * N + r] = sa;
       if (!(sa == sa) || isinf(sa)) nan_flag = 1;
+      vsq = fmaf(sv, sv, vsq);
     }
-    vv[j] = (j < N) ? sv : 0.f;
+    zs.vv[r] = (r < N) ? sv : 0.f;
   }
-  nan_flag = __syncthreads_or(nan_flag);
+  nan_flag = __any_sync(0xffffffffu, nan_flag);
+  const float vinv = rotate ? 1.f / sqrtf(wsum(vsq)) : 0.f;
+  __syncwarp();  // buf read by every lane before W overwrites it
   {
-    const float qj = qs[j];
+    const float q0 = zs.qs[j0], q1 = zs.qs[j1];
 #pragma unroll
-    for (int i = 0; i < NB; i++) x[i] *= qj;
-    vstore(x, Us + j * LDV);  // W = U diag(qs); padding vectors stay unit vectors
-    if (rotate) {
-      float s = (j < N) ? vv[j] * vv[j] : 0.f;
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) red[warp] = s;
+    for (int i = 0; i < NB; i++) {
+      x0[i] *= q0;
+      x1[i] *= q1;
+    }
+    vstore(x0, buf + j0 * LDV);  // W = U diag(qs); padding vectors stay unit vectors
+    vstore(x1, buf + j1 * LDV);
+  }
+  float sv_ = 1.f;
+  if (rotate) {
+    const float vN = zs.vv[N - 1] * vinv;
+    sv_ = signbit(vN) ? -1.f : 1.f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int col = lane + 32 * h;
+      const float vn = (col < N) ? zs.vv[col] * vinv : 0.f;
+      zs.vn[col] = vn;
+      zs.uv[col] = vn + ((col == N - 1) ? sv_ : 0.f);
     }
   }
-  __syncthreads();
-  // T_sym = W W^T: thread (rb, cb) = (j / 4, j % 4) computes rows 4 rb .. 4 rb + 3 and the
-  // columns of 16-byte chunks cb, cb + 4, cb + 8, cb + 12 (interleaved: conflict-free loads)
-  const int rb = j >> 2, cb = j & 3;
-  float T[4][16];
+  __syncwarp();
+  // T_sym = W W^T: lane computes rows lane and lane + 32 (64 columns each, in registers)
+  float T0[NB], T1[NB];
 #pragma unroll
-  for (int i = 0; i < 4; i++)
-#pragma unroll
-    for (int c = 0; c < 16; c++) T[i][c] = 0.f;
-#pragma unroll 2
+  for (int b = 0; b < NB; b++) {
+    T0[b] = 0.f;
+    T1[b] = 0.f;
+  }
   for (int jj = 0; jj < N; jj++) {
-    const float* w = Us + jj * LDV;
-    const float4 wa = *reinterpret_cast<const float4*>(w + 4 * rb);
-    const float ra[4] = {wa.x, wa.y, wa.z, wa.w};
+    const float* w = buf + jj * LDV;
+    const float wa0 = w[j0], wa1 = w[j1];
 #pragma unroll
-    for (int m = 0; m < 4; m++) {
-      const float4 wb = *reinterpret_cast<const float4*>(w + 4 * (cb + 4 * m));
-      const float rbv[4] = {wb.x, wb.y, wb.z, wb.w};
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int t = 0; t < 4; t++) T[i][4 * m + t] = fmaf(ra[i], rbv[t], T[i][4 * m + t]);
+    for (int b = 0; b < NB; b += 4) {
+      const float4 wb = *reinterpret_cast<const float4*>(w + b);
+      T0[b] = fmaf(wa0, wb.x, T0[b]);
+      T0[b + 1] = fmaf(wa0, wb.y, T0[b + 1]);
+      T0[b + 2] = fmaf(wa0, wb.z, T0[b + 2]);
+      T0[b + 3] = fmaf(wa0, wb.w, T0[b + 3]);
+      T1[b] = fmaf(wa1, wb.x, T1[b]);
+      T1[b + 1] = fmaf(wa1, wb.y, T1[b + 1]);
+      T1[b + 2] = fmaf(wa1, wb.z, T1[b + 2]);
+      T1[b + 3] = fmaf(wa1, wb.w, T1[b + 3]);
     }
   }
   if (rotate) {
     // Omega = P_v P_w + (1 - s_v s_w) v w^T with P_x = I - u_x u_x^T / (1 + |x_N|),
-    // u_x = x + sign(x_N) e_N, w = 1/sqrt(N) (s_w = +1)  (matoper.F90:509-535)
-    const float inv = 1.f / sqrtf(red[0] + red[1]);
-    const float vN = vv[N - 1] * inv;
-    const float sv = signbit(vN) ? -1.f : 1.f;
-    const float icv = 1.f / (1.f + fabsf(vN));
+    // u_x = x + sign(x_N) e_N, w = 1/sqrt(N) (s_w = +1)  (matoper.F90:509-535); the lane owns
+    // whole rows, so the row dots need no reduction
+    const float icv = 1.f / (1.f + fabsf(zs.vn[N - 1]));
     const float wv = (float)(1.0 / sqrt((double)N));
     const float icw = 1.f / (1.f + wv);
-    float pa[4], pb[4];
+    const float extra = 1.f - sv_;
+    float pa0 = 0.f, pb0 = 0.f, pa1 = 0.f, pb1 = 0.f;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-      float sa = 0.f, sb = 0.f;
+    for (int b = 0; b < NB; b += 4) {
+      const float4 u4 = *reinterpret_cast<const float4*>(zs.uv + b);
+      const float4 n4 = *reinterpret_cast<const float4*>(zs.vn + b);
+      const float uvb[4] = {u4.x, u4.y, u4.z, u4.w}, vnb[4] = {n4.x, n4.y, n4.z, n4.w};
 #pragma unroll
-      for (int m = 0; m < 4; m++)
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int col = 4 * (cb + 4 * m) + t;
-          const float vn = (col < N) ? vv[col] * inv : 0.f;
-          const float uv = vn + ((col == N - 1) ? sv : 0.f);
-          sa = fmaf(T[i][4 * m + t], uv, sa);
-          sb = fmaf(T[i][4 * m + t], vn, sb);
-        }
-      pa[i] = qsum4(sa) * icv;  // (T_sym u_v)_row / c_v
-      pb[i] = qsum4(sb);        // (T_sym v)_row
-    }
-    const float extra = 1.f - sv;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      float sg = 0.f;
-#pragma unroll
-      for (int m = 0; m < 4; m++)
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int col = 4 * (cb + 4 * m) + t;
-          const float vn = (col < N) ? vv[col] * inv : 0.f;
-          const float uv = vn + ((col == N - 1) ? sv : 0.f);
-          const float uw = (col < N) ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
-          const float t1 = fmaf(-pa[i], uv, T[i][4 * m + t]);  // T1 = T_sym - t0 u_v^T / c_v
-          T[i][4 * m + t] = t1;
-          sg = fmaf(t1, uw, sg);
-        }
-      const float g = qsum4(sg) * icw;  // (T1 u_w)_row / c_w
-#pragma unroll
-      for (int m = 0; m < 4; m++)
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int col = 4 * (cb + 4 * m) + t;
-          const float uw = (col < N) ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
-          float tv = fmaf(-g, uw, T[i][4 * m + t]);
-          if (extra != 0.f && col < N) tv = fmaf(extra * pb[i], wv, tv);
-          T[i][4 * m + t] = tv;
-        }
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int row = 4 * rb + i;
-    if (row >= N) continue;
-#pragma unroll
-    for (int m = 0; m < 4; m++) {
-      const int col = 4 * (cb + 4 * m);
-      if (N == NB) {
-        *reinterpret_cast<float4*>(Gz + row * N + col) =
-            make_float4(T[i][4 * m], T[i][4 * m + 1], T[i][4 * m + 2], T[i][4 * m + 3]);
-      } else {
-#pragma unroll
-        for (int t = 0; t < 4; t++)
-          if (col + t < N) Gz[row * N + col + t] = T[i][4 * m + t];
+      for (int t = 0; t < 4; t++) {
+        pa0 = fmaf(T0[b + t], uvb[t], pa0);
+        pb0 = fmaf(T0[b + t], vnb[t], pb0);
+        pa1 = fmaf(T1[b + t], uvb[t], pa1);
+        pb1 = fmaf(T1[b + t], vnb[t], pb1);
       }
     }
+    pa0 *= icv;
+    pa1 *= icv;
+    float pg0 = 0.f, pg1 = 0.f;
+#pragma unroll
+    for (int b = 0; b < NB; b += 4) {
+      const float4 u4 = *reinterpret_cast<const float4*>(zs.uv + b);
+      const float uvb[4] = {u4.x, u4.y, u4.z, u4.w};
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int col = b + t;
+        const float uw = (col < N) ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
+        T0[col] = fmaf(-pa0, uvb[t], T0[col]);  // T1 = T_sym - t0 u_v^T / c_v
+        T1[col] = fmaf(-pa1, uvb[t], T1[col]);
+        pg0 = fmaf(T0[col], uw, pg0);
+        pg1 = fmaf(T1[col], uw, pg1);
+      }
+    }
+    pg0 *= icw;
+    pg1 *= icw;
+#pragma unroll
+    for (int col = 0; col < NB; col++) {
+      const float uw = (col < N) ? wv + ((col == N - 1) ? 1.f : 0.f) : 0.f;
+      float t0v = fmaf(-pg0, uw, T0[col]), t1v = fmaf(-pg1, uw, T1[col]);
+      if (extra != 0.f && col < N) {
+        t0v = fmaf(extra * pb0, wv, t0v);
+        t1v = fmaf(extra * pb1, wv, t1v);
+      }
+      T0[col] = t0v;
+      T1[col] = t1v;
+    }
   }
-  if (j == 0 && nan_flag) status[zl] |= ZST_NAN;
+  __syncwarp();  // W read by every lane before T is staged in buf
+  vstore(T0, buf + j0 * LDV);
+  vstore(T1, buf + j1 * LDV);
+  __syncwarp();
+  if (N == NB) {
+#pragma unroll 4
+    for (int i = 0; i < NB * NB / 4 / 32; i++) {
+      const int idx4 = lane + 32 * i;
+      const int row = idx4 >> 4, c = (idx4 & 15) * 4;
+      reinterpret_cast<float4*>(Gz)[idx4] = *reinterpret_cast<const float4*>(buf + row * LDV + c);
+    }
+  } else {
+    for (int idx = lane; idx < N * N; idx += 32) {
+      const int row = idx / N, c = idx - row * N;
+      Gz[idx] = buf[row * LDV + c];
+    }
+  }
+  if (lane == 0 && nan_flag) status[zl] |= ZST_NAN;
 }
 
 // ------------------------------------------------------------------------------------ E2a
@@ -823,7 +873,8 @@ cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform32,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem3);
   if (e != cudaSuccess) return e;
-  k_eig_transform32<<<nzc > 0 ? nzc : 1, kT3, kSmem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
+  const int blocks = (nzc + kZpb3 - 1) / kZpb3;
+  k_eig_transform32<<<blocks > 0 ? blocks : 1, 32 * kZpb3, kSmem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
                                                             d_nobs, rotate, d_ampl, d_status);
   return cudaGetLastError();
 }

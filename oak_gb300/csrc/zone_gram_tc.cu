@@ -17,6 +17,15 @@
 //   and B accumulates D = S S^T, whose four 64 x 64 blocks are X_hi^T X_hi, X_hi^T X_lo,
 //   X_lo^T X_hi and X_lo^T X_lo; G is their sum (symmetrised from the lower triangle).
 //
+// The tensor-core accumulator is FP32 and its error grows with the length of the chain: zones on
+// dense observation tracks select thousands of observations, and one chain over all of them
+// leaves G with an error several times 1e-5 relative to its largest entries, which the
+// eigendecomposition carries into the small eigenvalues. The chain is therefore cut into chunks
+// of kChunkTiles K-tiles (256 observations): after each chunk the accumulator is read and added
+// into a lower-triangle FP32 accumulator in shared memory, and the next chunk's first MMA
+// overwrites the tensor-memory accumulator. The error of G is then that of a 256-term sum plus
+// a few FP32 additions, whatever the number of observations.
+//
 // The innovation projection g = X^T (sqrt(c) d) (rrsqrt.F90:142) is accumulated on the CUDA
 // cores by the staging threads with compensated (Kahan) FP32 sums.
 //
@@ -24,7 +33,7 @@
 // observations go to a ring of (index, sqrt(c), sqrt(c) d); every full K-tile is staged into
 // one of two shared buffers and handed to the tensor core by one thread (4 MMAs of K = 8 and a
 // commit to the buffer's mbarrier), so staging of the next tile overlaps the MMAs. At the end
-// of the zone the accumulator is read with tcgen05.ld. Every mbarrier wait is bounded; on
+// of every chunk and of the zone the accumulator is read with tcgen05.ld. Every mbarrier wait is bounded; on
 // expiry the kernel records ZST_TIMEOUT, stops taking zones, waits (bounded) for its MMAs and
 // frees its tensor memory.
 #include <cuda_runtime.h>
@@ -44,12 +53,14 @@ constexpr int kRing = 512;        // selected-observation ring (power of two)
 constexpr uint32_t kTileBytes = 128u * 128u;
 constexpr uint32_t kTmemCols = 128;
 constexpr int kWaitPolls = 1 << 22;
-constexpr int GLD = NB + 1;       // row stride of the shared G staging (floats)
-// dynamic shared memory: 1 KB alignment slack, two tiles (also reused for G at the end of a
-// zone), compensated innovation partials; padded so that at most 4 CTAs share an SM (4 x 128
+constexpr int kChunkTiles = 8;    // K-tiles accumulated in tensor memory between reads
+constexpr int kTri = NB * (NB + 1) / 2;  // lower triangle of G
+constexpr size_t kTail = 12 * 1024;
+// dynamic shared memory: 1 KB alignment slack, two tiles, compensated innovation partials and
+// the lower-triangle G accumulator, padded (kTail) so that at most 4 CTAs share an SM (4 x 128
 // tensor-memory columns = all 512)
-constexpr size_t kDynSmem = 1024 + 2 * kTileBytes + 2 * 4 * NB * sizeof(float) + 12 * 1024;
-static_assert(NB * GLD * sizeof(float) <= 2 * kTileBytes, "G staging must fit in the tiles");
+constexpr size_t kDynSmem = 1024 + 2 * kTileBytes + 2 * 4 * NB * sizeof(float) + kTail;
+static_assert(kTri * sizeof(float) <= kTail, "G accumulator must fit in the tail");
 
 struct TcShared {
   int32_t ring_q[kRing];
@@ -122,19 +133,17 @@ __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// 16 consecutive accumulator columns of this warp's 32 tensor-memory lanes
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 8 consecutive accumulator columns of this warp's 32 tensor-memory lanes
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-      "%12, %13, %14, %15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
+        "=r"(r[7])
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 
 // byte offset of the 16-byte chunk `chunk` (4 observations) of operand row `row` in a tile
@@ -174,7 +183,7 @@ __global__ void __launch_bounds__(kThreads, 4)
   const uint32_t tile_addr = raw_addr + pad;
   float* gps = reinterpret_cast<float*>(tiles + 2 * kTileBytes);  // [4][NB] partial sums
   float* gpc = gps + 4 * NB;                                       // [4][NB] compensations
-  float* Gs = reinterpret_cast<float*>(tiles);                     // [NB][GLD] (end of zone)
+  float* gacc = gpc + 4 * NB;  // G lower triangle, entry (i, j <= i) at i (i + 1) / 2 + j
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int a = tid & (NB - 1), kq = tid >> 6;  // staging: member a, observation quads kq, kq+4
@@ -219,6 +228,35 @@ __global__ void __launch_bounds__(kThreads, 4)
     }
   };
 
+  // add the tensor-memory accumulator into gacc (all MMAs complete and published by a barrier).
+  // Warp w reads lanes 32 (w % 4) .. + 31 (rows of D) and column half w / 4 of both column
+  // blocks; G(i, j) = (D(i, j) + D(i, j + 64)) + (D(i + 64, j) + D(i + 64, j + 64)). The rows of
+  // the lo parts are added first, then those of the hi parts, so the sums are deterministic.
+  auto flush = [&]() {
+    fence_after();
+    const int q = warp & 3, h = warp >> 2;
+    const int i = (32 * q + lane) & (NB - 1);
+    const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16);
+    float* gi = gacc + i * (i + 1) / 2;
+#pragma unroll
+    for (int phase = 0; phase < 2; phase++) {
+      if ((q >> 1) == 1 - phase) {
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+          const int c0 = 32 * h + 8 * s;
+          float v0[8], v1[8];
+          tmem_ld8(ta + c0, v0);
+          tmem_ld8(ta + 64 + c0, v1);
+#pragma unroll
+          for (int t = 0; t < 8; t++)
+            if (c0 + t <= i) gi[c0 + t] += v0[t] + v1[t];
+        }
+      }
+      fence_before();
+      __syncthreads();
+    }
+  };
+
   for (;;) {
     if (tid == 0) ts.zone = atomicAdd(work, 1);
     __syncthreads();
@@ -233,11 +271,23 @@ __global__ void __launch_bounds__(kThreads, 4)
     const float iL32 = (float)(1.0 / L);
     const float r_lo = (float)Rmax * (1.f - 1e-6f), r_hi = (float)Rmax * (1.f + 1e-6f);
     if (tid == 0) ts.nrel = 0;
-    int head = 0, tail = 0, ntile = 0, nrel_local = 0;
+    for (int e = tid; e < kTri; e += kThreads) gacc[e] = 0.f;
+    int head = 0, tail = 0, ntile = 0, ctile = 0, nrel_local = 0;
     float gsum = 0.f, gcmp = 0.f;
 
     // stage ring entries [head, head + rows) as one K-tile and issue its MMAs
     auto do_tile = [&](int rows) {
+      if (ctile == kChunkTiles) {
+        if (pend0) drain(0);
+        if (pend1) drain(1);
+        __syncthreads();  // MMA completion and flag published
+        if (ts.flag) {
+          abort = true;
+          return;
+        }
+        flush();
+        ctile = 0;
+      }
       const int b = ntile & 1;
       if (b ? pend1 : pend0) drain(b);
       __syncthreads();  // buffer free (flag published), ring entries visible
@@ -276,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         const uint32_t base = tile_addr + b * kTileBytes;
 #pragma unroll
         for (int kk = 0; kk < KT / 8; kk++)
-          mma_tf32(tmem, make_desc(base + kk * 32), (ntile > 0 || kk > 0) ? 1u : 0u);
+          mma_tf32(tmem, make_desc(base + kk * 32), (ctile > 0 || kk > 0) ? 1u : 0u);
         mma_commit(mbar0 + 8 * b);
       }
       if (b)
@@ -284,6 +334,7 @@ __global__ void __launch_bounds__(kThreads, 4)
       else
         pend0 = 1;
       ntile++;
+      ctile++;
       head += rows;
     };
 
@@ -418,43 +469,11 @@ __global__ void __launch_bounds__(kThreads, 4)
     const int nrel = ts.nrel;
     if (tid == 0) nobs[z] = nrel;
     if (nrel > 0 && ntile > 0) {
-      fence_after();
-      // G = sum of the four 64 x 64 blocks of D; warps 2-3 hold rows 64-127 (lo parts),
-      // warps 0-1 rows 0-63 (hi parts); each adds its two column halves
-      if (warp == 2 || warp == 3) {
-        const int r = lane + 32 * (warp - 2);
-        const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16);
-#pragma unroll
-        for (int h = 0; h < 4; h++) {
-          float v0[16], v1[16];
-          tmem_ld16(ta + 16 * h, v0);
-          tmem_ld16(ta + 64 + 16 * h, v1);
-#pragma unroll
-          for (int i = 0; i < 16; i++) Gs[r * GLD + 16 * h + i] = v0[i] + v1[i];
-        }
-      }
-      __syncthreads();
-      if (warp == 0 || warp == 1) {
-        const int r = lane + 32 * warp;
-        const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16);
-#pragma unroll
-        for (int h = 0; h < 4; h++) {
-          float v0[16], v1[16];
-          tmem_ld16(ta + 16 * h, v0);
-          tmem_ld16(ta + 64 + 16 * h, v1);
-#pragma unroll
-          for (int i = 0; i < 16; i++) {
-            float* p = Gs + r * GLD + 16 * h + i;
-            *p = (v0[i] + v1[i]) + *p;
-          }
-        }
-      }
-      fence_before();
-      __syncthreads();
+      flush();
       float* Gz = G + (int64_t)zl * N * N;
       for (int idx = tid; idx < N * N; idx += kThreads) {
         const int i = idx / N, j = idx - i * N;
-        Gz[idx] = (j <= i) ? Gs[i * GLD + j] : Gs[j * GLD + i];
+        Gz[idx] = (j <= i) ? gacc[i * (i + 1) / 2 + j] : gacc[j * (j + 1) / 2 + i];
       }
       if (tid < N) {
         // compensated combination of the four partial sums of member tid
