@@ -20,12 +20,14 @@
 // E2a: one thread per zone, implicit QR sweeps (working arrays in shared memory).
 // E2b: thread j = eigenpair j, inverse iteration (LU factor in shared memory).
 // E3: one warp per zone, lane t holding eigenvectors t and t + 32.
+//   orthogonalisation of the eigenvectors Z of Tri: right-looking modified Gram-Schmidt,
+//     largest eigenvalue first (a vector is final when every larger-eigenvalue vector has been
+//     projected out of it); a vector that keeps at least half its squared norm is accepted
+//     after this one projection (Kahan-Parlett "twice is enough"), one that does not is marked
+//     collapsed and replaced by a pseudo-random vector orthogonalised (two passes) against
+//     every accepted one and refined by inverse iteration with its own shift inside that
+//     orthogonal complement;
 //   back-transform U = H_0 ... H_{N-3} Z: per reflector a register dot and axpy, no barrier;
-//   orthogonalisation: right-looking modified Gram-Schmidt, largest eigenvalue first (a vector
-//     is final when every larger-eigenvalue vector has been projected out of it); a vector that
-//     keeps at least half its squared norm is accepted after this one projection (Kahan-Parlett
-//     "twice is enough"), one that does not is marked collapsed and replaced by a
-//     pseudo-random vector orthogonalised (two passes) against every accepted one;
 //   T_sym = (U Q)(U Q)^T with Q = diag((1+lambda)^-1/4): each lane computes two full rows
 //     (128-bit broadcast loads of W's rows); Omega = RotateVector(w, v) applied to those rows
 //     in its reflector form (rank-one updates, matoper.F90:509-535).
@@ -297,6 +299,45 @@ __device__ __forceinline__ float wsum(float x) {
   return x;
 }
 
+constexpr int kFillIters = 2;     // inverse-iteration steps of a pseudo-random complement fill
+constexpr float kResidMin = 1e-6f;  // smallest squared residual norm used as a fill
+
+// x <- (Tri - s I)^-1 x in place, Tri = (d, e); partial-pivoting LU with tiny pivots replaced,
+// as in the inverse iteration of E2b (u1, u2, ui: scratch of N)
+__device__ void tri_solve32(float* x, const float* d, const float* e, int N, float s, float tiny,
+                            float* u1, float* u2, float* ui) {
+  float cd = d[0] - s, csup = (N > 1) ? e[0] : 0.f;
+  for (int i = 0; i < N - 1; i++) {
+    const float sub = e[i], dg = d[i + 1] - s, sp = (i + 1 < N - 1) ? e[i + 1] : 0.f;
+    const bool swap = fabsf(cd) < fabsf(sub);
+    float pivot = swap ? sub : cd;
+    if (!swap && fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
+    const float inv = __fdividef(1.f, pivot);  // |pivot| >= tiny > 0; ~2 ulp suffices here
+    const float li = (swap ? cd : sub) * inv;
+    u1[i] = swap ? dg : csup;
+    u2[i] = swap ? sp : 0.f;
+    ui[i] = inv;
+    const float aa = swap ? csup : dg, bb = swap ? dg : csup;
+    cd = fmaf(-li, bb, aa);
+    csup = swap ? -li * sp : sp;
+    const float xi = swap ? x[i + 1] : x[i], xn = swap ? x[i] : x[i + 1];
+    x[i] = xi;
+    x[i + 1] = fmaf(-li, xi, xn);
+  }
+  float pivot = cd;
+  if (fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
+  ui[N - 1] = __fdividef(1.f, pivot);
+  u1[N - 1] = 0.f;
+  u2[N - 1] = 0.f;
+  if (N >= 2) u2[N - 2] = 0.f;
+  for (int i = N - 1; i >= 0; i--) {
+    float v = x[i];
+    if (i + 1 < N) v = fmaf(-u1[i], x[i + 1], v);
+    if (i + 2 < N) v = fmaf(-u2[i], x[i + 2], v);
+    x[i] = v * ui[i];
+  }
+}
+
 // the owner lane normalises its vector (or marks it collapsed) and publishes it in row c
 __device__ __forceinline__ void mgs_owner(float (&x)[NB], int c, Zone3& zs) {
   float s0 = 0.f, s1 = 0.f;
@@ -307,7 +348,7 @@ __device__ __forceinline__ void mgs_owner(float (&x)[NB], int c, Zone3& zs) {
   }
   const float s = s0 + s1;
   const bool ok = zs.flag[c] && (s >= 0.5f);
-  const float sc = ok ? rsqrtf(s) : 0.f;
+  const float sc = ok ? rsqrtf(s) : 1.f;  // a collapsed vector keeps its residual
 #pragma unroll
   for (int i = 0; i < NB; i++) x[i] *= sc;
   vstore(x, zs.buf + c * LDV);
@@ -329,21 +370,6 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
   const float* Zz = Zg + (int64_t)zl * N * N;
   const int j0 = lane, j1 = lane + 32;
   float* buf = zs.buf;
-  // reflectors into buf (rows k < N-2, zero padded)
-  if (N == NB) {
-#pragma unroll 4
-    for (int i = 0; i < NB * NB / 4 / 32; i++) {
-      const int idx4 = lane + 32 * i;
-      const int k = idx4 >> 4, c = (idx4 & 15) * 4;
-      *reinterpret_cast<float4*>(buf + k * LDV + c) =
-          (k < N - 2) ? reinterpret_cast<const float4*>(Gz)[idx4] : make_float4(0, 0, 0, 0);
-    }
-  } else {
-    for (int idx = lane; idx < NB * NB; idx += 32) {
-      const int k = idx >> 6, c = idx & (NB - 1);
-      buf[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
-    }
-  }
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     const int i = lane + 32 * h;
@@ -365,22 +391,12 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
     x1[i] = (j1 < N) ? ((i < N) ? Zz[(int64_t)j1 * N + i] : 0.f) : ((i == j1) ? 1.f : 0.f);
   }
   __syncwarp();
-  // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k)
-  for (int k = N - 3; k >= 0; k--) {
-    const float bk = zs.bet[k];
-    if (bk == 0.f) continue;  // warp-uniform
-    const float* vk = buf + k * LDV;
-    const int g0 = (k + 1) >> 4;
-    float d0, d1;
-    vdot2(x0, x1, vk, g0, true, d0, d1);
-    vaxpy2(x0, x1, bk * d0, bk * d1, vk, g0, true, true);
-  }
-  __syncwarp();  // the reflectors are read: buf holds the final vectors from here on
-  // modified Gram-Schmidt, largest eigenvalue first: vector c is final once every
-  // larger-eigenvalue vector has been projected out of it. A vector that keeps at least half
-  // its squared norm is orthogonal to working precision after this one projection ("twice is
-  // enough", Kahan-Parlett; Parlett, The Symmetric Eigenvalue Problem, 6-9); one that does not
-  // is marked collapsed and replaced below.
+  // modified Gram-Schmidt on the eigenvectors of Tri (the back-transform below is orthogonal),
+  // largest eigenvalue first: vector c is final once every larger-eigenvalue vector has been
+  // projected out of it. A vector that keeps at least half its squared norm is orthogonal to
+  // working precision after this one projection ("twice is enough", Kahan-Parlett; Parlett,
+  // The Symmetric Eigenvalue Problem, 6-9); one that does not is marked collapsed and replaced
+  // below.
   for (int c = N - 1; c >= 0; c--) {
     if (lane == (c & 31)) {
       if (c >= 32)
@@ -404,56 +420,145 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
   if (j0 < N && !zs.flag[j0]) ncol = 1;
   if (j1 < N && !zs.flag[j1]) ncol = 1;
   if (__any_sync(0xffffffffu, ncol)) {
-    // complement fill (rare): a collapsed vector is replaced by a pseudo-random vector made
-    // orthogonal (two classical Gram-Schmidt passes) to every accepted eigenvector
+    // complement fill. Inverse iteration gives nearly parallel vectors for eigenvalues that
+    // FP32 does not separate (gaps below eps ||G||), so one of them collapses above, and the
+    // span of the accepted vectors misses directions whose eigenvalues can lie anywhere in the
+    // collapsed group: a replacement must point at the right one. The collapsed vector's
+    // residual (what the larger-eigenvalue vectors left of it) is its inverse iterate with
+    // those directions removed, i.e. already filtered toward its shift inside the missing
+    // subspace; made orthogonal (two classical Gram-Schmidt passes) to every accepted vector,
+    // it is the replacement. A residual too small to carry that information (squared norm
+    // below kResidMin, FP32 noise then dominates) is replaced by a pseudo-random vector that
+    // kFillIters steps of inverse iteration with the collapsed vector's shift refine inside the
+    // orthogonal complement (x <- P (Tri - shift_c)^-1 x, P the projector of the two passes).
+    // Filled vectors count as accepted for the later ones.
+    const float onenrm = ax[5 * N + 1];
+    // the last replacement spans the remaining one-dimensional complement: no choice to refine
+    int left = 0;
+    for (int c = 0; c < N; c++) left += zs.flag[c] ? 0 : 1;
+    float* td = zs.uv;  // Tri (d, e) for the solves; uv and vn are free until the rotation
+    float* te = zs.vn;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int i = lane + 32 * h;
+      td[i] = (i < N) ? ax[i] : 0.f;
+      te[i] = (i < N - 1) ? ax[N + i] : 0.f;
+    }
+    __syncwarp();
     for (int c = 0; c < N; c++) {
       if (zs.flag[c]) continue;  // warp-uniform
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int i = lane + 32 * h;
-        unsigned hsh = (unsigned)i * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
-        hsh ^= hsh >> 15;
-        hsh *= 2654435761u;
-        hsh ^= hsh >> 13;
-        buf[c * LDV + i] =
-            (i < N) ? (float)((double)(hsh & 0xffffff) * (1.0 / 16777216.0) - 0.5) : 0.f;
-      }
-      __syncwarp();
-      for (int pass = 0; pass < 2; pass++) {
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const int k = lane + 32 * h;
-          float s = 0.f;
-          if (k < N && k != c && zs.flag[k])
-            for (int i = 0; i < N; i++) s = fmaf(buf[k * LDV + i], buf[c * LDV + i], s);
-          zs.t0[k] = s;
-        }
-        __syncwarp();
-        float sv[2];
+      const float r0 = buf[c * LDV + lane], r1 = buf[c * LDV + lane + 32];
+      const bool resid = wsum(fmaf(r0, r0, r1 * r1)) >= kResidMin;
+      --left;
+      const bool refine = !resid && left > 0 && onenrm > 1e4f * 1e-36f;
+      if (!resid) {
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int i = lane + 32 * h;
-          float s = buf[c * LDV + i];
-          for (int k = 0; k < N; k++) s = fmaf(-zs.t0[k], buf[k * LDV + i], s);
-          sv[h] = s;
+          unsigned hsh = (unsigned)i * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
+          hsh ^= hsh >> 15;
+          hsh *= 2654435761u;
+          hsh ^= hsh >> 13;
+          buf[c * LDV + i] =
+              (i < N) ? (float)((double)(hsh & 0xffffff) * (1.0 / 16777216.0) - 0.5) : 0.f;
+        }
+      }
+      __syncwarp();
+      for (int it = 0;; it++) {
+        for (int pass = 0; pass < 2; pass++) {
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const int k = lane + 32 * h;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // padding components are zero
+            if (k < N && k != c && zs.flag[k]) {
+              const float* uk = buf + k * LDV;
+              const float* uc = buf + c * LDV;
+#pragma unroll 4
+              for (int i = 0; i < NB; i += 4) {
+                const float4 a = *reinterpret_cast<const float4*>(uk + i);
+                const float4 b = *reinterpret_cast<const float4*>(uc + i);
+                s0 = fmaf(a.x, b.x, s0);
+                s1 = fmaf(a.y, b.y, s1);
+                s2 = fmaf(a.z, b.z, s2);
+                s3 = fmaf(a.w, b.w, s3);
+              }
+            }
+            zs.t0[k] = (s0 + s1) + (s2 + s3);
+          }
+          __syncwarp();
+          float sv[2];
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const int i = lane + 32 * h;
+            float s0 = buf[c * LDV + i], s1 = 0.f;
+            for (int k = 0; k < N; k += 2) {
+              s0 = fmaf(-zs.t0[k], buf[k * LDV + i], s0);
+              if (k + 1 < N) s1 = fmaf(-zs.t0[k + 1], buf[(k + 1) * LDV + i], s1);
+            }
+            sv[h] = s0 + s1;
+          }
+          __syncwarp();
+          buf[c * LDV + lane] = sv[0];
+          buf[c * LDV + lane + 32] = sv[1];
+          __syncwarp();
+        }
+        float u0 = buf[c * LDV + lane], u1 = buf[c * LDV + lane + 32];
+        const float tot = wsum(u0 * u0 + u1 * u1);
+        const float sc = (tot > 0.f) ? rsqrtf(tot) : 0.f;
+        u0 *= sc;
+        u1 *= sc;
+        if (it == kFillIters || !refine) {
+          __syncwarp();
+          buf[c * LDV + lane] = u0;
+          buf[c * LDV + lane + 32] = u1;
+          break;
         }
         __syncwarp();
-        buf[c * LDV + lane] = sv[0];
-        buf[c * LDV + lane + 32] = sv[1];
+        buf[c * LDV + lane] = u0;
+        buf[c * LDV + lane + 32] = u1;
+        __syncwarp();
+        if (lane == 0)
+          tri_solve32(buf + c * LDV, td, te, N, ax[4 * N + c], 5.9604645e-8f * onenrm, zs.tt,
+                      zs.cc, zs.vv);
         __syncwarp();
       }
-      const float u0 = buf[c * LDV + lane], u1 = buf[c * LDV + lane + 32];
-      const float tot = wsum(u0 * u0 + u1 * u1);
-      const float sc = (tot > 0.f) ? rsqrtf(tot) : 0.f;
-      __syncwarp();
-      buf[c * LDV + lane] = u0 * sc;
-      buf[c * LDV + lane + 32] = u1 * sc;
       if (lane == 0) zs.flag[c] = 1;
       __syncwarp();
     }
     if (j0 < N) vload(x0, buf + j0 * LDV);
     if (j1 < N) vload(x1, buf + j1 * LDV);
   }
+  __syncwarp();  // every lane holds its final vectors: buf takes the reflectors
+  // reflectors into buf (rows k < N-2, zero padded)
+  if (N == NB) {
+#pragma unroll 4
+    for (int i = 0; i < NB * NB / 4 / 32; i++) {
+      const int idx4 = lane + 32 * i;
+      const int k = idx4 >> 4, c = (idx4 & 15) * 4;
+      *reinterpret_cast<float4*>(buf + k * LDV + c) =
+          (k < N - 2) ? reinterpret_cast<const float4*>(Gz)[idx4] : make_float4(0, 0, 0, 0);
+    }
+  } else {
+    for (int idx = lane; idx < NB * NB; idx += 32) {
+      const int k = idx >> 6, c = idx & (NB - 1);
+      buf[k * LDV + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
+    }
+  }
+  __syncwarp();
+  // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k)
+  for (int k = N - 3; k >= 0; k--) {
+    const float bk = zs.bet[k];
+    if (bk == 0.f) continue;  // warp-uniform
+    const float* vk = buf + k * LDV;
+    const int g0 = (k + 1) >> 4;
+    float d0, d1;
+    vdot2(x0, x1, vk, g0, true, d0, d1);
+    vaxpy2(x0, x1, bk * d0, bk * d1, vk, g0, true, true);
+  }
+  __syncwarp();  // the reflectors are read: buf holds U from here on
+  vstore(x0, buf + j0 * LDV);
+  vstore(x1, buf + j1 * LDV);
+  __syncwarp();
   // per-vector scalars: lambda' (u_j . g), colsum(u_j) / sqrt(lambda')
   {
     float y0, y1;
