@@ -1,11 +1,14 @@
-"""Command-line runner for the synthetic local-analysis workload.
+"""Command-line runner for the synthetic local-analysis workloads.
 
   python -m oak_gb300 local [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--m M]
+  python -m oak_gb300 batched [--scale S] [--precision fp64|mixed] [--calls K] [--N N]
 
-Builds the seeded local case (360 x 180 x 20 columns scaled horizontally by S, Gaspari-Cohn
-radius 12 cells), moves it to cuda:0 and calls :func:`oak_gb300.loc_analysis` K times, printing
-the device time of each stage of the last call. Used to run one precision's kernels in
-isolation (profiling, quick timing); the full benchmark is bench.py.
+``local`` builds the seeded single-variable case (360 x 180 x 20 columns scaled horizontally by
+S, N = 64, Gaspari-Cohn radius 12 cells); ``batched`` the 5-variable case (720 x 360 columns of
+121 elements scaled by S, N = 100, bilinear observations clustered on tracks). Either is moved
+to cuda:0 and :func:`oak_gb300.loc_analysis` is called K times, printing the device time of
+each stage of the last call. Used to run one precision's kernels in isolation (profiling,
+quick timing); the full benchmark is bench.py.
 """
 from __future__ import annotations
 
@@ -25,13 +28,21 @@ def main(argv=None):
     lp.add_argument("--N", type=int, default=64)
     lp.add_argument("--m", type=int, default=50000,
                     help="observations at scale 1 (the case scales them by S^2)")
+    bp = sub.add_parser("batched", help="run the 5-variable batched workload on cuda:0")
+    bp.add_argument("--scale", type=float, default=0.25)
+    bp.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    bp.add_argument("--calls", type=int, default=2)
+    bp.add_argument("--N", type=int, default=100)
     a = p.parse_args(argv)
 
     import torch
     import oak_gb300
-    from oak_gb300.workloads import local_case
+    from oak_gb300.workloads import batched_case, local_case
 
-    c = local_case(scale=a.scale, N=a.N, m=a.m)
+    if a.cmd == "local":
+        c = local_case(scale=a.scale, N=a.N, m=a.m)
+    else:
+        c = batched_case(scale=a.scale, N=a.N)
     dev = torch.device("cuda", 0)
     T = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=dev)
     F = lambda x: torch.as_tensor(np.ascontiguousarray(np.asarray(x).T), device=dev).t()

@@ -154,8 +154,8 @@ int scratch(Ctx* c, BufId id, size_t count, T** out, const char* name) {
 int check_dims(const oakg_dims* d) {
   if (!d) return fail(OAKG_ERR_ARGS, "dims is NULL");
   if (d->n <= 0) return fail(OAKG_ERR_ARGS, "n must be positive (got %lld)", (long long)d->n);
-  if (d->N < 2 || d->N > max_fp64_ensemble())
-    return fail(OAKG_ERR_ARGS, "ensemble size N=%d outside [2, %d]", d->N, max_fp64_ensemble());
+  if (d->N < 2 || d->N > max_ensemble())
+    return fail(OAKG_ERR_ARGS, "ensemble size N=%d outside [2, %d]", d->N, max_ensemble());
   if (d->m < 0) return fail(OAKG_ERR_ARGS, "m must be >= 0");
   if (d->m > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "m above 2^31-2");
   if (d->ldS < d->n) return fail(OAKG_ERR_ARGS, "ldS < n");
@@ -351,6 +351,9 @@ int check_loc(const oakg_dims* dims, const oakg_loc* loc, int32_t Z) {
     return fail(OAKG_ERR_ARGS, "loctype must be 1, 2 or 3 (got %d)", loc->loctype);
   if (loc->precision != OAKG_PREC_FP64 && loc->precision != OAKG_PREC_MIXED)
     return fail(OAKG_ERR_ARGS, "unknown precision mode %d", loc->precision);
+  if (loc->precision == OAKG_PREC_FP64 && dims->N > max_fp64_ensemble())
+    return fail(OAKG_ERR_ARGS, "the FP64 form takes N <= %d (N=%d: use OAKG_PREC_MIXED)",
+                max_fp64_ensemble(), dims->N);
   return OAKG_OK;
 }
 
@@ -600,6 +603,8 @@ int adjoint_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z, const in
                  double* dJ_dinfl) {
   int rc = check_loc(dims, loc, Z);
   if (rc) return rc;
+  if (dims->N > max_fp64_ensemble())
+    return fail(OAKG_ERR_ARGS, "the adjoint (FP64) takes N <= %d", max_fp64_ensemble());
   if (!dJ_dxa) return fail(OAKG_ERR_ARGS, "dJ_dxa is required");
   if (!(inflation > 0.0)) return fail(OAKG_ERR_ARGS, "inflation must be positive");
   const int64_t n = dims->n, m = dims->m, ldS = dims->ldS;
@@ -693,6 +698,8 @@ int analysis_impl(const oakg_dims* dims, const double* xf, const double* Hxf,
                   double* xa, double* Sa, double* ampl) {
   int rc = check_dims(dims);
   if (rc) return rc;
+  if (dims->N > max_fp64_ensemble())
+    return fail(OAKG_ERR_ARGS, "the global analysis (FP64) takes N <= %d", max_fp64_ensemble());
   const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
   const int N = dims->N, mem = dims->mem;
   if (!xf || !Sf || !xa) return fail(OAKG_ERR_ARGS, "xf, Sf and xa are required");

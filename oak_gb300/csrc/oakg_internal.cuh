@@ -128,6 +128,14 @@ cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
 cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
                             float* d_ampl, int32_t* d_status, cudaStream_t st);
+// E1 and E3 for eig32_max_n() < N <= eig128_max_n() (one 128-thread block per zone; E2 is the
+// generic one)
+int eig128_max_n();
+cudaError_t eig128_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
+                           cudaStream_t st);
+cudaError_t eig128_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
+                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
+                             float* d_ampl, int32_t* d_status, cudaStream_t st);
 
 // ---- ensemble.cu: the ensemble prologue (mean, anomalies, sparse H E + Hshift) and epilogue
 // (inflation, correction clip, reconstruction); HEf_scratch holds m x N values.
@@ -157,6 +165,7 @@ cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d
                                   cudaStream_t st);
 
 int max_fp64_ensemble();  // largest N the FP64 kernels accept
+int max_ensemble();       // largest N of the mixed-precision form
 
 // ---- oakg_api.cu
 void count_launches(int k);       // kernel-launch accounting (oakg_launch_count)

@@ -39,7 +39,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kNMax = 112;               // largest N (matches max_fp64_ensemble)
+constexpr int kNMax = 128;               // largest N of the eigensolve stages
 constexpr int kMaxSweepsPerN = 30;
 
 template <typename R>
@@ -702,13 +702,15 @@ cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z,
   return cudaSuccess;
 }
 
-// FP32 with at most 64 members: the register-blocked E1/E3 of zone_eig32.cu (they share the
+// FP32 with at most 128 members: the register-blocked E1/E3 of zone_eig32.cu (they share the
 // aux layout and the inverse-iteration output with E2a/E2b, and store the reflectors
-// vector-major, so both are used together)
+// vector-major, so both are used together): warp-per-zone kernels up to 64 members,
+// block-per-zone kernels up to 128
 template <>
 cudaError_t launch_e1<float>(int N, int32_t nzc, float* d_GT, float* d_aux,
                              const int32_t* d_nobs, int32_t* d_work, cudaStream_t st) {
   if (N <= eig32_max_n()) return eig32_tridiag(N, nzc, d_GT, d_aux, d_nobs, st);
+  if (N <= eig128_max_n()) return eig128_tridiag(N, nzc, d_GT, d_aux, d_nobs, st);
   size_t smem1 = (size_t)(N * (N + 1) + 2 * N) * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_eig_tridiag<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
@@ -726,6 +728,9 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
   if (N <= eig32_max_n())
     return eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
                            st);
+  if (N <= eig128_max_n())
+    return eig128_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
+                            st);
   size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(float) + (size_t)N * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);

@@ -46,9 +46,10 @@ constexpr int LDV = NB + 4;   // row stride of vector-major shared matrices (16-
 
 __host__ __device__ inline int aux_stride32(int N) { return 5 * N + 2; }
 
-__device__ __forceinline__ void vload(float (&x)[NB], const float* p) {
+template <int L>
+__device__ __forceinline__ void vload(float (&x)[L], const float* p) {
 #pragma unroll
-  for (int c = 0; c < NB; c += 4) {
+  for (int c = 0; c < L; c += 4) {
     const float4 v = *reinterpret_cast<const float4*>(p + c);
     x[c] = v.x;
     x[c + 1] = v.y;
@@ -57,9 +58,10 @@ __device__ __forceinline__ void vload(float (&x)[NB], const float* p) {
   }
 }
 
-__device__ __forceinline__ void vstore(const float (&x)[NB], float* p) {
+template <int L>
+__device__ __forceinline__ void vstore(const float (&x)[L], float* p) {
 #pragma unroll
-  for (int c = 0; c < NB; c += 4)
+  for (int c = 0; c < L; c += 4)
     *reinterpret_cast<float4*>(p + c) = make_float4(x[c], x[c + 1], x[c + 2], x[c + 3]);
 }
 
@@ -72,8 +74,8 @@ __device__ __forceinline__ void vstore(const float (&x)[NB], float* p) {
 // its rows are final (k >= 31).
 constexpr int kZpb = 4;
 
-template <int SLOT>
-__device__ __forceinline__ void owner_reflector(const float (&row)[NB], int k, int N, float* vbuf,
+template <int SLOT, int L>
+__device__ __forceinline__ void owner_reflector(const float (&row)[L], int k, int N, float* vbuf,
                                                 float* ax, float* beta_slot) {
   // single entries are read back through shared memory: an equality-selected register
   // element would become a dynamic index and move the row to local memory
@@ -81,7 +83,7 @@ __device__ __forceinline__ void owner_reflector(const float (&row)[NB], int k, i
   const float x0 = vbuf[k + 1], dk = vbuf[k];
   float sig = 0.f;
 #pragma unroll
-  for (int c = 0; c < NB; c++)
+  for (int c = 0; c < L; c++)
     if (c > k + 1) sig = fmaf(row[c], row[c], sig);
   const float mu = sqrtf(fmaf(x0, x0, sig));
   const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
@@ -89,7 +91,7 @@ __device__ __forceinline__ void owner_reflector(const float (&row)[NB], int k, i
   const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
   const float bk = skip ? 0.f : 2.f / vv;
 #pragma unroll
-  for (int c = 0; c < NB; c += 4) {
+  for (int c = 0; c < L; c += 4) {
     float4 q4;
     q4.x = (c + 0 > k + 1) ? row[c + 0] : 0.f;
     q4.y = (c + 1 > k + 1) ? row[c + 1] : 0.f;
@@ -945,6 +947,445 @@ __global__ void __launch_bounds__(kT2)
   }
 }
 
+// ------------------------------------------------------------------------- N <= 128: E1, E3
+// Ensembles of 65 to 128 members: one block of NB2 = 128 threads per zone, thread t holding row
+// t (E1) or eigenvector t (E3) of up to 128 elements in registers, so products stay
+// thread-local as in the warp-per-zone kernels above; rows and vectors are shared through
+// shared memory with block barriers. The arithmetic is that of E1 and E3 above.
+constexpr int NB2 = 128;
+constexpr int LDV2 = NB2 + 4;
+
+// block-wide sum (every thread gets it); red: 4 floats of shared scratch
+__device__ __forceinline__ float block_sum128(float x, float* red) {
+  x = wsum(x);
+  __syncthreads();  // red free (a previous use is complete)
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  return (red[0] + red[1]) + (red[2] + red[3]);
+}
+
+// E1 for N <= 128. Thread t holds row t of the scaled symmetric matrix (a[c] = A[t][c]); the
+// owner of row k forms reflector k; p = beta A v is a register dot per row; kc = beta (p . v) / 2
+// from per-warp partials; the update A -= v w^T + w v^T takes w_c = p_c - kc v_c from the
+// published p. v, p and the partials are double-buffered by step parity: two barriers a step.
+// Rows <= k are final after step k and columns <= k are not read again, so 16-column groups
+// lying there are skipped.
+__global__ void __launch_bounds__(NB2, 3)
+    k_eig_tridiag128(int N, int32_t nzc, float* __restrict__ GT, float* __restrict__ aux,
+                     const int32_t* __restrict__ nobs) {
+  __shared__ __align__(16) float vbuf[2][NB2];
+  __shared__ __align__(16) float pbuf[2][NB2];
+  __shared__ float red[2][4];
+  __shared__ float beta_s[2];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  float* Gz = GT + (int64_t)zl * N * N;
+  float* ax = aux + (int64_t)zl * aux_stride32(N);
+  float a[NB2];
+#pragma unroll
+  for (int c = 0; c < NB2; c++) a[c] = (t < N && c < N) ? Gz[t * N + c] : 0.f;
+  float amax = 0.f;
+#pragma unroll
+  for (int c = 0; c < NB2; c++) amax = fmaxf(amax, fabsf(a[c]));
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if (lane == 0) red[0][warp] = amax;
+  __syncthreads();  // also: every row read before reflectors overwrite the slot
+  float scale = fmaxf(fmaxf(red[0][0], red[0][1]), fmaxf(red[0][2], red[0][3]));
+  if (!(scale > 0.f) || isinf(scale)) scale = 1.f;
+  const float iscale = 1.f / scale;
+#pragma unroll
+  for (int c = 0; c < NB2; c++) a[c] *= iscale;
+  if (t == 0) ax[5 * N] = scale;
+  __syncthreads();  // red[0] read before step 0 reuses it
+  for (int k = 0; k < N - 2; k++) {
+    const int b = k & 1;
+    float* vb = vbuf[b];
+    float* pb = pbuf[b];
+    if (t == k) owner_reflector<0>(a, k, N, vb, ax, &beta_s[b]);
+    __syncthreads();  // v and beta published
+    const float bk = beta_s[b];
+    const float vr = vb[t];
+    if (t < N) Gz[(int64_t)k * N + t] = vr;  // reflector k, vector-major, zero padded
+    if (bk == 0.f) continue;                 // block-uniform; an identity reflector
+    const bool act = t > k;
+    float p0 = 0.f, p1 = 0.f;
+    if (act) {
+#pragma unroll
+      for (int g = 0; g < NB2 / 16; g++) {
+        if (16 * g + 15 > k) {
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            const int c = 16 * g + 4 * m;
+            const float4 v4 = *reinterpret_cast<const float4*>(vb + c);
+            p0 = fmaf(a[c + 0], v4.x, p0);
+            p1 = fmaf(a[c + 1], v4.y, p1);
+            p0 = fmaf(a[c + 2], v4.z, p0);
+            p1 = fmaf(a[c + 3], v4.w, p1);
+          }
+        }
+      }
+    }
+    const float p = bk * (p0 + p1);
+    pb[t] = p;
+    const float pv = wsum(p * vr);
+    if (lane == 0) red[b][warp] = pv;
+    __syncthreads();  // p and the partials published
+    const float kc = 0.5f * bk * ((red[b][0] + red[b][1]) + (red[b][2] + red[b][3]));
+    if (act) {
+      const float wr = fmaf(-kc, vr, p);
+#pragma unroll
+      for (int g = 0; g < NB2 / 16; g++) {
+        if (16 * g + 15 > k) {
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            const int c = 16 * g + 4 * m;
+            const float4 v4 = *reinterpret_cast<const float4*>(vb + c);
+            const float4 p4 = *reinterpret_cast<const float4*>(pb + c);
+            const float vc[4] = {v4.x, v4.y, v4.z, v4.w};
+            const float pc[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const float wc = fmaf(-kc, vc[q], pc[q]);
+              a[c + q] = fmaf(-vr, wc, fmaf(-wr, vc[q], a[c + q]));
+            }
+          }
+        }
+      }
+    }
+  }
+  // trailing 2 x 2 block: rows N-2 and N-1, read back through shared memory
+  __syncthreads();  // the last step's buffers consumed
+  if (t == N - 2) vstore(a, vbuf[0]);
+  if (t == N - 1) vstore(a, vbuf[1]);
+  __syncthreads();
+  if (t == 0) {
+    ax[N - 2] = vbuf[0][N - 2];
+    ax[2 * N + N - 2] = 0.f;
+    ax[N + N - 2] = vbuf[1][N - 2];
+    ax[N - 1] = vbuf[1][N - 1];
+    ax[N + N - 1] = 0.f;
+    ax[2 * N + N - 1] = 0.f;
+  }
+}
+
+// E3 for N <= 128: thread j holds eigenvector j; the steps of k_eig_transform32 with block
+// barriers. One shared NB2 x NB2 matrix (vector-major, 16-byte rows) holds the final vectors
+// of the Gram-Schmidt sweep, then the reflectors, U, W = U diag(lambda'^1/4) and T.
+struct Zone128 {
+  float buf[NB2 * LDV2];
+  float lam[NB2], sq[NB2], qs[NB2], gs[NB2], bet[NB2], tt[NB2], cc[NB2], vv[NB2], uv[NB2],
+      vn[NB2], t0[NB2];
+  int flag[NB2];
+  float red[4];
+};
+constexpr size_t kSmem128 = sizeof(Zone128);
+
+// x . u over the 16-component groups g0 <= g < ng
+__device__ __forceinline__ float vdot128(const float (&x)[NB2], const float* u, int g0, int ng) {
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+  for (int g = 0; g < NB2 / 16; g++) {
+    if (g >= g0 && g < ng) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const int c = 16 * g + 4 * m;
+        const float4 v = *reinterpret_cast<const float4*>(u + c);
+        s0 = fmaf(x[c], v.x, s0);
+        s1 = fmaf(x[c + 1], v.y, s1);
+        s0 = fmaf(x[c + 2], v.z, s0);
+        s1 = fmaf(x[c + 3], v.w, s1);
+      }
+    }
+  }
+  return s0 + s1;
+}
+
+// x -= f u over the groups g0 <= g < ng
+__device__ __forceinline__ void vaxpy128(float (&x)[NB2], float f, const float* u, int g0,
+                                         int ng) {
+#pragma unroll
+  for (int g = 0; g < NB2 / 16; g++) {
+    if (g >= g0 && g < ng) {
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const int c = 16 * g + 4 * m;
+        const float4 v = *reinterpret_cast<const float4*>(u + c);
+        x[c] = fmaf(-f, v.x, x[c]);
+        x[c + 1] = fmaf(-f, v.y, x[c + 1]);
+        x[c + 2] = fmaf(-f, v.z, x[c + 2]);
+        x[c + 3] = fmaf(-f, v.w, x[c + 3]);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NB2, 3)
+    k_eig_transform128(int N, int32_t nzc, float* __restrict__ GT, const float* __restrict__ aux,
+                       const float* __restrict__ Zg, const float* __restrict__ gv,
+                       const int32_t* __restrict__ nobs, int rotate,
+                       float* __restrict__ ampl_out, int32_t* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  Zone128& zs = *reinterpret_cast<Zone128*>(sm_raw);
+  const int t = threadIdx.x;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  float* Gz = GT + (int64_t)zl * N * N;
+  const float* ax = aux + (int64_t)zl * aux_stride32(N);
+  const float* Zz = Zg + (int64_t)zl * N * N;
+  float* buf = zs.buf;
+  const int ng = (N + 15) >> 4;  // 16-component groups holding the N components
+  {
+    double l = (t < N) ? (double)ax[3 * N + t] : 0.0;
+    if (l < 0.0) l = 0.0;
+    const double li = 1.0 / (1.0 + l);
+    const double s = sqrt(li);
+    zs.lam[t] = (float)li;
+    zs.sq[t] = (float)s;
+    zs.qs[t] = (float)sqrt(s);
+    zs.gs[t] = (t < N) ? gv[(int64_t)zl * N + t] : 0.f;
+    zs.bet[t] = (t < N - 2) ? ax[2 * N + t] : 0.f;
+    zs.flag[t] = 1;
+  }
+  float x[NB2];
+#pragma unroll
+  for (int i = 0; i < NB2; i++)
+    x[i] = (t < N) ? ((i < N) ? Zz[(int64_t)t * N + i] : 0.f) : ((i == t) ? 1.f : 0.f);
+  __syncthreads();
+  // modified Gram-Schmidt on the eigenvectors of Tri, largest eigenvalue first, with the
+  // acceptance test and residual-keeping of k_eig_transform32
+  for (int c = N - 1; c >= 0; c--) {
+    if (t == c) {
+      float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+      for (int i = 0; i < NB2; i += 2) {
+        s0 = fmaf(x[i], x[i], s0);
+        s1 = fmaf(x[i + 1], x[i + 1], s1);
+      }
+      const float s = s0 + s1;
+      const bool ok = s >= 0.5f;
+      const float sc = ok ? rsqrtf(s) : 1.f;  // a collapsed vector keeps its residual
+#pragma unroll
+      for (int i = 0; i < NB2; i++) x[i] *= sc;
+      vstore(x, buf + c * LDV2);
+      if (!ok) zs.flag[c] = 0;
+    }
+    __syncthreads();  // vector c final and published
+    if (t < c && zs.flag[c]) {
+      const float* uc = buf + c * LDV2;
+      vaxpy128(x, vdot128(x, uc, 0, ng), uc, 0, ng);
+    }
+  }
+  int ncol = 0;
+  if (t < N && !zs.flag[t]) ncol = 1;
+  if (__syncthreads_or(ncol)) {
+    // complement fill, as in k_eig_transform32
+    const float onenrm = ax[5 * N + 1];
+    int left = 0;
+    for (int c = 0; c < N; c++) left += zs.flag[c] ? 0 : 1;
+    float* td = zs.uv;
+    float* te = zs.vn;
+    td[t] = (t < N) ? ax[t] : 0.f;
+    te[t] = (t < N - 1) ? ax[N + t] : 0.f;
+    for (int c = 0; c < N; c++) {
+      if (zs.flag[c]) continue;  // block-uniform (flags change only between barriers)
+      const float r = buf[c * LDV2 + t];
+      const bool resid = block_sum128(r * r, zs.red) >= kResidMin;
+      --left;
+      const bool refine = !resid && left > 0 && onenrm > 1e4f * 1e-36f;
+      if (!resid) {
+        unsigned hsh = (unsigned)t * 2246822519u ^ ((unsigned)c * 3266489917u + 0x27d4eb2fu);
+        hsh ^= hsh >> 15;
+        hsh *= 2654435761u;
+        hsh ^= hsh >> 13;
+        buf[c * LDV2 + t] =
+            (t < N) ? (float)((double)(hsh & 0xffffff) * (1.0 / 16777216.0) - 0.5) : 0.f;
+      }
+      __syncthreads();
+      for (int it = 0;; it++) {
+        for (int pass = 0; pass < 2; pass++) {
+          float s = 0.f;
+          if (t < N && t != c && zs.flag[t]) {
+            const float* uk = buf + t * LDV2;
+            const float* uc = buf + c * LDV2;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+            for (int i = 0; i < 16 * ng; i += 4) {
+              const float4 a4 = *reinterpret_cast<const float4*>(uk + i);
+              const float4 b4 = *reinterpret_cast<const float4*>(uc + i);
+              s0 = fmaf(a4.x, b4.x, s0);
+              s1 = fmaf(a4.y, b4.y, s1);
+              s2 = fmaf(a4.z, b4.z, s2);
+              s3 = fmaf(a4.w, b4.w, s3);
+            }
+            s = (s0 + s1) + (s2 + s3);
+          }
+          zs.t0[t] = s;
+          __syncthreads();
+          float s0 = buf[c * LDV2 + t], s1 = 0.f;
+          for (int k = 0; k < N; k += 2) {
+            s0 = fmaf(-zs.t0[k], buf[k * LDV2 + t], s0);
+            if (k + 1 < N) s1 = fmaf(-zs.t0[k + 1], buf[(k + 1) * LDV2 + t], s1);
+          }
+          __syncthreads();
+          buf[c * LDV2 + t] = s0 + s1;
+          __syncthreads();
+        }
+        const float u = buf[c * LDV2 + t];
+        const float tot = block_sum128(u * u, zs.red);
+        buf[c * LDV2 + t] = u * ((tot > 0.f) ? rsqrtf(tot) : 0.f);
+        __syncthreads();
+        if (it == kFillIters || !refine) break;
+        if (t == 0)
+          tri_solve32(buf + c * LDV2, td, te, N, ax[4 * N + c], 5.9604645e-8f * onenrm, zs.tt,
+                      zs.cc, zs.vv);
+        __syncthreads();
+      }
+      if (t == 0) zs.flag[c] = 1;
+      __syncthreads();
+    }
+  }
+  // buf row j holds final vector j (stored by its owner, or filled): reload, so that no
+  // vector stays live in registers across the fill
+#pragma unroll
+  for (int i = 0; i < NB2; i++)
+    x[i] = (t < N) ? buf[t * LDV2 + i] : ((i == t) ? 1.f : 0.f);
+  __syncthreads();  // every thread holds its final vector: buf takes the reflectors
+  for (int idx = t; idx < NB2 * NB2; idx += NB2) {
+    const int k = idx >> 7, c = idx & (NB2 - 1);
+    buf[k * LDV2 + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
+  }
+  __syncthreads();
+  // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k)
+  for (int k = N - 3; k >= 0; k--) {
+    const float bk = zs.bet[k];
+    if (bk == 0.f) continue;  // block-uniform
+    const float* vk = buf + k * LDV2;
+    const int g0 = (k + 1) >> 4;
+    vaxpy128(x, bk * vdot128(x, vk, g0, ng), vk, g0, ng);
+  }
+  __syncthreads();  // the reflectors are read: buf holds U from here on
+  vstore(x, buf + t * LDV2);
+  {
+    // per-vector scalars: lambda' (u_t . g), colsum(u_t) / sqrt(lambda')
+    const float y = vdot128(x, zs.gs, 0, ng);
+    float cs = 0.f;
+#pragma unroll
+    for (int i = 0; i < NB2; i++) cs += x[i];
+    zs.tt[t] = (t < N) ? zs.lam[t] * y : 0.f;
+    zs.cc[t] = (t < N) ? cs / zs.sq[t] : 0.f;
+  }
+  __syncthreads();
+  // ampl = U tt, v = U cc (thread: component t)
+  int nan_flag = 0;
+  float vsq = 0.f;
+  {
+    float sa = 0.f, sv = 0.f;
+    for (int jj = 0; jj < N; jj++) {
+      const float u = buf[jj * LDV2 + t];
+      sa = fmaf(u, zs.tt[jj], sa);
+      sv = fmaf(u, zs.cc[jj], sv);
+    }
+    if (t < N) {
+      ampl_out[(int64_t)zl * N + t] = sa;
+      if (!(sa == sa) || isinf(sa)) nan_flag = 1;
+      vsq = sv * sv;
+    }
+    zs.vv[t] = (t < N) ? sv : 0.f;
+  }
+  nan_flag = __syncthreads_or(nan_flag);
+  const float vinv = rotate ? 1.f / sqrtf(block_sum128(vsq, zs.red)) : 0.f;
+  __syncthreads();  // buf read by every thread before W overwrites it
+  {
+    const float q = zs.qs[t];
+#pragma unroll
+    for (int i = 0; i < NB2; i++) x[i] *= q;
+    vstore(x, buf + t * LDV2);  // W = U diag(qs); padding vectors stay unit vectors
+  }
+  float sv_ = 1.f;
+  const float wv = (float)(1.0 / sqrt((double)N));
+  if (rotate) {
+    const float vN = zs.vv[N - 1] * vinv;
+    sv_ = signbit(vN) ? -1.f : 1.f;
+    const float vn = (t < N) ? zs.vv[t] * vinv : 0.f;
+    zs.vn[t] = vn;
+    zs.uv[t] = vn + ((t == N - 1) ? sv_ : 0.f);
+    zs.t0[t] = (t < N) ? wv : 0.f;                            // w (padded)
+    zs.tt[t] = (t < N) ? wv + ((t == N - 1) ? 1.f : 0.f) : 0.f;  // u_w = w + e_N
+  }
+  __syncthreads();
+  // T_sym = W W^T: thread t computes row t
+  float T0[NB2];
+#pragma unroll
+  for (int b = 0; b < NB2; b++) T0[b] = 0.f;
+  for (int jj = 0; jj < N; jj++) {
+    const float* w = buf + jj * LDV2;
+    const float wa = w[t];
+#pragma unroll
+    for (int g = 0; g < NB2 / 16; g++) {
+      if (g < ng) {
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          const int b = 16 * g + 4 * m;
+          const float4 wb = *reinterpret_cast<const float4*>(w + b);
+          T0[b] = fmaf(wa, wb.x, T0[b]);
+          T0[b + 1] = fmaf(wa, wb.y, T0[b + 1]);
+          T0[b + 2] = fmaf(wa, wb.z, T0[b + 2]);
+          T0[b + 3] = fmaf(wa, wb.w, T0[b + 3]);
+        }
+      }
+    }
+  }
+  if (rotate) {
+    // Omega = P_v P_w + (1 - s_v s_w) v w^T (matoper.F90:509-535), as in k_eig_transform32:
+    // T1 = T_sym - (T_sym u_v) u_v^T / c_v, T2 = T1 - (T1 u_w) u_w^T / c_w + (1 - s_v) (T_sym v) w^T.
+    // T1 u_w = T_sym u_w - (T_sym u_v / c_v)(u_v . u_w), so one pass gives every row dot and a
+    // second applies the three rank-one terms (u_v, u_w, w and v through shared memory: a
+    // per-column select would be kept live for all 128 columns between the passes).
+    const float icv = 1.f / (1.f + fabsf(zs.vn[N - 1]));
+    const float icw = 1.f / (1.f + wv);
+    const float extra = 1.f - sv_;
+    float pa = 0.f, pb = 0.f, pw = 0.f, suu = 0.f;
+#pragma unroll
+    for (int b = 0; b < NB2; b += 4) {
+      const float4 u4 = *reinterpret_cast<const float4*>(zs.uv + b);
+      const float4 n4 = *reinterpret_cast<const float4*>(zs.vn + b);
+      const float4 w4 = *reinterpret_cast<const float4*>(zs.tt + b);
+      const float uvb[4] = {u4.x, u4.y, u4.z, u4.w}, vnb[4] = {n4.x, n4.y, n4.z, n4.w};
+      const float uwb[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        pa = fmaf(T0[b + q], uvb[q], pa);
+        pb = fmaf(T0[b + q], vnb[q], pb);
+        pw = fmaf(T0[b + q], uwb[q], pw);
+        suu = fmaf(uvb[q], uwb[q], suu);
+      }
+    }
+    pa *= icv;
+    const float pg = icw * fmaf(-pa, suu, pw);
+    const float eb = extra * pb;
+    __syncthreads();  // the pass below reads the vectors again (no 128 values kept live)
+#pragma unroll
+    for (int b = 0; b < NB2; b += 4) {
+      const float4 u4 = *reinterpret_cast<const float4*>(zs.uv + b);
+      const float4 w4 = *reinterpret_cast<const float4*>(zs.tt + b);
+      const float4 m4 = *reinterpret_cast<const float4*>(zs.t0 + b);
+      const float uvb[4] = {u4.x, u4.y, u4.z, u4.w}, uwb[4] = {w4.x, w4.y, w4.z, w4.w};
+      const float wb[4] = {m4.x, m4.y, m4.z, m4.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        T0[b + q] = fmaf(eb, wb[q], fmaf(-pg, uwb[q], fmaf(-pa, uvb[q], T0[b + q])));
+    }
+  }
+  __syncthreads();  // W read by every thread before T is staged in buf
+  vstore(T0, buf + t * LDV2);
+  __syncthreads();
+  for (int idx = t; idx < N * N; idx += NB2) {
+    const int row = idx / N, c = idx - row * N;
+    Gz[idx] = buf[row * LDV2 + c];
+  }
+  if (t == 0 && nan_flag) status[zl] |= ZST_NAN;
+}
+
 }  // namespace
 
 int eig32_max_n() { return NB; }
@@ -981,6 +1422,28 @@ cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
   const int blocks = (nzc + kZpb3 - 1) / kZpb3;
   k_eig_transform32<<<blocks > 0 ? blocks : 1, 32 * kZpb3, kSmem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
                                                             d_nobs, rotate, d_ampl, d_status);
+  return cudaGetLastError();
+}
+
+int eig128_max_n() { return NB2; }
+
+cudaError_t eig128_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
+                           cudaStream_t st) {
+  if (N < 2 || N > NB2) return cudaErrorInvalidValue;
+  k_eig_tridiag128<<<nzc > 0 ? nzc : 1, NB2, 0, st>>>(N, nzc, d_GT, d_aux, d_nobs);
+  return cudaGetLastError();
+}
+
+cudaError_t eig128_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
+                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
+                             float* d_ampl, int32_t* d_status, cudaStream_t st) {
+  if (N < 2 || N > NB2) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_eig_transform128,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kSmem128);
+  if (e != cudaSuccess) return e;
+  k_eig_transform128<<<nzc > 0 ? nzc : 1, NB2, kSmem128, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
+                                                               d_nobs, rotate, d_ampl, d_status);
   return cudaGetLastError();
 }
 

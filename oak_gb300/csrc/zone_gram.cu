@@ -394,6 +394,7 @@ cudaError_t launch_global(int64_t m, int N, const double* HSf, int64_t ldH, cons
 }  // namespace
 
 int max_fp64_ensemble() { return 112; }
+int max_ensemble() { return 128; }
 
 // Per-thread entry count classes: ceil((N(N+1)/2 + N) / 256).
 #define OAKG_GRAM_DISPATCH(FN, ...)                                         \
@@ -404,6 +405,7 @@ int max_fp64_ensemble() { return 112; }
     if (per_ <= 9) return FN<9>(__VA_ARGS__);                               \
     if (per_ <= 19) return FN<19>(__VA_ARGS__);                             \
     if (per_ <= 26) return FN<26>(__VA_ARGS__);                             \
+    if (per_ <= 33) return FN<33>(__VA_ARGS__);                             \
     return cudaErrorInvalidValue;                                           \
   } while (0)
 #define OAKG_GRAM_DISPATCH_T(FN, R, ...)                                    \
@@ -414,6 +416,7 @@ int max_fp64_ensemble() { return 112; }
     if (per_ <= 9) return FN<9, R>(__VA_ARGS__);                            \
     if (per_ <= 19) return FN<19, R>(__VA_ARGS__);                          \
     if (per_ <= 26) return FN<26, R>(__VA_ARGS__);                          \
+    if (per_ <= 33) return FN<33, R>(__VA_ARGS__);                          \
     return cudaErrorInvalidValue;                                           \
   } while (0)
 

@@ -81,84 +81,88 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Mixed form, N <= 64 and N % 8 == 0. A task is a tile of up to kRows rows of one zone, as in
-// k_zone_update, with T, the amplitudes and the Sf tile (converted to FP32) staged in shared
-// memory in one round of coalesced loads. A work item is one row x 8 columns of Sa; the items
-// of a warp share their 8 columns (consecutive threads take consecutive rows), so each k costs
-// the warp one broadcast 128-bit T load pair and one Sf load for 8 FMAs per thread. The FMA
+// Mixed form (any N). A block takes whole zones (grid-stride over zones), so T and the
+// amplitudes are staged in shared memory once per zone: T with its rows padded to NP columns (N
+// rounded up to a multiple of 8, zero padding). The zone's rows then go through in tiles of
+// kRows, each tile of Sf converted to FP32 and staged column by column (coalesced along rows).
+// A work item is one row x 8 columns of Sa; the items of a warp share their 8 columns
+// (consecutive threads take consecutive rows), so each k costs the warp one broadcast 128-bit
+// T load pair and one Sf load for 8 FMAs per thread; padding columns are not written. The FMA
 // order over k is that of k_zone_update<float>.
 constexpr int kColBlk = 8;
 
 __global__ void __launch_bounds__(kThreads)
-    k_zone_update_f32(int N, int32_t z0, int32_t nzc, const int64_t* __restrict__ zone_start,
-                      int tiles_per_zone, const double* __restrict__ xf,
+    k_zone_update_f32(int N, int NP, int32_t z0, int32_t nzc,
+                      const int64_t* __restrict__ zone_start, const double* __restrict__ xf,
                       const double* __restrict__ Sf, int64_t ldS, const float* __restrict__ T,
                       const float* __restrict__ ampl, const int32_t* __restrict__ nobs,
                       double* __restrict__ xa, double* __restrict__ Sa) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
-  float* Ts = reinterpret_cast<float*>(dyn_raw);  // [N][N]
-  float* Ss = Ts + N * N;                          // [N][kRows]
+  float* Ts = reinterpret_cast<float*>(dyn_raw);  // [N][NP]
+  float* Ss = Ts + N * NP;                         // [N][kRows]
   float* as = Ss + N * kRows;                      // [N]
-  const int64_t ntasks = (int64_t)nzc * tiles_per_zone;
-  const int ncb = N / kColBlk;
-  for (int64_t task = blockIdx.x; task < ntasks; task += gridDim.x) {
-    const int32_t zl = (int32_t)(task / tiles_per_zone);
-    const int tile = (int)(task - (int64_t)zl * tiles_per_zone);
+  const int ncb = NP / kColBlk;
+  for (int32_t zl = blockIdx.x; zl < nzc; zl += gridDim.x) {
     const int32_t z = z0 + zl;
     const int64_t i1 = zone_start[z], i2 = zone_start[z + 1];
-    const int64_t r0 = i1 + (int64_t)tile * kRows;
-    if (r0 >= i2) continue;  // uniform across the block
-    const int R_ = (int)((i2 - r0) < kRows ? (i2 - r0) : kRows);
     if (nobs[zl] == 0) {
-      for (int idx = threadIdx.x; idx < R_; idx += kThreads) xa[r0 + idx] = xf[r0 + idx];
+      for (int64_t i = i1 + threadIdx.x; i < i2; i += kThreads) xa[i] = xf[i];
       if (Sa && Sa != Sf) {
-        for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
-          const int k = idx / R_, r = idx - k * R_;
-          Sa[r0 + r + (int64_t)k * ldS] = Sf[r0 + r + (int64_t)k * ldS];
+        const int nr = (int)(i2 - i1);
+        for (int idx = threadIdx.x; idx < nr * N; idx += kThreads) {
+          const int k = idx / nr, r = idx - k * nr;
+          Sa[i1 + r + (int64_t)k * ldS] = Sf[i1 + r + (int64_t)k * ldS];
         }
       }
       continue;
     }
-    __syncthreads();  // previous task's shared data consumed
-    const float4* Tz4 = reinterpret_cast<const float4*>(T + (int64_t)zl * N * N);
-    float4* Ts4 = reinterpret_cast<float4*>(Ts);
+    __syncthreads();  // previous zone's shared data consumed
+    const float* Tz = T + (int64_t)zl * N * N;
     if (Sa) {
-      for (int idx = threadIdx.x; idx < N * N / 4; idx += kThreads) Ts4[idx] = Tz4[idx];
+      for (int idx = threadIdx.x; idx < N * NP; idx += kThreads) {
+        const int k = idx / NP, c = idx - k * NP;
+        Ts[idx] = (c < N) ? Tz[k * N + c] : 0.f;
+      }
     }
     for (int idx = threadIdx.x; idx < N; idx += kThreads) as[idx] = ampl[(int64_t)zl * N + idx];
-    for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
-      const int k = idx / R_, r = idx - k * R_;
-      Ss[k * kRows + r] = (float)Sf[r0 + r + (int64_t)k * ldS];
-    }
-    __syncthreads();
-    for (int r = threadIdx.x; r < R_; r += kThreads) {  // xa = xf + Sf ampl
-      float sx = 0.f;
-      for (int k = 0; k < N; k++) sx = fmaf(Ss[k * kRows + r], as[k], sx);
-      xa[r0 + r] = xf[r0 + r] + (double)sx;
-    }
-    if (Sa) {
-      for (int it = threadIdx.x; it < R_ * ncb; it += kThreads) {
-        const int cb = it / R_, r = it - cb * R_;
-        const int c0 = kColBlk * cb;
-        float acc[kColBlk];
+    for (int64_t r0 = i1; r0 < i2; r0 += kRows) {
+      const int R_ = (int)((i2 - r0) < kRows ? (i2 - r0) : kRows);
+      if (r0 > i1) __syncthreads();  // previous tile consumed
+      for (int idx = threadIdx.x; idx < R_ * N; idx += kThreads) {
+        const int k = idx / R_, r = idx - k * R_;
+        Ss[k * kRows + r] = (float)Sf[r0 + r + (int64_t)k * ldS];
+      }
+      __syncthreads();
+      for (int r = threadIdx.x; r < R_; r += kThreads) {  // xa = xf + Sf ampl
+        float sx = 0.f;
+        for (int k = 0; k < N; k++) sx = fmaf(Ss[k * kRows + r], as[k], sx);
+        xa[r0 + r] = xf[r0 + r] + (double)sx;
+      }
+      if (Sa) {
+        for (int it = threadIdx.x; it < R_ * ncb; it += kThreads) {
+          const int cb = it / R_, r = it - cb * R_;
+          const int c0 = kColBlk * cb;
+          float acc[kColBlk];
 #pragma unroll
-        for (int t = 0; t < kColBlk; t++) acc[t] = 0.f;
+          for (int t = 0; t < kColBlk; t++) acc[t] = 0.f;
 #pragma unroll 4
-        for (int k = 0; k < N; k++) {
-          const float sk = Ss[k * kRows + r];
-          const float4 ta = *reinterpret_cast<const float4*>(Ts + k * N + c0);
-          const float4 tb = *reinterpret_cast<const float4*>(Ts + k * N + c0 + 4);
-          acc[0] = fmaf(sk, ta.x, acc[0]);
-          acc[1] = fmaf(sk, ta.y, acc[1]);
-          acc[2] = fmaf(sk, ta.z, acc[2]);
-          acc[3] = fmaf(sk, ta.w, acc[3]);
-          acc[4] = fmaf(sk, tb.x, acc[4]);
-          acc[5] = fmaf(sk, tb.y, acc[5]);
-          acc[6] = fmaf(sk, tb.z, acc[6]);
-          acc[7] = fmaf(sk, tb.w, acc[7]);
-        }
+          for (int k = 0; k < N; k++) {
+            const float sk = Ss[k * kRows + r];
+            const float4 ta = *reinterpret_cast<const float4*>(Ts + k * NP + c0);
+            const float4 tb = *reinterpret_cast<const float4*>(Ts + k * NP + c0 + 4);
+            acc[0] = fmaf(sk, ta.x, acc[0]);
+            acc[1] = fmaf(sk, ta.y, acc[1]);
+            acc[2] = fmaf(sk, ta.z, acc[2]);
+            acc[3] = fmaf(sk, ta.w, acc[3]);
+            acc[4] = fmaf(sk, tb.x, acc[4]);
+            acc[5] = fmaf(sk, tb.y, acc[5]);
+            acc[6] = fmaf(sk, tb.z, acc[6]);
+            acc[7] = fmaf(sk, tb.w, acc[7]);
+          }
 #pragma unroll
-        for (int t = 0; t < kColBlk; t++) Sa[r0 + r + (int64_t)(c0 + t) * ldS] = (double)acc[t];
+          for (int t = 0; t < kColBlk; t++)
+            if (c0 + t < N) Sa[r0 + r + (int64_t)(c0 + t) * ldS] = (double)acc[t];
+        }
       }
     }
   }
@@ -222,22 +226,20 @@ cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zo
                              int32_t zone_max, const double* xf, const double* Sf,
                              int64_t ldS, const float* d_T, const float* d_ampl,
                              const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
-  if (N % kColBlk == 0) {
-    size_t smem = (size_t)(N * N + N * kRows + N) * sizeof(float);
+  const int NP = (N + kColBlk - 1) / kColBlk * kColBlk;
+  const size_t smem = (size_t)(N * NP + N * kRows + N) * sizeof(float);
+  if (smem <= 200 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_zone_update_f32,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int tiles = (zone_max + kRows - 1) / kRows;
-    if (tiles < 1) tiles = 1;
-    const int64_t ntasks = (int64_t)nzc * tiles;
     int bps = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_update_f32, kThreads, smem);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t cap = (int64_t)sms * (bps > 0 ? bps : 1) * 8;
-    const int grid = (int)(ntasks < cap ? (ntasks < 1 ? 1 : ntasks) : cap);
-    k_zone_update_f32<<<grid, kThreads, smem, st>>>(N, z0, nzc, d_zone_start, tiles, xf, Sf, ldS,
+    const int64_t cap = (int64_t)sms * (bps > 0 ? bps : 1) * 4;
+    const int grid = (int)(nzc < cap ? (nzc < 1 ? 1 : nzc) : cap);
+    k_zone_update_f32<<<grid, kThreads, smem, st>>>(N, NP, z0, nzc, d_zone_start, xf, Sf, ldS,
                                                     d_T, d_ampl, d_nobs, xa, Sa);
     count_launches(1);
     return cudaGetLastError();

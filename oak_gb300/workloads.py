@@ -3,6 +3,12 @@ configurations (the reference publishes no dataset for this path; these stand in
 
 * ``global_case``  -- one 2-D field 100 x 80, N = 30 members, m = 500 observations at distinct
   uniform cells, y = x_true + N(0, 0.1^2), R = 0.01 I (global analysis, rrsqrt.F90:196-208).
+* ``batched_case`` -- 5-variable state (temp, salt, u, v on 30 levels and the 2-D ssh) on a
+  720 x 360 grid, zone = one column of 4 * 30 + 1 = 121 elements, N = 100 members with
+  per-variable sd (temp 1.0, salt 0.2, ssh 0.05, u 0.1, v 0.1), m = 200,000 observations
+  (ssh 50 %, temp 30 %, salt 20 %) through bilinear interpolation (4 columns, nearest level),
+  70 % of them on 8 track segments so that zones near them select up to ~3,000, noise sd 0.1
+  of the variable's sd, Gaspari-Cohn support radius 12 cells.
 * ``local_case``   -- 3-D grid 360 x 180 x 20, one variable, N = 64 members (Gaussian
   random fields, horizontal length 8 cells, vertical 3 levels), m = 50,000 observations
   (70 % on 40 great-circle-like tracks, 30 % uniform, noise sd 0.1), zones = the 64,800
@@ -44,6 +50,8 @@ class Case:
     metric: int = 0
     loctype: int = 1
     obs_index: np.ndarray | None = None   # (m,) state index observed (nearest cell H)
+    H_index: np.ndarray | None = None     # (m, K) state indices of an interpolating H
+    H_weight: np.ndarray | None = None    # (m, K) their weights
     Ef: np.ndarray | None = None          # (n, N) ensemble, when kept
     HEf: np.ndarray | None = None
 
@@ -179,6 +187,95 @@ def local_case(scale=1.0, N=64, nz=20, m=50_000, radius=12.0, seed_cfg=1, track_
              Sf.astype(dtype, copy=False), HSf.astype(dtype, copy=False), np.full(m, 0.01),
              truth, zone_size, zone_pos, obs_pos, corr, maxl, weight=1, metric=0, loctype=1,
              obs_index=idx)
+    if keep_ensemble:
+        c.Ef, c.HEf = Ef, HEf
+    return c
+
+
+# variables of the batched state: (name, levels per column, sd)
+BATCHED_VARS = (("temp", 1.0), ("salt", 0.2), ("u", 0.1), ("v", 0.1), ("ssh", 0.05))
+
+
+def batched_case(scale=0.25, N=100, nz=30, m=200_000, radius=12.0, seed_cfg=2,
+                 track_frac=0.7, ntracks=8, keep_ensemble=False) -> Case:
+    """Config: batched mixed-precision local analysis, 720 x 360 columns of temp, salt, u, v
+    (nz levels) and ssh, N = 100, m = 200,000 bilinear observations clustered on tracks
+    (each track a segment a quarter of the grid long).
+
+    ``scale`` shrinks the horizontal grid by ``scale``, m by ``scale**2`` and the number of
+    tracks by ``scale`` (so the observation density along a track, and with it the largest
+    per-zone counts, stay those of the full grid). Column (i, j) is zone j*nx + i; inside it,
+    temp, salt, u, v levels 0..nz-1 then ssh: offset var*nz + k (ssh at 4*nz). Observations
+    sit at continuous (x, y) in cell units; H interpolates the 4 surrounding columns
+    bilinearly at the observation's level.
+    """
+    cfg = seed_cfg
+    nx = max(4, int(round(720 * scale)))
+    ny = max(4, int(round(360 * scale)))
+    if scale != 1.0:
+        m = max(1, int(round(m * scale * scale)))
+        ntracks = max(1, int(round(ntracks * scale)))
+    Z = nx * ny
+    zsz = 4 * nz + 1
+    n = Z * zsz
+    lengths3, lengths2 = (8.0, 8.0, 3.0), (8.0, 8.0)
+
+    def draw(seed):
+        x = np.empty((Z, zsz))
+        rng = np.random.default_rng(seed)
+        for v, (_, sd) in enumerate(BATCHED_VARS[:4]):
+            x[:, v * nz:(v + 1) * nz] = sd * gaussian_field((ny, nx, nz), lengths3, rng).reshape(Z, nz)
+        x[:, 4 * nz] = BATCHED_VARS[4][1] * gaussian_field((ny, nx), lengths2, rng).reshape(Z)
+        return x.reshape(-1)
+
+    truth = draw(1000 * cfg + 0)
+    Ef = np.empty((n, N), order="F")
+    for k in range(N):
+        Ef[:, k] = draw(1000 * cfg + 1 + k)
+    # observation positions: tracks (continuous along-track coordinate) + uniform
+    rng_pos = np.random.default_rng(1000 * cfg + 900)
+    m_track = int(round(track_frac * m))
+    rng_t = np.random.default_rng(1000 * cfg + 902)
+    per = np.full(ntracks, m_track // ntracks)
+    per[: m_track - per.sum()] += 1
+    xs, ys = [], []
+    for t in range(ntracks):
+        a = np.deg2rad(rng_t.uniform(10.0, 80.0))
+        i0 = rng_t.uniform(0.0, nx)
+        s0 = rng_t.uniform(0.0, 0.75 * (nx - 1))
+        i = rng_t.uniform(s0, s0 + 0.25 * (nx - 1), per[t])
+        j = ny / 2 + (ny / 2) * np.arctan(np.tan(a) * np.sin(2 * np.pi * (i - i0) / nx)) / (np.pi / 2)
+        xs.append(i)
+        ys.append(np.clip(j, 0.0, ny - 1.0))
+    xs.append(rng_pos.uniform(0.0, nx - 1, m - m_track))
+    ys.append(rng_pos.uniform(0.0, ny - 1, m - m_track))
+    ox, oy = np.concatenate(xs), np.concatenate(ys)
+    # variable split ssh 50 %, temp 30 %, salt 20 %; level uniform for the 3-D variables
+    u = rng_pos.uniform(0.0, 1.0, m)
+    var = np.where(u < 0.5, 4, np.where(u < 0.8, 0, 1))
+    lev = np.where(var == 4, 0, rng_pos.integers(0, nz, m))
+    off = np.where(var == 4, 4 * nz, var * nz + lev)
+    ix = np.minimum(np.floor(ox).astype(np.int64), nx - 2)
+    iy = np.minimum(np.floor(oy).astype(np.int64), ny - 2)
+    fx, fy = ox - ix, oy - iy
+    cols = np.stack([iy * nx + ix, iy * nx + ix + 1, (iy + 1) * nx + ix, (iy + 1) * nx + ix + 1], 1)
+    H_index = cols * zsz + off[:, None]
+    H_weight = np.stack([(1 - fx) * (1 - fy), fx * (1 - fy), (1 - fx) * fy, fx * fy], 1)
+    HEf = np.einsum("mk,mkn->mn", H_weight, Ef[H_index.reshape(-1), :].reshape(m, 4, N))
+    sd_obs = 0.1 * np.array([sd for _, sd in BATCHED_VARS])[var]
+    noise = np.random.default_rng(1000 * cfg + 901).standard_normal(m) * sd_obs
+    yo = np.einsum("mk,mk->m", H_weight, truth[H_index]) + noise
+    xf, Hxf, Sf, HSf = _anomalies(Ef, HEf)
+    zone_size = np.full(Z, zsz, dtype=np.int32)
+    zc = np.arange(Z)
+    zone_pos = np.zeros((Z, 4))
+    zone_pos[:, 0] = zc % nx
+    zone_pos[:, 1] = zc // nx
+    obs_pos = (ox, oy, lev.astype(np.float64), np.zeros(m))
+    c = Case(f"batched {nx}x{ny}x{nz} 5 variables N={N} m={m} GC radius {radius:g}", xf, Hxf,
+             yo, Sf, HSf, sd_obs ** 2, truth, zone_size, zone_pos, obs_pos,
+             np.full(Z, radius / 2.0), np.full(Z, radius), weight=1, metric=0, loctype=1,
+             H_index=H_index, H_weight=H_weight)
     if keep_ensemble:
         c.Ef, c.HEf = Ef, HEf
     return c

@@ -7,7 +7,7 @@ relevant-observation counts must be identical.
 import numpy as np
 import pytest
 
-from oak_gb300.workloads import local_case
+from oak_gb300.workloads import batched_case, local_case
 from oracle import cref
 
 pytestmark = pytest.mark.gpu
@@ -20,10 +20,11 @@ def _errs(xa, Sa, xa_o, Sa_o, xf):
             np.linalg.norm(Sa - Sa_o) / np.linalg.norm(Sa_o))
 
 
-# 64: the register-blocked FP32 eigensolve at its full width; 32 and 37: padded inside it
-# (37 is not a multiple of 4); 65 and 100: the generic FP32 kernels
+# 64: the warp-per-zone FP32 eigensolve at its full width; 32 and 37: padded inside it (37 is
+# not a multiple of 4); 65, 97, 100 and 128: the block-per-zone FP32 eigensolve (97 leaves a
+# partial 16-component group and a partial 8-column block of the update)
 @pytest.mark.parametrize("N,scale", [(64, 1 / 6), (32, 1 / 8), (37, 1 / 8), (65, 1 / 10),
-                                     (100, 1 / 10)])
+                                     (97, 1 / 10), (100, 1 / 10), (128, 1 / 10)])
 def test_mixed_local_matches_fp64_oracle(oakg, N, scale):
     c = local_case(scale=scale, N=N)
     xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
@@ -89,3 +90,35 @@ def test_dense_clusters_fill_many_tiles(oakg):
         assert np.array_equal(nobs, nobs_o)
         e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
         assert e_mean < tol and e_anom < tol, (prec, e_mean, e_anom)
+
+
+def test_mixed_batched_bilinear_case(oakg):
+    """The 5-variable batched case (121-element columns, N = 100, bilinear observations
+    clustered on track segments) against the oracle."""
+    c = batched_case(scale=1 / 16)
+    xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        weight=c.weight, precision=oakg.PREC_MIXED)
+    xa_o, Sa_o, _, nobs_o = cref.locanalysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                             c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                             c.max_len, kind=c.weight)
+    assert np.array_equal(nobs, nobs_o) and nobs_o.max() > 300
+    e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
+    assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)
+
+
+def test_ensemble_size_limits(oakg):
+    """N <= 128 in the mixed form, N <= 112 in the FP64 form (with a message naming the
+    mixed form)."""
+    c = local_case(scale=1 / 16, N=113, m=300)
+    args = (c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag, c.zone_pos, c.obs_pos,
+            c.corr_len, c.max_len)
+    with pytest.raises(oakg.OakError) as ei:
+        oakg.loc_analysis(*args, weight=c.weight, precision=oakg.PREC_FP64)
+    assert "OAKG_PREC_MIXED" in str(ei.value)
+    oakg.loc_analysis(*args, weight=c.weight, precision=oakg.PREC_MIXED)
+    c = local_case(scale=1 / 16, N=129, m=300)
+    with pytest.raises(oakg.OakError):
+        oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag, c.zone_pos,
+                          c.obs_pos, c.corr_len, c.max_len, weight=c.weight,
+                          precision=oakg.PREC_MIXED)
