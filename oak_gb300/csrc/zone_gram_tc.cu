@@ -1,4 +1,4 @@
-// K1 + K2, mixed-precision form on the tensor cores (ensembles of up to 64 members).
+// K1 + K2, mixed-precision form on the tensor cores (ensembles of up to 128 members).
 //
 // Selection makes the decisions of zone_gram.cu (assimilation.F90:3683-3771): d <= maxLength
 // and, for Gaspari-Cohn, locfun(d/L) /= 0. For Cartesian and 1-D distances they are taken from
@@ -6,16 +6,22 @@
 // than a relative 1e-6 from maxLength and r = d/L is below 2 - 1e-3 or above 2 + 1e-5; inside
 // those margins the reference's FP64 distance and locfun with IEEE rounding decide, as they do
 // for the spherical metrics. The selected set is therefore identical to the plain form's. The
-// weights themselves are FP32 (locfun or exp of the FP32 ratio). The Gram matrix G = HS_sel^T diag(c) HS_sel (rrsqrt.F90:135, c = w^2 / r from the
-// DCDCovar of rrsqrt.F90:395) is written as G = X^T X with X = diag(sqrt(c)) HS_sel and
-// computed by tcgen05.mma kind::tf32 with FP32 accumulation in tensor memory:
+// weights themselves are FP32 (locfun or exp of the FP32 ratio). The Gram matrix
+// G = HS_sel^T diag(c) HS_sel (rrsqrt.F90:135, c = w^2 / r from the DCDCovar of
+// rrsqrt.F90:395) is written as G = X^T X with X = diag(sqrt(c)) HS_sel and computed by
+// tcgen05.mma kind::tf32 with FP32 accumulation in tensor memory:
 //
 //   X (FP32) is split into two TF32 parts, X = X_hi + X_lo (X_lo = tf32(X - X_hi)), leaving a
-//   residual of ~2^-22 |X|. A K-tile of 32 selected observations is staged in shared memory as
-//   one 128-row operand S = [X_hi^T ; X_lo^T] (rows 0-63: hi parts of members 0-63, rows
-//   64-127: lo parts; K-major, 128-byte swizzle). One M=128, N=128 MMA chain with S as both A
-//   and B accumulates D = S S^T, whose four 64 x 64 blocks are X_hi^T X_hi, X_hi^T X_lo,
-//   X_lo^T X_hi and X_lo^T X_lo; G is their sum (symmetrised from the lower triangle).
+//   residual of ~2^-22 |X|. A K-tile of 32 selected observations is staged in shared memory
+//   (K-major, 128-byte swizzle).
+//   Up to 64 members: one 128-row operand S = [X_hi^T ; X_lo^T] (rows 0-63: hi parts of
+//   members 0-63, rows 64-127: lo parts). One M=128, N=128 MMA chain with S as both A and B
+//   accumulates D = S S^T, whose four 64 x 64 blocks are X_hi^T X_hi, X_hi^T X_lo, X_lo^T X_hi
+//   and X_lo^T X_lo; G is their sum.
+//   65 to 128 members: two 128-row operands X_hi^T and X_lo^T; three MMAs per K-step
+//   accumulate D = X_hi^T X_hi + X_hi^T X_lo + X_lo^T X_hi = G (the X_lo^T X_lo term, 2^-22
+//   relative, below the FP32 accumulation error, is left out).
+//   G is symmetrised from its lower triangle.
 //
 // The tensor-core accumulator is FP32 and its error grows with the length of the chain: zones on
 // dense observation tracks select thousands of observations, and one chain over all of them
@@ -47,20 +53,34 @@ namespace oakg {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int NB = 64;            // padded ensemble size
 constexpr int KT = 32;            // observations per K-tile (128 bytes of TF32 per row)
 constexpr int kRing = 512;        // selected-observation ring (power of two)
-constexpr uint32_t kTileBytes = 128u * 128u;
+constexpr uint32_t kOpBytes = 128u * 128u;  // one 128-row operand tile of a K-tile
 constexpr uint32_t kTmemCols = 128;
 constexpr int kWaitPolls = 1 << 22;
 constexpr int kChunkTiles = 8;    // K-tiles accumulated in tensor memory between reads
-constexpr int kTri = NB * (NB + 1) / 2;  // lower triangle of G
-constexpr size_t kTail = 12 * 1024;
-// dynamic shared memory: 1 KB alignment slack, two tiles, compensated innovation partials and
-// the lower-triangle G accumulator, padded (kTail) so that at most 4 CTAs share an SM (4 x 128
-// tensor-memory columns = all 512)
-constexpr size_t kDynSmem = 1024 + 2 * kTileBytes + 2 * 4 * NB * sizeof(float) + kTail;
-static_assert(kTri * sizeof(float) <= kTail, "G accumulator must fit in the tail");
+
+// Per padded ensemble width NB:
+//   NB = 64: one operand tile per K-tile buffer, S = [X_hi^T ; X_lo^T] (rows 0-63 / 64-127);
+//            D = S S^T and G is the sum of D's four 64 x 64 blocks; 4 CTAs per SM.
+//   NB = 128: two operand tiles, X_hi^T and X_lo^T; D = X_hi^T X_hi + X_hi^T X_lo + X_lo^T X_hi
+//            (X_lo^T X_lo, ~2^-22 relative, is left out) is G; 2 CTAs per SM.
+// Dynamic shared memory: 1 KB alignment slack, two K-tile buffers, compensated innovation
+// partials and the lower-triangle G accumulator (a tail padded, for NB = 64, so that at most 4
+// CTAs share an SM: 4 x 128 tensor-memory columns = all 512).
+template <int NB>
+struct TcCfg {
+  static constexpr int kOps = NB / 64;                    // operand tiles per buffer
+  static constexpr uint32_t kBufBytes = kOps * kOpBytes;  // one K-tile buffer
+  static constexpr int kTri = NB * (NB + 1) / 2;          // lower triangle of G
+  static constexpr int kQ = kThreads / NB;                // staging thread groups per member
+  static constexpr int kPasses = 8 / kQ;                  // 4-observation quads per thread
+  static constexpr int kCtas = (NB == 64) ? 4 : 2;
+  static constexpr size_t kTail = (NB == 64) ? 12 * 1024 : (size_t)kTri * sizeof(float);
+  static constexpr size_t kDynSmem =
+      1024 + 2 * kBufBytes + 2 * kQ * NB * sizeof(float) + kTail;
+  static_assert(kTri * sizeof(float) <= kTail, "G accumulator must fit in the tail");
+};
 
 struct TcShared {
   int32_t ring_q[kRing];
@@ -99,11 +119,12 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
 constexpr uint32_t kIdesc =
     (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t desc, uint32_t accum) {
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t accum) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %3, 0;\n"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %4, p;\n}\n" ::"r"(tmem_d),
-      "l"(desc), "l"(desc), "r"(accum), "r"(kIdesc));
+      "l"(adesc), "l"(bdesc), "r"(accum), "r"(kIdesc));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -169,24 +190,27 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float term) {
   s = t;
 }
 
-__global__ void __launch_bounds__(kThreads, 4)
+template <int NB>
+__global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
     k_zone_gram_tc(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
                    const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
                    const double* __restrict__ max_len, float* __restrict__ G,
                    float* __restrict__ gv, int32_t* __restrict__ nobs, int brute,
                    int32_t* __restrict__ work, int32_t* __restrict__ err) {
+  using C = TcCfg<NB>;
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   __shared__ __align__(16) TcShared ts;
   const uint32_t raw_addr = smem_u32(dyn_raw);
   const uint32_t pad = ((raw_addr + 1023u) & ~1023u) - raw_addr;
-  unsigned char* tiles = dyn_raw + pad;                 // 2 x kTileBytes, 1024-aligned
+  unsigned char* tiles = dyn_raw + pad;                 // 2 x C::kBufBytes, 1024-aligned
   const uint32_t tile_addr = raw_addr + pad;
-  float* gps = reinterpret_cast<float*>(tiles + 2 * kTileBytes);  // [4][NB] partial sums
-  float* gpc = gps + 4 * NB;                                       // [4][NB] compensations
-  float* gacc = gpc + 4 * NB;  // G lower triangle, entry (i, j <= i) at i (i + 1) / 2 + j
+  float* gps = reinterpret_cast<float*>(tiles + 2 * C::kBufBytes);  // [kQ][NB] partial sums
+  float* gpc = gps + C::kQ * NB;                                     // [kQ][NB] compensations
+  float* gacc = gpc + C::kQ * NB;  // G lower triangle, entry (i, j <= i) at i (i + 1) / 2 + j
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int a = tid & (NB - 1), kq = tid >> 6;  // staging: member a, observation quads kq, kq+4
+  // staging: member a, observation quads kq, kq + kQ, ...
+  const int a = tid & (NB - 1), kq = tid / NB;
   const uint32_t mbar0 = smem_u32(&ts.mbar[0]);
 
   if (tid == 0) {
@@ -229,27 +253,45 @@ __global__ void __launch_bounds__(kThreads, 4)
   };
 
   // add the tensor-memory accumulator into gacc (all MMAs complete and published by a barrier).
-  // Warp w reads lanes 32 (w % 4) .. + 31 (rows of D) and column half w / 4 of both column
-  // blocks; G(i, j) = (D(i, j) + D(i, j + 64)) + (D(i + 64, j) + D(i + 64, j + 64)). The rows of
-  // the lo parts are added first, then those of the hi parts, so the sums are deterministic.
+  // Warp w reads lanes 32 (w % 4) .. + 31 (rows of D).
+  // NB = 64: column half w / 4 of both column blocks; G(i, j) = (D(i, j) + D(i, j + 64)) +
+  //   (D(i + 64, j) + D(i + 64, j + 64)); the rows of the lo parts are added first, then those
+  //   of the hi parts, so the sums are deterministic.
+  // NB = 128: D is G; warp w adds columns 64 (w / 4) .. + 63 of its rows (lower triangle).
   auto flush = [&]() {
     fence_after();
     const int q = warp & 3, h = warp >> 2;
     const int i = (32 * q + lane) & (NB - 1);
     const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16);
     float* gi = gacc + i * (i + 1) / 2;
+    if constexpr (NB == 64) {
 #pragma unroll
-    for (int phase = 0; phase < 2; phase++) {
-      if ((q >> 1) == 1 - phase) {
+      for (int phase = 0; phase < 2; phase++) {
+        if ((q >> 1) == 1 - phase) {
 #pragma unroll
-        for (int s = 0; s < 4; s++) {
-          const int c0 = 32 * h + 8 * s;
-          float v0[8], v1[8];
-          tmem_ld8(ta + c0, v0);
-          tmem_ld8(ta + 64 + c0, v1);
+          for (int s = 0; s < 4; s++) {
+            const int c0 = 32 * h + 8 * s;
+            float v0[8], v1[8];
+            tmem_ld8(ta + c0, v0);
+            tmem_ld8(ta + 64 + c0, v1);
+#pragma unroll
+            for (int t = 0; t < 8; t++)
+              if (c0 + t <= i) gi[c0 + t] += v0[t] + v1[t];
+          }
+        }
+        fence_before();
+        __syncthreads();
+      }
+    } else {
+      if (64 * h <= 32 * q + 31) {  // warp-uniform: the block has lower-triangle entries
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+          const int c0 = 64 * h + 8 * s;
+          float v[8];
+          tmem_ld8(ta + c0, v);
 #pragma unroll
           for (int t = 0; t < 8; t++)
-            if (c0 + t <= i) gi[c0 + t] += v0[t] + v1[t];
+            if (c0 + t <= i) gi[c0 + t] += v[t];
         }
       }
       fence_before();
@@ -271,7 +313,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     const float iL32 = (float)(1.0 / L);
     const float r_lo = (float)Rmax * (1.f - 1e-6f), r_hi = (float)Rmax * (1.f + 1e-6f);
     if (tid == 0) ts.nrel = 0;
-    for (int e = tid; e < kTri; e += kThreads) gacc[e] = 0.f;
+    for (int e = tid; e < C::kTri; e += kThreads) gacc[e] = 0.f;
     int head = 0, tail = 0, ntile = 0, ctile = 0, nrel_local = 0;
     float gsum = 0.f, gcmp = 0.f;
 
@@ -295,10 +337,14 @@ __global__ void __launch_bounds__(kThreads, 4)
         abort = true;
         return;
       }
-      unsigned char* tb = tiles + b * kTileBytes;
+      unsigned char* tb = tiles + b * C::kBufBytes;
+      // hi parts: rows 0..NB-1 of the first operand tile; lo parts: rows 64..127 of the same
+      // tile (NB = 64) or the second tile (NB = 128)
+      unsigned char* tlo = (NB == 64) ? tb : tb + kOpBytes;
+      const int rlo = (NB == 64) ? a + 64 : a;
 #pragma unroll
-      for (int pass = 0; pass < 2; pass++) {
-        const int quad = kq + 4 * pass;
+      for (int pass = 0; pass < C::kPasses; pass++) {
+        const int quad = kq + C::kQ * pass;
         uint32_t hi[4], lo[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -316,17 +362,27 @@ __global__ void __launch_bounds__(kThreads, 4)
           kahan_add(gsum, gcmp, X * y);
         }
         *reinterpret_cast<uint4*>(tb + tile_off(a, quad)) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(tb + tile_off(a + NB, quad)) =
+        *reinterpret_cast<uint4*>(tlo + tile_off(rlo, quad)) =
             make_uint4(lo[0], lo[1], lo[2], lo[3]);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();  // tile complete
       if (tid == 0) {
         fence_after();
-        const uint32_t base = tile_addr + b * kTileBytes;
+        const uint32_t base = tile_addr + b * C::kBufBytes;
 #pragma unroll
-        for (int kk = 0; kk < KT / 8; kk++)
-          mma_tf32(tmem, make_desc(base + kk * 32), (ctile > 0 || kk > 0) ? 1u : 0u);
+        for (int kk = 0; kk < KT / 8; kk++) {
+          const uint32_t acc = (ctile > 0 || kk > 0) ? 1u : 0u;
+          const uint64_t dh = make_desc(base + kk * 32);
+          if constexpr (NB == 64) {
+            mma_tf32(tmem, dh, dh, acc);
+          } else {
+            const uint64_t dl = make_desc(base + kOpBytes + kk * 32);
+            mma_tf32(tmem, dh, dh, acc);
+            mma_tf32(tmem, dh, dl, 1u);
+            mma_tf32(tmem, dl, dh, 1u);
+          }
+        }
         mma_commit(mbar0 + 8 * b);
       }
       if (b)
@@ -479,7 +535,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         // compensated combination of the four partial sums of member tid
         float s = 0.f, cmp = 0.f;
 #pragma unroll
-        for (int p = 0; p < 4; p++) {
+        for (int p = 0; p < C::kQ; p++) {
           kahan_add(s, cmp, gps[p * NB + tid]);
           kahan_add(s, cmp, -gpc[p * NB + tid]);
         }
@@ -500,35 +556,49 @@ __global__ void __launch_bounds__(kThreads, 4)
                  "r"(kTmemCols));
 }
 
+template <int NB>
+cudaError_t launch_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
+                           int32_t z0, int32_t nzc, const double* zone_xyzt,
+                           const double* corr_len, const double* max_len, float* d_G,
+                           float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                           int32_t* d_err, cudaStream_t st) {
+  using C = TcCfg<NB>;
+  cudaError_t e = cudaFuncSetAttribute(k_zone_gram_tc<NB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)C::kDynSmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_zone_gram_tc<NB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  // the shared-memory size admits at most kCtas CTAs per SM (kCtas x 128 TMEM columns <= 512)
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = sms * C::kCtas;
+  if (grid > nzc) grid = nzc > 0 ? nzc : 1;
+  e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  k_zone_gram_tc<NB><<<grid, kThreads, C::kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt,
+                                                          corr_len, max_len, d_G, d_g, d_nobs,
+                                                          brute, d_work, d_err);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
-int gram_tc_max_n() { return NB; }
+int gram_tc_max_n() { return 128; }
 
 cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                          int32_t nzc, const double* zone_xyzt, const double* corr_len,
                          const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
                          int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st) {
-  if (N < 1 || N > NB || !so.HSt32 || !so.r32 || !so.innov32) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_zone_gram_tc,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kDynSmem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_zone_gram_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           (int)cudaSharedmemCarveoutMaxShared);
-  if (e != cudaSuccess) return e;
-  const int bps = 4;  // the shared-memory size admits at most 4 CTAs (4 x 128 TMEM columns)
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int grid = sms * bps;
-  if (grid > nzc) grid = nzc > 0 ? nzc : 1;
-  e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
-  if (e != cudaSuccess) return e;
-  k_zone_gram_tc<<<grid, kThreads, kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
-                                                   max_len, d_G, d_g, d_nobs, brute, d_work,
-                                                   d_err);
-  count_launches(1);
-  return cudaGetLastError();
+  if (N < 1 || N > 128 || !so.HSt32 || !so.r32 || !so.innov32) return cudaErrorInvalidValue;
+  if (N <= 64)
+    return launch_gram_tc<64>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len, d_G, d_g,
+                              d_nobs, brute, d_work, d_err, st);
+  return launch_gram_tc<128>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len, d_G, d_g,
+                             d_nobs, brute, d_work, d_err, st);
 }
 
 }  // namespace oakg
