@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-global", action="store_true")
     p.add_argument("--no-graph", action="store_true")
+    p.add_argument("--batched-scale", type=float, default=0.25,
+                   help="horizontal scale of the 5-variable N = 100 batched workload "
+                        "(0 skips it)")
     return p.parse_args()
 
 
@@ -419,6 +422,59 @@ def main():
             glob["cpu_ms_per_analysis"] = (time.perf_counter() - t0) / 10 * 1e3
             glob["cpu_kind"] = "port (oracle/oakref.c, LAPACK dsyev)"
 
+    # the 5-variable batched workload (720 x 360 columns of 121 elements scaled by
+    # --batched-scale, N = 100, bilinear observations on track segments): both forms on the
+    # same device inputs, the mixed form's errors against the FP64 form's outputs
+    batched = None
+    if args.batched_scale > 0:
+        from oak_gb300.workloads import batched_case
+        cb = batched_case(scale=args.batched_scale)
+        bd = (T(cb.zone_size), T(cb.xf), T(cb.Hxf), T(cb.yo), F(cb.Sf), F(cb.HSf),
+              T(cb.r_diag), T(cb.zone_pos), tuple(T(x) for x in cb.obs_pos), T(cb.corr_len),
+              T(cb.max_len))
+
+        def bstep(prec):
+            return oak_gb300.loc_analysis(*bd, weight=cb.weight, metric=cb.metric,
+                                          loctype=cb.loctype, want_ampl=False, precision=prec)
+
+        def btime(prec):
+            for _ in range(args.warmup):
+                o = bstep(prec)
+            st = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
+            barrier()
+            torch.cuda.synchronize(dev)
+            b0 = torch.cuda.Event(enable_timing=True)
+            b1 = torch.cuda.Event(enable_timing=True)
+            b0.record(stream)
+            for _ in range(args.steps):
+                o = bstep(prec)
+                for k, v in oak_gb300.last_timings().items():
+                    st[k] += v
+            b1.record(stream)
+            torch.cuda.synchronize(dev)
+            barrier()
+            return o, b0.elapsed_time(b1) / args.steps, {k: v / args.steps for k, v in st.items()}
+
+        o64, bms64, bst64 = btime(oak_gb300.PREC_FP64)
+        xa64, Sa64 = o64[0].clone(), o64[1].clone()
+        bnobs = o64[3].cpu().numpy()
+        del o64
+        om, bmsm, bstm = btime(oak_gb300.PREC_MIXED)
+        be_mean = float(torch.linalg.norm(om[0] - xa64) / torch.linalg.norm(xa64 - bd[1]))
+        be_anom = float(torch.linalg.norm(om[1] - Sa64) / torch.linalg.norm(Sa64))
+        batched = {"workload": cb.name, "scale": args.batched_scale, "zones": int(cb.Z),
+                   "N": int(cb.N), "m": int(cb.m), "obs_per_zone_max": int(bnobs.max()),
+                   "obs_per_zone_mean": float(bnobs.mean()),
+                   "fp64": {"value": ws * cb.Z / (bms64 / 1e3), "unit": UNIT,
+                            "ms_per_step": bms64, "stage_ms_per_step": bst64},
+                   "mixed": {"value": ws * cb.Z / (bmsm / 1e3), "unit": UNIT,
+                             "ms_per_step": bmsm, "stage_ms_per_step": bstm},
+                   "speedup_vs_fp64": bms64 / bmsm, "rel_err_mean_increment": be_mean,
+                   "rel_err_anomalies": be_anom,
+                   "note": "errors of the mixed form against the FP64 form on the GPU (which "
+                           "matches the oracle to 1e-10); state stored in FP64 at the boundary"}
+        del om, xa64, Sa64, bd, cb
+
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
     if not args.no_e2e:
@@ -477,6 +533,7 @@ def main():
                                                      "zones_with_obs": int((nobs > 0).sum())},
         "e2e": e2e,
         "mixed": mixed,
+        "batched": batched,
         "adjoint": adjoint,
         "global_analysis": glob,
         "graph": graph,
