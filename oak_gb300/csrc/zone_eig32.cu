@@ -81,10 +81,11 @@ __device__ __forceinline__ void owner_reflector(const float (&row)[L], int k, in
   // element would become a dynamic index and move the row to local memory
   vstore(row, vbuf);
   const float x0 = vbuf[k + 1], dk = vbuf[k];
-  float sig = 0.f;
+  float sg[4] = {0.f, 0.f, 0.f, 0.f};  // four chains: the other threads wait on this sum
 #pragma unroll
   for (int c = 0; c < L; c++)
-    if (c > k + 1) sig = fmaf(row[c], row[c], sig);
+    if (c > k + 1) sg[c & 3] = fmaf(row[c], row[c], sg[c & 3]);
+  const float sig = (sg[0] + sg[1]) + (sg[2] + sg[3]);
   const float mu = sqrtf(fmaf(x0, x0, sig));
   const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
   const float vv = fmaf(v0, v0, sig);
@@ -841,38 +842,41 @@ __global__ void __launch_bounds__(kT2)
 // One block of 64 threads per zone, thread j = eigenpair j: inverse iteration on Tri - shift_j I
 // (two solves from a fixed pseudo-random start, as the generic E2b). The partial-pivoting LU
 // is recomputed in each forward sweep (fused with the elimination), its upper factor kept in
-// shared memory; the iterate lives in registers (loops unrolled to 64).
+// shared memory; the iterate lives in registers (loops unrolled to NV, the padded length).
+// Pivots are at least eps ||Tri||_1 in magnitude, so their reciprocals use the fast
+// approximate division (a few ulp: inverse iteration only needs the direction).
+template <int NV>
 __global__ void __launch_bounds__(kT2)
     k_eig_vectors32(int N, int32_t nzc, const float* __restrict__ aux, float* __restrict__ Zg,
                     const int32_t* __restrict__ nobs) {
-  __shared__ float sfac[3 * NB * kT2];  // upper factor u1, u2, 1/diag: [i][j] each
-  __shared__ float sd[NB], se[NB];
+  extern __shared__ __align__(16) float sfac[];  // upper factor u1, u2, 1/diag: [i][jl] each
+  __shared__ float sd[NV], se[NV];
   float* su1 = sfac;
-  float* su2 = sfac + NB * kT2;
-  float* sui = sfac + 2 * NB * kT2;
-  const int j = threadIdx.x;
+  float* su2 = sfac + NV * kT2;
+  float* sui = sfac + 2 * NV * kT2;
+  const int jl = threadIdx.x, j = kT2 * blockIdx.y + jl;  // eigenpair j of this block's kT2
   const int32_t zl = blockIdx.x;
   if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
   const float* ax = aux + (int64_t)zl * aux_stride32(N);
-  if (j < N) {
-    sd[j] = ax[j];
-    se[j] = (j < N - 1) ? ax[N + j] : 0.f;
+  for (int i = jl; i < N; i += kT2) {
+    sd[i] = ax[i];
+    se[i] = (i < N - 1) ? ax[N + i] : 0.f;
   }
   __syncthreads();
   const float onenrm = ax[5 * N + 1];
   float* Zz = Zg + (int64_t)zl * N * N;
-  float* tr = sfac;  // [i][NB + 1] transpose staging, used at the end
-  float x[NB];
+  float* tr = sfac;  // [i][kT2 + 1] transpose staging, used at the end
+  float x[NV];
 #pragma unroll
-  for (int i = 0; i < NB; i++) x[i] = 0.f;
+  for (int i = 0; i < NV; i++) x[i] = 0.f;
   if (!(onenrm > 1e4f * 1e-36f)) {  // Tri = 0: every vector is an eigenvector
 #pragma unroll
-    for (int i = 0; i < NB; i++) x[i] = (i == j) ? 1.f : 0.f;
+    for (int i = 0; i < NV; i++) x[i] = (i == j) ? 1.f : 0.f;
   } else if (j < N) {
     const float l = ax[4 * N + j];
     const float tiny = 5.9604645e-8f * onenrm;
 #pragma unroll
-    for (int i = 0; i < NB; i++) {
+    for (int i = 0; i < NV; i++) {
       unsigned h = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
       h ^= h >> 15;
       h *= 2246822519u;
@@ -883,18 +887,18 @@ __global__ void __launch_bounds__(kT2)
     for (int it = 0; it < 2; it++) {
       float cd = sd[0] - l, csup = (N > 1) ? se[0] : 0.f;
 #pragma unroll
-      for (int i = 0; i < NB - 1; i++) {
+      for (int i = 0; i < NV - 1; i++) {
         if (i < N - 1) {
           const float sub = se[i], dg = sd[i + 1] - l, sp = (i + 1 < N - 1) ? se[i + 1] : 0.f;
           const bool swap = fabsf(cd) < fabsf(sub);
           float pivot = swap ? sub : cd;
           if (!swap && fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
-          const float ui = 1.f / pivot;
+          const float ui = __fdividef(1.f, pivot);  // |pivot| >= tiny > 0
           const float li = (swap ? cd : sub) * ui;
           if (it == 0) {
-            su1[i * kT2 + j] = swap ? dg : csup;
-            su2[i * kT2 + j] = swap ? sp : 0.f;
-            sui[i * kT2 + j] = ui;
+            su1[i * kT2 + jl] = swap ? dg : csup;
+            su2[i * kT2 + jl] = swap ? sp : 0.f;
+            sui[i * kT2 + jl] = ui;
           }
           const float aa = swap ? csup : dg, bb = swap ? dg : csup;
           cd = fmaf(-li, bb, aa);
@@ -907,43 +911,46 @@ __global__ void __launch_bounds__(kT2)
       if (it == 0) {
         float pivot = cd;
         if (fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
-        sui[(N - 1) * kT2 + j] = 1.f / pivot;
-        su1[(N - 1) * kT2 + j] = 0.f;
-        su2[(N - 1) * kT2 + j] = 0.f;
-        if (N >= 2) su2[(N - 2) * kT2 + j] = 0.f;
+        sui[(N - 1) * kT2 + jl] = __fdividef(1.f, pivot);
+        su1[(N - 1) * kT2 + jl] = 0.f;
+        su2[(N - 1) * kT2 + jl] = 0.f;
+        if (N >= 2) su2[(N - 2) * kT2 + jl] = 0.f;
       }
       // back substitution with the upper factor (diagonal + two super-diagonals)
 #pragma unroll
-      for (int i = NB - 1; i >= 0; i--) {
+      for (int i = NV - 1; i >= 0; i--) {
         if (i < N) {
           float v = x[i];
-          if (i + 1 < NB) v = fmaf(-su1[i * kT2 + j], x[i + 1], v);
-          if (i + 2 < NB) v = fmaf(-su2[i * kT2 + j], x[i + 2], v);
-          x[i] = v * sui[i * kT2 + j];
+          if (i + 1 < NV) v = fmaf(-su1[i * kT2 + jl], x[i + 1], v);
+          if (i + 2 < NV) v = fmaf(-su2[i * kT2 + jl], x[i + 2], v);
+          x[i] = v * sui[i * kT2 + jl];
         }
       }
       float mx = 0.f;
 #pragma unroll
-      for (int i = 0; i < NB; i++) mx = fmaxf(mx, fabsf(x[i]));
+      for (int i = 0; i < NV; i++) mx = fmaxf(mx, fabsf(x[i]));
       const float im = 1.f / mx;
-      float nrm = 0.f;
+      float nr[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int i = 0; i < NB; i++) {
+      for (int i = 0; i < NV; i++) {
         x[i] *= im;
-        nrm = fmaf(x[i], x[i], nrm);
+        nr[i & 3] = fmaf(x[i], x[i], nr[i & 3]);
       }
-      const float sc = rsqrtf(nrm);
+      const float sc = rsqrtf((nr[0] + nr[1]) + (nr[2] + nr[3]));
 #pragma unroll
-      for (int i = 0; i < NB; i++) x[i] *= sc;
+      for (int i = 0; i < NV; i++) x[i] *= sc;
     }
   }
   __syncthreads();  // factors no longer read: reuse su1/su2 as the transpose buffer
 #pragma unroll
-  for (int i = 0; i < NB; i++) tr[i * (NB + 1) + j] = x[i];
+  for (int i = 0; i < NV; i++) tr[i * (kT2 + 1) + jl] = x[i];
   __syncthreads();
-  for (int idx = j; idx < N * N; idx += kT2) {
+  // this block's vectors kT2 * blockIdx.y + jj (rows of Z), coalesced along the rows
+  const int j0 = kT2 * blockIdx.y;
+  const int nv = (N - j0 < kT2) ? N - j0 : kT2;
+  for (int idx = jl; idx < nv * N; idx += kT2) {
     const int jj = idx / N, i = idx - jj * N;
-    Zz[idx] = tr[i * (NB + 1) + jj];
+    Zz[(int64_t)(j0 + jj) * N + i] = tr[i * (kT2 + 1) + jj];
   }
 }
 
@@ -1009,7 +1016,7 @@ __global__ void __launch_bounds__(NB2, 3)
     if (t < N) Gz[(int64_t)k * N + t] = vr;  // reflector k, vector-major, zero padded
     if (bk == 0.f) continue;                 // block-uniform; an identity reflector
     const bool act = t > k;
-    float p0 = 0.f, p1 = 0.f;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
     if (act) {
 #pragma unroll
       for (int g = 0; g < NB2 / 16; g++) {
@@ -1020,13 +1027,13 @@ __global__ void __launch_bounds__(NB2, 3)
             const float4 v4 = *reinterpret_cast<const float4*>(vb + c);
             p0 = fmaf(a[c + 0], v4.x, p0);
             p1 = fmaf(a[c + 1], v4.y, p1);
-            p0 = fmaf(a[c + 2], v4.z, p0);
-            p1 = fmaf(a[c + 3], v4.w, p1);
+            p2 = fmaf(a[c + 2], v4.z, p2);
+            p3 = fmaf(a[c + 3], v4.w, p3);
           }
         }
       }
     }
-    const float p = bk * (p0 + p1);
+    const float p = bk * ((p0 + p1) + (p2 + p3));
     pb[t] = p;
     const float pv = wsum(p * vr);
     if (lane == 0) red[b][warp] = pv;
@@ -1083,7 +1090,7 @@ constexpr size_t kSmem128 = sizeof(Zone128);
 
 // x . u over the 16-component groups g0 <= g < ng
 __device__ __forceinline__ float vdot128(const float (&x)[NB2], const float* u, int g0, int ng) {
-  float s0 = 0.f, s1 = 0.f;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll
   for (int g = 0; g < NB2 / 16; g++) {
     if (g >= g0 && g < ng) {
@@ -1093,12 +1100,12 @@ __device__ __forceinline__ float vdot128(const float (&x)[NB2], const float* u, 
         const float4 v = *reinterpret_cast<const float4*>(u + c);
         s0 = fmaf(x[c], v.x, s0);
         s1 = fmaf(x[c + 1], v.y, s1);
-        s0 = fmaf(x[c + 2], v.z, s0);
-        s1 = fmaf(x[c + 3], v.w, s1);
+        s2 = fmaf(x[c + 2], v.z, s2);
+        s3 = fmaf(x[c + 3], v.w, s3);
       }
     }
   }
-  return s0 + s1;
+  return (s0 + s1) + (s2 + s3);
 }
 
 // x -= f u over the groups g0 <= g < ng
@@ -1156,13 +1163,15 @@ __global__ void __launch_bounds__(NB2, 3)
   // acceptance test and residual-keeping of k_eig_transform32
   for (int c = N - 1; c >= 0; c--) {
     if (t == c) {
-      float s0 = 0.f, s1 = 0.f;
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll
-      for (int i = 0; i < NB2; i += 2) {
+      for (int i = 0; i < NB2; i += 4) {
         s0 = fmaf(x[i], x[i], s0);
         s1 = fmaf(x[i + 1], x[i + 1], s1);
+        s2 = fmaf(x[i + 2], x[i + 2], s2);
+        s3 = fmaf(x[i + 3], x[i + 3], s3);
       }
-      const float s = s0 + s1;
+      const float s = (s0 + s1) + (s2 + s3);
       const bool ok = s >= 0.5f;
       const float sc = ok ? rsqrtf(s) : 1.f;  // a collapsed vector keeps its residual
 #pragma unroll
@@ -1400,7 +1409,12 @@ cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs
 cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
                           const int32_t* d_nobs, cudaStream_t st) {
   if (N < 2 || N > NB) return cudaErrorInvalidValue;
-  k_eig_vectors32<<<nzc > 0 ? nzc : 1, kT2, 0, st>>>(N, nzc, d_aux, d_Z, d_nobs);
+  const size_t smem = (size_t)3 * NB * kT2 * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_eig_vectors32<NB><<<dim3(nzc > 0 ? nzc : 1, 1), kT2, smem, st>>>(N, nzc, d_aux, d_Z,
+                                                                     d_nobs);
   return cudaGetLastError();
 }
 

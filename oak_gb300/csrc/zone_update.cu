@@ -119,9 +119,19 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();  // previous zone's shared data consumed
     const float* Tz = T + (int64_t)zl * N * N;
     if (Sa) {
-      for (int idx = threadIdx.x; idx < N * NP; idx += kThreads) {
-        const int k = idx / NP, c = idx - k * NP;
-        Ts[idx] = (c < N) ? Tz[k * N + c] : 0.f;
+      if ((N & 3) == 0) {  // rows of T start on 16-byte boundaries: 128-bit loads
+        const int nq = NP >> 2;
+        const float4* Tz4 = reinterpret_cast<const float4*>(Tz);
+        float4* Ts4 = reinterpret_cast<float4*>(Ts);
+        for (int idx = threadIdx.x; idx < N * nq; idx += kThreads) {
+          const int k = idx / nq, c4 = idx - k * nq;
+          Ts4[idx] = (4 * c4 < N) ? Tz4[(k * N >> 2) + c4] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      } else {
+        for (int idx = threadIdx.x; idx < N * NP; idx += kThreads) {
+          const int k = idx / NP, c = idx - k * NP;
+          Ts[idx] = (c < N) ? Tz[k * N + c] : 0.f;
+        }
       }
     }
     for (int idx = threadIdx.x; idx < N; idx += kThreads) as[idx] = ampl[(int64_t)zl * N + idx];
