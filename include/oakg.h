@@ -69,12 +69,11 @@ extern "C" {
 #define OAKG_METRIC_SPHERICAL_APPROX 2
 
 /* precision of the local analysis */
-#define OAKG_PREC_FP64 0  /* every product in FP64 (the plain form); N <= 112, as for the
-                             global analysis and the adjoint                              */
+#define OAKG_PREC_FP64 0  /* every product in FP64 (the plain form)                     */
 #define OAKG_PREC_MIXED 1 /* FP64 selection and (1+lambda)^-1/2, (1+lambda)^-1 scalings;
                              Gram (tensor cores, chunked FP32 accumulation), eigensolve and
-                             update in FP32, compensated innovation sums; N <= 128
-                             (relative analysis error ~1e-5)                               */
+                             update in FP32, compensated innovation sums
+                             (relative analysis error ~1e-5). Both forms take N <= 128.    */
 
 /* oakg_loc.flags */
 #define OAKG_FLAG_AMPL_ALWAYS 1 /* write amplitudes for every analysed zone (the reference

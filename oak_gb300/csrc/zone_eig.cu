@@ -397,12 +397,15 @@ __global__ void __launch_bounds__(kThreads)
     k_eig_transform(int N, int32_t nzc, R* __restrict__ GT, const R* __restrict__ aux,
                     const R* __restrict__ Zg, const R* __restrict__ gv,
                     const int32_t* __restrict__ nobs, int rotate, R* __restrict__ ampl_out,
-                    int32_t* __restrict__ status, int32_t* __restrict__ work) {
+                    int32_t* __restrict__ status, int32_t* __restrict__ work, int a_global) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   R* dyn = reinterpret_cast<R*>(dyn_raw);
   const int ld = N + 1;
-  R* A = dyn;           // [N][ld] reflectors, then T_sym
-  R* U = A + N * ld;    // [N][ld] Z, then U
+  // A: [N][ld] reflectors, then T_sym. When two N x N matrices do not fit in shared memory
+  // (a_global), A is the zone's own slot of GT ([N][N]: the reflectors E1 left there, then
+  // T_sym), read and written only between block barriers
+  R* A = dyn;
+  R* U = a_global ? dyn : A + N * ld;  // [N][ld] Z, then U
   R* lam = U + N * ld;  // [N] 1/(1+lambda)         (evaluated in FP64)
   R* sq = lam + N;      // [N] sqrt(1/(1+lambda))   (evaluated in FP64)
   R* g = sq + N;        // [N]
@@ -427,9 +430,11 @@ __global__ void __launch_bounds__(kThreads)
     R* Gz = GT + (int64_t)zl * N * N;
     const R* ax = aux + (int64_t)zl * aux_stride(N);
     const R* Z = Zg + (int64_t)zl * N * N;
+    R* Aw = a_global ? Gz : A;
+    const int la = a_global ? N : ld;
     for (int idx = tid; idx < N * N; idx += kThreads) {
       int i = idx / N, j = idx - i * N;
-      A[i * ld + j] = (i > j) ? Gz[idx] : R(0);
+      if (!a_global) A[i * ld + j] = (i > j) ? Gz[idx] : R(0);
       U[j * ld + i] = Z[idx];  // Z[i*N + j] = component j of eigenvector i -> U[j][i]
     }
     for (int i = tid; i < N; i += kThreads) {
@@ -542,14 +547,14 @@ __global__ void __launch_bounds__(kThreads)
       const int L = N - k - 1;
       for (int j = tid; j < N; j += kThreads) {
         R s = 0;
-        for (int i = 0; i < L; i++) s = fma(A[(k + 1 + i) * ld + k], U[(k + 1 + i) * ld + j], s);
+        for (int i = 0; i < L; i++) s = fma(Aw[(k + 1 + i) * la + k], U[(k + 1 + i) * ld + j], s);
         t0[j] = bk * s;
       }
       __syncthreads();
       for (int idx = tid; idx < L * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
         R* u = U + (k + 1 + i) * ld + j;
-        *u = fma(-A[(k + 1 + i) * ld + k], t0[j], *u);
+        *u = fma(-Aw[(k + 1 + i) * la + k], t0[j], *u);
       }
       __syncthreads();
     }
@@ -606,8 +611,8 @@ __global__ void __launch_bounds__(kThreads)
       const R* qb = U + b * ld;
       R s = 0;
       for (int k = 0; k < N; k++) s = fma(qa[k], qb[k], s);
-      A[a * ld + b] = s;
-      A[b * ld + a] = s;
+      Aw[a * la + b] = s;
+      Aw[b * la + a] = s;
     }
     __syncthreads();
     if (rotate) {
@@ -618,7 +623,7 @@ __global__ void __launch_bounds__(kThreads)
       const R cw = R(1) + wv;
       // t0 = T_sym u_v, t1 = T_sym v
       for (int i = tid; i < N; i += kThreads) {
-        const R* ti = A + i * ld;
+        const R* ti = Aw + i * la;
         R sa = 0, sb = 0;
         for (int j = 0; j < N; j++) {
           sa = fma(ti[j], vv[j] + ((j == N - 1) ? sv : R(0)), sa);
@@ -633,12 +638,12 @@ __global__ void __launch_bounds__(kThreads)
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
         R uj = vv[j] + ((j == N - 1) ? sv : R(0));
-        A[i * ld + j] = fma(-t0[i] * icv, uj, A[i * ld + j]);
+        Aw[i * la + j] = fma(-t0[i] * icv, uj, Aw[i * la + j]);
       }
       __syncthreads();
       // g <- T1 u_w (g is no longer needed)
       for (int i = tid; i < N; i += kThreads) {
-        const R* ti = A + i * ld;
+        const R* ti = Aw + i * la;
         R s = 0;
         for (int j = 0; j < N; j++) s = fma(ti[j], wv + ((j == N - 1) ? R(1) : R(0)), s);
         g[i] = s * icw;
@@ -649,14 +654,14 @@ __global__ void __launch_bounds__(kThreads)
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
         R uj = wv + ((j == N - 1) ? R(1) : R(0));
-        R t = fma(-g[i], uj, A[i * ld + j]);
+        R t = fma(-g[i], uj, Aw[i * la + j]);
         if (extra != R(0)) t = fma(extra * t1[i], wv, t);
         Gz[idx] = t;
       }
     } else {
       for (int idx = tid; idx < N * N; idx += kThreads) {
         int i = idx / N, j = idx - i * N;
-        Gz[idx] = A[i * ld + j];
+        Gz[idx] = Aw[i * la + j];
       }
     }
     if (tid == 0 && nan_flag) status[zl] |= ZST_NAN;
@@ -692,13 +697,19 @@ template <typename R>
 cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z, const R* d_g,
                       const int32_t* d_nobs, int rotate, R* d_ampl, int32_t* d_status,
                       int32_t* d_work, cudaStream_t st) {
+  // two N x N matrices in shared memory when they fit (227 KB a block), else one (A in GT)
   size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
+  int a_global = 0;
+  if (smem3 > (size_t)227 * 1024) {
+    smem3 = (size_t)(N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
+    a_global = 1;
+  }
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<R>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
   if (e != cudaSuccess) return e;
   k_eig_transform<R><<<grid_for_smem((const void*)k_eig_transform<R>, smem3, nzc), kThreads,
                        smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl,
-                                    d_status, d_work);
+                                    d_status, d_work, a_global);
   return cudaSuccess;
 }
 
@@ -737,7 +748,7 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
   if (e != cudaSuccess) return e;
   k_eig_transform<float><<<grid_for_smem((const void*)k_eig_transform<float>, smem3, nzc),
                            kThreads, smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate,
-                                                  d_ampl, d_status, d_work);
+                                                  d_ampl, d_status, d_work, 0);
   return cudaSuccess;
 }
 

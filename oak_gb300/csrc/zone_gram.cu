@@ -393,7 +393,7 @@ cudaError_t launch_global(int64_t m, int N, const double* HSf, int64_t ldH, cons
 
 }  // namespace
 
-int max_fp64_ensemble() { return 112; }
+int max_fp64_ensemble() { return 128; }
 int max_ensemble() { return 128; }
 
 // Per-thread entry count classes: ceil((N(N+1)/2 + N) / 256).

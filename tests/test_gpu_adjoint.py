@@ -48,10 +48,10 @@ def _forward(oakg, P, yo, r, kappa=1.0, s=1.0):
     return xa
 
 
-@pytest.mark.parametrize("kind", [0, 1])
-def test_adjoint_matches_reference_gradient(oakg, kind):
+@pytest.mark.parametrize("kind,N", [(0, 16), (1, 16), (1, 128)])
+def test_adjoint_matches_reference_gradient(oakg, kind, N):
     import torch
-    P = _problem(kind=kind)
+    P = _problem(kind=kind, N=N)
     s = 1.05
     xa = _forward(oakg, P, P["yo"], P["r"], 1.0, s)
     _, seed = _J_and_seed(xa, P)

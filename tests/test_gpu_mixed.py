@@ -108,17 +108,11 @@ def test_mixed_batched_bilinear_case(oakg):
 
 
 def test_ensemble_size_limits(oakg):
-    """N <= 128 in the mixed form, N <= 112 in the FP64 form (with a message naming the
-    mixed form)."""
-    c = local_case(scale=1 / 16, N=113, m=300)
-    args = (c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag, c.zone_pos, c.obs_pos,
-            c.corr_len, c.max_len)
-    with pytest.raises(oakg.OakError) as ei:
-        oakg.loc_analysis(*args, weight=c.weight, precision=oakg.PREC_FP64)
-    assert "OAKG_PREC_MIXED" in str(ei.value)
-    oakg.loc_analysis(*args, weight=c.weight, precision=oakg.PREC_MIXED)
+    """Both forms take N <= 128; N = 129 is rejected with an argument error."""
     c = local_case(scale=1 / 16, N=129, m=300)
-    with pytest.raises(oakg.OakError):
-        oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag, c.zone_pos,
-                          c.obs_pos, c.corr_len, c.max_len, weight=c.weight,
-                          precision=oakg.PREC_MIXED)
+    for prec in (oakg.PREC_FP64, oakg.PREC_MIXED):
+        with pytest.raises(oakg.OakError) as ei:
+            oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                              c.zone_pos, c.obs_pos, c.corr_len, c.max_len, weight=c.weight,
+                              precision=prec)
+        assert ei.value.code == oakg.ERR_ARGS and "128" in str(ei.value)

@@ -137,7 +137,7 @@ def test_random_local_matches_oracle(oakg, metric, loctype, kind):
         check_local(xa, Sa, xa_o, Sa_o, P["xf"])
 
 
-@pytest.mark.parametrize("N", [2, 7, 30, 64, 100])
+@pytest.mark.parametrize("N", [2, 7, 30, 64, 100, 113, 128])
 def test_ensemble_sizes(oakg, N):
     P = _random_local(100 + N, N=N, nzones=40, m=250, ragged=True)
     (xa, Sa, _, nobs), (xa_o, Sa_o, nobs_o) = _run_both(oakg, P)
