@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--batched-scale", type=float, default=0.25,
                    help="horizontal scale of the 5-variable N = 100 batched workload "
                         "(0 skips it)")
+    p.add_argument("--large-scale", type=float, default=0.125,
+                   help="horizontal scale of the 2-variable N = 128 large workload "
+                        "(0 skips it)")
     return p.parse_args()
 
 
@@ -422,13 +425,14 @@ def main():
             glob["cpu_ms_per_analysis"] = (time.perf_counter() - t0) / 10 * 1e3
             glob["cpu_kind"] = "port (oracle/oakref.c, LAPACK dsyev)"
 
-    # the 5-variable batched workload (720 x 360 columns of 121 elements scaled by
-    # --batched-scale, N = 100, bilinear observations on track segments): both forms on the
-    # same device inputs, the mixed form's errors against the FP64 form's outputs
-    batched = None
-    if args.batched_scale > 0:
-        from oak_gb300.workloads import batched_case
-        cb = batched_case(scale=args.batched_scale)
+    # column workloads of the mixed-precision configurations, both forms on the same device
+    # inputs, the mixed form's errors against the FP64 form's outputs:
+    #   batched: 5 variables on 720 x 360 columns of 121 elements, N = 100, bilinear
+    #            observations on track segments (--batched-scale of the grid);
+    #   large:   2 variables on 1440 x 720 columns of 100 elements, N = 128, 1M clustered
+    #            observations (--large-scale of the grid), with the adjoint of J = mean over a
+    #            200 x 200 column sub-region (scaled with the grid) of (xa - x_true)^2
+    def two_forms(cb, scale, adjoint_sub=None):
         bd = (T(cb.zone_size), T(cb.xf), T(cb.Hxf), T(cb.yo), F(cb.Sf), F(cb.HSf),
               T(cb.r_diag), T(cb.zone_pos), tuple(T(x) for x in cb.obs_pos), T(cb.corr_len),
               T(cb.max_len))
@@ -437,9 +441,9 @@ def main():
             return oak_gb300.loc_analysis(*bd, weight=cb.weight, metric=cb.metric,
                                           loctype=cb.loctype, want_ampl=False, precision=prec)
 
-        def btime(prec):
+        def timed(fn):
             for _ in range(args.warmup):
-                o = bstep(prec)
+                o = fn()
             st = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
             barrier()
             torch.cuda.synchronize(dev)
@@ -447,7 +451,7 @@ def main():
             b1 = torch.cuda.Event(enable_timing=True)
             b0.record(stream)
             for _ in range(args.steps):
-                o = bstep(prec)
+                o = fn()
                 for k, v in oak_gb300.last_timings().items():
                     st[k] += v
             b1.record(stream)
@@ -455,25 +459,56 @@ def main():
             barrier()
             return o, b0.elapsed_time(b1) / args.steps, {k: v / args.steps for k, v in st.items()}
 
-        o64, bms64, bst64 = btime(oak_gb300.PREC_FP64)
+        o64, ms64, st64 = timed(lambda: bstep(oak_gb300.PREC_FP64))
         xa64, Sa64 = o64[0].clone(), o64[1].clone()
         bnobs = o64[3].cpu().numpy()
         del o64
-        om, bmsm, bstm = btime(oak_gb300.PREC_MIXED)
-        be_mean = float(torch.linalg.norm(om[0] - xa64) / torch.linalg.norm(xa64 - bd[1]))
-        be_anom = float(torch.linalg.norm(om[1] - Sa64) / torch.linalg.norm(Sa64))
-        batched = {"workload": cb.name, "scale": args.batched_scale, "zones": int(cb.Z),
-                   "N": int(cb.N), "m": int(cb.m), "obs_per_zone_max": int(bnobs.max()),
-                   "obs_per_zone_mean": float(bnobs.mean()),
-                   "fp64": {"value": ws * cb.Z / (bms64 / 1e3), "unit": UNIT,
-                            "ms_per_step": bms64, "stage_ms_per_step": bst64},
-                   "mixed": {"value": ws * cb.Z / (bmsm / 1e3), "unit": UNIT,
-                             "ms_per_step": bmsm, "stage_ms_per_step": bstm},
-                   "speedup_vs_fp64": bms64 / bmsm, "rel_err_mean_increment": be_mean,
-                   "rel_err_anomalies": be_anom,
-                   "note": "errors of the mixed form against the FP64 form on the GPU (which "
-                           "matches the oracle to 1e-10); state stored in FP64 at the boundary"}
-        del om, xa64, Sa64, bd, cb
+        om, msm, stm = timed(lambda: bstep(oak_gb300.PREC_MIXED))
+        e_mean = float(torch.linalg.norm(om[0] - xa64) / torch.linalg.norm(xa64 - bd[1]))
+        e_anom = float(torch.linalg.norm(om[1] - Sa64) / torch.linalg.norm(Sa64))
+        del om, Sa64
+        res = {"workload": cb.name, "scale": scale, "zones": int(cb.Z), "N": int(cb.N),
+               "m": int(cb.m), "obs_per_zone_max": int(bnobs.max()),
+               "obs_per_zone_mean": float(bnobs.mean()),
+               "fp64": {"value": ws * cb.Z / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64,
+                        "stage_ms_per_step": st64},
+               "mixed": {"value": ws * cb.Z / (msm / 1e3), "unit": UNIT, "ms_per_step": msm,
+                         "stage_ms_per_step": stm},
+               "speedup_vs_fp64": ms64 / msm, "rel_err_mean_increment": e_mean,
+               "rel_err_anomalies": e_anom,
+               "note": "errors of the mixed form against the FP64 form on the GPU (which "
+                       "matches the oracle to 1e-10); state stored in FP64 at the boundary"}
+        if adjoint_sub is not None:
+            nxb = int(round(1440 * scale))
+            w = max(1, int(round(adjoint_sub * scale)))
+            zc = np.arange(cb.Z)
+            subz = ((zc % nxb) >= nxb // 3) & ((zc % nxb) < nxb // 3 + w) & \
+                   ((zc // nxb) >= w // 2) & ((zc // nxb) < w // 2 + w)
+            sub_d = T(np.repeat(subz, cb.zone_size).astype(np.float64))
+            seed = 2.0 * (xa64 - T(cb.x_true)) * sub_d / float(sub_d.sum())
+            a_args = (bd[0], bd[2], bd[3], bd[4], bd[5], bd[6], bd[7], bd[8], bd[9], bd[10])
+            ga, ams, _ = timed(lambda: oak_gb300.loc_analysis_adjoint(
+                *a_args, seed, inflation=1.05, weight=cb.weight, metric=cb.metric,
+                loctype=cb.loctype))
+            res["adjoint"] = {"ms_per_call": ams, "cost_vs_forward_fp64": ams / ms64,
+                              "cost_vs_forward_mixed": ams / msm,
+                              "zones_seeded": int(subz.sum()),
+                              "cost": f"J = mean over a {w}x{w} column sub-region (all "
+                                      "levels) of (xa - x_true)^2; gradients w.r.t. all yo, r, "
+                                      "the localisation length factor and the prior "
+                                      "inflation 1.05",
+                              "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
+        del xa64, bd
+        return res
+
+    batched = None
+    if args.batched_scale > 0:
+        from oak_gb300.workloads import batched_case
+        batched = two_forms(batched_case(scale=args.batched_scale), args.batched_scale)
+    large = None
+    if args.large_scale > 0:
+        from oak_gb300.workloads import large_case
+        large = two_forms(large_case(scale=args.large_scale), args.large_scale, adjoint_sub=200)
 
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
@@ -534,6 +569,7 @@ def main():
         "e2e": e2e,
         "mixed": mixed,
         "batched": batched,
+        "large": large,
         "adjoint": adjoint,
         "global_analysis": glob,
         "graph": graph,

@@ -9,6 +9,9 @@ configurations (the reference publishes no dataset for this path; these stand in
   (ssh 50 %, temp 30 %, salt 20 %) through bilinear interpolation (4 columns, nearest level),
   70 % of them on 8 track segments so that zones near them select up to ~3,000, noise sd 0.1
   of the variable's sd, Gaspari-Cohn support radius 12 cells.
+* ``large_case``   -- 2 variables (temp, salt) on 1440 x 720 x 50 (zone = 100 elements),
+  N = 128, m = 1,000,000 clustered bilinear point observations with error sd ~ U(0.05, 0.5),
+  Gaspari-Cohn support radius 10 cells.
 * ``local_case``   -- 3-D grid 360 x 180 x 20, one variable, N = 64 members (Gaussian
   random fields, horizontal length 8 cells, vertical 3 levels), m = 50,000 observations
   (70 % on 40 great-circle-like tracks, 30 % uniform, noise sd 0.1), zones = the 64,800
@@ -192,47 +195,52 @@ def local_case(scale=1.0, N=64, nz=20, m=50_000, radius=12.0, seed_cfg=1, track_
     return c
 
 
-# variables of the batched state: (name, levels per column, sd)
+# variables of the batched state: (name, sd); the first four have nz levels, the last (ssh) one
 BATCHED_VARS = (("temp", 1.0), ("salt", 0.2), ("u", 0.1), ("v", 0.1), ("ssh", 0.05))
+# variables of the large state: two 3-D variables
+LARGE_VARS = (("temp", 1.0), ("salt", 0.2))
 
 
-def batched_case(scale=0.25, N=100, nz=30, m=200_000, radius=12.0, seed_cfg=2,
-                 track_frac=0.7, ntracks=8, keep_ensemble=False) -> Case:
-    """Config: batched mixed-precision local analysis, 720 x 360 columns of temp, salt, u, v
-    (nz levels) and ssh, N = 100, m = 200,000 bilinear observations clustered on tracks
-    (each track a segment a quarter of the grid long).
+def _column_case(name, gx, gy, scale, N, nz, vars3, var2, m, radius, cfg, track_frac, ntracks,
+                 obs_split, obs_sd, keep_ensemble):
+    """Columns of several variables (zone = one horizontal column), bilinear observations.
 
-    ``scale`` shrinks the horizontal grid by ``scale``, m by ``scale**2`` and the number of
-    tracks by ``scale`` (so the observation density along a track, and with it the largest
-    per-zone counts, stay those of the full grid). Column (i, j) is zone j*nx + i; inside it,
-    temp, salt, u, v levels 0..nz-1 then ssh: offset var*nz + k (ssh at 4*nz). Observations
-    sit at continuous (x, y) in cell units; H interpolates the 4 surrounding columns
-    bilinearly at the observation's level.
+    vars3: (name, sd) of the 3-D variables (nz levels each), var2: (name, sd) of a 2-D variable
+    or None. Column (i, j) is zone j*nx + i; inside it the 3-D variables' levels 0..nz-1 in
+    order, then the 2-D one. obs_split = (variables, bounds): observation l observes
+    variables[searchsorted(bounds, u_l)] (u_l uniform, bounds the cumulative fractions but the
+    last; variable index into vars3 + var2); obs_sd(var, rng) gives each observation's error
+    sd. Observations sit
+    at continuous (x, y) in cell units, 70 % (track_frac) on track segments a quarter of the
+    grid long; H interpolates the 4 surrounding columns bilinearly at the observation's level.
+    ``scale`` shrinks the grid by ``scale``, m by ``scale**2`` and the number of tracks by
+    ``scale`` (the density along a track, and with it the largest per-zone counts, stay those
+    of the full grid).
     """
-    cfg = seed_cfg
-    nx = max(4, int(round(720 * scale)))
-    ny = max(4, int(round(360 * scale)))
+    nx = max(4, int(round(gx * scale)))
+    ny = max(4, int(round(gy * scale)))
     if scale != 1.0:
         m = max(1, int(round(m * scale * scale)))
         ntracks = max(1, int(round(ntracks * scale)))
     Z = nx * ny
-    zsz = 4 * nz + 1
+    n3 = len(vars3)
+    zsz = n3 * nz + (1 if var2 else 0)
     n = Z * zsz
     lengths3, lengths2 = (8.0, 8.0, 3.0), (8.0, 8.0)
 
     def draw(seed):
         x = np.empty((Z, zsz))
         rng = np.random.default_rng(seed)
-        for v, (_, sd) in enumerate(BATCHED_VARS[:4]):
+        for v, (_, sd) in enumerate(vars3):
             x[:, v * nz:(v + 1) * nz] = sd * gaussian_field((ny, nx, nz), lengths3, rng).reshape(Z, nz)
-        x[:, 4 * nz] = BATCHED_VARS[4][1] * gaussian_field((ny, nx), lengths2, rng).reshape(Z)
+        if var2:
+            x[:, n3 * nz] = var2[1] * gaussian_field((ny, nx), lengths2, rng).reshape(Z)
         return x.reshape(-1)
 
     truth = draw(1000 * cfg + 0)
     Ef = np.empty((n, N), order="F")
     for k in range(N):
         Ef[:, k] = draw(1000 * cfg + 1 + k)
-    # observation positions: tracks (continuous along-track coordinate) + uniform
     rng_pos = np.random.default_rng(1000 * cfg + 900)
     m_track = int(round(track_frac * m))
     rng_t = np.random.default_rng(1000 * cfg + 902)
@@ -250,11 +258,11 @@ def batched_case(scale=0.25, N=100, nz=30, m=200_000, radius=12.0, seed_cfg=2,
     xs.append(rng_pos.uniform(0.0, nx - 1, m - m_track))
     ys.append(rng_pos.uniform(0.0, ny - 1, m - m_track))
     ox, oy = np.concatenate(xs), np.concatenate(ys)
-    # variable split ssh 50 %, temp 30 %, salt 20 %; level uniform for the 3-D variables
     u = rng_pos.uniform(0.0, 1.0, m)
-    var = np.where(u < 0.5, 4, np.where(u < 0.8, 0, 1))
-    lev = np.where(var == 4, 0, rng_pos.integers(0, nz, m))
-    off = np.where(var == 4, 4 * nz, var * nz + lev)
+    var = np.asarray(obs_split[0])[np.searchsorted(np.asarray(obs_split[1]), u, side="right")]
+    is2 = var == n3
+    lev = np.where(is2, 0, rng_pos.integers(0, nz, m))
+    off = np.where(is2, n3 * nz, var * nz + lev)
     ix = np.minimum(np.floor(ox).astype(np.int64), nx - 2)
     iy = np.minimum(np.floor(oy).astype(np.int64), ny - 2)
     fx, fy = ox - ix, oy - iy
@@ -262,7 +270,7 @@ def batched_case(scale=0.25, N=100, nz=30, m=200_000, radius=12.0, seed_cfg=2,
     H_index = cols * zsz + off[:, None]
     H_weight = np.stack([(1 - fx) * (1 - fy), fx * (1 - fy), (1 - fx) * fy, fx * fy], 1)
     HEf = np.einsum("mk,mkn->mn", H_weight, Ef[H_index.reshape(-1), :].reshape(m, 4, N))
-    sd_obs = 0.1 * np.array([sd for _, sd in BATCHED_VARS])[var]
+    sd_obs = obs_sd(var, np.random.default_rng(1000 * cfg + 903))
     noise = np.random.default_rng(1000 * cfg + 901).standard_normal(m) * sd_obs
     yo = np.einsum("mk,mk->m", H_weight, truth[H_index]) + noise
     xf, Hxf, Sf, HSf = _anomalies(Ef, HEf)
@@ -272,13 +280,36 @@ def batched_case(scale=0.25, N=100, nz=30, m=200_000, radius=12.0, seed_cfg=2,
     zone_pos[:, 0] = zc % nx
     zone_pos[:, 1] = zc // nx
     obs_pos = (ox, oy, lev.astype(np.float64), np.zeros(m))
-    c = Case(f"batched {nx}x{ny}x{nz} 5 variables N={N} m={m} GC radius {radius:g}", xf, Hxf,
-             yo, Sf, HSf, sd_obs ** 2, truth, zone_size, zone_pos, obs_pos,
-             np.full(Z, radius / 2.0), np.full(Z, radius), weight=1, metric=0, loctype=1,
-             H_index=H_index, H_weight=H_weight)
+    c = Case(f"{name} {nx}x{ny}x{nz} N={N} m={m} GC radius {radius:g}", xf, Hxf, yo, Sf, HSf,
+             sd_obs ** 2, truth, zone_size, zone_pos, obs_pos, np.full(Z, radius / 2.0),
+             np.full(Z, radius), weight=1, metric=0, loctype=1, H_index=H_index,
+             H_weight=H_weight)
     if keep_ensemble:
         c.Ef, c.HEf = Ef, HEf
     return c
+
+
+def batched_case(scale=0.25, N=100, nz=30, m=200_000, radius=12.0, seed_cfg=2,
+                 track_frac=0.7, ntracks=8, keep_ensemble=False) -> Case:
+    """Config: batched mixed-precision local analysis, 720 x 360 columns of temp, salt, u, v
+    (nz levels) and ssh, N = 100, m = 200,000 bilinear observations clustered on 8 track
+    segments (ssh 50 %, temp 30 %, salt 20 %; noise sd 0.1 of the variable's sd)."""
+    sds = np.array([sd for _, sd in BATCHED_VARS])
+    return _column_case("batched 5 variables", 720, 360, scale, N, nz, BATCHED_VARS[:4],
+                        BATCHED_VARS[4], m, radius, seed_cfg, track_frac, ntracks,
+                        ((4, 0, 1), (0.5, 0.8)), lambda var, rng: 0.1 * sds[var],
+                        keep_ensemble)
+
+
+def large_case(scale=0.125, N=128, nz=50, m=1_000_000, radius=10.0, seed_cfg=4,
+               track_frac=0.7, ntracks=16, keep_ensemble=False) -> Case:
+    """Config: large mixed-precision analysis, 1440 x 720 columns of 2 variables (temp, salt) on
+    nz = 50 levels (100 elements a zone), N = 128, m = 1,000,000 clustered point observations
+    (bilinear, half per variable) with error sd drawn uniformly from 0.05-0.5, Gaspari-Cohn
+    support radius 10 cells."""
+    return _column_case("large 2 variables", 1440, 720, scale, N, nz, LARGE_VARS, None, m,
+                        radius, seed_cfg, track_frac, ntracks, ((0, 1), (0.5,)),
+                        lambda var, rng: rng.uniform(0.05, 0.5, var.size), keep_ensemble)
 
 
 def rrsqrt_test_case():

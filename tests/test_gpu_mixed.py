@@ -7,7 +7,7 @@ relevant-observation counts must be identical.
 import numpy as np
 import pytest
 
-from oak_gb300.workloads import batched_case, local_case
+from oak_gb300.workloads import batched_case, large_case, local_case
 from oracle import cref
 
 pytestmark = pytest.mark.gpu
@@ -105,6 +105,24 @@ def test_mixed_batched_bilinear_case(oakg):
     assert np.array_equal(nobs, nobs_o) and nobs_o.max() > 300
     e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
     assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)
+
+
+def test_large_case_both_forms(oakg):
+    """The 2-variable large case (100-element columns, N = 128, clustered bilinear
+    observations with error sd ~ U(0.05, 0.5)) at 1/16 of its grid: the FP64 form at 1e-10 and
+    the mixed form at 1e-4 against the oracle."""
+    c = large_case(scale=1 / 16)
+    xa_o, Sa_o, _, nobs_o = cref.locanalysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                             c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                             c.max_len, kind=c.weight)
+    assert nobs_o.max() > 500
+    for prec, tol in ((oakg.PREC_FP64, 1e-10), (oakg.PREC_MIXED, TOL)):
+        xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                            c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                            c.max_len, weight=c.weight, precision=prec)
+        assert np.array_equal(nobs, nobs_o)
+        e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
+        assert e_mean < tol and e_anom < tol, (prec, e_mean, e_anom)
 
 
 def test_ensemble_size_limits(oakg):
