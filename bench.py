@@ -393,7 +393,8 @@ def main():
                  "mixed_tuned_value": ws * c.Z / (gmx / 1e3),
                  "mixed_tuned_speedup_vs_fp64": ms / gmx,
                  "mixed_cell_size": info["cell_size"], "mixed_graph_nodes": info["graph_nodes"],
-                 "tuning_cell_ms": info["tuning"]}
+                 "tuning_cell_ms": info["tuning"], "mixed_zone_order": info["zone_order"],
+                 "zone_order_gram_ms": info["zone_order_ms"]}
 
     # global analysis (rrsqrt.F90:196-208) of the 100 x 80, N = 30, m = 500 configuration:
     # device-resident time per analysis, and the CPU port on the host cores beside it

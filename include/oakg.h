@@ -215,8 +215,13 @@ int oakg_ens_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzo
  * sizes and pointers are those of the plan -- and waits for it: same status codes as
  * oakg_locanalysis. With tune != 0 (and loc->cell_size <= 0) the cell edge of the observation
  * grid is chosen among 0.25, 0.35, 0.5, 0.7 and 1 times the localisation reach by timing the
- * selection + Gram stage on the data. oakg_plan_info reports the chosen edge, the graph's
- * node count and up to ntune (edge, ms) tuning samples; it returns the number of samples.
+ * selection + Gram stage on the data; then the zone schedule of that stage: its persistent
+ * blocks take zones off a counter in index order, or in descending observation count of the
+ * tuning run (longest tasks first), whichever measures faster. oakg_plan_info reports the
+ * chosen edge, the graph's node count and up to ntune (edge, ms) tuning samples; it returns
+ * the number of samples. oakg_plan_schedule reports the zone schedule: 1 for the
+ * descending-count order, 0 for index order, and the two measured stage times (ms, either may
+ * be NULL; both 0 without tuning).
  * A plan holds the caller's pointers: keep the buffers alive until oakg_plan_destroy. */
 typedef struct oakg_plan oakg_plan;
 int oakg_plan_locanalysis(oakg_plan** plan, const oakg_dims* dims, const oakg_loc* loc,
@@ -229,6 +234,7 @@ int oakg_plan_locanalysis(oakg_plan** plan, const oakg_dims* dims, const oakg_lo
 int oakg_plan_execute(oakg_plan* plan, void* stream);
 int oakg_plan_info(const oakg_plan* plan, double* cell_size, int64_t* graph_nodes,
                    double* tune_cell, double* tune_ms, int32_t ntune);
+int oakg_plan_schedule(const oakg_plan* plan, double* index_order_ms, double* count_order_ms);
 void oakg_plan_destroy(oakg_plan* plan);
 
 /* Message of the last failed call on this thread (empty if none); returns its length. */

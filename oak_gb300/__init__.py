@@ -115,6 +115,9 @@ def lib() -> ctypes.CDLL:
                                  ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                  ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
     L.oakg_plan_info.restype = ctypes.c_int
+    L.oakg_plan_schedule.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]
+    L.oakg_plan_schedule.restype = ctypes.c_int
     L.oakg_plan_destroy.argtypes = [ctypes.c_void_p]
     L.oakg_plan_destroy.restype = None
     L.oakg_ensemble_prologue.argtypes = [ctypes.POINTER(Dims), P, ctypes.c_int64,
@@ -491,14 +494,21 @@ class Plan:
 
     @property
     def info(self) -> dict:
-        """Chosen cell edge, graph node count and the tuning samples (edge, ms)."""
+        """Chosen cell edge, graph node count, the tuning samples (edge, ms) and the zone
+        schedule of the selection + Gram stage (descending observation count or index order,
+        with both measured stage times)."""
         cs = ctypes.c_double(0.0)
         nodes = ctypes.c_int64(0)
         tc = (ctypes.c_double * 8)()
         tm = (ctypes.c_double * 8)()
         k = lib().oakg_plan_info(self._h, ctypes.byref(cs), ctypes.byref(nodes), tc, tm, 8)
+        t_idx = ctypes.c_double(0.0)
+        t_cnt = ctypes.c_double(0.0)
+        used = lib().oakg_plan_schedule(self._h, ctypes.byref(t_idx), ctypes.byref(t_cnt))
         return {"cell_size": cs.value, "graph_nodes": nodes.value,
-                "tuning": [(tc[i], tm[i]) for i in range(k)]}
+                "tuning": [(tc[i], tm[i]) for i in range(k)],
+                "zone_order": "descending observation count" if used else "index",
+                "zone_order_ms": {"index": t_idx.value, "count": t_cnt.value}}
 
     def close(self):
         if self._h is not None:

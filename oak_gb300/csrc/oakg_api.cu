@@ -70,7 +70,7 @@ enum BufId {
   B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
   B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_OBS32, B_E_EF, B_E_HIDX, B_E_HW, B_E_HSH, B_E_HEF, B_E_XF, B_E_SF,
   B_E_HXF, B_E_HSF, B_E_XA, B_E_SA, B_E_MC, B_E_EA, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
-  B_COUNT_
+  B_ORDER, B_COUNT_
 };
 
 struct Ctx {
@@ -208,9 +208,9 @@ struct ZoneKernels<double> {
   static cudaError_t gram(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                           int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
                           double* d_G, double* d_g, int32_t* nobs, int brute, int32_t* work,
-                          int32_t* /*err*/, cudaStream_t st) {
+                          int32_t* /*err*/, cudaStream_t st, const int32_t* order) {
     return zone_gram_fp64(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
-                          st);
+                          st, order);
   }
   template <typename... A>
   static cudaError_t eig(A... a) { return zone_eig_fp64(a...); }
@@ -225,12 +225,12 @@ struct ZoneKernels<float> {
   static cudaError_t gram(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                           int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
                           float* d_G, float* d_g, int32_t* nobs, int brute, int32_t* work,
-                          int32_t* err, cudaStream_t st) {
+                          int32_t* err, cudaStream_t st, const int32_t* order) {
     if (N <= gram_tc_max_n() && so.HSt32 && so.r32)
       return zone_gram_tc(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
-                          err, st);
+                          err, st, order);
     return zone_gram_fp32(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
-                          st);
+                          st, order);
   }
   template <typename... A>
   static cudaError_t eig(A... a) { return zone_eig_fp32(a...); }
@@ -254,6 +254,8 @@ struct ChunkArgs {
   const double *xf, *Sf;
   double *xa, *Sa, *ampl;
   int32_t* nobs;
+  // optional pick order of the selection + Gram stage (chunk-local zone indices, Z entries)
+  const int32_t* zorder = nullptr;
 };
 
 // How run_chunks issues its work: timed (events + a host wait per chunk), captured into a CUDA
@@ -292,7 +294,7 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     const int32_t nzc = (int32_t)std::min<int64_t>(chunk, a.Z - z0);
     if (timed) cudaEventRecord(c->ev[2], st);
     e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv, a.nobs,
-                a.brute, d_work, *status_all, st);
+                a.brute, d_work, *status_all, st, a.zorder);
     if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
     if (mode == RunMode::kGramOnly) {
       cudaEventRecord(c->ev[3], st);
@@ -812,6 +814,10 @@ struct Plan {
   double tune_ms[8] = {};
   double tune_cell[8] = {};
   int ntune = 0;
+  // zone schedule of the selection + Gram stage: descending observation count (1) or index
+  // order (0), with the two measured stage times
+  int32_t zorder_used = 0;
+  double order_ms[2] = {0.0, 0.0};
 };
 
 void plan_free(Plan* pl) {
@@ -927,6 +933,53 @@ int plan_create_impl(Plan** out, const oakg_dims* dims, const oakg_loc* loc, int
         2 * sizeof(int32_t);
     const int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
     c->chunk_override = std::max<int64_t>(1, std::min<int64_t>(chunk, Z));
+  }
+  // zone schedule: the persistent selection + Gram blocks take zones off a counter, and the
+  // observation counts of a zone range from 0 to thousands; taking each chunk's zones in
+  // descending count (longest tasks first) shortens the tail. Kept when it measures faster.
+  if (tune && m > 0) {
+    double ms_nat = 0.0, ms_ord = 0.0;
+    if ((rc = plan_run_mode(pl, RunMode::kGramOnly)) ||
+        (rc = plan_run_mode(pl, RunMode::kGramOnly, &ms_nat))) {
+      plan_free(pl);
+      return rc;
+    }
+    std::vector<int32_t> cnt((size_t)Z), ord((size_t)Z);
+    if ((e = cudaMemcpyAsync(cnt.data(), pl->ca.nobs, sizeof(int32_t) * (size_t)Z,
+                             cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+      plan_free(pl);
+      return cuda_fail(e, "observation counts");
+    }
+    const int64_t chunk = c->chunk_override;
+    for (int64_t z0 = 0; z0 < Z; z0 += chunk) {
+      const int64_t nzc = std::min<int64_t>(chunk, Z - z0);
+      int32_t* o = ord.data() + z0;
+      for (int64_t i = 0; i < nzc; i++) o[i] = (int32_t)i;
+      const int32_t* cz = cnt.data() + z0;
+      std::stable_sort(o, o + nzc, [cz](int32_t a, int32_t b) { return cz[a] > cz[b]; });
+    }
+    int32_t* d_ord;
+    if ((rc = scratch(c, B_ORDER, (size_t)Z, &d_ord, "zone order"))) {
+      plan_free(pl);
+      return rc;
+    }
+    if ((e = cudaMemcpyAsync(d_ord, ord.data(), sizeof(int32_t) * (size_t)Z,
+                             cudaMemcpyHostToDevice, c->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
+      plan_free(pl);
+      return cuda_fail(e, "zone order");
+    }
+    pl->ca.zorder = d_ord;
+    if ((rc = plan_run_mode(pl, RunMode::kGramOnly)) ||
+        (rc = plan_run_mode(pl, RunMode::kGramOnly, &ms_ord))) {
+      plan_free(pl);
+      return rc;
+    }
+    pl->order_ms[0] = ms_nat;
+    pl->order_ms[1] = ms_ord;
+    pl->zorder_used = (ms_ord < ms_nat) ? 1 : 0;
+    if (!pl->zorder_used) pl->ca.zorder = nullptr;
   }
   if ((rc = plan_run_mode(pl, RunMode::kTimed))) {
     plan_free(pl);
@@ -1352,6 +1405,14 @@ int oakg_plan_info(const oakg_plan* plan, double* cell_size, int64_t* graph_node
     if (tune_ms) tune_ms[i] = p->tune_ms[i];
   }
   return p->ntune;
+}
+
+int oakg_plan_schedule(const oakg_plan* plan, double* index_order_ms, double* count_order_ms) {
+  if (!plan || !plan->p) return 0;
+  const oakg::Plan* p = plan->p;
+  if (index_order_ms) *index_order_ms = p->order_ms[0];
+  if (count_order_ms) *count_order_ms = p->order_ms[1];
+  return p->zorder_used;
 }
 
 void oakg_plan_destroy(oakg_plan* plan) {

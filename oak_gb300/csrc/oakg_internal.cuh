@@ -59,25 +59,28 @@ cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_st
 
 // ---- zone_gram.cu
 // Selection + Gram + innovation projection for zones [z0, z0 + nzc); writes G (N x N, both
-// triangles, row-major per zone), gvec (N), nobs per zone.
+// triangles, row-major per zone), gvec (N), nobs per zone. The persistent blocks take zones
+// in order (chunk-local indices: the w-th zone taken is order[z0 + w]) when `order` is given,
+// else in index order; outputs stay at each zone's own slot.
 cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
                            int32_t z0, int32_t nzc, const double* zone_xyzt,
                            const double* corr_len, const double* max_len, double* d_G,
                            double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
-                           cudaStream_t st);
+                           cudaStream_t st, const int32_t* order = nullptr);
 // Mixed precision: same selection, products accumulated in FP32 (G, g in float).
 cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
                            int32_t z0, int32_t nzc, const double* zone_xyzt,
                            const double* corr_len, const double* max_len, float* d_G,
                            float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
-                           cudaStream_t st);
+                           cudaStream_t st, const int32_t* order = nullptr);
 // Mixed precision on the tensor cores (zone_gram_tc.cu), N <= gram_tc_max_n(); needs
 // so.HSt32. d_err receives ZST_TIMEOUT (OR) if a bounded device wait expired.
 int gram_tc_max_n();
 cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                          int32_t nzc, const double* zone_xyzt, const double* corr_len,
                          const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
-                         int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st);
+                         int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st,
+                         const int32_t* order = nullptr);
 // FP32 copy of count doubles (HS rows for the mixed form).
 cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st);
 // Same as zone_gram_fp64 for the zones listed in zlist[0..nzc) (G, g slots in list order).

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads)
                 const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
                 const double* __restrict__ max_len, R* __restrict__ G, R* __restrict__ gv,
                 int32_t* __restrict__ nobs, int brute, int CH, int32_t* __restrict__ work,
-                const int32_t* __restrict__ zlist) {
+                const int32_t* __restrict__ zlist, const int32_t* __restrict__ order) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   R* dyn = reinterpret_cast<R*>(dyn_raw);
   R* sh = dyn;            // [CH][N]
@@ -127,8 +127,9 @@ __global__ void __launch_bounds__(kThreads)
   for (;;) {
     if (threadIdx.x == 0) zs.zone = atomicAdd(work, 1);
     __syncthreads();
-    const int32_t zl = zs.zone;
-    if (zl >= nzc) break;
+    const int32_t w = zs.zone;  // pick number; zone order[z0 + w] when a pick order is given
+    if (w >= nzc) break;
+    const int32_t zl = order ? order[z0 + w] : w;
     const int32_t z = zlist ? zlist[zl] : z0 + zl;
     const double zx = zone_xyzt[4 * (int64_t)z + 0], zy = zone_xyzt[4 * (int64_t)z + 1];
     const double zzc = zone_xyzt[4 * (int64_t)z + 2], ztc = zone_xyzt[4 * (int64_t)z + 3];
@@ -346,7 +347,7 @@ cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams
                         int32_t nzc, const double* zone_xyzt, const double* corr_len,
                         const double* max_len, R* d_G, R* d_g, int32_t* d_nobs,
                         int brute, int32_t* d_work, cudaStream_t st,
-                        const int32_t* zlist = nullptr) {
+                        const int32_t* zlist = nullptr, const int32_t* order = nullptr) {
   int CH = chunk_rows(N);
   size_t smem = (size_t)(2 * CH * N + CH) * sizeof(R);
   cudaError_t e = cudaFuncSetAttribute(k_zone_gram<MAXE, R>,
@@ -365,7 +366,7 @@ cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams
   if (e != cudaSuccess) return e;
   k_zone_gram<MAXE, R><<<grid, kThreads, smem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
                                                       max_len, d_G, d_g, d_nobs, brute, CH,
-                                                      d_work, zlist);
+                                                      d_work, zlist, order);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -424,18 +425,18 @@ cudaError_t zone_gram_fp64(const CellGrid& g, const SortedObs& so, int N, LocPar
                            int32_t z0, int32_t nzc, const double* zone_xyzt,
                            const double* corr_len, const double* max_len, double* d_G,
                            double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
-                           cudaStream_t st) {
+                           cudaStream_t st, const int32_t* order) {
   OAKG_GRAM_DISPATCH_T(launch_zone, double, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len,
-                       d_G, d_g, d_nobs, brute, d_work, st);
+                       d_G, d_g, d_nobs, brute, d_work, st, nullptr, order);
 }
 
 cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
                            int32_t z0, int32_t nzc, const double* zone_xyzt,
                            const double* corr_len, const double* max_len, float* d_G,
                            float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
-                           cudaStream_t st) {
+                           cudaStream_t st, const int32_t* order) {
   OAKG_GRAM_DISPATCH_T(launch_zone, float, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len,
-                       d_G, d_g, d_nobs, brute, d_work, st);
+                       d_G, d_g, d_nobs, brute, d_work, st, nullptr, order);
 }
 
 cudaError_t zone_gram_fp64_list(const CellGrid& g, const SortedObs& so, int N, LocParams lp,

@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
                    const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
                    const double* __restrict__ max_len, float* __restrict__ G,
                    float* __restrict__ gv, int32_t* __restrict__ nobs, int brute,
-                   int32_t* __restrict__ work, int32_t* __restrict__ err) {
+                   int32_t* __restrict__ work, int32_t* __restrict__ err,
+                   const int32_t* __restrict__ order) {
   using C = TcCfg<NB>;
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   __shared__ __align__(16) TcShared ts;
@@ -302,8 +303,9 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
   for (;;) {
     if (tid == 0) ts.zone = atomicAdd(work, 1);
     __syncthreads();
-    const int32_t zl = ts.zone;
-    if (zl >= nzc || ts.flag) break;
+    const int32_t w = ts.zone;  // pick number; zone order[z0 + w] when a pick order is given
+    if (w >= nzc || ts.flag) break;
+    const int32_t zl = order ? order[z0 + w] : w;
     const int32_t z = z0 + zl;
     const double zx = zone_xyzt[4 * (int64_t)z + 0], zy = zone_xyzt[4 * (int64_t)z + 1];
     const double zzc = zone_xyzt[4 * (int64_t)z + 2], ztc = zone_xyzt[4 * (int64_t)z + 3];
@@ -561,7 +563,7 @@ cudaError_t launch_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocPar
                            int32_t z0, int32_t nzc, const double* zone_xyzt,
                            const double* corr_len, const double* max_len, float* d_G,
                            float* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
-                           int32_t* d_err, cudaStream_t st) {
+                           int32_t* d_err, cudaStream_t st, const int32_t* order) {
   using C = TcCfg<NB>;
   cudaError_t e = cudaFuncSetAttribute(k_zone_gram_tc<NB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -580,7 +582,7 @@ cudaError_t launch_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocPar
   if (e != cudaSuccess) return e;
   k_zone_gram_tc<NB><<<grid, kThreads, C::kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt,
                                                           corr_len, max_len, d_G, d_g, d_nobs,
-                                                          brute, d_work, d_err);
+                                                          brute, d_work, d_err, order);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -592,13 +594,14 @@ int gram_tc_max_n() { return 128; }
 cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                          int32_t nzc, const double* zone_xyzt, const double* corr_len,
                          const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
-                         int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st) {
+                         int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st,
+                         const int32_t* order) {
   if (N < 1 || N > 128 || !so.HSt32 || !so.r32 || !so.innov32) return cudaErrorInvalidValue;
   if (N <= 64)
     return launch_gram_tc<64>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len, d_G, d_g,
-                              d_nobs, brute, d_work, d_err, st);
+                              d_nobs, brute, d_work, d_err, st, order);
   return launch_gram_tc<128>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len, d_G, d_g,
-                             d_nobs, brute, d_work, d_err, st);
+                             d_nobs, brute, d_work, d_err, st, order);
 }
 
 }  // namespace oakg

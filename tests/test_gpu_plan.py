@@ -83,11 +83,32 @@ def test_tuned_plan(oakg):
     info = pl.info
     assert len(info["tuning"]) == 5
     assert info["cell_size"] == min(info["tuning"], key=lambda t: t[1])[0]
+    # the zone schedule is the faster of the two measured orders
+    t = info["zone_order_ms"]
+    assert t["index"] > 0 and t["count"] > 0
+    assert info["zone_order"] == ("descending observation count" if t["count"] < t["index"]
+                                  else "index")
     xa, Sa, nobs = (t.cpu().numpy() for t in pl.execute())
     assert np.array_equal(nobs, ref[2])
     # another cell edge changes the order of the FP32 Gram sums only
     assert np.linalg.norm(xa - ref[0]) <= 1e-5 * np.linalg.norm(ref[0] - c.xf)
     assert np.linalg.norm(Sa - ref[1]) <= 1e-5 * np.linalg.norm(ref[1])
+    pl.close()
+
+
+def test_tuned_plan_fp64(oakg):
+    """The tuned FP64 plan (edge and zone schedule chosen on the data) against the direct
+    call: selection identical, products summed in another order only."""
+    c = local_case(scale=1 / 8, N=24)
+    d = _dev(c)
+    kw = dict(weight=c.weight, precision=0)
+    ref = _direct(oakg, d, **kw)
+    pl = _plan(oakg, d, tune=True, **kw)
+    assert pl.info["zone_order"] in ("index", "descending observation count")
+    xa, Sa, nobs = (t.cpu().numpy() for t in pl.execute())
+    assert np.array_equal(nobs, ref[2])
+    assert np.linalg.norm(xa - ref[0]) <= 1e-12 * np.linalg.norm(ref[0] - c.xf)
+    assert np.linalg.norm(Sa - ref[1]) <= 1e-12 * np.linalg.norm(ref[1])
     pl.close()
 
 
