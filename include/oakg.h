@@ -193,6 +193,42 @@ int oakg_ensemble_epilogue(const oakg_dims* dims, const double* xf, const double
                            const double* Sa, double inflation, const double* max_correction,
                            double* Ea, int64_t ldE);
 
+/* ens2sqrt (rrsqrt.F90:786-806, Pham 2001): the mean (n) and N - 1 anomaly columns
+ * S (dims->ldS x (N-1)) of the ensemble E (n x N, leading dimension ldE):
+ * alpha = (sqrt(N) - 1)/(N - 1), shift = (1 - alpha) mean + alpha E(:,N),
+ * S(:,i) = (E(:,i) - shift)/sqrt(N - 1); S S^T is the ensemble covariance. N = dims->N. */
+int oakg_ens2sqrt(const oakg_dims* dims, const double* E, int64_t ldE, double* mean, double* S);
+
+/* sqrt2ens (rrsqrt.F90:815-839): the N-member ensemble E (n x N, leading dimension ldE) with
+ * mean `mean` and covariance S S^T from N - 1 columns S (dims->ldS): E = mean + S Om^T,
+ * Om = sqrt(N - 1) perpSpace(w) Theta, w = 1/sqrt(N) (perpSpace: matoper.F90:509-535). The
+ * reference draws Theta with randOrthMatrix; here theta is the caller's (N-1) x (N-1)
+ * orthogonal matrix (column-major, memory kind of dims->mem), or NULL for the identity. */
+int oakg_sqrt2ens(const oakg_dims* dims, const double* mean, const double* S,
+                  const double* theta, double* E, int64_t ldE);
+
+/* ensAnalysis (rrsqrt.F90:613-671): the global analysis of an ensemble Ef (n x N, ldE) with
+ * observed ensemble HEf (m x N, ldHE): mean and scaled anomalies of both, oakg_analysis,
+ * Ea = xa + sqrt(N-1) Sa (n x N, ldE; may alias Ef). xa (n) and ampl (N) are optional. */
+int oakg_ens_analysis(const oakg_dims* dims, const double* Ef, int64_t ldE, const double* HEf,
+                      int64_t ldHE, const double* yo, const double* r_diag, double* Ea,
+                      double* xa, double* ampl);
+
+/* biasedLocAnalysis (rrsqrt.F90:476-546), the bias-aware local analysis: inc = the local
+ * analysis increment of (Hxf, yo, Sf, HSf, R); ba = bf - gamma inc; the unbiased forecast
+ * ux = xf - ba and H ux + Hshift (the operator H, shift included); xa = ux + the local analysis
+ * increment of (H ux + Hshift, yo, Sf, HSf, (1 - gamma) R) (the reference's DCDCovar with
+ * D = 1/sqrt(1 - gamma)); Sa = Sf (NULL: not written). 0 <= gamma < 1. Geometry arguments as
+ * for oakg_locanalysis. */
+int oakg_biased_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                            const int32_t* zone_size, double gamma, const oakg_obsoper* H,
+                            const double* xf, const double* bf, const double* Hxf,
+                            const double* yo, const double* Sf, const double* HSf,
+                            const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                            const double* obs_y, const double* obs_z, const double* obs_t,
+                            const double* corr_len, const double* max_len, double* xa,
+                            double* ba, double* Sa);
+
 /* The local analysis of an ensemble, all on the device: prologue, oakg_locanalysis (dims->ldS
  * and dims->ldH are ignored: the anomalies are the library's), epilogue. Ea may alias Ef. The
  * numerical core of oak_assim for schemetype = 1 without the file I/O. */

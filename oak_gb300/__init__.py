@@ -131,6 +131,17 @@ def lib() -> ctypes.CDLL:
                                         ctypes.POINTER(ObsOper)] + [P] * 9
                                        + [ctypes.c_double, P, P])
     L.oakg_ens_locanalysis.restype = ctypes.c_int
+    L.oakg_ens2sqrt.argtypes = [ctypes.POINTER(Dims), P, ctypes.c_int64, P, P]
+    L.oakg_ens2sqrt.restype = ctypes.c_int
+    L.oakg_sqrt2ens.argtypes = [ctypes.POINTER(Dims), P, P, P, P, ctypes.c_int64]
+    L.oakg_sqrt2ens.restype = ctypes.c_int
+    L.oakg_ens_analysis.argtypes = [ctypes.POINTER(Dims), P, ctypes.c_int64, P, ctypes.c_int64,
+                                    P, P, P, P, P]
+    L.oakg_ens_analysis.restype = ctypes.c_int
+    L.oakg_biased_locanalysis.argtypes = ([ctypes.POINTER(Dims), ctypes.POINTER(Loc),
+                                           ctypes.c_int32, P, ctypes.c_double,
+                                           ctypes.POINTER(ObsOper)] + [P] * 17)
+    L.oakg_biased_locanalysis.restype = ctypes.c_int
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -425,6 +436,103 @@ def ens_loc_analysis(zone_size, Ef, H_index, H_weight, yo, r_diag, zone_pos, obs
         A.vec(max_correction, n=n, name="max_correction"), A.mat(Ea, n, N, "Ea")[0])
     _check(rc)
     return Ea
+
+
+def ens2sqrt(E):
+    """Mean and the N - 1 anomaly columns of Pham's reduction (oakg_ens2sqrt,
+    rrsqrt.F90:786-806). Returns ``(mean (n,), S (n, N-1))``."""
+    n, N = int(E.shape[0]), int(E.shape[1])
+    device = _device_mode(E)
+    A = _Args(device)
+    pE, ldE = A.mat(E, n, N, "E")
+    mean = _empty_like_mode(device, (n,), like=E)
+    S = _empty_like_mode(device, (n, N - 1), order="F", like=E)
+    dims = Dims(n=n, N=N, m=0, ldS=n, ldH=1, mem=MEM_DEVICE if device else MEM_HOST)
+    _sync_torch(device, E)
+    _check(lib().oakg_ens2sqrt(ctypes.byref(dims), pE, ldE, A.vec(mean, name="mean"),
+                               A.mat(S, n, N - 1, "S")[0]))
+    return mean, S
+
+
+def sqrt2ens(mean, S, theta=None):
+    """The N-member ensemble with this mean and covariance S S^T (oakg_sqrt2ens,
+    rrsqrt.F90:815-839): ``E = mean + S Om^T``, ``Om = sqrt(N-1) perpSpace(1/sqrt(N)) theta``
+    with ``theta`` an (N-1) x (N-1) orthogonal matrix (the identity if None; the reference
+    draws it at random). Returns ``E (n, N)``."""
+    n, K = int(S.shape[0]), int(S.shape[1])
+    N = K + 1
+    device = _device_mode(mean, S, theta)
+    A = _Args(device)
+    pS, ldS = A.mat(S, n, K, "S")
+    E = _empty_like_mode(device, (n, N), order="F", like=S)
+    pT = None if theta is None else A.mat(theta, K, K, "theta")[0]
+    dims = Dims(n=n, N=N, m=0, ldS=ldS, ldH=1, mem=MEM_DEVICE if device else MEM_HOST)
+    _sync_torch(device, S)
+    _check(lib().oakg_sqrt2ens(ctypes.byref(dims), A.vec(mean, n=n, name="mean"), pS, pT,
+                               A.mat(E, n, N, "E")[0], n))
+    return E
+
+
+def ens_analysis(Ef, HEf, yo, r_diag):
+    """Global analysis of an ensemble (oakg_ens_analysis, ensAnalysis of
+    rrsqrt.F90:613-671). Returns ``(Ea (n, N), xa (n,), amplitudes (N,))``."""
+    n, N = int(Ef.shape[0]), int(Ef.shape[1])
+    m = int(yo.shape[0])
+    device = _device_mode(Ef, HEf, yo, r_diag)
+    A = _Args(device)
+    pE, ldE = A.mat(Ef, n, N, "Ef")
+    pH, ldH = A.mat(HEf, m, N, "HEf") if m > 0 else (None, 1)
+    Ea = _empty_like_mode(device, (n, N), order="F", like=Ef)
+    xa = _empty_like_mode(device, (n,), like=Ef)
+    ampl = _empty_like_mode(device, (N,), like=Ef)
+    dims = Dims(n=n, N=N, m=m, ldS=n, ldH=max(m, 1), mem=MEM_DEVICE if device else MEM_HOST)
+    _sync_torch(device, Ef)
+    _check(lib().oakg_ens_analysis(ctypes.byref(dims), pE, ldE, pH, ldH,
+                                   A.vec(yo, n=m, name="yo"), A.vec(r_diag, n=m, name="r_diag"),
+                                   A.mat(Ea, n, N, "Ea")[0], A.vec(xa, name="xa"),
+                                   A.vec(ampl, name="ampl")))
+    return Ea, xa, ampl
+
+
+def biased_loc_analysis(gamma, zone_size, xf, bf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos,
+                        corr_len, max_len, H_index, H_weight, *, H_shift=None,
+                        weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1, localise_obs=True,
+                        rotate=True, precision=PREC_FP64, want_sa=True):
+    """Bias-aware local analysis (oakg_biased_locanalysis, biasedLocAnalysis of
+    rrsqrt.F90:476-546) with the sparse observation operator (H_index, H_weight, H_shift).
+    Returns ``(xa, ba, Sa)`` (Sa = Sf, or None without ``want_sa``)."""
+    Z = int(zone_size.shape[0])
+    n, N = int(xf.shape[0]), int(Sf.shape[1])
+    m = int(yo.shape[0])
+    ox, oy, oz, ot = (tuple(obs_pos) + (None,) * 4)[:4]
+    device = _device_mode(zone_size, xf, bf, Hxf, yo, Sf, HSf, r_diag, zone_pos, corr_len,
+                          max_len, H_weight, ox, oy, oz, ot)
+    A = _Args(device)
+    pSf, ldS = A.mat(Sf, n, N, "Sf")
+    pHS, ldH = A.mat(HSf, m, N, "HSf")
+    H = _obsoper(A, H_index, H_weight, H_shift, m)
+    dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
+    loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
+              rotate=int(bool(rotate)), precision=int(precision), flags=0, cell_size=0.0)
+    zp = zone_pos.reshape(-1) if device else np.ascontiguousarray(
+        np.asarray(zone_pos, dtype=np.float64).reshape(Z, 4))
+    xa = _empty_like_mode(device, (n,), like=Sf)
+    ba = _empty_like_mode(device, (n,), like=Sf)
+    Sa = _empty_like_mode(device, (n, N), order="F", like=Sf) if want_sa else None
+    if device and want_sa and ldS != n:
+        raise OakError(ERR_ARGS, "device Sf with ld != n is not supported by this wrapper")
+    _sync_torch(device, Sf)
+    rc = lib().oakg_biased_locanalysis(
+        ctypes.byref(dims), ctypes.byref(loc), Z, A.vec(zone_size, np.int32, "zone_size", Z),
+        float(gamma), None if H is None else ctypes.byref(H), A.vec(xf, n=n, name="xf"),
+        A.vec(bf, n=n, name="bf"), A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"), pSf,
+        pHS, A.vec(r_diag, n=m, name="r_diag"), A.vec(zp, n=4 * Z, name="zone_pos"),
+        A.vec(ox, n=m, name="obs_x"), A.vec(oy, n=m, name="obs_y"), A.vec(oz, n=m, name="obs_z"),
+        A.vec(ot, n=m, name="obs_t"), A.vec(corr_len, n=Z, name="corr_len"),
+        A.vec(max_len, n=Z, name="max_len"), A.vec(xa, name="xa"), A.vec(ba, name="ba"),
+        None if Sa is None else A.mat(Sa, n, N, "Sa")[0])
+    _check(rc)
+    return xa, ba, Sa
 
 
 class Plan:

@@ -6,6 +6,8 @@
 //   epilogue  S_a = mult S_a                                   (inflation, :3299-3304)
 //             x_a clipped to x_f +- maxCorrection              (:3305-3312)
 //             E_a(:,k) = x_a + scaling S_a(:,k)                 (:3558-3565)
+// and the ensemble conversions of rrsqrt.F90 (ens2sqrt, sqrt2ens: N <-> N - 1 columns) and the
+// elementwise steps of the bias-aware analysis (biasedLocAnalysis).
 // The observation operator is the reference's sparse interpolation matrix H (m x n, a few
 // non-zeros per row: nearest cell, n-linear), stored row-wise as K (index, weight) pairs per
 // observation; a negative index marks an unused pair.
@@ -83,7 +85,120 @@ __global__ void k_epilogue(int64_t n, int N, const double* __restrict__ xf,
   }
 }
 
+// Pham's reduction of an ensemble to N - 1 anomaly columns (ens2sqrt, rrsqrt.F90:786-806):
+//   alpha = (sqrt(N) - 1) / (N - 1), shift = (1 - alpha) mean + alpha E(:, N),
+//   S(:, i) = (E(:, i) - shift) / sqrt(N - 1), i < N
+__global__ void k_ens2sqrt(int64_t rows, int N, const double* __restrict__ E, int64_t ldE,
+                           double* __restrict__ mean, double* __restrict__ S, int64_t ldS) {
+  const double alpha = (-1.0 + sqrt((double)N)) / (N - 1.0);
+  const double isc = 1.0 / sqrt(N - 1.0);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < N; k++) s += E[i + (int64_t)k * ldE];
+    const double mu = s / N;
+    mean[i] = mu;
+    const double shift = (1.0 - alpha) * mu + alpha * E[i + (int64_t)(N - 1) * ldE];
+    for (int k = 0; k < N - 1; k++) S[i + (int64_t)k * ldS] = (E[i + (int64_t)k * ldE] - shift) * isc;
+  }
+}
+
+// sqrt2ens (rrsqrt.F90:815-839): E(i, j) = mean(i) + sum_k S(i, k) Om(j, k), Om (N x N-1,
+// row-major, staged in shared memory); a block takes tiles of kRowsE rows, the S tile staged
+// column by column (coalesced along rows), one thread per (row, member) item
+constexpr int kRowsE = 64;
+__global__ void __launch_bounds__(kThreads)
+    k_sqrt2ens(int64_t rows, int N, const double* __restrict__ mean, const double* __restrict__ S,
+               int64_t ldS, const double* __restrict__ Om, double* __restrict__ E, int64_t ldE) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  double* so = reinterpret_cast<double*>(dyn_raw);  // [N][N-1]
+  double* st = so + N * (N - 1);                    // [N-1][kRowsE]
+  const int K = N - 1;
+  for (int idx = threadIdx.x; idx < N * K; idx += kThreads) so[idx] = Om[idx];
+  const int64_t ntiles = (rows + kRowsE - 1) / kRowsE;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t r0 = t * kRowsE;
+    const int R_ = (int)((rows - r0) < kRowsE ? (rows - r0) : kRowsE);
+    __syncthreads();  // Om staged / previous tile consumed
+    for (int idx = threadIdx.x; idx < R_ * K; idx += kThreads) {
+      const int k = idx / R_, r = idx - k * R_;
+      st[k * kRowsE + r] = S[r0 + r + (int64_t)k * ldS];
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < R_ * N; it += kThreads) {
+      const int j = it / R_, r = it - j * R_;
+      const double* oj = so + j * K;
+      double acc = 0.0;
+      for (int k = 0; k < K; k++) acc = fma(st[k * kRowsE + r], oj[k], acc);
+      E[r0 + r + (int64_t)j * ldE] = mean[r0 + r] + acc;
+    }
+  }
+}
+
+// the elementwise steps of the bias-aware analysis (rrsqrt.F90:520-540):
+//   ba = bf - gamma inc, ux = xf - ba
+__global__ void k_bias_update(int64_t n, double gamma, const double* __restrict__ bf,
+                              const double* __restrict__ inc, const double* __restrict__ xf,
+                              double* __restrict__ ba, double* __restrict__ ux) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double b = bf[i] - gamma * inc[i];
+    ba[i] = b;
+    ux[i] = xf[i] - b;
+  }
+}
+
+// y = a x + b z (any of b, z may be absent: y = a x)
+__global__ void k_axpby(int64_t n, double a, const double* __restrict__ x, double b,
+                        const double* __restrict__ z, double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = z ? fma(b, z[i], a * x[i]) : a * x[i];
+}
+
 }  // namespace
+
+cudaError_t ensemble_ens2sqrt(int64_t n, int N, const double* E, int64_t ldE, double* mean,
+                              double* S, int64_t ldS, cudaStream_t st) {
+  k_ens2sqrt<<<grid_for(n), kThreads, 0, st>>>(n, N, E, ldE, mean, S, ldS);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t ensemble_sqrt2ens(int64_t n, int N, const double* mean, const double* S, int64_t ldS,
+                              const double* Om, double* E, int64_t ldE, cudaStream_t st) {
+  const size_t smem = ((size_t)N * (N - 1) + (size_t)(N - 1) * kRowsE) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_sqrt2ens, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int64_t tiles = (n + kRowsE - 1) / kRowsE;
+  const int grid = (int)(tiles < 152 * 4 ? (tiles < 1 ? 1 : tiles) : 152 * 4);
+  k_sqrt2ens<<<grid, kThreads, smem, st>>>(n, N, mean, S, ldS, Om, E, ldE);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t obsoper_apply(int64_t m, int K, const int64_t* idx, const double* w,
+                          const double* shift, const double* x, int64_t ldx, double* y,
+                          cudaStream_t st) {
+  k_obsoper<<<grid_for(m), kThreads, 0, st>>>(m, 1, K, idx, w, shift, x, ldx, y, m);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t bias_update(int64_t n, double gamma, const double* bf, const double* inc,
+                        const double* xf, double* ba, double* ux, cudaStream_t st) {
+  k_bias_update<<<grid_for(n), kThreads, 0, st>>>(n, gamma, bf, inc, xf, ba, ux);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t axpby(int64_t n, double a, const double* x, double b, const double* z, double* y,
+                  cudaStream_t st) {
+  k_axpby<<<grid_for(n), kThreads, 0, st>>>(n, a, x, b, z, y);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t ensemble_prologue(int64_t n, int N, const double* Ef, int64_t ldE, int64_t m, int K,
                               const int64_t* idx, const double* w, const double* shift,

@@ -70,7 +70,8 @@ enum BufId {
   B_MAXL, B_XA, B_SA, B_AMPL, B_NOBS, B_ZSTART, B_SMALL, B_CELL, B_COUNT, B_CSTART, B_POS,
   B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_OBS32, B_E_EF, B_E_HIDX, B_E_HW, B_E_HSH, B_E_HEF, B_E_XF, B_E_SF,
   B_E_HXF, B_E_HSF, B_E_XA, B_E_SA, B_E_MC, B_E_EA, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
-  B_ORDER, B_COUNT_
+  B_ORDER, B_C_E, B_C_MEAN, B_C_S, B_C_OM, B_C_EO, B_C_HE, B_C_HXF, B_C_HSF, B_C_XA, B_C_SA,
+  B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_COUNT_
 };
 
 struct Ctx {
@@ -1222,6 +1223,245 @@ int ens_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
   return OAKG_OK;
 }
 
+// ens2sqrt (rrsqrt.F90:786-806): mean and the N - 1 anomaly columns of Pham's reduction
+int ens2sqrt_impl(const oakg_dims* d, const double* E, int64_t ldE, double* mean, double* S) {
+  int rc = check_dims(d);
+  if (rc) return rc;
+  if (!E || !mean || !S) return fail(OAKG_ERR_ARGS, "E, mean and S are required");
+  if (ldE < d->n) return fail(OAKG_ERR_ARGS, "ldE < n");
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t n = d->n;
+  const int N = d->N, mem = d->mem;
+  const double* dE;
+  double *dmean, *dS;
+  if ((rc = stage_in(c, B_C_E, E, (size_t)ldE * N, mem, &dE, "E")) ||
+      (rc = stage_out(c, B_C_MEAN, mean, (size_t)n, mem, &dmean, "mean")) ||
+      (rc = stage_out(c, B_C_S, S, (size_t)d->ldS * (N - 1), mem, &dS, "S")))
+    return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = ensemble_ens2sqrt(n, N, dE, ldE, dmean, dS, d->ldS, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST) {
+    e = cudaMemcpyAsync(mean, dmean, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(S, dS, (size_t)d->ldS * (N - 1) * sizeof(double),
+                          cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "ens2sqrt");
+  return OAKG_OK;
+}
+
+// sqrt2ens (rrsqrt.F90:815-839): E = mean + S Om^T, Om = sqrt(N-1) perpSpace(w) Theta, w = 1/sqrt(N)
+// (perpSpace: matoper.F90:509-535). The reference draws Theta at random (randOrthMatrix);
+// here it is the caller's (N-1) x (N-1) orthogonal matrix, or the identity.
+int sqrt2ens_impl(const oakg_dims* d, const double* mean, const double* S, const double* theta,
+                  double* E, int64_t ldE) {
+  int rc = check_dims(d);
+  if (rc) return rc;
+  if (!mean || !S || !E) return fail(OAKG_ERR_ARGS, "mean, S and E are required");
+  if (ldE < d->n) return fail(OAKG_ERR_ARGS, "ldE < n");
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t n = d->n;
+  const int N = d->N, K = N - 1, mem = d->mem;
+  cudaStream_t st = c->stream;
+  cudaError_t e = cudaSuccess;
+  std::vector<double> th((size_t)K * K, 0.0), om((size_t)N * K, 0.0), P((size_t)N * K, 0.0);
+  if (theta) {
+    e = cudaMemcpy(th.data(), theta, th.size() * sizeof(double),
+                   mem == OAKG_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "theta");
+  } else {
+    for (int i = 0; i < K; i++) th[(size_t)i * K + i] = 1.0;
+  }
+  const double w = 1.0 / std::sqrt((double)N), alpha = -1.0 / (w + 1.0);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < K; j++)
+      P[(size_t)i * K + j] = (i < K) ? alpha * w * w + (i == j ? 1.0 : 0.0) : alpha * (w + 1.0) * w;
+  const double sc = std::sqrt((double)N - 1.0);
+  for (int i = 0; i < N; i++)
+    for (int k = 0; k < K; k++) {
+      double acc = 0.0;
+      for (int l = 0; l < K; l++) acc += P[(size_t)i * K + l] * th[(size_t)l + (size_t)k * K];
+      om[(size_t)i * K + k] = sc * acc;
+    }
+  double* dOm;
+  if ((rc = scratch(c, B_C_OM, om.size(), &dOm, "Omega"))) return rc;
+  const double *dmean, *dS;
+  double* dE;
+  if ((rc = stage_in(c, B_C_MEAN, mean, (size_t)n, mem, &dmean, "mean")) ||
+      (rc = stage_in(c, B_C_S, S, (size_t)d->ldS * K, mem, &dS, "S")) ||
+      (rc = stage_out(c, B_C_EO, E, (size_t)ldE * N, mem, &dE, "E")))
+    return rc;
+  e = cudaMemcpyAsync(dOm, om.data(), om.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = ensemble_sqrt2ens(n, N, dmean, dS, d->ldS, dOm, dE, ldE, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(E, dE, (size_t)ldE * N * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // also keeps om alive for the copy
+  if (e != cudaSuccess) return cuda_fail(e, "sqrt2ens");
+  return OAKG_OK;
+}
+
+// ensAnalysis (rrsqrt.F90:613-671): mean and scaled anomalies of Ef and HEf, the global
+// analysis, Ea = xa + sqrt(N-1) Sa
+int ens_analysis_impl(const oakg_dims* d, const double* Ef, int64_t ldE, const double* HEf,
+                      int64_t ldHE, const double* yo, const double* r_diag, double* Ea,
+                      double* xa, double* ampl) {
+  int rc = check_dims(d);
+  if (rc) return rc;
+  if (!Ef || !Ea) return fail(OAKG_ERR_ARGS, "Ef and Ea are required");
+  if (ldE < d->n) return fail(OAKG_ERR_ARGS, "ldE < n");
+  if (d->m > 0 && (!HEf || !yo || !r_diag || ldHE < d->m))
+    return fail(OAKG_ERR_ARGS, "HEf (ldHE >= m), yo and r_diag are required when m > 0");
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t n = d->n, m = d->m;
+  const int N = d->N, mem = d->mem;
+  cudaStream_t st = c->stream;
+  const double *dEf, *dHE = nullptr, *dyo = nullptr, *dr = nullptr;
+  double *xf, *Sf, *Hxf, *HSf, *dxa, *Sa, *dEa, *dampl;
+  if ((rc = stage_in(c, B_C_E, Ef, (size_t)ldE * N, mem, &dEf, "Ef")) ||
+      (rc = stage_in(c, B_C_HE, HEf, (size_t)(m > 0 ? ldHE : 0) * N, mem, &dHE, "HEf")) ||
+      (rc = stage_in(c, B_YO, m > 0 ? yo : nullptr, (size_t)m, mem, &dyo, "yo")) ||
+      (rc = stage_in(c, B_R, m > 0 ? r_diag : nullptr, (size_t)m, mem, &dr, "r_diag")) ||
+      (rc = scratch(c, B_C_MEAN, (size_t)n, &xf, "xf")) ||
+      (rc = scratch(c, B_C_S, (size_t)n * N, &Sf, "Sf")) ||
+      (rc = scratch(c, B_C_HXF, (size_t)(m > 0 ? m : 1), &Hxf, "Hxf")) ||
+      (rc = scratch(c, B_C_HSF, (size_t)(m > 0 ? m : 1) * N, &HSf, "HSf")) ||
+      (rc = scratch(c, B_C_XA, (size_t)n, &dxa, "xa")) ||
+      (rc = scratch(c, B_C_SA, (size_t)n * N, &Sa, "Sa")) ||
+      (rc = stage_out(c, B_C_EO, Ea, (size_t)ldE * N, mem, &dEa, "Ea")) ||
+      (rc = stage_out(c, B_C_AMPL, ampl, (size_t)N, mem, &dampl, "amplitudes")))
+    return rc;
+  // the prologue's mean/anomaly kernel on Ef and on HEf (no operator: HEf is given)
+  cudaError_t e = ensemble_prologue(n, N, dEf, ldE, 0, 1, nullptr, nullptr, nullptr, xf, Sf, n,
+                                    nullptr, nullptr, 1, nullptr, st);
+  if (e == cudaSuccess && m > 0)
+    e = ensemble_prologue(m, N, dHE, ldHE, 0, 1, nullptr, nullptr, nullptr, Hxf, HSf, m,
+                          nullptr, nullptr, 1, nullptr, st);
+  if (e != cudaSuccess) return cuda_fail(e, "ensemble anomalies");
+  oakg_dims dd = *d;
+  dd.mem = OAKG_MEM_DEVICE;
+  dd.ldS = n;
+  dd.ldH = m > 0 ? m : 1;
+  if ((rc = analysis_impl(&dd, xf, m > 0 ? Hxf : nullptr, dyo, Sf, m > 0 ? HSf : nullptr, dr,
+                          dxa, Sa, dampl)))
+    return rc;
+  e = ensemble_epilogue(n, N, xf, dxa, Sa, n, 1.0, nullptr, dEa, ldE, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST) {
+    e = cudaMemcpyAsync(Ea, dEa, (size_t)ldE * N * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && ampl)
+      e = cudaMemcpyAsync(ampl, dampl, N * sizeof(double), cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess && xa)
+    e = cudaMemcpyAsync(xa, dxa, n * sizeof(double),
+                        mem == OAKG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                        st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "ensemble analysis");
+  return OAKG_OK;
+}
+
+// biasedLocAnalysis (rrsqrt.F90:476-546): the bias increment from a first local analysis, the
+// bias ba = bf - gamma inc, the state analysed from xf - ba with R scaled by (1 - gamma)
+// (DCDCovar with D = 1/sqrt(1 - gamma): R^-1 -> R^-1 / (1 - gamma), covariance.F90:611-618);
+// Sa = Sf.
+int biased_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
+                            const int32_t* zone_size, double gamma, const oakg_obsoper* H,
+                            const double* xf, const double* bf, const double* Hxf,
+                            const double* yo, const double* Sf, const double* HSf,
+                            const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                            const double* obs_y, const double* obs_z, const double* obs_t,
+                            const double* corr_len, const double* max_len, double* xa,
+                            double* ba, double* Sa) {
+  int rc = check_loc(d, loc, Z);
+  if (rc) return rc;
+  if (!xf || !bf || !Sf || !xa || !ba) return fail(OAKG_ERR_ARGS, "xf, bf, Sf, xa, ba are required");
+  if (!(gamma >= 0.0 && gamma < 1.0)) return fail(OAKG_ERR_ARGS, "gamma must be in [0, 1)");
+  if ((rc = check_obsoper(H, d->m))) return rc;
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t n = d->n, m = d->m;
+  const int N = d->N, mem = d->mem;
+  cudaStream_t st = c->stream;
+  // device views of the inputs the two analyses share
+  const int32_t* dzs;
+  const double *dxf, *dbf, *dHxf = nullptr, *dyo = nullptr, *dSf, *dHSf = nullptr, *dr = nullptr,
+               *dzp, *dox = nullptr, *doy = nullptr, *doz = nullptr, *dot = nullptr, *dcorr,
+               *dmaxl;
+  if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &dzs, "zone_size")) ||
+      (rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &dzp, "zone_xyzt")) ||
+      (rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &dcorr, "corr_len")) ||
+      (rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &dmaxl, "max_len")) ||
+      (rc = stage_in(c, B_XF, xf, (size_t)n, mem, &dxf, "xf")) ||
+      (rc = stage_in(c, B_C_BF, bf, (size_t)n, mem, &dbf, "bf")) ||
+      (rc = stage_in(c, B_SF, Sf, (size_t)d->ldS * N, mem, &dSf, "Sf")))
+    return rc;
+  oakg_obsoper Hd{};
+  if (m > 0) {
+    if ((rc = stage_in(c, B_HXF, Hxf, (size_t)m, mem, &dHxf, "Hxf")) ||
+        (rc = stage_in(c, B_YO, yo, (size_t)m, mem, &dyo, "yo")) ||
+        (rc = stage_in(c, B_HSF, HSf, (size_t)d->ldH * N, mem, &dHSf, "HSf")) ||
+        (rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &dr, "r_diag")) ||
+        (rc = stage_in(c, B_OX, obs_x, (size_t)m, mem, &dox, "obs_x")) ||
+        (rc = stage_in(c, B_OY, obs_y, (size_t)m, mem, &doy, "obs_y")) ||
+        (rc = stage_in(c, B_OZ, obs_z, (size_t)m, mem, &doz, "obs_z")) ||
+        (rc = stage_in(c, B_OT, obs_t, (size_t)m, mem, &dot, "obs_t")))
+      return rc;
+    Hd = *H;
+    const size_t mk = (size_t)m * H->K;
+    if ((rc = stage_in(c, B_E_HIDX, H->index, mk, mem, &Hd.index, "operator index")) ||
+        (rc = stage_in(c, B_E_HW, H->weight, mk, mem, &Hd.weight, "operator weight")) ||
+        (rc = stage_in(c, B_E_HSH, H->shift, (size_t)m, mem, &Hd.shift, "Hshift")))
+      return rc;
+  }
+  double *zero, *inc, *ux, *uHx = nullptr, *r2 = nullptr, *dba, *dxa, *dSa = nullptr;
+  if ((rc = scratch(c, B_C_ZERO, (size_t)n, &zero, "zeros")) ||
+      (rc = scratch(c, B_C_INC, (size_t)n, &inc, "increment")) ||
+      (rc = scratch(c, B_C_UX, (size_t)n, &ux, "unbiased xf")) ||
+      (rc = stage_out(c, B_C_BA, ba, (size_t)n, mem, &dba, "ba")) ||
+      (rc = stage_out(c, B_C_XA, xa, (size_t)n, mem, &dxa, "xa")) ||
+      (rc = stage_out(c, B_C_SA, Sa, (size_t)d->ldS * N, mem, &dSa, "Sa")))
+    return rc;
+  if (m > 0 && ((rc = scratch(c, B_C_UHX, (size_t)m, &uHx, "unbiased Hxf")) ||
+                (rc = scratch(c, B_C_R2, (size_t)m, &r2, "scaled R"))))
+    return rc;
+  cudaError_t e = cudaMemsetAsync(zero, 0, n * sizeof(double), st);
+  if (e != cudaSuccess) return cuda_fail(e, "zeros");
+  oakg_dims dd = *d;
+  dd.mem = OAKG_MEM_DEVICE;
+  // 1. the bias increment: locAnalysisIncrement with the forecast (xf = 0 gives xa = increment)
+  if ((rc = locanalysis_impl(&dd, loc, Z, dzs, zero, dHxf, dyo, dSf, dHSf, dr, dzp, dox, doy, doz,
+                             dot, dcorr, dmaxl, inc, nullptr, nullptr, nullptr)))
+    return rc;
+  // 2. ba = bf - gamma inc, ux = xf - ba; H ux + Hshift; R (1 - gamma)
+  e = bias_update(n, gamma, dbf, inc, dxf, dba, ux, st);
+  if (e == cudaSuccess && m > 0)
+    e = obsoper_apply(m, Hd.K, Hd.index, Hd.weight, Hd.shift, ux, n, uHx, st);
+  if (e == cudaSuccess && m > 0) e = axpby(m, 1.0 - gamma, dr, 0.0, nullptr, r2, st);
+  if (e != cudaSuccess) return cuda_fail(e, "bias update");
+  // 3. the state increment from the unbiased forecast, xa = ux + increment
+  if ((rc = locanalysis_impl(&dd, loc, Z, dzs, zero, uHx, dyo, dSf, dHSf, r2, dzp, dox, doy, doz,
+                             dot, dcorr, dmaxl, inc, nullptr, nullptr, nullptr)))
+    return rc;
+  e = axpby(n, 1.0, ux, 1.0, inc, dxa, st);
+  if (e == cudaSuccess && dSa && dSa != dSf)
+    e = cudaMemcpy2DAsync(dSa, d->ldS * sizeof(double), dSf, d->ldS * sizeof(double),
+                          n * sizeof(double), N, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST) {
+    e = cudaMemcpyAsync(xa, dxa, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ba, dba, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && Sa)
+      e = cudaMemcpyAsync(Sa, dSa, (size_t)d->ldS * N * sizeof(double), cudaMemcpyDeviceToHost,
+                          st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "bias-aware analysis");
+  return OAKG_OK;
+}
+
 int release_impl() {
   for (auto& cp : g_ctx) {
     if (!cp) continue;
@@ -1454,6 +1694,51 @@ int oakg_ens_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzo
   int rc = oakg::ens_locanalysis_impl(dims, loc, nzones, zone_size, Ef, ldE, H, yo, r_diag,
                                       zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len,
                                       inflation, max_correction, Ea);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_ens2sqrt(const oakg_dims* dims, const double* E, int64_t ldE, double* mean,
+                  double* S) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::ens2sqrt_impl(dims, E, ldE, mean, S);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_sqrt2ens(const oakg_dims* dims, const double* mean, const double* S,
+                  const double* theta, double* E, int64_t ldE) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::sqrt2ens_impl(dims, mean, S, theta, E, ldE);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_ens_analysis(const oakg_dims* dims, const double* Ef, int64_t ldE, const double* HEf,
+                      int64_t ldHE, const double* yo, const double* r_diag, double* Ea,
+                      double* xa, double* ampl) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::ens_analysis_impl(dims, Ef, ldE, HEf, ldHE, yo, r_diag, Ea, xa, ampl);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_biased_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                            const int32_t* zone_size, double gamma, const oakg_obsoper* H,
+                            const double* xf, const double* bf, const double* Hxf,
+                            const double* yo, const double* Sf, const double* HSf,
+                            const double* r_diag, const double* zone_xyzt, const double* obs_x,
+                            const double* obs_y, const double* obs_z, const double* obs_t,
+                            const double* corr_len, const double* max_len, double* xa,
+                            double* ba, double* Sa) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::biased_locanalysis_impl(dims, loc, nzones, zone_size, gamma, H, xf, bf, Hxf, yo,
+                                         Sf, HSf, r_diag, zone_xyzt, obs_x, obs_y, obs_z, obs_t,
+                                         corr_len, max_len, xa, ba, Sa);
   oakg::last_status() = rc;
   return rc;
 }

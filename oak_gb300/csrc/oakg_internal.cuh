@@ -146,6 +146,20 @@ cudaError_t ensemble_prologue(int64_t n, int N, const double* Ef, int64_t ldE, i
                               const int64_t* idx, const double* w, const double* shift,
                               double* xf, double* Sf, int64_t ldS, double* Hxf, double* HSf,
                               int64_t ldH, double* HEf_scratch, cudaStream_t st);
+// ens2sqrt: mean and N - 1 anomaly columns of an ensemble; sqrt2ens: E = mean + S Om^T with
+// Om (N x N-1, row-major); the bias-aware steps ba = bf - gamma inc, ux = xf - ba; y = a x + b z.
+cudaError_t ensemble_ens2sqrt(int64_t n, int N, const double* E, int64_t ldE, double* mean,
+                              double* S, int64_t ldS, cudaStream_t st);
+cudaError_t ensemble_sqrt2ens(int64_t n, int N, const double* mean, const double* S, int64_t ldS,
+                              const double* Om, double* E, int64_t ldE, cudaStream_t st);
+// y = H x + shift for one state vector (the sparse operator of ensemble_prologue)
+cudaError_t obsoper_apply(int64_t m, int K, const int64_t* idx, const double* w,
+                          const double* shift, const double* x, int64_t ldx, double* y,
+                          cudaStream_t st);
+cudaError_t bias_update(int64_t n, double gamma, const double* bf, const double* inc,
+                        const double* xf, double* ba, double* ux, cudaStream_t st);
+cudaError_t axpby(int64_t n, double a, const double* x, double b, const double* z, double* y,
+                  cudaStream_t st);
 cudaError_t ensemble_epilogue(int64_t n, int N, const double* xf, const double* xa,
                               const double* Sa, int64_t ldS, double inflation,
                               const double* maxcorr, double* Ea, int64_t ldE, cudaStream_t st);

@@ -265,3 +265,78 @@ def kalman_reference(xf, Sf, H, yo, R):
     Pa = Pf - K @ (H @ Pf)
     xa = xf + K @ (yo - H @ xf)
     return xa, Pa
+
+
+def ens2sqrt(E):
+    """Mean and N - 1 anomaly columns of an ensemble (ens2sqrt, rrsqrt.F90:786-806, Pham 2001).
+
+    Returns ``(mean, S)`` with ``S S^T`` the ensemble covariance.
+    """
+    E = np.asarray(E, dtype=np.float64)
+    N = E.shape[1]
+    mean = E.sum(axis=1) / N
+    alpha = (-1.0 + math.sqrt(1.0 * N)) / (N - 1)
+    shift = (1.0 - alpha) * mean + alpha * E[:, N - 1]
+    S = (E[:, : N - 1] - shift[:, None]) / math.sqrt(N - 1.0)
+    return mean, S
+
+
+def sqrt2ens(mean, S, theta=None):
+    """Ensemble with the given mean and covariance ``S S^T`` (sqrt2ens, rrsqrt.F90:815-839):
+    ``E = mean + S Om^T``, ``Om = sqrt(N-1) perpSpace(w) theta``, ``w = 1/sqrt(N)``.
+
+    The reference draws ``theta`` with ``randOrthMatrix(N-1)``; it is an argument here (the
+    identity if None).
+    """
+    S = np.asarray(S, dtype=np.float64)
+    K = S.shape[1]
+    N = K + 1
+    w = np.full(N, 1.0 / math.sqrt(1.0 * N))
+    th = np.eye(K) if theta is None else np.asarray(theta, dtype=np.float64)
+    Om = math.sqrt(N - 1.0) * (perp_space(w) @ th)
+    return np.asarray(mean, dtype=np.float64)[:, None] + S @ Om.T
+
+
+def ens_analysis(Ef, HEf, yo, r_diag, rotate=True):
+    """Global analysis of an ensemble (ensAnalysis, rrsqrt.F90:613-671): mean and scaled
+    anomalies of Ef and HEf, ``analysis``, ``Ea = xa + sqrt(N-1) Sa``.
+
+    Returns ``(Ea, xa, amplitudes)``.
+    """
+    xf, Hxf, Sf, HSf = ensemble_prologue(np.asarray(Ef, dtype=np.float64),
+                                         np.asarray(HEf, dtype=np.float64))
+    xa, Sa, ampl = analysis(xf, Hxf, yo, Sf, HSf, r_diag, rotate)
+    N = Sf.shape[1]
+    return xa[:, None] + math.sqrt(N - 1.0) * Sa, xa, ampl
+
+
+def sparse_apply(H_index, H_weight, x, shift=None):
+    """``H x + shift`` for the operator given as K (index, weight) pairs per row (a negative
+    index marks an unused pair): the SparseMatrix product of matoper_inc.F90:220-242."""
+    idx = np.asarray(H_index)
+    w = np.asarray(H_weight, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    y = np.where(idx >= 0, w * x[np.maximum(idx, 0)], 0.0).sum(axis=1)
+    return y if shift is None else y + np.asarray(shift, dtype=np.float64)
+
+
+def biased_loc_analysis(gamma, zone_size, select, H_index, H_weight, Hshift, xf, bf, Hxf, yo,
+                        Sf, HSf, r_diag, localise_obs=True, rotate=True):
+    """Bias-aware local analysis (biasedLocAnalysis, rrsqrt.F90:476-546).
+
+    The bias increment is the local analysis increment of (Hxf, yo, Sf, HSf, R);
+    ``ba = bf - gamma inc``; the unbiased forecast ``xf - ba`` is analysed with
+    ``H (xf - ba) + Hshift`` and R scaled by (1 - gamma) (``DCDCovar`` with
+    ``D = 1/sqrt(1 - gamma)``: ``mldivide(x) = D C^-1 (D x)``, covariance.F90:611-618);
+    ``Sa = Sf``. Returns ``(xa, ba, Sa)``.
+    """
+    zeros = np.zeros_like(np.asarray(xf, dtype=np.float64))
+    inc, _, _, _ = loc_analysis(zone_size, select, zeros, Hxf, yo, Sf, HSf, r_diag,
+                                localise_obs, rotate)
+    ba = np.asarray(bf, dtype=np.float64) - gamma * inc
+    ux = np.asarray(xf, dtype=np.float64) - ba
+    uHx = sparse_apply(H_index, H_weight, ux, Hshift)
+    inc2, _, _, _ = loc_analysis(zone_size, select, zeros, uHx, yo, Sf, HSf,
+                                 (1.0 - gamma) * np.asarray(r_diag, dtype=np.float64),
+                                 localise_obs, rotate)
+    return ux + inc2, ba, np.asarray(Sf, dtype=np.float64).copy()

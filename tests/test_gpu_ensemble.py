@@ -72,3 +72,65 @@ def test_ensemble_local_analysis_matches_oracle(oakg, device):
                                     c.obs_pos, c.corr_len, c.max_len, kind=c.weight)
     Ea_o = oakref.ensemble_epilogue(xf, xa, Sa, inflation=1.05, max_correction=mc)
     assert np.linalg.norm(Ea - Ea_o) <= 1e-10 * np.linalg.norm(Ea_o - c.Ef)
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_ens2sqrt_sqrt2ens_match_oracle(oakg, device):
+    rng = np.random.default_rng(21)
+    n, N = 3000, 33
+    E = np.asfortranarray(rng.standard_normal((n, N)))
+    theta, _ = np.linalg.qr(rng.standard_normal((N - 1, N - 1)))
+    theta = np.asfortranarray(theta)
+    mean_o, S_o = oakref.ens2sqrt(E)
+    if device:
+        import torch
+        T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda:0")
+        F = lambda a: torch.as_tensor(np.ascontiguousarray(np.asarray(a).T), device="cuda:0").t()
+        mean, S = oakg.ens2sqrt(F(E))
+        mean, S = mean.cpu().numpy(), S.cpu().numpy()
+        E2 = oakg.sqrt2ens(T(mean_o), F(S_o), F(theta)).cpu().numpy()
+    else:
+        mean, S = oakg.ens2sqrt(E)
+        E2 = oakg.sqrt2ens(mean_o, S_o, theta)
+    assert np.allclose(mean, mean_o, rtol=1e-14, atol=1e-14)
+    assert np.allclose(S, S_o, rtol=1e-13, atol=1e-13)
+    E2_o = oakref.sqrt2ens(mean_o, S_o, theta)
+    assert np.allclose(E2, E2_o, rtol=1e-12, atol=1e-12)
+    if not device:  # theta = identity
+        assert np.allclose(oakg.sqrt2ens(mean_o, S_o), oakref.sqrt2ens(mean_o, S_o),
+                           rtol=1e-12, atol=1e-12)
+
+
+def test_ens_analysis_matches_oracle(oakg):
+    rng = np.random.default_rng(22)
+    n, N, m = 4000, 30, 300
+    Ef = np.asfortranarray(rng.standard_normal((n, N)))
+    idx = rng.choice(n, m, replace=False)
+    HEf = np.asfortranarray(Ef[idx] + 0.01 * rng.standard_normal((m, N)))
+    yo = HEf.mean(axis=1) + 0.3 * rng.standard_normal(m)
+    r = rng.uniform(0.05, 0.2, m)
+    Ea, xa, ampl = oakg.ens_analysis(Ef, HEf, yo, r)
+    Ea_o, xa_o, ampl_o = oakref.ens_analysis(Ef, HEf, yo, r)
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(xa, xa_o) < 1e-10 and rel(Ea, Ea_o) < 1e-10 and rel(ampl, ampl_o) < 1e-10
+
+
+@pytest.mark.parametrize("gamma", [0.0, 0.35])
+def test_biased_local_analysis_matches_oracle(oakg, gamma):
+    rng = np.random.default_rng(23)
+    c = local_case(scale=1 / 12, N=24, keep_ensemble=True)
+    index, weight, shift, H = _sparse_operator(c, rng)
+    Hxf = H @ c.xf + shift
+    HSf = np.asfortranarray(H @ c.Sf)
+    bf = 0.05 * rng.standard_normal(c.n)
+    xa, ba, Sa = oakg.biased_loc_analysis(gamma, c.zone_size, c.xf, bf, Hxf, c.yo, c.Sf, HSf,
+                                          c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                          c.max_len, index, weight, H_shift=shift,
+                                          weight=c.weight)
+    sel = oakref.geometric_selector(c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                    kind=c.weight)
+    xa_o, ba_o, _ = oakref.biased_loc_analysis(gamma, c.zone_size, sel, index, weight, shift,
+                                               c.xf, bf, Hxf, c.yo, c.Sf, HSf, c.r_diag)
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(ba, ba_o) < 1e-10 and rel(xa, xa_o) < 1e-10
+    assert np.array_equal(Sa, c.Sf)

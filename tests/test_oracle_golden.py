@@ -173,3 +173,78 @@ def test_rotation_preserves_zero_sum_anomalies():
     xf, Hxf, Sf, HSf = oakref.ensemble_prologue(E, HE)
     xa, Sa, _ = oakref.analysis(xf, Hxf, rng.standard_normal(m), Sf, HSf, np.full(m, 0.5))
     assert np.max(np.abs(Sa.sum(axis=1))) < 1e-12
+
+
+def test_ens2sqrt_sqrt2ens_identities():
+    """test/assimtest2.F90:65-103: Ef(jmax = 5, kmax + 1 = 3) = sin(1..15) (column-major);
+    ens2sqrt gives S with S S^T = enscov(Ef) and the ensemble mean; sqrt2ens gives back an
+    ensemble with that covariance and mean (for any orthogonal theta: the reference draws it
+    at random)."""
+    jmax, N = 5, 3
+    Ef = np.sin(np.arange(1, jmax * N + 1, dtype=np.float64)).reshape(N, jmax).T.copy()
+    cov = np.cov(Ef)
+    mean, S = oakref.ens2sqrt(Ef)
+    assert S.shape == (jmax, N - 1)
+    assert np.max(np.abs(S @ S.T - cov)) < 1e-14
+    assert np.max(np.abs(mean - Ef.mean(axis=1))) < 1e-15
+    rng = np.random.default_rng(7)
+    theta, _ = np.linalg.qr(rng.standard_normal((N - 1, N - 1)))
+    for th in (None, theta):
+        Ea = oakref.sqrt2ens(mean, S, th)
+        assert np.max(np.abs(np.cov(Ea) - cov)) < 1e-14
+        assert np.max(np.abs(Ea.mean(axis=1) - mean)) < 1e-14
+
+
+def test_ens_analysis_equals_kalman():
+    """ensAnalysis (rrsqrt.F90:613-671) on the test_assim.F90 case: the analysed ensemble's mean
+    and covariance are the Kalman ones."""
+    n, N, m = 18, 10, 1
+    i = np.arange(1, n * N + 1, dtype=np.float64)
+    Ef = np.sin(3.0 * i).reshape(N, n).T.copy()
+    H = np.zeros((m, n))
+    H[0, 4] = 1.0
+    yo, R = np.ones(m), 2.0 * np.eye(m)
+    Pf = np.cov(Ef)
+    K = Pf @ H.T @ np.linalg.inv(H @ Pf @ H.T + R)
+    xf = Ef.mean(axis=1)
+    Ea, xa, _ = oakref.ens_analysis(Ef, H @ Ef, yo, np.diag(R))
+    assert np.max(np.abs(xa - (xf + K @ (yo - H @ xf)))) < 1e-12
+    assert np.max(np.abs(Ea.mean(axis=1) - xa)) < 1e-12
+    assert np.max(np.abs(np.cov(Ea) - (Pf - K @ H @ Pf))) < 1e-12
+
+
+def test_biased_analysis_reduces_to_plain_and_scales_r():
+    """biasedLocAnalysis (rrsqrt.F90:476-546): with gamma = 0 and no prior bias it is the plain
+    local analysis (H xf + Hshift = Hxf); with gamma > 0 the second pass is the plain analysis
+    of the unbiased forecast with R (1 - gamma), and ba = bf - gamma (first-pass increment)."""
+    rng = np.random.default_rng(5)
+    n, N, m, Z = 40, 8, 25, 10
+    zone_size = np.full(Z, n // Z)
+    idx = np.stack([rng.integers(0, n, m), rng.integers(0, n, m)], 1)
+    idx[::4, 1] = -1
+    w = rng.uniform(0.2, 0.8, (m, 2))
+    shift = 0.1 * rng.standard_normal(m)
+    xf = rng.standard_normal(n)
+    Sf = rng.standard_normal((n, N))
+    Hxf = oakref.sparse_apply(idx, w, xf, shift)
+    HSf = np.stack([oakref.sparse_apply(idx, w, Sf[:, k]) for k in range(N)], 1)
+    yo = Hxf + rng.standard_normal(m)
+    r = rng.uniform(0.5, 2.0, m)
+    zone_pos = np.column_stack([np.arange(Z), np.zeros(Z), np.zeros(Z), np.zeros(Z)]) * 1.0
+    obs_pos = (rng.uniform(0, Z, m), np.zeros(m), np.zeros(m), np.zeros(m))
+    sel = oakref.geometric_selector(zone_pos, obs_pos, np.full(Z, 2.0), np.full(Z, 4.0),
+                                    kind=oakref.GASPARI_COHN)
+    xa0, Sa0, _, _ = oakref.loc_analysis(zone_size, sel, xf, Hxf, yo, Sf, HSf, r)
+    xa, ba, Sa = oakref.biased_loc_analysis(0.0, zone_size, sel, idx, w, shift, xf,
+                                            np.zeros(n), Hxf, yo, Sf, HSf, r)
+    assert np.max(np.abs(xa - xa0)) < 1e-12 and np.max(np.abs(ba)) == 0.0
+    assert np.array_equal(Sa, Sf)
+    g, bf = 0.3, 0.2 * rng.standard_normal(n)
+    xa, ba, _ = oakref.biased_loc_analysis(g, zone_size, sel, idx, w, shift, xf, bf, Hxf, yo, Sf,
+                                           HSf, r)
+    inc = oakref.loc_analysis(zone_size, sel, np.zeros(n), Hxf, yo, Sf, HSf, r)[0]
+    assert np.max(np.abs(ba - (bf - g * inc))) < 1e-14
+    ux = xf - ba
+    xa2 = oakref.loc_analysis(zone_size, sel, ux, oakref.sparse_apply(idx, w, ux, shift), yo, Sf,
+                              HSf, (1 - g) * r)[0]
+    assert np.max(np.abs(xa - xa2)) < 1e-12
