@@ -193,6 +193,26 @@ int oakg_ensemble_epilogue(const oakg_dims* dims, const double* xf, const double
                            const double* Sa, double inflation, const double* max_correction,
                            double* Ea, int64_t ldE);
 
+/* The local and global analyses with the non-diagonal observation error covariance of the
+ * SMWCovar kind (covariance.F90:464-570): R = diag(r_diag) + B B^T, B (m x k, leading
+ * dimension ldB, host or device per dims->mem). As in the reference, the zone covariance is R
+ * packed to the zone's relevant observations with the localisation weights outside
+ * (DCDCovar(w, R), rrsqrt.F90:395), solved by Sherman-Morrison-Woodbury with the k x k matrix
+ * of the packed rows. FP64 form only (loc->precision = OAKG_PREC_FP64); N + k <= 128. Other
+ * arguments and results as for oakg_locanalysis / oakg_analysis. */
+int oakg_locanalysis_smw(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                         const int32_t* zone_size, const double* xf, const double* Hxf,
+                         const double* yo, const double* Sf, const double* HSf,
+                         const double* r_diag, int32_t k, const double* B, int64_t ldB,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, double* xa, double* Sa, double* ampl,
+                         int32_t* nobs);
+int oakg_analysis_smw(const oakg_dims* dims, const double* xf, const double* Hxf,
+                      const double* yo, const double* Sf, const double* HSf,
+                      const double* r_diag, int32_t k, const double* B, int64_t ldB, double* xa,
+                      double* Sa, double* ampl);
+
 /* ens2sqrt (rrsqrt.F90:786-806, Pham 2001): the mean (n) and N - 1 anomaly columns
  * S (dims->ldS x (N-1)) of the ensemble E (n x N, leading dimension ldE):
  * alpha = (sqrt(N) - 1)/(N - 1), shift = (1 - alpha) mean + alpha E(:,N),

@@ -86,6 +86,13 @@ def lib() -> ctypes.CDLL:
     L.oakg_analysis.restype = ctypes.c_int
     L.oakg_locanalysis.argtypes = [ctypes.POINTER(Dims), ctypes.POINTER(Loc), ctypes.c_int32] + [P] * 18
     L.oakg_locanalysis.restype = ctypes.c_int
+    L.oakg_locanalysis_smw.argtypes = ([ctypes.POINTER(Dims), ctypes.POINTER(Loc),
+                                        ctypes.c_int32] + [P] * 7 + [ctypes.c_int32, P,
+                                                                     ctypes.c_int64] + [P] * 11)
+    L.oakg_locanalysis_smw.restype = ctypes.c_int
+    L.oakg_analysis_smw.argtypes = ([ctypes.POINTER(Dims)] + [P] * 6
+                                    + [ctypes.c_int32, P, ctypes.c_int64] + [P] * 3)
+    L.oakg_analysis_smw.restype = ctypes.c_int
     L.oakg_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.oakg_last_error.restype = ctypes.c_size_t
     L.oakg_last_status.argtypes = []
@@ -249,8 +256,9 @@ def _sync_torch(device: bool, ref) -> None:
 
 # ----------------------------------------------------------------------------- entry points
 
-def analysis(xf, Hxf, yo, Sf, HSf, r_diag, *, want_sa=True, out=None):
-    """Global analysis (rrsqrt.F90:196-208) with diagonal R = diag(r_diag).
+def analysis(xf, Hxf, yo, Sf, HSf, r_diag, *, want_sa=True, out=None, smw_B=None):
+    """Global analysis (rrsqrt.F90:196-208) with diagonal R = diag(r_diag), or with
+    R = diag(r_diag) + B B^T (SMWCovar, covariance.F90:464-570) when ``smw_B`` (m x k) is given.
 
     Returns ``(xa, Sa, amplitudes)``.
     """
@@ -271,6 +279,17 @@ def analysis(xf, Hxf, yo, Sf, HSf, r_diag, *, want_sa=True, out=None):
             raise OakError(ERR_ARGS, "device Sf with ld != n: pass out arrays explicitly")
     ampl = _empty_like_mode(device, (N,), like=like)
     _sync_torch(device, like)
+    if smw_B is not None:
+        k = int(smw_B.shape[1])
+        pB, ldB = A.mat(smw_B, m, k, "B")
+        rc = lib().oakg_analysis_smw(ctypes.byref(dims), A.vec(xf, n=n, name="xf"),
+                                     A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"),
+                                     pSf, pHS, A.vec(r_diag, n=m, name="r_diag"), k, pB, ldB,
+                                     A.vec(xa, name="xa"),
+                                     None if Sa is None else A.mat(Sa, n, N, "Sa")[0],
+                                     A.vec(ampl, name="ampl"))
+        _check(rc)
+        return xa, Sa, ampl
     rc = lib().oakg_analysis(ctypes.byref(dims), A.vec(xf, n=n, name="xf"),
                              A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"), pSf, pHS,
                              A.vec(r_diag, n=m, name="r_diag"), A.vec(xa, name="xa"),
@@ -284,7 +303,7 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
                  max_len, *, weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1,
                  localise_obs=True, rotate=True, want_sa=True, want_ampl=True,
                  ampl_always=False, brute_search=False, cell_size=0.0, out=None,
-                 precision=PREC_FP64):
+                 precision=PREC_FP64, smw_B=None):
     """Local analysis (rrsqrt.F90:433-466) with geometric observation selection.
 
     ``zone_pos``: (Z, 4) x, y, z, t of each zone's first state element
@@ -296,7 +315,8 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     only written for the non-localised branch unless ``ampl_always`` is set. ``out`` may give
     preallocated ``(xa, Sa)`` arrays of the same memory kind as the inputs (e.g. pinned host
     arrays). ``precision``: PREC_FP64 (plain form) or PREC_MIXED (FP32 Gram, eigensolve and
-    update; FP64 selection and eigenvalue scalings).
+    update; FP64 selection and eigenvalue scalings). ``smw_B`` (m x k): the observation error
+    covariance R = diag(r_diag) + B B^T (SMWCovar, covariance.F90:464-570; FP64 form).
     """
     Z = int(zone_size.shape[0])
     n = int(xf.shape[0])
@@ -328,6 +348,23 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     ampl = _empty_like_mode(device, (N, Z), order="F", like=like) if want_ampl else None
     nobs = _empty_like_mode(device, (Z,), dtype=np.int32, like=like)
     _sync_torch(device, like)
+    if smw_B is not None:
+        k = int(smw_B.shape[1])
+        pB, ldB = A.mat(smw_B, m, k, "B")
+        rc = lib().oakg_locanalysis_smw(
+            ctypes.byref(dims), ctypes.byref(loc), Z,
+            A.vec(zone_size, np.int32, "zone_size", Z), A.vec(xf, n=n, name="xf"),
+            A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"), pSf, pHS,
+            A.vec(r_diag, n=m, name="r_diag"), k, pB, ldB,
+            A.vec(zp, n=4 * Z, name="zone_pos"), A.vec(ox, n=m, name="obs_x"),
+            A.vec(oy, n=m, name="obs_y"), A.vec(oz, n=m, name="obs_z"),
+            A.vec(ot, n=m, name="obs_t"), A.vec(corr_len, n=Z, name="corr_len"),
+            A.vec(max_len, n=Z, name="max_len"), A.vec(xa, name="xa"),
+            None if Sa is None else A.mat(Sa, n, N, "Sa")[0],
+            None if ampl is None else A.mat(ampl, N, Z, "ampl")[0],
+            A.vec(nobs, np.int32, "nobs"))
+        _check(rc)
+        return xa, Sa, ampl, nobs
     rc = lib().oakg_locanalysis(
         ctypes.byref(dims), ctypes.byref(loc), Z, A.vec(zone_size, np.int32, "zone_size", Z),
         A.vec(xf, n=n, name="xf"), A.vec(Hxf, n=m, name="Hxf"), A.vec(yo, n=m, name="yo"),

@@ -71,7 +71,8 @@ enum BufId {
   B_PERM, B_SU, B_SV, B_SINNOV, B_SR, B_HST, B_HST32, B_OBS32, B_E_EF, B_E_HIDX, B_E_HW, B_E_HSH, B_E_HEF, B_E_XF, B_E_SF,
   B_E_HXF, B_E_HSF, B_E_XA, B_E_SA, B_E_MC, B_E_EA, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
   B_ORDER, B_C_E, B_C_MEAN, B_C_S, B_C_OM, B_C_EO, B_C_HE, B_C_HXF, B_C_HSF, B_C_XA, B_C_SA,
-  B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_COUNT_
+  B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_SMWB, B_HSTA, B_GAUG,
+  B_GVAUG, B_GLOB, B_COUNT_
 };
 
 struct Ctx {
@@ -257,6 +258,10 @@ struct ChunkArgs {
   int32_t* nobs;
   // optional pick order of the selection + Gram stage (chunk-local zone indices, Z entries)
   const int32_t* zorder = nullptr;
+  // SMWCovar R = diag(r) + B B^T (FP64 form): k columns of B and the augmented cell-sorted
+  // rows [HS_q | B_q] (m x (N + k))
+  int smw_k = 0;
+  const double* hst_aug = nullptr;
 };
 
 // How run_chunks issues its work: timed (events + a host wait per chunk), captured into a CUDA
@@ -273,8 +278,10 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   cudaStream_t st = c->stream;
   cudaError_t e;
   int rc;
+  const int NA = N + a.smw_k;
   const size_t per_zone =
-      ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) * sizeof(R) + 2 * sizeof(int32_t);
+      ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) * sizeof(R) + 2 * sizeof(int32_t) +
+      (a.smw_k > 0 ? ((size_t)NA * NA + NA) * sizeof(double) : 0);
   int64_t chunk = c->chunk_override > 0 ? c->chunk_override
                                         : (int64_t)(chunk_budget_bytes() / per_zone);
   if (chunk < 1) chunk = 1;
@@ -288,14 +295,34 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   if ((rc = scratch(c, B_WORK, 8, &d_work, "work counters"))) return rc;
   if ((rc = scratch(c, B_AUX, (size_t)chunk * zone_eig_aux(N), &d_aux, "zone aux"))) return rc;
   if ((rc = scratch(c, B_ZVEC, (size_t)chunk * N * N, &d_zvec, "zone eigenvectors"))) return rc;
+  double *d_Ga = nullptr, *d_ga = nullptr;
+  if (a.smw_k > 0 && ((rc = scratch(c, B_GAUG, (size_t)chunk * NA * NA, &d_Ga, "augmented Gram")) ||
+                      (rc = scratch(c, B_GVAUG, (size_t)chunk * NA, &d_ga, "augmented g"))))
+    return rc;
   *status_all = d_work + 2;
   k_set_int<<<1, 1, 0, st>>>(*status_all, 0);
   count_launches(1);
   for (int64_t z0 = 0; z0 < a.Z; z0 += chunk) {
     const int32_t nzc = (int32_t)std::min<int64_t>(chunk, a.Z - z0);
     if (timed) cudaEventRecord(c->ev[2], st);
-    e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv, a.nobs,
-                a.brute, d_work, *status_all, st, a.zorder);
+    if constexpr (sizeof(R) == sizeof(double)) {
+      if (a.smw_k > 0) {
+        // SMWCovar: products of the augmented rows, then the per-zone Woodbury reduction
+        SortedObs soa = a.so;
+        soa.HSt = a.hst_aug;
+        e = zone_gram_fp64_aug(a.g, soa, NA, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl,
+                               d_Ga, d_ga, a.nobs, a.brute, d_work, st);
+        if (e == cudaSuccess)
+          e = smw_reduce(N, a.smw_k, nzc, d_Ga, d_ga, a.nobs + z0, (double*)d_G, (double*)d_gv,
+                         st);
+      } else {
+        e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv,
+                    a.nobs, a.brute, d_work, *status_all, st, a.zorder);
+      }
+    } else {
+      e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv,
+                  a.nobs, a.brute, d_work, *status_all, st, a.zorder);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
     if (mode == RunMode::kGramOnly) {
       cudaEventRecord(c->ev[3], st);
@@ -518,16 +545,33 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
 }
 
 // ------------------------------------------------------------------------------------------
+// SMWCovar R = diag(r_diag) + B B^T: k columns of B (m x k, leading dimension ldB)
+struct SmwArg {
+  int32_t k = 0;
+  const double* B = nullptr;
+  int64_t ldB = 0;
+};
+
 int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
                      const int32_t* zone_size, const double* xf, const double* Hxf,
                      const double* yo, const double* Sf, const double* HSf,
                      const double* r_diag, const double* zone_xyzt, const double* obs_x,
                      const double* obs_y, const double* obs_z, const double* obs_t,
                      const double* corr_len, const double* max_len, double* xa, double* Sa,
-                     double* ampl, int32_t* nobs_out) {
+                     double* ampl, int32_t* nobs_out, const SmwArg* smw = nullptr) {
   int rc = check_loc(dims, loc, Z);
   if (rc) return rc;
   if (!xf || !xa) return fail(OAKG_ERR_ARGS, "xf and xa are required");
+  const int smw_k = (smw && dims->m > 0) ? smw->k : 0;
+  if (smw) {
+    if (smw->k < 0) return fail(OAKG_ERR_ARGS, "k must be >= 0");
+    if (smw_k > 0 && loc->precision != OAKG_PREC_FP64)
+      return fail(OAKG_ERR_ARGS, "the SMWCovar observation covariance needs OAKG_PREC_FP64");
+    if (smw_k > 0 && (!smw->B || smw->ldB < dims->m))
+      return fail(OAKG_ERR_ARGS, "B (ldB >= m) is required when k > 0");
+    if (dims->N + smw_k > max_fp64_ensemble())
+      return fail(OAKG_ERR_ARGS, "N + k must be <= %d", max_fp64_ensemble());
+  }
   const int64_t n = dims->n, ldS = dims->ldS;
   const int N = dims->N, mem = dims->mem;
   Ctx* c = nullptr;
@@ -564,6 +608,20 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   int32_t* d_status_all = nullptr;
   ChunkArgs ca{P.g, P.so, lp, Z, N, ldS, P.zone_max, P.brute, all_ampl, P.zxyzt, P.corr, P.maxl,
                P.zstart, P.xf, P.Sf, d_xa, d_Sa, d_ampl, d_nobs};
+  if (smw_k > 0) {
+    // the augmented cell-sorted rows [HS_q | B_q] of the SMWCovar products
+    const int64_t m = dims->m;
+    const double* dB;
+    double* d_hsta;
+    if ((rc = stage_in(c, B_SMWB, smw->B, (size_t)smw->ldB * smw_k, mem, &dB, "B")) ||
+        (rc = scratch(c, B_HSTA, (size_t)m * (N + smw_k), &d_hsta, "augmented rows")))
+      return rc;
+    if ((e = smw_rows(m, N, smw_k, P.so.HSt, P.so.perm, dB, smw->ldB, d_hsta, st)) !=
+        cudaSuccess)
+      return cuda_fail(e, "augmented rows");
+    ca.smw_k = smw_k;
+    ca.hst_aug = d_hsta;
+  }
   double t_gram = 0, t_eig = 0, t_upd = 0;
   rc = (loc->precision == OAKG_PREC_MIXED)
            ? run_chunks<float>(c, ca, &d_status_all, &t_gram, &t_eig, &t_upd)
@@ -1462,6 +1520,61 @@ int biased_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
   return OAKG_OK;
 }
 
+// The global analysis with R = diag(r_diag) + B B^T (rrsqrt.F90:196-208 with an SMWCovar R):
+// one zone holding the whole state with every observation at weight 1 (zone and observations
+// at one point, Gaussian weight exp(-(0/1)^2) = 1, the non-localised branch: R unpacked).
+int analysis_smw_impl(const oakg_dims* d, const double* xf, const double* Hxf, const double* yo,
+                      const double* Sf, const double* HSf, const double* r_diag, int32_t k,
+                      const double* B, int64_t ldB, double* xa, double* Sa, double* ampl) {
+  int rc = check_dims(d);
+  if (rc) return rc;
+  Ctx* c = nullptr;
+  if ((rc = get_ctx(&c))) return rc;
+  const int64_t m = d->m;
+  const int mem = d->mem;
+  // zone geometry (host or device like the other arrays): one zone at the origin, every
+  // observation there
+  const size_t geo = (size_t)4 + 2 + (size_t)(m > 0 ? m : 1);
+  std::vector<double> h0(geo, 0.0);
+  h0[4] = 1.0;  // corr_len
+  h0[5] = 1.0;  // max_len
+  const int32_t zsz = (int32_t)d->n;
+  const double* g0;
+  const int32_t* zs;
+  double* dgeo;
+  int32_t* dzs;
+  if (mem == OAKG_MEM_DEVICE) {
+    if ((rc = scratch(c, B_GLOB, geo + 1, &dgeo, "geometry"))) return rc;
+    cudaError_t e = cudaMemcpyAsync(dgeo, h0.data(), geo * sizeof(double),
+                                    cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dgeo + geo, &zsz, sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "geometry");
+    g0 = dgeo;
+    dzs = reinterpret_cast<int32_t*>(dgeo + geo);
+    zs = dzs;
+  } else {
+    g0 = h0.data();
+    zs = &zsz;
+  }
+  oakg_loc loc{};
+  loc.weight = OAKG_WEIGHT_GAUSS_CUTOFF;
+  loc.metric = OAKG_METRIC_CARTESIAN;
+  loc.loctype = 1;
+  loc.localise_obs = 0;
+  loc.rotate = 1;
+  loc.precision = OAKG_PREC_FP64;
+  loc.flags = OAKG_FLAG_BRUTE_SEARCH | OAKG_FLAG_AMPL_ALWAYS;
+  SmwArg sa;
+  sa.k = k;
+  sa.B = B;
+  sa.ldB = ldB;
+  const double* obs = g0 + 6;
+  return locanalysis_impl(d, &loc, 1, zs, xf, Hxf, yo, Sf, HSf, r_diag, g0, obs, obs, nullptr,
+                          nullptr, g0 + 4, g0 + 5, xa, Sa, ampl, nullptr, &sa);
+}
+
 int release_impl() {
   for (auto& cp : g_ctx) {
     if (!cp) continue;
@@ -1694,6 +1807,38 @@ int oakg_ens_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzo
   int rc = oakg::ens_locanalysis_impl(dims, loc, nzones, zone_size, Ef, ldE, H, yo, r_diag,
                                       zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len,
                                       inflation, max_correction, Ea);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_locanalysis_smw(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                         const int32_t* zone_size, const double* xf, const double* Hxf,
+                         const double* yo, const double* Sf, const double* HSf,
+                         const double* r_diag, int32_t k, const double* B, int64_t ldB,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, double* xa, double* Sa, double* ampl,
+                         int32_t* nobs) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  oakg::SmwArg sa;
+  sa.k = k;
+  sa.B = B;
+  sa.ldB = ldB;
+  int rc = oakg::locanalysis_impl(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf, r_diag,
+                                  zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, xa,
+                                  Sa, ampl, nobs, &sa);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_analysis_smw(const oakg_dims* dims, const double* xf, const double* Hxf,
+                      const double* yo, const double* Sf, const double* HSf,
+                      const double* r_diag, int32_t k, const double* B, int64_t ldB, double* xa,
+                      double* Sa, double* ampl) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::analysis_smw_impl(dims, xf, Hxf, yo, Sf, HSf, r_diag, k, B, ldB, xa, Sa, ampl);
   oakg::last_status() = rc;
   return rc;
 }

@@ -83,6 +83,20 @@ cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParam
                          const int32_t* order = nullptr);
 // FP32 copy of count doubles (HS rows for the mixed form).
 cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st);
+// zone_gram_fp64 on augmented observation rows so.HSt = [HS_q | B_q] (N columns, the first nx
+// weighted): the products for the SMWCovar Woodbury reduction (zone_smw.cu).
+cudaError_t zone_gram_fp64_aug(const CellGrid& g, const SortedObs& so, int N, int nx,
+                               LocParams lp, int32_t z0, int32_t nzc, const double* zone_xyzt,
+                               const double* corr_len, const double* max_len, double* d_G,
+                               double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                               cudaStream_t st);
+// ---- zone_smw.cu: SMWCovar (R = diag(C) + B B^T) support. smw_rows writes the augmented
+// cell-sorted rows [HSt_q | B_perm(q)] (m x (N + k)); smw_reduce turns each zone's augmented
+// products (NA = N + k) into G = X^T X - X^T Y (Y^T Y + I)^-1 Y^T X and the matching g.
+cudaError_t smw_rows(int64_t m, int N, int k, const double* HSt, const int32_t* perm,
+                     const double* B, int64_t ldB, double* HStA, cudaStream_t st);
+cudaError_t smw_reduce(int N, int k, int32_t nzc, const double* Ga, const double* ga,
+                       const int32_t* nobs, double* G, double* gv, cudaStream_t st);
 // Same as zone_gram_fp64 for the zones listed in zlist[0..nzc) (G, g slots in list order).
 cudaError_t zone_gram_fp64_list(const CellGrid& g, const SortedObs& so, int N, LocParams lp,
                                 const int32_t* zlist, int32_t nzc, const double* zone_xyzt,

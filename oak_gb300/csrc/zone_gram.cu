@@ -15,6 +15,13 @@
 //              accumulated, both triangles stored)
 //   innovation g = HS_sel^T diag(c) (yo - Hxf)_sel   (the inner product of :142)
 //
+// Non-diagonal R of the SMWCovar kind (R = diag(C) + B B^T, covariance.F90:464-570): the rows
+// are augmented, [HS_q | B_q] (N + k columns, nx = N weighted ones), staged as
+// sh = s_j h, st = s_j h / C_q with s_j = w_q for j < nx and 1 beyond, and the innovation as
+// w_q d_q / C_q; the products are then the blocks X^T X, X^T Y, Y^T Y, X^T z, Y^T z of
+// X = C^-1/2 W HS, Y = C^-1/2 B, z = C^-1/2 W d that the Woodbury reduction (zone_smw.cu)
+// turns into the zone's Gram matrix and innovation projection.
+//
 // Only the cells of the observation grid that can contain observations within maxLength are
 // visited (cell rows are contiguous ranges of the cell-sorted arrays); with
 // OAKG_FLAG_BRUTE_SEARCH or localise_obs = false every observation is visited, which is the
@@ -34,7 +41,7 @@ constexpr int kListCap = 512;   // selected-observation staging list (flushed at
 constexpr int kFlushAt = 256;
 struct ZoneShared {
   int32_t list_q[kListCap];
-  double list_c[kListCap];
+  double list_c[kListCap];  // c = w (w / r), or w itself for augmented (SMW) rows
   int32_t warp_cnt[kThreads / 32];
   int32_t list_len;
   int32_t nrel;
@@ -46,20 +53,35 @@ template <int MAXE, typename R>
 __device__ __forceinline__ void flush_list(ZoneShared& zs, int len, const SortedObs& so, int N,
                                            int CH, R* sh, R* st, R* sinn,
                                            const int32_t (&ea)[MAXE], const int32_t (&eb)[MAXE],
-                                           R (&acc)[MAXE], R (&cmp)[MAXE], int E, int nent) {
+                                           R (&acc)[MAXE], R (&cmp)[MAXE], int E, int nent,
+                                           int nx) {
   for (int c0 = 0; c0 < len; c0 += CH) {
     int rows = min(CH, len - c0);
     __syncthreads();  // previous chunk fully consumed
-    for (int idx = threadIdx.x; idx < rows * N; idx += kThreads) {
-      int i = idx / N, k = idx - i * N;
-      int32_t q = zs.list_q[c0 + i];
-      double h = so.HSt[(int64_t)q * N + k];
-      sh[i * N + k] = (R)h;
-      st[i * N + k] = (R)(zs.list_c[c0 + i] * h);
-    }
-    for (int i = threadIdx.x; i < rows; i += kThreads) {
-      int32_t q = zs.list_q[c0 + i];
-      sinn[i] = (R)(zs.list_c[c0 + i] * so.innov[q]);
+    if (nx >= N) {
+      for (int idx = threadIdx.x; idx < rows * N; idx += kThreads) {
+        int i = idx / N, k = idx - i * N;
+        int32_t q = zs.list_q[c0 + i];
+        double h = so.HSt[(int64_t)q * N + k];
+        sh[i * N + k] = (R)h;
+        st[i * N + k] = (R)(zs.list_c[c0 + i] * h);
+      }
+      for (int i = threadIdx.x; i < rows; i += kThreads) {
+        int32_t q = zs.list_q[c0 + i];
+        sinn[i] = (R)(zs.list_c[c0 + i] * so.innov[q]);
+      }
+    } else {  // augmented rows [HS_q | B_q]: list_c holds w_q
+      for (int idx = threadIdx.x; idx < rows * N; idx += kThreads) {
+        int i = idx / N, k = idx - i * N;
+        int32_t q = zs.list_q[c0 + i];
+        const double h = so.HSt[(int64_t)q * N + k] * ((k < nx) ? zs.list_c[c0 + i] : 1.0);
+        sh[i * N + k] = (R)h;
+        st[i * N + k] = (R)(h / so.r[q]);
+      }
+      for (int i = threadIdx.x; i < rows; i += kThreads) {
+        int32_t q = zs.list_q[c0 + i];
+        sinn[i] = (R)(zs.list_c[c0 + i] * so.innov[q] / so.r[q]);
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -95,7 +117,7 @@ __global__ void __launch_bounds__(kThreads)
                 const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
                 const double* __restrict__ max_len, R* __restrict__ G, R* __restrict__ gv,
                 int32_t* __restrict__ nobs, int brute, int CH, int32_t* __restrict__ work,
-                const int32_t* __restrict__ zlist, const int32_t* __restrict__ order) {
+                const int32_t* __restrict__ zlist, const int32_t* __restrict__ order, int nx) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   R* dyn = reinterpret_cast<R*>(dyn_raw);
   R* sh = dyn;            // [CH][N]
@@ -207,7 +229,7 @@ __global__ void __launch_bounds__(kThreads)
               rel = (d <= Rmax) && (w != 0.0);
             }
             sel = rel || !lp.localise;
-            if (sel) c = w * (w / so.r[q]);
+            if (sel) c = (nx >= N) ? w * (w / so.r[q]) : w;
           }
           nrel_local += rel;
           unsigned ball = __ballot_sync(0xffffffffu, sel);
@@ -229,7 +251,7 @@ __global__ void __launch_bounds__(kThreads)
           __syncthreads();
           if (zs.list_len >= kFlushAt) {
             int len = zs.list_len;
-            flush_list<MAXE, R>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, cmp, E, nent);
+            flush_list<MAXE, R>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, cmp, E, nent, nx);
             __syncthreads();
             if (threadIdx.x == 0) zs.list_len = 0;
             __syncthreads();
@@ -239,7 +261,7 @@ __global__ void __launch_bounds__(kThreads)
     }
     if (zs.list_len > 0) {
       int len = zs.list_len;
-      flush_list<MAXE, R>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, cmp, E, nent);
+      flush_list<MAXE, R>(zs, len, so, N, CH, sh, st, sinn, ea, eb, acc, cmp, E, nent, nx);
     }
     // relevant-observation count of the zone
     for (int o = 16; o > 0; o >>= 1) nrel_local += __shfl_xor_sync(0xffffffffu, nrel_local, o);
@@ -347,7 +369,8 @@ cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams
                         int32_t nzc, const double* zone_xyzt, const double* corr_len,
                         const double* max_len, R* d_G, R* d_g, int32_t* d_nobs,
                         int brute, int32_t* d_work, cudaStream_t st,
-                        const int32_t* zlist = nullptr, const int32_t* order = nullptr) {
+                        const int32_t* zlist = nullptr, const int32_t* order = nullptr,
+                        int nx = -1) {
   int CH = chunk_rows(N);
   size_t smem = (size_t)(2 * CH * N + CH) * sizeof(R);
   cudaError_t e = cudaFuncSetAttribute(k_zone_gram<MAXE, R>,
@@ -366,7 +389,7 @@ cudaError_t launch_zone(const CellGrid& g, const SortedObs& so, int N, LocParams
   if (e != cudaSuccess) return e;
   k_zone_gram<MAXE, R><<<grid, kThreads, smem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
                                                       max_len, d_G, d_g, d_nobs, brute, CH,
-                                                      d_work, zlist, order);
+                                                      d_work, zlist, order, nx < 0 ? N : nx);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -437,6 +460,15 @@ cudaError_t zone_gram_fp32(const CellGrid& g, const SortedObs& so, int N, LocPar
                            cudaStream_t st, const int32_t* order) {
   OAKG_GRAM_DISPATCH_T(launch_zone, float, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len,
                        d_G, d_g, d_nobs, brute, d_work, st, nullptr, order);
+}
+
+cudaError_t zone_gram_fp64_aug(const CellGrid& g, const SortedObs& so, int N, int nx,
+                               LocParams lp, int32_t z0, int32_t nzc, const double* zone_xyzt,
+                               const double* corr_len, const double* max_len, double* d_G,
+                               double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
+                               cudaStream_t st) {
+  OAKG_GRAM_DISPATCH_T(launch_zone, double, g, so, N, lp, z0, nzc, zone_xyzt, corr_len, max_len,
+                       d_G, d_g, d_nobs, brute, d_work, st, nullptr, nullptr, nx);
 }
 
 cudaError_t zone_gram_fp64_list(const CellGrid& g, const SortedObs& so, int N, LocParams lp,

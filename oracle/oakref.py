@@ -135,17 +135,20 @@ def analysis_increment(Hxf, yo, Sf, HSf, rinv_eff, rotate=True):
 
     ``rinv_eff`` is the diagonal of the (localised) inverse observation error covariance,
     i.e. ``R%mldivide`` for DiagCovar (covariance.F90:425-432) or DCDCovar with D = w
-    (covariance.F90:612-619): ``w**2 / r``.
+    (covariance.F90:612-619): ``w**2 / r``; or the full matrix of a non-diagonal one (SMWCovar).
     Returns ``(xa_xf, Sa, ampl)``.
     """
     HSf = np.asarray(HSf, dtype=np.float64)
     Sf = np.asarray(Sf, dtype=np.float64)
     N = Sf.shape[1]
-    temp = HSf.T @ (rinv_eff[:, None] * HSf)  # :135 (HSf .tx. R%mldivide(HSf))
+    rinv_eff = np.asarray(rinv_eff, dtype=np.float64)
+    mld = (lambda x: rinv_eff @ x) if rinv_eff.ndim == 2 else (
+        lambda x: (rinv_eff[:, None] * x) if x.ndim == 2 else rinv_eff * x)
+    temp = HSf.T @ mld(HSf)  # :135 (HSf .tx. R%mldivide(HSf))
     lam, U = np.linalg.eigh(temp, UPLO="L")  # :136 symeig -> dsyev('V','L')
     lam = np.where(lam < 0, 0.0, lam)  # :137
     lam = 1.0 / (1.0 + lam)  # :140
-    ampl = U @ (lam * (U.T @ (HSf.T @ (rinv_eff * (yo - Hxf)))))  # :142
+    ampl = U @ (lam * (U.T @ (HSf.T @ mld(yo - Hxf))))  # :142
     if np.any(ampl != ampl):  # :145-149
         raise FloatingPointError("NaN in analysis amplitudes")
     xa_xf = Sf @ ampl  # :151
@@ -160,16 +163,36 @@ def analysis_increment(Hxf, yo, Sf, HSf, rinv_eff, rotate=True):
     return xa_xf, Sa, ampl
 
 
-def analysis(xf, Hxf, yo, Sf, HSf, r_diag, rotate=True):
-    """Global analysis with diagonal R (rrsqrt.F90:196-208). Returns ``(xa, Sa, ampl)``."""
+def smw_rinv(C, B):
+    """Inverse of the SMWCovar R = diag(C) + B B^T (covariance.F90:464-570) as its mldivide
+    computes it: C^-1 - C^-1 B D B^T C^-1 with D = (B^T C^-1 B + I)^-1 (SMWCovar_init :475-483,
+    SMWCovar_mldivide_vec :525-535)."""
+    C = np.asarray(C, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    CiB = B / C[:, None]
+    D = np.linalg.inv(B.T @ CiB + np.eye(B.shape[1]))
+    return np.diag(1.0 / C) - CiB @ D @ CiB.T
+
+
+def analysis(xf, Hxf, yo, Sf, HSf, r_diag, rotate=True, smw_B=None):
+    """Global analysis with diagonal R (rrsqrt.F90:196-208), or R = diag(r_diag) + B B^T
+    (SMWCovar) when ``smw_B`` is given. Returns ``(xa, Sa, ampl)``."""
+    if smw_B is not None:
+        xa_xf, Sa, ampl = analysis_increment(Hxf, yo, Sf, HSf, smw_rinv(r_diag, smw_B), rotate)
+        return xf + xa_xf, Sa, ampl
     rinv = 1.0 / np.asarray(r_diag, dtype=np.float64)
     xa_xf, Sa, ampl = analysis_increment(Hxf, yo, Sf, HSf, rinv, rotate)
     return xf + xa_xf, Sa, ampl
 
 
 def loc_analysis(zone_size, select, xf, Hxf, yo, Sf, HSf, r_diag, localise_obs=True,
-                 rotate=True):
+                 rotate=True, smw_B=None):
     """Local analysis (rrsqrt.F90:258-466) with a selection callback.
+
+    With ``smw_B`` (m x k) the observation error covariance is R = diag(r_diag) + B B^T
+    (SMWCovar): the zone uses DCDCovar(w, R) (rrsqrt.F90:385-391) or, with observation
+    localisation and not every observation relevant, DCDCovar(w_sel, R%pack(sel)) (:395,
+    SMWCovar_pack covariance.F90:540-570: the Woodbury matrix of the packed rows).
 
     ``select(zi, start_index) -> (weight(m), relevant(m))`` plays the role of
     ``selectObservations`` (called with the zone's first state index, :368).
@@ -199,18 +222,22 @@ def loc_analysis(zone_size, select, xf, Hxf, yo, Sf, HSf, r_diag, localise_obs=T
         nobs[zi] = nb
         if nb == 0:
             continue
+        if smw_B is None:
+            full_rinv = lambda: weight**2 / r_diag
+            sel_rinv = lambda s: weight[s] ** 2 / r_diag[s]
+        else:
+            Bm = np.asarray(smw_B, dtype=np.float64)
+            full_rinv = lambda: np.outer(weight, weight) * smw_rinv(r_diag, Bm)
+            sel_rinv = lambda s: np.outer(weight[s], weight[s]) * smw_rinv(r_diag[s], Bm[s])
         if not localise_obs:
-            rinv = weight**2 / r_diag
-            dxa, dSa, ampl = analysis_increment(Hxf, yo, Sf[i1:i2], HSf, rinv, rotate)
+            dxa, dSa, ampl = analysis_increment(Hxf, yo, Sf[i1:i2], HSf, full_rinv(), rotate)
             amplitudes[:, zi] = ampl
         elif nb == m:
-            rinv = weight**2 / r_diag
-            dxa, dSa, _ = analysis_increment(Hxf, yo, Sf[i1:i2], HSf, rinv, rotate)
+            dxa, dSa, _ = analysis_increment(Hxf, yo, Sf[i1:i2], HSf, full_rinv(), rotate)
         else:
             sel = np.nonzero(relevant)[0]
-            rinv = weight[sel] ** 2 / r_diag[sel]
-            dxa, dSa, _ = analysis_increment(Hxf[sel], yo[sel], Sf[i1:i2], HSf[sel], rinv,
-                                             rotate)
+            dxa, dSa, _ = analysis_increment(Hxf[sel], yo[sel], Sf[i1:i2], HSf[sel],
+                                             sel_rinv(sel), rotate)
         xa_xf[i1:i2] = dxa
         Sa[i1:i2] = dSa
     return xf + xa_xf, Sa, amplitudes, nobs

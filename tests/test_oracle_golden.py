@@ -9,6 +9,8 @@ known-answer tests -- this is what pins the oracle before it judges the CUDA pat
                                     observation localisation, == explicit per-zone formula
 * test/test_assim.F90:59-172        ensemble prologue + analysis + epilogue: ensemble mean
                                     and covariance == Kalman (tol 1e-5)
+* test/test_rrsqrt.F90:326-340      the same analyses with R = SMWCovar(2 I, B), B = sin(3 i)
+                                    (m x dim_ens, column-major)
 """
 import numpy as np
 import pytest
@@ -248,3 +250,50 @@ def test_biased_analysis_reduces_to_plain_and_scales_r():
     xa2 = oakref.loc_analysis(zone_size, sel, ux, oakref.sparse_apply(idx, w, ux, shift), yo, Sf,
                               HSf, (1 - g) * r)[0]
     assert np.max(np.abs(xa - xa2)) < 1e-12
+
+
+def _smw_B(m, k=12):
+    """test_rrsqrt.F90:329-332: B = reshape(sin(3 i), [m, dim_ens]), i = 1..m*dim_ens."""
+    return np.sin(3.0 * np.arange(1, m * k + 1)).reshape(k, m).T.copy()
+
+
+def test_smw_analysis_equals_kalman():
+    xf, Sf, H, y, r, HSf, Hxf = _kalman_case()
+    B = _smw_B(y.size)
+    R = np.diag(r) + B @ B.T
+    xa_k, Pa_k = oakref.kalman_reference(xf, Sf, H, y, R)
+    xa, Sa, _ = oakref.analysis(xf, Hxf, y, Sf, HSf, r, smw_B=B)
+    assert np.max(np.abs(xa - xa_k)) < TOL
+    assert np.max(np.abs(Sa @ Sa.T - Pa_k)) < TOL
+    n = xf.size
+    sel_all = lambda zi, start: (np.ones(y.size), np.ones(y.size, dtype=bool))
+    for zs in (np.array([n]), np.ones(n, dtype=int)):
+        xa, Sa, _, _ = oakref.loc_analysis(zs, sel_all, xf, Hxf, y, Sf, HSf, r, smw_B=B)
+        assert np.max(np.abs(xa - xa_k)) < TOL
+        assert np.max(np.abs(Sa @ Sa.T - Pa_k)) < TOL
+
+
+@pytest.mark.parametrize("localise", [False, True])
+def test_smw_gc_local_equals_explicit_formula(localise):
+    """test_rrsqrt.F90:163-236 with R = SMWCovar: the zone's inverse covariance is
+    inv(R(iloc, iloc)) .* (w w^T) (R(iloc, iloc) is the packed SMWCovar)."""
+    xf, Sf, H, y, r, HSf, Hxf = _kalman_case()
+    n, m = xf.size, y.size
+    B = _smw_B(m)
+    R = np.diag(r) + B @ B.T
+    zone_pos, obs_pos, corr, maxl = _gc_geometry(n, m)
+    sel = oakref.geometric_selector(zone_pos, obs_pos, corr, maxl, kind=oakref.GASPARI_COHN)
+    Pf = Sf @ Sf.T
+    xa_x = np.empty_like(xf)
+    for i in range(n):
+        w, rel = sel(i, i)
+        if not localise:
+            rel = np.ones_like(rel)
+        iloc = np.nonzero(rel)[0]
+        Hloc = H[iloc]
+        invRloc = np.linalg.inv(R[np.ix_(iloc, iloc)]) * np.outer(w[iloc], w[iloc])
+        Pa = np.linalg.inv(np.linalg.inv(Pf) + Hloc.T @ invRloc @ Hloc)
+        xa_x[i] = xf[i] + (Pa[i] @ (Hloc.T @ (invRloc @ (y[iloc] - Hloc @ xf))))
+    xa, _, _, _ = oakref.loc_analysis(np.ones(n, dtype=np.int32), sel, xf, Hxf, y, Sf, HSf, r,
+                                      localise_obs=localise, smw_B=B)
+    assert np.max(np.abs(xa - xa_x)) < TOL
