@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-global", action="store_true")
     p.add_argument("--no-graph", action="store_true")
+    p.add_argument("--no-layout", action="store_true")
     p.add_argument("--batched-scale", type=float, default=0.25,
                    help="horizontal scale of the 5-variable N = 100 batched workload "
                         "(0 skips it)")
@@ -511,6 +512,14 @@ def main():
         from oak_gb300.workloads import large_case
         large = two_forms(large_case(scale=args.large_scale), args.large_scale, adjoint_sub=200)
 
+    # layout builders on one 3-D variable of 720 x 360 x 50 points (x fastest), zones = the
+    # 259,200 columns (partition = column number), a land mask, 10^6 observations: zone
+    # layout (initPartition), sea packing, rectilinear observation operator (cinterp), the
+    # zone-order permutation of a 16-member ensemble; CPU: the oracle on bounded samples
+    layout = None
+    if not args.no_layout:
+        layout = layout_section(torch, dev, stream, args, barrier)
+
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
     if not args.no_e2e:
@@ -573,6 +582,7 @@ def main():
         "large": large,
         "adjoint": adjoint,
         "global_analysis": glob,
+        "layout": layout,
         "graph": graph,
         "gpu_launches": int(launches),
         "stage_ms_per_step": per_step,
@@ -585,6 +595,87 @@ def main():
         "clocks": clk,
     }
     print(json.dumps(line))
+
+
+def layout_section(torch, dev, stream, args, barrier):
+    import oak_gb300
+    nx, ny, nz = 720, 360, 50
+    n = nx * ny * nz
+    Z = nx * ny
+    rng = np.random.default_rng(12)
+    e = torch.arange(n, device=dev, dtype=torch.int64)
+    part = (e % Z + 1).to(torch.int32)
+    del e
+    x = np.linspace(-180.0, 179.5, nx)
+    y = np.linspace(-89.75, 89.75, ny)
+    z = np.cumsum(rng.uniform(1.0, 50.0, nz))
+    mask = np.zeros((nx, ny, nz), dtype=bool)
+    mask[100:200, 50:120, :] = True
+    mask[:, :, 30:] |= (np.arange(nx)[:, None, None] % 5 == 0)
+    mask_d = torch.as_tensor(mask.reshape(-1, order="F"), device=dev)
+    m = 1_000_000
+    pos = [torch.as_tensor(rng.uniform(-180.0, 179.5, m), device=dev),
+           torch.as_tensor(rng.uniform(-89.75, 89.75, m), device=dev),
+           torch.as_tensor(rng.uniform(z[0], z[-1], m), device=dev)]
+    axes = [torch.as_tensor(a, device=dev) for a in (x, y, z)]
+    ens = torch.empty((16, n), dtype=torch.float64, device=dev).normal_().t()
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            out = fn()
+        barrier()
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            out = fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return out, a.elapsed_time(b) / args.steps
+
+    L = oak_gb300.lib()
+    l0 = L.oakg_launch_count()
+    (zs, zi, inv), ms_layout = timed(lambda: oak_gb300.zone_layout(part, Z))
+    (sea, nsea), ms_sea = timed(lambda: oak_gb300.sea_index(mask_d))
+    (idx, w), ms_oper = timed(lambda: oak_gb300.obsoper_rectilinear(axes, pos, sea=sea))
+    _, ms_perm = timed(lambda: oak_gb300.permute_rows(zi, ens))
+    launches = L.oakg_launch_count() - l0
+    ok_layout = bool((zs == nz).all().item()) and int(zi[nz - 1].item()) == (nz - 1) * Z
+    inside = float((idx[:, 0] >= 0).float().mean().item())
+    perm_bytes = n * 16 * 16 + n * 4
+    res = {"grid": f"{nx} x {ny} x {nz} points, x fastest; {Z} column zones; {m} observations",
+           "zone_layout": {"ms": ms_layout, "elements_per_s": n / (ms_layout / 1e3),
+                           "check": ok_layout},
+           "sea_index": {"ms": ms_sea, "points_per_s": n / (ms_sea / 1e3), "nsea": nsea},
+           "obsoper_rectilinear": {"ms": ms_oper, "obs_per_s": m / (ms_oper / 1e3),
+                                   "inside_fraction": inside},
+           "permute_rows": {"ms": ms_perm, "columns": 16,
+                            "achieved_GBs": perm_bytes / (ms_perm / 1e3) / 1e9,
+                            "algorithmic_bytes": perm_bytes},
+           "gpu_launches": int(launches),
+           "note": "timed through the Python API (device arrays), includes the host "
+                   "allocation of the outputs; steps as --steps"}
+    del idx, w, zs, zi, inv, sea, ens
+    if not args.no_cpu_baseline:
+        from oracle import oakref as R
+        ps = part[:1_000_000].cpu().numpy()
+        t0 = time.perf_counter()
+        R.init_partition(ps)
+        t_part = time.perf_counter() - t0
+        ns = 300
+        ph = [p[:ns].cpu().numpy() for p in pos]
+        sea_h, _ = R.sea_index(mask.reshape(-1, order="F"))
+        t0 = time.perf_counter()
+        R.obsoper_rectilinear([x, y, z], ph, sea=sea_h)
+        t_oper = time.perf_counter() - t0
+        res["cpu_baseline"] = {
+            "kind": "port", "cores": 1,
+            "zone_layout_elements_per_s": ps.size / t_part,
+            "obsoper_obs_per_s": ns / t_oper,
+            "sample": f"oracle init_partition on {ps.size} elements, "
+                      f"obsoper_rectilinear on {ns} observations (NumPy, one thread)"}
+    return res
 
 
 def read_traffic(kernel):

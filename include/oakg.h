@@ -249,6 +249,55 @@ int oakg_biased_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t 
                             const double* corr_len, const double* max_len, double* xa,
                             double* ba, double* Sa);
 
+/* ---- layout builders (the host preprocessing of the reference, on the device) ---------- */
+
+/* initPartition (assimilation.F90:578-641): the zone layout of a partition vector.
+ * partition (n): the zone number, 1..nzones, of every state element. Results: zone_size
+ * (nzones); zone_index (n): the elements of zone 1, then of zone 2, ..., each zone's elements
+ * in ascending order (0-based; the reference's zoneIndex minus 1); inv_index (n, optional):
+ * position of every element in zone_index (invZoneIndex minus 1). A zone number outside
+ * 1..nzones, or a zone without elements, is OAKG_ERR_ARGS (the reference stops on both,
+ * :605-617). Arrays on the host or the device per mem (OAKG_MEM_*). */
+int oakg_zone_layout(int64_t n, const int32_t* partition, int32_t nzones, int32_t mem,
+                     int32_t* zone_size, int32_t* zone_index, int32_t* inv_index);
+
+/* Y(i, :) = X(index(i), :) for i < n and ncols columns (column-major, leading dimensions ldX,
+ * ldY >= n; X and Y must not alias): with index = zone_index it puts a state vector or an
+ * ensemble in zone order (permute, matoper.F90:1166-1183, as in assimilation.F90:766, 4040),
+ * with inv_index it puts it back (ipermute, matoper.F90:1187-1205; assimilation.F90:3994). */
+int oakg_permute_rows(int64_t n, int32_t ncols, const int32_t* index, const double* X,
+                      int64_t ldX, double* Y, int64_t ldY, int32_t mem);
+
+/* The sea packing of a masked grid of npts points (the state vector holds the unmasked points
+ * only: StateVectorSizeSea): sea[i] = number of unmasked points before point i, or -1 where
+ * mask[i] != 0; *nsea (optional) = the number of unmasked points. */
+int oakg_sea_index(int64_t npts, const uint8_t* mask, int32_t mem, int64_t* sea, int64_t* nsea);
+
+/* The observation operator on the zone-ordered state (assimilation.F90:2404-2407,
+ * H%j = invZoneIndex(H%j)): index[t] = inv_index[index[t]] in place for the count entries with
+ * 0 <= index[t] < n; negative entries (unused pairs) stay; an entry >= n is OAKG_ERR_ARGS
+ * (those entries are left as they were). */
+int oakg_obsoper_to_zone_order(int64_t count, int64_t* index, const int32_t* inv_index,
+                               int64_t n, int32_t mem);
+
+/* genObservationOper (assimilation.F90:2471-2656) for one variable on a rectilinear grid of
+ * ndim = 1..4 axes: shape[ndim] points per axis (each >= 2, host array), coords = the axes'
+ * coordinates one after the other (shape[0] + ... values, each axis strictly monotone, either
+ * direction), points in Fortran order (axis 0 fastest). sea: the sea packing of the grid's
+ * points (oakg_sea_index) or NULL for an unmasked grid; offset: the variable's first row in the
+ * state vector. For observation j at pos[k*m + j] (k < ndim), cinterp (ndgrid.F90:1183-1257):
+ * the grid cell holding it, and if none of its 2^ndim corners is masked, the first simplex of
+ * the cell's split (split, :357-435) whose barycentric coordinates lie in [-1e-8, 1 + 1e-8]
+ * (interp_tetrahedron, :464-629), giving the corner weights. Row j of the operator:
+ * index[j*2^ndim + c] = offset + sea[corner c], weight[...] its weight (corner c: bit k set =
+ * upper side of axis k), in the oakg_obsoper row form. An observation outside the grid or next
+ * to a masked point: index -1, weight 0 in all its pairs (the reference's out-of-domain
+ * entry). A cell whose simplices have |det| <= 1e-8 (cell volume <= 2^(ndim-1) 1e-8, where the
+ * reference falls back to an SVD solve): index -2, weight 0. */
+int oakg_obsoper_rectilinear(int32_t ndim, const int32_t* shape, const double* coords,
+                             const int64_t* sea, int64_t offset, int64_t m, const double* pos,
+                             int32_t mem, int64_t* index, double* weight);
+
 /* The local analysis of an ensemble, all on the device: prologue, oakg_locanalysis (dims->ldS
  * and dims->ldH are ignored: the anomalies are the library's), epilogue. Ea may alias Ef. The
  * numerical core of oak_assim for schemetype = 1 without the file I/O. */

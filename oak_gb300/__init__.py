@@ -27,7 +27,10 @@ import numpy as np
 __all__ = ["analysis", "loc_analysis", "loc_analysis_adjoint", "OakError", "lib", "last_timings", "release",
            "PREC_FP64", "PREC_MIXED",
            "GAUSS_CUTOFF", "GASPARI_COHN", "CARTESIAN", "SPHERICAL", "SPHERICAL_APPROX",
-           "zone_positions"]
+           "zone_positions", "ensemble_prologue", "ensemble_epilogue", "ens_loc_analysis",
+           "ens2sqrt", "sqrt2ens", "ens_analysis", "biased_loc_analysis", "Plan",
+           "zone_layout", "permute_rows", "sea_index", "obsoper_rectilinear",
+           "obsoper_to_zone_order"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "liboakg.so")
@@ -149,6 +152,19 @@ def lib() -> ctypes.CDLL:
                                            ctypes.c_int32, P, ctypes.c_double,
                                            ctypes.POINTER(ObsOper)] + [P] * 17)
     L.oakg_biased_locanalysis.restype = ctypes.c_int
+    L.oakg_zone_layout.argtypes = [ctypes.c_int64, P, ctypes.c_int32, ctypes.c_int32, P, P, P]
+    L.oakg_zone_layout.restype = ctypes.c_int
+    L.oakg_permute_rows.argtypes = [ctypes.c_int64, ctypes.c_int32, P, P, ctypes.c_int64, P,
+                                    ctypes.c_int64, ctypes.c_int32]
+    L.oakg_permute_rows.restype = ctypes.c_int
+    L.oakg_sea_index.argtypes = [ctypes.c_int64, P, ctypes.c_int32, P,
+                                 ctypes.POINTER(ctypes.c_int64)]
+    L.oakg_sea_index.restype = ctypes.c_int
+    L.oakg_obsoper_to_zone_order.argtypes = [ctypes.c_int64, P, P, ctypes.c_int64, ctypes.c_int32]
+    L.oakg_obsoper_to_zone_order.restype = ctypes.c_int
+    L.oakg_obsoper_rectilinear.argtypes = [ctypes.c_int32, P, P, P, ctypes.c_int64,
+                                           ctypes.c_int64, P, ctypes.c_int32, P, P]
+    L.oakg_obsoper_rectilinear.restype = ctypes.c_int
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -196,8 +212,7 @@ class _Args:
         if a is None:
             return None
         if self.device:
-            import torch
-            tdt = torch.float64 if dtype == np.float64 else torch.int32
+            tdt = _torch_dtype(dtype)
             if not (_is_torch(a) and a.is_cuda):
                 raise OakError(ERR_ARGS, f"{name}: expected a CUDA tensor")
             if a.dtype != tdt or not a.is_contiguous():
@@ -231,6 +246,12 @@ class _Args:
         return ctypes.c_void_p(arr.ctypes.data), rows
 
 
+def _torch_dtype(dtype):
+    import torch
+    return {np.dtype(np.float64): torch.float64, np.dtype(np.int32): torch.int32,
+            np.dtype(np.int64): torch.int64, np.dtype(np.uint8): torch.uint8}[np.dtype(dtype)]
+
+
 def _device_mode(*arrays) -> bool:
     dev = [_is_torch(a) and a.is_cuda for a in arrays if a is not None]
     if any(dev) and not all(dev):
@@ -241,7 +262,7 @@ def _device_mode(*arrays) -> bool:
 def _empty_like_mode(device: bool, shape, dtype=np.float64, order="C", like=None):
     if device:
         import torch
-        tdt = torch.float64 if dtype == np.float64 else torch.int32
+        tdt = _torch_dtype(dtype)
         if order == "F" and len(shape) == 2:
             return torch.empty((shape[1], shape[0]), dtype=tdt, device=like.device).t()
         return torch.empty(shape, dtype=tdt, device=like.device)
@@ -724,3 +745,131 @@ def loc_analysis_adjoint(zone_size, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos,
         ctypes.byref(dinfl))
     _check(rc)
     return dyo, dr, dlen.value, dinfl.value
+
+
+# ----------------------------------------------------------------------------- layout builders
+
+def zone_layout(partition, nzones=None):
+    """initPartition (oakg_zone_layout, assimilation.F90:578-641) of a partition vector of
+    1-based zone numbers: ``(zone_size (Z,), zone_index (n,), inv_index (n,))``, int32, the
+    indices 0-based (zone_index lists zone 1's elements in ascending order, then zone 2's, ...;
+    inv_index is its inverse). ``nzones`` defaults to ``max(partition)``. A zone number outside
+    1..nzones or an empty zone raises OakError (ERR_ARGS)."""
+    device = _device_mode(partition)
+    n = int(partition.numel() if _is_torch(partition) else np.asarray(partition).size)
+    if nzones is None:
+        nzones = int(partition.max()) if n else 0
+    A = _Args(device)
+    p = A.vec(partition, dtype=np.int32, name="partition", n=n)
+    zs = _empty_like_mode(device, (max(int(nzones), 0),), dtype=np.int32, like=partition)
+    zi = _empty_like_mode(device, (n,), dtype=np.int32, like=partition)
+    inv = _empty_like_mode(device, (n,), dtype=np.int32, like=partition)
+    _sync_torch(device, partition)
+    _check(lib().oakg_zone_layout(n, p, int(nzones), MEM_DEVICE if device else MEM_HOST,
+                                  A.vec(zs, dtype=np.int32), A.vec(zi, dtype=np.int32),
+                                  A.vec(inv, dtype=np.int32)))
+    return zs, zi, inv
+
+
+def permute_rows(index, X):
+    """``X[index]`` for a vector (n,) or a column-major matrix (n, k) (oakg_permute_rows):
+    with ``index = zone_index`` the state in zone order, with ``inv_index`` back."""
+    device = _device_mode(index, X)
+    n = int(X.shape[0])
+    k = 1 if X.ndim == 1 else int(X.shape[1])
+    A = _Args(device)
+    pi = A.vec(index, dtype=np.int32, name="index", n=n)
+    if X.ndim == 1:
+        px, ldx = A.vec(X, name="X", n=n), n
+        Y = _empty_like_mode(device, (n,), like=X)
+        py, ldy = A.vec(Y), n
+    else:
+        px, ldx = A.mat(X, n, k, "X")
+        Y = _empty_like_mode(device, (n, k), order="F", like=X)
+        py, ldy = A.mat(Y, n, k, "Y")
+    _sync_torch(device, X)
+    _check(lib().oakg_permute_rows(n, k, pi, px, ldx, py, ldy,
+                                   MEM_DEVICE if device else MEM_HOST))
+    return Y
+
+
+def sea_index(mask):
+    """Sea packing of a masked grid (oakg_sea_index): ``(sea (npts,) int64, nsea)`` with
+    ``sea[i]`` the number of unmasked points before point ``i`` (flat index of ``mask``, which
+    callers pass in Fortran order) or -1 where ``mask`` is true."""
+    device = _device_mode(mask)
+    if device:
+        import torch
+        mk = mask.reshape(-1)
+        mk = (mk != 0).to(torch.uint8).contiguous()
+    else:
+        mk = np.ascontiguousarray((np.asarray(mask) != 0).reshape(-1, order="F"), dtype=np.uint8)
+    npts = int(mk.numel() if device else mk.size)
+    A = _Args(device)
+    pm = A.vec(mk, dtype=np.uint8, name="mask", n=npts)
+    sea = _empty_like_mode(device, (npts,), dtype=np.int64, like=mask)
+    cnt = ctypes.c_int64(0)
+    _sync_torch(device, mask)
+    _check(lib().oakg_sea_index(npts, pm, MEM_DEVICE if device else MEM_HOST,
+                                A.vec(sea, dtype=np.int64), ctypes.byref(cnt)))
+    return sea, int(cnt.value)
+
+
+def obsoper_rectilinear(axes, obs_pos, sea=None, offset=0):
+    """genObservationOper for one variable on a rectilinear grid (oakg_obsoper_rectilinear,
+    assimilation.F90:2471-2656 with cinterp, ndgrid.F90:1183-1257). ``axes``: the 1..4 axis
+    coordinate vectors (each strictly monotone, >= 2 points; grid points in Fortran order);
+    ``obs_pos``: one coordinate array per axis (m each); ``sea``: the grid's sea packing
+    (:func:`sea_index`) or None; ``offset``: the variable's first state row. Returns
+    ``(index (m, 2^d) int64, weight (m, 2^d))`` in the oakg_obsoper row form: index -1 for an
+    observation outside the grid or next to a masked point, -2 in a cell too small for the
+    1e-8 determinant tolerance."""
+    d = len(axes)
+    device = _device_mode(*axes, *obs_pos, sea)
+    shape = np.asarray([int(a.numel() if _is_torch(a) else np.asarray(a).size) for a in axes],
+                       dtype=np.int32)
+    if len(obs_pos) != d:
+        raise OakError(ERR_ARGS, f"obs_pos: expected {d} coordinate arrays")
+    m = int(obs_pos[0].numel() if _is_torch(obs_pos[0]) else np.asarray(obs_pos[0]).size)
+    K = 1 << d
+    if device:
+        import torch
+        coords = torch.cat([a.reshape(-1).to(torch.float64) for a in axes]).contiguous()
+        pos = torch.stack([p.reshape(-1).to(torch.float64) for p in obs_pos]).contiguous()
+    else:
+        coords = np.concatenate([np.asarray(a, dtype=np.float64).reshape(-1) for a in axes])
+        pos = np.ascontiguousarray(np.stack([np.asarray(p, dtype=np.float64).reshape(-1)
+                                             for p in obs_pos]))
+    A = _Args(device)
+    pc = A.vec(coords, name="coords")
+    pp = A.vec(pos, name="pos")
+    ps = A.vec(sea, dtype=np.int64, name="sea", n=int(np.prod(shape)))
+    index = _empty_like_mode(device, (m, K), dtype=np.int64, like=coords)
+    weight = _empty_like_mode(device, (m, K), like=coords)
+    _sync_torch(device, coords)
+    _check(lib().oakg_obsoper_rectilinear(d, shape.ctypes.data_as(ctypes.c_void_p), pc, ps,
+                                          int(offset), m, pp,
+                                          MEM_DEVICE if device else MEM_HOST,
+                                          A.vec(index, dtype=np.int64),
+                                          A.vec(weight)))
+    return index, weight
+
+
+def obsoper_to_zone_order(index, inv_index):
+    """The operator's state rows mapped to the zone-ordered state (oakg_obsoper_to_zone_order,
+    assimilation.F90:2404-2407): ``index`` (int64, any shape, negative entries kept) is updated
+    in place and returned."""
+    device = _device_mode(index, inv_index)
+    n = int(inv_index.numel() if _is_torch(inv_index) else np.asarray(inv_index).size)
+    cnt = int(index.numel() if _is_torch(index) else np.asarray(index).size)
+    A = _Args(device)
+    if not device:
+        if not (isinstance(index, np.ndarray) and index.dtype == np.int64
+                and index.flags.c_contiguous):
+            raise OakError(ERR_ARGS, "index: expected a C-contiguous int64 array (updated in place)")
+    pi = A.vec(index, dtype=np.int64, name="index")
+    pv = A.vec(inv_index, dtype=np.int32, name="inv_index", n=n)
+    _sync_torch(device, index)
+    _check(lib().oakg_obsoper_to_zone_order(cnt, pi, pv, n, MEM_DEVICE if device else MEM_HOST))
+    return index
+

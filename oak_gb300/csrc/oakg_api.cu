@@ -72,7 +72,8 @@ enum BufId {
   B_E_HXF, B_E_HSF, B_E_XA, B_E_SA, B_E_MC, B_E_EA, B_G, B_GV, B_ZAMPL, B_STATUS, B_WORK, B_AUX, B_ZVEC,
   B_ORDER, B_C_E, B_C_MEAN, B_C_S, B_C_OM, B_C_EO, B_C_HE, B_C_HXF, B_C_HSF, B_C_XA, B_C_SA,
   B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_SMWB, B_HSTA, B_GAUG,
-  B_GVAUG, B_GLOB, B_COUNT_
+  B_GVAUG, B_GLOB, B_L_PART, B_L_WORK, B_L_ZS, B_L_ZI, B_L_INV, B_L_X, B_L_Y, B_L_IDX, B_L_MASK,
+  B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_COUNT_
 };
 
 struct Ctx {
@@ -1575,6 +1576,271 @@ int analysis_smw_impl(const oakg_dims* d, const double* xf, const double* Hxf, c
                           nullptr, g0 + 4, g0 + 5, xa, Sa, ampl, nullptr, &sa);
 }
 
+// ---- layout builders: initPartition, the sea packing and genObservationOper / cinterp
+
+// initPartition (assimilation.F90:578-641) on the device: zone sizes, zoneIndex and its inverse
+// (0-based here). A zone number outside 1..nzones or an empty zone is OAKG_ERR_ARGS (the
+// reference stops on both, :605-617).
+int zone_layout_impl(int64_t n, const int32_t* partition, int32_t nzones, int32_t mem,
+                     int32_t* zone_size, int32_t* zone_index, int32_t* inv_index) {
+  if (n <= 0 || n > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "n must be in [1, 2^31-2]");
+  if (nzones < 1) return fail(OAKG_ERR_ARGS, "nzones must be positive (got %d)", nzones);
+  if (!partition || !zone_size || !zone_index)
+    return fail(OAKG_ERR_ARGS, "partition, zone_size and zone_index are required");
+  if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  const int32_t* dpart;
+  int32_t *dzs, *dzi, *dinv, *work;
+  const int64_t nw = zone_layout_work(n, nzones);
+  if ((rc = stage_in(c, B_L_PART, partition, (size_t)n, mem, &dpart, "partition")) ||
+      (rc = stage_out(c, B_L_ZS, zone_size, (size_t)nzones, mem, &dzs, "zone_size")) ||
+      (rc = stage_out(c, B_L_ZI, zone_index, (size_t)n, mem, &dzi, "zone_index")) ||
+      (rc = stage_out(c, B_L_INV, inv_index, (size_t)n, mem, &dinv, "inv_index")) ||
+      (rc = scratch(c, B_L_WORK, (size_t)nw + 1, &work, "layout scratch")))
+    return rc;
+  cudaStream_t st = c->stream;
+  int32_t* dbad = work + nw;
+  cudaError_t e = cudaMemsetAsync(dbad, 0, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = zone_layout(n, dpart, nzones, work, dzs, dzi, dinv, dbad, st);
+  int32_t bad = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, dbad, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST) {
+    e = cudaMemcpyAsync(zone_size, dzs, (size_t)nzones * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(zone_index, dzi, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && inv_index)
+      e = cudaMemcpyAsync(inv_index, dinv, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "zone layout");
+  if (bad & 1) return fail(OAKG_ERR_ARGS, "partition values must lie in 1..%d", nzones);
+  if (bad & 2)
+    return fail(OAKG_ERR_ARGS, "every zone 1..%d must hold at least one element", nzones);
+  return OAKG_OK;
+}
+
+// Y(i, :) = X(index(i), :), i < n, for ncols columns
+int permute_rows_impl(int64_t n, int32_t ncols, const int32_t* index, const double* X,
+                      int64_t ldX, double* Y, int64_t ldY, int32_t mem) {
+  if (n <= 0 || ncols <= 0) return fail(OAKG_ERR_ARGS, "n and ncols must be positive");
+  if (!index || !X || !Y) return fail(OAKG_ERR_ARGS, "index, X and Y are required");
+  if (ldX < n || ldY < n) return fail(OAKG_ERR_ARGS, "ldX and ldY must be >= n");
+  if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  if (mem == OAKG_MEM_DEVICE && X == Y) return fail(OAKG_ERR_ARGS, "X and Y must not alias");
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  const int32_t* didx;
+  const double* dX;
+  double* dY;
+  int32_t* dbad;
+  if ((rc = stage_in(c, B_L_IDX, index, (size_t)n, mem, &didx, "index")) ||
+      (rc = stage_in(c, B_L_X, X, (size_t)ldX * ncols, mem, &dX, "X")) ||
+      (rc = stage_out(c, B_L_Y, Y, (size_t)ldY * ncols, mem, &dY, "Y")) ||
+      (rc = scratch(c, B_L_WORK, 1, &dbad, "permute flag")))
+    return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = cudaMemsetAsync(dbad, 0, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = permute_rows(n, ncols, didx, dX, ldX, dY, ldY, dbad, st);
+  int32_t bad = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, dbad, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(Y, dY, (size_t)ldY * ncols * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "permute rows");
+  if (bad) return fail(OAKG_ERR_ARGS, "index values must lie in [0, %lld)", (long long)n);
+  return OAKG_OK;
+}
+
+// H%j = invZoneIndex(H%j) (assimilation.F90:2404-2407) on an operator's row-form indices
+int obsoper_to_zone_order_impl(int64_t count, int64_t* index, const int32_t* inv_index,
+                               int64_t n, int32_t mem) {
+  if (count < 0 || n <= 0) return fail(OAKG_ERR_ARGS, "count must be >= 0 and n positive");
+  if (count == 0) return OAKG_OK;
+  if (!index || !inv_index) return fail(OAKG_ERR_ARGS, "index and inv_index are required");
+  if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  const int32_t* dinv;
+  int64_t* didx;
+  int32_t* dbad;
+  if ((rc = stage_in(c, B_L_IDX, inv_index, (size_t)n, mem, &dinv, "inv_index")) ||
+      (rc = stage_out(c, B_L_OIDX, index, (size_t)count, mem, &didx, "index")) ||
+      (rc = scratch(c, B_L_WORK, 1, &dbad, "remap flag")))
+    return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(didx, index, (size_t)count * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dbad, 0, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = remap_index(count, didx, dinv, n, dbad, st);
+  int32_t bad = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, dbad, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(index, didx, (size_t)count * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "operator remap");
+  if (bad) return fail(OAKG_ERR_ARGS, "operator index >= n = %lld", (long long)n);
+  return OAKG_OK;
+}
+
+// The sea packing of a masked grid (the reference's StateVectorSizeSea / removeLandPoints):
+// sea[i] = number of unmasked points before point i, or -1 where mask[i] != 0.
+int sea_index_impl(int64_t npts, const uint8_t* mask, int32_t mem, int64_t* sea, int64_t* nsea) {
+  if (npts <= 0 || npts > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "npts must be in [1, 2^31-2]");
+  if (!mask || !sea) return fail(OAKG_ERR_ARGS, "mask and sea are required");
+  if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  const int64_t nt = sea_index_tiles(npts);
+  const uint8_t* dmask;
+  int64_t* dsea;
+  int32_t* tiles;
+  if ((rc = stage_in(c, B_L_MASK, mask, (size_t)npts, mem, &dmask, "mask")) ||
+      (rc = stage_out(c, B_L_SEA, sea, (size_t)npts, mem, &dsea, "sea")) ||
+      (rc = scratch(c, B_L_WORK, (size_t)(2 * (nt + 1)), &tiles, "sea scratch")))
+    return rc;
+  cudaStream_t st = c->stream;
+  cudaError_t e = sea_index(npts, dmask, tiles, dsea, st);
+  int32_t cnt = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&cnt, tiles + (nt + 1) + nt, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(sea, dsea, (size_t)npts * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "sea index");
+  if (nsea) *nsea = cnt;
+  return OAKG_OK;
+}
+
+// split (ndgrid.F90:357-435): the simplices of the unit n-cube, each vertex a combination of
+// the 2^n corners (corner c: bit k set = upper side of axis k). A sub-cube of dimension subn
+// (the corners in sel, the axes in fixed held) becomes, for each free axis and each of its two
+// faces, the face's own split extended by the centroid of sel as vertex subn; an edge
+// (subn = 1) is its two corners in corner order. T[l][v][c], simplex l of the block starting
+// at l0.
+void split_cube(int n, int subn, unsigned fixed, const std::vector<char>& sel, int l0,
+                std::vector<double>& T, int stride) {
+  const int K = 1 << n;
+  auto at = [&](int l, int v, int c) -> double& { return T[(size_t)l * stride + (size_t)v * K + c]; };
+  if (subn == 1) {
+    for (int v = 0; v < 2; v++)
+      for (int cc = 0; cc < K; cc++) at(l0, v, cc) = 0.0;
+    int j = 0;
+    for (int cc = 0; cc < K && j < 2; cc++)
+      if (sel[cc]) at(l0, j++, cc) = 1.0;
+    return;
+  }
+  int cnt = 0;
+  for (int cc = 0; cc < K; cc++) cnt += sel[cc] ? 1 : 0;
+  auto fact = [](int k) {
+    int f = 1;
+    for (int i = 2; i <= k; i++) f *= i;
+    return f;
+  };
+  const int nbth = fact(subn) << (subn - 1), subnbth = fact(subn - 1) << (subn - 2);
+  for (int l = l0; l < l0 + nbth; l++)
+    for (int cc = 0; cc < K; cc++) at(l, subn, cc) = sel[cc] ? 1.0 / cnt : 0.0;
+  int m = l0;
+  std::vector<char> sub(K);
+  for (int i = 0; i < n; i++) {
+    if ((fixed >> i) & 1u) continue;
+    for (int j = 0; j < 2; j++) {
+      for (int cc = 0; cc < K; cc++) sub[cc] = sel[cc] && (((cc >> i) & 1) == j);
+      split_cube(n, subn - 1, fixed | (1u << i), sub, m, T, stride);
+      m += subnbth;
+    }
+  }
+}
+
+// genObservationOper (assimilation.F90:2471-2656) for one variable on a rectilinear grid, with
+// cinterp (ndgrid.F90:1183-1257) and interp_cube (:636-665) on the cells of the grid.
+int obsoper_rectilinear_impl(int32_t ndim, const int32_t* shape, const double* coords,
+                             const int64_t* sea, int64_t offset, int64_t m, const double* pos,
+                             int32_t mem, int64_t* index, double* weight) {
+  if (ndim < 1 || ndim > 4) return fail(OAKG_ERR_ARGS, "ndim must be 1..4 (got %d)", ndim);
+  if (!shape || !coords || !index || !weight || (m > 0 && !pos))
+    return fail(OAKG_ERR_ARGS, "shape, coords, pos, index and weight are required");
+  if (m < 0 || m > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "m must be in [0, 2^31-2]");
+  if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  int64_t npts = 1, ncoord = 0;
+  for (int k = 0; k < ndim; k++) {
+    if (shape[k] < 2)
+      return fail(OAKG_ERR_ARGS, "every axis needs at least 2 points (axis %d has %d)", k,
+                  shape[k]);
+    npts *= shape[k];
+    ncoord += shape[k];
+    if (npts > ((int64_t)1 << 40)) return fail(OAKG_ERR_ARGS, "grid too large");
+  }
+  if (m == 0) return OAKG_OK;
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  // the axes must be strictly monotone (the cell search is a bisection)
+  std::vector<double> hc((size_t)ncoord);
+  cudaError_t e = cudaMemcpy(hc.data(), coords, (size_t)ncoord * sizeof(double),
+                             mem == OAKG_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "coords");
+  for (int k = 0, o = 0; k < ndim; o += shape[k], k++) {
+    const double s = hc[o + 1] - hc[o];
+    for (int i = 0; i + 1 < shape[k]; i++) {
+      const double d = hc[o + i + 1] - hc[o + i];
+      if (!(s > 0 ? d > 0 : d < 0))
+        return fail(OAKG_ERR_ARGS, "coordinates of axis %d are not strictly monotone", k);
+    }
+  }
+  const int K = 1 << ndim, NV = ndim + 1;
+  int nsimplex = 1;
+  for (int i = 2; i <= ndim; i++) nsimplex *= i;
+  nsimplex <<= (ndim - 1);
+  const int stride = NV * K + ndim * NV;
+  std::vector<double> T((size_t)nsimplex * stride, 0.0);
+  split_cube(ndim, ndim, 0u, std::vector<char>(K, 1), 0, T, stride);
+  for (int l = 0; l < nsimplex; l++)
+    for (int k = 0; k < ndim; k++)
+      for (int v = 0; v < NV; v++) {
+        double u = 0.0;
+        for (int cc = 0; cc < K; cc++)
+          if ((cc >> k) & 1) u += T[(size_t)l * stride + (size_t)v * K + cc];
+        T[(size_t)l * stride + NV * K + (size_t)k * NV + v] = u;
+      }
+  const double *dcoords, *dpos;
+  const int64_t* dsea;
+  int64_t* didx;
+  double *dw, *dsimp;
+  if ((rc = stage_in(c, B_L_COORD, coords, (size_t)ncoord, mem, &dcoords, "coords")) ||
+      (rc = stage_in(c, B_L_SEA, sea, (size_t)npts, mem, &dsea, "sea")) ||
+      (rc = stage_in(c, B_L_POS, pos, (size_t)m * ndim, mem, &dpos, "pos")) ||
+      (rc = stage_out(c, B_L_OIDX, index, (size_t)m * K, mem, &didx, "index")) ||
+      (rc = stage_out(c, B_L_OW, weight, (size_t)m * K, mem, &dw, "weight")) ||
+      (rc = scratch(c, B_L_SIMP, T.size(), &dsimp, "simplex table")))
+    return rc;
+  cudaStream_t st = c->stream;
+  e = cudaMemcpyAsync(dsimp, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = rectilinear_oper(ndim, shape, dcoords, dsea, dsimp, nsimplex, m, dpos, offset, didx, dw,
+                         st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST) {
+    e = cudaMemcpyAsync(index, didx, (size_t)m * K * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(weight, dw, (size_t)m * K * sizeof(double), cudaMemcpyDeviceToHost, st);
+  }
+  // T and hc are host vectors read by async copies: finish before they go out of scope
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "rectilinear observation operator");
+  return OAKG_OK;
+}
+
 int release_impl() {
   for (auto& cp : g_ctx) {
     if (!cp) continue;
@@ -1888,6 +2154,50 @@ int oakg_biased_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t 
   return rc;
 }
 
+int oakg_zone_layout(int64_t n, const int32_t* partition, int32_t nzones, int32_t mem,
+                     int32_t* zone_size, int32_t* zone_index, int32_t* inv_index) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::zone_layout_impl(n, partition, nzones, mem, zone_size, zone_index, inv_index);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_permute_rows(int64_t n, int32_t ncols, const int32_t* index, const double* X,
+                      int64_t ldX, double* Y, int64_t ldY, int32_t mem) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::permute_rows_impl(n, ncols, index, X, ldX, Y, ldY, mem);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_obsoper_to_zone_order(int64_t count, int64_t* index, const int32_t* inv_index,
+                               int64_t n, int32_t mem) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::obsoper_to_zone_order_impl(count, index, inv_index, n, mem);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_sea_index(int64_t npts, const uint8_t* mask, int32_t mem, int64_t* sea, int64_t* nsea) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::sea_index_impl(npts, mask, mem, sea, nsea);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_obsoper_rectilinear(int32_t ndim, const int32_t* shape, const double* coords,
+                             const int64_t* sea, int64_t offset, int64_t m, const double* pos,
+                             int32_t mem, int64_t* index, double* weight) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::obsoper_rectilinear_impl(ndim, shape, coords, sea, offset, m, pos, mem, index,
+                                          weight);
+  oakg::last_status() = rc;
+  return rc;
+}
+
 }  // extern "C"
-
-

@@ -90,6 +90,32 @@ cudaError_t zone_gram_fp64_aug(const CellGrid& g, const SortedObs& so, int N, in
                                const double* corr_len, const double* max_len, double* d_G,
                                double* d_g, int32_t* d_nobs, int brute, int32_t* d_work,
                                cudaStream_t st);
+// exclusive scan of n int32 values (out[n] = total), one block
+cudaError_t scan_exclusive_i32(const int32_t* d_in, int64_t n, int32_t* d_out, cudaStream_t st);
+// ---- zone_layout.cu: the zone layout of initPartition and the rectilinear-grid observation
+// operator of genObservationOper / cinterp
+// zone layout of a partition vector (1-based zone numbers): zone sizes, zone_index (sorted
+// position -> element, stable), its inverse (optional); *d_bad |= 1 for a zone number outside
+// 1..nzones, |= 2 for an empty zone. d_work: zone_layout_work(n, nzones) int32 of scratch.
+int64_t zone_layout_work(int64_t n, int32_t nzones);
+cudaError_t zone_layout(int64_t n, const int32_t* d_partition, int32_t nzones, int32_t* d_work,
+                        int32_t* d_zone_size, int32_t* d_zone_index, int32_t* d_inv_index,
+                        int32_t* d_bad, cudaStream_t st);
+// index[t] = inv[index[t]] for 0 <= index[t] < n; *d_bad |= 1 for an entry >= n
+cudaError_t remap_index(int64_t count, int64_t* d_index, const int32_t* d_inv, int64_t n,
+                        int32_t* d_bad, cudaStream_t st);
+// Y(i, :) = X(index(i), :); an index outside [0, n) sets *d_bad and leaves the row 0
+cudaError_t permute_rows(int64_t n, int ncols, const int32_t* d_index, const double* X,
+                         int64_t ldX, double* Y, int64_t ldY, int32_t* d_bad, cudaStream_t st);
+// packed index of the unmasked points (-1 for masked ones); d_tiles: 2 (sea_index_tiles + 1)
+// int32 of scratch, d_tiles[2 tiles + 1] the unmasked count afterwards
+int64_t sea_index_tiles(int64_t npts);
+cudaError_t sea_index(int64_t npts, const uint8_t* d_mask, int32_t* d_tiles, int64_t* d_sea,
+                      cudaStream_t st);
+cudaError_t rectilinear_oper(int ndim, const int32_t* shape, const double* d_coords,
+                             const int64_t* d_sea, const double* d_simplex, int nsimplex,
+                             int64_t m, const double* d_pos, int64_t offset, int64_t* d_index,
+                             double* d_weight, cudaStream_t st);
 // ---- zone_smw.cu: SMWCovar (R = diag(C) + B B^T) support. smw_rows writes the augmented
 // cell-sorted rows [HSt_q | B_perm(q)] (m x (N + k)); smw_reduce turns each zone's augmented
 // products (NA = N + k) into G = X^T X - X^T Y (Y^T Y + I)^-1 Y^T X and the matching g.

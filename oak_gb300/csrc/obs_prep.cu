@@ -295,6 +295,12 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
   return cudaGetLastError();
 }
 
+cudaError_t scan_exclusive_i32(const int32_t* d_in, int64_t n, int32_t* d_out, cudaStream_t st) {
+  k_scan_single<int32_t, int32_t><<<1, kScanThreads, 0, st>>>(d_in, n, d_out, nullptr);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 __global__ void k_to_fp32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)

@@ -367,3 +367,162 @@ def biased_loc_analysis(gamma, zone_size, select, H_index, H_weight, Hshift, xf,
                                  (1.0 - gamma) * np.asarray(r_diag, dtype=np.float64),
                                  localise_obs, rotate)
     return ux + inc2, ba, np.asarray(Sf, dtype=np.float64).copy()
+
+
+# ---------------------------------------------------------------------------- layout builders
+
+def init_partition(partition):
+    """initPartition (assimilation.F90:578-641): zone sizes, zoneIndex and invZoneIndex of a
+    partition vector of 1-based zone numbers (indices 0-based here). Counting pass, start
+    offsets, then every element appended to its zone in element order. Raises ValueError where
+    the reference stops (a zone number < 1, an empty zone)."""
+    p = np.asarray(partition, dtype=np.int64).reshape(-1)
+    if p.size and p.min() < 1:
+        raise ValueError("partition values must be >= 1")
+    nz = int(p.max()) if p.size else 0
+    size = np.bincount(p - 1, minlength=nz).astype(np.int32)
+    if (size == 0).any():
+        raise ValueError("empty zone")
+    start = np.concatenate([[0], np.cumsum(size)[:-1]])
+    cur = start.copy()
+    zone_index = np.empty(p.size, dtype=np.int32)
+    inv = np.empty(p.size, dtype=np.int32)
+    for j, zi in enumerate(p - 1):
+        zone_index[cur[zi]] = j
+        inv[j] = cur[zi]
+        cur[zi] += 1
+    return size, zone_index, inv
+
+
+def sea_index(mask):
+    """Sea packing of a flat mask: running count of the unmasked points, -1 on masked ones."""
+    mk = np.asarray(mask).reshape(-1) != 0
+    sea = np.cumsum(~mk) - 1
+    sea[mk] = -1
+    return sea.astype(np.int64), int((~mk).sum())
+
+
+def split(n):
+    """split (ndgrid.F90:357-435) called as in initgrid (:892): the simplices of the n-cube.
+    Returns T (nbth, n+1, 2^n): vertex v of simplex l as shares of the cube corners (corner c:
+    bit k set = upper side of axis k), nbth = n! 2^(n-1)."""
+    K = 1 << n
+    nbth = math.factorial(n) << (n - 1)
+    T = np.zeros((nbth, n + 1, K))
+
+    def rec(subn, fixed, sel, l0):
+        if subn == 1:
+            T[l0, 0:2, :] = 0.0
+            j = 0
+            for c in range(K):
+                if sel[c]:
+                    T[l0, j, c] = 1.0
+                    j += 1
+            return
+        nb = math.factorial(subn) << (subn - 1)
+        sub_nb = math.factorial(subn - 1) << (subn - 2)
+        cnt = sum(sel)
+        for l in range(l0, l0 + nb):
+            T[l, subn, :] = [1.0 / cnt if s else 0.0 for s in sel]
+        m = l0
+        for i in range(n):
+            if fixed[i]:
+                continue
+            fd = list(fixed)
+            fd[i] = True
+            for j in (0, 1):
+                sub = [sel[c] and (((c >> i) & 1) == j) for c in range(K)]
+                rec(subn - 1, fd, sub, m)
+                m += sub_nb
+
+    rec(n, [False] * n, [True] * K, 0)
+    return T
+
+
+def interp_tetrahedron(X, xi, tol=1e-8):
+    """interp_tetrahedron (ndgrid.F90:464-629), non-degenerate branch: barycentric
+    coordinates c of xi in the simplex X (n, n+1) from [1; X - xc] c = [1; xi - xc] (xc the
+    vertex mean). Returns (out, c, det); det <= tol in magnitude marks the degenerate case
+    (the reference's SVD branch, not restated)."""
+    n = X.shape[0]
+    xc = X.mean(axis=1)
+    M = np.ones((n + 1, n + 1))
+    M[1:, :] = X - xc[:, None]
+    d = np.ones(n + 1)
+    d[1:] = np.asarray(xi) - xc
+    det = np.linalg.det(M)
+    if not abs(det) > tol:
+        return True, None, det
+    c = np.linalg.solve(M, d)
+    out = not bool(np.all((c >= -tol) & (c <= 1 + tol)))
+    return out, c, det
+
+
+def cinterp_rectilinear(axes, xi, sea=None, T=None):
+    """cinterp (ndgrid.F90:1183-1257) on a rectilinear grid: the cell [c(i), c(i+1)] of every
+    axis holding xi (the largest i <= len - 2 with c(i) on the lower side; axes ascending or
+    descending), its 2^n corners (Fortran-order linear index, then the sea packing), out if one
+    is masked, else interp_cube (:636-665): the first simplex of split(n) accepting xi.
+    Returns (status, corner indices (2^n), weights (2^n)); status 'in', 'out' or
+    'degenerate'."""
+    n = len(axes)
+    K = 1 << n
+    if T is None:
+        T = split(n)
+    lo = []
+    for k, c in enumerate(axes):
+        c = np.asarray(c, dtype=np.float64)
+        x = xi[k]
+        asc = c[-1] > c[0]
+        if not (min(c[0], c[-1]) <= x <= max(c[0], c[-1])):
+            return "out", None, None
+        i, hi = 0, len(c) - 1
+        while hi - i > 1:
+            mid = (i + hi) // 2
+            if (c[mid] <= x) if asc else (c[mid] >= x):
+                i = mid
+            else:
+                hi = mid
+        lo.append(i)
+    shape = [len(c) for c in axes]
+    stride = np.cumprod([1] + shape[:-1])
+    px = np.zeros((n, K))
+    idx = np.zeros(K, dtype=np.int64)
+    for cc in range(K):
+        lin = 0
+        for k in range(n):
+            ik = lo[k] + ((cc >> k) & 1)
+            lin += ik * stride[k]
+            px[k, cc] = axes[k][ik]
+        idx[cc] = lin if sea is None else sea[lin]
+    if sea is not None and (idx < 0).any():
+        return "out", None, None
+    for l in range(T.shape[0]):
+        out, c, det = interp_tetrahedron(px @ T[l].T, xi)
+        if c is None:
+            return "degenerate", None, None
+        if not out:
+            return "in", idx, T[l].T @ c
+    return "out", None, None
+
+
+def obsoper_rectilinear(axes, obs_pos, sea=None, offset=0):
+    """genObservationOper (assimilation.F90:2471-2656) for one variable on a rectilinear grid,
+    in the fixed-width row form: (index (m, 2^n), weight (m, 2^n)), index = offset + packed
+    corner index, -1 and weight 0 for an observation outside the grid or next to a masked
+    point, -2 in a degenerate cell."""
+    n = len(axes)
+    K = 1 << n
+    T = split(n)
+    pos = [np.asarray(p, dtype=np.float64).reshape(-1) for p in obs_pos]
+    m = pos[0].size
+    index = np.full((m, K), -1, dtype=np.int64)
+    weight = np.zeros((m, K))
+    for j in range(m):
+        st, idx, w = cinterp_rectilinear(axes, [p[j] for p in pos], sea, T)
+        if st == "in":
+            index[j] = offset + idx
+            weight[j] = w
+        elif st == "degenerate":
+            index[j] = -2
+    return index, weight
