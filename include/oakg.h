@@ -261,6 +261,14 @@ int oakg_biased_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t 
 int oakg_zone_layout(int64_t n, const int32_t* partition, int32_t nzones, int32_t mem,
                      int32_t* zone_size, int32_t* zone_index, int32_t* inv_index);
 
+/* The zone numbering of globalInit (assimilation.F90:416-424): the partition file's labels (any
+ * int32 values, gaps allowed) replaced by their rank, 1-based, among the distinct labels in
+ * ascending order (unique(..., ind2 = partition), matoper.F90:1821-1882); *nzones (optional)
+ * = the number of distinct labels. The result is a partition for oakg_zone_layout. labels and
+ * partition must not alias. */
+int oakg_partition_compact(int64_t n, const int32_t* labels, int32_t mem, int32_t* partition,
+                           int32_t* nzones);
+
 /* Y(i, :) = X(index(i), :) for i < n and ncols columns (column-major, leading dimensions ldX,
  * ldY >= n; X and Y must not alias): with index = zone_index it puts a state vector or an
  * ensemble in zone order (permute, matoper.F90:1166-1183, as in assimilation.F90:766, 4040),
@@ -371,14 +379,43 @@ int64_t oakg_launch_count(void);
  * denominator of the FP64 kernels. */
 int oakg_fp64_peak(double* tflops);
 
-/* OAK's C interface (assimilation.F90:4885-4935), same names and signatures. oak_init checks
- * that the init file is readable (OAKG_ERR_INIT otherwise) and creates the library's device
- * context (stream, events; buffers grow on use); oak_done frees it (as oakg_release). The
- * reference's init-file driver behind oak_assim -- model and observation files (NetCDF / GHER),
- * state packing by masks, observation-operator generation, diagnostics -- is not part of this
- * library: oak_assim records OAKG_ERR_NOTIMPL. Its numerical core is oakg_ens_locanalysis,
- * which a driver calls once it has read the files. The reference's functions return nothing;
- * the status of the last call is oakg_last_status() / oakg_last_error(). */
+/* The data-file reader of the oak_init / oak_assim driver, as the reference's uload
+ * (ufileformat.F90:555-745) reads a NetCDF variable: spec "file.nc#var" (NetCDF classic,
+ * 64-bit-offset or CDF-5 format; NetCDF-4 / HDF5 and GHER binary files are not read). Values in
+ * Fortran order (first dimension fastest) into values (capacity elements; NULL: sizes only),
+ * *count values, shape[0..*ndim) in Fortran order (at most 8 written), *valex the missing
+ * value (missing_value or _FillValue attribute, else -9999); scale_factor / add_offset are
+ * applied to the other values and the compact "shape"-attribute form is expanded. Host only
+ * (no GPU needed). */
+int oakg_read_variable(const char* spec, double* values, int64_t capacity, int64_t* count,
+                       int64_t* shape, int32_t* ndim, double* valex);
+
+/* OAK's C interface (assimilation.F90:4885-4935), same names and signatures, with the
+ * init-file driver of globalInit / Assim for the global (schemetype 0) and local (1) schemes:
+ *  - oak_init(fname) (globalInit, assimilation.F90:253-493) reads the init file. From it:
+ *    - the model's layout from Model.mask (a point is in the state where the mask value is not
+ *      the file's missing value; Model.variables names the variables);
+ *    - the model grids from Model.gridX/Y/Z/T (rectilinear: each coordinate array must be
+ *      separable into one axis per dimension, else OAKG_ERR_NOTIMPL);
+ *    - Model.hres, Model.maxCorrection and inflation.mult;
+ *    - for schemetype 1, the zones: Zones.partition renumbered as the reference does, the zone
+ *      layout, and Zones.corrLength / Zones.maxLength (files or .const) at each zone's first
+ *      element.
+ *    It creates the library's device context.
+ *  - oak_assim(ntime, n, r, Ef, Ea) (Assim, :2977-3574) analyses the n x r ensemble Ef
+ *    (column-major) with the observations ObsNNN.* of time index ntime. Those are: mask,
+ *    variables, value, gridX/Y[/Z/T], rmse (or .const) or SMWCovar.SqrtDiag /
+ *    SMWCovar.ErrorSpace / SMWCovar.dimension, and shift. The steps are:
+ *    - the observation operator is generated on the model grids (oakg_obsoper_rectilinear);
+ *    - observations outside every grid are excluded;
+ *    - on the GPU: H Ef, mean and anomalies, the global or local analysis (the local one in
+ *      zone order), inflation, the maxCorrection clip and Ea = xa + sqrt(r - 1) Sa.
+ *    runtype 0 or 1 returns Ea = Ef.
+ *  - oak_done frees the driver state and the device buffers (as oakg_release).
+ * Not done: diagnostics files (Diag*), biastype, anamorphosis, other schemetypes and operators
+ * read from files (OAKG_ERR_NOTIMPL where the init file asks for them). The reference's
+ * functions return nothing and stop the process on error; these record the status for
+ * oakg_last_status() / oakg_last_error() and leave Ea unchanged. Call them from one thread. */
 void oak_init(const char* fname);
 void oak_assim(int ntime, int n, int r, double* Ef, double* Ea);
 void oak_done(void);

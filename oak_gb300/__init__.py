@@ -29,7 +29,7 @@ __all__ = ["analysis", "loc_analysis", "loc_analysis_adjoint", "OakError", "lib"
            "GAUSS_CUTOFF", "GASPARI_COHN", "CARTESIAN", "SPHERICAL", "SPHERICAL_APPROX",
            "zone_positions", "ensemble_prologue", "ensemble_epilogue", "ens_loc_analysis",
            "ens2sqrt", "sqrt2ens", "ens_analysis", "biased_loc_analysis", "Plan",
-           "zone_layout", "permute_rows", "sea_index", "obsoper_rectilinear",
+           "zone_layout", "partition_compact", "permute_rows", "sea_index", "obsoper_rectilinear",
            "obsoper_to_zone_order"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -154,6 +154,9 @@ def lib() -> ctypes.CDLL:
     L.oakg_biased_locanalysis.restype = ctypes.c_int
     L.oakg_zone_layout.argtypes = [ctypes.c_int64, P, ctypes.c_int32, ctypes.c_int32, P, P, P]
     L.oakg_zone_layout.restype = ctypes.c_int
+    L.oakg_partition_compact.argtypes = [ctypes.c_int64, P, ctypes.c_int32, P,
+                                         ctypes.POINTER(ctypes.c_int32)]
+    L.oakg_partition_compact.restype = ctypes.c_int
     L.oakg_permute_rows.argtypes = [ctypes.c_int64, ctypes.c_int32, P, P, ctypes.c_int64, P,
                                     ctypes.c_int64, ctypes.c_int32]
     L.oakg_permute_rows.restype = ctypes.c_int
@@ -165,6 +168,11 @@ def lib() -> ctypes.CDLL:
     L.oakg_obsoper_rectilinear.argtypes = [ctypes.c_int32, P, P, P, ctypes.c_int64,
                                            ctypes.c_int64, P, ctypes.c_int32, P, P]
     L.oakg_obsoper_rectilinear.restype = ctypes.c_int
+    L.oakg_read_variable.argtypes = [ctypes.c_char_p, P, ctypes.c_int64,
+                                     ctypes.POINTER(ctypes.c_int64), P,
+                                     ctypes.POINTER(ctypes.c_int32),
+                                     ctypes.POINTER(ctypes.c_double)]
+    L.oakg_read_variable.restype = ctypes.c_int
     L.oak_init.argtypes = [ctypes.c_char_p]
     L.oak_init.restype = None
     L.oak_assim.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
@@ -771,6 +779,22 @@ def zone_layout(partition, nzones=None):
     return zs, zi, inv
 
 
+def partition_compact(labels):
+    """The zone numbering of globalInit (oakg_partition_compact, assimilation.F90:416-424):
+    ``(partition, nzones)`` with every label replaced by its 1-based rank among the distinct
+    labels (int32; gaps and any int32 values allowed)."""
+    device = _device_mode(labels)
+    n = int(labels.numel() if _is_torch(labels) else np.asarray(labels).size)
+    A = _Args(device)
+    pl = A.vec(labels, dtype=np.int32, name="labels", n=n)
+    out = _empty_like_mode(device, (n,), dtype=np.int32, like=labels)
+    nz = ctypes.c_int32(0)
+    _sync_torch(device, labels)
+    _check(lib().oakg_partition_compact(n, pl, MEM_DEVICE if device else MEM_HOST,
+                                        A.vec(out, dtype=np.int32), ctypes.byref(nz)))
+    return out, int(nz.value)
+
+
 def permute_rows(index, X):
     """``X[index]`` for a vector (n,) or a column-major matrix (n, k) (oakg_permute_rows):
     with ``index = zone_index`` the state in zone order, with ``inv_index`` back."""
@@ -872,4 +896,49 @@ def obsoper_to_zone_order(index, inv_index):
     _sync_torch(device, index)
     _check(lib().oakg_obsoper_to_zone_order(cnt, pi, pv, n, MEM_DEVICE if device else MEM_HOST))
     return index
+
+
+# ----------------------------------------------------------------------------- OAK driver
+
+def read_variable(spec):
+    """A NetCDF classic-format variable ``"file.nc#var"`` read as the oak_init / oak_assim
+    driver reads it (oakg_read_variable): ``(values (Fortran-ordered array), valex)``, the
+    missing values left as ``valex``. Host only."""
+    L = lib()
+    cnt = ctypes.c_int64(0)
+    nd = ctypes.c_int32(0)
+    vx = ctypes.c_double(0.0)
+    shape = (ctypes.c_int64 * 8)()
+    _check(L.oakg_read_variable(spec.encode(), None, 0, ctypes.byref(cnt), shape,
+                                ctypes.byref(nd), ctypes.byref(vx)))
+    out = np.empty(cnt.value)
+    _check(L.oakg_read_variable(spec.encode(), out.ctypes.data_as(ctypes.c_void_p), out.size,
+                                ctypes.byref(cnt), shape, ctypes.byref(nd), ctypes.byref(vx)))
+    return out.reshape([shape[k] for k in range(nd.value)], order="F"), vx.value
+
+
+def oak_init(fname):
+    """oak_init (assimilation.F90:4911-4916): read the init file; raises OakError on failure."""
+    L = lib()
+    L.oak_init(str(fname).encode())
+    _check(L.oakg_last_status())
+
+
+def oak_assim(ntime, Ef):
+    """oak_assim (assimilation.F90:4919-4927) on a host ensemble ``Ef (n, r)``: returns Ea."""
+    L = lib()
+    E = np.asfortranarray(np.asarray(Ef, dtype=np.float64))
+    n, r = E.shape
+    Ea = np.empty_like(E, order="F")
+    L.oak_assim(int(ntime), int(n), int(r), E.ctypes.data_as(ctypes.c_void_p),
+                Ea.ctypes.data_as(ctypes.c_void_p))
+    _check(L.oakg_last_status())
+    return Ea
+
+
+def oak_done():
+    """oak_done (assimilation.F90:4929-4933)."""
+    L = lib()
+    L.oak_done()
+    _check(L.oakg_last_status())
 

@@ -1,4 +1,5 @@
-"""Build liboakg.so in-tree: every .cu under oak_gb300/csrc compiled for sm_103a, in parallel.
+"""Build liboakg.so in-tree: every .cu (and host-only .cpp) under oak_gb300/csrc compiled, in
+parallel, the CUDA sources for sm_103a.
 
     python -m oak_gb300.build            # incremental
     python -m oak_gb300.build --force    # rebuild everything
@@ -34,7 +35,8 @@ def nvcc_path() -> str:
 
 
 def _deps_mtime() -> float:
-    files = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    files = (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+             + glob.glob(os.path.join(INCLUDE, "*.h")))
     return max((os.path.getmtime(f) for f in files), default=0.0)
 
 
@@ -52,7 +54,7 @@ def _compile(src: str, force: bool, extra: list[str]) -> str:
 
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     extra = list(extra or [])
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, force, extra), srcs))

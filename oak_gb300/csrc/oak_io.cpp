@@ -1,0 +1,491 @@
+// Init-file parser and NetCDF classic-format reader (see oak_io.h). The NetCDF reader follows
+// the published classic / 64-bit-offset / CDF-5 format specification (Unidata, "NetCDF
+// Classic Format Specification"): a big-endian header (magic, record count, dimension,
+// global-attribute and variable lists) followed by the variables' data, record variables
+// interleaved record by record.
+#include "oak_io.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cmath>
+#include <memory>
+
+namespace oakg {
+namespace io {
+
+namespace {
+
+bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\n'; }
+
+bool parse_number(const std::string& tok, double& out) {
+  std::string t = tok;
+  for (char& ch : t)
+    if (ch == 'd' || ch == 'D') ch = 'e';
+  const char* b = t.c_str();
+  char* e = nullptr;
+  out = strtod(b, &e);
+  if (e == b) return false;
+  while (*e && is_space(*e)) e++;
+  return *e == '\0';
+}
+
+}  // namespace
+
+bool InitFile::load(const std::string& fname, std::string& err) {
+  FILE* f = fopen(fname.c_str(), "r");
+  if (!f) {
+    err = "cannot read init file '" + fname + "'";
+    return false;
+  }
+  kv_.clear();
+  quoted_.clear();
+  is_list_.clear();
+  char buf[1 << 14];
+  int lineno = 0;
+  while (fgets(buf, sizeof buf, f)) {
+    lineno++;
+    std::string line(buf);
+    size_t i = 0;
+    auto skip = [&]() {
+      while (i < line.size() && is_space(line[i])) i++;
+    };
+    skip();
+    if (i >= line.size() || line[i] == '#' || line[i] == '!') continue;
+    size_t k0 = i;
+    while (i < line.size() && !is_space(line[i]) && line[i] != '=') i++;
+    std::string key = line.substr(k0, i - k0);
+    skip();
+    if (i >= line.size() || line[i] != '=') {
+      fclose(f);
+      err = fname + ":" + std::to_string(lineno) + ": expected 'key = value'";
+      return false;
+    }
+    i++;
+    std::vector<std::string> items;
+    std::vector<char> quoted;
+    bool list = false, ok = true;
+    auto read_item = [&](bool in_list) -> bool {
+      skip();
+      if (i >= line.size()) return false;
+      if (line[i] == '\'') {
+        std::string s;
+        i++;
+        for (;;) {
+          if (i >= line.size()) return false;  // unterminated
+          if (line[i] == '\'') {
+            if (i + 1 < line.size() && line[i + 1] == '\'') {
+              s += '\'';
+              i += 2;
+              continue;
+            }
+            i++;
+            break;
+          }
+          s += line[i++];
+        }
+        items.push_back(s);
+        quoted.push_back(1);
+        return true;
+      }
+      size_t t0 = i;
+      while (i < line.size() && !is_space(line[i]) && line[i] != ',' &&
+             !(in_list && line[i] == ']') && line[i] != '#' && line[i] != '!')
+        i++;
+      if (i == t0) return false;
+      items.push_back(line.substr(t0, i - t0));
+      quoted.push_back(0);
+      return true;
+    };
+    skip();
+    if (i < line.size() && line[i] == '[') {
+      list = true;
+      i++;
+      skip();
+      if (i < line.size() && line[i] == ']') {
+        i++;
+      } else {
+        for (;;) {
+          if (!read_item(true)) {
+            ok = false;
+            break;
+          }
+          skip();
+          if (i < line.size() && line[i] == ',') {
+            i++;
+            continue;
+          }
+          if (i < line.size() && line[i] == ']') {
+            i++;
+            break;
+          }
+          ok = false;
+          break;
+        }
+      }
+    } else {
+      ok = read_item(false);
+    }
+    if (ok) {
+      skip();
+      ok = i >= line.size() || line[i] == '#' || line[i] == '!';
+    }
+    if (!ok) {
+      fclose(f);
+      err = fname + ":" + std::to_string(lineno) + ": cannot parse the value of '" + key + "'";
+      return false;
+    }
+    if (!kv_.count(key)) {
+      kv_[key] = items;
+      quoted_[key] = quoted;
+      is_list_[key] = list;
+    }
+  }
+  fclose(f);
+  return true;
+}
+
+bool InitFile::str(const std::string& key, std::string& out, std::string& err) const {
+  auto it = kv_.find(key);
+  if (it == kv_.end() || it->second.size() != 1) {
+    err = "init file: '" + key + "' must be one value";
+    return false;
+  }
+  out = it->second[0];
+  return true;
+}
+
+bool InitFile::num(const std::string& key, double& out, std::string& err) const {
+  std::string s;
+  if (!str(key, s, err)) return false;
+  if (quoted_.at(key)[0] || !parse_number(s, out)) {
+    err = "init file: '" + key + "' must be a number";
+    return false;
+  }
+  return true;
+}
+
+bool InitFile::strs(const std::string& key, std::vector<std::string>& out,
+                    std::string& err) const {
+  auto it = kv_.find(key);
+  if (it == kv_.end()) {
+    err = "init file: '" + key + "' is missing";
+    return false;
+  }
+  out = it->second;
+  return true;
+}
+
+bool InitFile::nums(const std::string& key, std::vector<double>& out, std::string& err) const {
+  auto it = kv_.find(key);
+  if (it == kv_.end()) {
+    err = "init file: '" + key + "' is missing";
+    return false;
+  }
+  out.clear();
+  for (size_t q = 0; q < it->second.size(); q++) {
+    double v;
+    if (quoted_.at(key)[q] || !parse_number(it->second[q], v)) {
+      err = "init file: '" + key + "' must hold numbers";
+      return false;
+    }
+    out.push_back(v);
+  }
+  return true;
+}
+
+std::string InitFile::str_or(const std::string& key, const std::string& dflt) const {
+  auto it = kv_.find(key);
+  return (it == kv_.end() || it->second.size() != 1) ? dflt : it->second[0];
+}
+
+double InitFile::num_or(const std::string& key, double dflt) const {
+  std::string e;
+  double v;
+  return (has(key) && num(key, v, e)) ? v : dflt;
+}
+
+// ------------------------------------------------------------------------------ NetCDF
+
+namespace {
+
+enum : int32_t {
+  NC_DIMENSION = 10,
+  NC_VARIABLE = 11,
+  NC_ATTRIBUTE = 12,
+};
+
+int type_size(int t) {
+  switch (t) {
+    case 1: case 2: case 7: return 1;  // byte, char, ubyte
+    case 3: case 8: return 2;          // short, ushort
+    case 4: case 5: case 9: return 4;  // int, float, uint
+    case 6: case 10: case 11: return 8;  // double, int64, uint64
+    default: return 0;
+  }
+}
+
+uint64_t be(const unsigned char* p, int n) {
+  uint64_t v = 0;
+  for (int i = 0; i < n; i++) v = (v << 8) | p[i];
+  return v;
+}
+
+double decode(const unsigned char* p, int t) {
+  switch (t) {
+    case 1: return (double)(int8_t)p[0];
+    case 2: return (double)p[0];
+    case 7: return (double)p[0];
+    case 3: return (double)(int16_t)(uint16_t)be(p, 2);
+    case 8: return (double)(uint16_t)be(p, 2);
+    case 4: return (double)(int32_t)(uint32_t)be(p, 4);
+    case 9: return (double)(uint32_t)be(p, 4);
+    case 10: return (double)(int64_t)be(p, 8);
+    case 11: return (double)be(p, 8);
+    case 5: {
+      uint32_t u = (uint32_t)be(p, 4);
+      float f;
+      memcpy(&f, &u, 4);
+      return (double)f;
+    }
+    case 6: {
+      uint64_t u = be(p, 8);
+      double d;
+      memcpy(&d, &u, 8);
+      return d;
+    }
+    default: return NAN;
+  }
+}
+
+struct Reader {
+  FILE* f = nullptr;
+  int version = 1;
+  bool fail = false;
+  bool bytes(unsigned char* p, size_t n) {
+    if (fail || fread(p, 1, n, f) != n) fail = true;
+    return !fail;
+  }
+  uint64_t u(int n) {
+    unsigned char b[8] = {0};
+    bytes(b, n);
+    return be(b, n);
+  }
+  uint64_t count() { return u(version == 5 ? 8 : 4); }
+  std::string name() {
+    const uint64_t n = count();
+    if (fail || n > 4096) {
+      fail = true;
+      return "";
+    }
+    std::string s(n, '\0');
+    bytes(reinterpret_cast<unsigned char*>(&s[0]), n);
+    const size_t pad = (4 - n % 4) % 4;
+    unsigned char b[4];
+    bytes(b, pad);
+    return s;
+  }
+};
+
+struct Att {
+  std::string name;
+  int type = 0;
+  std::vector<double> vals;
+};
+
+bool read_atts(Reader& r, std::vector<Att>& atts) {
+  const uint64_t tag = r.u(4);
+  const uint64_t n = r.count();
+  if (r.fail) return false;
+  if (tag == 0 && n == 0) return true;
+  if (tag != NC_ATTRIBUTE || n > 100000) return false;
+  for (uint64_t a = 0; a < n; a++) {
+    Att at;
+    at.name = r.name();
+    at.type = (int)r.u(4);
+    const uint64_t ne = r.count();
+    const int ts = type_size(at.type);
+    if (r.fail || ts == 0 || ne > (1u << 24)) return false;
+    const size_t nb = ne * ts, pad = (4 - nb % 4) % 4;
+    std::vector<unsigned char> buf(nb + pad);
+    if (!r.bytes(buf.data(), nb + pad)) return false;
+    if (at.type != 2)
+      for (uint64_t q = 0; q < ne; q++) at.vals.push_back(decode(buf.data() + q * ts, at.type));
+    atts.push_back(at);
+  }
+  return true;
+}
+
+}  // namespace
+
+bool read_array(const std::string& path, const std::string& spec, Array& out, std::string& err) {
+  const size_t hash = spec.rfind('#');
+  if (hash == std::string::npos) {
+    err = "'" + spec + "': only NetCDF variables (file.nc#variable) are read by this library";
+    return false;
+  }
+  const std::string file = path + spec.substr(0, hash), var = spec.substr(hash + 1);
+  std::unique_ptr<FILE, int (*)(FILE*)> fp(fopen(file.c_str(), "rb"), fclose);
+  if (!fp) {
+    err = "cannot open '" + file + "'";
+    return false;
+  }
+  Reader r;
+  r.f = fp.get();
+  unsigned char magic[4];
+  if (!r.bytes(magic, 4) || memcmp(magic, "CDF", 3) != 0 ||
+      (magic[3] != 1 && magic[3] != 2 && magic[3] != 5)) {
+    err = "'" + file + "' is not a NetCDF classic-format file (NetCDF-4/HDF5 is not read)";
+    return false;
+  }
+  r.version = magic[3];
+  const uint64_t numrecs = r.count();
+  // dimensions
+  std::vector<std::string> dname;
+  std::vector<uint64_t> dlen;
+  int recdim = -1;
+  {
+    const uint64_t tag = r.u(4), n = r.count();
+    if (!(tag == 0 && n == 0)) {
+      if (tag != NC_DIMENSION || n > 100000) r.fail = true;
+      for (uint64_t d = 0; d < n && !r.fail; d++) {
+        dname.push_back(r.name());
+        dlen.push_back(r.count());
+        if (dlen.back() == 0) recdim = (int)d;
+      }
+    }
+  }
+  std::vector<Att> gatts;
+  if (r.fail || !read_atts(r, gatts)) {
+    err = "'" + file + "': damaged header";
+    return false;
+  }
+  struct Var {
+    std::string name;
+    std::vector<uint64_t> dims;
+    std::vector<Att> atts;
+    int type = 0;
+    uint64_t vsize = 0, begin = 0;
+  };
+  std::vector<Var> vars;
+  {
+    const uint64_t tag = r.u(4), n = r.count();
+    if (!(tag == 0 && n == 0)) {
+      if (tag != NC_VARIABLE || n > 100000) r.fail = true;
+      for (uint64_t q = 0; q < n && !r.fail; q++) {
+        Var v;
+        v.name = r.name();
+        const uint64_t nd = r.count();
+        if (nd > 64) r.fail = true;
+        for (uint64_t d = 0; d < nd && !r.fail; d++) v.dims.push_back(r.count());
+        if (!r.fail && !read_atts(r, v.atts)) r.fail = true;
+        v.type = (int)r.u(4);
+        v.vsize = r.count();
+        v.begin = r.u(r.version == 1 ? 4 : 8);
+        vars.push_back(v);
+      }
+    }
+  }
+  if (r.fail) {
+    err = "'" + file + "': damaged header";
+    return false;
+  }
+  const Var* vp = nullptr;
+  uint64_t recsize = 0;
+  int nrecvars = 0;
+  for (const Var& v : vars) {
+    const bool rec = !v.dims.empty() && (int)v.dims[0] == recdim;
+    if (rec) {
+      recsize += v.vsize;
+      nrecvars++;
+    }
+    if (v.name == var) vp = &v;
+  }
+  if (!vp) {
+    err = "'" + file + "' has no variable '" + var + "'";
+    return false;
+  }
+  const int ts = type_size(vp->type);
+  if (ts == 0) {
+    err = "'" + file + "#" + var + "': unsupported type";
+    return false;
+  }
+  const bool rec = !vp->dims.empty() && (int)vp->dims[0] == recdim;
+  std::vector<uint64_t> cshape;  // C order
+  for (uint64_t d : vp->dims) {
+    if (d >= dlen.size()) {
+      err = "'" + file + "': bad dimension id";
+      return false;
+    }
+    cshape.push_back((int)d == recdim ? numrecs : dlen[d]);
+  }
+  uint64_t per_rec = 1;
+  for (size_t d = rec ? 1 : 0; d < cshape.size(); d++) per_rec *= cshape[d];
+  const uint64_t nrec = rec ? numrecs : 1;
+  if (rec && nrecvars == 1) recsize = per_rec * ts;  // a lone record variable is not padded
+  // attributes of the variable
+  double scale = 1.0, offset = 0.0;
+  out.valex = -9999.0;
+  std::vector<double> compact_shape;
+  for (const Att& a : vp->atts) {
+    if (a.vals.empty()) continue;
+    if (a.name == "missing_value" || a.name == "_FillValue") out.valex = a.vals[0];
+    else if (a.name == "scale_factor") scale = a.vals[0];
+    else if (a.name == "add_offset") offset = a.vals[0];
+    else if (a.name == "shape") compact_shape = a.vals;
+  }
+  const uint64_t total = per_rec * nrec;
+  if (total > ((uint64_t)1 << 34)) {
+    err = "'" + file + "#" + var + "' is too large";
+    return false;
+  }
+  std::vector<unsigned char> raw((size_t)(total * ts));
+  for (uint64_t q = 0; q < nrec; q++) {
+    const uint64_t off = vp->begin + (rec ? q * recsize : 0);
+    if (fseek(fp.get(), (long)off, SEEK_SET) != 0 ||
+        fread(raw.data() + q * per_rec * ts, 1, per_rec * ts, fp.get()) != per_rec * ts) {
+      err = "'" + file + "#" + var + "': truncated data";
+      return false;
+    }
+  }
+  std::vector<double> vals((size_t)total);
+  for (uint64_t q = 0; q < total; q++) vals[q] = decode(raw.data() + q * ts, vp->type);
+  if (!compact_shape.empty()) {
+    // the compact regular form: x(i_1..i_n) = c(0) + sum_k c(k) (i_k - 1), shape in the
+    // attribute (Fortran order)
+    const size_t nd = compact_shape.size();
+    if (vals.size() < nd + 1) {
+      err = "'" + file + "#" + var + "': compact form needs " + std::to_string(nd + 1) + " values";
+      return false;
+    }
+    out.shape.clear();
+    uint64_t cnt = 1;
+    for (double s : compact_shape) {
+      out.shape.push_back((int64_t)s);
+      cnt *= (uint64_t)s;
+    }
+    out.v.assign((size_t)cnt, 0.0);
+    for (uint64_t e = 0; e < cnt; e++) {
+      uint64_t rem = e;
+      double x = vals[0];
+      for (size_t k = 0; k < nd; k++) {
+        const uint64_t ik = rem % (uint64_t)out.shape[k];
+        rem /= (uint64_t)out.shape[k];
+        x += vals[k + 1] * (double)ik;
+      }
+      out.v[e] = x;
+    }
+    return true;
+  }
+  out.shape.assign(cshape.rbegin(), cshape.rend());
+  if (out.shape.empty()) out.shape.push_back(1);
+  if (scale != 1.0 || offset != 0.0)
+    for (double& x : vals)
+      if (x != out.valex) x = x * scale + offset;
+  out.v.swap(vals);
+  return true;
+}
+
+}  // namespace io
+}  // namespace oakg

@@ -84,6 +84,8 @@ struct Ctx {
   Buf buf[B_COUNT_];
   double timings[5] = {0, 0, 0, 0, 0};
   int64_t chunk_override = 0;  // > 0: zones per chunk fixed (plans: no memory query in capture)
+  // host-memory calls: Sf rows in and Sa / xa rows out per zone chunk, beside the kernels
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
 };
 
 Ctx* g_ctx[64] = {};
@@ -263,7 +265,21 @@ struct ChunkArgs {
   // rows [HS_q | B_q] (m x (N + k))
   int smw_k = 0;
   const double* hst_aug = nullptr;
+  // host-memory pipeline: Sf (host) rows of each chunk copied into a.Sf on a copy stream, the
+  // chunk's Sa / xa rows copied back to the host after its update (rows < n only)
+  const double* sf_host = nullptr;
+  double* sa_host = nullptr;
+  double* xa_host = nullptr;
+  const int64_t* zstart_host = nullptr;  // Z + 1 row offsets
 };
+
+int copy_streams(Ctx* c) {
+  cudaError_t e = cudaSuccess;
+  if (!c->copy_in) e = cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !c->copy_out)
+    e = cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking);
+  return e == cudaSuccess ? OAKG_OK : cuda_fail(e, "copy streams");
+}
 
 // How run_chunks issues its work: timed (events + a host wait per chunk), captured into a CUDA
 // graph (no event, no host wait), or the selection + Gram stage alone (autotuning).
@@ -285,6 +301,10 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
       (a.smw_k > 0 ? ((size_t)NA * NA + NA) * sizeof(double) : 0);
   int64_t chunk = c->chunk_override > 0 ? c->chunk_override
                                         : (int64_t)(chunk_budget_bytes() / per_zone);
+  // host-memory calls: the Sf rows of every chunk go in while the selection, Gram and
+  // eigensolve stages run (they do not read Sf); the zones are not split further for it, as
+  // smaller chunks leave SMs idle in the per-zone stages
+  const bool pipe = a.sf_host != nullptr && mode == RunMode::kTimed;
   if (chunk < 1) chunk = 1;
   if (chunk > a.Z) chunk = a.Z;
   R *d_G, *d_gv, *d_za, *d_aux, *d_zvec;
@@ -303,6 +323,40 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   *status_all = d_work + 2;
   k_set_int<<<1, 1, 0, st>>>(*status_all, 0);
   count_launches(1);
+  // host-memory pipeline: every chunk's Sf rows queued on the input copy stream up front (the
+  // selection + Gram stage needs none of them); the update of chunk q waits for its rows
+  const int64_t nchunks = (a.Z + chunk - 1) / chunk;
+  std::vector<cudaEvent_t> ev_in, ev_out;
+  struct EventsGuard {
+    std::vector<cudaEvent_t>* v[2];
+    ~EventsGuard() {
+      for (auto* p : v)
+        for (cudaEvent_t ev : *p) cudaEventDestroy(ev);
+    }
+  } guard{{&ev_in, &ev_out}};
+  const size_t pitch = (size_t)a.ldS * sizeof(double);
+  if (pipe) {
+    if ((rc = copy_streams(c))) return rc;
+    ev_in.resize(nchunks);
+    ev_out.resize(nchunks);
+    for (int64_t q = 0; q < nchunks; q++) {
+      cudaEventCreateWithFlags(&ev_in[q], cudaEventDisableTiming);
+      cudaEventCreateWithFlags(&ev_out[q], cudaEventDisableTiming);
+    }
+    // the staging buffer is free once the stream's earlier work is done
+    cudaEventRecord(c->ev[7], st);
+    cudaStreamWaitEvent(c->copy_in, c->ev[7], 0);
+    for (int64_t q = 0; q < nchunks; q++) {
+      const int64_t r0 = a.zstart_host[q * chunk],
+                    r1 = a.zstart_host[std::min<int64_t>((q + 1) * chunk, a.Z)];
+      if (r1 > r0 &&
+          (e = cudaMemcpy2DAsync(const_cast<double*>(a.Sf) + r0, pitch, a.sf_host + r0, pitch,
+                                 (size_t)(r1 - r0) * sizeof(double), N, cudaMemcpyHostToDevice,
+                                 c->copy_in)) != cudaSuccess)
+        return cuda_fail(e, "H2D Sf rows");
+      cudaEventRecord(ev_in[q], c->copy_in);
+    }
+  }
   for (int64_t z0 = 0; z0 < a.Z; z0 += chunk) {
     const int32_t nzc = (int32_t)std::min<int64_t>(chunk, a.Z - z0);
     if (timed) cudaEventRecord(c->ev[2], st);
@@ -336,6 +390,7 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
                d_status, d_aux, d_zvec, d_work + 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
     if (timed) cudaEventRecord(c->ev[4], st);
+    if (pipe) cudaStreamWaitEvent(st, ev_in[z0 / chunk], 0);
     e = K::update(N, (int32_t)z0, nzc, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, (const R*)d_G,
                   (const R*)d_za, (const int32_t*)(a.nobs + z0), a.xa, a.Sa, st);
     if (e != cudaSuccess) return cuda_fail(e, "update kernel");
@@ -347,11 +402,31 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     }
     k_or_status<<<64, 256, 0, st>>>(d_status, nzc, *status_all);
     count_launches(1);
+    if (pipe) {
+      const int64_t q = z0 / chunk, r0 = a.zstart_host[z0], r1 = a.zstart_host[z0 + nzc];
+      cudaEventRecord(ev_out[q], st);
+      cudaStreamWaitEvent(c->copy_out, ev_out[q], 0);
+      if (r1 > r0) {
+        if (a.sa_host &&
+            (e = cudaMemcpy2DAsync(a.sa_host + r0, pitch, a.Sa + r0, pitch,
+                                   (size_t)(r1 - r0) * sizeof(double), N,
+                                   cudaMemcpyDeviceToHost, c->copy_out)) != cudaSuccess)
+          return cuda_fail(e, "D2H Sa rows");
+        if ((e = cudaMemcpyAsync(a.xa_host + r0, a.xa + r0, (size_t)(r1 - r0) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, c->copy_out)) != cudaSuccess)
+          return cuda_fail(e, "D2H xa rows");
+      }
+    }
     if (!timed) continue;
     if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
     *t_gram += elapsed(c->ev[2], c->ev[3]);
     *t_eig += elapsed(c->ev[3], c->ev[4]);
     *t_upd += elapsed(c->ev[4], c->ev[5]);
+  }
+  if (pipe) {
+    // the call's final synchronisation of the stream covers the output copies
+    cudaEventRecord(c->ev[7], c->copy_out);
+    cudaStreamWaitEvent(st, c->ev[7], 0);
   }
   return OAKG_OK;
 }
@@ -449,7 +524,7 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
                 const double* yo, const double* Sf, const double* HSf, const double* r_diag,
                 const double* zone_xyzt, const double* obs_x, const double* obs_y,
                 const double* obs_z, const double* obs_t, const double* corr_len,
-                const double* max_len, Prep* P) {
+                const double* max_len, Prep* P, bool defer_sf = false) {
   const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
   const int N = dims->N, mem = dims->mem;
   int rc;
@@ -467,7 +542,14 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   *P = Prep{};
   if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &P->zsize, "zone_size"))) return rc;
   if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &P->xf, "xf"))) return rc;
-  if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &P->Sf, "Sf"))) return rc;
+  if (defer_sf && mem == OAKG_MEM_HOST) {
+    // host-memory pipeline: the rows are copied per zone chunk by run_chunks
+    double* d_sf;
+    if ((rc = scratch(c, B_SF, (size_t)ldS * N, &d_sf, "Sf"))) return rc;
+    P->Sf = d_sf;
+  } else if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &P->Sf, "Sf"))) {
+    return rc;
+  }
   if ((rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &P->zxyzt, "zone_xyzt"))) return rc;
   if ((rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &P->corr, "corr_len"))) return rc;
   if ((rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &P->maxl, "max_len"))) return rc;
@@ -580,9 +662,18 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   cudaStream_t st = c->stream;
   cudaError_t e;
   cudaEventRecord(c->ev[0], st);
+  // host memory: Sf in and Sa / xa out per zone chunk beside the kernels (rows < n; with
+  // ldS > n the whole arrays are staged as before)
+  const bool pipe = mem == OAKG_MEM_HOST && Sa && Sf && ldS == n && Z >= 2;
+  std::vector<int64_t> zstart_h;
+  if (pipe) {
+    zstart_h.resize((size_t)Z + 1);
+    zstart_h[0] = 0;
+    for (int32_t z = 0; z < Z; z++) zstart_h[z + 1] = zstart_h[z] + zone_size[z];
+  }
   Prep P;
   if ((rc = prepare_loc(c, dims, loc, Z, zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
-                        obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &P)))
+                        obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &P, pipe)))
     return rc;
   double *d_xa, *d_Sa, *d_ampl;
   int32_t* d_nobs;
@@ -594,7 +685,7 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   } else if ((rc = scratch(c, B_NOBS, (size_t)Z, &d_nobs, "nobs"))) {
     return rc;
   }
-  if (mem == OAKG_MEM_HOST && Sa) {
+  if (mem == OAKG_MEM_HOST && Sa && !pipe) {
     // rows beyond n (ldS > n) are returned unchanged
     e = cudaMemcpyAsync(d_Sa, P.Sf, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToDevice,
                         st);
@@ -609,6 +700,12 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   int32_t* d_status_all = nullptr;
   ChunkArgs ca{P.g, P.so, lp, Z, N, ldS, P.zone_max, P.brute, all_ampl, P.zxyzt, P.corr, P.maxl,
                P.zstart, P.xf, P.Sf, d_xa, d_Sa, d_ampl, d_nobs};
+  if (pipe) {
+    ca.sf_host = Sf;
+    ca.sa_host = Sa;
+    ca.xa_host = xa;
+    ca.zstart_host = zstart_h.data();
+  }
   if (smw_k > 0) {
     // the augmented cell-sorted rows [HS_q | B_q] of the SMWCovar products
     const int64_t m = dims->m;
@@ -634,10 +731,11 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
       cudaSuccess)
     return cuda_fail(e, "D2H");
   if (mem == OAKG_MEM_HOST) {
-    if ((e = cudaMemcpyAsync(xa, d_xa, n * sizeof(double), cudaMemcpyDeviceToHost, st)))
+    if (!pipe && (e = cudaMemcpyAsync(xa, d_xa, n * sizeof(double), cudaMemcpyDeviceToHost, st)))
       return cuda_fail(e, "D2H xa");
-    if (Sa && (e = cudaMemcpyAsync(Sa, d_Sa, (size_t)ldS * N * sizeof(double),
-                                   cudaMemcpyDeviceToHost, st)))
+    if (Sa && !pipe &&
+        (e = cudaMemcpyAsync(Sa, d_Sa, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToHost,
+                             st)))
       return cuda_fail(e, "D2H Sa");
     if (ampl && (e = cudaMemcpyAsync(ampl, d_ampl, (size_t)N * Z * sizeof(double),
                                      cudaMemcpyDeviceToHost, st)))
@@ -1585,6 +1683,9 @@ int zone_layout_impl(int64_t n, const int32_t* partition, int32_t nzones, int32_
                      int32_t* zone_size, int32_t* zone_index, int32_t* inv_index) {
   if (n <= 0 || n > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "n must be in [1, 2^31-2]");
   if (nzones < 1) return fail(OAKG_ERR_ARGS, "nzones must be positive (got %d)", nzones);
+  if (nzones > n)
+    return fail(OAKG_ERR_ARGS, "every zone 1..%d must hold at least one element (n = %lld)",
+                nzones, (long long)n);
   if (!partition || !zone_size || !zone_index)
     return fail(OAKG_ERR_ARGS, "partition, zone_size and zone_index are required");
   if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
@@ -1619,6 +1720,40 @@ int zone_layout_impl(int64_t n, const int32_t* partition, int32_t nzones, int32_
   if (bad & 1) return fail(OAKG_ERR_ARGS, "partition values must lie in 1..%d", nzones);
   if (bad & 2)
     return fail(OAKG_ERR_ARGS, "every zone 1..%d must hold at least one element", nzones);
+  return OAKG_OK;
+}
+
+// The zone numbering of globalInit (assimilation.F90:416-424): partition labels, any int32
+// values with gaps, replaced by their rank among the distinct labels (unique(..., ind2 =
+// partition), matoper.F90:1821-1882).
+int partition_compact_impl(int64_t n, const int32_t* labels, int32_t mem, int32_t* partition,
+                           int32_t* nzones) {
+  if (n <= 0 || n > INT32_MAX - 1) return fail(OAKG_ERR_ARGS, "n must be in [1, 2^31-2]");
+  if (!labels || !partition) return fail(OAKG_ERR_ARGS, "labels and partition are required");
+  if (mem != OAKG_MEM_HOST && mem != OAKG_MEM_DEVICE)
+    return fail(OAKG_ERR_ARGS, "mem must be OAKG_MEM_HOST or OAKG_MEM_DEVICE");
+  Ctx* c = nullptr;
+  int rc = get_ctx(&c);
+  if (rc) return rc;
+  const int32_t* dl;
+  int32_t *dp, *work;
+  const int64_t nw = partition_compact_work(n);
+  if ((rc = stage_in(c, B_L_PART, labels, (size_t)n, mem, &dl, "labels")) ||
+      (rc = stage_out(c, B_L_ZI, partition, (size_t)n, mem, &dp, "partition")) ||
+      (rc = scratch(c, B_L_WORK, (size_t)nw, &work, "compaction scratch")))
+    return rc;
+  if (mem == OAKG_MEM_DEVICE && (const void*)labels == (const void*)partition)
+    return fail(OAKG_ERR_ARGS, "labels and partition must not alias");
+  cudaStream_t st = c->stream;
+  cudaError_t e = partition_compact(n, dl, work, dp, st);
+  int32_t nz = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&nz, work + 5 * n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+    e = cudaMemcpyAsync(partition, dp, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "partition compaction");
+  if (nzones) *nzones = nz;
   return OAKG_OK;
 }
 
@@ -1850,6 +1985,8 @@ int release_impl() {
     cudaStreamSynchronize(cp->stream);
     for (auto& b : cp->buf) b.release();
     for (auto& ev : cp->ev) cudaEventDestroy(ev);
+    if (cp->copy_in) cudaStreamDestroy(cp->copy_in);
+    if (cp->copy_out) cudaStreamDestroy(cp->copy_out);
     cudaStreamDestroy(cp->own_stream);
     cudaSetDevice(prev);
     delete cp;
@@ -2159,6 +2296,15 @@ int oakg_zone_layout(int64_t n, const int32_t* partition, int32_t nzones, int32_
   std::lock_guard<std::mutex> lk(oakg::api_mutex());
   oakg::set_ok();
   int rc = oakg::zone_layout_impl(n, partition, nzones, mem, zone_size, zone_index, inv_index);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_partition_compact(int64_t n, const int32_t* labels, int32_t mem, int32_t* partition,
+                           int32_t* nzones) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::partition_compact_impl(n, labels, mem, partition, nzones);
   oakg::last_status() = rc;
   return rc;
 }

@@ -101,6 +101,12 @@ int64_t zone_layout_work(int64_t n, int32_t nzones);
 cudaError_t zone_layout(int64_t n, const int32_t* d_partition, int32_t nzones, int32_t* d_work,
                         int32_t* d_zone_size, int32_t* d_zone_index, int32_t* d_inv_index,
                         int32_t* d_bad, cudaStream_t st);
+// the reference's unique(partition, n, ind2 = partition) (assimilation.F90:420-424): every
+// label replaced by its rank (1-based) among the distinct labels in ascending order; the number
+// of distinct labels is d_work[5 n] afterwards
+int64_t partition_compact_work(int64_t n);
+cudaError_t partition_compact(int64_t n, const int32_t* d_labels, int32_t* d_work,
+                              int32_t* d_out, cudaStream_t st);
 // index[t] = inv[index[t]] for 0 <= index[t] < n; *d_bad |= 1 for an entry >= n
 cudaError_t remap_index(int64_t count, int64_t* d_index, const int32_t* d_inv, int64_t n,
                         int32_t* d_bad, cudaStream_t st);

@@ -387,55 +387,168 @@ __global__ void k_sea_tile_write(int64_t npts, const uint8_t* __restrict__ mask,
     }
 }
 
-}  // namespace
-
-int64_t zone_layout_work(int64_t n, int32_t nzones) {
-  const int64_t ntiles = (n + kRadixTile - 1) / kRadixTile;
-  return 3 * n + 2 * (kThreads * ntiles + 1) + 2 * ((int64_t)nzones + 1) + 4;
+// exclusive scan of int32 values in tiles of kScanTile (kPerThread consecutive values per
+// thread): tile sums, a scan of the sums, then each tile's values from its start
+__global__ void k_tile_sum_i32(int64_t n, const int32_t* __restrict__ in,
+                               int32_t* __restrict__ tile_sum) {
+  const int64_t t0 = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kPerThread;
+  int s = 0;
+#pragma unroll
+  for (int q = 0; q < kPerThread; q++) s += t0 + q < n ? in[t0 + q] : 0;
+  int total;
+  block_excl_scan(s, &total);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
 }
 
-cudaError_t zone_layout(int64_t n, const int32_t* d_partition, int32_t nzones, int32_t* d_work,
-                        int32_t* d_zone_size, int32_t* d_zone_index, int32_t* d_inv_index,
-                        int32_t* d_bad, cudaStream_t st) {
+__global__ void k_tile_scan_i32(int64_t n, const int32_t* __restrict__ in,
+                                const int32_t* __restrict__ tile_start,
+                                int32_t* __restrict__ out) {
+  const int64_t t0 = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kPerThread;
+  int v[kPerThread];
+  int s = 0;
+#pragma unroll
+  for (int q = 0; q < kPerThread; q++) {
+    v[q] = t0 + q < n ? in[t0 + q] : 0;
+    s += v[q];
+  }
+  int total;
+  int32_t run = tile_start[blockIdx.x] + block_excl_scan(s, &total);
+#pragma unroll
+  for (int q = 0; q < kPerThread; q++)
+    if (t0 + q < n) {
+      out[t0 + q] = run;
+      run += v[q];
+      if (t0 + q == n - 1) out[n] = run;
+    }
+}
+
+// element indices in the stable order of the low 8 * passes bits of key (as unsigned digits)
+__global__ void k_flag_new(int64_t n, const int32_t* __restrict__ sorted,
+                           int32_t* __restrict__ flag) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x)
+    flag[s] = (s == 0 || sorted[s] != sorted[s - 1]) ? 1 : 0;
+}
+
+__global__ void k_bias_keys(int64_t n, const int32_t* __restrict__ in, int32_t* __restrict__ out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = (int32_t)((uint32_t)in[j] ^ 0x80000000u);  // signed order as unsigned digits
+}
+
+__global__ void k_scatter_rank(int64_t n, const int32_t* __restrict__ perm,
+                               const int32_t* __restrict__ rank, const int32_t* __restrict__ flag,
+                               int32_t* __restrict__ out) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x)
+    out[perm[s]] = rank[s] + flag[s];
+}
+
+int64_t scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
+// out[0..n] = exclusive scan of in[0..n), out[n] the total; tiles: 2 (scan_tiles(n) + 1) int32
+cudaError_t scan_tiled_i32(int64_t n, const int32_t* in, int32_t* out, int32_t* tiles,
+                           cudaStream_t st) {
+  const int64_t nt = scan_tiles(n);
+  int32_t* sum = tiles;
+  int32_t* start = tiles + nt + 1;
+  k_tile_sum_i32<<<(unsigned)nt, kThreads, 0, st>>>(n, in, sum);
+  count_launches(1);
+  cudaError_t e = scan_exclusive_i32(sum, nt, start, st);
+  if (e != cudaSuccess) return e;
+  k_tile_scan_i32<<<(unsigned)nt, kThreads, 0, st>>>(n, in, start, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// scratch of radix_sort_index, in int32
+int64_t radix_work(int64_t n) {
   const int64_t ntiles = (n + kRadixTile - 1) / kRadixTile, nh = kThreads * ntiles;
-  int32_t* key = d_work;
-  int32_t* ktmp = key + n;
-  int32_t* vtmp = ktmp + n;
+  return 3 * n + 2 * (nh + 1) + 2 * (scan_tiles(nh) + 1);
+}
+
+// Stable LSD radix sort over the low 8 * passes bits of key: vals_out[s] = the element at sorted
+// position s; keys_out (optional) the sorted keys.
+cudaError_t radix_sort_index(int64_t n, const int32_t* key, int passes, int32_t* work,
+                             int32_t* vals_out, int32_t* keys_out, cudaStream_t st) {
+  const int64_t ntiles = (n + kRadixTile - 1) / kRadixTile, nh = kThreads * ntiles;
+  int32_t* kA = work;
+  int32_t* kB = kA + n;
+  int32_t* vtmp = kB + n;
   int32_t* hist = vtmp + n;
   int32_t* offs = hist + nh + 1;
-  int32_t* count = offs + nh + 1;
-  int32_t* start = count + nzones + 1;
-  k_zone_keys<<<grid_for(n), kThreads, 0, st>>>(n, d_partition, key);
-  cudaError_t e = cudaMemsetAsync(count, 0, ((size_t)nzones + 1) * sizeof(int32_t), st);
-  if (e != cudaSuccess) return e;
-  k_key_count_i32<<<grid_for(n), kThreads, 0, st>>>(n, key, nzones, count, d_bad);
-  count_launches(2);
-  if ((e = scan_exclusive_i32(count, nzones, start, st)) != cudaSuccess) return e;
-  k_zone_sizes<<<grid_for(nzones), kThreads, 0, st>>>(nzones, start, d_zone_size, d_bad);
-  count_launches(1);
-  int bits = 1;
-  while (bits < 31 && ((int64_t)1 << bits) < (int64_t)nzones) bits++;
-  const int passes = (bits + 7) / 8;
+  int32_t* tiles = offs + nh + 1;
   const int32_t* kin = key;
   const int32_t* vin = nullptr;
+  cudaError_t e = cudaSuccess;
   for (int p = 0; p < passes; p++) {
     const bool last = p == passes - 1;
-    // the last pass writes zone_index; ping-pong so that it does
-    int32_t* vout = ((passes - 1 - p) % 2 == 0) ? d_zone_index : vtmp;
-    int32_t* kout = last ? nullptr : (p % 2 == 0 ? ktmp : key);
+    int32_t* vout = ((passes - 1 - p) % 2 == 0) ? vals_out : vtmp;  // the last pass: vals_out
+    int32_t* kout = last ? keys_out : (p % 2 == 0 ? kA : kB);
     k_radix_hist<<<(unsigned)ntiles, kThreads, 0, st>>>(n, kin, 8 * p, hist, ntiles);
     count_launches(1);
-    if ((e = scan_exclusive_i32(hist, nh, offs, st)) != cudaSuccess) return e;
+    if ((e = scan_tiled_i32(nh, hist, offs, tiles, st)) != cudaSuccess) return e;
     k_radix_scatter<<<(unsigned)ntiles, kThreads, 0, st>>>(n, kin, vin, 8 * p, offs, ntiles,
                                                            kout, vout);
     count_launches(1);
     kin = kout;
     vin = vout;
   }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int64_t zone_layout_work(int64_t n, int32_t nzones) {
+  return n + 2 * ((int64_t)nzones + 1) + radix_work(n) + 4;
+}
+
+cudaError_t zone_layout(int64_t n, const int32_t* d_partition, int32_t nzones, int32_t* d_work,
+                        int32_t* d_zone_size, int32_t* d_zone_index, int32_t* d_inv_index,
+                        int32_t* d_bad, cudaStream_t st) {
+  int32_t* key = d_work;
+  int32_t* count = key + n;
+  int32_t* start = count + nzones + 1;
+  int32_t* rwork = start + nzones + 1;
+  k_zone_keys<<<grid_for(n), kThreads, 0, st>>>(n, d_partition, key);
+  cudaError_t e = cudaMemsetAsync(count, 0, ((size_t)nzones + 1) * sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  k_key_count_i32<<<grid_for(n), kThreads, 0, st>>>(n, key, nzones, count, d_bad);
+  count_launches(2);
+  if ((e = scan_tiled_i32(nzones, count, start, rwork, st)) != cudaSuccess) return e;
+  k_zone_sizes<<<grid_for(nzones), kThreads, 0, st>>>(nzones, start, d_zone_size, d_bad);
+  count_launches(1);
+  int bits = 1;
+  while (bits < 31 && ((int64_t)1 << bits) < (int64_t)nzones) bits++;
+  if ((e = radix_sort_index(n, key, (bits + 7) / 8, rwork, d_zone_index, nullptr, st)) !=
+      cudaSuccess)
+    return e;
   if (d_inv_index) {
     k_invert<<<grid_for(n), kThreads, 0, st>>>(n, d_zone_index, d_inv_index);
     count_launches(1);
   }
+  return cudaGetLastError();
+}
+
+int64_t partition_compact_work(int64_t n) { return 5 * n + 1 + radix_work(n) + 4; }
+
+cudaError_t partition_compact(int64_t n, const int32_t* d_labels, int32_t* d_work,
+                              int32_t* d_out, cudaStream_t st) {
+  int32_t* key = d_work;
+  int32_t* perm = key + n;
+  int32_t* sorted = perm + n;
+  int32_t* flag = sorted + n;
+  int32_t* rank = flag + n;  // n + 1, rank[n] = number of distinct labels
+  int32_t* rwork = rank + n + 1;
+  k_bias_keys<<<grid_for(n), kThreads, 0, st>>>(n, d_labels, key);
+  count_launches(1);
+  cudaError_t e = radix_sort_index(n, key, 4, rwork, perm, sorted, st);
+  if (e != cudaSuccess) return e;
+  k_flag_new<<<grid_for(n), kThreads, 0, st>>>(n, sorted, flag);
+  count_launches(1);
+  if ((e = scan_tiled_i32(n, flag, rank, rwork, st)) != cudaSuccess) return e;
+  k_scatter_rank<<<grid_for(n), kThreads, 0, st>>>(n, perm, rank, flag, d_out);
+  count_launches(1);
   return cudaGetLastError();
 }
 

@@ -526,3 +526,12 @@ def obsoper_rectilinear(axes, obs_pos, sea=None, offset=0):
         elif st == "degenerate":
             index[j] = -2
     return index, weight
+
+
+def partition_compact(labels):
+    """globalInit's zone numbering (assimilation.F90:416-424): unique(..., ind2 = partition)
+    (matoper.F90:1821-1882), every label replaced by its 1-based rank among the distinct labels
+    in ascending order. Returns (partition, number of distinct labels)."""
+    lab = np.asarray(labels).reshape(-1)
+    u, inv = np.unique(lab, return_inverse=True)
+    return (inv + 1).astype(np.int32), int(u.size)

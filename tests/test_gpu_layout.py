@@ -168,3 +168,19 @@ def test_operator_to_zone_order(oakg):
     bad[0, 0] = 2000
     with pytest.raises(oakg.OakError):
         oakg.obsoper_to_zone_order(bad, inv)
+
+
+@pytest.mark.parametrize("n", [1, 5000, 2_000_000])
+def test_partition_compact_matches_unique(oakg, n):
+    """Labels over the whole int32 range, with gaps and repeats, host and device memory."""
+    rng = np.random.default_rng(n)
+    pool = rng.integers(-2**31, 2**31 - 1, size=max(1, n // 7), dtype=np.int64)
+    labels = pool[rng.integers(0, pool.size, size=n)].astype(np.int32)
+    part_o, nz_o = R.partition_compact(labels)
+    part, nz = oakg.partition_compact(labels)
+    assert nz == nz_o and np.array_equal(part, part_o)
+    part_d, nz_d = oakg.partition_compact(_dev(labels))
+    assert nz_d == nz_o and np.array_equal(part_d.cpu().numpy(), part_o)
+    # the compacted partition feeds the zone layout directly
+    zs, zi, _ = oakg.zone_layout(part, nz)
+    assert np.array_equal(zs, np.bincount(part_o)[1:])

@@ -284,3 +284,41 @@ def test_rank_deficient_zones(oakg, N):
     assert np.array_equal(nobs, nobs_o)
     assert nobs.max() < N
     check_local(xa, Sa, xa_o, Sa_o, P["xf"])
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_pipeline_matches_device(oakg, pinned):
+    """Host-memory calls copy Sf in on a copy stream while the selection, Gram and eigensolve
+    stages run, and Sa / xa out per zone chunk; the kernels are those of device-memory calls,
+    so both forms must agree bit for bit, with pageable and with pinned host buffers."""
+    import torch
+    from oak_gb300.workloads import local_case
+    c = local_case(scale=1 / 6, N=64)
+    dev = torch.device("cuda:0")
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    F = lambda a: torch.as_tensor(np.ascontiguousarray(np.asarray(a).T), device=dev).t()
+
+    def host(a, fortran=False):
+        a = np.asarray(a)
+        if not pinned:
+            return np.asfortranarray(a) if fortran else np.ascontiguousarray(a)
+        if fortran:
+            t = torch.empty((a.shape[1], a.shape[0]), dtype=torch.float64, pin_memory=True)
+            t.numpy()[...] = a.T
+            return t.numpy().T
+        t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0].copy()).dtype, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    for prec in (oakg.PREC_FP64, oakg.PREC_MIXED):
+        kw = dict(weight=c.weight, precision=prec)
+        h = oakg.loc_analysis(host(c.zone_size), host(c.xf), host(c.Hxf), host(c.yo),
+                              host(c.Sf, True), host(c.HSf, True), host(c.r_diag),
+                              host(c.zone_pos), tuple(host(x) for x in c.obs_pos),
+                              host(c.corr_len), host(c.max_len), **kw)
+        d = oakg.loc_analysis(T(c.zone_size), T(c.xf), T(c.Hxf), T(c.yo), F(c.Sf), F(c.HSf),
+                              T(c.r_diag), T(c.zone_pos), tuple(T(x) for x in c.obs_pos),
+                              T(c.corr_len), T(c.max_len), **kw)
+        assert np.array_equal(h[3], d[3].cpu().numpy())
+        assert np.array_equal(h[0], d[0].cpu().numpy())
+        assert np.array_equal(h[1], d[1].cpu().numpy())

@@ -118,3 +118,9 @@ def test_init_partition():
         R.init_partition(np.array([1, 0, 2]))
     with pytest.raises(ValueError):
         R.init_partition(np.array([1, 3, 3]))
+
+
+def test_partition_compact_hand_case():
+    """unique(..., ind2 = partition): labels replaced by their rank among the distinct ones."""
+    part, nz = R.partition_compact(np.array([5, -3, 5, 100, -3, 7]))
+    assert nz == 4 and list(part) == [2, 1, 2, 4, 1, 3]
