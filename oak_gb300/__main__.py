@@ -2,13 +2,17 @@
 
   python -m oak_gb300 local [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--m M]
   python -m oak_gb300 batched [--scale S] [--precision fp64|mixed] [--calls K] [--N N]
+  python -m oak_gb300 layout [--obs M] [--calls K]
 
 ``local`` builds the seeded single-variable case (360 x 180 x 20 columns scaled horizontally by
 S, N = 64, Gaspari-Cohn radius 12 cells); ``batched`` the 5-variable case (720 x 360 columns of
 121 elements scaled by S, N = 100, bilinear observations clustered on tracks). Either is moved
 to cuda:0 and :func:`oak_gb300.loc_analysis` is called K times, printing the device time of
 each stage of the last call. Used to run one precision's kernels in isolation (profiling,
-quick timing); the full benchmark is bench.py.
+quick timing); the full benchmark is bench.py. ``layout`` runs the layout builders on one
+3-D variable of 720 x 360 x 50 points with a land mask and 259,200 column zones: the zone
+layout, the sea packing and the rectilinear observation operator for M observations (K
+calls each), printing the last call's wall time per builder.
 """
 from __future__ import annotations
 
@@ -33,11 +37,18 @@ def main(argv=None):
     bp.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     bp.add_argument("--calls", type=int, default=2)
     bp.add_argument("--N", type=int, default=100)
+    yp = sub.add_parser("layout", help="run the layout builders on cuda:0")
+    yp.add_argument("--obs", type=int, default=1_000_000)
+    yp.add_argument("--calls", type=int, default=2)
     a = p.parse_args(argv)
 
     import torch
     import oak_gb300
     from oak_gb300.workloads import batched_case, local_case
+
+    if a.cmd == "layout":
+        layout(a, torch, oak_gb300)
+        return
 
     if a.cmd == "local":
         c = local_case(scale=a.scale, N=a.N, m=a.m)
@@ -56,6 +67,36 @@ def main(argv=None):
     print(json.dumps({"workload": c.name, "zones": int(c.Z), "N": int(c.N), "m": int(c.m),
                       "precision": a.precision, "calls": a.calls,
                       "stage_ms_last_call": oak_gb300.last_timings()}))
+
+
+def layout(a, torch, oak_gb300):
+    import time
+    dev = torch.device("cuda", 0)
+    nx, ny, nz = 720, 360, 50
+    rng = np.random.default_rng(12)
+    part = (torch.arange(nx * ny * nz, device=dev) % (nx * ny) + 1).to(torch.int32)
+    mask = np.zeros((nx, ny, nz), dtype=bool)
+    mask[100:200, 50:120, :] = True
+    mask_d = torch.as_tensor(mask.reshape(-1, order="F"), device=dev)
+    z = np.cumsum(rng.uniform(1.0, 50.0, nz))
+    axes = [torch.as_tensor(v, device=dev) for v in
+            (np.linspace(-180.0, 179.5, nx), np.linspace(-89.75, 89.75, ny), z)]
+    pos = [torch.as_tensor(rng.uniform(lo, hi, a.obs), device=dev)
+           for lo, hi in ((-180.0, 179.5), (-89.75, 89.75), (z[0], z[-1]))]
+    ms = {}
+    for name, fn in (("zone_layout", lambda: oak_gb300.zone_layout(part, nx * ny)),
+                     ("sea_index", lambda: oak_gb300.sea_index(mask_d)),
+                     ("obsoper_rectilinear",
+                      lambda: oak_gb300.obsoper_rectilinear(axes, pos,
+                                                            sea=oak_gb300.sea_index(mask_d)[0]))):
+        for _ in range(a.calls):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize(dev)
+            ms[name] = (time.perf_counter() - t0) * 1e3
+    print(json.dumps({"grid": [nx, ny, nz], "zones": nx * ny, "obs": a.obs, "calls": a.calls,
+                      "wall_ms_last_call": ms}))
 
 
 if __name__ == "__main__":

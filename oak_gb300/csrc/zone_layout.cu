@@ -177,6 +177,145 @@ struct RectGrid {
   int64_t ioffset[4];  // linear-index stride of axis k (first axis fastest)
 };
 
+// interp_tetrahedron (ndgrid.F90:464-629) on simplex l of the cell: 3 and the corner weights
+// wc when xi lies in it (barycentric coordinates in [-tol, 1 + tol]), 0 when it does not, 2
+// when the simplex is degenerate (|det| <= tol)
+template <int ND>
+__device__ __forceinline__ int solve_simplex(int l, const double* __restrict__ T,
+                                             const double (&clo)[ND], const double (&chi)[ND],
+                                             const double (&xi)[ND], double (&wc)[1 << ND]) {
+  constexpr int K = 1 << ND, NV = ND + 1;
+  const double tol = 1e-8;
+  // Tl[v * K + c]: corner c's share of vertex v; Ul[k * NV + v]: the share of the corners
+  // on the upper side of axis k (the shares of a vertex sum to 1), so that the vertex
+  // X(k, v) = sum_c px(k, c) T(c, v) = clo(k) + (chi(k) - clo(k)) U(k, v)
+  const double* Tl = T + (int64_t)l * (NV * K + ND * NV);
+  const double* Ul = Tl + NV * K;
+  double M[NV][NV + 1];
+  double xc[ND];
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    xc[k] = 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      const double a = fma(chi[k] - clo[k], Ul[k * NV + v], clo[k]);
+      M[1 + k][v] = a;
+      xc[k] += a;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) M[0][v] = 1.0;
+  M[0][NV] = 1.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    xc[k] /= NV;
+#pragma unroll
+    for (int v = 0; v < NV; v++) M[1 + k][v] -= xc[k];
+    M[1 + k][NV] = xi[k] - xc[k];
+  }
+  // [1; X - xc] c = [1; xi - xc] by Gaussian elimination with partial pivoting
+  double det = 1.0;
+#pragma unroll
+  for (int col = 0; col < NV; col++) {
+    int piv = col;
+    double best = fabs(M[col][col]);
+#pragma unroll
+    for (int r = col + 1; r < NV; r++)
+      if (fabs(M[r][col]) > best) {
+        best = fabs(M[r][col]);
+        piv = r;
+      }
+#pragma unroll
+    for (int r = col + 1; r < NV; r++)
+      if (r == piv) {
+        det = -det;
+#pragma unroll
+        for (int q = 0; q <= NV; q++) {
+          const double t = M[col][q];
+          M[col][q] = M[r][q];
+          M[r][q] = t;
+        }
+      }
+    det *= M[col][col];
+    const double inv = M[col][col] != 0.0 ? 1.0 / M[col][col] : 0.0;
+#pragma unroll
+    for (int r = col + 1; r < NV; r++) {
+      const double f = M[r][col] * inv;
+#pragma unroll
+      for (int q = col; q <= NV; q++) M[r][q] = fma(-f, M[col][q], M[r][q]);
+    }
+  }
+  if (!(fabs(det) > tol)) return 2;  // every simplex of a rectilinear cell has the same |det|
+  double cb[NV];
+#pragma unroll
+  for (int r = NV - 1; r >= 0; r--) {
+    double s = M[r][NV];
+#pragma unroll
+    for (int q = r + 1; q < NV; q++) s = fma(-M[r][q], cb[q], s);
+    cb[r] = s / M[r][r];
+  }
+  bool inside = true;
+#pragma unroll
+  for (int v = 0; v < NV; v++) inside = inside && (cb[v] >= -tol) && (cb[v] <= 1.0 + tol);
+  if (!inside) return 0;
+#pragma unroll
+  for (int cc = 0; cc < K; cc++) {
+    double a = 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; v++) a = fma(Tl[v * K + cc], cb[v], a);
+    wc[cc] = a;
+  }
+  return 3;
+}
+
+// The simplex of the cell's split holding xi, found directly instead of by trying the
+// simplices in turn: in coordinates normalised to the cell ([0, 1] per axis), the pyramid of
+// split's first level that holds a point is the one over the face its ray from the centroid
+// leaves through (the free axis of largest |p - 1/2|, side p > 1/2); inside it, the simplex is
+// the cone over the face simplex holding the point's projection from the centroid onto that
+// face, so the same choice repeats on the face. Simplex numbering follows split: per level,
+// blocks of (subn - 1)! 2^(subn - 2) simplices in (free axis ascending, side 0 then 1) order.
+// Ties go to the lower block, the one split tries first.
+template <int ND>
+__device__ __forceinline__ int locate_simplex(const double (&clo)[ND], const double (&chi)[ND],
+                                              const double (&xi)[ND]) {
+  double p[ND];
+#pragma unroll
+  for (int k = 0; k < ND; k++) p[k] = (xi[k] - clo[k]) / (chi[k] - clo[k]);
+  unsigned fixed = 0;
+  int l = 0;
+#pragma unroll
+  for (int subn = ND; subn > 1; subn--) {
+    int sub = 1;
+    for (int f = 2; f < subn; f++) sub *= f;
+    sub <<= (subn - 2);
+    int best = 0, best_rank = 0, rank = 0;
+    double dev = -1.0;
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+      if ((fixed >> k) & 1u) continue;
+      const double d = fabs(p[k] - 0.5);
+      if (d > dev) {
+        dev = d;
+        best = k;
+        best_rank = rank;
+      }
+      rank++;
+    }
+    const int side = p[best] > 0.5 ? 1 : 0;
+    l += (2 * best_rank + side) * sub;
+    if (dev > 0.0) {
+      const double t = 0.5 / dev;
+#pragma unroll
+      for (int k = 0; k < ND; k++)
+        if (!((fixed >> k) & 1u) && k != best) p[k] = fma(p[k] - 0.5, t, 0.5);
+    }
+    p[best] = (double)side;
+    fixed |= 1u << best;
+  }
+  return l;
+}
+
 template <int ND>
 __global__ void k_rect_oper(RectGrid gr, const double* __restrict__ coords,
                             const int64_t* __restrict__ sea, const double* __restrict__ T,
@@ -233,90 +372,13 @@ __global__ void k_rect_oper(RectGrid gr, const double* __restrict__ coords,
     }
     int status = out ? 1 : 0;  // 0 searching, 1 outside / masked, 2 degenerate cell, 3 found
     double wc[K];
-    for (int l = 0; l < nsimplex && status == 0; l++) {
-      // Tl[v * K + c]: corner c's share of vertex v; Ul[k * NV + v]: the share of the corners
-      // on the upper side of axis k (the shares of a vertex sum to 1), so that the vertex
-      // X(k, v) = sum_c px(k, c) T(c, v) = clo(k) + (chi(k) - clo(k)) U(k, v)
-      const double* Tl = T + (int64_t)l * (NV * K + ND * NV);
-      const double* Ul = Tl + NV * K;
-      double M[NV][NV + 1];
-      double xc[ND];
-#pragma unroll
-      for (int k = 0; k < ND; k++) {
-        xc[k] = 0.0;
-#pragma unroll
-        for (int v = 0; v < NV; v++) {
-          const double a = fma(chi[k] - clo[k], Ul[k * NV + v], clo[k]);
-          M[1 + k][v] = a;
-          xc[k] += a;
-        }
-      }
-#pragma unroll
-      for (int v = 0; v < NV; v++) M[0][v] = 1.0;
-      M[0][NV] = 1.0;
-#pragma unroll
-      for (int k = 0; k < ND; k++) {
-        xc[k] /= NV;
-#pragma unroll
-        for (int v = 0; v < NV; v++) M[1 + k][v] -= xc[k];
-        M[1 + k][NV] = xi[k] - xc[k];
-      }
-      // [1; X - xc] c = [1; xi - xc] by Gaussian elimination with partial pivoting
-      double det = 1.0;
-#pragma unroll
-      for (int col = 0; col < NV; col++) {
-        int piv = col;
-        double best = fabs(M[col][col]);
-#pragma unroll
-        for (int r = col + 1; r < NV; r++)
-          if (fabs(M[r][col]) > best) {
-            best = fabs(M[r][col]);
-            piv = r;
-          }
-#pragma unroll
-        for (int r = col + 1; r < NV; r++)
-          if (r == piv) {
-            det = -det;
-#pragma unroll
-            for (int q = 0; q <= NV; q++) {
-              const double t = M[col][q];
-              M[col][q] = M[r][q];
-              M[r][q] = t;
-            }
-          }
-        det *= M[col][col];
-        const double inv = M[col][col] != 0.0 ? 1.0 / M[col][col] : 0.0;
-#pragma unroll
-        for (int r = col + 1; r < NV; r++) {
-          const double f = M[r][col] * inv;
-#pragma unroll
-          for (int q = col; q <= NV; q++) M[r][q] = fma(-f, M[col][q], M[r][q]);
-        }
-      }
-      if (!(fabs(det) > tol)) {
-        status = 2;  // every simplex of a rectilinear cell has the same |det|
-        break;
-      }
-      double cb[NV];
-#pragma unroll
-      for (int r = NV - 1; r >= 0; r--) {
-        double s = M[r][NV];
-#pragma unroll
-        for (int q = r + 1; q < NV; q++) s = fma(-M[r][q], cb[q], s);
-        cb[r] = s / M[r][r];
-      }
-      bool inside = true;
-#pragma unroll
-      for (int v = 0; v < NV; v++) inside = inside && (cb[v] >= -tol) && (cb[v] <= 1.0 + tol);
-      if (!inside) continue;
-#pragma unroll
-      for (int cc = 0; cc < K; cc++) {
-        double a = 0.0;
-#pragma unroll
-        for (int v = 0; v < NV; v++) a = fma(Tl[v * K + cc], cb[v], a);
-        wc[cc] = a;
-      }
-      status = 3;
+    if (status == 0) {
+      const int l0 = locate_simplex<ND>(clo, chi, xi);
+      status = solve_simplex<ND>(l0, T, clo, chi, xi, wc);
+      // a point on a shared face that rounding put outside the located simplex: split's
+      // order, as interp_cube tries the simplices
+      for (int l = 0; l < nsimplex && status == 0; l++)
+        if (l != l0) status = solve_simplex<ND>(l, T, clo, chi, xi, wc);
     }
 #pragma unroll
     for (int cc = 0; cc < K; cc++) {
