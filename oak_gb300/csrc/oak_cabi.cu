@@ -422,6 +422,10 @@ void assim_state(const State& s, int ntime, int n, int r, const double* Ef, doub
   if (ntime < 999) snprintf(pre, sizeof pre, "Obs%03d.", ntime);
   else snprintf(pre, sizeof pre, "Obs%d.", ntime);
   const std::string P(pre);
+  for (const char* k : {"operator", "HperObs", "shiftMod", "filterMod"})
+    need(!s.cfg.has(P + k), P + k + ": operators read from files are not supported (the "
+                                      "operator is generated on the model grids)",
+         OAKG_ERR_NOTIMPL);
   const Layout O = load_layout(s, P);
   const int64_t m0 = O.total_sea;
   std::vector<double> yo = load_vector(s, P + "value", O);

@@ -251,3 +251,10 @@ def test_driver_errors(oakg, tmp_path):
     with pytest.raises(oakg.OakError) as ei:
         oakg.oak_init(bad)
     assert ei.value.code == oakg.ERR_NOTIMPL
+    op = tmp_path / "op.init"
+    op.write_text(fname.read_text() + "Obs001.operator = 'H.nc#H'" + chr(10))
+    oakg.oak_init(op)
+    with pytest.raises(oakg.OakError) as ei:
+        oakg.oak_assim(1, Ef)
+    assert ei.value.code == oakg.ERR_NOTIMPL and "operator" in str(ei.value)
+    oakg.oak_done()
