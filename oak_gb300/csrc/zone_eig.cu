@@ -41,6 +41,7 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNMax = 128;               // largest N of the eigensolve stages
 constexpr int kMaxSweepsPerN = 30;
+constexpr int32_t kFewZones = 152;  // below this zone count E2a runs one block per zone
 
 template <typename R>
 struct Prec;
@@ -308,6 +309,121 @@ __global__ void __launch_bounds__(128)
   }
   ax[5 * N + 1] = onenrm;
   if (st) status[zl] |= st;
+}
+
+// E2a for few zones (fewer than the GPU has SMs, e.g. the one-zone global analysis), where the
+// thread-per-zone QR above leaves the GPU idle and its latency is the whole stage: one warp per
+// eigenvalue (grid N x zones), so that the zone's eigenvalues spread over the SMs. Eigenvalue
+// k is the point where the Sturm count of Tri - x I passes k: the number of sign changes along
+// the leading principal minors p_i = det(Tri_{1:i} - x I), from
+// p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2} (bisection after Givens; a zero minor takes the
+// sign opposite to its predecessor, as the pivot -pivmin of the ratio form does), rescaled by
+// powers of two to stay in range, with no division. Each step evaluates the count at the 32
+// lanes' interior points of the current interval and keeps the sub-interval where it passes k
+// (multisection, a 33-fold narrowing per step), until the interval is at the rounding level of
+// Tri. k_eig_shifts then writes the outputs of the QR kernel.
+template <typename R>
+__device__ __forceinline__ int sturm_count(const R* __restrict__ d, const R* __restrict__ e2,
+                                           int N, R x) {
+  R p0 = R(1), p1 = d[0] - x;
+  bool s1 = !(p1 > R(0));  // a zero takes the sign opposite to p0 > 0
+  int c = s1;
+  for (int i = 1; i < N; i++) {
+    const R p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
+    const bool s2 = (p2 == R(0)) ? !s1 : (p2 < R(0));
+    c += s2 != s1;
+    s1 = s2;
+    p0 = p1;
+    p1 = p2;
+    if ((i & 7) == 0) {
+      const R mx = fmax(fabs(p0), fabs(p1));
+      if (mx > R(1e150) || (mx < R(1e-150) && mx > R(0))) {
+        int ex;
+        frexp(mx, &ex);
+        p0 = ldexp(p0, -ex);
+        p1 = ldexp(p1, -ex);
+      }
+    }
+  }
+  return c;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(32)
+    k_eig_values_multisect(int N, int32_t nzc, R* __restrict__ aux,
+                           const int32_t* __restrict__ nobs) {
+  __shared__ R sd[kNMax], se2[kNMax];
+  const int k = blockIdx.x;
+  const int32_t zl = blockIdx.y;
+  if (zl >= nzc || nobs[zl] == 0) return;  // uniform across the block
+  const R eps = Prec<R>::eps();
+  R* ax = aux + (int64_t)zl * aux_stride(N);
+  const int lane = threadIdx.x;
+  R onenrm = 0, gl = 0, gu = 0;
+  bool first = true;
+  for (int i0 = 0; i0 < N; i0 += 32) {
+    const int i = i0 + lane;
+    R di = 0, r = 0;
+    if (i < N) {
+      di = ax[i];
+      const R ei = (i < N - 1) ? ax[N + i] : R(0), em = (i > 0) ? ax[N + i - 1] : R(0);
+      sd[i] = di;
+      se2[i] = ei * ei;
+      r = fabs(ei) + fabs(em);
+    }
+    R nrm = (i < N) ? fabs(di) + r : R(0);
+    R lo = (i < N) ? di - r : R(INFINITY), hi = (i < N) ? di + r : R(-INFINITY);
+    for (int o = 16; o > 0; o >>= 1) {
+      nrm = fmax(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    onenrm = fmax(onenrm, nrm);
+    gl = first ? lo : fmin(gl, lo);
+    gu = first ? hi : fmax(gu, hi);
+    first = false;
+  }
+  __syncwarp();
+  const R pad = R(2) * eps * onenrm + Prec<R>::tiny();
+  R a = gl - pad, b = gu + pad;
+  for (int it = 0; it < 64; it++) {
+    const R x = a + (b - a) * R(lane + 1) / R(33);
+    const unsigned past = __ballot_sync(0xffffffffu, sturm_count(sd, se2, N, x) > k);
+    const int ss = past ? __ffs(past) - 1 : 32;  // first point past eigenvalue k
+    const R xl = (ss == 0) ? a : a + (b - a) * R(ss) / R(33);
+    const R xu = (ss == 32) ? b : a + (b - a) * R(ss + 1) / R(33);
+    a = xl;
+    b = xu;
+    if (b - a <= R(2) * eps * fmax(fabs(a), fabs(b)) + eps * onenrm) break;  // uniform
+  }
+  if (lane == 0) {
+    ax[3 * N + k] = R(0.5) * (a + b);  // unscaled until k_eig_shifts
+    if (k == 0) ax[5 * N + 1] = onenrm;
+  }
+}
+
+// the QR kernel's outputs from the multisection eigenvalues: scaled eigenvalues and the
+// inverse-iteration shifts separated as LAPACK dstein does (one thread per zone)
+template <typename R>
+__global__ void k_eig_shifts(int N, int32_t nzc, R* __restrict__ aux,
+                             const int32_t* __restrict__ nobs) {
+  const int32_t zl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;
+  const R eps = Prec<R>::eps();
+  R* ax = aux + (int64_t)zl * aux_stride(N);
+  const R scale = ax[5 * N];
+  R prev = 0;
+  for (int j = 0; j < N; j++) {
+    const R lam = ax[3 * N + j];
+    ax[3 * N + j] = lam * scale;
+    R sh = lam;
+    if (j > 0) {
+      const R pert = R(10) * eps * fabs(sh);
+      if (sh - prev < pert) sh = prev + pert;
+    }
+    ax[4 * N + j] = sh;
+    prev = sh;
+  }
 }
 
 // ------------------------------------------------------------------------------------ E2b
@@ -755,7 +871,13 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
 template <typename R>
 cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nobs,
                       int32_t* d_status, cudaStream_t st) {
-  k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  if (nzc < kFewZones) {
+    k_eig_values_multisect<R><<<dim3((unsigned)N, (unsigned)nzc), 32, 0, st>>>(N, nzc, d_aux,
+                                                                               d_nobs);
+    k_eig_shifts<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs);
+  } else {
+    k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  }
   const int64_t pairs = (int64_t)nzc * N;
   k_eig_tridiag_vectors<R><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
                                                                              d_nobs);
