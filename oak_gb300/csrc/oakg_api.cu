@@ -273,6 +273,10 @@ struct ChunkArgs {
   const int64_t* zstart_host = nullptr;  // Z + 1 row offsets
 };
 
+// host-memory calls: the update of a chunk in this many zone ranges, so that all but the
+// last range's output copy overlaps the update
+constexpr int32_t kOutPieces = 4;
+
 int copy_streams(Ctx* c) {
   cudaError_t e = cudaSuccess;
   if (!c->copy_in) e = cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking);
@@ -338,11 +342,9 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   if (pipe) {
     if ((rc = copy_streams(c))) return rc;
     ev_in.resize(nchunks);
-    ev_out.resize(nchunks);
-    for (int64_t q = 0; q < nchunks; q++) {
-      cudaEventCreateWithFlags(&ev_in[q], cudaEventDisableTiming);
-      cudaEventCreateWithFlags(&ev_out[q], cudaEventDisableTiming);
-    }
+    ev_out.resize(nchunks * kOutPieces);
+    for (auto& ev : ev_in) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    for (auto& ev : ev_out) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     // the staging buffer is free once the stream's earlier work is done
     cudaEventRecord(c->ev[7], st);
     cudaStreamWaitEvent(c->copy_in, c->ev[7], 0);
@@ -390,10 +392,38 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
                d_status, d_aux, d_zvec, d_work + 4, st);
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
     if (timed) cudaEventRecord(c->ev[4], st);
-    if (pipe) cudaStreamWaitEvent(st, ev_in[z0 / chunk], 0);
-    e = K::update(N, (int32_t)z0, nzc, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, (const R*)d_G,
-                  (const R*)d_za, (const int32_t*)(a.nobs + z0), a.xa, a.Sa, st);
-    if (e != cudaSuccess) return cuda_fail(e, "update kernel");
+    if (!pipe) {
+      e = K::update(N, (int32_t)z0, nzc, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, (const R*)d_G,
+                    (const R*)d_za, (const int32_t*)(a.nobs + z0), a.xa, a.Sa, st);
+      if (e != cudaSuccess) return cuda_fail(e, "update kernel");
+    } else {
+      // host memory: the update in kOutPieces zone ranges, each range's Sa / xa rows copied
+      // out while the next range updates
+      cudaStreamWaitEvent(st, ev_in[z0 / chunk], 0);
+      const int32_t per = (nzc + kOutPieces - 1) / kOutPieces;
+      for (int32_t q0 = 0; q0 < nzc; q0 += per) {
+        const int32_t nq = std::min(per, nzc - q0);
+        e = K::update(N, (int32_t)(z0 + q0), nq, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS,
+                      (const R*)d_G + (size_t)q0 * N * N, (const R*)d_za + (size_t)q0 * N,
+                      (const int32_t*)(a.nobs + z0 + q0), a.xa, a.Sa, st);
+        if (e != cudaSuccess) return cuda_fail(e, "update kernel");
+        const int64_t r0 = a.zstart_host[z0 + q0], r1 = a.zstart_host[z0 + q0 + nq];
+        cudaEvent_t evp = ev_out[(z0 / chunk) * kOutPieces + q0 / per];
+        cudaEventRecord(evp, st);
+        cudaStreamWaitEvent(c->copy_out, evp, 0);
+        if (r1 > r0) {
+          if (a.sa_host &&
+              (e = cudaMemcpy2DAsync(a.sa_host + r0, pitch, a.Sa + r0, pitch,
+                                     (size_t)(r1 - r0) * sizeof(double), N,
+                                     cudaMemcpyDeviceToHost, c->copy_out)) != cudaSuccess)
+            return cuda_fail(e, "D2H Sa rows");
+          if ((e = cudaMemcpyAsync(a.xa_host + r0, a.xa + r0,
+                                   (size_t)(r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                   c->copy_out)) != cudaSuccess)
+            return cuda_fail(e, "D2H xa rows");
+        }
+      }
+    }
     if (timed) cudaEventRecord(c->ev[5], st);
     if (a.ampl) {
       e = K::ampl(N, (int32_t)z0, nzc, (const R*)d_za, (const int32_t*)(a.nobs + z0), a.all_ampl,
@@ -402,21 +432,6 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     }
     k_or_status<<<64, 256, 0, st>>>(d_status, nzc, *status_all);
     count_launches(1);
-    if (pipe) {
-      const int64_t q = z0 / chunk, r0 = a.zstart_host[z0], r1 = a.zstart_host[z0 + nzc];
-      cudaEventRecord(ev_out[q], st);
-      cudaStreamWaitEvent(c->copy_out, ev_out[q], 0);
-      if (r1 > r0) {
-        if (a.sa_host &&
-            (e = cudaMemcpy2DAsync(a.sa_host + r0, pitch, a.Sa + r0, pitch,
-                                   (size_t)(r1 - r0) * sizeof(double), N,
-                                   cudaMemcpyDeviceToHost, c->copy_out)) != cudaSuccess)
-          return cuda_fail(e, "D2H Sa rows");
-        if ((e = cudaMemcpyAsync(a.xa_host + r0, a.xa + r0, (size_t)(r1 - r0) * sizeof(double),
-                                 cudaMemcpyDeviceToHost, c->copy_out)) != cudaSuccess)
-          return cuda_fail(e, "D2H xa rows");
-      }
-    }
     if (!timed) continue;
     if ((e = cudaEventSynchronize(c->ev[5])) != cudaSuccess) return cuda_fail(e, "kernels");
     *t_gram += elapsed(c->ev[2], c->ev[3]);
