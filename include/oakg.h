@@ -380,13 +380,20 @@ int64_t oakg_launch_count(void);
 int oakg_fp64_peak(double* tflops);
 
 /* The data-file reader of the oak_init / oak_assim driver, as the reference's uload
- * (ufileformat.F90:555-745) reads a NetCDF variable: spec "file.nc#var" (NetCDF classic,
- * 64-bit-offset or CDF-5 format; NetCDF-4 / HDF5 and GHER binary files are not read). Values in
- * Fortran order (first dimension fastest) into values (capacity elements; NULL: sizes only),
- * *count values, shape[0..*ndim) in Fortran order (at most 8 written), *valex the missing
- * value (missing_value or _FillValue attribute, else -9999); scale_factor / add_offset are
- * applied to the other values and the compact "shape"-attribute form is expanded. Host only
- * (no GPU needed). */
+ * (ufileformat.F90:555-745) reads a file:
+ *  - spec "file.nc#var": a NetCDF variable (classic, 64-bit-offset or CDF-5 format;
+ *    NetCDF-4 / HDF5 is not read);
+ *  - spec "file" without '#': a GHER binary file in either byte order.
+ * Outputs:
+ *  - values: the values in Fortran order (first dimension fastest), capacity elements; NULL
+ *    asks for the sizes only;
+ *  - *count: the number of values;
+ *  - shape[0..*ndim): the shape in Fortran order (at most 8 written);
+ *  - *valex: the missing value. For NetCDF, the missing_value or _FillValue attribute, else
+ *    -9999; for GHER, the header's.
+ * scale_factor / add_offset are applied to the other values. The compact forms (the "shape"
+ * attribute, negative GHER extents) are expanded as uexplo does, with 1-based indices. Host
+ * only: no GPU is needed. */
 int oakg_read_variable(const char* spec, double* values, int64_t capacity, int64_t* count,
                        int64_t* shape, int32_t* ndim, double* valex);
 
@@ -412,6 +419,7 @@ int oakg_read_variable(const char* spec, double* values, int64_t capacity, int64
  *      zone order), inflation, the maxCorrection clip and Ea = xa + sqrt(r - 1) Sa.
  *    runtype 0 or 1 returns Ea = Ef.
  *  - oak_done frees the driver state and the device buffers (as oakg_release).
+ * Files: NetCDF classic variables ("file.nc#var") and GHER binary files (names without '#').
  * Not done: diagnostics files (Diag*), biastype, anamorphosis, other schemetypes and operators
  * read from files (OAKG_ERR_NOTIMPL where the init file asks for them). The reference's
  * functions return nothing and stop the process on error; these record the status for

@@ -319,12 +319,123 @@ bool read_atts(Reader& r, std::vector<Att>& atts) {
 
 }  // namespace
 
-bool read_array(const std::string& path, const std::string& spec, Array& out, std::string& err) {
-  const size_t hash = spec.rfind('#');
-  if (hash == std::string::npos) {
-    err = "'" + spec + "': only NetCDF variables (file.nc#variable) are read by this library";
+// GHER binary file (ufileformat.F90: UREADC, :1072-1160): Fortran unformatted sequential
+// records with 4-byte length markers in either byte order (the reference's FORMAT=big_endian
+// build writes big-endian): KBLANC = 10 records skipped, the header record (imax, jmax, kmax,
+// iprec, nbmots as int32, valex as float32), then the values in records of nbmots words of
+// iprec bytes. A negative extent marks the compact form: four values c0, dci, dcj, dck.
+bool read_gher(const std::string& file, Array& out, std::string& err) {
+  std::unique_ptr<FILE, int (*)(FILE*)> fp(fopen(file.c_str(), "rb"), fclose);
+  if (!fp) {
+    err = "cannot open '" + file + "'";
     return false;
   }
+  std::vector<unsigned char> buf;
+  {
+    unsigned char chunk[1 << 16];
+    size_t got;
+    while ((got = fread(chunk, 1, sizeof chunk, fp.get())) > 0) {
+      buf.insert(buf.end(), chunk, chunk + got);
+      if (buf.size() > ((size_t)1 << 36)) {
+        err = "'" + file + "' is too large";
+        return false;
+      }
+    }
+  }
+  auto marker = [&](size_t off, bool big) -> int64_t {
+    if (off + 4 > buf.size()) return -1;
+    const unsigned char* p = buf.data() + off;
+    return big ? (int64_t)be(p, 4)
+               : (int64_t)((uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) |
+                           ((uint32_t)p[3] << 24));
+  };
+  // records: (payload offset, length); the byte order whose first 11 records are consistent
+  // and whose 11th is the 24-byte header
+  std::vector<std::pair<size_t, size_t>> recs;
+  bool big = false, ok = false;
+  for (int order = 0; order < 2 && !ok; order++) {
+    big = order == 1;
+    recs.clear();
+    size_t off = 0;
+    ok = true;
+    while (off < buf.size()) {
+      const int64_t len = marker(off, big);
+      if (len < 0 || off + 8 + (size_t)len > buf.size() ||
+          marker(off + 4 + (size_t)len, big) != len) {
+        ok = false;
+        break;
+      }
+      recs.emplace_back(off + 4, (size_t)len);
+      off += 8 + (size_t)len;
+    }
+    ok = ok && recs.size() >= 12 && recs[10].second == 24;
+  }
+  if (!ok) {
+    err = "'" + file + "' is neither a NetCDF variable (file.nc#var) nor a GHER binary file";
+    return false;
+  }
+  auto i32 = [&](size_t off) {
+    const int64_t v = marker(off, big);
+    return (int32_t)(uint32_t)v;
+  };
+  const size_t h = recs[10].first;
+  const int32_t imax = i32(h), jmax = i32(h + 4), kmax = i32(h + 8), iprec = i32(h + 12);
+  const uint32_t vx = (uint32_t)marker(h + 20, big);
+  float valex4;
+  memcpy(&valex4, &vx, 4);
+  if (iprec != 4 && iprec != 8) {
+    err = "'" + file + "': precision " + std::to_string(iprec) + " (expected 4 or 8)";
+    return false;
+  }
+  const bool degen = imax < 0 || jmax < 0 || kmax < 0;
+  const int64_t ni = imax < 0 ? -(int64_t)imax : imax, nj = jmax < 0 ? -(int64_t)jmax : jmax,
+                nk = kmax < 0 ? -(int64_t)kmax : kmax;
+  const int64_t total = ni * nj * nk, want = degen ? 4 : total;
+  if (total <= 0 || total > ((int64_t)1 << 34)) {
+    err = "'" + file + "': bad extents";
+    return false;
+  }
+  std::vector<double> vals;
+  vals.reserve((size_t)want);
+  for (size_t r = 11; r < recs.size() && (int64_t)vals.size() < want; r++)
+    for (size_t q = 0; q + iprec <= recs[r].second && (int64_t)vals.size() < want; q += iprec) {
+      const unsigned char* p = buf.data() + recs[r].first + q;
+      unsigned char tmp[8];
+      for (int b = 0; b < iprec; b++) tmp[b] = big ? p[b] : p[iprec - 1 - b];  // to big-endian
+      vals.push_back(decode(tmp, iprec == 4 ? 5 : 6));
+    }
+  if ((int64_t)vals.size() < want) {
+    err = "'" + file + "': truncated data";
+    return false;
+  }
+  // the extents as uread_prim reads them: trailing unit extents dropped
+  out.shape = {ni};
+  if (nk != 1) out.shape = {ni, nj, nk};
+  else if (nj != 1) out.shape = {ni, nj};
+  out.valex = (double)valex4;
+  if (degen) {
+    // uexplo (:2300-2337), 1-based indices
+    const size_t nd = out.shape.size();
+    out.v.assign((size_t)total, 0.0);
+    for (int64_t e = 0; e < total; e++) {
+      int64_t rem = e;
+      double x = vals[0];
+      for (size_t k = 0; k < nd; k++) {
+        const int64_t ik = rem % out.shape[k];
+        rem /= out.shape[k];
+        x += vals[k + 1] * (double)(ik + 1);
+      }
+      out.v[e] = x;
+    }
+  } else {
+    out.v.swap(vals);
+  }
+  return true;
+}
+
+bool read_array(const std::string& path, const std::string& spec, Array& out, std::string& err) {
+  const size_t hash = spec.rfind('#');
+  if (hash == std::string::npos) return read_gher(path + spec, out, err);
   const std::string file = path + spec.substr(0, hash), var = spec.substr(hash + 1);
   std::unique_ptr<FILE, int (*)(FILE*)> fp(fopen(file.c_str(), "rb"), fclose);
   if (!fp) {
@@ -452,8 +563,8 @@ bool read_array(const std::string& path, const std::string& spec, Array& out, st
   std::vector<double> vals((size_t)total);
   for (uint64_t q = 0; q < total; q++) vals[q] = decode(raw.data() + q * ts, vp->type);
   if (!compact_shape.empty()) {
-    // the compact regular form: x(i_1..i_n) = c(0) + sum_k c(k) (i_k - 1), shape in the
-    // attribute (Fortran order)
+    // the compact regular form (uexplo, ufileformat.F90:2300-2337): with 1-based indices,
+    // x(i_1..i_n) = c(0) + sum_k c(k) i_k; the shape in the attribute (Fortran order)
     const size_t nd = compact_shape.size();
     if (vals.size() < nd + 1) {
       err = "'" + file + "#" + var + "': compact form needs " + std::to_string(nd + 1) + " values";
@@ -472,7 +583,7 @@ bool read_array(const std::string& path, const std::string& spec, Array& out, st
       for (size_t k = 0; k < nd; k++) {
         const uint64_t ik = rem % (uint64_t)out.shape[k];
         rem /= (uint64_t)out.shape[k];
-        x += vals[k + 1] * (double)ik;
+        x += vals[k + 1] * (double)(ik + 1);
       }
       out.v[e] = x;
     }

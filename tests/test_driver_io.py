@@ -1,8 +1,10 @@
 """The oak_init / oak_assim driver's data-file reader (oakg_read_variable, host only): NetCDF
-classic and 64-bit-offset files written by SciPy's independent NetCDF-3 writer, read back as
-the reference's uload returns them (ufileformat.F90:555-745): Fortran order and shape, the
-missing value from missing_value / _FillValue (else -9999), scale_factor / add_offset on the
-other values, record variables, and the compact "shape" form."""
+classic and 64-bit-offset files written by SciPy's independent NetCDF-3 writer, and GHER
+binary files written here record by record, read back as the reference's uload returns them
+(ufileformat.F90:555-745): Fortran order and shape, the missing value from missing_value /
+_FillValue (else -9999, or the GHER header's), scale_factor / add_offset on the other values,
+record variables, and the compact forms."""
+import struct
 import numpy as np
 import pytest
 
@@ -79,7 +81,8 @@ def test_record_variables_interleaved(oakg, tmp_path):
 
 
 def test_compact_shape_form(oakg, tmp_path):
-    """A variable with a "shape" attribute holds x0 and one increment per dimension."""
+    """A variable with a "shape" attribute holds x0 and one increment per dimension, expanded
+    with 1-based indices as uexplo does (ufileformat.F90:2300-2337)."""
     f = tmp_path / "c.nc"
     with netcdf(str(f), "w") as nc:
         nc.createDimension("n", 3)
@@ -88,7 +91,7 @@ def test_compact_shape_form(oakg, tmp_path):
         v.shape = np.array([4, 3], dtype=np.int32)
     x, _ = oakg.read_variable(f"{f}#lon")
     i, j = np.meshgrid(np.arange(4), np.arange(3), indexing="ij")
-    assert x.shape == (4, 3) and np.array_equal(x, 10.0 + 0.5 * i + 2.0 * j)
+    assert x.shape == (4, 3) and np.array_equal(x, 10.0 + 0.5 * (i + 1) + 2.0 * (j + 1))
 
 
 def test_errors(oakg, tmp_path):
@@ -103,3 +106,67 @@ def test_errors(oakg, tmp_path):
         oakg.read_variable(f"{tmp_path / 't.nc'}#v")
     with pytest.raises(oakg.OakError, match="cannot open"):
         oakg.read_variable(f"{tmp_path / 'missing.nc'}#v")
+
+
+def _gher(path, data, valex=-99.0, prec=4, nbmots=7, big=False, degen=None):
+    """A GHER file as the reference's writer lays it out: 10 empty records, the header record
+    (imax, jmax, kmax, iprec, nbmots, valex), then records of nbmots values (4-byte record
+    markers, one byte order)."""
+    e = ">" if big else "<"
+    fl = "f" if prec == 4 else "d"
+
+    def rec(payload):
+        return struct.pack(e + "i", len(payload)) + payload + struct.pack(e + "i", len(payload))
+
+    if degen is not None:
+        shape, coeffs = degen
+        ext = [-s for s in shape] + [1] * (3 - len(shape))
+        vals = list(coeffs)
+    else:
+        a = np.asarray(data, dtype=np.float64)
+        ext = list(a.shape) + [1] * (3 - a.ndim)
+        vals = list(a.reshape(-1, order="F"))
+    out = b"".join(rec(b"") for _ in range(10))
+    out += rec(struct.pack(e + "5if", ext[0], ext[1], ext[2], prec, nbmots, valex))
+    for q in range(0, len(vals), nbmots):
+        chunk = vals[q:q + nbmots]
+        out += rec(struct.pack(e + fl * len(chunk), *chunk))
+    path.write_bytes(out)
+
+
+@pytest.mark.parametrize("big", [False, True])
+@pytest.mark.parametrize("prec", [4, 8])
+def test_gher_files(oakg, tmp_path, big, prec):
+    rng = np.random.default_rng(prec + big)
+    a = rng.normal(size=(5, 4, 3)).astype(np.float32 if prec == 4 else np.float64)
+    a[1, 2, 0] = -99.0
+    f = tmp_path / "field.TEM"
+    _gher(f, a, prec=prec, big=big)
+    x, valex = oakg.read_variable(str(f))
+    assert valex == -99.0 and x.shape == (5, 4, 3)
+    assert np.array_equal(x, a.astype(np.float64))
+    # a 2-D field (kmax = 1) and a 1-D one (jmax = kmax = 1)
+    _gher(f, a[:, :, 0], prec=prec, big=big)
+    x, _ = oakg.read_variable(str(f))
+    assert x.shape == (5, 4) and np.array_equal(x, a[:, :, 0].astype(np.float64))
+    _gher(f, a[:, 0, 0], prec=prec, big=big, nbmots=5)
+    x, _ = oakg.read_variable(str(f))
+    assert x.shape == (5,) and np.array_equal(x, a[:, 0, 0].astype(np.float64))
+
+
+def test_gher_compact_form(oakg, tmp_path):
+    """Negative extents: c0, dci, dcj, dck expanded with 1-based indices (uexplo)."""
+    f = tmp_path / "lon.TEM"
+    _gher(f, None, prec=8, degen=((6, 4), (-10.0, 0.25, 1.5, 0.0)))
+    x, _ = oakg.read_variable(str(f))
+    i, j = np.meshgrid(np.arange(1, 7), np.arange(1, 5), indexing="ij")
+    assert x.shape == (6, 4) and np.array_equal(x, -10.0 + 0.25 * i + 1.5 * j)
+
+
+def test_gher_damaged(oakg, tmp_path):
+    f = tmp_path / "bad.TEM"
+    _gher(f, np.arange(12.0).reshape(3, 4))
+    f.write_bytes(f.read_bytes()[:-6])
+    with pytest.raises(oakg.OakError, match="GHER"):
+        oakg.read_variable(str(f))
+
