@@ -18,7 +18,8 @@
 // analysis in zone order (schemetype 1), inflation, the maxCorrection clip and
 // Ea = xa + sqrt(N - 1) Sa. runtype 0 and 1 return Ea = Ef (no analysis).
 //
-// Files are read as NetCDF classic-format variables ("file.nc#var", oak_io.cpp). Not done
+// Files are NetCDF classic-format variables ("file.nc#var") or GHER binary files (oak_io.cpp).
+// Not done
 // here: diagnostics files (Diag*), biastype / anamorphosis / other schemetypes (refused with
 // OAKG_ERR_NOTIMPL), curvilinear model grids (OAKG_ERR_NOTIMPL), operators read from files.
 // The reference stops the process on an error; these functions record it for

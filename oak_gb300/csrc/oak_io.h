@@ -1,6 +1,7 @@
 // Host-side readers for OAK's configuration and data files: the init file (key = value lines,
-// initfile.F90) and NetCDF classic-format variables (the "file.nc#variable" specifications of
-// ufileformat.F90). Used by the oak_init / oak_assim driver.
+// initfile.F90), NetCDF classic-format variables (the "file.nc#variable" specifications of
+// ufileformat.F90) and GHER binary files (names without '#'). Used by the oak_init /
+// oak_assim driver.
 #pragma once
 #include <stdint.h>
 
@@ -42,7 +43,8 @@ struct Array {
   double valex = -9999.0;
 };
 
-// spec "file.nc#var" (NetCDF classic, 64-bit-offset or CDF-5 format); path prefixed
+// spec "file.nc#var" (NetCDF classic, 64-bit-offset or CDF-5 format) or "file" (GHER binary);
+// path prefixed
 bool read_array(const std::string& path, const std::string& spec, Array& out, std::string& err);
 
 }  // namespace io
