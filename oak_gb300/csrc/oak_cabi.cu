@@ -19,9 +19,9 @@
 // Ea = xa + sqrt(N - 1) Sa. runtype 0 and 1 return Ea = Ef (no analysis).
 //
 // Files are NetCDF classic-format variables ("file.nc#var") or GHER binary files (oak_io.cpp).
-// Not done
-// here: diagnostics files (Diag*), biastype / anamorphosis / other schemetypes (refused with
-// OAKG_ERR_NOTIMPL), curvilinear model grids (OAKG_ERR_NOTIMPL), operators read from files.
+// Not done here: diagnostics files (Diag*), biastype / anamorphosis / other schemetypes
+// (refused with OAKG_ERR_NOTIMPL), curvilinear model grids (OAKG_ERR_NOTIMPL), operators read
+// from files (OAKG_ERR_NOTIMPL).
 // The reference stops the process on an error; these functions record it for
 // oakg_last_status() / oakg_last_error() and leave Ea unchanged.
 #include <math.h>
