@@ -258,3 +258,66 @@ def test_driver_errors(oakg, tmp_path):
         oakg.oak_assim(1, Ef)
     assert ei.value.code == oakg.ERR_NOTIMPL and "operator" in str(ei.value)
     oakg.oak_done()
+
+
+def test_nested_grids_take_the_finest(oakg, tmp_path):
+    """Two model variables of the same name: a coarse grid (Model.hres 1) and a nested fine
+    one (hres 0.25). genObservationOper keeps, per observation, the finest grid that holds it
+    (assimilation.F90:2557-2590); observations outside both are excluded. Global scheme: the
+    analysis ensemble's mean and covariance against the Kalman formulas with that operator."""
+    rng = np.random.default_rng(5)
+    d = tmp_path / "data"
+    d.mkdir()
+    cx, cy = np.arange(0.0, 11.0), np.arange(0.0, 9.0)
+    fx, fy = np.arange(2.0, 5.01, 0.25), np.arange(2.0, 4.01, 0.25)
+    CX, CY = np.meshgrid(cx, cy, indexing="ij")
+    FX, FY = np.meshgrid(fx, fy, indexing="ij")
+    _write(d / "grids.nc", clon=CX, clat=CY, cmask=np.ones_like(CX), flon=FX, flat=FY,
+           fmask=np.ones_like(FX))
+    m = 40
+    ox = rng.uniform(0.0, 10.0, m)
+    oy = rng.uniform(0.0, 8.0, m)
+    ox[:12] = rng.uniform(2.0, 5.0, 12)
+    oy[:12] = rng.uniform(2.0, 4.0, 12)
+    ox[-1] = 11.5  # outside both grids
+    yo = rng.normal(size=m)
+    rmse = rng.uniform(0.5, 1.0, m)
+    _write(d / "obs.nc", x=ox, y=oy, v=yo, r=rmse)
+    lines = ["Model.variables = ['temp', 'temp']",
+             "Model.mask = ['grids.nc#cmask', 'grids.nc#fmask']",
+             "Model.gridX = ['grids.nc#clon', 'grids.nc#flon']",
+             "Model.gridY = ['grids.nc#clat', 'grids.nc#flat']",
+             "Model.hres = [1.0, 0.25]",
+             f"Model.path = '{d}/'", "schemetype = 0",
+             f"Obs001.path = '{d}/'", "Obs001.variables = ['temp']",
+             "Obs001.mask = ['obs.nc#v']", "Obs001.value = ['obs.nc#v']",
+             "Obs001.rmse = ['obs.nc#r']", "Obs001.gridX = ['obs.nc#x']",
+             "Obs001.gridY = ['obs.nc#y']"]
+    fname = _init(tmp_path / "nested.init", lines)
+    nc, nf = CX.size, FX.size
+    ic, wc = R.obsoper_rectilinear([cx, cy], [ox, oy])
+    i_f, wf = R.obsoper_rectilinear([fx, fy], [ox, oy], offset=nc)
+    fine = i_f[:, 0] >= 0
+    idx = np.where(fine[:, None], i_f, ic)
+    w = np.where(fine[:, None], wf, wc)
+    keep = idx[:, 0] >= 0
+    assert fine.sum() >= 12 and (~keep).sum() == 1
+    n, Nens = nc + nf, 12
+    H = np.zeros((keep.sum(), n))
+    for q, j in enumerate(np.nonzero(keep)[0]):
+        for c in range(4):
+            H[q, idx[j, c]] += w[j, c]
+    Ef = rng.normal(size=(n, Nens))
+    xf = Ef.mean(axis=1)
+    Efp = Ef - xf[:, None]
+    Pf = Efp @ Efp.T / (Nens - 1)
+    Rm = np.diag(rmse[keep] ** 2)
+    K = Pf @ H.T @ np.linalg.inv(H @ Pf @ H.T + Rm)
+    xa = xf + K @ (yo[keep] - H @ xf)
+    Pa = Pf - K @ H @ Pf
+    oakg.oak_init(fname)
+    Ea = oakg.oak_assim(1, Ef)
+    oakg.oak_done()
+    Eap = Ea - Ea.mean(axis=1)[:, None]
+    assert np.abs(Ea.mean(axis=1) - xa).max() < 1e-10
+    assert np.abs(Eap @ Eap.T / (Nens - 1) - Pa).max() < 1e-10
