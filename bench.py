@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--no-global", action="store_true")
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--no-layout", action="store_true")
+    p.add_argument("--no-rows", action="store_true",
+                   help="skip the ensemble / SMWCovar / rrsqrt-wrapper section")
     p.add_argument("--batched-scale", type=float, default=0.25,
                    help="horizontal scale of the 5-variable N = 100 batched workload "
                         "(0 skips it)")
@@ -520,6 +522,13 @@ def main():
     if not args.no_layout:
         layout = layout_section(torch, dev, stream, args, barrier)
 
+    # the analysis path's neighbours on the same workload: the whole-ensemble entry (H Ef,
+    # prologue, local analysis, epilogue), the SMWCovar observation covariance (k = 8), and the
+    # rrsqrt.F90 wrappers (ens2sqrt / sqrt2ens, ensAnalysis, biasedLocAnalysis)
+    rows = None
+    if not args.no_rows and rank == 0:
+        rows = rows_section(torch, dev, stream, args, c, d_args, ms, T, F)
+
     # e2e through the public API with host (pinned) buffers: H2D + D2H inside the timed region
     e2e = None
     if not args.no_e2e:
@@ -583,6 +592,7 @@ def main():
         "adjoint": adjoint,
         "global_analysis": glob,
         "layout": layout,
+        "rows": rows,
         "graph": graph,
         "gpu_launches": int(launches),
         "stage_ms_per_step": per_step,
@@ -675,6 +685,93 @@ def layout_section(torch, dev, stream, args, barrier):
             "obsoper_obs_per_s": ns / t_oper,
             "sample": f"oracle init_partition on {ps.size} elements, "
                       f"obsoper_rectilinear on {ns} observations (NumPy, one thread)"}
+    return res
+
+
+def rows_section(torch, dev, stream, args, c, d_args, fp64_ms, T, F):
+    import oak_gb300
+
+    def timed(fn, k=None):
+        k = k or args.steps
+        for _ in range(max(args.warmup, 3)):
+            out = fn()
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(k):
+            out = fn()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return out, a.elapsed_time(b) / k
+
+    res = {}
+    try:
+        zs, xf, Hxf, yo, Sf, HSf, r, zp, op, corr, maxl = d_args
+        n, N = int(Sf.shape[0]), int(Sf.shape[1])
+        m = int(yo.shape[0])
+        kw = dict(weight=c.weight, metric=c.metric, loctype=c.loctype)
+        # row 1: the ensemble (xf + sqrt(N-1) Sf) through H Ef, mean and anomalies, the local
+        # analysis, inflation and Ea
+        Ef = (xf[:, None] + Sf * float(np.sqrt(N - 1.0))).t().contiguous().t()
+        Hi = torch.as_tensor(np.asarray(c.obs_index, dtype=np.int64)[:, None], device=dev)
+        Hw = torch.ones((m, 1), dtype=torch.float64, device=dev)
+        _, ms1 = timed(lambda: oak_gb300.ens_loc_analysis(zs, Ef, Hi, Hw, yo, r, zp, op, corr,
+                                                           maxl, inflation=1.02, **kw))
+        res["ens_loc_analysis"] = {
+            "ms_per_call": ms1, "value": c.Z / (ms1 / 1e3), "unit": "local analyses/s",
+            "overhead_vs_loc_analysis_ms": ms1 - fp64_ms,
+            "what": "H Ef (K = 1), mean and anomalies, FP64 local analysis, inflation 1.02, "
+                    "Ea = xa + sqrt(N-1) Sa, all on the device"}
+        _, msp = timed(lambda: oak_gb300.ensemble_prologue(Ef, Hi, Hw))
+        pro_bytes = 2 * n * N * 8 + 2 * m * N * 8 + n * 8
+        res["ensemble_prologue"] = {"ms": msp, "achieved_GBs": pro_bytes / (msp / 1e3) / 1e9,
+                                    "algorithmic_bytes": pro_bytes}
+        # row 4: ens2sqrt / sqrt2ens
+        (mean, S), ms_e2s = timed(lambda: oak_gb300.ens2sqrt(Ef))
+        _, ms_s2e = timed(lambda: oak_gb300.sqrt2ens(mean, S))
+        e_bytes = 2 * n * N * 8
+        res["ens2sqrt"] = {"ms": ms_e2s, "achieved_GBs": e_bytes / (ms_e2s / 1e3) / 1e9}
+        res["sqrt2ens"] = {"ms": ms_s2e, "achieved_GBs": e_bytes / (ms_s2e / 1e3) / 1e9}
+        del Ef, mean, S
+        # row 2: R = diag(r) + B B^T with k = 8 columns
+        kB = 8
+        B = torch.empty((kB, m), dtype=torch.float64, device=dev).normal_(0.0, 0.05).t()
+        _, ms2 = timed(lambda: oak_gb300.loc_analysis(*d_args, want_ampl=False, smw_B=B, **kw))
+        res["smw_loc_analysis"] = {"ms_per_call": ms2, "value": c.Z / (ms2 / 1e3),
+                                   "unit": "local analyses/s", "k": kB,
+                                   "cost_vs_diagonal_R": ms2 / fp64_ms}
+        del B
+        # row 4: biasedLocAnalysis (two local analyses) on the same device inputs, gamma 0.3
+        bf = torch.zeros_like(xf)
+        _, ms3 = timed(lambda: oak_gb300.biased_loc_analysis(
+            0.3, zs, xf, bf, Hxf, yo, Sf, HSf, r, zp, op, corr, maxl, Hi, Hw, want_sa=False,
+            **kw), k=2)
+        res["biased_loc_analysis"] = {"ms_per_call": ms3, "cost_vs_loc_analysis": ms3 / fp64_ms}
+        # row 4: ensAnalysis on the global configuration (100 x 80, N = 30, m = 500)
+        from oak_gb300.workloads import global_case
+        g = global_case(keep_ensemble=True)
+        gE, gH = F(g.Ef), F(g.HEf)
+        gy, gr = T(g.yo), T(g.r_diag)
+        _, ms4 = timed(lambda: oak_gb300.ens_analysis(gE, gH, gy, gr), k=20)
+        res["ens_analysis_global"] = {"ms_per_call": ms4}
+        if not args.no_cpu_baseline:
+            # NumPy on one core, a port: the prologue's mean and anomalies and ens2sqrt on a
+            # 64-member sample of 10^6 state rows
+            import time
+            rng = np.random.default_rng(3)
+            Eh = np.asfortranarray(rng.normal(size=(1_000_000, N)))
+            t0 = time.perf_counter()
+            mu = Eh.mean(axis=1)
+            _ = (Eh - mu[:, None]) / np.sqrt(N - 1.0)
+            t_pro = time.perf_counter() - t0
+            res["cpu_baseline"] = {
+                "kind": "port", "cores": 1,
+                "prologue_rows_per_s": Eh.shape[0] / t_pro,
+                "sample": "NumPy mean and scaled anomalies of a 10^6 x 64 ensemble, one core"}
+        res["gpu_rows_per_s_prologue"] = n / (msp / 1e3)
+    except Exception as ex:  # the section is auxiliary: report, keep the bench line
+        res["error"] = f"{type(ex).__name__}: {ex}"
     return res
 
 
