@@ -109,49 +109,11 @@ io::Array read(const State& s, const std::string& path, const std::string& spec)
   return a;
 }
 
-// ureadfull_srepmat (ufileformat.F90:980-1035): a file whose shape differs from the
-// variable's is replicated along the dimensions it lacks (each file dimension 1 or equal to
-// the variable's, after padding with trailing ones; else matched in order by length).
 std::vector<double> replicate(const io::Array& a, const std::vector<int64_t>& t,
                               const std::string& what) {
-  int64_t nt = 1;
-  for (int64_t x : t) nt *= x;
-  if ((int64_t)a.v.size() == nt) return a.v;
-  const size_t nd = t.size();
-  std::vector<int64_t> map(nd, -1);  // target dim -> file dim (or -1: replicated)
-  std::vector<int64_t> s = a.shape;
-  bool ok = s.size() <= nd;
-  if (ok) {
-    for (size_t k = 0; k < s.size() && ok; k++) ok = s[k] == t[k] || s[k] == 1;
-    if (ok)
-      for (size_t k = 0; k < s.size(); k++) map[k] = s[k] == 1 ? -1 : (int64_t)k;
-  }
-  if (!ok) {
-    std::fill(map.begin(), map.end(), -1);
-    size_t k = 0;
-    ok = true;
-    for (size_t q = 0; q < a.shape.size() && ok; q++) {
-      if (a.shape[q] == 1) continue;
-      while (k < nd && t[k] != a.shape[q]) k++;
-      ok = k < nd;
-      if (ok) map[k++] = (int64_t)q;
-    }
-  }
-  need(ok, what + ": file shape does not fit the variable's shape");
-  std::vector<int64_t> fstride(a.shape.size(), 1);
-  for (size_t q = 1; q < a.shape.size(); q++) fstride[q] = fstride[q - 1] * a.shape[q - 1];
-  std::vector<double> out((size_t)nt);
-  std::vector<int64_t> idx(nd, 0);
-  for (int64_t e = 0; e < nt; e++) {
-    int64_t f = 0;
-    for (size_t k = 0; k < nd; k++)
-      if (map[k] >= 0) f += idx[k] * fstride[map[k]];
-    out[e] = a.v[f];
-    for (size_t k = 0; k < nd; k++) {
-      if (++idx[k] < t[k]) break;
-      idx[k] = 0;
-    }
-  }
+  std::vector<double> out;
+  std::string err;
+  need(io::replicate(a, t, out, err), what + ": " + err);
   return out;
 }
 
@@ -215,44 +177,9 @@ std::vector<double> load_vector(const State& s, const std::string& key, const La
   return out;
 }
 
-// Fortran edit descriptors of the ensemble file formats, e.g. ("Ens",I3.3,"/m.nc#v"): quoted
-// literals and Iw / Iw.m integers (loadVectorSpace, :1214-1220)
 std::string fortran_format(const std::string& fmt, int k) {
-  std::string f = fmt;
-  while (!f.empty() && (f.front() == ' ')) f.erase(f.begin());
-  while (!f.empty() && (f.back() == ' ')) f.pop_back();
-  need(f.size() >= 2 && f.front() == '(' && f.back() == ')', "format '" + fmt + "'");
-  f = f.substr(1, f.size() - 2);
-  std::string out;
-  size_t i = 0;
-  while (i < f.size()) {
-    const char c = f[i];
-    if (c == ' ' || c == ',') {
-      i++;
-    } else if (c == '"' || c == '\'') {
-      size_t j = f.find(c, i + 1);
-      need(j != std::string::npos, "format '" + fmt + "'");
-      out += f.substr(i + 1, j - i - 1);
-      i = j + 1;
-    } else if (c == 'I' || c == 'i') {
-      size_t j = i + 1;
-      int w = 0, m = 0;
-      while (j < f.size() && isdigit((unsigned char)f[j])) w = w * 10 + (f[j++] - '0');
-      if (j < f.size() && f[j] == '.') {
-        j++;
-        while (j < f.size() && isdigit((unsigned char)f[j])) m = m * 10 + (f[j++] - '0');
-      }
-      need(w > 0, "format '" + fmt + "': I needs a width");
-      std::string d = std::to_string(k);
-      while ((int)d.size() < m) d = "0" + d;
-      if ((int)d.size() > w) d = std::string(w, '*');
-      while ((int)d.size() < w) d = " " + d;
-      out += d;
-      i = j;
-    } else {
-      throw Fail{OAKG_ERR_NOTIMPL, "format '" + fmt + "': only quoted text and I edits"};
-    }
-  }
+  std::string out, err;
+  need(io::fortran_format(fmt, k, out, err), err, OAKG_ERR_NOTIMPL);
   return out;
 }
 

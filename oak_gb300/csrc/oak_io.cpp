@@ -9,6 +9,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <memory>
 
@@ -204,6 +206,109 @@ double InitFile::num_or(const std::string& key, double dflt) const {
   std::string e;
   double v;
   return (has(key) && num(key, v, e)) ? v : dflt;
+}
+
+// ureadfull_srepmat (ufileformat.F90:980-1035): a file whose shape differs from the
+// variable's is replicated along the dimensions it lacks (each file dimension 1 or equal to
+// the variable's, after padding with trailing ones; else matched in order by length).
+bool replicate(const Array& a, const std::vector<int64_t>& t, std::vector<double>& out,
+               std::string& err) {
+  int64_t nt = 1;
+  for (int64_t x : t) nt *= x;
+  if ((int64_t)a.v.size() == nt) {
+    out = a.v;
+    return true;
+  }
+  const size_t nd = t.size();
+  std::vector<int64_t> map(nd, -1);  // target dim -> file dim (or -1: replicated)
+  const std::vector<int64_t>& s = a.shape;
+  bool ok = s.size() <= nd;
+  if (ok) {
+    for (size_t k = 0; k < s.size() && ok; k++) ok = s[k] == t[k] || s[k] == 1;
+    if (ok)
+      for (size_t k = 0; k < s.size(); k++) map[k] = s[k] == 1 ? -1 : (int64_t)k;
+  }
+  if (!ok) {
+    std::fill(map.begin(), map.end(), -1);
+    size_t k = 0;
+    ok = true;
+    for (size_t q = 0; q < s.size() && ok; q++) {
+      if (s[q] == 1) continue;
+      while (k < nd && t[k] != s[q]) k++;
+      ok = k < nd;
+      if (ok) map[k++] = (int64_t)q;
+    }
+  }
+  if (!ok) {
+    err = "file shape does not fit the variable's shape";
+    return false;
+  }
+  std::vector<int64_t> fstride(s.size(), 1);
+  for (size_t q = 1; q < s.size(); q++) fstride[q] = fstride[q - 1] * s[q - 1];
+  out.assign((size_t)nt, 0.0);
+  std::vector<int64_t> idx(nd, 0);
+  for (int64_t e = 0; e < nt; e++) {
+    int64_t f = 0;
+    for (size_t k = 0; k < nd; k++)
+      if (map[k] >= 0) f += idx[k] * fstride[map[k]];
+    out[e] = a.v[f];
+    for (size_t k = 0; k < nd; k++) {
+      if (++idx[k] < t[k]) break;
+      idx[k] = 0;
+    }
+  }
+  return true;
+}
+
+// Fortran edit descriptors of the ensemble file formats, e.g. ("Ens",I3.3,"/m.nc#v"): quoted
+// literals and Iw / Iw.m integers (loadVectorSpace, assimilation.F90:1214-1220)
+bool fortran_format(const std::string& fmt, int k, std::string& out, std::string& err) {
+  std::string f = fmt;
+  while (!f.empty() && f.front() == ' ') f.erase(f.begin());
+  while (!f.empty() && f.back() == ' ') f.pop_back();
+  out.clear();
+  if (f.size() < 2 || f.front() != '(' || f.back() != ')') {
+    err = "format '" + fmt + "': expected (...)";
+    return false;
+  }
+  f = f.substr(1, f.size() - 2);
+  size_t i = 0;
+  while (i < f.size()) {
+    const char c = f[i];
+    if (c == ' ' || c == ',') {
+      i++;
+    } else if (c == '"' || c == '\'') {
+      const size_t j = f.find(c, i + 1);
+      if (j == std::string::npos) {
+        err = "format '" + fmt + "': unterminated text";
+        return false;
+      }
+      out += f.substr(i + 1, j - i - 1);
+      i = j + 1;
+    } else if (c == 'I' || c == 'i') {
+      size_t j = i + 1;
+      int w = 0, m = 0;
+      while (j < f.size() && isdigit((unsigned char)f[j])) w = w * 10 + (f[j++] - '0');
+      if (j < f.size() && f[j] == '.') {
+        j++;
+        while (j < f.size() && isdigit((unsigned char)f[j])) m = m * 10 + (f[j++] - '0');
+      }
+      if (w <= 0) {
+        err = "format '" + fmt + "': I needs a width";
+        return false;
+      }
+      std::string d = std::to_string(k);
+      while ((int)d.size() < m) d = "0" + d;
+      if ((int)d.size() > w) d = std::string(w, '*');
+      while ((int)d.size() < w) d = " " + d;
+      out += d;
+      i = j;
+    } else {
+      err = "format '" + fmt + "': only quoted text and I edits are supported";
+      return false;
+    }
+  }
+  return true;
 }
 
 // ------------------------------------------------------------------------------ NetCDF

@@ -43,6 +43,15 @@ struct Array {
   double valex = -9999.0;
 };
 
+// The values of a file whose shape is smaller than the variable's shape t, replicated along the
+// missing dimensions (ureadfull_srepmat, ufileformat.F90:980-1035); false when they do not fit.
+bool replicate(const Array& a, const std::vector<int64_t>& t, std::vector<double>& out,
+               std::string& err);
+
+// A file name from a Fortran format of quoted text and Iw / Iw.m edits applied to k, e.g.
+// ("Ens",I3.3,"/model.nc#var1") -> Ens007/model.nc#var1; false for other edits.
+bool fortran_format(const std::string& fmt, int k, std::string& out, std::string& err);
+
 // spec "file.nc#var" (NetCDF classic, 64-bit-offset or CDF-5 format) or "file" (GHER binary);
 // path prefixed
 bool read_array(const std::string& path, const std::string& spec, Array& out, std::string& err);

@@ -67,3 +67,42 @@ def test_reference_syntax(probe, tmp_path):
 def test_malformed_lines(probe, tmp_path, bad):
     lines = _run(probe, bad + "\n", tmp_path, "k")
     assert lines[0].startswith("ERROR") and ":1:" in lines[0]
+
+
+@pytest.fixture(scope="module")
+def io_probe(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    out = tmp_path_factory.mktemp("ioprobe") / "io_probe"
+    subprocess.run([cxx, "-std=c++17", "-O1", "-I", CSRC, os.path.join(HERE, "io_probe.cpp"),
+                    os.path.join(CSRC, "oak_io.cpp"), "-o", str(out)], check=True)
+    return str(out)
+
+
+def _io(io_probe, *args):
+    return subprocess.run([io_probe, *map(str, args)], capture_output=True, text=True,
+                          check=True).stdout.strip()
+
+
+def test_fortran_format_file_names(io_probe):
+    """loadVectorSpace's file names (assimilation.F90:1214-1220): Fortran I edits."""
+    assert _io(io_probe, "fmt", '("Ens",I3.3,"/model.nc#var1")', 7) == "Ens007/model.nc#var1"
+    assert _io(io_probe, "fmt", "('S',I3.3,'-obs.nc#var1')", 12) == "S012-obs.nc#var1"
+    assert _io(io_probe, "fmt", '("m",I4,".nc#v")', 42) == "m  42.nc#v"
+    assert _io(io_probe, "fmt", '("m",I2,".nc")', 123) == "m**.nc"  # Fortran overflow stars
+    assert _io(io_probe, "fmt", '("m",F5.2)', 1).startswith("ERROR")
+    assert _io(io_probe, "fmt", '"no parentheses"', 1).startswith("ERROR")
+
+
+def test_replication_of_smaller_files(io_probe):
+    """ureadfull_srepmat: a 2-D field replicated along a third dimension, a depth profile
+    matched to the third dimension, identical sizes passed through, misfits refused."""
+    # file 2 x 3 (values 0..5) onto 2 x 3 x 2: repeated per level
+    assert _io(io_probe, "rep", 2, 3, "-", 2, 3, 2) == "0 1 2 3 4 5 0 1 2 3 4 5"
+    # file of 3 levels onto 2 x 2 x 3: constant over the horizontal
+    assert _io(io_probe, "rep", 3, "-", 2, 2, 3) == "0 0 0 0 1 1 1 1 2 2 2 2"
+    # a unit dimension in the file broadcasts
+    assert _io(io_probe, "rep", 1, 3, "-", 2, 3) == "0 0 1 1 2 2"
+    assert _io(io_probe, "rep", 6, "-", 2, 3) == "0 1 2 3 4 5"
+    assert _io(io_probe, "rep", 4, "-", 2, 3).startswith("ERROR")
