@@ -688,6 +688,35 @@ def layout_section(torch, dev, stream, args, barrier):
     return res
 
 
+def rows_cpu_baseline(c, N, zones=128):
+    """The oracle (NumPy, one core, a port) beside the rows section: the prologue's mean and
+    anomalies of a 10^6 x N ensemble, and the SMWCovar (k = 8) and diagonal-R local analyses on
+    a sample of every k-th zone with all observations."""
+    import time
+    from oracle import oakref as R
+    rng = np.random.default_rng(3)
+    Eh = np.asfortranarray(rng.normal(size=(1_000_000, N)))
+    t0 = time.perf_counter()
+    mu = Eh.mean(axis=1)
+    _ = (Eh - mu[:, None]) / np.sqrt(N - 1.0)
+    t_pro = time.perf_counter() - t0
+    del Eh, _
+    zsel, rows = cpu_sample(c, zones)
+    sel = R.geometric_selector(c.zone_pos[zsel], c.obs_pos, c.corr_len[zsel], c.max_len[zsel],
+                               c.metric, c.loctype, c.weight)
+    B = np.random.default_rng(4).normal(0.0, 0.05, size=(c.m, 8))
+    out = {"kind": "port", "cores": 1, "prologue_rows_per_s": 1_000_000 / t_pro}
+    for name, smw in (("loc_analysis", None), ("smw_loc_analysis", B)):
+        t0 = time.perf_counter()
+        R.loc_analysis(c.zone_size[zsel], sel, c.xf[rows], c.Hxf, c.yo, c.Sf[rows], c.HSf,
+                       c.r_diag, smw_B=smw)
+        out[name + "_zones_per_s"] = len(zsel) / (time.perf_counter() - t0)
+    out["sample"] = (f"NumPy mean and scaled anomalies of a 10^6 x {N} ensemble; the oracle's "
+                     f"local analyses (diagonal R and SMWCovar k = 8) on {len(zsel)} of "
+                     f"{c.Z} zones with all {c.m} observations, one core")
+    return out
+
+
 def rows_section(torch, dev, stream, args, c, d_args, fp64_ms, T, F):
     import oak_gb300
 
@@ -756,19 +785,7 @@ def rows_section(torch, dev, stream, args, c, d_args, fp64_ms, T, F):
         _, ms4 = timed(lambda: oak_gb300.ens_analysis(gE, gH, gy, gr), k=20)
         res["ens_analysis_global"] = {"ms_per_call": ms4}
         if not args.no_cpu_baseline:
-            # NumPy on one core, a port: the prologue's mean and anomalies and ens2sqrt on a
-            # 64-member sample of 10^6 state rows
-            import time
-            rng = np.random.default_rng(3)
-            Eh = np.asfortranarray(rng.normal(size=(1_000_000, N)))
-            t0 = time.perf_counter()
-            mu = Eh.mean(axis=1)
-            _ = (Eh - mu[:, None]) / np.sqrt(N - 1.0)
-            t_pro = time.perf_counter() - t0
-            res["cpu_baseline"] = {
-                "kind": "port", "cores": 1,
-                "prologue_rows_per_s": Eh.shape[0] / t_pro,
-                "sample": "NumPy mean and scaled anomalies of a 10^6 x 64 ensemble, one core"}
+            res["cpu_baseline"] = rows_cpu_baseline(c, N)
         res["gpu_rows_per_s_prologue"] = n / (msp / 1e3)
     except Exception as ex:  # the section is auxiliary: report, keep the bench line
         res["error"] = f"{type(ex).__name__}: {ex}"
