@@ -9,9 +9,12 @@ reference's own argument order, with 0-based indices where the reference is 1-ba
 Arrays follow the reference layout: state/observation vectors are 1-D, ensembles are
 ``(n, N)`` matrices (members are columns).
 
-Pinned against the reference's own known-answer tests (``test/test_rrsqrt.F90`` Kalman-formula
-identities, ``test/test_covariance.F90:612-617`` ``locfun`` values) by
-``tests/test_oracle_golden.py``.
+Pinned against the reference's own known-answer tests:
+- ``test/test_rrsqrt.F90`` Kalman-formula identities and its SMWCovar cases,
+  ``test/test_covariance.F90:612-617`` ``locfun`` values, ``test/assimtest2.F90`` identities
+  and ``test/test_assim.F90``'s Kalman case, by ``tests/test_oracle_golden.py``;
+- ``test/test_ndgrid.F90``'s linear-function checks for ``split`` / ``cinterp`` and the
+  ``initPartition`` error cases, by ``tests/test_oracle_layout.py``.
 """
 from __future__ import annotations
 
