@@ -59,3 +59,16 @@ def test_python_argtypes_match_header():
         if at is not None and len(at) != k:
             bad[name] = (len(at), k)
     assert not bad, f"argtypes length != header parameter count: {bad}"
+
+
+def test_header_compiles_as_c_and_cpp(tmp_path):
+    """include/oakg.h is a plain C header (C99) usable from C++ as well."""
+    import shutil
+    import subprocess
+    header = os.path.join(ROOT, "include", "oakg.h")
+    for comp, lang, std in (("gcc", "c", "-std=c99"), ("g++", "c++", "-std=c++11")):
+        exe = shutil.which(comp)
+        if exe is None:
+            pytest.skip(f"no {comp}")
+        subprocess.run([exe, "-fsyntax-only", std, "-Wall", "-Werror", "-x", lang, header],
+                       check=True)
