@@ -124,3 +124,50 @@ def test_partition_compact_hand_case():
     """unique(..., ind2 = partition): labels replaced by their rank among the distinct ones."""
     part, nz = R.partition_compact(np.array([5, -3, 5, 100, -3, 7]))
     assert nz == 4 and list(part) == [2, 1, 2, 4, 1, 3]
+
+
+def _locate(p, n):
+    """The operator kernel's direct simplex location (zone_layout.cu, locate_simplex) restated:
+    per level, the free axis of largest |p - 1/2| and its side pick the block of split's
+    numbering; the point is projected from the centroid onto that face."""
+    p = list(p)
+    fixed, l = 0, 0
+    for subn in range(n, 1, -1):
+        sub = math.factorial(subn - 1) << (subn - 2)
+        best, best_rank, rank, dev = 0, 0, 0, -1.0
+        for k in range(n):
+            if (fixed >> k) & 1:
+                continue
+            d = abs(p[k] - 0.5)
+            if d > dev:
+                dev, best, best_rank = d, k, rank
+            rank += 1
+        side = 1 if p[best] > 0.5 else 0
+        l += (2 * best_rank + side) * sub
+        if dev > 0:
+            t = 0.5 / dev
+            for k in range(n):
+                if not (fixed >> k) & 1 and k != best:
+                    p[k] = 0.5 + (p[k] - 0.5) * t
+        p[best] = float(side)
+        fixed |= 1 << best
+    return l
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+def test_direct_location_is_the_first_accepting_simplex(n):
+    """For points in general position the located simplex is the one interp_cube's ordered
+    search accepts first; for corners, centres and half-integer points it accepts the point."""
+    rng = np.random.default_rng(70 + n)
+    T = R.split(n)
+    K = 1 << n
+    P = np.array([[(c >> k) & 1 for c in range(K)] for k in range(n)], dtype=float)
+    for u in rng.random((300, n)):
+        l = _locate(u, n)
+        first = next(q for q in range(T.shape[0])
+                     if not R.interp_tetrahedron(P @ T[q].T, u)[0])
+        assert l == first
+    special = [np.full(n, 0.5), np.zeros(n), np.ones(n)]
+    special += [rng.integers(0, 3, n) / 2.0 for _ in range(60)]
+    for u in special:
+        assert not R.interp_tetrahedron(P @ T[_locate(u, n)].T, u)[0]
