@@ -90,26 +90,33 @@ def cpu_sample(c, target_zones):
     return zsel, rows
 
 
-def run_cpu_oracle(c, zsel, rows, threads):
+def run_cpu_oracle(c, zsel, rows, threads, keep=None):
+    """Times one oracle pass over the zones `zsel` (state rows `rows`); with a list `keep`,
+    keeps the pass's outputs (zsel, rows, xa, Sa, nobs) in it for the parity record."""
     from oracle import cref
     t0 = time.perf_counter()
-    cref.locanalysis(c.zone_size[zsel], c.xf[rows], c.Hxf, c.yo, c.Sf[rows], c.HSf, c.r_diag,
-                     c.zone_pos[zsel], c.obs_pos, c.corr_len[zsel], c.max_len[zsel],
-                     kind=c.weight, metric=c.metric, loctype=c.loctype, nthreads=threads)
-    return time.perf_counter() - t0
+    xa, Sa, _, nobs = cref.locanalysis(
+        c.zone_size[zsel], c.xf[rows], c.Hxf, c.yo, c.Sf[rows], c.HSf, c.r_diag,
+        c.zone_pos[zsel], c.obs_pos, c.corr_len[zsel], c.max_len[zsel], kind=c.weight,
+        metric=c.metric, loctype=c.loctype, nthreads=threads)
+    dt = time.perf_counter() - t0
+    if keep is not None:
+        keep[:] = [(zsel, rows, xa, Sa, nobs)]
+    return dt
 
 
-def cpu_baseline(c, seconds, threads):
+def cpu_baseline(c, seconds, threads, keep=None):
     """Times the C/OpenMP oracle for ~`seconds` of CPU work: whole passes over the workload
-    while one pass fits the budget, else a zone sample sized from a calibration run."""
+    while one pass fits the budget, else a zone sample sized from a calibration run. The last
+    pass's outputs go to `keep` (see run_cpu_oracle)."""
     zsel, rows = cpu_sample(c, 2048)
-    dt = run_cpu_oracle(c, zsel, rows, threads)          # calibration
+    dt = run_cpu_oracle(c, zsel, rows, threads, keep)    # calibration
     per_zone = dt / len(zsel)
     if per_zone * c.Z <= seconds:
         zsel, rows = np.arange(c.Z), np.arange(c.n)
         total, passes = 0.0, 0
         while total < seconds and passes < 8:
-            total += run_cpu_oracle(c, zsel, rows, threads)
+            total += run_cpu_oracle(c, zsel, rows, threads, keep)
             passes += 1
         return {"value": passes * c.Z / total, "unit": UNIT, "cores": threads, "kind": "port",
                 "sample": f"{passes} full passes over all {c.Z} zones and {c.m} observations "
@@ -118,11 +125,40 @@ def cpu_baseline(c, seconds, threads):
                           f"schedule"}
     target = int(min(c.Z, max(256, seconds / max(per_zone, 1e-9))))
     zsel, rows = cpu_sample(c, target)
-    dt = run_cpu_oracle(c, zsel, rows, threads)
+    dt = run_cpu_oracle(c, zsel, rows, threads, keep)
     return {"value": len(zsel) / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(zsel)} of {c.Z} zones (every {c.Z // len(zsel)}-th), all {c.m} "
                       f"observations, brute-force selection as assimilation.F90:3745-3757, "
                       f"LAPACK dsyev via SciPy, OpenMP dynamic schedule, {dt:.2f} s"}
+
+
+def parity_record(xa_d, Sa_d, nobs_d, c, ref, tol):
+    """Errors of one form's outputs (device tensors xa (n), Sa (n, N), nobs (Z)) against the
+    oracle pass in `ref` (zsel, rows, xa, Sa, nobs): the increment-relative error of the mean
+    ||xa - xa_o|| / ||xa_o - xf||, the relative Frobenius error of the anomalies, and the
+    selection counts (compared exactly). Rows of zones whose count differs are left out of
+    the norms (none, for the Cartesian metric)."""
+    zsel, rows, xa_o, Sa_o, nobs_o = ref
+    full = len(rows) == c.n
+    xa = xa_d.cpu().numpy() if full else xa_d[torch_index(xa_d, rows)].cpu().numpy()
+    Sa = Sa_d.cpu().numpy() if full else Sa_d[torch_index(Sa_d, rows)].cpu().numpy()
+    nobs = nobs_d.cpu().numpy()[zsel]
+    same = nobs == nobs_o
+    keep = np.repeat(same, c.zone_size[zsel])
+    xf = c.xf[rows][keep]
+    inc = max(float(np.linalg.norm(xa_o[keep] - xf)), 1e-300)
+    e_mean = float(np.linalg.norm(xa[keep] - xa_o[keep])) / inc
+    e_anom = float(np.linalg.norm(Sa[keep] - Sa_o[keep]) / max(np.linalg.norm(Sa_o[keep]), 1e-300))
+    e_abs = float(np.linalg.norm(xa[keep] - xa_o[keep]) / max(np.linalg.norm(xa_o[keep]), 1e-300))
+    return {"zones": int(len(zsel)), "zones_same_selection": int(same.sum()),
+            "rel_err_mean_increment": e_mean, "rel_err_mean": e_abs,
+            "rel_err_anomalies": e_anom, "tolerance": tol,
+            "pass": bool(same.all() and e_mean <= tol and e_anom <= tol)}
+
+
+def torch_index(t, rows):
+    import torch
+    return torch.as_tensor(rows, device=t.device)
 
 
 # --------------------------------------------------------------------------- clocks
@@ -211,8 +247,9 @@ def main():
     # workload first (numpy), CPU baseline before any CUDA work
     c = local_case(scale=args.scale)
     cpu = None
+    oracle_out = []   # the oracle's outputs of its last timed pass, for the parity record
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(c, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = cpu_baseline(c, args.cpu_seconds, os.cpu_count() or 1, oracle_out)
 
     if ws > 1:
         import torch.distributed as dist
@@ -272,6 +309,12 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * c.Z / (ms / 1e3)
+    parity = None
+    if oracle_out:
+        parity = {"oracle": "oracle/oakref.c (C/OpenMP restatement, LAPACK dsyev), the passes "
+                            "of cpu_baseline",
+                  "fp64": parity_record(out[0], out[1], out[3], c,
+                                        oracle_out[0], 1e-10)}
 
     # mixed-precision form on the same device inputs; errors against the FP64 form's outputs
     mixed = None
@@ -301,6 +344,8 @@ def main():
         xf_d = d_args[1]
         e_mean = float(torch.linalg.norm(mout[0] - ref_xa) / torch.linalg.norm(ref_xa - xf_d))
         e_anom = float(torch.linalg.norm(mout[1] - ref_Sa) / torch.linalg.norm(ref_Sa))
+        if parity is not None:
+            parity["mixed"] = parity_record(mout[0], mout[1], mout[3], c, oracle_out[0], 1e-4)
         mixed = {"value": ws * c.Z / (mms / 1e3), "unit": UNIT, "ms_per_step": mms,
                  "speedup_vs_fp64": ms / mms, "rel_err_mean_increment": e_mean,
                  "rel_err_anomalies": e_anom,
@@ -586,6 +631,7 @@ def main():
         "config": workload_config(c, args.scale) | {"parallelism": f"zones sharded, {ws} GPU(s)",
                                                      "zones_with_obs": int((nobs > 0).sum())},
         "e2e": e2e,
+        "parity": parity,
         "mixed": mixed,
         "batched": batched,
         "large": large,

@@ -160,7 +160,8 @@ int oakg_locanalysis_adjoint(const oakg_dims* dims, const oakg_loc* loc, int32_t
  *   - dims->mem must be OAKG_MEM_DEVICE; N (dims->N) must be <= 112, else OAKG_ERR_ARGS.
  *   - Calls share the array: calls that overlap on the GPU race, so serialise them.
  *   - The first call on a device also looks up the array's device address; make that first
- *     call before any stream capture. */
+ *     call before any stream capture. The address is kept until the process exits: do not
+ *     reset the device's primary context (cudaDeviceReset) while the library is loaded. */
 int oakg_analysis_noalloc(const oakg_dims* dims, const double* xf, const double* Hxf,
                           const double* yo, const double* Sf, const double* HSf,
                           const double* r_diag, double* xa, double* Sa, double* ampl,

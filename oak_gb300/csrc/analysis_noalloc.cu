@@ -14,7 +14,9 @@
 //    on the GPU (other threads, other streams) race on the array: serialise them.
 //  - the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (once per device, with that device current); make that first call
-//    before any stream capture.
+//    before any stream capture. The address is kept for the life of the process, which
+//    assumes the device's primary context is not reset (cudaDeviceReset) while the library is
+//    loaded: a reset reloads the module and leaves the kept address stale.
 //  - no cudaMalloc, cudaFree or other allocating routine is called.
 #include <cuda_runtime.h>
 

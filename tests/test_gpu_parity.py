@@ -28,6 +28,14 @@ def check_local(xa, Sa, xa_r, Sa_r, xf, tol=REL):
     assert rel_err(Sa, Sa_r) < tol, "Sa"
 
 
+def check_local_on_zones(xa, Sa, xa_r, Sa_r, xf, zone_size, keep, tol=REL):
+    """check_local restricted to the rows of the zones where `keep` is true (zones are
+    consecutive row blocks of zone_size rows, rrsqrt.F90:328-335)."""
+    rows = np.repeat(np.asarray(keep, bool), np.asarray(zone_size))
+    assert rows.any()
+    check_local(xa[rows], Sa[rows], xa_r[rows], Sa_r[rows], xf[rows], tol)
+
+
 # ------------------------------------------------------------------ reference known answers
 
 def test_analysis_rrsqrt_case_kalman(oakg):
@@ -128,13 +136,15 @@ def test_random_local_matches_oracle(oakg, metric, loctype, kind):
     P = _random_local(11 + metric * 7 + loctype * 3 + kind, metric=metric, loctype=loctype,
                       kind=kind)
     (xa, Sa, _, nobs), (xa_o, Sa_o, nobs_o) = _run_both(oakg, P)
+    same = nobs == nobs_o
     if metric == 0:
-        assert np.array_equal(nobs, nobs_o)
-    else:  # transcendental functions may differ by an ulp at the cut-off radius
-        assert np.sum(nobs != nobs_o) <= 1
-    assert nobs.max() > 0 and (nobs == 0).any() or True
-    if np.array_equal(nobs, nobs_o):
-        check_local(xa, Sa, xa_o, Sa_o, P["xf"])
+        assert same.all()
+    else:  # CUDA's sin/cos/acos may differ from the host's by an ulp at the cut-off radius
+        assert np.sum(~same) <= 1
+    assert nobs.max() > 0
+    # the numbers are compared on every zone whose selection agrees (all of them, or all but
+    # the one zone an ulp at the cut-off moved)
+    check_local_on_zones(xa, Sa, xa_o, Sa_o, P["xf"], P["zs"], same)
 
 
 @pytest.mark.parametrize("N", [2, 7, 30, 64, 100, 113, 128])

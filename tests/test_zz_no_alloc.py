@@ -4,7 +4,9 @@ cudaMalloc/cudaFree synchronise the device inside an assimilation cycle).
 
 Called through the C ABI with device arrays, twice in a row on different problems (different
 ensemble sizes, so a stale scratch array would show), and compared with oakg_analysis, the
-existing entry point, at the tolerance of the other parity tests (1e-10 relative). This file
+existing entry point, at the tolerance of the other parity tests (1e-10 relative). Also: a call
+without observations right after one with observations (nothing stale may leak through the
+shared array), and the device's free memory unchanged across calls. This file
 sorts last so that a run stopping at the first failure has run every other test first; it
 also passes on its own in a fresh process.
 """
@@ -36,19 +38,30 @@ def _device_case(torch, xf, Hxf, yo, Sf, HSf, r):
     return T(xf), T(Hxf), T(yo), F(Sf), F(HSf), T(r)
 
 
-def _run_noalloc(oakg, torch, fn, args):
+def _outputs(torch, args):
+    xf, Sf = args[0], args[3]
+    n, N = xf.numel(), Sf.shape[1]
+    return (torch.empty_like(xf), torch.empty((N, n), dtype=torch.float64, device=xf.device).t(),
+            torch.empty(N, dtype=torch.float64, device=xf.device))
+
+
+def _call(oakg, torch, fn, args, outs):
+    """One call into the C ABI on torch's current stream; the outputs are the caller's."""
     xf, Hxf, yo, Sf, HSf, r = args
-    n, N, m = xf.numel(), Sf.shape[1], yo.numel()
-    xa = torch.empty_like(xf)
-    Sa = torch.empty((N, n), dtype=torch.float64, device=xf.device).t()
-    ampl = torch.empty(N, dtype=torch.float64, device=xf.device)
+    xa, Sa, ampl = outs
+    n, N, m = xf.numel(), Sf.shape[1], (0 if yo is None else yo.numel())
     dims = oakg.Dims(n=n, N=N, m=m, ldS=n, ldH=m, mem=oakg.MEM_DEVICE)
-    torch.cuda.synchronize()
-    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    p = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
     rc = fn(ctypes.byref(dims), p(xf), p(Hxf), p(yo), p(Sf), p(HSf), p(r), p(xa), p(Sa), p(ampl),
             ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == 0, oakg.lib().oakg_last_status()
-    return xa.cpu().numpy(), Sa.cpu().numpy(), ampl.cpu().numpy()
+
+
+def _run_noalloc(oakg, torch, fn, args):
+    outs = _outputs(torch, args)
+    torch.cuda.synchronize()
+    _call(oakg, torch, fn, args, outs)
+    return tuple(t.cpu().numpy() for t in outs)
 
 
 def _rel(a, b):
@@ -83,3 +96,42 @@ def test_noalloc_rejects_oversized_ensemble(oakg):
     buf = ctypes.create_string_buffer(256)
     oakg.lib().oakg_last_error(buf, 256)
     assert b"112" in buf.value
+
+
+def test_noalloc_no_observations_after_observations(oakg):
+    """m = 0 right after an m > 0 call: the Gram is skipped, so a stale Gram matrix or stale
+    amplitudes left in the shared array by the previous call must not leak into the result;
+    the reference returns xa = xf, Sa = Sf and zero amplitudes (rrsqrt.F90:371)."""
+    torch = pytest.importorskip("torch")
+    fn = _noalloc(oakg)
+    c = global_case()
+    args = _device_case(torch, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag)
+    _run_noalloc(oakg, torch, fn, args)
+    xf, _, _, Sf, _, _ = args
+    xa, Sa, ampl = _run_noalloc(oakg, torch, fn, (xf, None, None, Sf, None, None))
+    assert np.array_equal(xa, c.xf)
+    assert np.array_equal(Sa, c.Sf)
+    assert np.all(ampl == 0)
+
+
+def test_noalloc_allocates_no_device_memory(oakg):
+    """The free device memory is the same before and after two calls (inputs and outputs made
+    beforehand, and oakg_analysis run first since it grows buffers of its own)."""
+    torch = pytest.importorskip("torch")
+    fn = _noalloc(oakg)
+    xf, Sf, H, y, r = rrsqrt_test_case()
+    c = global_case()
+    cases = [(xf, H @ xf, y, Sf, H @ Sf, r), (c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag)]
+    dev_cases = [_device_case(torch, *a) for a in cases]
+    outs = [_outputs(torch, a) for a in dev_cases]
+    for a in cases:
+        oakg.analysis(*a)
+    for a, o in zip(dev_cases, outs):   # warm-up: the first call also looks up the array
+        _call(oakg, torch, fn, a, o)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for a, o in zip(dev_cases, outs):
+        _call(oakg, torch, fn, a, o)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
