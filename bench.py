@@ -55,12 +55,12 @@ def parse():
     p.add_argument("--no-layout", action="store_true")
     p.add_argument("--no-rows", action="store_true",
                    help="skip the ensemble / SMWCovar / rrsqrt-wrapper section")
-    p.add_argument("--batched-scale", type=float, default=0.25,
-                   help="horizontal scale of the 5-variable N = 100 batched workload "
-                        "(0 skips it)")
-    p.add_argument("--large-scale", type=float, default=0.125,
-                   help="horizontal scale of the 2-variable N = 128 large workload "
-                        "(0 skips it)")
+    p.add_argument("--batched-scale", type=float, default=1.0,
+                   help="horizontal scale of the 5-variable N = 100 batched workload, FP32 "
+                        "storage, generated on the GPU (0 skips it)")
+    p.add_argument("--large-scale", type=float, default=1.0,
+                   help="horizontal scale of the 2-variable N = 128 large workload, FP32 "
+                        "storage, generated on the GPU (0 skips it)")
     return p.parse_args()
 
 
@@ -474,90 +474,27 @@ def main():
             glob["cpu_ms_per_analysis"] = (time.perf_counter() - t0) / 10 * 1e3
             glob["cpu_kind"] = "port (oracle/oakref.c, LAPACK dsyev)"
 
-    # column workloads of the mixed-precision configurations, both forms on the same device
-    # inputs, the mixed form's errors against the FP64 form's outputs:
-    #   batched: 5 variables on 720 x 360 columns of 121 elements, N = 100, bilinear
-    #            observations on track segments (--batched-scale of the grid);
+    # column workloads of the mixed-precision configurations at full size, FP32 storage,
+    # generated on the GPU (column_section): both forms, oracle parity on a zone sample
+    #   batched: 5 variables on 720 x 360 columns of 121 elements, N = 100, 200,000 bilinear
+    #            observations on track segments;
     #   large:   2 variables on 1440 x 720 columns of 100 elements, N = 128, 1M clustered
-    #            observations (--large-scale of the grid), with the adjoint of J = mean over a
-    #            200 x 200 column sub-region (scaled with the grid) of (xa - x_true)^2
-    def two_forms(cb, scale, adjoint_sub=None):
-        bd = (T(cb.zone_size), T(cb.xf), T(cb.Hxf), T(cb.yo), F(cb.Sf), F(cb.HSf),
-              T(cb.r_diag), T(cb.zone_pos), tuple(T(x) for x in cb.obs_pos), T(cb.corr_len),
-              T(cb.max_len))
-
-        def bstep(prec):
-            return oak_gb300.loc_analysis(*bd, weight=cb.weight, metric=cb.metric,
-                                          loctype=cb.loctype, want_ampl=False, precision=prec)
-
-        def timed(fn):
-            for _ in range(args.warmup):
-                o = fn()
-            st = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
-            barrier()
-            torch.cuda.synchronize(dev)
-            b0 = torch.cuda.Event(enable_timing=True)
-            b1 = torch.cuda.Event(enable_timing=True)
-            b0.record(stream)
-            for _ in range(args.steps):
-                o = fn()
-                for k, v in oak_gb300.last_timings().items():
-                    st[k] += v
-            b1.record(stream)
-            torch.cuda.synchronize(dev)
-            barrier()
-            return o, b0.elapsed_time(b1) / args.steps, {k: v / args.steps for k, v in st.items()}
-
-        o64, ms64, st64 = timed(lambda: bstep(oak_gb300.PREC_FP64))
-        xa64, Sa64 = o64[0].clone(), o64[1].clone()
-        bnobs = o64[3].cpu().numpy()
-        del o64
-        om, msm, stm = timed(lambda: bstep(oak_gb300.PREC_MIXED))
-        e_mean = float(torch.linalg.norm(om[0] - xa64) / torch.linalg.norm(xa64 - bd[1]))
-        e_anom = float(torch.linalg.norm(om[1] - Sa64) / torch.linalg.norm(Sa64))
-        del om, Sa64
-        res = {"workload": cb.name, "scale": scale, "zones": int(cb.Z), "N": int(cb.N),
-               "m": int(cb.m), "obs_per_zone_max": int(bnobs.max()),
-               "obs_per_zone_mean": float(bnobs.mean()),
-               "fp64": {"value": ws * cb.Z / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64,
-                        "stage_ms_per_step": st64},
-               "mixed": {"value": ws * cb.Z / (msm / 1e3), "unit": UNIT, "ms_per_step": msm,
-                         "stage_ms_per_step": stm},
-               "speedup_vs_fp64": ms64 / msm, "rel_err_mean_increment": e_mean,
-               "rel_err_anomalies": e_anom,
-               "note": "errors of the mixed form against the FP64 form on the GPU (which "
-                       "matches the oracle to 1e-10); state stored in FP64 at the boundary"}
-        if adjoint_sub is not None:
-            nxb = int(round(1440 * scale))
-            w = max(1, int(round(adjoint_sub * scale)))
-            zc = np.arange(cb.Z)
-            subz = ((zc % nxb) >= nxb // 3) & ((zc % nxb) < nxb // 3 + w) & \
-                   ((zc // nxb) >= w // 2) & ((zc // nxb) < w // 2 + w)
-            sub_d = T(np.repeat(subz, cb.zone_size).astype(np.float64))
-            seed = 2.0 * (xa64 - T(cb.x_true)) * sub_d / float(sub_d.sum())
-            a_args = (bd[0], bd[2], bd[3], bd[4], bd[5], bd[6], bd[7], bd[8], bd[9], bd[10])
-            ga, ams, _ = timed(lambda: oak_gb300.loc_analysis_adjoint(
-                *a_args, seed, inflation=1.05, weight=cb.weight, metric=cb.metric,
-                loctype=cb.loctype))
-            res["adjoint"] = {"ms_per_call": ams, "cost_vs_forward_fp64": ams / ms64,
-                              "cost_vs_forward_mixed": ams / msm,
-                              "zones_seeded": int(subz.sum()),
-                              "cost": f"J = mean over a {w}x{w} column sub-region (all "
-                                      "levels) of (xa - x_true)^2; gradients w.r.t. all yo, r, "
-                                      "the localisation length factor and the prior "
-                                      "inflation 1.05",
-                              "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
-        del xa64, bd
-        return res
-
+    #            observations, with the adjoint of J = mean over a 200 x 200 column sub-region
     batched = None
     if args.batched_scale > 0:
-        from oak_gb300.workloads import batched_case
-        batched = two_forms(batched_case(scale=args.batched_scale), args.batched_scale)
+        from oak_gb300.workloads import batched_case_device
+        dc = batched_case_device(scale=args.batched_scale, device=dev)
+        batched = column_section(torch, dev, stream, args, barrier, ws, dc, args.batched_scale)
+        del dc
+        torch.cuda.empty_cache()
     large = None
     if args.large_scale > 0:
-        from oak_gb300.workloads import large_case
-        large = two_forms(large_case(scale=args.large_scale), args.large_scale, adjoint_sub=200)
+        from oak_gb300.workloads import large_case_device
+        dc = large_case_device(scale=args.large_scale, device=dev)
+        large = column_section(torch, dev, stream, args, barrier, ws, dc, args.large_scale,
+                               adjoint_sub=200)
+        del dc
+        torch.cuda.empty_cache()
 
     # layout builders on one 3-D variable of 720 x 360 x 50 points (x fastest), zones = the
     # 259,200 columns (partition = column number), a land mask, 10^6 observations: zone
@@ -651,6 +588,164 @@ def main():
         "clocks": clk,
     }
     print(json.dumps(line))
+
+
+def column_oracle_sample(dc, nobs, k=96, seed=7):
+    """The oracle on a zone sample of a device workload: the k zones with the most observations
+    and k random zones with observations; inputs are the FP32 arrays widened to FP64, every
+    observation tested (brute-force selection). Returns (zsel, rows, xa, Sa, nobs)."""
+    from oracle import cref
+    rng = np.random.default_rng(seed)
+    act = np.flatnonzero(nobs > 0)
+    top = np.argsort(-nobs, kind="stable")[:k]
+    rnd = rng.choice(act, size=min(k, act.size), replace=False) if act.size else act
+    zsel = np.unique(np.concatenate([top, rnd]))
+    starts = np.concatenate([[0], np.cumsum(dc.zone_size)[:-1]])
+    rows = np.concatenate([np.arange(starts[z], starts[z] + dc.zone_size[z]) for z in zsel])
+    import torch
+    rows_d = torch.as_tensor(rows, device=dc.Sf.device)
+    Sf = dc.Sf[rows_d].double().cpu().numpy()
+    xf = dc.xf[rows_d].double().cpu().numpy()
+    HSf = dc.HSf.double().cpu().numpy()
+    xa, Sa, _, nob = cref.locanalysis(
+        dc.zone_size[zsel], xf, dc.Hxf.double().cpu().numpy(), dc.yo.double().cpu().numpy(),
+        Sf, HSf, dc.r_diag.double().cpu().numpy(), dc.zone_pos[zsel], dc.obs_pos,
+        dc.corr_len[zsel], dc.max_len[zsel], kind=dc.weight, metric=dc.metric,
+        loctype=dc.loctype, nthreads=os.cpu_count() or 1)
+    return zsel, rows, xa, Sa, nob, xf
+
+
+def column_parity(xa_d, Sa_d, nobs_d, ref, zone_size, tol):
+    """Errors of one form's outputs against the oracle sample (see parity_record)."""
+    import torch
+    zsel, rows, xa_o, Sa_o, nobs_o, xf = ref
+    rows_d = torch.as_tensor(rows, device=xa_d.device)
+    xa = xa_d[rows_d].double().cpu().numpy()
+    Sa = Sa_d[rows_d].double().cpu().numpy()
+    nobs = nobs_d.cpu().numpy()[zsel]
+    same = nobs == nobs_o
+    keep = np.repeat(same, zone_size[zsel])
+    inc = max(float(np.linalg.norm(xa_o[keep] - xf[keep])), 1e-300)
+    e_mean = float(np.linalg.norm(xa[keep] - xa_o[keep])) / inc
+    e_anom = float(np.linalg.norm(Sa[keep] - Sa_o[keep]) / max(np.linalg.norm(Sa_o[keep]), 1e-300))
+    return {"zones": int(len(zsel)), "zones_same_selection": int(same.sum()),
+            "obs_per_zone_max_in_sample": int(nobs_o.max()) if len(nobs_o) else 0,
+            "rel_err_mean_increment": e_mean, "rel_err_anomalies": e_anom, "tolerance": tol,
+            "pass": bool(same.all() and e_mean <= tol and e_anom <= tol)}
+
+
+def column_section(torch, dev, stream, args, barrier, ws, dc, scale, adjoint_sub=None):
+    """Both forms on a column workload held on the GPU in FP32 (oakg_locanalysis_f32): the
+    mixed form, then the FP64 form (FP32 inputs widened, FP64 products, outputs rounded to FP32),
+    each checked against the oracle on a zone sample; the mixed form's errors against the FP64
+    form's outputs over every zone; with adjoint_sub, the FP64 adjoint of J = mean over an
+    adjoint_sub^2 column sub-region (scaled with the grid) of (xa - x_true)^2."""
+    import oak_gb300
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    bd = (T(dc.zone_size), dc.xf, dc.Hxf, dc.yo, dc.Sf, dc.HSf, dc.r_diag, T(dc.zone_pos),
+          tuple(T(x) for x in dc.obs_pos), T(dc.corr_len), T(dc.max_len))
+    n, N = dc.n, dc.N
+    xa = torch.empty(n, dtype=torch.float32, device=dev)
+    Sa = torch.empty((N, n), dtype=torch.float32, device=dev).t()
+
+    def bstep(prec):
+        return oak_gb300.loc_analysis(*bd, weight=dc.weight, metric=dc.metric,
+                                      loctype=dc.loctype, want_ampl=False, precision=prec,
+                                      out=(xa, Sa))
+
+    def timed(fn, warm, steps):
+        for _ in range(warm):
+            o = fn()
+        st = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
+        barrier()
+        torch.cuda.synchronize(dev)
+        b0 = torch.cuda.Event(enable_timing=True)
+        b1 = torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        for _ in range(steps):
+            o = fn()
+            for k, v in oak_gb300.last_timings().items():
+                st[k] += v
+        b1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        return o, b0.elapsed_time(b1) / steps, {k: v / steps for k, v in st.items()}
+
+    # the FP64 form costs ~N^3 FP64 flops a zone: bounded warm-up and steps at full size
+    big = dc.Z * N ** 3 > 4e11
+    wm, sm = (2, 3) if big else (args.warmup, args.steps)
+    w64, s64 = (1, 1) if big else (args.warmup, args.steps)
+    om, msm, stm = timed(lambda: bstep(oak_gb300.PREC_MIXED), wm, sm)
+    nobs = om[3].cpu().numpy()
+    ref = column_oracle_sample(dc, nobs)
+    par_m = column_parity(xa, Sa, om[3], ref, dc.zone_size, 1e-4)
+    xam, Sam = xa.clone(), Sa.clone()
+    o64, ms64, st64 = timed(lambda: bstep(oak_gb300.PREC_FP64), w64, s64)
+    # FP64 products, outputs rounded to FP32: the rounding bounds the error against the oracle
+    par_64 = column_parity(xa, Sa, o64[3], ref, dc.zone_size, 1e-5)
+    inc = torch.linalg.norm(xa.double() - dc.xf.double())
+    e_mean = float(torch.linalg.norm(xam.double() - xa.double()) / inc)
+    d2 = s2 = 0.0
+    for k in range(N):  # member by member: FP64 temporaries of one column only
+        a64, m64 = Sa[:, k].double(), Sam[:, k].double()
+        d2 += float(torch.sum((m64 - a64) ** 2))
+        s2 += float(torch.sum(a64 ** 2))
+    e_anom = (d2 / max(s2, 1e-300)) ** 0.5
+    del xam, Sam
+    res = {"workload": dc.name, "scale": scale, "zones": dc.Z, "N": N, "m": dc.m,
+           "storage": "fp32 (oakg_locanalysis_f32)",
+           "obs_per_zone_max": int(nobs.max()), "obs_per_zone_mean": float(nobs.mean()),
+           "mixed": {"value": ws * dc.Z / (msm / 1e3), "unit": UNIT, "ms_per_step": msm,
+                     "warmup": wm, "steps": sm, "stage_ms_per_step": stm,
+                     "parity_oracle_sample": par_m},
+           "fp64": {"value": ws * dc.Z / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64,
+                    "warmup": w64, "steps": s64, "stage_ms_per_step": st64,
+                    "parity_oracle_sample": par_64},
+           "speedup_vs_fp64": ms64 / msm,
+           "mixed_vs_fp64_rel_err_mean_increment": e_mean,
+           "mixed_vs_fp64_rel_err_anomalies": e_anom,
+           "generation": "seeded Gaussian random fields generated on the GPU (torch FFTs, FP32)",
+           "update_bytes_per_step_fp32": int(2 * n * N * 4 + 2 * n * 4)}
+    if adjoint_sub is not None:
+        res["adjoint"] = column_adjoint(torch, dev, stream, dc, xa, scale, adjoint_sub, ms64,
+                                        msm, timed)
+    del xa, Sa, bd
+    return res
+
+
+def column_adjoint(torch, dev, stream, dc, xa, scale, sub, ms64, msm, timed):
+    """The FP64 adjoint of J = mean over a sub x sub column sub-region of (xa - x_true)^2. Only
+    the zones of the sub-region have a non-zero seed; zones are independent, so the adjoint
+    runs on the sub-problem of those zones (their rows of Sf, all observations), widened to
+    FP64, which gives the same gradients as the whole state."""
+    import oak_gb300
+    nx = dc.nx
+    w = max(1, int(round(sub * scale)))
+    zc = np.arange(dc.Z)
+    subz = ((zc % nx) >= nx // 3) & ((zc % nx) < nx // 3 + w) & \
+           ((zc // nx) >= w // 2) & ((zc // nx) < w // 2 + w)
+    zsel = np.flatnonzero(subz)
+    starts = np.concatenate([[0], np.cumsum(dc.zone_size)[:-1]])
+    rows = np.concatenate([np.arange(starts[z], starts[z] + dc.zone_size[z]) for z in zsel])
+    rows_d = torch.as_tensor(rows, device=dev)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)
+    Sf_sub = dc.Sf[rows_d].double().t().contiguous().t()
+    HSf = dc.HSf.double().t().contiguous().t()
+    seed = 2.0 * (xa[rows_d].double() - dc.x_true[rows_d].double()) / float(rows.size)
+    a_args = (T(dc.zone_size[zsel]), dc.Hxf.double(), dc.yo.double(), Sf_sub, HSf,
+              dc.r_diag.double(), T(dc.zone_pos[zsel]), tuple(T(x) for x in dc.obs_pos),
+              T(dc.corr_len[zsel]), T(dc.max_len[zsel]))
+    ga, ams, _ = timed(lambda: oak_gb300.loc_analysis_adjoint(
+        *a_args, seed, inflation=1.05, weight=dc.weight, metric=dc.metric,
+        loctype=dc.loctype), 2, 3)
+    return {"ms_per_call": ams, "cost_vs_forward_fp64": ams / ms64,
+            "cost_vs_forward_mixed": ams / msm, "zones_seeded": int(zsel.size),
+            "cost": f"J = mean over a {w}x{w} column sub-region (all levels) of "
+                    "(xa - x_true)^2 at the FP64 analysis; gradients w.r.t. all yo, r, the "
+                    "localisation length factor and the prior inflation 1.05; run on the "
+                    "sub-region's zones (FP64 copies of their rows), which the seed confines "
+                    "the adjoint to",
+            "dJ_dlen": ga[2], "dJ_dinfl": ga[3]}
 
 
 def layout_section(torch, dev, stream, args, barrier):

@@ -8,6 +8,7 @@
 !   gpu_analysis     <- analysis(xf,Hxf,yo,Sf,HSf,R,xa,Sa,amplitudes)      rrsqrt.F90:196-208
 !   gpu_locAnalysis  <- locAnalysis(zoneSize,selectObservations,xf,Hxf,yo,Sf,HSf,R,xa,Sa,
 !                                   amplitudes,localise_obs)                rrsqrt.F90:433-466
+!   gpu_locAnalysis_r4  <- the same for the reference's single-precision build (real(4))
 !   gpu_locAnalysis_adjoint  gradients of a cost of the analysis mean (no reference
 !                            counterpart: the reference has no derivative code)
 !
@@ -19,7 +20,8 @@
 !     the coordinates of each zone's first element, the observation coordinates and the
 !     correlation / maximum lengths, with the weight kind, metric and loctype of
 !     selectObservations (assimilation.F90:3683-3771).
-!   - real is real(c_double) (the reference's PRECISION=double build, -fdefault-real-8).
+!   - real is real(c_double) (the reference's PRECISION=double build, -fdefault-real-8), or
+!     real(c_float) in gpu_locAnalysis_r4 (PRECISION=single).
 !   - A non-zero status stops the program with the library's message, as the reference stops
 !     on errors (ERROR_STOP, ppdef.h:22); the bind(C) interfaces return the status instead.
 !   - Call the wrappers from one thread (inside !$omp master, then !$omp barrier, where the
@@ -122,6 +124,23 @@ module oakg
       real(c_double), intent(out), optional :: Sa(*), ampl(*)
       integer(c_int32_t), intent(out), optional :: nobs(*)
     end function oakg_locanalysis
+
+    integer(c_int) function oakg_locanalysis_f32(dims, loc, nzones, zone_size, xf, Hxf, yo, &
+         Sf, HSf, r_diag, zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, xa, Sa, &
+         ampl, nobs) bind(C, name="oakg_locanalysis_f32")
+      import
+      type(oakg_dims), intent(in) :: dims
+      type(oakg_loc), intent(in) :: loc
+      integer(c_int32_t), value :: nzones
+      integer(c_int32_t), intent(in) :: zone_size(*)
+      real(c_float), intent(in) :: xf(*), Hxf(*), yo(*), Sf(*), HSf(*), r_diag(*)
+      real(c_double), intent(in) :: zone_xyzt(*)
+      real(c_double), intent(in), optional :: obs_x(*), obs_y(*), obs_z(*), obs_t(*)
+      real(c_double), intent(in) :: corr_len(*), max_len(*)
+      real(c_float), intent(out) :: xa(*)
+      real(c_float), intent(out), optional :: Sa(*), ampl(*)
+      integer(c_int32_t), intent(out), optional :: nobs(*)
+    end function oakg_locanalysis_f32
 
     integer(c_int) function oakg_locanalysis_adjoint(dims, loc, nzones, zone_size, Hxf, yo, &
          Sf, HSf, r_diag, zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &
@@ -519,6 +538,36 @@ contains
          geometry%obs_t, geometry%corr_len, geometry%max_len, xa, Sa, amplitudes), &
          'gpu_locAnalysis')
   end subroutine gpu_locAnalysis
+
+  ! gpu_locAnalysis for the reference's single-precision build (PRECISION=single: real is
+  ! real(4)); the geometry stays real(c_double).
+  subroutine gpu_locAnalysis_r4(zoneSize, geometry, xf, Hxf, yo, Sf, HSf, R, xa, Sa, &
+       amplitudes, localise_obs)
+    integer(c_int32_t), intent(in) :: zoneSize(:)
+    type(oakg_geometry), intent(in) :: geometry
+    real(c_float), intent(in) :: xf(:), Hxf(:), yo(:), R(:)
+    real(c_float), intent(in), contiguous :: Sf(:,:), HSf(:,:)
+    real(c_float), intent(out) :: xa(:)
+    real(c_float), intent(out), optional, contiguous :: Sa(:,:), amplitudes(:,:)
+    logical, intent(in), optional :: localise_obs
+    type(oakg_dims) :: dims
+    type(oakg_loc) :: loc
+    dims%n = size(xf)
+    dims%nens = size(Sf, 2)
+    dims%m = size(yo)
+    dims%ldS = size(Sf, 1)
+    dims%ldH = max(size(HSf, 1), 1)
+    dims%mem = OAKG_MEM_HOST
+    loc = geometry%loc
+    loc%localise_obs = 1
+    if (present(localise_obs)) then
+      if (.not. localise_obs) loc%localise_obs = 0
+    end if
+    call check(oakg_locanalysis_f32(dims, loc, int(size(zoneSize), c_int32_t), zoneSize, xf, &
+         Hxf, yo, Sf, HSf, R, geometry%zone_xyzt, geometry%obs_x, geometry%obs_y, &
+         geometry%obs_z, geometry%obs_t, geometry%corr_len, geometry%max_len, xa, Sa, &
+         amplitudes), 'gpu_locAnalysis_r4')
+  end subroutine gpu_locAnalysis_r4
 
   ! Gradients of a cost J(xa) of gpu_locAnalysis's mean, given dJ/dxa: with respect to the
   ! observations (dJ_dyo), their error variances (dJ_dr), a common factor on the correlation

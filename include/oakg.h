@@ -129,6 +129,21 @@ int oakg_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
                      const double* corr_len, const double* max_len, double* xa, double* Sa,
                      double* ampl, int32_t* nobs);
 
+/* locAnalysis of the reference's single-precision build (PRECISION = single,
+ * config.mk.template:17: real is real(4)): oakg_locanalysis with the state and observation
+ * arrays xf, Hxf, yo, Sf, HSf, r_diag, xa, Sa and ampl in FP32 (real(c_float)); the geometry
+ * (zone_xyzt, obs_*, corr_len, max_len) stays double, so the selection decisions are those of
+ * oakg_locanalysis. Both precision modes: OAKG_PREC_FP64 widens the FP32 inputs and computes
+ * in FP64 (rounding only the outputs); OAKG_PREC_MIXED reads and writes FP32 directly, half
+ * the state bytes of the FP64 arrays. */
+int oakg_locanalysis_f32(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                         const int32_t* zone_size, const float* xf, const float* Hxf,
+                         const float* yo, const float* Sf, const float* HSf, const float* r_diag,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, float* xa, float* Sa, float* ampl,
+                         int32_t* nobs);
+
 /* Adjoint of the local analysis mean -- no counterpart in the reference (it has no derivative
  * code). For a scalar cost J(xa) given by its gradient dJ_dxa(n) at the analysis of
  * oakg_locanalysis with the same inputs, where the prior anomalies are inflated by

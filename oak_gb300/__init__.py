@@ -89,6 +89,8 @@ def lib() -> ctypes.CDLL:
     L.oakg_analysis.restype = ctypes.c_int
     L.oakg_locanalysis.argtypes = [ctypes.POINTER(Dims), ctypes.POINTER(Loc), ctypes.c_int32] + [P] * 18
     L.oakg_locanalysis.restype = ctypes.c_int
+    L.oakg_locanalysis_f32.argtypes = L.oakg_locanalysis.argtypes
+    L.oakg_locanalysis_f32.restype = ctypes.c_int
     L.oakg_locanalysis_smw.argtypes = ([ctypes.POINTER(Dims), ctypes.POINTER(Loc),
                                         ctypes.c_int32] + [P] * 7 + [ctypes.c_int32, P,
                                                                      ctypes.c_int64] + [P] * 11)
@@ -235,19 +237,19 @@ class _Args:
         self.keep.append(arr)
         return ctypes.c_void_p(arr.ctypes.data)
 
-    def mat(self, a, rows, cols, name):
+    def mat(self, a, rows, cols, name, dtype=np.float64):
         """Column-major (rows, cols) matrix; returns (pointer, leading dimension)."""
         if self.device:
             if not (_is_torch(a) and a.is_cuda):
                 raise OakError(ERR_ARGS, f"{name}: expected a CUDA tensor")
-            import torch
-            if a.dtype != torch.float64 or tuple(a.shape) != (rows, cols):
-                raise OakError(ERR_ARGS, f"{name}: expected float64 of shape ({rows}, {cols})")
+            tdt = _torch_dtype(dtype)
+            if a.dtype != tdt or tuple(a.shape) != (rows, cols):
+                raise OakError(ERR_ARGS, f"{name}: expected {tdt} of shape ({rows}, {cols})")
             if a.stride(0) != 1 or (cols > 1 and a.stride(1) < rows):
                 raise OakError(ERR_ARGS, f"{name}: expected column-major strides (1, ld>=rows)")
             self.keep.append(a)
             return ctypes.c_void_p(a.data_ptr()), (a.stride(1) if cols > 1 else rows)
-        arr = np.asfortranarray(np.asarray(a, dtype=np.float64))
+        arr = np.asfortranarray(np.asarray(a, dtype=dtype))
         if arr.shape != (rows, cols):
             raise OakError(ERR_ARGS, f"{name}: expected shape ({rows}, {cols}), got {arr.shape}")
         self.keep.append(arr)
@@ -256,8 +258,17 @@ class _Args:
 
 def _torch_dtype(dtype):
     import torch
-    return {np.dtype(np.float64): torch.float64, np.dtype(np.int32): torch.int32,
-            np.dtype(np.int64): torch.int64, np.dtype(np.uint8): torch.uint8}[np.dtype(dtype)]
+    return {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
+            np.dtype(np.int32): torch.int32, np.dtype(np.int64): torch.int64,
+            np.dtype(np.uint8): torch.uint8}[np.dtype(dtype)]
+
+
+def _is_float32(a) -> bool:
+    """True for a float32 array or tensor (FP32 storage at the boundary)."""
+    if _is_torch(a):
+        import torch
+        return a.dtype == torch.float32
+    return np.asarray(a).dtype == np.float32
 
 
 def _device_mode(*arrays) -> bool:
@@ -346,6 +357,10 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     arrays). ``precision``: PREC_FP64 (plain form) or PREC_MIXED (FP32 Gram, eigensolve and
     update; FP64 selection and eigenvalue scalings). ``smw_B`` (m x k): the observation error
     covariance R = diag(r_diag) + B B^T (SMWCovar, covariance.F90:464-570; FP64 form).
+
+    A float32 ``Sf`` selects FP32 storage at the boundary (oakg_locanalysis_f32): xf, Hxf, yo,
+    HSf, r_diag are then taken, and xa, Sa, amplitudes returned, in float32; the geometry
+    stays float64.
     """
     Z = int(zone_size.shape[0])
     n = int(xf.shape[0])
@@ -354,9 +369,13 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     ox, oy, oz, ot = (tuple(obs_pos) + (None,) * 4)[:4]
     device = _device_mode(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, corr_len, max_len,
                           ox, oy, oz, ot)
+    f32 = _is_float32(Sf)
+    fdt = np.float32 if f32 else np.float64
+    if f32 and smw_B is not None:
+        raise OakError(ERR_ARGS, "the SMWCovar form takes float64 arrays")
     A = _Args(device)
-    pSf, ldS = A.mat(Sf, n, N, "Sf")
-    pHS, ldH = A.mat(HSf, m, N, "HSf")
+    pSf, ldS = A.mat(Sf, n, N, "Sf", fdt)
+    pHS, ldH = A.mat(HSf, m, N, "HSf", fdt)
     dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
     flags = (FLAG_AMPL_ALWAYS if ampl_always else 0) | (FLAG_BRUTE_SEARCH if brute_search else 0)
     loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
@@ -370,13 +389,29 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     if out is not None:
         xa, Sa = out
     else:
-        xa = _empty_like_mode(device, (n,), like=like)
-        Sa = _empty_like_mode(device, (n, N), order="F", like=like) if want_sa else None
+        xa = _empty_like_mode(device, (n,), dtype=fdt, like=like)
+        Sa = (_empty_like_mode(device, (n, N), dtype=fdt, order="F", like=like) if want_sa
+              else None)
     if device and want_sa and ldS != n:
         raise OakError(ERR_ARGS, "device Sf with ld != n is not supported by this wrapper")
-    ampl = _empty_like_mode(device, (N, Z), order="F", like=like) if want_ampl else None
+    ampl = (_empty_like_mode(device, (N, Z), dtype=fdt, order="F", like=like) if want_ampl
+            else None)
     nobs = _empty_like_mode(device, (Z,), dtype=np.int32, like=like)
     _sync_torch(device, like)
+    if f32:
+        rc = lib().oakg_locanalysis_f32(
+            ctypes.byref(dims), ctypes.byref(loc), Z, A.vec(zone_size, np.int32, "zone_size", Z),
+            A.vec(xf, fdt, n=n, name="xf"), A.vec(Hxf, fdt, n=m, name="Hxf"),
+            A.vec(yo, fdt, n=m, name="yo"), pSf, pHS, A.vec(r_diag, fdt, n=m, name="r_diag"),
+            A.vec(zp, n=4 * Z, name="zone_pos"), A.vec(ox, n=m, name="obs_x"),
+            A.vec(oy, n=m, name="obs_y"), A.vec(oz, n=m, name="obs_z"),
+            A.vec(ot, n=m, name="obs_t"), A.vec(corr_len, n=Z, name="corr_len"),
+            A.vec(max_len, n=Z, name="max_len"), A.vec(xa, fdt, name="xa"),
+            None if Sa is None else A.mat(Sa, n, N, "Sa", fdt)[0],
+            None if ampl is None else A.mat(ampl, N, Z, "ampl", fdt)[0],
+            A.vec(nobs, np.int32, "nobs"))
+        _check(rc)
+        return xa, Sa, ampl, nobs
     if smw_B is not None:
         k = int(smw_B.shape[1])
         pB, ldB = A.mat(smw_B, m, k, "B")

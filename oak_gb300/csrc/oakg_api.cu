@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "oakg_internal.cuh"
@@ -73,7 +74,7 @@ enum BufId {
   B_ORDER, B_C_E, B_C_MEAN, B_C_S, B_C_OM, B_C_EO, B_C_HE, B_C_HXF, B_C_HSF, B_C_XA, B_C_SA,
   B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_SMWB, B_HSTA, B_GAUG,
   B_GVAUG, B_GLOB, B_L_PART, B_L_WORK, B_L_ZS, B_L_ZI, B_L_INV, B_L_X, B_L_Y, B_L_IDX, B_L_MASK,
-  B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_COUNT_
+  B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_HXF64, B_YO64, B_R64, B_COUNT_
 };
 
 struct Ctx {
@@ -259,6 +260,11 @@ struct ChunkArgs {
   const double *xf, *Sf;
   double *xa, *Sa, *ampl;
   int32_t* nobs;
+  // FP32 storage at the boundary (oakg_locanalysis_f32): these state arrays replace the five
+  // above, which are then null
+  bool store32 = false;
+  const float *xf32 = nullptr, *Sf32 = nullptr;
+  float *xa32 = nullptr, *Sa32 = nullptr, *ampl32 = nullptr;
   // optional pick order of the selection + Gram stage (chunk-local zone indices, Z entries)
   const int32_t* zorder = nullptr;
   // SMWCovar R = diag(r) + B B^T (FP64 form): k columns of B and the augmented cell-sorted
@@ -266,10 +272,11 @@ struct ChunkArgs {
   int smw_k = 0;
   const double* hst_aug = nullptr;
   // host-memory pipeline: Sf (host) rows of each chunk copied into a.Sf on a copy stream, the
-  // chunk's Sa / xa rows copied back to the host after its update (rows < n only)
-  const double* sf_host = nullptr;
-  double* sa_host = nullptr;
-  double* xa_host = nullptr;
+  // chunk's Sa / xa rows copied back to the host after its update (rows < n only); elements
+  // are those of the state (double, or float with store32)
+  const void* sf_host = nullptr;
+  void* sa_host = nullptr;
+  void* xa_host = nullptr;
   const int64_t* zstart_host = nullptr;  // Z + 1 row offsets
 };
 
@@ -338,7 +345,18 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
         for (cudaEvent_t ev : *p) cudaEventDestroy(ev);
     }
   } guard{{&ev_in, &ev_out}};
-  const size_t pitch = (size_t)a.ldS * sizeof(double);
+  const size_t esz = a.store32 ? sizeof(float) : sizeof(double);
+  const size_t pitch = (size_t)a.ldS * esz;
+  char* dSf = a.store32 ? (char*)const_cast<float*>(a.Sf32) : (char*)const_cast<double*>(a.Sf);
+  char* dSa = a.store32 ? (char*)a.Sa32 : (char*)a.Sa;
+  char* dxa = a.store32 ? (char*)a.xa32 : (char*)a.xa;
+  // the update of zones [zz0, zz0 + nq) (T and amplitudes at the chunk-local slot)
+  auto update = [&](int32_t zz0, int32_t nq, const R* T, const R* za, const int32_t* nb) {
+    return a.store32 ? K::update(N, zz0, nq, a.zstart, a.zone_max, a.xf32, a.Sf32, a.ldS, T, za,
+                                 nb, a.xa32, a.Sa32, st)
+                     : K::update(N, zz0, nq, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, T, za, nb,
+                                 a.xa, a.Sa, st);
+  };
   if (pipe) {
     if ((rc = copy_streams(c))) return rc;
     ev_in.resize(nchunks);
@@ -352,8 +370,8 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
       const int64_t r0 = a.zstart_host[q * chunk],
                     r1 = a.zstart_host[std::min<int64_t>((q + 1) * chunk, a.Z)];
       if (r1 > r0 &&
-          (e = cudaMemcpy2DAsync(const_cast<double*>(a.Sf) + r0, pitch, a.sf_host + r0, pitch,
-                                 (size_t)(r1 - r0) * sizeof(double), N, cudaMemcpyHostToDevice,
+          (e = cudaMemcpy2DAsync(dSf + r0 * esz, pitch, (const char*)a.sf_host + r0 * esz, pitch,
+                                 (size_t)(r1 - r0) * esz, N, cudaMemcpyHostToDevice,
                                  c->copy_in)) != cudaSuccess)
         return cuda_fail(e, "H2D Sf rows");
       cudaEventRecord(ev_in[q], c->copy_in);
@@ -393,8 +411,7 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
     if (timed) cudaEventRecord(c->ev[4], st);
     if (!pipe) {
-      e = K::update(N, (int32_t)z0, nzc, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, (const R*)d_G,
-                    (const R*)d_za, (const int32_t*)(a.nobs + z0), a.xa, a.Sa, st);
+      e = update((int32_t)z0, nzc, (const R*)d_G, (const R*)d_za, (const int32_t*)(a.nobs + z0));
       if (e != cudaSuccess) return cuda_fail(e, "update kernel");
     } else {
       // host memory: the update in kOutPieces zone ranges, each range's Sa / xa rows copied
@@ -403,9 +420,8 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
       const int32_t per = (nzc + kOutPieces - 1) / kOutPieces;
       for (int32_t q0 = 0; q0 < nzc; q0 += per) {
         const int32_t nq = std::min(per, nzc - q0);
-        e = K::update(N, (int32_t)(z0 + q0), nq, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS,
-                      (const R*)d_G + (size_t)q0 * N * N, (const R*)d_za + (size_t)q0 * N,
-                      (const int32_t*)(a.nobs + z0 + q0), a.xa, a.Sa, st);
+        e = update((int32_t)(z0 + q0), nq, (const R*)d_G + (size_t)q0 * N * N,
+                   (const R*)d_za + (size_t)q0 * N, (const int32_t*)(a.nobs + z0 + q0));
         if (e != cudaSuccess) return cuda_fail(e, "update kernel");
         const int64_t r0 = a.zstart_host[z0 + q0], r1 = a.zstart_host[z0 + q0 + nq];
         cudaEvent_t evp = ev_out[(z0 / chunk) * kOutPieces + q0 / per];
@@ -413,12 +429,12 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
         cudaStreamWaitEvent(c->copy_out, evp, 0);
         if (r1 > r0) {
           if (a.sa_host &&
-              (e = cudaMemcpy2DAsync(a.sa_host + r0, pitch, a.Sa + r0, pitch,
-                                     (size_t)(r1 - r0) * sizeof(double), N,
-                                     cudaMemcpyDeviceToHost, c->copy_out)) != cudaSuccess)
+              (e = cudaMemcpy2DAsync((char*)a.sa_host + r0 * esz, pitch, dSa + r0 * esz, pitch,
+                                     (size_t)(r1 - r0) * esz, N, cudaMemcpyDeviceToHost,
+                                     c->copy_out)) != cudaSuccess)
             return cuda_fail(e, "D2H Sa rows");
-          if ((e = cudaMemcpyAsync(a.xa_host + r0, a.xa + r0,
-                                   (size_t)(r1 - r0) * sizeof(double), cudaMemcpyDeviceToHost,
+          if ((e = cudaMemcpyAsync((char*)a.xa_host + r0 * esz, dxa + r0 * esz,
+                                   (size_t)(r1 - r0) * esz, cudaMemcpyDeviceToHost,
                                    c->copy_out)) != cudaSuccess)
             return cuda_fail(e, "D2H xa rows");
         }
@@ -428,6 +444,10 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     if (a.ampl) {
       e = K::ampl(N, (int32_t)z0, nzc, (const R*)d_za, (const int32_t*)(a.nobs + z0), a.all_ampl,
                   a.ampl, st);
+      if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
+    } else if (a.ampl32) {
+      e = K::ampl(N, (int32_t)z0, nzc, (const R*)d_za, (const int32_t*)(a.nobs + z0), a.all_ampl,
+                  a.ampl32, st);
       if (e != cudaSuccess) return cuda_fail(e, "amplitudes");
     }
     k_or_status<<<64, 256, 0, st>>>(d_status, nzc, *status_all);
@@ -451,6 +471,9 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
 struct Prep {
   const int32_t* zsize;
   const double *xf, *Hxf, *yo, *r, *Sf, *HSf, *zxyzt, *u, *v, *corr, *maxl;
+  // FP32 storage at the boundary: the state and HSf in FP32 (xf, Sf, HSf above are null);
+  // Hxf, yo and r are widened to FP64 copies
+  const float *xf32, *Sf32, *HSf32;
   int64_t* zstart;
   int32_t zone_max;
   int brute;
@@ -501,7 +524,8 @@ int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH,
     if ((rc = scratch(c, B_SINNOV, (size_t)m, &d_sinnov, "obs"))) return rc;
     if ((rc = scratch(c, B_SR, (size_t)m, &d_sr, "obs"))) return rc;
     if ((rc = scratch(c, B_HST, (size_t)m * N, &d_hst, "obs rows"))) return rc;
-    e = obs_bin_and_sort(g, m, N, P->u, P->v, P->yo, P->Hxf, P->r, P->HSf, ldH, d_cell, d_count,
+    e = obs_bin_and_sort(g, m, N, P->u, P->v, P->yo, P->Hxf, P->r, P->HSf, P->HSf32, ldH,
+                         d_cell, d_count,
                          d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr, d_hst, st);
     if (e != cudaSuccess) return cuda_fail(e, "observation binning");
     so.u = d_su;
@@ -534,12 +558,34 @@ int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH,
   return OAKG_OK;
 }
 
+// Stages an m-vector of observation values as FP64 (a widened copy when S = float).
+template <typename S>
+int stage_obs_vec(Ctx* c, BufId id, BufId id64, const S* src, int64_t m, int mem,
+                  const double** out, const char* name) {
+  if constexpr (std::is_same<S, double>::value) {
+    (void)id64;
+    return stage_in(c, id, src, (size_t)m, mem, out, name);
+  } else {
+    const float* d_src;
+    double* d_out;
+    int rc;
+    if ((rc = stage_in(c, id, src, (size_t)m, mem, &d_src, name))) return rc;
+    if ((rc = scratch(c, id64, (size_t)m, &d_out, name))) return rc;
+    cudaError_t e = rows_to_fp64(d_src, d_out, m, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, name);
+    *out = d_out;
+    return OAKG_OK;
+  }
+}
+
+template <typename S>
 int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
-                const int32_t* zone_size, const double* xf, const double* Hxf,
-                const double* yo, const double* Sf, const double* HSf, const double* r_diag,
-                const double* zone_xyzt, const double* obs_x, const double* obs_y,
-                const double* obs_z, const double* obs_t, const double* corr_len,
-                const double* max_len, Prep* P, bool defer_sf = false) {
+                const int32_t* zone_size, const S* xf, const S* Hxf, const S* yo, const S* Sf,
+                const S* HSf, const S* r_diag, const double* zone_xyzt, const double* obs_x,
+                const double* obs_y, const double* obs_z, const double* obs_t,
+                const double* corr_len, const double* max_len, Prep* P,
+                bool defer_sf = false) {
+  constexpr bool f32 = std::is_same<S, float>::value;
   const int64_t n = dims->n, m = dims->m, ldS = dims->ldS, ldH = dims->ldH;
   const int N = dims->N, mem = dims->mem;
   int rc;
@@ -556,23 +602,35 @@ int prepare_loc(Ctx* c, const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   cudaError_t e;
   *P = Prep{};
   if ((rc = stage_in(c, B_ZONE_SIZE, zone_size, (size_t)Z, mem, &P->zsize, "zone_size"))) return rc;
-  if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &P->xf, "xf"))) return rc;
+  const S *d_xf = nullptr, *d_Sf = nullptr, *d_HSf = nullptr;
+  if ((rc = stage_in(c, B_XF, xf, (size_t)n, mem, &d_xf, "xf"))) return rc;
   if (defer_sf && mem == OAKG_MEM_HOST) {
     // host-memory pipeline: the rows are copied per zone chunk by run_chunks
-    double* d_sf;
+    S* d_sf;
     if ((rc = scratch(c, B_SF, (size_t)ldS * N, &d_sf, "Sf"))) return rc;
-    P->Sf = d_sf;
-  } else if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &P->Sf, "Sf"))) {
+    d_Sf = d_sf;
+  } else if ((rc = stage_in(c, B_SF, Sf, (size_t)ldS * N, mem, &d_Sf, "Sf"))) {
     return rc;
+  }
+  if constexpr (f32) {
+    P->xf32 = d_xf;
+    P->Sf32 = d_Sf;
+  } else {
+    P->xf = d_xf;
+    P->Sf = d_Sf;
   }
   if ((rc = stage_in(c, B_ZXYZT, zone_xyzt, (size_t)4 * Z, mem, &P->zxyzt, "zone_xyzt"))) return rc;
   if ((rc = stage_in(c, B_CORR, corr_len, (size_t)Z, mem, &P->corr, "corr_len"))) return rc;
   if ((rc = stage_in(c, B_MAXL, max_len, (size_t)Z, mem, &P->maxl, "max_len"))) return rc;
   if (m > 0) {
-    if ((rc = stage_in(c, B_HXF, Hxf, (size_t)m, mem, &P->Hxf, "Hxf"))) return rc;
-    if ((rc = stage_in(c, B_YO, yo, (size_t)m, mem, &P->yo, "yo"))) return rc;
-    if ((rc = stage_in(c, B_R, r_diag, (size_t)m, mem, &P->r, "r_diag"))) return rc;
-    if ((rc = stage_in(c, B_HSF, HSf, (size_t)ldH * N, mem, &P->HSf, "HSf"))) return rc;
+    if ((rc = stage_obs_vec(c, B_HXF, B_HXF64, Hxf, m, mem, &P->Hxf, "Hxf"))) return rc;
+    if ((rc = stage_obs_vec(c, B_YO, B_YO64, yo, m, mem, &P->yo, "yo"))) return rc;
+    if ((rc = stage_obs_vec(c, B_R, B_R64, r_diag, m, mem, &P->r, "r_diag"))) return rc;
+    if ((rc = stage_in(c, B_HSF, HSf, (size_t)ldH * N, mem, &d_HSf, "HSf"))) return rc;
+    if constexpr (f32)
+      P->HSf32 = d_HSf;
+    else
+      P->HSf = d_HSf;
     if ((rc = stage_in(c, B_OX, u_src_h, (size_t)m, mem, &P->u, "obs coordinate u"))) return rc;
     if (v_src_h && (rc = stage_in(c, B_OY, v_src_h, (size_t)m, mem, &P->v, "obs coordinate v")))
       return rc;
@@ -650,15 +708,19 @@ struct SmwArg {
   int64_t ldB = 0;
 };
 
+// S: element type of the state and observation arrays at the boundary (double, or float for
+// oakg_locanalysis_f32); the geometry is double either way.
+template <typename S>
 int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
-                     const int32_t* zone_size, const double* xf, const double* Hxf,
-                     const double* yo, const double* Sf, const double* HSf,
-                     const double* r_diag, const double* zone_xyzt, const double* obs_x,
-                     const double* obs_y, const double* obs_z, const double* obs_t,
-                     const double* corr_len, const double* max_len, double* xa, double* Sa,
-                     double* ampl, int32_t* nobs_out, const SmwArg* smw = nullptr) {
+                     const int32_t* zone_size, const S* xf, const S* Hxf, const S* yo,
+                     const S* Sf, const S* HSf, const S* r_diag, const double* zone_xyzt,
+                     const double* obs_x, const double* obs_y, const double* obs_z,
+                     const double* obs_t, const double* corr_len, const double* max_len, S* xa,
+                     S* Sa, S* ampl, int32_t* nobs_out, const SmwArg* smw = nullptr) {
+  constexpr bool f32 = std::is_same<S, float>::value;
   int rc = check_loc(dims, loc, Z);
   if (rc) return rc;
+  if (f32 && smw) return fail(OAKG_ERR_ARGS, "the SMWCovar form takes FP64 arrays");
   if (!xf || !xa) return fail(OAKG_ERR_ARGS, "xf and xa are required");
   const int smw_k = (smw && dims->m > 0) ? smw->k : 0;
   if (smw) {
@@ -690,7 +752,7 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   if ((rc = prepare_loc(c, dims, loc, Z, zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
                         obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &P, pipe)))
     return rc;
-  double *d_xa, *d_Sa, *d_ampl;
+  S *d_xa, *d_Sa, *d_ampl;
   int32_t* d_nobs;
   if ((rc = stage_out(c, B_XA, xa, (size_t)n, mem, &d_xa, "xa"))) return rc;
   if ((rc = stage_out(c, B_SA, Sa, (size_t)ldS * N, mem, &d_Sa, "Sa"))) return rc;
@@ -702,8 +764,8 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   }
   if (mem == OAKG_MEM_HOST && Sa && !pipe) {
     // rows beyond n (ldS > n) are returned unchanged
-    e = cudaMemcpyAsync(d_Sa, P.Sf, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToDevice,
-                        st);
+    const void* d_Sf = f32 ? (const void*)P.Sf32 : (const void*)P.Sf;
+    e = cudaMemcpyAsync(d_Sa, d_Sf, (size_t)ldS * N * sizeof(S), cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "Sa init");
   }
   cudaEventRecord(c->ev[1], st);
@@ -714,14 +776,28 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
   const int all_ampl = (!loc->localise_obs) || (loc->flags & OAKG_FLAG_AMPL_ALWAYS);
   int32_t* d_status_all = nullptr;
   ChunkArgs ca{P.g, P.so, lp, Z, N, ldS, P.zone_max, P.brute, all_ampl, P.zxyzt, P.corr, P.maxl,
-               P.zstart, P.xf, P.Sf, d_xa, d_Sa, d_ampl, d_nobs};
+               P.zstart, nullptr, nullptr, nullptr, nullptr, nullptr, d_nobs};
+  if constexpr (f32) {
+    ca.store32 = true;
+    ca.xf32 = P.xf32;
+    ca.Sf32 = P.Sf32;
+    ca.xa32 = d_xa;
+    ca.Sa32 = d_Sa;
+    ca.ampl32 = d_ampl;
+  } else {
+    ca.xf = P.xf;
+    ca.Sf = P.Sf;
+    ca.xa = d_xa;
+    ca.Sa = d_Sa;
+    ca.ampl = d_ampl;
+  }
   if (pipe) {
     ca.sf_host = Sf;
     ca.sa_host = Sa;
     ca.xa_host = xa;
     ca.zstart_host = zstart_h.data();
   }
-  if (smw_k > 0) {
+  if constexpr (!f32) if (smw_k > 0) {
     // the augmented cell-sorted rows [HS_q | B_q] of the SMWCovar products
     const int64_t m = dims->m;
     const double* dB;
@@ -746,13 +822,13 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
       cudaSuccess)
     return cuda_fail(e, "D2H");
   if (mem == OAKG_MEM_HOST) {
-    if (!pipe && (e = cudaMemcpyAsync(xa, d_xa, n * sizeof(double), cudaMemcpyDeviceToHost, st)))
+    if (!pipe && (e = cudaMemcpyAsync(xa, d_xa, n * sizeof(S), cudaMemcpyDeviceToHost, st)))
       return cuda_fail(e, "D2H xa");
     if (Sa && !pipe &&
-        (e = cudaMemcpyAsync(Sa, d_Sa, (size_t)ldS * N * sizeof(double), cudaMemcpyDeviceToHost,
+        (e = cudaMemcpyAsync(Sa, d_Sa, (size_t)ldS * N * sizeof(S), cudaMemcpyDeviceToHost,
                              st)))
       return cuda_fail(e, "D2H Sa");
-    if (ampl && (e = cudaMemcpyAsync(ampl, d_ampl, (size_t)N * Z * sizeof(double),
+    if (ampl && (e = cudaMemcpyAsync(ampl, d_ampl, (size_t)N * Z * sizeof(S),
                                      cudaMemcpyDeviceToHost, st)))
       return cuda_fail(e, "D2H amplitudes");
     if (nobs_out && (e = cudaMemcpyAsync(nobs_out, d_nobs, (size_t)Z * sizeof(int32_t),
@@ -790,7 +866,8 @@ int adjoint_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z, const in
   cudaError_t e;
   cudaEventRecord(c->ev[0], st);
   Prep P;
-  if ((rc = prepare_loc(c, dims, loc, Z, zone_size, nullptr, Hxf, yo, Sf, HSf, r_diag, zone_xyzt,
+  if ((rc = prepare_loc<double>(c, dims, loc, Z, zone_size, nullptr, Hxf, yo, Sf, HSf, r_diag,
+                               zone_xyzt,
                         obs_x, obs_y, obs_z, obs_t, corr_len, max_len, &P)))
     return rc;
   const double* d_seed;
@@ -1381,7 +1458,7 @@ int ens_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
   if ((rc = scratch(c, B_E_XA, (size_t)n, &xa, "xa")) ||
       (rc = scratch(c, B_E_SA, (size_t)n * N, &Sa, "Sa")))
     return rc;
-  rc = locanalysis_impl(&dd, loc, Z, dzs, E.xf, E.Hxf, dyo, E.Sf, E.HSf, dr, dzp, dox, doy, doz,
+  rc = locanalysis_impl<double>(&dd, loc, Z, dzs, E.xf, E.Hxf, dyo, E.Sf, E.HSf, dr, dzp, dox, doy, doz,
                         dot, dcorr, dmaxl, xa, Sa, nullptr, nullptr);
   if (rc) return rc;
   double* dEa;
@@ -1604,7 +1681,7 @@ int biased_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
   oakg_dims dd = *d;
   dd.mem = OAKG_MEM_DEVICE;
   // 1. the bias increment: locAnalysisIncrement with the forecast (xf = 0 gives xa = increment)
-  if ((rc = locanalysis_impl(&dd, loc, Z, dzs, zero, dHxf, dyo, dSf, dHSf, dr, dzp, dox, doy, doz,
+  if ((rc = locanalysis_impl<double>(&dd, loc, Z, dzs, zero, dHxf, dyo, dSf, dHSf, dr, dzp, dox, doy, doz,
                              dot, dcorr, dmaxl, inc, nullptr, nullptr, nullptr)))
     return rc;
   // 2. ba = bf - gamma inc, ux = xf - ba; H ux + Hshift; R (1 - gamma)
@@ -1614,7 +1691,7 @@ int biased_locanalysis_impl(const oakg_dims* d, const oakg_loc* loc, int32_t Z,
   if (e == cudaSuccess && m > 0) e = axpby(m, 1.0 - gamma, dr, 0.0, nullptr, r2, st);
   if (e != cudaSuccess) return cuda_fail(e, "bias update");
   // 3. the state increment from the unbiased forecast, xa = ux + increment
-  if ((rc = locanalysis_impl(&dd, loc, Z, dzs, zero, uHx, dyo, dSf, dHSf, r2, dzp, dox, doy, doz,
+  if ((rc = locanalysis_impl<double>(&dd, loc, Z, dzs, zero, uHx, dyo, dSf, dHSf, r2, dzp, dox, doy, doz,
                              dot, dcorr, dmaxl, inc, nullptr, nullptr, nullptr)))
     return rc;
   e = axpby(n, 1.0, ux, 1.0, inc, dxa, st);
@@ -1685,7 +1762,7 @@ int analysis_smw_impl(const oakg_dims* d, const double* xf, const double* Hxf, c
   sa.B = B;
   sa.ldB = ldB;
   const double* obs = g0 + 6;
-  return locanalysis_impl(d, &loc, 1, zs, xf, Hxf, yo, Sf, HSf, r_diag, g0, obs, obs, nullptr,
+  return locanalysis_impl<double>(d, &loc, 1, zs, xf, Hxf, yo, Sf, HSf, r_diag, g0, obs, obs, nullptr,
                           nullptr, g0 + 4, g0 + 5, xa, Sa, ampl, nullptr, &sa);
 }
 
@@ -2091,9 +2168,25 @@ int oakg_locanalysis(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
                      double* ampl, int32_t* nobs) {
   std::lock_guard<std::mutex> lk(oakg::api_mutex());
   oakg::set_ok();
-  int rc = oakg::locanalysis_impl(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf, r_diag,
-                                  zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, xa,
-                                  Sa, ampl, nobs);
+  int rc = oakg::locanalysis_impl<double>(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf,
+                                          r_diag, zone_xyzt, obs_x, obs_y, obs_z, obs_t,
+                                          corr_len, max_len, xa, Sa, ampl, nobs);
+  oakg::last_status() = rc;
+  return rc;
+}
+
+int oakg_locanalysis_f32(const oakg_dims* dims, const oakg_loc* loc, int32_t nzones,
+                         const int32_t* zone_size, const float* xf, const float* Hxf,
+                         const float* yo, const float* Sf, const float* HSf, const float* r_diag,
+                         const double* zone_xyzt, const double* obs_x, const double* obs_y,
+                         const double* obs_z, const double* obs_t, const double* corr_len,
+                         const double* max_len, float* xa, float* Sa, float* ampl,
+                         int32_t* nobs) {
+  std::lock_guard<std::mutex> lk(oakg::api_mutex());
+  oakg::set_ok();
+  int rc = oakg::locanalysis_impl<float>(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf,
+                                         r_diag, zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len,
+                                         max_len, xa, Sa, ampl, nobs);
   oakg::last_status() = rc;
   return rc;
 }
@@ -2243,7 +2336,7 @@ int oakg_locanalysis_smw(const oakg_dims* dims, const oakg_loc* loc, int32_t nzo
   sa.k = k;
   sa.B = B;
   sa.ldB = ldB;
-  int rc = oakg::locanalysis_impl(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf, r_diag,
+  int rc = oakg::locanalysis_impl<double>(dims, loc, nzones, zone_size, xf, Hxf, yo, Sf, HSf, r_diag,
                                   zone_xyzt, obs_x, obs_y, obs_z, obs_t, corr_len, max_len, xa,
                                   Sa, ampl, nobs, &sa);
   oakg::last_status() = rc;

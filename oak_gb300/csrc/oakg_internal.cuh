@@ -50,10 +50,11 @@ cudaError_t obs_bounds(const double* u, const double* v, int64_t m, double* d_ou
                        cudaStream_t st);
 cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* u_src,
                              const double* v_src, const double* yo, const double* Hxf,
-                             const double* r, const double* HSf, int64_t ldH,
-                             int32_t* d_cell, int32_t* d_count, int32_t* d_cell_start,
-                             int32_t* d_pos, int32_t* d_perm, double* d_u, double* d_v,
-                             double* d_innov, double* d_r, double* d_HSt, cudaStream_t st);
+                             const double* r, const double* HSf, const float* HSf32,
+                             int64_t ldH, int32_t* d_cell, int32_t* d_count,
+                             int32_t* d_cell_start, int32_t* d_pos, int32_t* d_perm,
+                             double* d_u, double* d_v, double* d_innov, double* d_r,
+                             double* d_HSt, cudaStream_t st);
 cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_start,
                          int32_t* d_zone_max, cudaStream_t st);
 
@@ -83,6 +84,8 @@ cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParam
                          const int32_t* order = nullptr);
 // FP32 copy of count doubles (HS rows for the mixed form).
 cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st);
+// FP64 copy of count floats (observation vectors given in FP32 storage).
+cudaError_t rows_to_fp64(const float* src, double* dst, int64_t count, cudaStream_t st);
 // zone_gram_fp64 on augmented observation rows so.HSt = [HS_q | B_q] (N columns, the first nx
 // weighted): the products for the SMWCovar Woodbury reduction (zone_smw.cu).
 cudaError_t zone_gram_fp64_aug(const CellGrid& g, const SortedObs& so, int N, int nx,
@@ -225,6 +228,21 @@ cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zo
                              const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st);
 cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d_ampl,
                                   const int32_t* d_nobs, int all_zones, double* ampl_out,
+                                  cudaStream_t st);
+// The same with FP32 storage of xf, Sf, xa, Sa and the amplitudes at the boundary.
+cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const float* xf, const float* Sf, int64_t ldS,
+                             const double* d_T, const double* d_ampl, const int32_t* d_nobs,
+                             float* xa, float* Sa, cudaStream_t st);
+cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_ampl,
+                             const int32_t* d_nobs, int all_zones, float* ampl_out,
+                             cudaStream_t st);
+cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const float* xf, const float* Sf, int64_t ldS,
+                             const float* d_T, const float* d_ampl, const int32_t* d_nobs,
+                             float* xa, float* Sa, cudaStream_t st);
+cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d_ampl,
+                                  const int32_t* d_nobs, int all_zones, float* ampl_out,
                                   cudaStream_t st);
 
 int max_fp64_ensemble();  // largest N the FP64 kernels accept

@@ -228,8 +228,10 @@ __global__ void k_gather_scalars(int64_t m, const int32_t* __restrict__ perm,
 }
 
 // HSt[pos[j]*N + k] = HSf[j + k*ldH]: 32 x 32 tiles, coalesced reads along j, rows of HSt
-// written as contiguous 32-element segments.
-__global__ void k_transpose_rows(int64_t m, int N, const double* __restrict__ HSf, int64_t ldH,
+// written as contiguous 32-element segments. HSf in FP64 or FP32 (FP32 storage at the
+// boundary); the rows are FP64 (exact widening).
+template <typename TIn>
+__global__ void k_transpose_rows(int64_t m, int N, const TIn* __restrict__ HSf, int64_t ldH,
                                  const int32_t* __restrict__ pos, double* __restrict__ HSt) {
   __shared__ double tile[32][33];
   int64_t j0 = (int64_t)blockIdx.x * 32;
@@ -238,7 +240,7 @@ __global__ void k_transpose_rows(int64_t m, int N, const double* __restrict__ HS
   for (int kk = ty; kk < 32; kk += 8) {
     int64_t j = j0 + tx;
     int k = k0 + kk;
-    tile[kk][tx] = (j < m && k < N) ? HSf[j + (int64_t)k * ldH] : 0.0;
+    tile[kk][tx] = (j < m && k < N) ? (double)HSf[j + (int64_t)k * ldH] : 0.0;
   }
   __syncthreads();
   for (int jj = ty; jj < 32; jj += 8) {
@@ -265,10 +267,11 @@ cudaError_t obs_bounds(const double* u, const double* v, int64_t m, double* d_ou
 
 cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* u_src,
                              const double* v_src, const double* yo, const double* Hxf,
-                             const double* r, const double* HSf, int64_t ldH,
-                             int32_t* d_cell, int32_t* d_count, int32_t* d_cell_start,
-                             int32_t* d_pos, int32_t* d_perm, double* d_u, double* d_v,
-                             double* d_innov, double* d_r, double* d_HSt, cudaStream_t st) {
+                             const double* r, const double* HSf, const float* HSf32,
+                             int64_t ldH, int32_t* d_cell, int32_t* d_count,
+                             int32_t* d_cell_start, int32_t* d_pos, int32_t* d_perm,
+                             double* d_u, double* d_v, double* d_innov, double* d_r,
+                             double* d_HSt, cudaStream_t st) {
   const int64_t ncells = (int64_t)g.nu * g.nv;
   cudaError_t e = cudaMemsetAsync(d_count, 0, (ncells + 1) * sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
@@ -289,7 +292,10 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
     k_gather_scalars<<<grid_for(m, 256), 256, 0, st>>>(m, d_perm, u_src, v_src, yo, Hxf, r,
                                                        d_pos, d_u, d_v, d_innov, d_r);
     dim3 tb(32, 8), tg((unsigned)((m + 31) / 32), (unsigned)((N + 31) / 32));
-    k_transpose_rows<<<tg, tb, 0, st>>>(m, N, HSf, ldH, d_pos, d_HSt);
+    if (HSf32)
+      k_transpose_rows<float><<<tg, tb, 0, st>>>(m, N, HSf32, ldH, d_pos, d_HSt);
+    else
+      k_transpose_rows<double><<<tg, tb, 0, st>>>(m, N, HSf, ldH, d_pos, d_HSt);
   }
   count_launches(m > 0 ? 7 : 1);
   return cudaGetLastError();
@@ -310,6 +316,19 @@ __global__ void k_to_fp32(const double* __restrict__ src, float* __restrict__ ds
 cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
   k_to_fp32<<<grid_for(count, 256), 256, 0, st>>>(src, dst, count);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+__global__ void k_to_fp64(const float* __restrict__ src, double* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+
+cudaError_t rows_to_fp64(const float* src, double* dst, int64_t count, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_to_fp64<<<grid_for(count, 256), 256, 0, st>>>(src, dst, count);
   count_launches(1);
   return cudaGetLastError();
 }

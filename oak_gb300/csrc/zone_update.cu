@@ -1,5 +1,6 @@
 // K5 -- ensemble update per zone (T and the amplitudes in R: double for the plain form, float
-// for the mixed-precision form; Sf, Sa, xf, xa stay double at the boundary):
+// for the mixed-precision form; Sf, Sa, xf, xa in S: the storage type at the boundary, double
+// or float):
 //   xa(i1:i2) = xf(i1:i2) + Sf(i1:i2,:) ampl          (rrsqrt.F90:151 and :462-464)
 //   Sa(i1:i2,:) = Sf(i1:i2,:) T                       (rrsqrt.F90:165-185 with T from K4)
 // Zones without relevant observations keep xa = xf and Sa = Sf (rrsqrt.F90:322-326, :371).
@@ -21,13 +22,12 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRows = 64;
 
-template <typename R>
+template <typename R, typename S>
 __global__ void __launch_bounds__(kThreads)
     k_zone_update(int N, int32_t z0, int32_t nzc, const int64_t* __restrict__ zone_start,
-                  int tiles_per_zone, const double* __restrict__ xf,
-                  const double* __restrict__ Sf, int64_t ldS, const R* __restrict__ T,
-                  const R* __restrict__ ampl, const int32_t* __restrict__ nobs,
-                  double* __restrict__ xa, double* __restrict__ Sa) {
+                  int tiles_per_zone, const S* __restrict__ xf, const S* __restrict__ Sf,
+                  int64_t ldS, const R* __restrict__ T, const R* __restrict__ ampl,
+                  const int32_t* __restrict__ nobs, S* __restrict__ xa, S* __restrict__ Sa) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   R* dyn = reinterpret_cast<R*>(dyn_raw);
   R* Ts = dyn;                // [N][N]
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kThreads)
     for (int r = threadIdx.x; r < R_; r += kThreads) {
       R s = 0;
       for (int k = 0; k < N; k++) s = fma(Ss[k * kRows + r], as[k], s);
-      xa[r0 + r] = xf[r0 + r] + (double)s;
+      xa[r0 + r] = (S)((double)xf[r0 + r] + (double)s);
     }
     if (Sa) {
       // Sa(r, c) = sum_k Sf(r, k) T(k, c); consecutive threads -> consecutive rows
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kThreads)
         int c = idx / R_, r = idx - c * R_;
         R s = 0;
         for (int k = 0; k < N; k++) s = fma(Ss[k * kRows + r], Ts[k * N + c], s);
-        Sa[r0 + r + (int64_t)c * ldS] = (double)s;
+        Sa[r0 + r + (int64_t)c * ldS] = (S)s;
       }
     }
   }
@@ -91,12 +91,13 @@ __global__ void __launch_bounds__(kThreads)
 // order over k is that of k_zone_update<float>.
 constexpr int kColBlk = 8;
 
+template <typename S>
 __global__ void __launch_bounds__(kThreads)
     k_zone_update_f32(int N, int NP, int32_t z0, int32_t nzc,
-                      const int64_t* __restrict__ zone_start, const double* __restrict__ xf,
-                      const double* __restrict__ Sf, int64_t ldS, const float* __restrict__ T,
+                      const int64_t* __restrict__ zone_start, const S* __restrict__ xf,
+                      const S* __restrict__ Sf, int64_t ldS, const float* __restrict__ T,
                       const float* __restrict__ ampl, const int32_t* __restrict__ nobs,
-                      double* __restrict__ xa, double* __restrict__ Sa) {
+                      S* __restrict__ xa, S* __restrict__ Sa) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   float* Ts = reinterpret_cast<float*>(dyn_raw);  // [N][NP]
   float* Ss = Ts + N * NP;                         // [N][kRows]
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(kThreads)
       for (int r = threadIdx.x; r < R_; r += kThreads) {  // xa = xf + Sf ampl
         float sx = 0.f;
         for (int k = 0; k < N; k++) sx = fmaf(Ss[k * kRows + r], as[k], sx);
-        xa[r0 + r] = xf[r0 + r] + (double)sx;
+        xa[r0 + r] = (S)((double)xf[r0 + r] + (double)sx);
       }
       if (Sa) {
         for (int it = threadIdx.x; it < R_ * ncb; it += kThreads) {
@@ -171,103 +172,145 @@ __global__ void __launch_bounds__(kThreads)
           }
 #pragma unroll
           for (int t = 0; t < kColBlk; t++)
-            if (c0 + t < N) Sa[r0 + r + (int64_t)(c0 + t) * ldS] = (double)acc[t];
+            if (c0 + t < N) Sa[r0 + r + (int64_t)(c0 + t) * ldS] = (S)acc[t];
         }
       }
     }
   }
 }
 
-template <typename R>
+template <typename R, typename S>
 __global__ void k_write_amplitudes(int N, int32_t z0, int32_t nzc, const R* __restrict__ za,
                                    const int32_t* __restrict__ nobs, int all_zones,
-                                   double* __restrict__ out) {
+                                   S* __restrict__ out) {
   const int64_t total = (int64_t)nzc * N;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     int32_t zl = (int32_t)(idx / N);
     double v = (all_zones && nobs[zl] > 0) ? (double)za[idx] : 0.0;
-    out[(int64_t)z0 * N + idx] = v;
+    out[(int64_t)z0 * N + idx] = (S)v;
   }
 }
 
 }  // namespace
 
-template <typename R>
+template <typename R, typename S>
 cudaError_t zone_update_impl(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
-                             int32_t zone_max, const double* xf, const double* Sf,
-                             int64_t ldS, const R* d_T, const R* d_ampl,
-                             const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
+                             int32_t zone_max, const S* xf, const S* Sf, int64_t ldS,
+                             const R* d_T, const R* d_ampl, const int32_t* d_nobs, S* xa, S* Sa,
+                             cudaStream_t st) {
   size_t smem = (size_t)(N * N + N * kRows + N) * sizeof(R);
-  cudaError_t e = cudaFuncSetAttribute(k_zone_update<R>,
+  cudaError_t e = cudaFuncSetAttribute(k_zone_update<R, S>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int tiles = (zone_max + kRows - 1) / kRows;
   if (tiles < 1) tiles = 1;
   int64_t ntasks = (int64_t)nzc * tiles;
   int grid = (int)(ntasks < 152 * 16 ? (ntasks < 1 ? 1 : ntasks) : 152 * 16);
-  k_zone_update<R><<<grid, kThreads, smem, st>>>(N, z0, nzc, d_zone_start, tiles, xf, Sf, ldS,
-                                                 d_T, d_ampl, d_nobs, xa, Sa);
+  k_zone_update<R, S><<<grid, kThreads, smem, st>>>(N, z0, nzc, d_zone_start, tiles, xf, Sf,
+                                                    ldS, d_T, d_ampl, d_nobs, xa, Sa);
   count_launches(1);
   return cudaGetLastError();
 }
 
-template <typename R>
+template <typename R, typename S>
 cudaError_t write_amplitudes_impl(int N, int32_t z0, int32_t nzc, const R* d_ampl,
-                                  const int32_t* d_nobs, int all_zones, double* ampl_out,
+                                  const int32_t* d_nobs, int all_zones, S* ampl_out,
                                   cudaStream_t st) {
   int64_t total = (int64_t)nzc * N;
   int grid = (int)((total + 255) / 256 < 152 * 8 ? (total + 255) / 256 : 152 * 8);
   if (grid < 1) grid = 1;
-  k_write_amplitudes<R><<<grid, 256, 0, st>>>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out);
+  k_write_amplitudes<R, S><<<grid, 256, 0, st>>>(N, z0, nzc, d_ampl, d_nobs, all_zones,
+                                                 ampl_out);
   count_launches(1);
   return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t zone_update_mixed_impl(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                                   int32_t zone_max, const S* xf, const S* Sf, int64_t ldS,
+                                   const float* d_T, const float* d_ampl, const int32_t* d_nobs,
+                                   S* xa, S* Sa, cudaStream_t st) {
+  const int NP = (N + kColBlk - 1) / kColBlk * kColBlk;
+  const size_t smem = (size_t)(N * NP + N * kRows + N) * sizeof(float);
+  if (smem <= 200 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_zone_update_f32<S>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int bps = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_update_f32<S>, kThreads, smem);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t cap = (int64_t)sms * (bps > 0 ? bps : 1) * 4;
+    const int grid = (int)(nzc < cap ? (nzc < 1 ? 1 : nzc) : cap);
+    k_zone_update_f32<S><<<grid, kThreads, smem, st>>>(N, NP, z0, nzc, d_zone_start, xf, Sf,
+                                                       ldS, d_T, d_ampl, d_nobs, xa, Sa);
+    count_launches(1);
+    return cudaGetLastError();
+  }
+  return zone_update_impl<float, S>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T,
+                                    d_ampl, d_nobs, xa, Sa, st);
 }
 
 cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
                              int32_t zone_max, const double* xf, const double* Sf,
                              int64_t ldS, const double* d_T, const double* d_ampl,
                              const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
-  return zone_update_impl<double>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T, d_ampl,
-                                  d_nobs, xa, Sa, st);
+  return zone_update_impl<double, double>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T,
+                                          d_ampl, d_nobs, xa, Sa, st);
+}
+
+cudaError_t zone_update_fp64(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const float* xf, const float* Sf, int64_t ldS,
+                             const double* d_T, const double* d_ampl, const int32_t* d_nobs,
+                             float* xa, float* Sa, cudaStream_t st) {
+  return zone_update_impl<double, float>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T,
+                                         d_ampl, d_nobs, xa, Sa, st);
 }
 
 cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
                              int32_t zone_max, const double* xf, const double* Sf,
                              int64_t ldS, const float* d_T, const float* d_ampl,
                              const int32_t* d_nobs, double* xa, double* Sa, cudaStream_t st) {
-  const int NP = (N + kColBlk - 1) / kColBlk * kColBlk;
-  const size_t smem = (size_t)(N * NP + N * kRows + N) * sizeof(float);
-  if (smem <= 200 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_zone_update_f32,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int bps = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_zone_update_f32, kThreads, smem);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t cap = (int64_t)sms * (bps > 0 ? bps : 1) * 4;
-    const int grid = (int)(nzc < cap ? (nzc < 1 ? 1 : nzc) : cap);
-    k_zone_update_f32<<<grid, kThreads, smem, st>>>(N, NP, z0, nzc, d_zone_start, xf, Sf, ldS,
-                                                    d_T, d_ampl, d_nobs, xa, Sa);
-    count_launches(1);
-    return cudaGetLastError();
-  }
-  return zone_update_impl<float>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T, d_ampl,
-                                 d_nobs, xa, Sa, st);
+  return zone_update_mixed_impl<double>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T,
+                                        d_ampl, d_nobs, xa, Sa, st);
+}
+
+cudaError_t zone_update_fp32(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                             int32_t zone_max, const float* xf, const float* Sf, int64_t ldS,
+                             const float* d_T, const float* d_ampl, const int32_t* d_nobs,
+                             float* xa, float* Sa, cudaStream_t st) {
+  return zone_update_mixed_impl<float>(N, z0, nzc, d_zone_start, zone_max, xf, Sf, ldS, d_T,
+                                       d_ampl, d_nobs, xa, Sa, st);
 }
 
 cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_ampl,
                              const int32_t* d_nobs, int all_zones, double* ampl_out,
                              cudaStream_t st) {
-  return write_amplitudes_impl<double>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out, st);
+  return write_amplitudes_impl<double, double>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out,
+                                               st);
+}
+
+cudaError_t write_amplitudes(int N, int32_t z0, int32_t nzc, const double* d_ampl,
+                             const int32_t* d_nobs, int all_zones, float* ampl_out,
+                             cudaStream_t st) {
+  return write_amplitudes_impl<double, float>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out,
+                                              st);
 }
 
 cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d_ampl,
                                   const int32_t* d_nobs, int all_zones, double* ampl_out,
                                   cudaStream_t st) {
-  return write_amplitudes_impl<float>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out, st);
+  return write_amplitudes_impl<float, double>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out,
+                                              st);
+}
+
+cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d_ampl,
+                                  const int32_t* d_nobs, int all_zones, float* ampl_out,
+                                  cudaStream_t st) {
+  return write_amplitudes_impl<float, float>(N, z0, nzc, d_ampl, d_nobs, all_zones, ampl_out,
+                                             st);
 }
 
 }  // namespace oakg

@@ -201,6 +201,45 @@ BATCHED_VARS = (("temp", 1.0), ("salt", 0.2), ("u", 0.1), ("v", 0.1), ("ssh", 0.
 LARGE_VARS = (("temp", 1.0), ("salt", 0.2))
 
 
+def _column_obs(nx, ny, nz, n3, zsz, m, cfg, track_frac, ntracks, obs_split, obs_sd):
+    """Observations of a column workload (numpy, seeded): positions in cell units, 70 %
+    (track_frac) on track segments a quarter of the grid long, the observed variable and
+    level, the bilinear operator (4 columns at the level; H_index into the column-ordered
+    state, H_weight), each observation's error sd and its noise draw."""
+    rng_pos = np.random.default_rng(1000 * cfg + 900)
+    m_track = int(round(track_frac * m))
+    rng_t = np.random.default_rng(1000 * cfg + 902)
+    per = np.full(ntracks, m_track // ntracks)
+    per[: m_track - per.sum()] += 1
+    xs, ys = [], []
+    for t in range(ntracks):
+        a = np.deg2rad(rng_t.uniform(10.0, 80.0))
+        i0 = rng_t.uniform(0.0, nx)
+        s0 = rng_t.uniform(0.0, 0.75 * (nx - 1))
+        i = rng_t.uniform(s0, s0 + 0.25 * (nx - 1), per[t])
+        j = ny / 2 + (ny / 2) * np.arctan(np.tan(a) * np.sin(2 * np.pi * (i - i0) / nx)) / (np.pi / 2)
+        xs.append(i)
+        ys.append(np.clip(j, 0.0, ny - 1.0))
+    xs.append(rng_pos.uniform(0.0, nx - 1, m - m_track))
+    ys.append(rng_pos.uniform(0.0, ny - 1, m - m_track))
+    ox, oy = np.concatenate(xs), np.concatenate(ys)
+    u = rng_pos.uniform(0.0, 1.0, m)
+    var = np.asarray(obs_split[0])[np.searchsorted(np.asarray(obs_split[1]), u, side="right")]
+    is2 = var == n3
+    lev = np.where(is2, 0, rng_pos.integers(0, nz, m))
+    off = np.where(is2, n3 * nz, var * nz + lev)
+    ix = np.minimum(np.floor(ox).astype(np.int64), nx - 2)
+    iy = np.minimum(np.floor(oy).astype(np.int64), ny - 2)
+    fx, fy = ox - ix, oy - iy
+    cols = np.stack([iy * nx + ix, iy * nx + ix + 1, (iy + 1) * nx + ix, (iy + 1) * nx + ix + 1], 1)
+    H_index = cols * zsz + off[:, None]
+    H_weight = np.stack([(1 - fx) * (1 - fy), fx * (1 - fy), (1 - fx) * fy, fx * fy], 1)
+    sd_obs = obs_sd(var, np.random.default_rng(1000 * cfg + 903))
+    noise = np.random.default_rng(1000 * cfg + 901).standard_normal(m) * sd_obs
+    return {"ox": ox, "oy": oy, "lev": lev, "var": var, "H_index": H_index,
+            "H_weight": H_weight, "sd_obs": sd_obs, "noise": noise}
+
+
 def _column_case(name, gx, gy, scale, N, nz, vars3, var2, m, radius, cfg, track_frac, ntracks,
                  obs_split, obs_sd, keep_ensemble):
     """Columns of several variables (zone = one horizontal column), bilinear observations.
@@ -241,38 +280,11 @@ def _column_case(name, gx, gy, scale, N, nz, vars3, var2, m, radius, cfg, track_
     Ef = np.empty((n, N), order="F")
     for k in range(N):
         Ef[:, k] = draw(1000 * cfg + 1 + k)
-    rng_pos = np.random.default_rng(1000 * cfg + 900)
-    m_track = int(round(track_frac * m))
-    rng_t = np.random.default_rng(1000 * cfg + 902)
-    per = np.full(ntracks, m_track // ntracks)
-    per[: m_track - per.sum()] += 1
-    xs, ys = [], []
-    for t in range(ntracks):
-        a = np.deg2rad(rng_t.uniform(10.0, 80.0))
-        i0 = rng_t.uniform(0.0, nx)
-        s0 = rng_t.uniform(0.0, 0.75 * (nx - 1))
-        i = rng_t.uniform(s0, s0 + 0.25 * (nx - 1), per[t])
-        j = ny / 2 + (ny / 2) * np.arctan(np.tan(a) * np.sin(2 * np.pi * (i - i0) / nx)) / (np.pi / 2)
-        xs.append(i)
-        ys.append(np.clip(j, 0.0, ny - 1.0))
-    xs.append(rng_pos.uniform(0.0, nx - 1, m - m_track))
-    ys.append(rng_pos.uniform(0.0, ny - 1, m - m_track))
-    ox, oy = np.concatenate(xs), np.concatenate(ys)
-    u = rng_pos.uniform(0.0, 1.0, m)
-    var = np.asarray(obs_split[0])[np.searchsorted(np.asarray(obs_split[1]), u, side="right")]
-    is2 = var == n3
-    lev = np.where(is2, 0, rng_pos.integers(0, nz, m))
-    off = np.where(is2, n3 * nz, var * nz + lev)
-    ix = np.minimum(np.floor(ox).astype(np.int64), nx - 2)
-    iy = np.minimum(np.floor(oy).astype(np.int64), ny - 2)
-    fx, fy = ox - ix, oy - iy
-    cols = np.stack([iy * nx + ix, iy * nx + ix + 1, (iy + 1) * nx + ix, (iy + 1) * nx + ix + 1], 1)
-    H_index = cols * zsz + off[:, None]
-    H_weight = np.stack([(1 - fx) * (1 - fy), fx * (1 - fy), (1 - fx) * fy, fx * fy], 1)
+    ob = _column_obs(nx, ny, nz, n3, zsz, m, cfg, track_frac, ntracks, obs_split, obs_sd)
+    ox, oy, lev, H_index, H_weight = ob["ox"], ob["oy"], ob["lev"], ob["H_index"], ob["H_weight"]
     HEf = np.einsum("mk,mkn->mn", H_weight, Ef[H_index.reshape(-1), :].reshape(m, 4, N))
-    sd_obs = obs_sd(var, np.random.default_rng(1000 * cfg + 903))
-    noise = np.random.default_rng(1000 * cfg + 901).standard_normal(m) * sd_obs
-    yo = np.einsum("mk,mk->m", H_weight, truth[H_index]) + noise
+    sd_obs = ob["sd_obs"]
+    yo = np.einsum("mk,mk->m", H_weight, truth[H_index]) + ob["noise"]
     xf, Hxf, Sf, HSf = _anomalies(Ef, HEf)
     zone_size = np.full(Z, zsz, dtype=np.int32)
     zc = np.arange(Z)
@@ -310,6 +322,168 @@ def large_case(scale=0.125, N=128, nz=50, m=1_000_000, radius=10.0, seed_cfg=4,
     return _column_case("large 2 variables", 1440, 720, scale, N, nz, LARGE_VARS, None, m,
                         radius, seed_cfg, track_frac, ntracks, ((0, 1), (0.5,)),
                         lambda var, rng: rng.uniform(0.05, 0.5, var.size), keep_ensemble)
+
+
+# ------------------------------------------------------------------------------------------
+# The column workloads at full size, generated on the GPU with FP32 storage: the state of the
+# large configuration is 104M values x 128 members (53 GB in FP32), which host-side NumPy FFTs
+# cannot generate in reasonable time. Same recipe as _column_case (Gaussian random fields by
+# FFT, seeded per member; observations from _column_obs), with torch's CUDA generator seeded
+# 1000*config + role and FP32 FFTs.
+
+@dataclasses.dataclass
+class DeviceCase:
+    """A workload whose state and observation arrays live on the GPU in FP32 (torch tensors):
+    xf (n), Sf (n, N) column-major, x_true (n), Hxf, yo, r_diag (m), HSf (m, N) column-major.
+    Geometry stays on the host in FP64 (zone_size, zone_pos, obs_pos, corr_len, max_len)."""
+    name: str
+    xf: object
+    Hxf: object
+    yo: object
+    Sf: object
+    HSf: object
+    r_diag: object
+    x_true: object
+    zone_size: np.ndarray
+    zone_pos: np.ndarray
+    obs_pos: tuple
+    corr_len: np.ndarray
+    max_len: np.ndarray
+    nx: int = 0
+    ny: int = 0
+    weight: int = 1
+    metric: int = 0
+    loctype: int = 1
+
+    @property
+    def n(self):
+        return int(self.xf.shape[0])
+
+    @property
+    def N(self):
+        return int(self.Sf.shape[1])
+
+    @property
+    def m(self):
+        return int(self.yo.shape[0])
+
+    @property
+    def Z(self):
+        return int(self.zone_size.size)
+
+
+def gaussian_field_torch(shape, lengths, gen, device):
+    """gaussian_field on the GPU in FP32: white noise from `gen`, the same spectral filter
+    exp(-(pi l k)^2) per axis, sd renormalised to 1."""
+    import math
+
+    import torch
+    noise = torch.randn(shape, generator=gen, device=device, dtype=torch.float32)
+    F = torch.fft.rfftn(noise)
+    del noise
+    for ax, (nax, l) in enumerate(zip(shape, lengths)):
+        if l <= 0:
+            continue
+        if ax == len(shape) - 1:
+            k = torch.fft.rfftfreq(nax, device=device)
+        else:
+            k = torch.fft.fftfreq(nax, device=device)
+        tf = torch.exp(-((math.pi * l * k) ** 2))
+        sh = [1] * len(shape)
+        sh[ax] = tf.numel()
+        F *= tf.reshape(sh)
+    f = torch.fft.irfftn(F, s=shape)
+    del F
+    f /= f.std()
+    return f
+
+
+def _column_case_device(name, gx, gy, scale, N, nz, vars3, var2, m, radius, cfg, track_frac,
+                        ntracks, obs_split, obs_sd, device):
+    import torch
+    nx = max(4, int(round(gx * scale)))
+    ny = max(4, int(round(gy * scale)))
+    if scale != 1.0:
+        m = max(1, int(round(m * scale * scale)))
+        ntracks = max(1, int(round(ntracks * scale)))
+    Z = nx * ny
+    n3 = len(vars3)
+    zsz = n3 * nz + (1 if var2 else 0)
+    n = Z * zsz
+    lengths3, lengths2 = (8.0, 8.0, 3.0), (8.0, 8.0)
+    gen = torch.Generator(device=device)
+
+    def draw(seed, out):  # out: (Z, zsz) view of one member (or the truth)
+        gen.manual_seed(seed)
+        for v, (_, sd) in enumerate(vars3):
+            out[:, v * nz:(v + 1) * nz] = sd * gaussian_field_torch(
+                (ny, nx, nz), lengths3, gen, device).reshape(Z, nz)
+        if var2:
+            out[:, n3 * nz] = var2[1] * gaussian_field_torch((ny, nx), lengths2, gen,
+                                                             device).reshape(Z)
+
+    f32 = torch.float32
+    truth = torch.empty(n, dtype=f32, device=device)
+    draw(1000 * cfg + 0, truth.view(Z, zsz))
+    E = torch.empty((N, n), dtype=f32, device=device)   # member k = row k; E.t() is (n, N)
+    for k in range(N):
+        draw(1000 * cfg + 1 + k, E[k].view(Z, zsz))
+    # mean and scaled anomalies (ASSIM_SCALING: (Ef - xf)/sqrt(N-1)), in FP64, stored in FP32
+    xf = torch.empty(n, dtype=f32, device=device)
+    s = float(np.sqrt(N - 1.0))
+    step = max(1, (1 << 29) // (8 * N))
+    for c0 in range(0, n, step):
+        c1 = min(n, c0 + step)
+        blk = E[:, c0:c1].double()
+        mu = blk.mean(0)
+        xf[c0:c1] = mu.float()
+        E[:, c0:c1] = ((blk - mu) / s).float()
+        del blk, mu
+    Sf = E.t()
+    ob = _column_obs(nx, ny, nz, n3, zsz, m, cfg, track_frac, ntracks, obs_split, obs_sd)
+    idx = torch.as_tensor(ob["H_index"], device=device)
+    w = torch.as_tensor(ob["H_weight"], device=device)
+    # H is linear: H xf and H Sf are the mean and anomalies of H Ef
+    Hxf = (w * xf.double()[idx]).sum(1).float()
+    HSt = torch.empty((N, m), dtype=f32, device=device)  # HSt.t() is HSf (m, N) column-major
+    mstep = max(1, (1 << 28) // (8 * 4 * N))
+    for j0 in range(0, m, mstep):
+        j1 = min(m, j0 + mstep)
+        rows = E[:, idx[j0:j1].reshape(-1)].double().reshape(N, j1 - j0, 4)
+        HSt[:, j0:j1] = (rows * w[j0:j1].unsqueeze(0)).sum(2).float()
+        del rows
+    yo = ((w * truth.double()[idx]).sum(1)
+          + torch.as_tensor(ob["noise"], device=device)).float()
+    r = torch.as_tensor(ob["sd_obs"] ** 2, device=device).float()
+    zone_size = np.full(Z, zsz, dtype=np.int32)
+    zc = np.arange(Z)
+    zone_pos = np.zeros((Z, 4))
+    zone_pos[:, 0] = zc % nx
+    zone_pos[:, 1] = zc // nx
+    obs_pos = (ob["ox"], ob["oy"], ob["lev"].astype(np.float64), np.zeros(m))
+    return DeviceCase(f"{name} {nx}x{ny}x{nz} N={N} m={m} GC radius {radius:g} (FP32)", xf, Hxf,
+                      yo, Sf, HSt.t(), r, truth, zone_size, zone_pos, obs_pos,
+                      np.full(Z, radius / 2.0), np.full(Z, radius), nx=nx, ny=ny)
+
+
+def batched_case_device(scale=1.0, device="cuda", N=100, nz=30, m=200_000, radius=12.0,
+                        seed_cfg=2, track_frac=0.7, ntracks=8) -> DeviceCase:
+    """batched_case generated on the GPU with FP32 storage (default: the full 720 x 360 grid,
+    259,200 zones of 121 elements, N = 100: 12.5 GB per ensemble array)."""
+    sds = np.array([sd for _, sd in BATCHED_VARS])
+    return _column_case_device("batched 5 variables", 720, 360, scale, N, nz, BATCHED_VARS[:4],
+                               BATCHED_VARS[4], m, radius, seed_cfg, track_frac, ntracks,
+                               ((4, 0, 1), (0.5, 0.8)), lambda var, rng: 0.1 * sds[var],
+                               device)
+
+
+def large_case_device(scale=1.0, device="cuda", N=128, nz=50, m=1_000_000, radius=10.0,
+                      seed_cfg=4, track_frac=0.7, ntracks=16) -> DeviceCase:
+    """large_case generated on the GPU with FP32 storage (default: the full 1440 x 720 grid,
+    1,036,800 zones of 100 elements, N = 128: 53 GB per ensemble array)."""
+    return _column_case_device("large 2 variables", 1440, 720, scale, N, nz, LARGE_VARS, None,
+                               m, radius, seed_cfg, track_frac, ntracks, ((0, 1), (0.5,)),
+                               lambda var, rng: rng.uniform(0.05, 0.5, var.size), device)
 
 
 def rrsqrt_test_case():

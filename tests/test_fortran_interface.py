@@ -166,4 +166,6 @@ def test_wrappers_keep_the_reference_argument_lists():
     assert [x.strip() for x in la.split(",")] == ["zoneSize", "geometry", "xf", "Hxf", "yo",
                                                   "Sf", "HSf", "R", "xa", "Sa", "amplitudes",
                                                   "localise_obs"]
+    la4 = re.search(r"subroutine gpu_locAnalysis_r4\(([^)]*)\)", src).group(1)
+    assert la4.split() == la.split()
     assert "subroutine gpu_locAnalysis_adjoint" in src
