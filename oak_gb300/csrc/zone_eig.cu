@@ -507,6 +507,161 @@ __global__ void __launch_bounds__(128)
   for (int i = 0; i < N; i++) zj[i] = x[i];
 }
 
+// E2b for N <= 64 in FP64: one block of kT64 = 64 threads per zone, thread j = eigenpair j,
+// with the arithmetic of k_eig_tridiag_vectors<double> (same LU, start vector and two solves;
+// reciprocals by Newton steps and a power-of-two prescaling before the normalisation, so the
+// vectors agree to rounding). The per-thread factor arrays of the generic kernel
+// live in local memory, and with thousands of threads per SM they go to DRAM (most of the
+// eigensolve's traffic); here the partial-pivoting LU is recomputed in each forward sweep
+// (fused with the elimination), the upper factor is kept in shared memory ([i][j] layout:
+// consecutive threads, consecutive words) and the iterate in registers (loops unrolled to 64).
+constexpr int kT64 = 64;
+
+// 1/p by two Newton steps from the FP32 reciprocal (relative error below 2^-52, not always
+// correctly rounded). The IEEE FP64 division is a called routine whose call keeps the live
+// register array x in local memory; this is inline. Valid for |p| inside FP32's normal range:
+// the tridiagonal is of G / max|G_ij|, so ||Tri||_F >= 1, ||Tri||_1 >= 1/sqrt(N) and every
+// pivot lies in [eps ||Tri||_1, 3 N].
+__device__ __forceinline__ double rcp_newton(double p) {
+  double r = (double)__frcp_rn((float)p);
+  double e = fma(-p, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-p, r, 1.0);
+  return fma(r, e, r);
+}
+
+// 1/sqrt(a) by Newton steps from the FP32 estimate, for a in [1, 4 N] (a normalised sum of
+// squares); inline for the same reason as rcp_newton.
+__device__ __forceinline__ double rsqrt_newton(double a) {
+  double y = (double)rsqrtf((float)a);
+#pragma unroll
+  for (int k = 0; k < 3; k++) y = y * fma(-0.5 * a * y, y, 1.5);
+  return y;
+}
+
+// 2^-e for the binary exponent e of x > 0 (normal), by its bits
+__device__ __forceinline__ double pow2_inv_exponent(double x) {
+  const long long e = ((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+  return __longlong_as_double((1023 - e) << 52);
+}
+
+__global__ void __launch_bounds__(kT64)
+    k_eig_vectors_fp64(int N, int32_t nzc, const double* __restrict__ aux,
+                       double* __restrict__ Zg, const int32_t* __restrict__ nobs) {
+  constexpr int NV = kT64;
+  extern __shared__ __align__(16) double sfac64[];  // u1, u2, 1/pivot: [i][j] each
+  __shared__ double sd[NV], se[NV];
+  double* su1 = sfac64;
+  double* su2 = sfac64 + NV * kT64;
+  double* sui = sfac64 + 2 * NV * kT64;
+  const int j = threadIdx.x;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  const double* ax = aux + (int64_t)zl * aux_stride(N);
+  for (int i = j; i < N; i += kT64) {
+    sd[i] = ax[i];
+    se[i] = (i < N - 1) ? ax[N + i] : 0.0;
+  }
+  __syncthreads();
+  const double onenrm = ax[5 * N + 1];
+  double* Zz = Zg + (int64_t)zl * N * N;
+  double x[NV];
+#pragma unroll
+  for (int i = 0; i < NV; i++) x[i] = 0.0;
+  if (!(onenrm > 1e4 * Prec<double>::tiny())) {  // Tri = 0: every vector is an eigenvector
+#pragma unroll
+    for (int i = 0; i < NV; i++) x[i] = (i == j) ? 1.0 : 0.0;
+  } else if (j < N) {
+    const double l = ax[4 * N + j];
+    const double tiny = Prec<double>::eps() * onenrm;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      unsigned h = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
+      h ^= h >> 15;
+      h *= 2246822519u;
+      h ^= h >> 13;
+      x[i] = (i < N) ? (double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5 : 0.0;
+    }
+#pragma unroll 1
+    for (int it = 0; it < 2; it++) {
+      double cd = sd[0] - l, csup = (N > 1) ? se[0] : 0.0;
+#pragma unroll
+      for (int i = 0; i < NV - 1; i++) {
+        if (i < N - 1) {
+          const double sub = se[i], dg = sd[i + 1] - l, sp = (i + 1 < N - 1) ? se[i + 1] : 0.0;
+          const bool swap = fabs(cd) < fabs(sub);
+          double pivot = swap ? sub : cd;
+          if (!swap && fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
+          const double ui = rcp_newton(pivot);
+          const double li = (swap ? cd : sub) * ui;
+          if (it == 0) {
+            su1[i * kT64 + j] = swap ? dg : csup;
+            su2[i * kT64 + j] = swap ? sp : 0.0;
+            sui[i * kT64 + j] = ui;
+          }
+          const double aa = swap ? csup : dg, bb = swap ? dg : csup;
+          cd = fma(-li, bb, aa);
+          const double nls = -li * sp;
+          csup = swap ? nls : sp;
+          const double xi = swap ? x[i + 1] : x[i], xn = swap ? x[i] : x[i + 1];
+          x[i] = xi;
+          x[i + 1] = fma(-li, xi, xn);
+        }
+      }
+      if (it == 0) {
+        double pivot = cd;
+        if (fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
+        sui[(N - 1) * kT64 + j] = rcp_newton(pivot);
+        // the factor has no entries right of the last column: zeros make one formula serve
+        // every row (x beyond N is 0)
+        su1[(N - 1) * kT64 + j] = 0.0;
+        su2[(N - 1) * kT64 + j] = 0.0;
+        su2[(N - 2) * kT64 + j] = 0.0;
+      }
+      // back substitution x[i] = (x[i] - u1 x[i+1] - u2 x[i+2]) / p; every index is a
+      // compile-time constant after unrolling (guards compare with N, never select by it), so
+      // x stays in registers
+#pragma unroll
+      for (int i = NV - 1; i >= 0; i--) {
+        if (i < N) {
+          double v = x[i];
+          if (i + 1 < NV) v = fma(-su1[i * kT64 + j], x[i + 1], v);
+          if (i + 2 < NV) v = fma(-su2[i * kT64 + j], x[i + 2], v);
+          x[i] = v * sui[i * kT64 + j];
+        }
+      }
+      // scale by a power of two near 1/max|x| (the sum of squares cannot overflow), then
+      // normalise
+      double mx = 0.0;
+#pragma unroll
+      for (int i = 0; i < NV; i++)
+        if (i < N) mx = fmax(mx, fabs(x[i]));
+      const double im = pow2_inv_exponent(mx);
+      double nrm = 0.0;
+#pragma unroll
+      for (int i = 0; i < NV; i++) {
+        if (i < N) {
+          x[i] *= im;
+          nrm = fma(x[i], x[i], nrm);
+        }
+      }
+      const double sc = rsqrt_newton(nrm);
+#pragma unroll
+      for (int i = 0; i < NV; i++) x[i] *= sc;
+    }
+  }
+  __syncthreads();  // factors no longer read: reuse them as the transpose buffer
+  double* tr = sfac64;  // [i][kT64 + 1]
+#pragma unroll
+  for (int i = 0; i < NV; i++) tr[i * (kT64 + 1) + j] = x[i];
+  __syncthreads();
+  // vectors (rows of Z), coalesced along the rows
+  for (int idx = j; idx < N * N; idx += kT64) {
+    const int jj = idx / N, i = idx - jj * N;
+    Zz[(int64_t)jj * N + i] = tr[i * (kT64 + 1) + jj];
+  }
+}
+
 // ------------------------------------------------------------------------------------ E3
 template <typename R>
 __global__ void __launch_bounds__(kThreads)
@@ -877,6 +1032,15 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
     k_eig_shifts<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs);
   } else {
     k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  }
+  if (sizeof(R) == sizeof(double) && N <= kT64) {
+    const size_t smem = (size_t)3 * kT64 * kT64 * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(k_eig_vectors_fp64,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_eig_vectors_fp64<<<(unsigned)(nzc > 0 ? nzc : 1), kT64, smem, st>>>(
+        N, nzc, reinterpret_cast<const double*>(d_aux), reinterpret_cast<double*>(d_Z), d_nobs);
+    return cudaSuccess;
   }
   const int64_t pairs = (int64_t)nzc * N;
   k_eig_tridiag_vectors<R><<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(N, nzc, d_aux, d_Z,
