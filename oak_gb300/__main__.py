@@ -1,13 +1,17 @@
 """Command-line runner for the synthetic local-analysis workloads.
 
   python -m oak_gb300 local [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--m M]
-  python -m oak_gb300 batched [--scale S] [--precision fp64|mixed] [--calls K] [--N N]
+  python -m oak_gb300 batched [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--fp32]
+  python -m oak_gb300 large [--scale S] [--precision fp64|mixed] [--calls K]
   python -m oak_gb300 layout [--obs M] [--calls K]
 
 ``local`` builds the seeded single-variable case (360 x 180 x 20 columns scaled horizontally by
 S, N = 64, Gaspari-Cohn radius 12 cells); ``batched`` the 5-variable case (720 x 360 columns of
-121 elements scaled by S, N = 100, bilinear observations clustered on tracks). Either is moved
-to cuda:0 and :func:`oak_gb300.loc_analysis` is called K times, printing the device time of
+121 elements scaled by S, N = 100, bilinear observations clustered on tracks); ``large`` the
+2-variable case (1440 x 720 columns of 100 elements scaled by S, N = 128, 1M clustered
+observations). ``batched --fp32`` and ``large`` generate the case on the GPU with FP32 storage
+(oakg_locanalysis_f32), the others on the host in FP64, moved to cuda:0. Then
+:func:`oak_gb300.loc_analysis` is called K times, printing the device time of
 each stage of the last call. Used to run one precision's kernels in isolation (profiling,
 quick timing); the full benchmark is bench.py. ``layout`` runs the layout builders on one
 3-D variable of 720 x 360 x 50 points with a land mask and 259,200 column zones: the zone
@@ -37,6 +41,12 @@ def main(argv=None):
     bp.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     bp.add_argument("--calls", type=int, default=2)
     bp.add_argument("--N", type=int, default=100)
+    bp.add_argument("--fp32", action="store_true",
+                    help="generate on the GPU with FP32 storage at the boundary")
+    gp = sub.add_parser("large", help="run the 2-variable N = 128 workload on cuda:0 (FP32)")
+    gp.add_argument("--scale", type=float, default=0.125)
+    gp.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    gp.add_argument("--calls", type=int, default=2)
     yp = sub.add_parser("layout", help="run the layout builders on cuda:0")
     yp.add_argument("--obs", type=int, default=1_000_000)
     yp.add_argument("--calls", type=int, default=2)
@@ -50,15 +60,22 @@ def main(argv=None):
         layout(a, torch, oak_gb300)
         return
 
-    if a.cmd == "local":
-        c = local_case(scale=a.scale, N=a.N, m=a.m)
-    else:
-        c = batched_case(scale=a.scale, N=a.N)
     dev = torch.device("cuda", 0)
     T = lambda x: torch.as_tensor(np.ascontiguousarray(x), device=dev)
     F = lambda x: torch.as_tensor(np.ascontiguousarray(np.asarray(x).T), device=dev).t()
-    args = (T(c.zone_size), T(c.xf), T(c.Hxf), T(c.yo), F(c.Sf), F(c.HSf), T(c.r_diag),
-            T(c.zone_pos), tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
+    if a.cmd == "large" or (a.cmd == "batched" and a.fp32):
+        from oak_gb300.workloads import batched_case_device, large_case_device
+        c = (large_case_device(scale=a.scale, device=dev) if a.cmd == "large"
+             else batched_case_device(scale=a.scale, device=dev, N=a.N))
+        args = (T(c.zone_size), c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag, T(c.zone_pos),
+                tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
+    else:
+        if a.cmd == "local":
+            c = local_case(scale=a.scale, N=a.N, m=a.m)
+        else:
+            c = batched_case(scale=a.scale, N=a.N)
+        args = (T(c.zone_size), T(c.xf), T(c.Hxf), T(c.yo), F(c.Sf), F(c.HSf), T(c.r_diag),
+                T(c.zone_pos), tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
     prec = oak_gb300.PREC_FP64 if a.precision == "fp64" else oak_gb300.PREC_MIXED
     for _ in range(a.calls):
         oak_gb300.loc_analysis(*args, weight=c.weight, metric=c.metric, loctype=c.loctype,
