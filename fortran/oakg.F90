@@ -52,7 +52,8 @@ module oakg
   ! precision of the local analysis
   integer(c_int32_t), parameter :: OAKG_PREC_FP64 = 0, OAKG_PREC_MIXED = 1
   ! oakg_loc%flags
-  integer(c_int32_t), parameter :: OAKG_FLAG_AMPL_ALWAYS = 1, OAKG_FLAG_BRUTE_SEARCH = 2
+  integer(c_int32_t), parameter :: OAKG_FLAG_AMPL_ALWAYS = 1, OAKG_FLAG_BRUTE_SEARCH = 2, &
+       OAKG_FLAG_SIMT_UPDATE = 4
 
   ! struct oakg_dims (the ensemble size is the C member N; Fortran names are case-blind)
   type, bind(C) :: oakg_dims

@@ -81,6 +81,9 @@ extern "C" {
 #define OAKG_FLAG_BRUTE_SEARCH 2 /* test every observation for every zone (the reference's
                                     O(Z m) loop, assimilation.F90:3745-3757) instead of the
                                     cell-grid search; same results, for validation         */
+#define OAKG_FLAG_SIMT_UPDATE 4  /* mixed form: the ensemble update on the CUDA cores (FP32
+                                    FMA) instead of the tensor cores (3xTF32); both give
+                                    FP32-level products, for comparison                    */
 
 typedef struct {
   int64_t n;        /* state vector size                                        */

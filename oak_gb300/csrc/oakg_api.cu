@@ -351,7 +351,16 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   char* dSa = a.store32 ? (char*)a.Sa32 : (char*)a.Sa;
   char* dxa = a.store32 ? (char*)a.xa32 : (char*)a.xa;
   // the update of zones [zz0, zz0 + nq) (T and amplitudes at the chunk-local slot)
-  auto update = [&](int32_t zz0, int32_t nq, const R* T, const R* za, const int32_t* nb) {
+  // (mixed form: on the tensor cores unless OAKG_FLAG_SIMT_UPDATE asks for the CUDA cores)
+  auto update = [&](int32_t zz0, int32_t nq, const R* T, const R* za,
+                    const int32_t* nb) -> cudaError_t {
+    if constexpr (std::is_same<R, float>::value) {
+      if (!(a.lp.flags & OAKG_FLAG_SIMT_UPDATE))
+        return a.store32 ? zone_update_tc(N, zz0, nq, a.zstart, a.xf32, a.Sf32, a.ldS, T, za, nb,
+                                          a.xa32, a.Sa32, *status_all, st)
+                         : zone_update_tc(N, zz0, nq, a.zstart, a.xf, a.Sf, a.ldS, T, za, nb,
+                                          a.xa, a.Sa, *status_all, st);
+    }
     return a.store32 ? K::update(N, zz0, nq, a.zstart, a.zone_max, a.xf32, a.Sf32, a.ldS, T, za,
                                  nb, a.xa32, a.Sa32, st)
                      : K::update(N, zz0, nq, a.zstart, a.zone_max, a.xf, a.Sf, a.ldS, T, za, nb,

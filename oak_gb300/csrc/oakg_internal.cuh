@@ -245,6 +245,18 @@ cudaError_t write_amplitudes_fp32(int N, int32_t z0, int32_t nzc, const float* d
                                   const int32_t* d_nobs, int all_zones, float* ampl_out,
                                   cudaStream_t st);
 
+// Mixed form on the tensor cores (zone_update_tc.cu), N <= 128: the same update with
+// Sa = Sf T and Sf ampl as one 3xTF32 product; d_err receives ZST_TIMEOUT (OR) if a bounded
+// device wait expired.
+cudaError_t zone_update_tc(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                           const double* xf, const double* Sf, int64_t ldS, const float* d_T,
+                           const float* d_ampl, const int32_t* d_nobs, double* xa, double* Sa,
+                           int32_t* d_err, cudaStream_t st);
+cudaError_t zone_update_tc(int N, int32_t z0, int32_t nzc, const int64_t* d_zone_start,
+                           const float* xf, const float* Sf, int64_t ldS, const float* d_T,
+                           const float* d_ampl, const int32_t* d_nobs, float* xa, float* Sa,
+                           int32_t* d_err, cudaStream_t st);
+
 int max_fp64_ensemble();  // largest N the FP64 kernels accept
 int max_ensemble();       // largest N of the mixed-precision form
 

@@ -18,7 +18,12 @@ from . import oakref
 
 def _locfun_t(r):
     r1 = (((-r / 4.0 + 0.5) * r + 5.0 / 8.0) * r - 5.0 / 3.0) * r * r + 1.0
-    r2 = ((((r / 12.0 - 0.5) * r + 5.0 / 8.0) * r + 5.0 / 3.0) * r - 5.0) * r + 4.0 - 2.0 / (3.0 * r)
+    # the 1 < r <= 2 branch is evaluated at a safe argument elsewhere: torch.where passes the
+    # gradient through both branches, and 2/(3r) at r = 0 (an observation at the zone's own
+    # position) would make it NaN
+    rs = torch.where(r > 1.0, r, torch.ones_like(r))
+    r2 = ((((rs / 12.0 - 0.5) * rs + 5.0 / 8.0) * rs + 5.0 / 3.0) * rs - 5.0) * rs + 4.0 \
+        - 2.0 / (3.0 * rs)
     return torch.where(r <= 1.0, r1, torch.where(r <= 2.0, r2, torch.zeros_like(r)))
 
 

@@ -134,3 +134,38 @@ def test_ensemble_size_limits(oakg):
                               c.zone_pos, c.obs_pos, c.corr_len, c.max_len, weight=c.weight,
                               precision=prec)
         assert ei.value.code == oakg.ERR_ARGS and "128" in str(ei.value)
+
+
+# the tensor-core update (3xTF32, the default) against the CUDA-core FP32 update: both give
+# FP32-level products, so they agree far below the mixed-form bar; ragged zones longer than a
+# 128-row tile, N not a multiple of 8 or 32, FP64 and FP32 storage
+@pytest.mark.parametrize("N,f32", [(16, False), (37, False), (64, True), (100, True),
+                                   (113, False), (128, True)])
+def test_tensor_core_update_matches_cuda_core_update(oakg, N, f32):
+    rng = np.random.default_rng(700 + N)
+    Z = 40
+    zs = rng.integers(1, 300, Z).astype(np.int32)   # some zones span up to three row tiles
+    n, m = int(zs.sum()), 500
+    Sf = np.asfortranarray(rng.standard_normal((n, N)) * 0.1)
+    HSf = np.asfortranarray(rng.standard_normal((m, N)) * 0.1)
+    xf, Hxf = rng.standard_normal(n), rng.standard_normal(m) * 0.1
+    yo = Hxf + rng.standard_normal(m) * 0.1
+    r = rng.uniform(0.01, 0.1, m)
+    zone_pos = np.column_stack([rng.uniform(0, 30, Z), rng.uniform(0, 30, Z), np.zeros(Z),
+                                np.zeros(Z)])
+    zone_pos[:4, :2] = 100.0   # far from every observation: copied zones
+    obs_pos = (rng.uniform(0, 30, m), rng.uniform(0, 30, m), np.zeros(m), np.zeros(m))
+    corr, maxl = np.full(Z, 4.0), np.full(Z, 8.0)
+    dt = np.float32 if f32 else np.float64
+    args = (zs, xf.astype(dt), Hxf.astype(dt), yo.astype(dt), np.asfortranarray(Sf.astype(dt)),
+            np.asfortranarray(HSf.astype(dt)), r.astype(dt), zone_pos, obs_pos, corr, maxl)
+    kw = dict(weight=1, precision=oakg.PREC_MIXED)
+    xa_t, Sa_t, _, nobs = oakg.loc_analysis(*args, **kw)
+    xa_s, Sa_s, _, nobs_s = oakg.loc_analysis(*args, simt_update=True, **kw)
+    assert np.array_equal(nobs, nobs_s) and (nobs > 0).any() and (nobs == 0).any()
+    xa_t, Sa_t, xa_s, Sa_s = (a.astype(np.float64) for a in (xa_t, Sa_t, xa_s, Sa_s))
+    e_mean = np.linalg.norm(xa_t - xa_s) / np.linalg.norm(xa_s - xf.astype(dt))
+    e_anom = np.linalg.norm(Sa_t - Sa_s) / np.linalg.norm(Sa_s)
+    assert e_mean < 1e-5 and e_anom < 1e-5, (e_mean, e_anom)
+    empty = np.repeat(nobs == 0, zs)
+    assert np.array_equal(Sa_t[empty], Sf.astype(dt)[empty].astype(np.float64))
