@@ -50,7 +50,8 @@ module oakg
   integer(c_int32_t), parameter :: OAKG_METRIC_CARTESIAN = 0, OAKG_METRIC_SPHERICAL = 1, &
        OAKG_METRIC_SPHERICAL_APPROX = 2
   ! precision of the local analysis
-  integer(c_int32_t), parameter :: OAKG_PREC_FP64 = 0, OAKG_PREC_MIXED = 1
+  integer(c_int32_t), parameter :: OAKG_PREC_FP64 = 0, OAKG_PREC_MIXED = 1, &
+       OAKG_PREC_MIXED_FP64EIG = 2
   ! oakg_loc%flags
   integer(c_int32_t), parameter :: OAKG_FLAG_AMPL_ALWAYS = 1, OAKG_FLAG_BRUTE_SEARCH = 2, &
        OAKG_FLAG_SIMT_UPDATE = 4

@@ -72,8 +72,13 @@ extern "C" {
 #define OAKG_PREC_FP64 0  /* every product in FP64 (the plain form)                     */
 #define OAKG_PREC_MIXED 1 /* FP64 selection and (1+lambda)^-1/2, (1+lambda)^-1 scalings;
                              Gram (tensor cores, chunked FP32 accumulation), eigensolve and
-                             update in FP32, compensated innovation sums
-                             (relative analysis error ~1e-5). Both forms take N <= 128.    */
+                             update (tensor cores, 3xTF32) in FP32, compensated innovation
+                             sums (relative analysis error ~1e-5). All forms take N <= 128. */
+#define OAKG_PREC_MIXED_FP64EIG 2 /* OAKG_PREC_MIXED with the FP32 eigenpairs refined to
+                             FP64 accuracy (Ogita-Aishima iterative refinement, exact
+                             products of the FP32 eigenvectors and G) before T and the
+                             amplitudes are formed: FP64 accuracy kept for the eigensolve
+                             and the (1+lambda) scalings only                              */
 
 /* oakg_loc.flags */
 #define OAKG_FLAG_AMPL_ALWAYS 1 /* write amplitudes for every analysed zone (the reference
@@ -82,8 +87,9 @@ extern "C" {
                                     O(Z m) loop, assimilation.F90:3745-3757) instead of the
                                     cell-grid search; same results, for validation         */
 #define OAKG_FLAG_SIMT_UPDATE 4  /* mixed form: the ensemble update on the CUDA cores (FP32
-                                    FMA) instead of the tensor cores (3xTF32); both give
-                                    FP32-level products, for comparison                    */
+                                    FMA) instead of the tensor cores (3xTF32, used when the
+                                    longest zone has at least 48 elements); both give
+                                    FP32-level products                                    */
 
 typedef struct {
   int64_t n;        /* state vector size                                        */

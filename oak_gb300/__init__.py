@@ -25,7 +25,7 @@ import os
 import numpy as np
 
 __all__ = ["analysis", "loc_analysis", "loc_analysis_adjoint", "OakError", "lib", "last_timings", "release",
-           "PREC_FP64", "PREC_MIXED",
+           "PREC_FP64", "PREC_MIXED", "PREC_MIXED_FP64EIG",
            "GAUSS_CUTOFF", "GASPARI_COHN", "CARTESIAN", "SPHERICAL", "SPHERICAL_APPROX",
            "zone_positions", "ensemble_prologue", "ensemble_epilogue", "ens_loc_analysis",
            "ens2sqrt", "sqrt2ens", "ens_analysis", "biased_loc_analysis", "Plan",
@@ -41,7 +41,7 @@ ERR_ARGS, ERR_CUDA, ERR_NAN, ERR_EIG, ERR_NOMEM, ERR_TIMEOUT, ERR_INIT, ERR_NOTI
 MEM_HOST, MEM_DEVICE = 0, 1
 GAUSS_CUTOFF, GASPARI_COHN = 0, 1
 CARTESIAN, SPHERICAL, SPHERICAL_APPROX = 0, 1, 2
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_MIXED_FP64EIG = 0, 1, 2
 FLAG_AMPL_ALWAYS, FLAG_BRUTE_SEARCH, FLAG_SIMT_UPDATE = 1, 2, 4
 
 
@@ -354,8 +354,9 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     Returns ``(xa, Sa, amplitudes (N, Z), nobs (Z,))``. As in the reference, amplitudes are
     only written for the non-localised branch unless ``ampl_always`` is set. ``out`` may give
     preallocated ``(xa, Sa)`` arrays of the same memory kind as the inputs (e.g. pinned host
-    arrays). ``precision``: PREC_FP64 (plain form) or PREC_MIXED (FP32 Gram, eigensolve and
-    update; FP64 selection and eigenvalue scalings). ``smw_B`` (m x k): the observation error
+    arrays). ``precision``: PREC_FP64 (plain form), PREC_MIXED (FP32 Gram, eigensolve and
+    update; FP64 selection and eigenvalue scalings) or PREC_MIXED_FP64EIG (PREC_MIXED with the
+    eigenpairs refined to FP64 accuracy). ``smw_B`` (m x k): the observation error
     covariance R = diag(r_diag) + B B^T (SMWCovar, covariance.F90:464-570; FP64 form).
     ``simt_update``: the mixed form's ensemble update on the CUDA cores instead of the tensor
     cores.

@@ -74,7 +74,8 @@ enum BufId {
   B_ORDER, B_C_E, B_C_MEAN, B_C_S, B_C_OM, B_C_EO, B_C_HE, B_C_HXF, B_C_HSF, B_C_XA, B_C_SA,
   B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_SMWB, B_HSTA, B_GAUG,
   B_GVAUG, B_GLOB, B_L_PART, B_L_WORK, B_L_ZS, B_L_ZI, B_L_INV, B_L_X, B_L_Y, B_L_IDX, B_L_MASK,
-  B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_HXF64, B_YO64, B_R64, B_COUNT_
+  B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_HXF64, B_YO64, B_R64, B_G0, B_SREF,
+  B_COUNT_
 };
 
 struct Ctx {
@@ -263,6 +264,8 @@ struct ChunkArgs {
   // FP32 storage at the boundary (oakg_locanalysis_f32): these state arrays replace the five
   // above, which are then null
   bool store32 = false;
+  // mixed form: refine the FP32 eigenpairs to FP64 accuracy (OAKG_PREC_MIXED_FP64EIG)
+  bool refine = false;
   const float *xf32 = nullptr, *Sf32 = nullptr;
   float *xa32 = nullptr, *Sa32 = nullptr, *ampl32 = nullptr;
   // optional pick order of the selection + Gram stage (chunk-local zone indices, Z entries)
@@ -309,7 +312,8 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   const int NA = N + a.smw_k;
   const size_t per_zone =
       ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) * sizeof(R) + 2 * sizeof(int32_t) +
-      (a.smw_k > 0 ? ((size_t)NA * NA + NA) * sizeof(double) : 0);
+      (a.smw_k > 0 ? ((size_t)NA * NA + NA) * sizeof(double) : 0) +
+      (a.refine ? ((size_t)N * N + zone_refine_scratch(N)) * sizeof(float) : 0);
   int64_t chunk = c->chunk_override > 0 ? c->chunk_override
                                         : (int64_t)(chunk_budget_bytes() / per_zone);
   // host-memory calls: the Sf rows of every chunk go in while the selection, Gram and
@@ -327,6 +331,11 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   if ((rc = scratch(c, B_WORK, 8, &d_work, "work counters"))) return rc;
   if ((rc = scratch(c, B_AUX, (size_t)chunk * zone_eig_aux(N), &d_aux, "zone aux"))) return rc;
   if ((rc = scratch(c, B_ZVEC, (size_t)chunk * N * N, &d_zvec, "zone eigenvectors"))) return rc;
+  float *d_G0 = nullptr, *d_Sref = nullptr;
+  if (a.refine && ((rc = scratch(c, B_G0, (size_t)chunk * N * N, &d_G0, "zone Gram copies")) ||
+                   (rc = scratch(c, B_SREF, (size_t)chunk * zone_refine_scratch(N), &d_Sref,
+                                 "refinement scratch"))))
+    return rc;
   double *d_Ga = nullptr, *d_ga = nullptr;
   if (a.smw_k > 0 && ((rc = scratch(c, B_GAUG, (size_t)chunk * NA * NA, &d_Ga, "augmented Gram")) ||
                       (rc = scratch(c, B_GVAUG, (size_t)chunk * NA, &d_ga, "augmented g"))))
@@ -351,11 +360,15 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   char* dSa = a.store32 ? (char*)a.Sa32 : (char*)a.Sa;
   char* dxa = a.store32 ? (char*)a.xa32 : (char*)a.xa;
   // the update of zones [zz0, zz0 + nq) (T and amplitudes at the chunk-local slot)
-  // (mixed form: on the tensor cores unless OAKG_FLAG_SIMT_UPDATE asks for the CUDA cores)
+  // (mixed form: on the tensor cores unless OAKG_FLAG_SIMT_UPDATE asks for the CUDA cores or
+  // the zones are shorter than kTcUpdateMinRows rows: the MMA tile is 128 rows, so for short
+  // zones it would be mostly padding and the CUDA-core kernel, which stages T once per zone
+  // for all its rows, is faster)
+  constexpr int32_t kTcUpdateMinRows = 48;
   auto update = [&](int32_t zz0, int32_t nq, const R* T, const R* za,
                     const int32_t* nb) -> cudaError_t {
     if constexpr (std::is_same<R, float>::value) {
-      if (!(a.lp.flags & OAKG_FLAG_SIMT_UPDATE))
+      if (!(a.lp.flags & OAKG_FLAG_SIMT_UPDATE) && a.zone_max >= kTcUpdateMinRows)
         return a.store32 ? zone_update_tc(N, zz0, nq, a.zstart, a.xf32, a.Sf32, a.ldS, T, za, nb,
                                           a.xa32, a.Sa32, *status_all, st)
                          : zone_update_tc(N, zz0, nq, a.zstart, a.xf, a.Sf, a.ldS, T, za, nb,
@@ -415,8 +428,18 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
       continue;
     }
     if (timed) cudaEventRecord(c->ev[3], st);
-    e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate, d_za,
-               d_status, d_aux, d_zvec, d_work + 4, st);
+    if constexpr (std::is_same<R, float>::value) {
+      if (a.refine)
+        e = zone_eig_fp32_refined(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0),
+                                  a.lp.rotate, d_za, d_status, d_aux, d_zvec, d_work + 4, d_G0,
+                                  d_Sref, st);
+      else
+        e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate,
+                   d_za, d_status, d_aux, d_zvec, d_work + 4, st);
+    } else {
+      e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate, d_za,
+                 d_status, d_aux, d_zvec, d_work + 4, st);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
     if (timed) cudaEventRecord(c->ev[4], st);
     if (!pipe) {
@@ -502,7 +525,8 @@ int check_loc(const oakg_dims* dims, const oakg_loc* loc, int32_t Z) {
                 loc->metric);
   if (loc->loctype < 1 || loc->loctype > 3)
     return fail(OAKG_ERR_ARGS, "loctype must be 1, 2 or 3 (got %d)", loc->loctype);
-  if (loc->precision != OAKG_PREC_FP64 && loc->precision != OAKG_PREC_MIXED)
+  if (loc->precision != OAKG_PREC_FP64 && loc->precision != OAKG_PREC_MIXED &&
+      loc->precision != OAKG_PREC_MIXED_FP64EIG)
     return fail(OAKG_ERR_ARGS, "unknown precision mode %d", loc->precision);
   if (loc->precision == OAKG_PREC_FP64 && dims->N > max_fp64_ensemble())
     return fail(OAKG_ERR_ARGS, "the FP64 form takes N <= %d (N=%d: use OAKG_PREC_MIXED)",
@@ -544,7 +568,7 @@ int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH,
     so.HSt = d_hst;
     so.cell_start = d_cstart;
     so.perm = d_perm;
-    if (loc->precision == OAKG_PREC_MIXED) {
+    if (loc->precision != OAKG_PREC_FP64) {
       float* d_hst32;
       if ((rc = scratch(c, B_HST32, (size_t)m * N, &d_hst32, "obs rows (FP32)"))) return rc;
       if ((e = rows_to_fp32(d_hst, d_hst32, m * N, st)) != cudaSuccess)
@@ -821,7 +845,8 @@ int locanalysis_impl(const oakg_dims* dims, const oakg_loc* loc, int32_t Z,
     ca.hst_aug = d_hsta;
   }
   double t_gram = 0, t_eig = 0, t_upd = 0;
-  rc = (loc->precision == OAKG_PREC_MIXED)
+  ca.refine = (loc->precision == OAKG_PREC_MIXED_FP64EIG);
+  rc = (loc->precision != OAKG_PREC_FP64)
            ? run_chunks<float>(c, ca, &d_status_all, &t_gram, &t_eig, &t_upd)
            : run_chunks<double>(c, ca, &d_status_all, &t_gram, &t_eig, &t_upd);
   if (rc) return rc;
@@ -1101,7 +1126,7 @@ int plan_run(Plan* pl, RunMode mode, double* t_gram) {
 }
 
 int plan_run_mode(Plan* pl, RunMode mode, double* t_gram = nullptr) {
-  return (pl->loc.precision == OAKG_PREC_MIXED) ? plan_run<float>(pl, mode, t_gram)
+  return (pl->loc.precision != OAKG_PREC_FP64) ? plan_run<float>(pl, mode, t_gram)
                                                 : plan_run<double>(pl, mode, t_gram);
 }
 
@@ -1146,6 +1171,7 @@ int plan_create_impl(Plan** out, const oakg_dims* dims, const oakg_loc* loc, int
     pl->ca = ChunkArgs{pl->P.g, pl->P.so, lp, Z, N, dims->ldS, pl->P.zone_max, pl->P.brute,
                        all_ampl, pl->P.zxyzt, pl->P.corr, pl->P.maxl, pl->P.zstart, pl->P.xf,
                        pl->P.Sf, xa, Sa, ampl, d_nobs};
+    pl->ca.refine = (lc->precision == OAKG_PREC_MIXED_FP64EIG);
     return OAKG_OK;
   };
   oakg_loc lc = *loc;
@@ -1188,8 +1214,11 @@ int plan_create_impl(Plan** out, const oakg_dims* dims, const oakg_loc* loc, int
   {
     const size_t per_zone =
         ((size_t)N * N * 2 + (size_t)N * 2 + zone_eig_aux(N)) *
-            (lc.precision == OAKG_PREC_MIXED ? sizeof(float) : sizeof(double)) +
-        2 * sizeof(int32_t);
+            (lc.precision != OAKG_PREC_FP64 ? sizeof(float) : sizeof(double)) +
+        2 * sizeof(int32_t) +
+        (lc.precision == OAKG_PREC_MIXED_FP64EIG
+             ? ((size_t)N * N + zone_refine_scratch(N)) * sizeof(float)
+             : 0);
     const int64_t chunk = (int64_t)(chunk_budget_bytes() / per_zone);
     c->chunk_override = std::max<int64_t>(1, std::min<int64_t>(chunk, Z));
   }

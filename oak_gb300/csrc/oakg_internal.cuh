@@ -167,6 +167,16 @@ cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,
                           const int32_t* d_nobs, int rotate, float* d_ampl, int32_t* d_status,
                           float* d_aux, float* d_Z, int32_t* d_work, cudaStream_t st);
 size_t zone_eig_aux(int N);
+// zone_eig_fp32 with the FP32 eigenpairs refined to FP64 accuracy (Ogita-Aishima) before T and
+// the amplitudes are formed (zone_refine.cu): d_G0 (N x N floats a zone) keeps G, d_S holds
+// zone_refine_scratch(N) floats a zone; N <= 128.
+cudaError_t zone_eig_fp32_refined(int N, int32_t nzc, float* d_GT, const float* d_g,
+                                  const int32_t* d_nobs, int rotate, float* d_ampl,
+                                  int32_t* d_status, float* d_aux, float* d_Z, int32_t* d_work,
+                                  float* d_G0, float* d_S, cudaStream_t st);
+size_t zone_refine_scratch(int N);
+cudaError_t zone_eig_refine(int N, int32_t nzc, const float* d_G0, float* d_Z, float* d_aux,
+                            const int32_t* d_nobs, float* d_S, cudaStream_t st);
 
 // ---- zone_eig32.cu: FP32 stages for N <= eig32_max_n() (one block per zone), used by
 // zone_eig_fp32 (same arguments as its stages)
@@ -177,17 +187,17 @@ cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs
                          int32_t* d_status, cudaStream_t st);
 cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
                           const int32_t* d_nobs, cudaStream_t st);
-cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
-                            const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
-                            float* d_ampl, int32_t* d_status, cudaStream_t st);
+cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux, float* d_Z,
+                            const float* d_g, const int32_t* d_nobs, int rotate, float* d_ampl,
+                            int32_t* d_status, cudaStream_t st, int mode = 0);
 // E1 and E3 for eig32_max_n() < N <= eig128_max_n() (one 128-thread block per zone; E2 is the
 // generic one)
 int eig128_max_n();
 cudaError_t eig128_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
                            cudaStream_t st);
-cudaError_t eig128_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
-                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
-                             float* d_ampl, int32_t* d_status, cudaStream_t st);
+cudaError_t eig128_transform(int N, int32_t nzc, float* d_GT, const float* d_aux, float* d_Z,
+                             const float* d_g, const int32_t* d_nobs, int rotate, float* d_ampl,
+                             int32_t* d_status, cudaStream_t st, int mode = 0);
 
 // ---- ensemble.cu: the ensemble prologue (mean, anomalies, sparse H E + Hshift) and epilogue
 // (inflation, correction clip, reconstruction); HEf_scratch holds m x N values.

@@ -507,15 +507,19 @@ __global__ void __launch_bounds__(128)
   for (int i = 0; i < N; i++) zj[i] = x[i];
 }
 
-// E2b for N <= 64 in FP64: one block of kT64 = 64 threads per zone, thread j = eigenpair j,
-// with the arithmetic of k_eig_tridiag_vectors<double> (same LU, start vector and two solves;
-// reciprocals by Newton steps and a power-of-two prescaling before the normalisation, so the
-// vectors agree to rounding). The per-thread factor arrays of the generic kernel
-// live in local memory, and with thousands of threads per SM they go to DRAM (most of the
-// eigensolve's traffic); here the partial-pivoting LU is recomputed in each forward sweep
-// (fused with the elimination), the upper factor is kept in shared memory ([i][j] layout:
-// consecutive threads, consecutive words) and the iterate in registers (loops unrolled to 64).
-constexpr int kT64 = 64;
+// E2b for N <= 64 in FP64: blocks of kT64 = 32 threads (one warp), two per zone, thread j =
+// eigenpair j, with the arithmetic of k_eig_tridiag_vectors<double> (same LU, start vector
+// and two solves; reciprocals by Newton steps and a power-of-two prescaling before the
+// normalisation, so the vectors agree to rounding). The per-thread factor arrays of the generic
+// kernel live in local memory, and with thousands of threads per SM they go to DRAM (most of
+// the eigensolve's traffic); here the partial-pivoting LU is recomputed in each forward sweep
+// (fused with the elimination), the iterate is kept in registers (loops unrolled to 64), the
+// factor's first superdiagonal and pivot reciprocals in shared memory ([i][j] layout:
+// consecutive threads, consecutive words) and its second superdiagonal as one bit per row (it
+// is the tridiagonal's next off-diagonal entry where rows were swapped, else 0). 32 KB a
+// block: seven warps per SM.
+constexpr int kT64 = 32;
+constexpr int kNV64 = 64;
 
 // 1/p by two Newton steps from the FP32 reciprocal (relative error below 2^-52, not always
 // correctly rounded). The IEEE FP64 division is a called routine whose call keeps the live
@@ -548,18 +552,17 @@ __device__ __forceinline__ double pow2_inv_exponent(double x) {
 __global__ void __launch_bounds__(kT64)
     k_eig_vectors_fp64(int N, int32_t nzc, const double* __restrict__ aux,
                        double* __restrict__ Zg, const int32_t* __restrict__ nobs) {
-  constexpr int NV = kT64;
-  extern __shared__ __align__(16) double sfac64[];  // u1, u2, 1/pivot: [i][j] each
-  __shared__ double sd[NV], se[NV];
+  constexpr int NV = kNV64;
+  extern __shared__ __align__(16) double sfac64[];  // u1, 1/pivot: [i][jl] each
+  __shared__ double sd[NV], se[NV + 1];
   double* su1 = sfac64;
-  double* su2 = sfac64 + NV * kT64;
-  double* sui = sfac64 + 2 * NV * kT64;
-  const int j = threadIdx.x;
+  double* sui = sfac64 + NV * kT64;
+  const int jl = threadIdx.x, j = kT64 * blockIdx.y + jl;  // eigenpair j
   const int32_t zl = blockIdx.x;
   if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
   const double* ax = aux + (int64_t)zl * aux_stride(N);
-  for (int i = j; i < N; i += kT64) {
-    sd[i] = ax[i];
+  for (int i = jl; i <= NV; i += kT64) {
+    if (i < NV) sd[i] = (i < N) ? ax[i] : 0.0;
     se[i] = (i < N - 1) ? ax[N + i] : 0.0;
   }
   __syncthreads();
@@ -582,22 +585,23 @@ __global__ void __launch_bounds__(kT64)
       h ^= h >> 13;
       x[i] = (i < N) ? (double)(h & 0xffffff) * (1.0 / 16777216.0) - 0.5 : 0.0;
     }
+    unsigned long long piv = 0ull;  // bit i: rows i and i + 1 swapped in step i
 #pragma unroll 1
     for (int it = 0; it < 2; it++) {
       double cd = sd[0] - l, csup = (N > 1) ? se[0] : 0.0;
 #pragma unroll
       for (int i = 0; i < NV - 1; i++) {
         if (i < N - 1) {
-          const double sub = se[i], dg = sd[i + 1] - l, sp = (i + 1 < N - 1) ? se[i + 1] : 0.0;
+          const double sub = se[i], dg = sd[i + 1] - l, sp = se[i + 1];  // se[i + 1] = 0 past N - 2
           const bool swap = fabs(cd) < fabs(sub);
           double pivot = swap ? sub : cd;
           if (!swap && fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
           const double ui = rcp_newton(pivot);
           const double li = (swap ? cd : sub) * ui;
           if (it == 0) {
-            su1[i * kT64 + j] = swap ? dg : csup;
-            su2[i * kT64 + j] = swap ? sp : 0.0;
-            sui[i * kT64 + j] = ui;
+            su1[i * kT64 + jl] = swap ? dg : csup;
+            sui[i * kT64 + jl] = ui;
+            if (swap) piv |= 1ull << i;
           }
           const double aa = swap ? csup : dg, bb = swap ? dg : csup;
           cd = fma(-li, bb, aa);
@@ -611,12 +615,10 @@ __global__ void __launch_bounds__(kT64)
       if (it == 0) {
         double pivot = cd;
         if (fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
-        sui[(N - 1) * kT64 + j] = rcp_newton(pivot);
+        sui[(N - 1) * kT64 + jl] = rcp_newton(pivot);
         // the factor has no entries right of the last column: zeros make one formula serve
         // every row (x beyond N is 0)
-        su1[(N - 1) * kT64 + j] = 0.0;
-        su2[(N - 1) * kT64 + j] = 0.0;
-        su2[(N - 2) * kT64 + j] = 0.0;
+        su1[(N - 1) * kT64 + jl] = 0.0;
       }
       // back substitution x[i] = (x[i] - u1 x[i+1] - u2 x[i+2]) / p; every index is a
       // compile-time constant after unrolling (guards compare with N, never select by it), so
@@ -625,9 +627,12 @@ __global__ void __launch_bounds__(kT64)
       for (int i = NV - 1; i >= 0; i--) {
         if (i < N) {
           double v = x[i];
-          if (i + 1 < NV) v = fma(-su1[i * kT64 + j], x[i + 1], v);
-          if (i + 2 < NV) v = fma(-su2[i * kT64 + j], x[i + 2], v);
-          x[i] = v * sui[i * kT64 + j];
+          if (i + 1 < NV) v = fma(-su1[i * kT64 + jl], x[i + 1], v);
+          if (i + 2 < NV) {
+            const double u2 = ((piv >> i) & 1ull) ? se[i + 1] : 0.0;
+            v = fma(-u2, x[i + 2], v);
+          }
+          x[i] = v * sui[i * kT64 + jl];
         }
       }
       // scale by a power of two near 1/max|x| (the sum of squares cannot overflow), then
@@ -653,12 +658,14 @@ __global__ void __launch_bounds__(kT64)
   __syncthreads();  // factors no longer read: reuse them as the transpose buffer
   double* tr = sfac64;  // [i][kT64 + 1]
 #pragma unroll
-  for (int i = 0; i < NV; i++) tr[i * (kT64 + 1) + j] = x[i];
+  for (int i = 0; i < NV; i++) tr[i * (kT64 + 1) + jl] = x[i];
   __syncthreads();
-  // vectors (rows of Z), coalesced along the rows
-  for (int idx = j; idx < N * N; idx += kT64) {
+  // this block's vectors kT64 blockIdx.y + jj (rows of Z), coalesced along the rows
+  const int j0 = kT64 * blockIdx.y;
+  const int nv = (N - j0 < kT64) ? N - j0 : kT64;
+  for (int idx = jl; idx < nv * N; idx += kT64) {
     const int jj = idx / N, i = idx - jj * N;
-    Zz[(int64_t)jj * N + i] = tr[i * (kT64 + 1) + jj];
+    Zz[(int64_t)(j0 + jj) * N + i] = tr[i * (kT64 + 1) + jj];
   }
 }
 
@@ -1007,12 +1014,13 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
                              const float* d_Z, const float* d_g, const int32_t* d_nobs,
                              int rotate, float* d_ampl, int32_t* d_status, int32_t* d_work,
                              cudaStream_t st) {
+  // mode 0 does not write Z
   if (N <= eig32_max_n())
-    return eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
-                           st);
+    return eig32_transform(N, nzc, d_GT, d_aux, const_cast<float*>(d_Z), d_g, d_nobs, rotate,
+                           d_ampl, d_status, st);
   if (N <= eig128_max_n())
-    return eig128_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
-                            st);
+    return eig128_transform(N, nzc, d_GT, d_aux, const_cast<float*>(d_Z), d_g, d_nobs, rotate,
+                            d_ampl, d_status, st);
   size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(float) + (size_t)N * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
@@ -1033,12 +1041,13 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
   } else {
     k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   }
-  if (sizeof(R) == sizeof(double) && N <= kT64) {
-    const size_t smem = (size_t)3 * kT64 * kT64 * sizeof(double);
+  if (sizeof(R) == sizeof(double) && N <= kNV64) {
+    const size_t smem = (size_t)2 * kNV64 * kT64 * sizeof(double);
     cudaError_t e = cudaFuncSetAttribute(k_eig_vectors_fp64,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_eig_vectors_fp64<<<(unsigned)(nzc > 0 ? nzc : 1), kT64, smem, st>>>(
+    const unsigned yb = (unsigned)((N + kT64 - 1) / kT64);
+    k_eig_vectors_fp64<<<dim3((unsigned)(nzc > 0 ? nzc : 1), yb), kT64, smem, st>>>(
         N, nzc, reinterpret_cast<const double*>(d_aux), reinterpret_cast<double*>(d_Z), d_nobs);
     return cudaSuccess;
   }
@@ -1100,6 +1109,43 @@ cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,
                           float* d_aux, float* d_Z, int32_t* d_work, cudaStream_t st) {
   return zone_eig_impl<float>(N, nzc, d_GT, d_g, d_nobs, rotate, d_ampl, d_status, d_aux, d_Z,
                               d_work, st);
+}
+
+// The FP32 eigensolve with its eigenpairs refined to FP64 accuracy before the transform: G is
+// kept in d_G0 (E1 overwrites it with reflectors), E3 stops after the back-transform and leaves
+// the eigenvectors of G in d_Z, zone_eig_refine refines them and the eigenvalues in place (its
+// S scratch: zone_refine_scratch(N) floats a zone), and E3 forms T and the amplitudes from
+// them.
+cudaError_t zone_eig_fp32_refined(int N, int32_t nzc, float* d_GT, const float* d_g,
+                                  const int32_t* d_nobs, int rotate, float* d_ampl,
+                                  int32_t* d_status, float* d_aux, float* d_Z, int32_t* d_work,
+                                  float* d_G0, float* d_S, cudaStream_t st) {
+  if (N < 2 || N > eig128_max_n()) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int32_t) * (nzc > 0 ? nzc : 1), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(d_work, 0, 2 * sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(d_G0, d_GT, sizeof(float) * (size_t)nzc * N * N, cudaMemcpyDeviceToDevice,
+                      st);
+  if (e != cudaSuccess) return e;
+  e = launch_e1<float>(N, nzc, d_GT, d_aux, d_nobs, d_work, st);
+  if (e != cudaSuccess) return e;
+  e = launch_e2<float>(N, nzc, d_aux, d_Z, d_nobs, d_status, st);
+  if (e != cudaSuccess) return e;
+  e = (N <= eig32_max_n())
+          ? eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, st, 1)
+          : eig128_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, st,
+                             1);
+  if (e != cudaSuccess) return e;
+  e = zone_eig_refine(N, nzc, d_G0, d_Z, d_aux, d_nobs, d_S, st);
+  if (e != cudaSuccess) return e;
+  e = (N <= eig32_max_n())
+          ? eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, st, 2)
+          : eig128_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, st,
+                             2);
+  if (e != cudaSuccess) return e;
+  count_launches(5);
+  return cudaGetLastError();
 }
 
 }  // namespace oakg

@@ -358,11 +358,14 @@ __device__ __forceinline__ void mgs_owner(float (&x)[NB], int c, Zone3& zs) {
   if (!ok) zs.flag[c] = 0;
 }
 
+// mode 0: the whole stage; 1: stop after the back-transform and write the eigenvectors of G
+// (vector-major, over Z); 2: start from eigenvectors of G given in Z (refined, with their
+// eigenvalues in aux) and form T and the amplitudes.
 __global__ void __launch_bounds__(32 * kZpb3, 4)
     k_eig_transform32(int N, int32_t nzc, float* __restrict__ GT, const float* __restrict__ aux,
-                      const float* __restrict__ Zg, const float* __restrict__ gv,
+                      float* __restrict__ Zg, const float* __restrict__ gv,
                       const int32_t* __restrict__ nobs, int rotate, float* __restrict__ ampl_out,
-                      int32_t* __restrict__ status) {
+                      int32_t* __restrict__ status, int mode) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   const int lane = threadIdx.x & 31, wz = threadIdx.x >> 5;
   Zone3& zs = reinterpret_cast<Zone3*>(sm_raw)[wz];
@@ -370,7 +373,7 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
   if (zl >= nzc || nobs[zl] == 0) return;  // warp-uniform; warp-level synchronisation only
   float* Gz = GT + (int64_t)zl * N * N;
   const float* ax = aux + (int64_t)zl * aux_stride32(N);
-  const float* Zz = Zg + (int64_t)zl * N * N;
+  float* Zz = Zg + (int64_t)zl * N * N;
   const int j0 = lane, j1 = lane + 32;
   float* buf = zs.buf;
 #pragma unroll
@@ -394,6 +397,7 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
     x1[i] = (j1 < N) ? ((i < N) ? Zz[(int64_t)j1 * N + i] : 0.f) : ((i == j1) ? 1.f : 0.f);
   }
   __syncwarp();
+  if (mode != 2) {  // eigenvectors of Tri: orthogonalisation and back-transform
   // modified Gram-Schmidt on the eigenvectors of Tri (the back-transform below is orthogonal),
   // largest eigenvalue first: vector c is final once every larger-eigenvalue vector has been
   // projected out of it. A vector that keeps at least half its squared norm is orthogonal to
@@ -558,6 +562,15 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
     vdot2(x0, x1, vk, g0, true, d0, d1);
     vaxpy2(x0, x1, bk * d0, bk * d1, vk, g0, true, true);
   }
+  if (mode == 1) {  // the eigenvectors of G for the refinement; this lane's rows of Z only
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+      if (j0 < N && i < N) Zz[(int64_t)j0 * N + i] = x0[i];
+      if (j1 < N && i < N) Zz[(int64_t)j1 * N + i] = x1[i];
+    }
+    return;
+  }
+  }  // mode != 2
   __syncwarp();  // the reflectors are read: buf holds U from here on
   vstore(x0, buf + j0 * LDV);
   vstore(x1, buf + j1 * LDV);
@@ -1127,11 +1140,12 @@ __device__ __forceinline__ void vaxpy128(float (&x)[NB2], float f, const float* 
   }
 }
 
+// mode as for k_eig_transform32
 __global__ void __launch_bounds__(NB2, 3)
     k_eig_transform128(int N, int32_t nzc, float* __restrict__ GT, const float* __restrict__ aux,
-                       const float* __restrict__ Zg, const float* __restrict__ gv,
+                       float* __restrict__ Zg, const float* __restrict__ gv,
                        const int32_t* __restrict__ nobs, int rotate,
-                       float* __restrict__ ampl_out, int32_t* __restrict__ status) {
+                       float* __restrict__ ampl_out, int32_t* __restrict__ status, int mode) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   Zone128& zs = *reinterpret_cast<Zone128*>(sm_raw);
   const int t = threadIdx.x;
@@ -1139,7 +1153,7 @@ __global__ void __launch_bounds__(NB2, 3)
   if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
   float* Gz = GT + (int64_t)zl * N * N;
   const float* ax = aux + (int64_t)zl * aux_stride32(N);
-  const float* Zz = Zg + (int64_t)zl * N * N;
+  float* Zz = Zg + (int64_t)zl * N * N;
   float* buf = zs.buf;
   const int ng = (N + 15) >> 4;  // 16-component groups holding the N components
   {
@@ -1159,6 +1173,7 @@ __global__ void __launch_bounds__(NB2, 3)
   for (int i = 0; i < NB2; i++)
     x[i] = (t < N) ? ((i < N) ? Zz[(int64_t)t * N + i] : 0.f) : ((i == t) ? 1.f : 0.f);
   __syncthreads();
+  if (mode != 2) {  // eigenvectors of Tri: orthogonalisation and back-transform (block-uniform)
   // modified Gram-Schmidt on the eigenvectors of Tri, largest eigenvalue first, with the
   // acceptance test and residual-keeping of k_eig_transform32
   for (int c = N - 1; c >= 0; c--) {
@@ -1272,6 +1287,13 @@ __global__ void __launch_bounds__(NB2, 3)
     const int g0 = (k + 1) >> 4;
     vaxpy128(x, bk * vdot128(x, vk, g0, ng), vk, g0, ng);
   }
+  if (mode == 1) {  // the eigenvectors of G for the refinement; this thread's row of Z only
+#pragma unroll
+    for (int i = 0; i < NB2; i++)
+      if (t < N && i < N) Zz[(int64_t)t * N + i] = x[i];
+    return;
+  }
+  }  // mode != 2
   __syncthreads();  // the reflectors are read: buf holds U from here on
   vstore(x, buf + t * LDV2);
   {
@@ -1426,16 +1448,16 @@ cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const i
   return cudaGetLastError();
 }
 
-cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
-                            const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
-                            float* d_ampl, int32_t* d_status, cudaStream_t st) {
+cudaError_t eig32_transform(int N, int32_t nzc, float* d_GT, const float* d_aux, float* d_Z,
+                            const float* d_g, const int32_t* d_nobs, int rotate, float* d_ampl,
+                            int32_t* d_status, cudaStream_t st, int mode) {
   if (N < 2 || N > NB) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform32,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem3);
   if (e != cudaSuccess) return e;
   const int blocks = (nzc + kZpb3 - 1) / kZpb3;
-  k_eig_transform32<<<blocks > 0 ? blocks : 1, 32 * kZpb3, kSmem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
-                                                            d_nobs, rotate, d_ampl, d_status);
+  k_eig_transform32<<<blocks > 0 ? blocks : 1, 32 * kZpb3, kSmem3, st>>>(
+      N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, mode);
   return cudaGetLastError();
 }
 
@@ -1448,16 +1470,16 @@ cudaError_t eig128_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const 
   return cudaGetLastError();
 }
 
-cudaError_t eig128_transform(int N, int32_t nzc, float* d_GT, const float* d_aux,
-                             const float* d_Z, const float* d_g, const int32_t* d_nobs, int rotate,
-                             float* d_ampl, int32_t* d_status, cudaStream_t st) {
+cudaError_t eig128_transform(int N, int32_t nzc, float* d_GT, const float* d_aux, float* d_Z,
+                             const float* d_g, const int32_t* d_nobs, int rotate, float* d_ampl,
+                             int32_t* d_status, cudaStream_t st, int mode) {
   if (N < 2 || N > NB2) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform128,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kSmem128);
   if (e != cudaSuccess) return e;
-  k_eig_transform128<<<nzc > 0 ? nzc : 1, NB2, kSmem128, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g,
-                                                               d_nobs, rotate, d_ampl, d_status);
+  k_eig_transform128<<<nzc > 0 ? nzc : 1, NB2, kSmem128, st>>>(
+      N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, mode);
   return cudaGetLastError();
 }
 

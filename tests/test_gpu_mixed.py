@@ -169,3 +169,61 @@ def test_tensor_core_update_matches_cuda_core_update(oakg, N, f32):
     assert e_mean < 1e-5 and e_anom < 1e-5, (e_mean, e_anom)
     empty = np.repeat(nobs == 0, zs)
     assert np.array_equal(Sa_t[empty], Sf.astype(dt)[empty].astype(np.float64))
+
+
+# ---------------------------------------------------------------- FP64-accurate eigensolve
+
+@pytest.mark.parametrize("N,scale", [(64, 1 / 6), (37, 1 / 8), (100, 1 / 10), (128, 1 / 10)])
+def test_refined_eigensolve_matches_oracle(oakg, N, scale):
+    """OAKG_PREC_MIXED_FP64EIG (the FP32 eigenpairs refined to FP64 accuracy) on the local
+    configuration, at the mixed-form bar."""
+    c = local_case(scale=scale, N=N)
+    xa, Sa, _, nobs = oakg.loc_analysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf, c.r_diag,
+                                        c.zone_pos, c.obs_pos, c.corr_len, c.max_len,
+                                        weight=c.weight, precision=oakg.PREC_MIXED_FP64EIG)
+    xa_o, Sa_o, _, nobs_o = cref.locanalysis(c.zone_size, c.xf, c.Hxf, c.yo, c.Sf, c.HSf,
+                                             c.r_diag, c.zone_pos, c.obs_pos, c.corr_len,
+                                             c.max_len, kind=c.weight)
+    assert np.array_equal(nobs, nobs_o)
+    e_mean, e_anom = _errs(xa, Sa, xa_o, Sa_o, c.xf)
+    assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)
+
+
+def _exact_gram_case(N, seed=11, Z=16, nz=3, p=200):
+    """Zones whose Gram matrix and innovation projection are exact in FP32 (integer
+    observation rows below 2^8, weight 1 -- every observation at its zone's position --, r = 1,
+    integer innovations), with a rank-2 dominant part: eigenvalues from ~1e6 down to ~1e2, so
+    an FP32 eigensolve misses the small ones by ~eps_32 * 1e6 while the refined eigensolve
+    resolves them."""
+    rng = np.random.default_rng(seed)
+    n, m = Z * nz, Z * p
+    u = rng.integers(-8, 9, N)
+    v = rng.integers(-8, 9, N)
+    a, b = rng.integers(-8, 9, m), rng.integers(-8, 9, m)
+    HSf = np.asfortranarray(a[:, None] * u[None, :] + b[:, None] * v[None, :]
+                            + rng.integers(-1, 2, (m, N))).astype(np.float64)
+    Hxf = np.zeros(m)
+    yo = rng.integers(-3, 4, m).astype(np.float64)
+    Sf = np.asfortranarray(rng.standard_normal((n, N)) * 0.1)
+    xf = rng.standard_normal(n)
+    zone_pos = np.zeros((Z, 4))
+    zone_pos[:, 0] = 100.0 * np.arange(Z)
+    obs_pos = (np.repeat(zone_pos[:, 0], p), np.zeros(m), np.zeros(m), np.zeros(m))
+    return (np.full(Z, nz, np.int32), xf, Hxf, yo, Sf, HSf, np.ones(m), zone_pos, obs_pos,
+            np.full(Z, 10.0), np.full(Z, 1.0))
+
+
+@pytest.mark.parametrize("N", [32, 100])
+def test_refined_eigensolve_is_fp64_accurate(oakg, N):
+    args = _exact_gram_case(N)
+    xa_o, Sa_o, _, nobs_o = cref.locanalysis(*args, kind=0)
+    out = {}
+    for prec in (oakg.PREC_MIXED, oakg.PREC_MIXED_FP64EIG):
+        xa, Sa, _, nobs = oakg.loc_analysis(*args, weight=oakg.GAUSS_CUTOFF, precision=prec)
+        assert np.array_equal(nobs, nobs_o) and np.all(nobs == 200)
+        out[prec] = _errs(xa, Sa, xa_o, Sa_o, args[1])
+    e32, e64 = out[oakg.PREC_MIXED], out[oakg.PREC_MIXED_FP64EIG]
+    # refined: only the FP32 transform and update remain (~1e-7); the FP32 eigensolve is far
+    # off on the small eigenvalues
+    assert e64[0] < 2e-6 and e64[1] < 2e-6, (e64, e32)
+    assert e64[0] < 0.1 * e32[0] or e64[1] < 0.1 * e32[1], (e64, e32)
