@@ -156,6 +156,12 @@ def parity_record(xa_d, Sa_d, nobs_d, c, ref, tol):
             "pass": bool(same.all() and e_mean <= tol and e_anom <= tol)}
 
 
+def update_bytes(n, N, nobs, zone_size, s):
+    """Algorithmic bytes of one update stage: Sf read and Sa written (n x N), xf read and xa
+    written (n), all of s bytes; T (N x N FP32) read for every zone with observations."""
+    return 2 * n * N * s + 2 * n * s + int((np.asarray(nobs) > 0).sum()) * N * N * 4
+
+
 def torch_index(t, rows):
     import torch
     return torch.as_tensor(rows, device=t.device)
@@ -321,37 +327,53 @@ def main():
     if not args.no_mixed:
         ref_xa, ref_Sa = out[0].clone(), out[1].clone()
 
-        def mstep():
-            return oak_gb300.loc_analysis(*d_args, weight=c.weight, metric=c.metric,
-                                          loctype=c.loctype, want_ampl=False,
-                                          precision=oak_gb300.PREC_MIXED)
-        for _ in range(args.warmup):
-            mout = mstep()
-        mstage = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
-        barrier()
-        torch.cuda.synchronize(dev)
-        m0 = torch.cuda.Event(enable_timing=True)
-        m1 = torch.cuda.Event(enable_timing=True)
-        m0.record(stream)
-        for _ in range(args.steps):
-            mout = mstep()
-            for k, v in oak_gb300.last_timings().items():
-                mstage[k] += v
-        m1.record(stream)
-        torch.cuda.synchronize(dev)
-        barrier()
-        mms = m0.elapsed_time(m1) / args.steps
-        xf_d = d_args[1]
-        e_mean = float(torch.linalg.norm(mout[0] - ref_xa) / torch.linalg.norm(ref_xa - xf_d))
-        e_anom = float(torch.linalg.norm(mout[1] - ref_Sa) / torch.linalg.norm(ref_Sa))
+        def timed_form(prec):
+            def mstep():
+                return oak_gb300.loc_analysis(*d_args, weight=c.weight, metric=c.metric,
+                                              loctype=c.loctype, want_ampl=False,
+                                              precision=prec)
+            for _ in range(args.warmup):
+                mout = mstep()
+            mstage = {"obs_prep": 0.0, "gram": 0.0, "eig": 0.0, "update": 0.0, "total": 0.0}
+            barrier()
+            torch.cuda.synchronize(dev)
+            m0 = torch.cuda.Event(enable_timing=True)
+            m1 = torch.cuda.Event(enable_timing=True)
+            m0.record(stream)
+            for _ in range(args.steps):
+                mout = mstep()
+                for k, v in oak_gb300.last_timings().items():
+                    mstage[k] += v
+            m1.record(stream)
+            torch.cuda.synchronize(dev)
+            barrier()
+            mms = m0.elapsed_time(m1) / args.steps
+            xf_d = d_args[1]
+            e_mean = float(torch.linalg.norm(mout[0] - ref_xa) / torch.linalg.norm(ref_xa - xf_d))
+            e_anom = float(torch.linalg.norm(mout[1] - ref_Sa) / torch.linalg.norm(ref_Sa))
+            st = {k: v / args.steps for k, v in mstage.items()}
+            res = {"value": ws * c.Z / (mms / 1e3), "unit": UNIT, "ms_per_step": mms,
+                   "speedup_vs_fp64": ms / mms, "rel_err_mean_increment": e_mean,
+                   "rel_err_anomalies": e_anom, "stage_ms_per_step": st,
+                   "update_GBs": update_bytes(c.n, c.N, nobs, c.zone_size, 8) / (st["update"] / 1e3)
+                   / 1e9}
+            return res, mout
+
+        mixed, mout = timed_form(oak_gb300.PREC_MIXED)
+        mixed["precision"] = ("FP64 selection and (1+lambda)^-1/2 scaling; FP32 Gram (tensor "
+                              "cores) and eigensolve; FP32 update (CUDA cores: 20-element zones); "
+                              "compensated FP32 innovation sums")
         if parity is not None:
             parity["mixed"] = parity_record(mout[0], mout[1], mout[3], c, oracle_out[0], 1e-4)
-        mixed = {"value": ws * c.Z / (mms / 1e3), "unit": UNIT, "ms_per_step": mms,
-                 "speedup_vs_fp64": ms / mms, "rel_err_mean_increment": e_mean,
-                 "rel_err_anomalies": e_anom,
-                 "precision": "FP64 selection and (1+lambda)^-1/2 scaling; FP32 Gram, "
-                              "eigensolve and update; compensated FP32 innovation sums",
-                 "stage_ms_per_step": {k: v / args.steps for k, v in mstage.items()}}
+        del mout
+        mixed64, mout = timed_form(oak_gb300.PREC_MIXED_FP64EIG)
+        mixed64["precision"] = ("the mixed form with the FP32 eigenpairs refined to FP64 "
+                                "accuracy (Ogita-Aishima, exact FP32 products): FP64 accuracy "
+                                "for the eigensolve and the (1+lambda)^-1/2 scalings only")
+        if parity is not None:
+            parity["mixed_fp64eig"] = parity_record(mout[0], mout[1], mout[3], c, oracle_out[0],
+                                                    1e-4)
+        mixed["fp64_eigensolve"] = mixed64
         del ref_xa, ref_Sa, mout
 
     # adjoint cost: J = mean over a 60 x 40 column sub-region (all levels) of (xa - x_true)^2,
@@ -679,6 +701,10 @@ def column_section(torch, dev, stream, args, barrier, ws, dc, scale, adjoint_sub
     nobs = om[3].cpu().numpy()
     ref = column_oracle_sample(dc, nobs)
     par_m = column_parity(xa, Sa, om[3], ref, dc.zone_size, 1e-4)
+    oe, mse, ste = timed(lambda: bstep(oak_gb300.PREC_MIXED_FP64EIG), wm, sm)
+    par_e = column_parity(xa, Sa, oe[3], ref, dc.zone_size, 1e-4)
+    del oe
+    om, _, _ = timed(lambda: bstep(oak_gb300.PREC_MIXED), 0, 1)  # the mixed outputs again
     xam, Sam = xa.clone(), Sa.clone()
     o64, ms64, st64 = timed(lambda: bstep(oak_gb300.PREC_FP64), w64, s64)
     # FP64 products, outputs rounded to FP32: the rounding bounds the error against the oracle
@@ -697,11 +723,20 @@ def column_section(torch, dev, stream, args, barrier, ws, dc, scale, adjoint_sub
            "obs_per_zone_max": int(nobs.max()), "obs_per_zone_mean": float(nobs.mean()),
            "mixed": {"value": ws * dc.Z / (msm / 1e3), "unit": UNIT, "ms_per_step": msm,
                      "warmup": wm, "steps": sm, "stage_ms_per_step": stm,
+                     "update_GBs": update_bytes(n, N, nobs, dc.zone_size, 4)
+                     / (stm["update"] / 1e3) / 1e9,
                      "parity_oracle_sample": par_m},
+           "mixed_fp64_eigensolve": {
+               "value": ws * dc.Z / (mse / 1e3), "unit": UNIT, "ms_per_step": mse,
+               "warmup": wm, "steps": sm, "stage_ms_per_step": ste,
+               "parity_oracle_sample": par_e,
+               "precision": "the FP32 eigenpairs refined to FP64 accuracy (Ogita-Aishima, "
+                            "exact FP32 products)"},
            "fp64": {"value": ws * dc.Z / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64,
                     "warmup": w64, "steps": s64, "stage_ms_per_step": st64,
                     "parity_oracle_sample": par_64},
            "speedup_vs_fp64": ms64 / msm,
+           "speedup_vs_fp64_fp64_eigensolve": ms64 / mse,
            "mixed_vs_fp64_rel_err_mean_increment": e_mean,
            "mixed_vs_fp64_rel_err_anomalies": e_anom,
            "generation": "seeded Gaussian random fields generated on the GPU (torch FFTs, FP32)",
