@@ -189,41 +189,41 @@ def test_refined_eigensolve_matches_oracle(oakg, N, scale):
     assert e_mean < TOL and e_anom < TOL, (e_mean, e_anom)
 
 
-def _exact_gram_case(N, seed=11, Z=16, nz=3, p=200):
-    """Zones whose Gram matrix and innovation projection are exact in FP32 (integer
-    observation rows below 2^8, weight 1 -- every observation at its zone's position --, r = 1,
-    integer innovations), with a rank-2 dominant part: eigenvalues from ~1e6 down to ~1e2, so
-    an FP32 eigensolve misses the small ones by ~eps_32 * 1e6 while the refined eigensolve
-    resolves them."""
+def _exact_gram_case(N, dmax, seed=1, Z=16, nz=3):
+    """Zones whose Gram matrix and innovation projection are exact in FP32: p = N integer
+    observation rows d_q (+-1, ...) with d_q from 1 to dmax (geometric), weight 1 (every
+    observation at its zone's position), r = 1, integer innovations. The eigenvalues spread
+    over ~5 decades (dmax 1-8), so an FP32 eigensolve misses the small ones by ~eps_32 ||G||
+    while the eigensolve is the only FP32 error source besides the transform and update."""
     rng = np.random.default_rng(seed)
-    n, m = Z * nz, Z * p
-    u = rng.integers(-8, 9, N)
-    v = rng.integers(-8, 9, N)
-    a, b = rng.integers(-8, 9, m), rng.integers(-8, 9, m)
-    HSf = np.asfortranarray(a[:, None] * u[None, :] + b[:, None] * v[None, :]
-                            + rng.integers(-1, 2, (m, N))).astype(np.float64)
-    Hxf = np.zeros(m)
+    p, m = N, Z * N
+    rows = []
+    for _ in range(Z):
+        M = rng.choice([-1.0, 1.0], size=(p, N))
+        rows.append(np.round(np.geomspace(1.0, dmax, p))[:, None] * M)
+    HSf = np.asfortranarray(np.vstack(rows))
     yo = rng.integers(-3, 4, m).astype(np.float64)
-    Sf = np.asfortranarray(rng.standard_normal((n, N)) * 0.1)
-    xf = rng.standard_normal(n)
+    Sf = np.asfortranarray(rng.standard_normal((Z * nz, N)) * 0.1)
+    xf = rng.standard_normal(Z * nz)
     zone_pos = np.zeros((Z, 4))
     zone_pos[:, 0] = 100.0 * np.arange(Z)
     obs_pos = (np.repeat(zone_pos[:, 0], p), np.zeros(m), np.zeros(m), np.zeros(m))
-    return (np.full(Z, nz, np.int32), xf, Hxf, yo, Sf, HSf, np.ones(m), zone_pos, obs_pos,
-            np.full(Z, 10.0), np.full(Z, 1.0))
+    return (np.full(Z, nz, np.int32), xf, np.zeros(m), yo, Sf, HSf, np.ones(m), zone_pos,
+            obs_pos, np.full(Z, 10.0), np.full(Z, 1.0))
 
 
-@pytest.mark.parametrize("N", [32, 100])
-def test_refined_eigensolve_is_fp64_accurate(oakg, N):
-    args = _exact_gram_case(N)
+# spectra that one refinement step separates (eigenvalue gaps above its threshold delta)
+@pytest.mark.parametrize("N,dmax", [(32, 8.0), (100, 2.0), (128, 1.0)])
+def test_refined_eigensolve_is_fp64_accurate(oakg, N, dmax):
+    """With G exact in FP32, the refined eigenpairs leave only the FP32 rounding of T and of
+    the update (~1e-6 of the oracle), several times closer than the FP32 eigensolve."""
+    args = _exact_gram_case(N, dmax)
     xa_o, Sa_o, _, nobs_o = cref.locanalysis(*args, kind=0)
     out = {}
     for prec in (oakg.PREC_MIXED, oakg.PREC_MIXED_FP64EIG):
         xa, Sa, _, nobs = oakg.loc_analysis(*args, weight=oakg.GAUSS_CUTOFF, precision=prec)
-        assert np.array_equal(nobs, nobs_o) and np.all(nobs == 200)
+        assert np.array_equal(nobs, nobs_o) and np.all(nobs == N)
         out[prec] = _errs(xa, Sa, xa_o, Sa_o, args[1])
     e32, e64 = out[oakg.PREC_MIXED], out[oakg.PREC_MIXED_FP64EIG]
-    # refined: only the FP32 transform and update remain (~1e-7); the FP32 eigensolve is far
-    # off on the small eigenvalues
-    assert e64[0] < 2e-6 and e64[1] < 2e-6, (e64, e32)
-    assert e64[0] < 0.1 * e32[0] or e64[1] < 0.1 * e32[1], (e64, e32)
+    assert e64[0] < 1e-5 and e64[1] < 1e-5, (e64, e32)
+    assert e64[0] < 0.2 * e32[0] and e64[1] < 0.4 * e32[1], (e64, e32)
