@@ -935,9 +935,19 @@ def rows_section(torch, dev, stream, args, c, d_args, fp64_ms, T, F):
         # row 4: ens2sqrt / sqrt2ens
         (mean, S), ms_e2s = timed(lambda: oak_gb300.ens2sqrt(Ef))
         _, ms_s2e = timed(lambda: oak_gb300.sqrt2ens(mean, S))
+        th_rng = np.random.default_rng(77)
+        theta = np.linalg.qr(th_rng.standard_normal((N - 1, N - 1)))[0]
+        theta_d = torch.as_tensor(np.ascontiguousarray(theta.T), device=dev).t()
+        _, ms_s2e_th = timed(lambda: oak_gb300.sqrt2ens(mean, S, theta_d))
         e_bytes = 2 * n * N * 8
         res["ens2sqrt"] = {"ms": ms_e2s, "achieved_GBs": e_bytes / (ms_e2s / 1e3) / 1e9}
-        res["sqrt2ens"] = {"ms": ms_s2e, "achieved_GBs": e_bytes / (ms_s2e / 1e3) / 1e9}
+        res["sqrt2ens"] = {"ms": ms_s2e, "achieved_GBs": e_bytes / (ms_s2e / 1e3) / 1e9,
+                           "theta": "identity (closed form, one read of S and one write of E)"}
+        res["sqrt2ens_random_theta"] = {
+            "ms": ms_s2e_th, "achieved_GBs": e_bytes / (ms_s2e_th / 1e3) / 1e9,
+            "gemm_tflops": 2.0 * n * N * (N - 1) / (ms_s2e_th / 1e3) / 1e12,
+            "theta": "random orthogonal (N-1) x (N-1): E = mean + S Om^T by cuBLAS DGEMM over E "
+                     "pre-filled with the mean"}
         del Ef, mean, S
         # row 2: R = diag(r) + B B^T with k = 8 columns
         kB = 8

@@ -54,7 +54,7 @@ module oakg
        OAKG_PREC_MIXED_FP64EIG = 2
   ! oakg_loc%flags
   integer(c_int32_t), parameter :: OAKG_FLAG_AMPL_ALWAYS = 1, OAKG_FLAG_BRUTE_SEARCH = 2, &
-       OAKG_FLAG_SIMT_UPDATE = 4
+       OAKG_FLAG_SIMT_UPDATE = 4, OAKG_FLAG_SIMT_GRAM = 8
 
   ! struct oakg_dims (the ensemble size is the C member N; Fortran names are case-blind)
   type, bind(C) :: oakg_dims

@@ -42,7 +42,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 GAUSS_CUTOFF, GASPARI_COHN = 0, 1
 CARTESIAN, SPHERICAL, SPHERICAL_APPROX = 0, 1, 2
 PREC_FP64, PREC_MIXED, PREC_MIXED_FP64EIG = 0, 1, 2
-FLAG_AMPL_ALWAYS, FLAG_BRUTE_SEARCH, FLAG_SIMT_UPDATE = 1, 2, 4
+FLAG_AMPL_ALWAYS, FLAG_BRUTE_SEARCH, FLAG_SIMT_UPDATE, FLAG_SIMT_GRAM = 1, 2, 4, 8
 
 
 class OakError(RuntimeError):
@@ -343,7 +343,7 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
                  max_len, *, weight=GAUSS_CUTOFF, metric=CARTESIAN, loctype=1,
                  localise_obs=True, rotate=True, want_sa=True, want_ampl=True,
                  ampl_always=False, brute_search=False, cell_size=0.0, out=None,
-                 precision=PREC_FP64, smw_B=None, simt_update=False):
+                 precision=PREC_FP64, smw_B=None, simt_update=False, simt_gram=False):
     """Local analysis (rrsqrt.F90:433-466) with geometric observation selection.
 
     ``zone_pos``: (Z, 4) x, y, z, t of each zone's first state element
@@ -359,7 +359,8 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     eigenpairs refined to FP64 accuracy). ``smw_B`` (m x k): the observation error
     covariance R = diag(r_diag) + B B^T (SMWCovar, covariance.F90:464-570; FP64 form).
     ``simt_update``: the mixed form's ensemble update on the CUDA cores instead of the tensor
-    cores.
+    cores. ``simt_gram``: the plain form's Gram products on the FP64 CUDA cores instead of the
+    tensor cores (exact 8-bit slice products, N <= 64).
 
     A float32 ``Sf`` selects FP32 storage at the boundary (oakg_locanalysis_f32): xf, Hxf, yo,
     HSf, r_diag are then taken, and xa, Sa, amplitudes returned, in float32; the geometry
@@ -381,7 +382,7 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     pHS, ldH = A.mat(HSf, m, N, "HSf", fdt)
     dims = Dims(n=n, N=N, m=m, ldS=ldS, ldH=ldH, mem=MEM_DEVICE if device else MEM_HOST)
     flags = ((FLAG_AMPL_ALWAYS if ampl_always else 0) | (FLAG_BRUTE_SEARCH if brute_search else 0)
-             | (FLAG_SIMT_UPDATE if simt_update else 0))
+             | (FLAG_SIMT_UPDATE if simt_update else 0) | (FLAG_SIMT_GRAM if simt_gram else 0))
     loc = Loc(weight=weight, metric=metric, loctype=loctype, localise_obs=int(bool(localise_obs)),
               rotate=int(bool(rotate)), precision=int(precision), flags=flags,
               cell_size=float(cell_size))

@@ -1,9 +1,12 @@
 """Command-line runner for the synthetic local-analysis workloads.
 
-  python -m oak_gb300 local [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--m M]
-  python -m oak_gb300 batched [--scale S] [--precision fp64|mixed] [--calls K] [--N N] [--fp32]
-  python -m oak_gb300 large [--scale S] [--precision fp64|mixed] [--calls K]
+  python -m oak_gb300 local [--scale S] [--precision P] [--calls K] [--N N] [--m M]
+  python -m oak_gb300 batched [--scale S] [--precision P] [--calls K] [--N N] [--fp32]
+  python -m oak_gb300 large [--scale S] [--precision P] [--calls K]
   python -m oak_gb300 layout [--obs M] [--calls K]
+
+P is fp64 (the plain form), mixed or mixed_fp64eig (the mixed form with the FP64-accurate
+eigensolve).
 
 ``local`` builds the seeded single-variable case (360 x 180 x 20 columns scaled horizontally by
 S, N = 64, Gaspari-Cohn radius 12 cells); ``batched`` the 5-variable case (720 x 360 columns of
@@ -31,21 +34,21 @@ def main(argv=None):
     sub = p.add_subparsers(dest="cmd", required=True)
     lp = sub.add_parser("local", help="run the local analysis workload on cuda:0")
     lp.add_argument("--scale", type=float, default=0.5)
-    lp.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    lp.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp64eig"], default="fp64")
     lp.add_argument("--calls", type=int, default=2)
     lp.add_argument("--N", type=int, default=64)
     lp.add_argument("--m", type=int, default=50000,
                     help="observations at scale 1 (the case scales them by S^2)")
     bp = sub.add_parser("batched", help="run the 5-variable batched workload on cuda:0")
     bp.add_argument("--scale", type=float, default=0.25)
-    bp.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    bp.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp64eig"], default="fp64")
     bp.add_argument("--calls", type=int, default=2)
     bp.add_argument("--N", type=int, default=100)
     bp.add_argument("--fp32", action="store_true",
                     help="generate on the GPU with FP32 storage at the boundary")
     gp = sub.add_parser("large", help="run the 2-variable N = 128 workload on cuda:0 (FP32)")
     gp.add_argument("--scale", type=float, default=0.125)
-    gp.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    gp.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp64eig"], default="mixed")
     gp.add_argument("--calls", type=int, default=2)
     yp = sub.add_parser("layout", help="run the layout builders on cuda:0")
     yp.add_argument("--obs", type=int, default=1_000_000)
@@ -76,7 +79,8 @@ def main(argv=None):
             c = batched_case(scale=a.scale, N=a.N)
         args = (T(c.zone_size), T(c.xf), T(c.Hxf), T(c.yo), F(c.Sf), F(c.HSf), T(c.r_diag),
                 T(c.zone_pos), tuple(T(x) for x in c.obs_pos), T(c.corr_len), T(c.max_len))
-    prec = oak_gb300.PREC_FP64 if a.precision == "fp64" else oak_gb300.PREC_MIXED
+    prec = {"fp64": oak_gb300.PREC_FP64, "mixed": oak_gb300.PREC_MIXED,
+            "mixed_fp64eig": oak_gb300.PREC_MIXED_FP64EIG}[a.precision]
     for _ in range(a.calls):
         oak_gb300.loc_analysis(*args, weight=c.weight, metric=c.metric, loctype=c.loctype,
                                want_ampl=False, precision=prec)

@@ -61,7 +61,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     newest = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = [nvcc_path(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
+        cmd = [nvcc_path(), *ARCH, "-shared", "-o", tmp, *objs, "-lcublas", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -43,7 +43,36 @@ __global__ void k_mean_anomalies(int64_t rows, int N, const double* __restrict__
     for (int k = 0; k < N; k++) s += E[i + (int64_t)k * ldE];
     const double mu = s / N;
     mean[i] = mu;
-    for (int k = 0; k < N; k++) S[i + (int64_t)k * ldS] = (E[i + (int64_t)k * ldE] - mu) / scaling;
+    // a product by 1/scaling, not a division: GB300's FP64 division is a multi-instruction
+    // sequence on the slow FP64 pipe, which bounded this kernel (within an ulp of the quotient)
+    const double isc = 1.0 / scaling;
+    for (int k = 0; k < N; k++) S[i + (int64_t)k * ldS] = (E[i + (int64_t)k * ldE] - mu) * isc;
+  }
+}
+
+// The same for N <= 64 with the row's members held in registers: E is read once, and the 64
+// loads of a row are independent (each coalesced across the warp), so they are all in flight
+// together. Same arithmetic: sequential sum over k, mean, (E - mean) * (1 / scaling).
+constexpr int kRegMembers = 64;
+__global__ void __launch_bounds__(kThreads)
+    k_mean_anomalies_reg(int64_t rows, int N, const double* __restrict__ E, int64_t ldE,
+                         double scaling, double* __restrict__ mean, double* __restrict__ S,
+                         int64_t ldS) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v[kRegMembers];
+#pragma unroll
+    for (int k = 0; k < kRegMembers; k++) v[k] = (k < N) ? E[i + (int64_t)k * ldE] : 0.0;
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < kRegMembers; k++)
+      if (k < N) s += v[k];
+    const double mu = s / N;
+    mean[i] = mu;
+    const double isc = 1.0 / scaling;
+#pragma unroll
+    for (int k = 0; k < kRegMembers; k++)
+      if (k < N) S[i + (int64_t)k * ldS] = (v[k] - mu) * isc;
   }
 }
 
@@ -135,6 +164,55 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// sqrt2ens with Theta = I: Om = sqrt(N-1) perpSpace(w) has rows sqrt(N-1) (e_i + a w^2 1) for
+// i < N-1 and sqrt(N-1) a (w + 1) w 1 for the last (a = -1 / (w + 1), w = 1/sqrt(N)), so
+//   E(:, i) = mean + sqrt(N-1) (S(:, i) + a w^2 rs),  E(:, N-1) = mean + sqrt(N-1) a (w+1) w rs,
+// rs the row sums of S: one read of S and one write of E, with no N x N-1 product. Rows with
+// K <= 64 anomaly columns keep them in registers; longer rows read S twice.
+template <bool kReg>
+__global__ void __launch_bounds__(kThreads)
+    k_sqrt2ens_identity(int64_t rows, int N, const double* __restrict__ mean,
+                        const double* __restrict__ S, int64_t ldS, double* __restrict__ E,
+                        int64_t ldE) {
+  const int K = N - 1;
+  const double w = 1.0 / sqrt((double)N), a = -1.0 / (w + 1.0), sc = sqrt((double)N - 1.0);
+  const double cw = a * w * w, cl = sc * a * (w + 1.0) * w;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double mu = mean[i];
+    if (kReg) {
+      double v[kRegMembers];
+#pragma unroll
+      for (int k = 0; k < kRegMembers; k++) v[k] = (k < K) ? S[i + (int64_t)k * ldS] : 0.0;
+      double rs = 0.0;
+#pragma unroll
+      for (int k = 0; k < kRegMembers; k++)
+        if (k < K) rs += v[k];
+      const double add = cw * rs;
+#pragma unroll
+      for (int k = 0; k < kRegMembers; k++)
+        if (k < K) E[i + (int64_t)k * ldE] = mu + sc * (v[k] + add);
+      E[i + (int64_t)K * ldE] = mu + cl * rs;
+    } else {
+      double rs = 0.0;
+      for (int k = 0; k < K; k++) rs += S[i + (int64_t)k * ldS];
+      const double add = cw * rs;
+      for (int k = 0; k < K; k++) E[i + (int64_t)k * ldE] = mu + sc * (S[i + (int64_t)k * ldS] + add);
+      E[i + (int64_t)K * ldE] = mu + cl * rs;
+    }
+  }
+}
+
+// E(:, j) = mean (the ensemble mean under the S Om^T product added by the library GEMM)
+__global__ void k_fill_columns(int64_t rows, int N, const double* __restrict__ mean,
+                               double* __restrict__ E, int64_t ldE) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double mu = mean[i];
+    for (int k = 0; k < N; k++) E[i + (int64_t)k * ldE] = mu;
+  }
+}
+
 // the elementwise steps of the bias-aware analysis (rrsqrt.F90:520-540):
 //   ba = bf - gamma inc, ux = xf - ba
 __global__ void k_bias_update(int64_t n, double gamma, const double* __restrict__ bf,
@@ -178,6 +256,23 @@ cudaError_t ensemble_sqrt2ens(int64_t n, int N, const double* mean, const double
   return cudaGetLastError();
 }
 
+cudaError_t ensemble_sqrt2ens_identity(int64_t n, int N, const double* mean, const double* S,
+                                       int64_t ldS, double* E, int64_t ldE, cudaStream_t st) {
+  if (N - 1 <= kRegMembers)
+    k_sqrt2ens_identity<true><<<grid_for(n), kThreads, 0, st>>>(n, N, mean, S, ldS, E, ldE);
+  else
+    k_sqrt2ens_identity<false><<<grid_for(n), kThreads, 0, st>>>(n, N, mean, S, ldS, E, ldE);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t ensemble_fill_columns(int64_t n, int N, const double* mean, double* E, int64_t ldE,
+                                  cudaStream_t st) {
+  k_fill_columns<<<grid_for(n), kThreads, 0, st>>>(n, N, mean, E, ldE);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t obsoper_apply(int64_t m, int K, const int64_t* idx, const double* w,
                           const double* shift, const double* x, int64_t ldx, double* y,
                           cudaStream_t st) {
@@ -205,7 +300,10 @@ cudaError_t ensemble_prologue(int64_t n, int N, const double* Ef, int64_t ldE, i
                               double* xf, double* Sf, int64_t ldS, double* Hxf, double* HSf,
                               int64_t ldH, double* HEf_scratch, cudaStream_t st) {
   const double scaling = sqrt((double)N - 1.0);
-  k_mean_anomalies<<<grid_for(n), kThreads, 0, st>>>(n, N, Ef, ldE, scaling, xf, Sf, ldS);
+  if (N <= kRegMembers)
+    k_mean_anomalies_reg<<<grid_for(n), kThreads, 0, st>>>(n, N, Ef, ldE, scaling, xf, Sf, ldS);
+  else
+    k_mean_anomalies<<<grid_for(n), kThreads, 0, st>>>(n, N, Ef, ldE, scaling, xf, Sf, ldS);
   count_launches(1);
   if (m > 0) {
     k_obsoper<<<grid_for(m * (int64_t)N), kThreads, 0, st>>>(m, N, K, idx, w, shift, Ef, ldE,

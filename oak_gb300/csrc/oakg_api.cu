@@ -1,6 +1,7 @@
 // C ABI of liboakg.so (declared in include/oakg.h): argument checking, the per-device
 // context (stream, events, buffers kept between calls), host<->device staging and the
 // stage sequence K0 -> (K1+K2) -> (K3+K4) -> K5 over chunks of zones.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -75,7 +76,7 @@ enum BufId {
   B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_SMWB, B_HSTA, B_GAUG,
   B_GVAUG, B_GLOB, B_L_PART, B_L_WORK, B_L_ZS, B_L_ZI, B_L_INV, B_L_X, B_L_Y, B_L_IDX, B_L_MASK,
   B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_HXF64, B_YO64, B_R64, B_G0, B_SREF,
-  B_COUNT_
+  B_OZSCR, B_COUNT_
 };
 
 struct Ctx {
@@ -88,6 +89,8 @@ struct Ctx {
   int64_t chunk_override = 0;  // > 0: zones per chunk fixed (plans: no memory query in capture)
   // host-memory calls: Sf rows in and Sa / xa rows out per zone chunk, beside the kernels
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  // the library GEMM of sqrt2ens with a general Theta (created on first use)
+  cublasHandle_t blas = nullptr;
 };
 
 Ctx* g_ctx[64] = {};
@@ -212,10 +215,15 @@ template <typename R>
 struct ZoneKernels;
 template <>
 struct ZoneKernels<double> {
+  // exact slice products on the tensor cores for ensembles of up to gram_oz_max_n() members
+  // (unless OAKG_FLAG_SIMT_GRAM), else the FP64 CUDA-core kernel
   static cudaError_t gram(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                           int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
                           double* d_G, double* d_g, int32_t* nobs, int brute, int32_t* work,
-                          int32_t* /*err*/, cudaStream_t st, const int32_t* order) {
+                          int32_t* err, cudaStream_t st, const int32_t* order, void* scratch) {
+    if (N <= gram_oz_max_n() && so.m > 0 && scratch && !(lp.flags & OAKG_FLAG_SIMT_GRAM))
+      return zone_gram_oz(g, so, so.m, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute,
+                          work, err, scratch, st, order);
     return zone_gram_fp64(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
                           st, order);
   }
@@ -232,7 +240,8 @@ struct ZoneKernels<float> {
   static cudaError_t gram(const CellGrid& g, const SortedObs& so, int N, LocParams lp, int32_t z0,
                           int32_t nzc, const double* zxyzt, const double* corr, const double* maxl,
                           float* d_G, float* d_g, int32_t* nobs, int brute, int32_t* work,
-                          int32_t* err, cudaStream_t st, const int32_t* order) {
+                          int32_t* err, cudaStream_t st, const int32_t* order,
+                          void* /*scratch*/) {
     if (N <= gram_tc_max_n() && so.HSt32 && so.r32)
       return zone_gram_tc(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
                           err, st, order);
@@ -340,6 +349,10 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   if (a.smw_k > 0 && ((rc = scratch(c, B_GAUG, (size_t)chunk * NA * NA, &d_Ga, "augmented Gram")) ||
                       (rc = scratch(c, B_GVAUG, (size_t)chunk * NA, &d_ga, "augmented g"))))
     return rc;
+  unsigned char* d_oz = nullptr;  // column exponents of the plain form's tensor-core Gram
+  if (sizeof(R) == sizeof(double) &&
+      (rc = scratch(c, B_OZSCR, gram_oz_scratch_bytes(), &d_oz, "Gram exponents")))
+    return rc;
   *status_all = d_work + 2;
   k_set_int<<<1, 1, 0, st>>>(*status_all, 0);
   count_launches(1);
@@ -414,11 +427,11 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
                          st);
       } else {
         e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv,
-                    a.nobs, a.brute, d_work, *status_all, st, a.zorder);
+                    a.nobs, a.brute, d_work, *status_all, st, a.zorder, d_oz);
       }
     } else {
       e = K::gram(a.g, a.so, N, a.lp, (int32_t)z0, nzc, a.zxyzt, a.corr, a.maxl, d_G, d_gv,
-                  a.nobs, a.brute, d_work, *status_all, st, a.zorder);
+                  a.nobs, a.brute, d_work, *status_all, st, a.zorder, nullptr);
     }
     if (e != cudaSuccess) return cuda_fail(e, "selection/Gram kernel");
     if (mode == RunMode::kGramOnly) {
@@ -568,6 +581,7 @@ int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH,
     so.HSt = d_hst;
     so.cell_start = d_cstart;
     so.perm = d_perm;
+    so.m = m;
     if (loc->precision != OAKG_PREC_FP64) {
       float* d_hst32;
       if ((rc = scratch(c, B_HST32, (size_t)m * N, &d_hst32, "obs rows (FP32)"))) return rc;
@@ -1541,7 +1555,9 @@ int ens2sqrt_impl(const oakg_dims* d, const double* E, int64_t ldE, double* mean
 
 // sqrt2ens (rrsqrt.F90:815-839): E = mean + S Om^T, Om = sqrt(N-1) perpSpace(w) Theta, w = 1/sqrt(N)
 // (perpSpace: matoper.F90:509-535). The reference draws Theta at random (randOrthMatrix);
-// here it is the caller's (N-1) x (N-1) orthogonal matrix, or the identity.
+// here it is the caller's (N-1) x (N-1) orthogonal matrix, or the identity. With the identity
+// E has a closed form (one read of S, one write of E); a general Theta takes the n x (N-1) by
+// (N-1) x N product, a plain dense GEMM, from cuBLAS over E pre-filled with the mean.
 int sqrt2ens_impl(const oakg_dims* d, const double* mean, const double* S, const double* theta,
                   double* E, int64_t ldE) {
   int rc = check_dims(d);
@@ -1554,6 +1570,21 @@ int sqrt2ens_impl(const oakg_dims* d, const double* mean, const double* S, const
   const int N = d->N, K = N - 1, mem = d->mem;
   cudaStream_t st = c->stream;
   cudaError_t e = cudaSuccess;
+  if (!theta) {
+    const double* dmean;
+    const double* dS;
+    double* dE;
+    if ((rc = stage_in(c, B_C_MEAN, mean, (size_t)n, mem, &dmean, "mean")) ||
+        (rc = stage_in(c, B_C_S, S, (size_t)d->ldS * K, mem, &dS, "S")) ||
+        (rc = stage_out(c, B_C_EO, E, (size_t)ldE * N, mem, &dE, "E")))
+      return rc;
+    e = ensemble_sqrt2ens_identity(n, N, dmean, dS, d->ldS, dE, ldE, st);
+    if (e == cudaSuccess && mem == OAKG_MEM_HOST)
+      e = cudaMemcpyAsync(E, dE, (size_t)ldE * N * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "sqrt2ens");
+    return OAKG_OK;
+  }
   std::vector<double> th((size_t)K * K, 0.0), om((size_t)N * K, 0.0), P((size_t)N * K, 0.0);
   if (theta) {
     e = cudaMemcpy(th.data(), theta, th.size() * sizeof(double),
@@ -1581,8 +1612,26 @@ int sqrt2ens_impl(const oakg_dims* d, const double* mean, const double* S, const
       (rc = stage_in(c, B_C_S, S, (size_t)d->ldS * K, mem, &dS, "S")) ||
       (rc = stage_out(c, B_C_EO, E, (size_t)ldE * N, mem, &dE, "E")))
     return rc;
+  if (!c->blas) {
+    if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) {
+      c->blas = nullptr;
+      return fail(OAKG_ERR_CUDA, "cublasCreate failed");
+    }
+  }
   e = cudaMemcpyAsync(dOm, om.data(), om.size() * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = ensemble_sqrt2ens(n, N, dmean, dS, d->ldS, dOm, dE, ldE, st);
+  if (e == cudaSuccess) e = ensemble_fill_columns(n, N, dmean, dE, ldE, st);
+  if (e == cudaSuccess) {
+    // E += S Om^T: om is Om row-major (N x K), i.e. Om^T column-major with leading dimension K
+    const double one = 1.0;
+    cublasStatus_t bs = cublasSetStream(c->blas, st);
+    if (bs == CUBLAS_STATUS_SUCCESS)
+      bs = cublasDgemm_64(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, n, N, K, &one, dS, d->ldS,
+                          dOm, K, &one, dE, ldE);
+    if (bs != CUBLAS_STATUS_SUCCESS) {
+      cudaStreamSynchronize(st);
+      return fail(OAKG_ERR_CUDA, "cublasDgemm failed (status %d)", (int)bs);
+    }
+  }
   if (e == cudaSuccess && mem == OAKG_MEM_HOST)
     e = cudaMemcpyAsync(E, dE, (size_t)ldE * N * sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // also keeps om alive for the copy
@@ -2117,6 +2166,7 @@ int release_impl() {
     for (auto& ev : cp->ev) cudaEventDestroy(ev);
     if (cp->copy_in) cudaStreamDestroy(cp->copy_in);
     if (cp->copy_out) cudaStreamDestroy(cp->copy_out);
+    if (cp->blas) cublasDestroy(cp->blas);
     cudaStreamDestroy(cp->own_stream);
     cudaSetDevice(prev);
     delete cp;

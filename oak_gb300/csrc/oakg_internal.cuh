@@ -37,6 +37,7 @@ struct SortedObs {
   const float* innov32; // yo - Hxf in FP32 (mixed precision only)
   const int32_t* cell_start;  // [ncells + 1]
   const int32_t* perm;  // sorted position -> original index                [m]
+  int64_t m;            // number of observations
 };
 
 struct LocParams {
@@ -82,6 +83,18 @@ cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParam
                          const double* max_len, float* d_G, float* d_g, int32_t* d_nobs,
                          int brute, int32_t* d_work, int32_t* d_err, cudaStream_t st,
                          const int32_t* order = nullptr);
+// Plain form on the tensor cores (zone_gram_oz.cu), N <= gram_oz_max_n(): G as an exact
+// product of 8-bit slices of X = diag(|w| / sqrt(r)) HS_sel on BF16 tensor cores, combined in
+// 64-bit integers and FP64; the same selection, weights and outputs as zone_gram_fp64. d_scratch:
+// gram_oz_scratch_bytes() of device memory (column exponents). d_err receives ZST_TIMEOUT (OR)
+// if a bounded device wait expired.
+int gram_oz_max_n();
+size_t gram_oz_scratch_bytes();
+cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int N, LocParams lp,
+                         int32_t z0, int32_t nzc, const double* zone_xyzt, const double* corr_len,
+                         const double* max_len, double* d_G, double* d_g, int32_t* d_nobs,
+                         int brute, int32_t* d_work, int32_t* d_err, void* d_scratch,
+                         cudaStream_t st, const int32_t* order = nullptr);
 // FP32 copy of count doubles (HS rows for the mixed form).
 cudaError_t rows_to_fp32(const double* src, float* dst, int64_t count, cudaStream_t st);
 // FP64 copy of count floats (observation vectors given in FP32 storage).
@@ -179,7 +192,8 @@ cudaError_t zone_eig_refine(int N, int32_t nzc, const float* d_G0, float* d_Z, f
                             const int32_t* d_nobs, float* d_S, cudaStream_t st);
 
 // ---- zone_eig32.cu: FP32 stages for N <= eig32_max_n() (one block per zone), used by
-// zone_eig_fp32 (same arguments as its stages)
+// zone_eig_fp32 (same arguments as its stages); eig32_values and eig32_vectors also take
+// N <= eig128_max_n() (bisection, and the shared-memory inverse iteration on 128 rows)
 int eig32_max_n();
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
                           cudaStream_t st);
@@ -211,6 +225,11 @@ cudaError_t ensemble_ens2sqrt(int64_t n, int N, const double* E, int64_t ldE, do
                               double* S, int64_t ldS, cudaStream_t st);
 cudaError_t ensemble_sqrt2ens(int64_t n, int N, const double* mean, const double* S, int64_t ldS,
                               const double* Om, double* E, int64_t ldE, cudaStream_t st);
+// sqrt2ens with Theta = I in closed form (one read of S, one write of E); E(:, j) = mean
+cudaError_t ensemble_sqrt2ens_identity(int64_t n, int N, const double* mean, const double* S,
+                                       int64_t ldS, double* E, int64_t ldE, cudaStream_t st);
+cudaError_t ensemble_fill_columns(int64_t n, int N, const double* mean, double* E, int64_t ldE,
+                                  cudaStream_t st);
 // y = H x + shift for one state vector (the sparse operator of ensemble_prologue)
 cudaError_t obsoper_apply(int64_t m, int K, const int64_t* idx, const double* w,
                           const double* shift, const double* x, int64_t ldx, double* y,

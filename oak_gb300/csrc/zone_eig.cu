@@ -1060,7 +1060,7 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
 template <>
 cudaError_t launch_e2<float>(int N, int32_t nzc, float* d_aux, float* d_Z, const int32_t* d_nobs,
                              int32_t* d_status, cudaStream_t st) {
-  if (N <= eig32_max_n()) {
+  if (N <= eig128_max_n()) {  // shared-memory E2a / E2b of zone_eig32.cu
     cudaError_t e = eig32_values(N, nzc, d_aux, d_nobs, d_status, st);
     if (e != cudaSuccess) return e;
     return eig32_vectors(N, nzc, d_aux, d_Z, d_nobs, st);

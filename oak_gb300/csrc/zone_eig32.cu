@@ -13,7 +13,8 @@
 // with 128-bit shared loads.
 //
 // E1: one warp per zone, lane t holding rows t and t + 32 of the scaled symmetric matrix. Row
-//   k equals column k, so the lane holding row k forms reflector k; p = beta A v is a register
+//   k equals column k, so the lane holding row k publishes it and the warp forms reflector k
+//   from it (two entries a lane, a warp reduction); p = beta A v is a register
 //   dot per row; w = p - kc v is formed once per row and shared; warp-level synchronisation.
 //   Reflector k is stored vector-major, zero padded, in row k of the zone's matrix slot:
 //   slot[k*N + r] = v_k[r] (v_k[r] = 0 for r <= k).
@@ -65,46 +66,48 @@ __device__ __forceinline__ void vstore(const float (&x)[L], float* p) {
     *reinterpret_cast<float4*>(p + c) = make_float4(x[c], x[c + 1], x[c + 2], x[c + 3]);
 }
 
+// warp-wide sum; the butterfly adds each pair in both orders, so every lane gets the same value
+__device__ __forceinline__ float wsum(float x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
 // ------------------------------------------------------------------------------------ E1
 // One warp per zone (kZpb zones per block). Lane t holds rows t and t + 32 of the scaled
 // symmetric matrix in registers (a0[c] = A[t][c], a1[c] = A[t+32][c]). Row k equals column k,
-// so the lane holding row k forms reflector k; p = beta A v is a register dot per row; every
+// so the lane holding row k publishes it and the warp forms reflector k from it; p = beta A v
+// is a register dot per row; every
 // synchronisation is warp-level. Columns at or left of k are not read after step k, so
 // 16-column groups lying entirely there are skipped, and the first row set is skipped once all
 // its rows are final (k >= 31).
 constexpr int kZpb = 4;
 
-template <int SLOT, int L>
-__device__ __forceinline__ void owner_reflector(const float (&row)[L], int k, int N, float* vbuf,
-                                                float* ax, float* beta_slot) {
-  // single entries are read back through shared memory: an equality-selected register
-  // element would become a dynamic index and move the row to local memory
-  vstore(row, vbuf);
-  const float x0 = vbuf[k + 1], dk = vbuf[k];
-  float sg[4] = {0.f, 0.f, 0.f, 0.f};  // four chains: the other threads wait on this sum
-#pragma unroll
-  for (int c = 0; c < L; c++)
-    if (c > k + 1) sg[c & 3] = fmaf(row[c], row[c], sg[c & 3]);
-  const float sig = (sg[0] + sg[1]) + (sg[2] + sg[3]);
+// Reflector k of E1 from row k of the matrix, published in rowbuf by the lane that holds it:
+// every lane takes entries lane and lane + 32 (sum of squares by a warp reduction), so the
+// reflector costs a few instructions a lane instead of a row's worth on one lane. v goes to
+// vbuf (zero at and left of k, v[k+1] = x0 -/+ mu), d_k, e_k and beta_k to the aux slots; the
+// return value, beta_k, is the same in every lane.
+__device__ __forceinline__ float warp_reflector(const float* rowbuf, int k, int N, int lane,
+                                                float* vbuf, float* ax) {
+  const float xa = rowbuf[lane], xb = rowbuf[lane + 32];
+  const float x0 = rowbuf[k + 1], dk = rowbuf[k];
+  float part = (lane > k + 1) ? xa * xa : 0.f;
+  if (lane + 32 > k + 1) part = fmaf(xb, xb, part);
+  const float sig = wsum(part);
   const float mu = sqrtf(fmaf(x0, x0, sig));
   const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
   const float vv = fmaf(v0, v0, sig);
   const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
   const float bk = skip ? 0.f : 2.f / vv;
-#pragma unroll
-  for (int c = 0; c < L; c += 4) {
-    float4 q4;
-    q4.x = (c + 0 > k + 1) ? row[c + 0] : 0.f;
-    q4.y = (c + 1 > k + 1) ? row[c + 1] : 0.f;
-    q4.z = (c + 2 > k + 1) ? row[c + 2] : 0.f;
-    q4.w = (c + 3 > k + 1) ? row[c + 3] : 0.f;
-    *reinterpret_cast<float4*>(vbuf + c) = q4;
+  const float vk1 = skip ? x0 : v0;
+  vbuf[lane] = (lane > k + 1) ? xa : ((lane == k + 1) ? vk1 : 0.f);
+  vbuf[lane + 32] = (lane + 32 > k + 1) ? xb : ((lane + 32 == k + 1) ? vk1 : 0.f);
+  if (lane == 0) {
+    ax[k] = dk;                                        // d_k
+    ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);  // e_k
+    ax[2 * N + k] = bk;                                // beta_k
   }
-  vbuf[k + 1] = skip ? x0 : v0;
-  ax[k] = dk;                                        // d_k
-  ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);  // e_k
-  ax[2 * N + k] = bk;                                // beta_k
-  *beta_slot = bk;
+  return bk;
 }
 
 __global__ void __launch_bounds__(32 * kZpb, 3)
@@ -112,7 +115,6 @@ __global__ void __launch_bounds__(32 * kZpb, 3)
                     const int32_t* __restrict__ nobs) {
   __shared__ __align__(16) float vbuf_s[kZpb][NB];
   __shared__ __align__(16) float wbuf_s[kZpb][NB];
-  __shared__ float beta_s[kZpb];
   const int lane = threadIdx.x & 31, wz = threadIdx.x >> 5;
   const int32_t zl = blockIdx.x * kZpb + wz;
   if (zl >= nzc || nobs[zl] == 0) return;  // warp-uniform; only warp-level synchronisation
@@ -142,14 +144,15 @@ __global__ void __launch_bounds__(32 * kZpb, 3)
   if (lane == 0) ax[5 * N] = scale;
   __syncwarp();  // every row read before reflectors overwrite the slot
   for (int k = 0; k < N - 2; k++) {
-    if (lane == (k & 31)) {
+    if (lane == (k & 31)) {  // row k = column k: its holder publishes it
       if (k < 32)
-        owner_reflector<0>(a0, k, N, vbuf, ax, &beta_s[wz]);
+        vstore(a0, wbuf);
       else
-        owner_reflector<1>(a1, k, N, vbuf, ax, &beta_s[wz]);
+        vstore(a1, wbuf);
     }
-    __syncwarp();  // v and beta published
-    const float bk = beta_s[wz];
+    __syncwarp();  // row k published (wbuf is free: the previous w was consumed)
+    const float bk = warp_reflector(wbuf, k, N, lane, vbuf, ax);
+    __syncwarp();  // v published; row k read by every lane before w overwrites it
     const float v0r = vbuf[r0], v1r = vbuf[r1];
     if (r0 < N) Gz[(int64_t)k * N + r0] = v0r;  // reflector k, vector-major, zero padded
     if (r1 < N) Gz[(int64_t)k * N + r1] = v1r;
@@ -297,11 +300,6 @@ __device__ __forceinline__ void vaxpy2(float (&x0)[NB], float (&x1)[NB], float f
   }
 }
 
-__device__ __forceinline__ float wsum(float x) {
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
-}
-
 constexpr int kFillIters = 2;     // inverse-iteration steps of a pseudo-random complement fill
 constexpr float kResidMin = 1e-6f;  // smallest squared residual norm used as a fill
 
@@ -341,21 +339,22 @@ __device__ void tri_solve32(float* x, const float* d, const float* e, int N, flo
   }
 }
 
-// the owner lane normalises its vector (or marks it collapsed) and publishes it in row c
-__device__ __forceinline__ void mgs_owner(float (&x)[NB], int c, Zone3& zs) {
-  float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-  for (int i = 0; i < NB; i += 2) {
-    s0 = fmaf(x[i], x[i], s0);
-    s1 = fmaf(x[i + 1], x[i + 1], s1);
-  }
-  const float s = s0 + s1;
+// Vector c, published in row c of buf by the lane that holds it, is normalised there by the
+// warp (two entries a lane, a warp reduction for the norm) or, when it keeps less than half its
+// squared norm, marked collapsed and left as its residual. Returns whether it was accepted (the
+// same in every lane). The holder's registers keep the unnormalised vector: the final vectors
+// are reloaded from buf after the orthogonalisation.
+__device__ __forceinline__ bool mgs_normalise(int c, int lane, Zone3& zs) {
+  float* row = zs.buf + c * LDV;
+  const float e0 = row[lane], e1 = row[lane + 32];
+  const float s = wsum(fmaf(e0, e0, e1 * e1));
   const bool ok = zs.flag[c] && (s >= 0.5f);
-  const float sc = ok ? rsqrtf(s) : 1.f;  // a collapsed vector keeps its residual
-#pragma unroll
-  for (int i = 0; i < NB; i++) x[i] *= sc;
-  vstore(x, zs.buf + c * LDV);
-  if (!ok) zs.flag[c] = 0;
+  if (ok) {  // each lane rewrites only the entries it read
+    const float sc = rsqrtf(s);
+    row[lane] = e0 * sc;
+    row[lane + 32] = e1 * sc;
+  }
+  return ok;
 }
 
 // mode 0: the whole stage; 1: stop after the back-transform and write the eigenvectors of G
@@ -407,12 +406,16 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
   for (int c = N - 1; c >= 0; c--) {
     if (lane == (c & 31)) {
       if (c >= 32)
-        mgs_owner(x1, c, zs);
+        vstore(x1, buf + c * LDV);
       else
-        mgs_owner(x0, c, zs);
+        vstore(x0, buf + c * LDV);
     }
-    __syncwarp();
-    if (zs.flag[c]) {
+    __syncwarp();  // vector c published
+    const bool ok = mgs_normalise(c, lane, zs);
+    __syncwarp();  // row c normalised; every lane has read flag[c]
+    if (!ok) {
+      if (lane == 0) zs.flag[c] = 0;
+    } else {
       const float* uc = buf + c * LDV;
       const bool use0 = j0 < c, use1 = j1 < c;
       if (use0 || use1) {
@@ -532,9 +535,10 @@ __global__ void __launch_bounds__(32 * kZpb3, 4)
       if (lane == 0) zs.flag[c] = 1;
       __syncwarp();
     }
-    if (j0 < N) vload(x0, buf + j0 * LDV);
-    if (j1 < N) vload(x1, buf + j1 * LDV);
   }
+  // the final (normalised or replaced) vectors are the rows of buf
+  if (j0 < N) vload(x0, buf + j0 * LDV);
+  if (j1 < N) vload(x1, buf + j1 * LDV);
   __syncwarp();  // every lane holds its final vectors: buf takes the reflectors
   // reflectors into buf (rows k < N-2, zero padded)
   if (N == NB) {
@@ -851,22 +855,122 @@ __global__ void __launch_bounds__(kT2)
   if (st) status[zl] |= st;
 }
 
+// E2a for 65..128 members: one block of NB2 threads per zone, thread j bisects eigenvalue j
+// (the j-th smallest) of Tri. count(x) = the number of negative pivots of the LDL^T of Tri - x I
+// (Sturm; the ratio form q_i = d_i - x - e_(i-1)^2 / q_(i-1), a pivot below pivmin in magnitude
+// taken as -pivmin, as LAPACK's bisection does) is the number of eigenvalues below x. Starting
+// from the Gershgorin interval, the step halves the interval until its width is below
+// 2 eps max(|lo|, |hi|) or eps ||Tri||_1 / 64 (at most kBisectSteps steps), so the eigenvalues
+// come sorted and as accurate as the QR sweeps' (whose deflation floor is eps ||Tri||_1). Every
+// thread is busy: the thread-per-zone QR sweeps leave most lanes idle at these sizes. Outputs
+// are those of k_eig_values32 (eigenvalues, inverse-iteration shifts, ||Tri||_1).
+constexpr int kBisectSteps = 40;
+
+__global__ void __launch_bounds__(128)
+    k_eig_values_bisect(int N, int32_t nzc, float* __restrict__ aux,
+                        const int32_t* __restrict__ nobs) {
+  __shared__ float sd[128], se2[128], sl[128];
+  __shared__ float red[3][4];
+  const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+  const int32_t zl = blockIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
+  const float eps = 5.9604645e-8f;
+  float* ax = aux + (int64_t)zl * aux_stride32(N);
+  const float dj = (j < N) ? ax[j] : 0.f;
+  const float ej = (j < N - 1) ? ax[N + j] : 0.f;
+  const float ejm = (j > 0 && j < N) ? ax[N + j - 1] : 0.f;
+  sd[j] = dj;
+  se2[j] = ej * ej;
+  // ||Tri||_1, the Gershgorin interval and max e^2 (block reductions)
+  const float rad = fabsf(ej) + fabsf(ejm);
+  float nrm = (j < N) ? fabsf(dj) + rad : 0.f;
+  float glo = (j < N) ? dj - rad : INFINITY;
+  float ghi = (j < N) ? dj + rad : -INFINITY;
+  for (int o = 16; o > 0; o >>= 1) {
+    nrm = fmaxf(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
+    glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+    ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+  }
+  if (lane == 0) {
+    red[0][warp] = nrm;
+    red[1][warp] = glo;
+    red[2][warp] = ghi;
+  }
+  __syncthreads();
+  const float onenrm = fmaxf(fmaxf(red[0][0], red[0][1]), fmaxf(red[0][2], red[0][3]));
+  float lo = fminf(fminf(red[1][0], red[1][1]), fminf(red[1][2], red[1][3]));
+  float hi = fmaxf(fmaxf(red[2][0], red[2][1]), fmaxf(red[2][2], red[2][3]));
+  const float pad = 2.f * eps * onenrm * (float)N + 1e-30f;
+  lo -= pad;
+  hi += pad;
+  float e2max = 0.f;
+  for (int i = 0; i < N - 1; i++) e2max = fmaxf(e2max, se2[i]);
+  const float pivmin = 1.17549435e-38f * fmaxf(1.f, e2max);
+  const float abs_w = eps * onenrm * (1.f / 64.f);
+  if (j < N) {
+#pragma unroll 1
+    for (int it = 0; it < kBisectSteps; it++) {
+      const float w = hi - lo;
+      if (!(w > fmaxf(abs_w, 2.f * eps * fmaxf(fabsf(lo), fabsf(hi))))) break;
+      const float x = 0.5f * (lo + hi);
+      float q = sd[0] - x;
+      if (fabsf(q) < pivmin) q = -pivmin;
+      int cnt = (q < 0.f);
+      for (int i = 1; i < N; i++) {
+        q = (sd[i] - x) - __fdividef(se2[i - 1], q);
+        if (fabsf(q) < pivmin) q = -pivmin;
+        cnt += (q < 0.f);
+      }
+      if (cnt > j)
+        hi = x;
+      else
+        lo = x;
+    }
+    sl[j] = 0.5f * (lo + hi);
+  }
+  __syncthreads();
+  const float scale = ax[5 * N];
+  if (j < N) ax[3 * N + j] = sl[j] * scale;
+  if (j == 0) {
+    // inverse-iteration shifts: separated by 10 eps |lambda| (as k_eig_values32)
+    float prev = 0.f;
+    for (int i = 0; i < N; i++) {
+      float sh = sl[i];
+      if (i > 0) {
+        const float pert = 10.f * eps * fabsf(sh);
+        if (sh - prev < pert) sh = prev + pert;
+      }
+      ax[4 * N + i] = sh;
+      prev = sh;
+    }
+    ax[5 * N + 1] = onenrm;
+  }
+}
+
 // ------------------------------------------------------------------------------------ E2b
-// One block of 64 threads per zone, thread j = eigenpair j: inverse iteration on Tri - shift_j I
+// One block of 64 threads per zone and 64 eigenpairs (a second block, blockIdx.y = 1, for
+// eigenpairs 64..127 of the 65..128-member ensembles), thread j = eigenpair j: inverse
+// iteration on Tri - shift_j I
 // (two solves from a fixed pseudo-random start, as the generic E2b). The partial-pivoting LU
 // is recomputed in each forward sweep (fused with the elimination), its upper factor kept in
-// shared memory; the iterate lives in registers (loops unrolled to NV, the padded length).
+// shared memory: the first super-diagonal and the pivot reciprocals, while the second
+// super-diagonal, e_{i+1} where rows i and i+1 were swapped and 0 elsewhere, is kept as one bit
+// a row in a register mask (32 KB of shared memory a block: 7 blocks an SM); the iterate lives
+// in registers (loops unrolled to NV, the padded length).
 // Pivots are at least eps ||Tri||_1 in magnitude, so their reciprocals use the fast
 // approximate division (a few ulp: inverse iteration only needs the direction).
 template <int NV>
 __global__ void __launch_bounds__(kT2)
     k_eig_vectors32(int N, int32_t nzc, const float* __restrict__ aux, float* __restrict__ Zg,
                     const int32_t* __restrict__ nobs) {
-  extern __shared__ __align__(16) float sfac[];  // upper factor u1, u2, 1/diag: [i][jl] each
+  extern __shared__ __align__(16) float sfac[];  // upper factor u1, 1/diag: [i][jl] each
   __shared__ float sd[NV], se[NV];
   float* su1 = sfac;
-  float* su2 = sfac + NV * kT2;
-  float* sui = sfac + 2 * NV * kT2;
+  float* sui = sfac + NV * kT2;
+  // bit i (of word i / 64): rows i, i + 1 swapped (u2[i] = e[i+1])
+  unsigned long long swapped[(NV + 63) / 64];
+#pragma unroll
+  for (int w = 0; w < (NV + 63) / 64; w++) swapped[w] = 0ull;
   const int jl = threadIdx.x, j = kT2 * blockIdx.y + jl;  // eigenpair j of this block's kT2
   const int32_t zl = blockIdx.x;
   if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
@@ -910,8 +1014,8 @@ __global__ void __launch_bounds__(kT2)
           const float li = (swap ? cd : sub) * ui;
           if (it == 0) {
             su1[i * kT2 + jl] = swap ? dg : csup;
-            su2[i * kT2 + jl] = swap ? sp : 0.f;
             sui[i * kT2 + jl] = ui;
+            if (swap) swapped[i >> 6] |= 1ull << (i & 63);
           }
           const float aa = swap ? csup : dg, bb = swap ? dg : csup;
           cd = fmaf(-li, bb, aa);
@@ -926,8 +1030,7 @@ __global__ void __launch_bounds__(kT2)
         if (fabsf(pivot) < tiny) pivot = copysignf(tiny, pivot);
         sui[(N - 1) * kT2 + jl] = __fdividef(1.f, pivot);
         su1[(N - 1) * kT2 + jl] = 0.f;
-        su2[(N - 1) * kT2 + jl] = 0.f;
-        if (N >= 2) su2[(N - 2) * kT2 + jl] = 0.f;
+        // u2[N-2] = u2[N-1] = 0: a swap at row N - 2 brings e[N-1] = 0, row N - 1 has no bit
       }
       // back substitution with the upper factor (diagonal + two super-diagonals)
 #pragma unroll
@@ -935,7 +1038,8 @@ __global__ void __launch_bounds__(kT2)
         if (i < N) {
           float v = x[i];
           if (i + 1 < NV) v = fmaf(-su1[i * kT2 + jl], x[i + 1], v);
-          if (i + 2 < NV) v = fmaf(-su2[i * kT2 + jl], x[i + 2], v);
+          if (i + 2 < NV && ((swapped[i >> 6] >> (i & 63)) & 1ull))
+            v = fmaf(-se[i + 1], x[i + 2], v);
           x[i] = v * sui[i * kT2 + jl];
         }
       }
@@ -954,7 +1058,7 @@ __global__ void __launch_bounds__(kT2)
       for (int i = 0; i < NV; i++) x[i] *= sc;
     }
   }
-  __syncthreads();  // factors no longer read: reuse su1/su2 as the transpose buffer
+  __syncthreads();  // factors no longer read: reuse them as the transpose buffer
 #pragma unroll
   for (int i = 0; i < NV; i++) tr[i * (kT2 + 1) + jl] = x[i];
   __syncthreads();
@@ -985,18 +1089,20 @@ __device__ __forceinline__ float block_sum128(float x, float* red) {
 }
 
 // E1 for N <= 128. Thread t holds row t of the scaled symmetric matrix (a[c] = A[t][c]); the
-// owner of row k forms reflector k; p = beta A v is a register dot per row; kc = beta (p . v) / 2
-// from per-warp partials; the update A -= v w^T + w v^T takes w_c = p_c - kc v_c from the
-// published p. v, p and the partials are double-buffered by step parity: two barriers a step.
-// Rows <= k are final after step k and columns <= k are not read again, so 16-column groups
-// lying there are skipped.
+// holder of row k publishes it, every warp forms reflector k from it (each lane takes four
+// entries; the sum of squares is a warp reduction, the same in every warp, so no block
+// reduction is needed) and thread t writes v_t; p = beta A v is a register dot per row;
+// kc = beta (p . v) / 2 from per-warp partials; the update A -= v w^T + w v^T takes
+// w_c = p_c - kc v_c from the published p. The row, v, p and the partials are double-buffered
+// by step parity: three barriers a step. Rows <= k are final after step k and columns <= k are
+// not read again, so 16-column groups lying there are skipped.
 __global__ void __launch_bounds__(NB2, 3)
     k_eig_tridiag128(int N, int32_t nzc, float* __restrict__ GT, float* __restrict__ aux,
                      const int32_t* __restrict__ nobs) {
   __shared__ __align__(16) float vbuf[2][NB2];
   __shared__ __align__(16) float pbuf[2][NB2];
+  __shared__ __align__(16) float rbuf[2][NB2];
   __shared__ float red[2][4];
-  __shared__ float beta_s[2];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int32_t zl = blockIdx.x;
   if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
@@ -1022,9 +1128,34 @@ __global__ void __launch_bounds__(NB2, 3)
     const int b = k & 1;
     float* vb = vbuf[b];
     float* pb = pbuf[b];
-    if (t == k) owner_reflector<0>(a, k, N, vb, ax, &beta_s[b]);
-    __syncthreads();  // v and beta published
-    const float bk = beta_s[b];
+    float* rb = rbuf[b];
+    if (t == k) vstore(a, rb);  // row k = column k
+    __syncthreads();            // row k published
+    float bk;
+    {
+      float part = 0.f;
+#pragma unroll
+      for (int i = 0; i < NB2 / 32; i++) {
+        const int c = lane + 32 * i;
+        const float x = rb[c];
+        if (c > k + 1) part = fmaf(x, x, part);
+      }
+      const float sig = wsum(part);  // the same sum in every warp
+      const float x0 = rb[k + 1];
+      const float mu = sqrtf(fmaf(x0, x0, sig));
+      const float v0 = (x0 <= 0.f) ? x0 - mu : x0 + mu;
+      const float vv = fmaf(v0, v0, sig);
+      const bool skip = (sig == 0.f) || !(vv > 0.f) || isinf(vv);
+      bk = skip ? 0.f : 2.f / vv;
+      const float xt = rb[t];
+      vb[t] = (t > k + 1) ? xt : ((t == k + 1) ? (skip ? x0 : v0) : 0.f);
+      if (t == 0) {
+        ax[k] = rb[k];                                     // d_k
+        ax[N + k] = skip ? x0 : ((x0 <= 0.f) ? mu : -mu);  // e_k
+        ax[2 * N + k] = bk;                                // beta_k
+      }
+    }
+    __syncthreads();  // v published
     const float vr = vb[t];
     if (t < N) Gz[(int64_t)k * N + t] = vr;  // reflector k, vector-major, zero padded
     if (bk == 0.f) continue;                 // block-uniform; an identity reflector
@@ -1175,31 +1306,32 @@ __global__ void __launch_bounds__(NB2, 3)
   __syncthreads();
   if (mode != 2) {  // eigenvectors of Tri: orthogonalisation and back-transform (block-uniform)
   // modified Gram-Schmidt on the eigenvectors of Tri, largest eigenvalue first, with the
-  // acceptance test and residual-keeping of k_eig_transform32
+  // acceptance test and residual-keeping of k_eig_transform32. The holder publishes vector c
+  // as it is; every warp takes its squared norm s (four entries a lane, a warp reduction: the
+  // same value in every warp) and the later vectors subtract (x . u_c) / s u_c. Row c is
+  // normalised in the next step (thread t scales entry t), when no thread reads it.
+  float pend_sc = 1.f;  // the scale owed to entry t of the previous row
   for (int c = N - 1; c >= 0; c--) {
-    if (t == c) {
-      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    if (t == c) vstore(x, buf + c * LDV2);
+    __syncthreads();  // vector c published; the readers of the previous row are done
+    if (c + 1 < N) buf[(c + 1) * LDV2 + t] *= pend_sc;
+    const float* uc = buf + c * LDV2;
+    float part = 0.f;
 #pragma unroll
-      for (int i = 0; i < NB2; i += 4) {
-        s0 = fmaf(x[i], x[i], s0);
-        s1 = fmaf(x[i + 1], x[i + 1], s1);
-        s2 = fmaf(x[i + 2], x[i + 2], s2);
-        s3 = fmaf(x[i + 3], x[i + 3], s3);
-      }
-      const float s = (s0 + s1) + (s2 + s3);
-      const bool ok = s >= 0.5f;
-      const float sc = ok ? rsqrtf(s) : 1.f;  // a collapsed vector keeps its residual
-#pragma unroll
-      for (int i = 0; i < NB2; i++) x[i] *= sc;
-      vstore(x, buf + c * LDV2);
-      if (!ok) zs.flag[c] = 0;
+    for (int i = 0; i < NB2 / 32; i++) {
+      const float e = uc[(t & 31) + 32 * i];
+      part = fmaf(e, e, part);
     }
-    __syncthreads();  // vector c final and published
-    if (t < c && zs.flag[c]) {
-      const float* uc = buf + c * LDV2;
-      vaxpy128(x, vdot128(x, uc, 0, ng), uc, 0, ng);
-    }
+    const float s = wsum(part);
+    // a rejected vector is flagged by thread 0 while the others read the flag: every reader
+    // computes ok = false either way
+    const bool ok = zs.flag[c] && (s >= 0.5f);
+    if (!ok && t == 0) zs.flag[c] = 0;
+    pend_sc = ok ? rsqrtf(s) : 1.f;  // a collapsed vector keeps its residual
+    if (ok && t < c) vaxpy128(x, vdot128(x, uc, 0, ng) * (pend_sc * pend_sc), uc, 0, ng);
   }
+  __syncthreads();  // the readers of row 0 are done
+  buf[t] *= pend_sc;
   int ncol = 0;
   if (t < N && !zs.flag[t]) ncol = 1;
   if (__syncthreads_or(ncol)) {
@@ -1278,9 +1410,98 @@ __global__ void __launch_bounds__(NB2, 3)
     const int k = idx >> 7, c = idx & (NB2 - 1);
     buf[k * LDV2 + c] = (k < N - 2 && c < N) ? Gz[k * N + c] : 0.f;
   }
+  // couplings of each reflector with the next three applied after it: p_s[k] = v_k . v_{k-s}
+  // (s = 1, 2, 3), shared by every vector of the zone (tt, cc, vv are free until the
+  // amplitudes)
+  float* p1 = zs.tt;
+  float* p2 = zs.cc;
+  float* p3 = zs.vv;
   __syncthreads();
-  // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k)
-  for (int k = N - 3; k >= 0; k--) {
+  if (t < N - 2) {
+    // v_k vanishes on components <= k; the rows are zero-padded past N
+    const float* vk = buf + t * LDV2;
+    const float* w1 = buf + (t >= 1 ? t - 1 : t) * LDV2;
+    const float* w2 = buf + (t >= 2 ? t - 2 : t) * LDV2;
+    const float* w3 = buf + (t >= 3 ? t - 3 : t) * LDV2;
+    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    for (int c = (t + 1) & ~3; c < NB2; c += 4) {
+      const float4 a = *reinterpret_cast<const float4*>(vk + c);
+      const float4 q1 = *reinterpret_cast<const float4*>(w1 + c);
+      const float4 q2 = *reinterpret_cast<const float4*>(w2 + c);
+      const float4 q3 = *reinterpret_cast<const float4*>(w3 + c);
+      s1 = fmaf(a.x, q1.x, fmaf(a.y, q1.y, fmaf(a.z, q1.z, fmaf(a.w, q1.w, s1))));
+      s2 = fmaf(a.x, q2.x, fmaf(a.y, q2.y, fmaf(a.z, q2.z, fmaf(a.w, q2.w, s2))));
+      s3 = fmaf(a.x, q3.x, fmaf(a.y, q3.y, fmaf(a.z, q3.z, fmaf(a.w, q3.w, s3))));
+    }
+    p1[t] = (t >= 1) ? s1 : 0.f;
+    p2[t] = (t >= 2) ? s2 : 0.f;
+    p3[t] = (t >= 3) ? s3 : 0.f;
+  }
+  __syncthreads();
+  // back-transform U = H_0 H_1 ... H_{N-3} Z (reflector k vanishes on components <= k), four
+  // reflectors at a time: with H_k = I - b_k v_k v_k^T applied in the order k, k-1, k-2, k-3,
+  // the four dots d_i = v_{k-i} . x of the original x are independent, the coefficients follow
+  // from c_i = b_{k-i} (d_i - sum_{j<i} c_j v_{k-i} . v_{k-j}), and one pass subtracts
+  // sum_i c_i v_{k-i}: the same products as one reflector at a time, a quarter of the
+  // dependent dot / update steps.
+  int k = N - 3;
+  for (; k >= 3; k -= 4) {
+    const float* v0 = buf + k * LDV2;
+    const float* v1 = v0 - LDV2;
+    const float* v2 = v1 - LDV2;
+    const float* v3 = v2 - LDV2;
+    const int g0 = (k - 2) >> 4;  // the widest support of the four: v_{k-3}
+    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f, e0 = 0.f, e1 = 0.f, f0 = 0.f, f1 = 0.f;
+#pragma unroll
+    for (int g = 0; g < NB2 / 16; g++) {
+      if (g >= g0 && g < ng) {
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          const int c = 16 * g + 4 * m;
+          const float4 q0 = *reinterpret_cast<const float4*>(v0 + c);
+          const float4 q1 = *reinterpret_cast<const float4*>(v1 + c);
+          const float4 q2 = *reinterpret_cast<const float4*>(v2 + c);
+          const float4 q3 = *reinterpret_cast<const float4*>(v3 + c);
+          a0 = fmaf(x[c], q0.x, fmaf(x[c + 2], q0.z, a0));
+          a1 = fmaf(x[c + 1], q0.y, fmaf(x[c + 3], q0.w, a1));
+          b0 = fmaf(x[c], q1.x, fmaf(x[c + 2], q1.z, b0));
+          b1 = fmaf(x[c + 1], q1.y, fmaf(x[c + 3], q1.w, b1));
+          e0 = fmaf(x[c], q2.x, fmaf(x[c + 2], q2.z, e0));
+          e1 = fmaf(x[c + 1], q2.y, fmaf(x[c + 3], q2.w, e1));
+          f0 = fmaf(x[c], q3.x, fmaf(x[c + 2], q3.z, f0));
+          f1 = fmaf(x[c + 1], q3.y, fmaf(x[c + 3], q3.w, f1));
+        }
+      }
+    }
+    const float d0 = a0 + a1, d1 = b0 + b1, d2 = e0 + e1, d3 = f0 + f1;
+    // v_{k-i} . v_{k-j} (j < i) = p_{i-j}[k - j]
+    const float c0 = zs.bet[k] * d0;
+    const float c1 = zs.bet[k - 1] * fmaf(-c0, p1[k], d1);
+    const float c2 = zs.bet[k - 2] * fmaf(-c1, p1[k - 1], fmaf(-c0, p2[k], d2));
+    const float c3 =
+        zs.bet[k - 3] * fmaf(-c2, p1[k - 2], fmaf(-c1, p2[k - 1], fmaf(-c0, p3[k], d3)));
+#pragma unroll
+    for (int g = 0; g < NB2 / 16; g++) {
+      if (g >= g0 && g < ng) {
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+          const int c = 16 * g + 4 * m;
+          const float4 q0 = *reinterpret_cast<const float4*>(v0 + c);
+          const float4 q1 = *reinterpret_cast<const float4*>(v1 + c);
+          const float4 q2 = *reinterpret_cast<const float4*>(v2 + c);
+          const float4 q3 = *reinterpret_cast<const float4*>(v3 + c);
+          x[c] = fmaf(-c3, q3.x, fmaf(-c2, q2.x, fmaf(-c1, q1.x, fmaf(-c0, q0.x, x[c]))));
+          x[c + 1] =
+              fmaf(-c3, q3.y, fmaf(-c2, q2.y, fmaf(-c1, q1.y, fmaf(-c0, q0.y, x[c + 1]))));
+          x[c + 2] =
+              fmaf(-c3, q3.z, fmaf(-c2, q2.z, fmaf(-c1, q1.z, fmaf(-c0, q0.z, x[c + 2]))));
+          x[c + 3] =
+              fmaf(-c3, q3.w, fmaf(-c2, q2.w, fmaf(-c1, q1.w, fmaf(-c0, q0.w, x[c + 3]))));
+        }
+      }
+    }
+  }
+  for (; k >= 0; k--) {  // the remaining reflectors one at a time
     const float bk = zs.bet[k];
     if (bk == 0.f) continue;  // block-uniform
     const float* vk = buf + k * LDV2;
@@ -1423,20 +1644,31 @@ int eig32_max_n() { return NB; }
 
 cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs,
                          int32_t* d_status, cudaStream_t st) {
-  if (N < 2 || N > NB) return cudaErrorInvalidValue;
-  k_eig_values32<<<(nzc + kT2 - 1) / kT2, kT2, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  if (N < 2 || N > NB2) return cudaErrorInvalidValue;
+  if (N <= NB)
+    k_eig_values32<<<(nzc + kT2 - 1) / kT2, kT2, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
+  else
+    k_eig_values_bisect<<<nzc > 0 ? nzc : 1, 128, 0, st>>>(N, nzc, d_aux, d_nobs);
   return cudaGetLastError();
 }
 
 cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
                           const int32_t* d_nobs, cudaStream_t st) {
-  if (N < 2 || N > NB) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)3 * NB * kT2 * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_eig_vectors32<NB><<<dim3(nzc > 0 ? nzc : 1, 1), kT2, smem, st>>>(N, nzc, d_aux, d_Z,
-                                                                     d_nobs);
+  if (N < 2 || N > NB2) return cudaErrorInvalidValue;
+  const unsigned nz = nzc > 0 ? nzc : 1;
+  if (N <= NB) {
+    const size_t smem = (size_t)2 * NB * kT2 * sizeof(float);  // >= NB x (kT2 + 1): transpose
+    cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_eig_vectors32<NB><<<dim3(nz, 1), kT2, smem, st>>>(N, nzc, d_aux, d_Z, d_nobs);
+  } else {
+    const size_t smem = (size_t)2 * NB2 * kT2 * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_eig_vectors32<NB2><<<dim3(nz, 2), kT2, smem, st>>>(N, nzc, d_aux, d_Z, d_nobs);
+  }
   return cudaGetLastError();
 }
 

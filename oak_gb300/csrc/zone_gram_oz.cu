@@ -1,0 +1,695 @@
+// K1 + K2 of the plain (FP64) form on the tensor cores, ensembles of up to 64 members.
+//
+// Selection and weights are those of zone_gram.cu (assimilation.F90:3683-3771): the relevance
+// decisions of the tensor-core mixed kernel (FP32 distances away from the thresholds, the
+// reference's FP64 evaluation near them; the selected set is identical to the plain form's),
+// and for every selected observation the FP64 weight w of zone_gram.cu (FP64 distance,
+// exp(-(d/L)^2) or locfun(d/L)). The Gram matrix G = HS_sel^T diag(c) HS_sel (rrsqrt.F90:135,
+// c = w (w / r), DCDCovar of rrsqrt.F90:395) is formed as X^T X with X = diag(|w| / sqrt(r))
+// HS_sel, in FP64, as an exact integer product on the BF16 tensor cores (the slice splitting
+// of Ozaki et al., "Error-free transformations of matrix multiplication by using fast routines
+// of matrix multiplication and its applications", Numer. Algorithms 59 (2012)):
+//
+//   Column a of X gets a fixed exponent E_a with |X_qa| <= 2^E_a for every observation q (from
+//   max_q |HS_qa| / sqrt(r_q), once per call), so F_qa = round(X_qa 2^(54 - E_a)) is
+//   an integer below 2^54 in magnitude, taken from the FP64 bit pattern with integer
+//   operations. F is written in 7 balanced base-256 digits, F = sum_p d_p 256^(6-p) with
+//   d_0 in [-64, 64] and d_1..d_6 in [-128, 127] (the bytes of F + 0x80808080808080 minus 128);
+//   every digit is exact in BF16.
+//   Then G_ab = 2^(E_a + E_b - 12) sum_L 256^-L level_L(a, b), level_L = sum_{p+q=L} D_p^T D_q
+//   (D_p the digit-p matrix of the zone's rows), for levels 0..6; the levels from 7 on weigh
+//   below 2^-56 of the column scale and are left out. A K-tile of 64 observations is staged as
+//   7 digit slices (64 members x 64 observations of BF16, K-major, 128-byte swizzle) and each
+//   K-step of 16 observations issues tcgen05.mma kind::f16 (BF16 x BF16 -> FP32) with
+//   A = [D_p ; D_(p+1)] (M = 128; only rows 0-63 are read back) and B = the run of slices whose
+//   level block lands in the right accumulator column: levels 0..3 in tensor-memory columns
+//   0..255 (4 MMAs a K-step), levels 4..6 in columns 256..447 (7 MMAs a K-step).
+//   Exactness: a digit product is at most 2^14 (2^13 with d_0), so the FP32 sums of levels 0..3
+//   stay exact integers below 2^24 over 256 observations; the accumulators are read every 4
+//   K-tiles and added into 64-bit integer sums (levels 0..3) and an FP32 sum of
+//   level_4 + level_5 / 256 + level_6 / 65536 (whose rounding weighs below 2^-56 of the column
+//   scale). At the end of the zone G = 2^(E_a + E_b - 36) (v + V456 / 256) with
+//   v = ((L0 256 + L1) 256 + L2) 256 + L3 as a 64-bit integer, converted once to FP64.
+//   The error of G is therefore the truncation of X to 54 bits below its column scale (and the
+//   dropped levels), not the length of the sums: about 2^-53 of max|X_a| max|X_b| per term.
+//
+// The innovation projection g = X^T (sqrt(c) d) (rrsqrt.F90:142) is accumulated in FP64 by the
+// staging threads (one FMA per staged element).
+//
+// Pipeline per CTA (one zone at a time, one CTA per SM: its shared memory and the 512
+// tensor-memory columns admit no second one): candidates are tested 256 at a time; selected
+// observations go to a ring of (index, |w| / sqrt(r), |w| / sqrt(r) d); every full K-tile is
+// staged into one of two shared buffers (7 slices) and handed to the tensor core by one thread
+// (44 MMAs and a commit to the buffer's mbarrier), so staging of the next tile overlaps the
+// MMAs. Every mbarrier wait is bounded; on expiry the kernel records ZST_TIMEOUT, stops taking
+// zones, waits (bounded) for its MMAs and frees its tensor memory.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "oakg_internal.cuh"
+#include "selection.cuh"
+
+namespace oakg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int NB = 64;                 // padded ensemble width
+constexpr int KT = 64;                 // observations per K-tile (128 bytes of BF16 a row)
+constexpr int kDigits = 7;
+constexpr int kRing = 512;             // selected-observation ring (power of two)
+constexpr uint32_t kSliceBytes = 64u * 128u;         // one digit slice of a K-tile
+constexpr uint32_t kBufBytes = kDigits * kSliceBytes;  // one K-tile buffer
+constexpr uint32_t kTmemCols = 512;
+constexpr int kWaitPolls = 1 << 22;
+constexpr int kFlushTiles = 4;         // K-tiles between accumulator reads (256 observations)
+constexpr int kTri = NB * (NB + 1) / 2;
+constexpr int kLevelsExact = 4;        // levels held as 64-bit integer sums
+constexpr unsigned long long kDigitBias = 0x80808080808080ull;
+// dynamic shared memory: alignment slack, two K-tile buffers, the slice past the second buffer
+// (rows 64-127 of the A operand of the last digit: read by the MMA, never read back), the
+// integer and FP32 level sums (lower triangle) and the FP64 innovation partials
+constexpr size_t kDynSmem = 1024 + 2 * (size_t)kBufBytes + kSliceBytes +
+                            (size_t)kLevelsExact * kTri * sizeof(long long) +
+                            (size_t)kTri * sizeof(float) + 4 * NB * sizeof(double);
+
+struct OzShared {
+  int32_t ring_q[kRing];
+  double ring_s[kRing];  // |w| / sqrt(r_q)
+  double ring_y[kRing];  // |w| / sqrt(r_q) (yo - Hxf)_q
+  unsigned long long mbar[2];
+  int32_t warp_cnt[kThreads / 32];
+  int32_t E[NB];         // column exponents
+  uint32_t tmem_base;
+  int32_t zone;
+  int32_t nrel;
+  int32_t flag;
+  int32_t bad;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1 << 16;                   // leading byte offset (unused: K fits one swizzle row)
+  d |= (uint64_t)(1024u >> 4) << 32;        // stride byte offset
+  d |= (uint64_t)1 << 46;                   // descriptor version
+  d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: D F32, A and B BF16, both K-major, M = 128, N = n
+__device__ __forceinline__ uint32_t idesc_bf16(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %3, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %4, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(accum), "r"(idesc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (int i = 0; i < kWaitPolls; i++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 8 consecutive accumulator columns of this warp's 32 tensor-memory lanes
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of the 16-byte chunk `chunk` (8 observations) of operand row `row` in a slice
+__device__ __forceinline__ uint32_t tile_off(int row, int chunk) {
+  return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
+}
+
+// round(x 2^(54 - E)) from the FP64 bit pattern (|x| <= 2^E); *bad set for a non-finite x or
+// one above the bound
+__device__ __forceinline__ long long fixed54(double x, int E, int& bad) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FFu);
+  if (ex == 0) return 0;  // zero or subnormal (below 2^-1022: far under the column scale)
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int sh = ex - 1021 - E;  // x 2^(54 - E) = mant 2^sh
+  long long F;
+  if (sh >= 0) {
+    if (sh > 1) {
+      bad = 1;
+      return 0;
+    }
+    F = (long long)(mant << sh);
+  } else {
+    const int r = -sh;
+    F = (r >= 62) ? 0 : (long long)((mant + (1ull << (r - 1))) >> r);
+  }
+  return (bits >> 63) ? -F : F;
+}
+
+// BF16 bits of the digit (byte - 128), exact: the FP32 value has at most 8 significant bits
+__device__ __forceinline__ uint32_t digit_bits(uint32_t byte) {
+  return __float_as_uint(__uint_as_float(0x4B3FFF80u + byte) - 12582912.f);
+}
+
+// 64-bit-integer / FP32 lower-triangle index of (row j, column c <= j)
+__device__ __forceinline__ int tri(int j) { return j * (j + 1) / 2; }
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_zone_gram_oz(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
+                   const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
+                   const double* __restrict__ max_len, const int32_t* __restrict__ col_exp,
+                   double* __restrict__ G, double* __restrict__ gv, int32_t* __restrict__ nobs,
+                   int brute, int32_t* __restrict__ work, int32_t* __restrict__ err,
+                   const int32_t* __restrict__ order) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  __shared__ __align__(16) OzShared ts;
+  const uint32_t raw_addr = smem_u32(dyn_raw);
+  const uint32_t pad = ((raw_addr + 1023u) & ~1023u) - raw_addr;
+  unsigned char* tiles = dyn_raw + pad;  // 2 x kBufBytes + one slice, 1024-aligned
+  const uint32_t tile_addr = raw_addr + pad;
+  long long* acc64 = reinterpret_cast<long long*>(tiles + 2 * kBufBytes + kSliceBytes);
+  float* accf = reinterpret_cast<float*>(acc64 + kLevelsExact * kTri);
+  double* gpart = reinterpret_cast<double*>(accf + kTri);  // [4][NB]
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // staging: member a, 8-observation chunks kq and kq + 4 of a K-tile
+  const int a = tid & (NB - 1), kq = tid >> 6;
+  const uint32_t mbar0 = smem_u32(&ts.mbar[0]);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ts.flag = 0;
+  }
+  if (tid < NB) ts.E[tid] = (tid < N) ? col_exp[tid] : 0;
+  // the slice past the second buffer is only read into accumulator rows that are never read
+  // back; it is cleared once so that those rows hold finite values
+  for (uint32_t i = tid; i < kSliceBytes / 16; i += kThreads)
+    reinterpret_cast<uint4*>(tiles + 2 * kBufBytes)[i] = make_uint4(0, 0, 0, 0);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ts.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = ts.tmem_base;
+  const int Ea = ts.E[a];
+
+  const int64_t ncells = (int64_t)g.nu * g.nv;
+  const int full_scan = brute || !lp.localise;
+  const bool fast = (lp.loctype != 1) || (lp.metric == OAKG_METRIC_CARTESIAN);
+  int pend0 = 0, pend1 = 0;   // buffer has MMAs not yet waited for (uniform)
+  uint32_t ph0 = 0, ph1 = 0;  // parity of the buffer's next completion (uniform)
+  bool abort = false;
+
+  // wait for buffer b's outstanding MMAs (thread 0, bounded); result published in ts.flag
+  auto drain = [&](int b) {
+    if (tid == 0) {
+      const uint32_t ph = b ? ph1 : ph0;
+      if (!mbar_wait(mbar0 + 8 * b, ph)) ts.flag = 1;
+    }
+    if (b) {
+      ph1 ^= 1u;
+      pend1 = 0;
+    } else {
+      ph0 ^= 1u;
+      pend0 = 0;
+    }
+  };
+
+  // add the accumulators into the level sums (all MMAs complete and published by a barrier).
+  // Warp w reads lanes 32 (w % 4) .. + 31, i.e. rows j of the lower (D_p) half for w % 4 < 2;
+  // warps 0-3 take levels 0..3, warps 4-7 levels 4..6; row j keeps columns c <= j.
+  auto flush = [&]() {
+    fence_after();
+    const int q = warp & 3, h = warp >> 2;
+    if (q < 2) {
+      const int j = 32 * q + lane;
+      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16);
+      const int ncol = 32 * (q + 1);  // warp-uniform bound of the row's lower triangle
+      const int tj = tri(j);
+      if (h == 0) {
+#pragma unroll
+        for (int L = 0; L < kLevelsExact; L++) {
+          long long* accL = acc64 + L * kTri + tj;
+          for (int c0 = 0; c0 < ncol; c0 += 8) {
+            float v[8];
+            tmem_ld8(ta + 64 * L + c0, v);
+#pragma unroll
+            for (int t = 0; t < 8; t++)
+              if (c0 + t <= j) accL[c0 + t] += (long long)__float2int_rn(v[t]);
+          }
+        }
+      } else {
+        float* af = accf + tj;
+        for (int c0 = 0; c0 < ncol; c0 += 8) {
+          float v4[8], v5[8], v6[8];
+          tmem_ld8(ta + 256 + c0, v4);
+          tmem_ld8(ta + 320 + c0, v5);
+          tmem_ld8(ta + 384 + c0, v6);
+#pragma unroll
+          for (int t = 0; t < 8; t++)
+            if (c0 + t <= j) af[c0 + t] += fmaf(v6[t], 1.f / 65536.f, fmaf(v5[t], 1.f / 256.f, v4[t]));
+        }
+      }
+    }
+    fence_before();
+    __syncthreads();
+  };
+
+  for (;;) {
+    if (tid == 0) ts.zone = atomicAdd(work, 1);
+    __syncthreads();
+    const int32_t w = ts.zone;  // pick number; zone order[z0 + w] when a pick order is given
+    if (w >= nzc || ts.flag) break;
+    const int32_t zl = order ? order[z0 + w] : w;
+    const int32_t z = z0 + zl;
+    const double zx = zone_xyzt[4 * (int64_t)z + 0], zy = zone_xyzt[4 * (int64_t)z + 1];
+    const double zzc = zone_xyzt[4 * (int64_t)z + 2], ztc = zone_xyzt[4 * (int64_t)z + 3];
+    const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
+    const double zv = (lp.loctype == 1) ? zy : 0.0;
+    const double L = corr_len[z], Rmax = max_len[z];
+    const float iL32 = (float)(1.0 / L);
+    const float r_lo = (float)Rmax * (1.f - 1e-6f), r_hi = (float)Rmax * (1.f + 1e-6f);
+    if (tid == 0) {
+      ts.nrel = 0;
+      ts.bad = 0;
+    }
+    for (int e = tid; e < kLevelsExact * kTri; e += kThreads) acc64[e] = 0;
+    for (int e = tid; e < kTri; e += kThreads) accf[e] = 0.f;
+    int head = 0, tail = 0, ntile = 0, ctile = 0, nrel_local = 0, bad = 0;
+    double gsum = 0.0;
+
+    // stage ring entries [head, head + rows) as one K-tile and issue its MMAs
+    auto do_tile = [&](int rows) {
+      if (ctile == kFlushTiles) {
+        if (pend0) drain(0);
+        if (pend1) drain(1);
+        __syncthreads();  // MMA completion and flag published
+        if (ts.flag) {
+          abort = true;
+          return;
+        }
+        flush();
+        ctile = 0;
+      }
+      const int b = ntile & 1;
+      if (b ? pend1 : pend0) drain(b);
+      __syncthreads();  // buffer free (flag published), ring entries visible
+      if (ts.flag) {
+        abort = true;
+        return;
+      }
+      unsigned char* tb = tiles + b * kBufBytes;
+#pragma unroll 1
+      for (int pass = 0; pass < 2; pass++) {
+        const int chunk = kq + 4 * pass;
+        uint32_t pk[kDigits][4];
+#pragma unroll
+        for (int i = 0; i < 8; i += 2) {
+          uint32_t lo2[2], hi2[2];
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            const int k = 8 * chunk + i + u;
+            long long F = 0;
+            if (k < rows && a < N) {
+              const int idx = (head + k) & (kRing - 1);
+              const int32_t q = ts.ring_q[idx];
+              const double X = ts.ring_s[idx] * so.HSt[(int64_t)q * N + a];
+              gsum = fma(X, ts.ring_y[idx], gsum);
+              F = fixed54(X, Ea, bad);
+            }
+            const unsigned long long U = (unsigned long long)F + kDigitBias;
+            lo2[u] = (uint32_t)U;
+            hi2[u] = (uint32_t)(U >> 32);
+          }
+          const int wd = i >> 1;
+          // digit p is byte 6 - p of U: p = 0..2 in the high word, 3..6 in the low word
+#pragma unroll
+          for (int p = 0; p < kDigits; p++) {
+            const int byte = 6 - p;
+            const uint32_t b0 = (byte >= 4) ? (hi2[0] >> (8 * (byte - 4))) & 255u
+                                            : (lo2[0] >> (8 * byte)) & 255u;
+            const uint32_t b1 = (byte >= 4) ? (hi2[1] >> (8 * (byte - 4))) & 255u
+                                            : (lo2[1] >> (8 * byte)) & 255u;
+            pk[p][wd] = __byte_perm(digit_bits(b0), digit_bits(b1), 0x7632);
+          }
+        }
+#pragma unroll
+        for (int p = 0; p < kDigits; p++)
+          *reinterpret_cast<uint4*>(tb + p * kSliceBytes + tile_off(a, chunk)) =
+              make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();  // tile complete
+      if (tid == 0) {
+        fence_after();
+        const uint32_t base = tile_addr + b * kBufBytes;
+#pragma unroll 1
+        for (int kk = 0; kk < KT / 16; kk++) {
+          const uint32_t ko = kk * 32;
+          const uint32_t acc0 = (ctile > 0 || kk > 0) ? 1u : 0u;
+          // levels 0..3, columns 64 L: A = [D_p ; D_p+1], B = D_0 .. D_(3-p) into L = p .. 3
+#pragma unroll
+          for (int p = 0; p < 4; p++)
+            mma_bf16(tmem + 64 * p, make_desc(base + p * kSliceBytes + ko), make_desc(base + ko),
+                     idesc_bf16(64u * (4 - p)), p == 0 ? acc0 : 1u);
+          // levels 4..6, columns 256 + 64 (L - 4): B = D_qlo .. D_qhi, q = L - p
+#pragma unroll
+          for (int p = 0; p < kDigits; p++) {
+            const int qlo = (4 - p > 0) ? 4 - p : 0;
+            const int qhi = (6 - p < kDigits - 1) ? 6 - p : kDigits - 1;
+            const int off = qlo - (4 - p);
+            mma_bf16(tmem + 256 + 64 * off, make_desc(base + p * kSliceBytes + ko),
+                     make_desc(base + qlo * kSliceBytes + ko),
+                     idesc_bf16(64u * (qhi - qlo + 1)), p == 0 ? acc0 : 1u);
+          }
+        }
+        mma_commit(mbar0 + 8 * b);
+      }
+      if (b)
+        pend1 = 1;
+      else
+        pend0 = 1;
+      ntile++;
+      ctile++;
+      head += rows;
+    };
+
+    sel::ScanRange sr;
+    if (full_scan) {
+      sr.cu0 = 0;
+      sr.cu1 = g.nu - 1;
+      sr.cv0 = 0;
+      sr.cv1 = g.nv - 1;
+      sr.all_u = 1;
+    } else {
+      sr = sel::zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
+    }
+    for (int cv = sr.cv0; cv <= sr.cv1 && !abort; cv++) {
+      for (int part = 0; part < 2 && !abort; part++) {
+        int cu_a, cu_b;
+        if (sr.all_u) {
+          if (part) break;
+          cu_a = 0;
+          cu_b = g.nu - 1;
+        } else if (!g.periodic_u) {
+          if (part) break;
+          cu_a = sr.cu0;
+          cu_b = sr.cu1;
+        } else {
+          const int a0 = sr.cu0, b0 = sr.cu1;
+          if (a0 < 0) {
+            cu_a = part ? 0 : a0 + g.nu;
+            cu_b = part ? b0 : g.nu - 1;
+          } else if (b0 >= g.nu) {
+            cu_a = part ? 0 : a0;
+            cu_b = part ? b0 - g.nu : g.nu - 1;
+          } else {
+            if (part) break;
+            cu_a = a0;
+            cu_b = b0;
+          }
+        }
+        const int64_t c_lo = (int64_t)cu_a + (int64_t)g.nu * cv;
+        const int64_t c_hi = (int64_t)cu_b + (int64_t)g.nu * cv;
+        if (c_lo > c_hi || c_lo < 0 || c_hi >= ncells) continue;
+        const int32_t q_lo = so.cell_start[c_lo], q_hi = so.cell_start[c_hi + 1];
+        for (int32_t qb = q_lo; qb < q_hi && !abort; qb += kThreads) {
+          const int32_t q = qb + tid;
+          int sel = 0, rel = 0;
+          double w64 = 0.0;
+          bool have_w = false;
+          if (q < q_hi) {
+            // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
+            bool done = false;
+            if (fast) {
+              const double du = so.u[q] - zu;
+              double D2 = du * du;
+              if (lp.loctype == 1) {
+                const double dv = so.v[q] - zv;
+                D2 = fma(dv, dv, D2);
+              }
+              const float d32 = sqrtf((float)D2);  // relative error < 2e-7
+              const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
+              if (inside >= 0) {
+                const float r32 = d32 * iL32;
+                if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+                  rel = inside;
+                  done = true;
+                } else if (r32 >= 2.f + 1e-5f) {  // locfun = 0
+                  rel = 0;
+                  done = true;
+                } else if (r32 <= 2.f - 1e-3f) {  // locfun > 3e-13, far above its FP64 rounding
+                  rel = inside;
+                  done = true;
+                }
+              }
+            }
+            if (!done) {
+              double d;
+              if (lp.loctype == 1)
+                d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
+              else
+                d = fabs(__dsub_rn(so.u[q], zu));
+              if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+                rel = (d <= Rmax);
+                const double t = d / L;
+                w64 = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
+              } else {
+                w64 = sel::locfun(d / L);
+                rel = (d <= Rmax) && (w64 != 0.0);
+              }
+              have_w = true;
+            }
+            sel = rel || !lp.localise;
+            if (sel && !have_w) {  // the plain form's FP64 weight (zone_gram.cu)
+              double d;
+              if (lp.loctype == 1)
+                d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
+              else
+                d = fabs(__dsub_rn(so.u[q], zu));
+              if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+                const double t = d / L;
+                w64 = exp(-(t * t));
+              } else {
+                w64 = sel::locfun(d / L);
+              }
+            }
+          }
+          nrel_local += rel;
+          const unsigned ball = __ballot_sync(0xffffffffu, sel);
+          if (lane == 0) ts.warp_cnt[warp] = __popc(ball);
+          __syncthreads();
+          int before = 0, total = 0;
+#pragma unroll
+          for (int w2 = 0; w2 < kThreads / 32; w2++) {
+            const int cnt = ts.warp_cnt[w2];
+            before += (w2 < warp) ? cnt : 0;
+            total += cnt;
+          }
+          if (sel) {
+            // c = w (w / r) (DCDCovar, covariance.F90:612-619); sqrt(c) = |w| / sqrt(r)
+            const double sc = fabs(w64) * rsqrt(so.r[q]);
+            const int slot = (tail + before + __popc(ball & ((1u << lane) - 1u))) & (kRing - 1);
+            ts.ring_q[slot] = q;
+            ts.ring_s[slot] = sc;
+            ts.ring_y[slot] = sc * so.innov[q];
+          }
+          __syncthreads();
+          tail += total;
+          while (tail - head >= KT && !abort) do_tile(KT);
+        }
+      }
+    }
+    if (!abort && tail > head) do_tile(tail - head);
+    if (abort) break;
+    // relevant-observation count of the zone
+    for (int o = 16; o > 0; o >>= 1) nrel_local += __shfl_xor_sync(0xffffffffu, nrel_local, o);
+    if (lane == 0) atomicAdd(&ts.nrel, nrel_local);
+    if (bad) atomicOr(&ts.bad, 1);
+    gpart[kq * NB + a] = gsum;
+    if (ntile > 0) {
+      if (pend0) drain(0);
+      if (pend1) drain(1);
+    }
+    __syncthreads();  // nrel, bad, partials and the MMA completion published
+    if (ts.flag) break;
+    const int nrel = ts.nrel;
+    if (tid == 0) nobs[z] = nrel;
+    if (nrel > 0 && ntile > 0) {
+      flush();
+      double* Gz = G + (int64_t)zl * N * N;
+      const bool zbad = ts.bad != 0;
+      for (int e = tid; e < kTri; e += kThreads) {
+        int j = (int)((__fsqrt_rn((float)(8 * e + 1)) - 1.0f) * 0.5f);
+        while ((j + 1) * (j + 2) / 2 <= e) j++;
+        while (j * (j + 1) / 2 > e) j--;
+        const int c = e - tri(j);
+        if (j >= N) continue;
+        const long long v =
+            ((acc64[e] * 256 + acc64[kTri + e]) * 256 + acc64[2 * kTri + e]) * 256 +
+            acc64[3 * kTri + e];
+        // 2^(E_j + E_c - 36), a power of two in the normal range for any practical scale
+        int ex = ts.E[j] + ts.E[c] - 36 + 1023;
+        ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+        const double scale = __longlong_as_double((long long)ex << 52);
+        double val = fma((double)accf[e], 1.0 / 256.0, (double)v) * scale;
+        if (zbad) val = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input
+        Gz[j * N + c] = val;
+        Gz[c * N + j] = val;
+      }
+      if (tid < N)
+        gv[(int64_t)zl * N + tid] =
+            ((gpart[tid] + gpart[NB + tid]) + gpart[2 * NB + tid]) + gpart[3 * NB + tid];
+    }
+    __syncthreads();  // G staging and partials consumed before the next zone's tiles
+  }
+  // teardown: no MMA may still write tensor memory when it is freed
+  if (pend0) drain(0);
+  if (pend1) drain(1);
+  if (tid == 0 && ts.flag) atomicOr(err, ZST_TIMEOUT);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+}
+
+// column exponents: E_a with max_q |HS_qa| r_q^-1/2 (1 + 2^-20) <= 2^E_a (|w| <= 1, so every
+// |X_qa| of every zone is below it). The maxima of non-negative FP64 values are taken on their
+// bit patterns (ordered like the values). Non-finite values and r <= 0 are left out: the zones
+// that select such an observation get a non-finite weight or element, which marks their G as
+// NaN (as the CUDA-core products would propagate it); the other zones keep the scale of the
+// finite data.
+__global__ void k_oz_colmax(int64_t m, int N, const double* __restrict__ HSt,
+                            const double* __restrict__ r, unsigned long long* __restrict__ mx) {
+  __shared__ unsigned long long smax[NB];
+  if (threadIdx.x < NB) smax[threadIdx.x] = 0ull;
+  __syncthreads();
+  const int a = threadIdx.x & (NB - 1);
+  unsigned long long loc = 0ull;
+  if (a < N) {
+    for (int64_t q = blockIdx.x * (int64_t)(blockDim.x / NB) + threadIdx.x / NB; q < m;
+         q += (int64_t)gridDim.x * (blockDim.x / NB)) {
+      const double rq = r[q];
+      if (!(rq > 0.0) || !(rq < INFINITY)) continue;
+      const double v = fabs(HSt[q * N + a]) * rsqrt(rq);
+      const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
+      if (vb < 0x7FF0000000000000ull) loc = vb > loc ? vb : loc;
+    }
+    atomicMax(&smax[a], loc);
+  }
+  __syncthreads();
+  if (threadIdx.x < N) atomicMax(&mx[threadIdx.x], smax[threadIdx.x]);
+}
+
+__global__ void k_oz_exponents(int N, const unsigned long long* __restrict__ mx,
+                               int32_t* __restrict__ E) {
+  const int a = threadIdx.x;
+  if (a >= N) return;
+  const double vmax = __longlong_as_double((long long)mx[a]);
+  int e;
+  if (vmax == 0.0) {
+    e = 0;  // an all-zero column (or no usable observation)
+  } else {
+    const double v = vmax * (1.0 + 0x1p-20);
+    if (!(v < INFINITY)) {
+      e = -4000;  // beyond the FP64 range: every nonzero element is out of range (G is NaN)
+    } else {
+      // v in [2^(k-1), 2^k) with k = biased exponent - 1022 (normal v)
+      const int be = (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF);
+      e = (be == 0) ? -1022 : be - 1022;
+    }
+  }
+  E[a] = e;
+}
+
+}  // namespace
+
+int gram_oz_max_n() { return NB; }
+
+size_t gram_oz_scratch_bytes() { return NB * sizeof(unsigned long long) + NB * sizeof(int32_t); }
+
+cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int N, LocParams lp,
+                         int32_t z0, int32_t nzc, const double* zone_xyzt, const double* corr_len,
+                         const double* max_len, double* d_G, double* d_g, int32_t* d_nobs,
+                         int brute, int32_t* d_work, int32_t* d_err, void* d_scratch,
+                         cudaStream_t st, const int32_t* order) {
+  if (N < 1 || N > NB || !so.HSt || !so.r || !d_scratch) return cudaErrorInvalidValue;
+  unsigned long long* mx = reinterpret_cast<unsigned long long*>(d_scratch);
+  int32_t* E = reinterpret_cast<int32_t*>(mx + NB);
+  cudaError_t e = cudaMemsetAsync(mx, 0, NB * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (m > 0) {
+    const int64_t per = kThreads / NB;
+    int64_t blocks = (m + per - 1) / per;
+    if (blocks > 4 * (int64_t)sms) blocks = 4 * (int64_t)sms;
+    k_oz_colmax<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, 0, st>>>(m, N, so.HSt, so.r, mx);
+    count_launches(1);
+  }
+  k_oz_exponents<<<1, NB, 0, st>>>(N, mx, E);
+  count_launches(1);
+  e = cudaFuncSetAttribute(k_zone_gram_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kDynSmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_zone_gram_oz, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  // the shared-memory size admits one CTA per SM (it holds all 512 tensor-memory columns)
+  int grid = sms;
+  if (grid > nzc) grid = nzc > 0 ? nzc : 1;
+  e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
+  if (e != cudaSuccess) return e;
+  k_zone_gram_oz<<<grid, kThreads, kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
+                                                   max_len, E, d_G, d_g, d_nobs, brute, d_work,
+                                                   d_err, order);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace oakg

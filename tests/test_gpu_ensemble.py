@@ -101,6 +101,35 @@ def test_ens2sqrt_sqrt2ens_match_oracle(oakg, device):
                            rtol=1e-12, atol=1e-12)
 
 
+@pytest.mark.parametrize("N", [2, 33, 65, 100])
+def test_sqrt2ens_identity_and_general_theta(oakg, N):
+    """Theta = I takes the closed form (registers up to 64 anomaly columns, two reads of S
+    beyond), a general Theta the library GEMM; both against the oracle's N x (N-1) product, on
+    device arrays with padded leading dimensions; ens2sqrt gives back the mean and S S^T."""
+    import torch
+    rng = np.random.default_rng(200 + N)
+    n = 2500
+    dev = torch.device("cuda:0")
+    S_full = torch.as_tensor(rng.standard_normal((N - 1, n + 7)), device=dev)
+    S = S_full.t()[:n]  # column-major, ldS = n + 7
+    mean = torch.as_tensor(rng.standard_normal(n), device=dev)
+    S_np, mean_np = S.cpu().numpy(), mean.cpu().numpy()
+    E = oakg.sqrt2ens(mean, S).cpu().numpy()
+    assert np.allclose(E, oakref.sqrt2ens(mean_np, S_np), rtol=1e-12, atol=1e-12)
+    theta, _ = np.linalg.qr(rng.standard_normal((N - 1, N - 1)))
+    th = torch.as_tensor(np.ascontiguousarray(theta.T), device=dev).t()
+    E2 = oakg.sqrt2ens(mean, S, th).cpu().numpy()
+    assert np.allclose(E2, oakref.sqrt2ens(mean_np, S_np, theta), rtol=1e-12, atol=1e-12)
+    # ens2sqrt inverts it: the same mean and covariance S S^T (the same S for Theta = I)
+    Edev = lambda E_: torch.as_tensor(np.ascontiguousarray(E_.T), device=dev).t()
+    m2, S2 = (t.cpu().numpy() for t in oakg.ens2sqrt(Edev(E)))
+    assert np.allclose(m2, mean_np, rtol=1e-12, atol=1e-12)
+    assert np.allclose(S2, S_np, rtol=1e-12, atol=1e-12)
+    m3, S3 = (t.cpu().numpy() for t in oakg.ens2sqrt(Edev(E2)))
+    assert np.allclose(m3, mean_np, rtol=1e-12, atol=1e-12)
+    assert np.allclose(S3 @ S3.T, S_np @ S_np.T, rtol=1e-11, atol=1e-11)
+
+
 def test_ens_analysis_matches_oracle(oakg):
     rng = np.random.default_rng(22)
     n, N, m = 4000, 30, 300
