@@ -33,46 +33,27 @@ inline unsigned grid_for(int64_t n) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
-// mean and scaled anomalies of the rows of E (rows x N, leading dimension ldE)
-__global__ void k_mean_anomalies(int64_t rows, int N, const double* __restrict__ E, int64_t ldE,
-                                 double scaling, double* __restrict__ mean,
-                                 double* __restrict__ S, int64_t ldS) {
+// mean and scaled anomalies of the rows of E (rows x N, leading dimension ldE). A thread takes
+// a row: the sum over the members, then (E - mean) / scaling as one FMA, E (1/scaling) -
+// mean (1/scaling): its error is within an ulp of mean / scaling, the resolution E itself has
+// at the mean's magnitude. The FP64 pipe is what bounds this kernel (the row's E is read twice,
+// the second time from L2): two FP64 operations an element instead of three (subtract,
+// multiply) is what lets it approach the HBM rate.
+__global__ void __launch_bounds__(kThreads)
+    k_mean_anomalies(int64_t rows, int N, const double* __restrict__ E, int64_t ldE,
+                     double scaling, double* __restrict__ mean, double* __restrict__ S,
+                     int64_t ldS) {
+  const double isc = 1.0 / scaling;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
        i += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
+#pragma unroll 8
     for (int k = 0; k < N; k++) s += E[i + (int64_t)k * ldE];
     const double mu = s / N;
     mean[i] = mu;
-    // a product by 1/scaling, not a division: GB300's FP64 division is a multi-instruction
-    // sequence on the slow FP64 pipe, which bounded this kernel (within an ulp of the quotient)
-    const double isc = 1.0 / scaling;
-    for (int k = 0; k < N; k++) S[i + (int64_t)k * ldS] = (E[i + (int64_t)k * ldE] - mu) * isc;
-  }
-}
-
-// The same for N <= 64 with the row's members held in registers: E is read once, and the 64
-// loads of a row are independent (each coalesced across the warp), so they are all in flight
-// together. Same arithmetic: sequential sum over k, mean, (E - mean) * (1 / scaling).
-constexpr int kRegMembers = 64;
-__global__ void __launch_bounds__(kThreads)
-    k_mean_anomalies_reg(int64_t rows, int N, const double* __restrict__ E, int64_t ldE,
-                         double scaling, double* __restrict__ mean, double* __restrict__ S,
-                         int64_t ldS) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double v[kRegMembers];
-#pragma unroll
-    for (int k = 0; k < kRegMembers; k++) v[k] = (k < N) ? E[i + (int64_t)k * ldE] : 0.0;
-    double s = 0.0;
-#pragma unroll
-    for (int k = 0; k < kRegMembers; k++)
-      if (k < N) s += v[k];
-    const double mu = s / N;
-    mean[i] = mu;
-    const double isc = 1.0 / scaling;
-#pragma unroll
-    for (int k = 0; k < kRegMembers; k++)
-      if (k < N) S[i + (int64_t)k * ldS] = (v[k] - mu) * isc;
+    const double off = -mu * isc;
+#pragma unroll 8
+    for (int k = 0; k < N; k++) S[i + (int64_t)k * ldS] = fma(E[i + (int64_t)k * ldE], isc, off);
   }
 }
 
@@ -109,8 +90,8 @@ __global__ void k_epilogue(int64_t n, int N, const double* __restrict__ xf,
       if (x - mc > f) x = f + mc;  // the reference's two where() in this order
       if (x < f - mc) x = f - mc;
     }
-    for (int k = 0; k < N; k++)
-      Ea[i + (int64_t)k * ldE] = x + scaling * (mult * Sa[i + (int64_t)k * ldS]);
+    const double f = scaling * mult;  // one FMA an element: the FP64 pipe bounds this loop
+    for (int k = 0; k < N; k++) Ea[i + (int64_t)k * ldE] = fma(f, Sa[i + (int64_t)k * ldS], x);
   }
 }
 
@@ -128,7 +109,8 @@ __global__ void k_ens2sqrt(int64_t rows, int N, const double* __restrict__ E, in
     const double mu = s / N;
     mean[i] = mu;
     const double shift = (1.0 - alpha) * mu + alpha * E[i + (int64_t)(N - 1) * ldE];
-    for (int k = 0; k < N - 1; k++) S[i + (int64_t)k * ldS] = (E[i + (int64_t)k * ldE] - shift) * isc;
+    const double off = -shift * isc;  // (E - shift) / sqrt(N - 1) as one FMA (as the prologue)
+    for (int k = 0; k < N - 1; k++) S[i + (int64_t)k * ldS] = fma(E[i + (int64_t)k * ldE], isc, off);
   }
 }
 
@@ -169,6 +151,7 @@ __global__ void __launch_bounds__(kThreads)
 //   E(:, i) = mean + sqrt(N-1) (S(:, i) + a w^2 rs),  E(:, N-1) = mean + sqrt(N-1) a (w+1) w rs,
 // rs the row sums of S: one read of S and one write of E, with no N x N-1 product. Rows with
 // K <= 64 anomaly columns keep them in registers; longer rows read S twice.
+constexpr int kRegMembers = 64;
 template <bool kReg>
 __global__ void __launch_bounds__(kThreads)
     k_sqrt2ens_identity(int64_t rows, int N, const double* __restrict__ mean,
@@ -188,17 +171,18 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
       for (int k = 0; k < kRegMembers; k++)
         if (k < K) rs += v[k];
-      const double add = cw * rs;
+      // mean + sqrt(N-1) (S + a w^2 rs) as one FMA an element (the FP64 pipe bounds the loop)
+      const double base = fma(sc * cw, rs, mu);
 #pragma unroll
       for (int k = 0; k < kRegMembers; k++)
-        if (k < K) E[i + (int64_t)k * ldE] = mu + sc * (v[k] + add);
-      E[i + (int64_t)K * ldE] = mu + cl * rs;
+        if (k < K) E[i + (int64_t)k * ldE] = fma(sc, v[k], base);
+      E[i + (int64_t)K * ldE] = fma(cl, rs, mu);
     } else {
       double rs = 0.0;
       for (int k = 0; k < K; k++) rs += S[i + (int64_t)k * ldS];
-      const double add = cw * rs;
-      for (int k = 0; k < K; k++) E[i + (int64_t)k * ldE] = mu + sc * (S[i + (int64_t)k * ldS] + add);
-      E[i + (int64_t)K * ldE] = mu + cl * rs;
+      const double base = fma(sc * cw, rs, mu);
+      for (int k = 0; k < K; k++) E[i + (int64_t)k * ldE] = fma(sc, S[i + (int64_t)k * ldS], base);
+      E[i + (int64_t)K * ldE] = fma(cl, rs, mu);
     }
   }
 }
@@ -300,10 +284,7 @@ cudaError_t ensemble_prologue(int64_t n, int N, const double* Ef, int64_t ldE, i
                               double* xf, double* Sf, int64_t ldS, double* Hxf, double* HSf,
                               int64_t ldH, double* HEf_scratch, cudaStream_t st) {
   const double scaling = sqrt((double)N - 1.0);
-  if (N <= kRegMembers)
-    k_mean_anomalies_reg<<<grid_for(n), kThreads, 0, st>>>(n, N, Ef, ldE, scaling, xf, Sf, ldS);
-  else
-    k_mean_anomalies<<<grid_for(n), kThreads, 0, st>>>(n, N, Ef, ldE, scaling, xf, Sf, ldS);
+  k_mean_anomalies<<<grid_for(n), kThreads, 0, st>>>(n, N, Ef, ldE, scaling, xf, Sf, ldS);
   count_launches(1);
   if (m > 0) {
     k_obsoper<<<grid_for(m * (int64_t)N), kThreads, 0, st>>>(m, N, K, idx, w, shift, Ef, ldE,

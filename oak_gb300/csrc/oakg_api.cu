@@ -351,7 +351,7 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
     return rc;
   unsigned char* d_oz = nullptr;  // column exponents of the plain form's tensor-core Gram
   if (sizeof(R) == sizeof(double) &&
-      (rc = scratch(c, B_OZSCR, gram_oz_scratch_bytes(), &d_oz, "Gram exponents")))
+      (rc = scratch(c, B_OZSCR, gram_oz_scratch_bytes(a.so.m), &d_oz, "Gram exponents")))
     return rc;
   *status_all = d_work + 2;
   k_set_int<<<1, 1, 0, st>>>(*status_all, 0);

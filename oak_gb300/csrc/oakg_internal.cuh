@@ -86,10 +86,10 @@ cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParam
 // Plain form on the tensor cores (zone_gram_oz.cu), N <= gram_oz_max_n(): G as an exact
 // product of 8-bit slices of X = diag(|w| / sqrt(r)) HS_sel on BF16 tensor cores, combined in
 // 64-bit integers and FP64; the same selection, weights and outputs as zone_gram_fp64. d_scratch:
-// gram_oz_scratch_bytes() of device memory (column exponents). d_err receives ZST_TIMEOUT (OR)
-// if a bounded device wait expired.
+// gram_oz_scratch_bytes(m) of device memory (column exponents, r^-1/2). d_err receives
+// ZST_TIMEOUT (OR) if a bounded device wait expired.
 int gram_oz_max_n();
-size_t gram_oz_scratch_bytes();
+size_t gram_oz_scratch_bytes(int64_t m);
 cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int N, LocParams lp,
                          int32_t z0, int32_t nzc, const double* zone_xyzt, const double* corr_len,
                          const double* max_len, double* d_G, double* d_g, int32_t* d_nobs,
@@ -192,8 +192,7 @@ cudaError_t zone_eig_refine(int N, int32_t nzc, const float* d_G0, float* d_Z, f
                             const int32_t* d_nobs, float* d_S, cudaStream_t st);
 
 // ---- zone_eig32.cu: FP32 stages for N <= eig32_max_n() (one block per zone), used by
-// zone_eig_fp32 (same arguments as its stages); eig32_values and eig32_vectors also take
-// N <= eig128_max_n() (bisection, and the shared-memory inverse iteration on 128 rows)
+// zone_eig_fp32 (same arguments as its stages)
 int eig32_max_n();
 cudaError_t eig32_tridiag(int N, int32_t nzc, float* d_GT, float* d_aux, const int32_t* d_nobs,
                           cudaStream_t st);

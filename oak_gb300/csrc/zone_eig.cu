@@ -40,6 +40,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNMax = 128;               // largest N of the eigensolve stages
+constexpr int kT64 = 32;    // threads a block of the FP64 E2a / E2b kernels for N <= kNV64
+constexpr int kNV64 = 64;
 constexpr int kMaxSweepsPerN = 30;
 constexpr int32_t kFewZones = 152;  // below this zone count E2a runs one block per zone
 
@@ -109,8 +111,11 @@ __global__ void __launch_bounds__(kThreads)
     }
     R* Gz = GT + (int64_t)zl * N * N;
     R* ax = aux + (int64_t)zl * aux_stride(N);
-    R amax = 0;
-    for (int idx = tid; idx < N * N; idx += kThreads) amax = fmax(amax, fabs(Gz[idx]));
+    R amax = 0;  // G is symmetric: its lower triangle (the half read below) holds the maximum
+    for (int idx = tid; idx < N * N; idx += kThreads) {
+      const int i = idx / N, j = idx - i * N;
+      if (j <= i) amax = fmax(amax, fabs(Gz[idx]));
+    }
     for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     if (lane == 0) red[warp] = amax;
     __syncthreads();
@@ -219,6 +224,118 @@ __global__ void __launch_bounds__(128)
   const R eps = Prec<R>::eps();
   R* ax = aux + (int64_t)zl * aux_stride(N);
   R d[kNMax], e[kNMax];
+  R onenrm = 0;
+  for (int i = 0; i < N; i++) {
+    d[i] = ax[i];
+    e[i] = (i < N - 1) ? ax[N + i] : R(0);
+  }
+  for (int i = 0; i < N; i++) {
+    R s = fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : R(0));
+    onenrm = fmax(onenrm, s);
+  }
+  const R scale = ax[5 * N];
+  int st = 0;
+  int hi = N - 1, sweeps = 0;
+  const int max_sweeps = kMaxSweepsPerN * N;
+  const R abs_tol = eps * onenrm;  // deflation floor: the rounding level of Tri
+  while (hi > 0) {
+    while (hi > 0) {
+      R t = fabs(e[hi - 1]);
+      if (t <= eps * (fabs(d[hi - 1]) + fabs(d[hi])) || t <= abs_tol) {
+        e[hi - 1] = 0;
+        hi--;
+      } else {
+        break;
+      }
+    }
+    if (hi == 0) break;
+    int lo = hi - 1;
+    while (lo > 0) {
+      R t = fabs(e[lo - 1]);
+      if (t <= eps * (fabs(d[lo - 1]) + fabs(d[lo])) || t <= abs_tol) {
+        e[lo - 1] = 0;
+        break;
+      }
+      lo--;
+    }
+    if (++sweeps > max_sweeps) {
+      st |= ZST_EIG;
+      break;
+    }
+    const R a = d[hi - 1], b = d[hi], f = e[hi - 1];
+    const R del = R(0.5) * (a - b);
+    const R den = del + copysign(Prec<R>::sqrt_(del * del + f * f), del == R(0) ? R(1) : del);
+    const R mu = (den == R(0)) ? b : b - f * f / den;
+    R x = d[lo] - mu, z = e[lo], bulge = 0;
+    for (int k = lo; k < hi; k++) {
+      if (k > lo) {
+        x = e[k - 1];
+        z = bulge;
+      }
+      const R r2 = x * x + z * z;
+      R c = 1, s = 0, r = 0;
+      if (r2 > R(0)) {
+        const R ri = Prec<R>::rsqrt_(r2);
+        c = x * ri;
+        s = z * ri;
+        r = r2 * ri;
+      }
+      if (k > lo) e[k - 1] = r;
+      const R dk = d[k], dk1 = d[k + 1], ek = e[k];
+      const R ek1 = (k + 1 < hi) ? e[k + 1] : R(0);
+      const R cc = c * c, ss = s * s, cs = c * s;
+      d[k] = cc * dk + R(2) * cs * ek + ss * dk1;
+      d[k + 1] = ss * dk - R(2) * cs * ek + cc * dk1;
+      e[k] = cs * (dk1 - dk) + (cc - ss) * ek;
+      if (k + 1 < hi) e[k + 1] = c * ek1;
+      bulge = s * ek1;
+    }
+  }
+  // ascending order (insertion sort)
+  for (int i = 1; i < N; i++) {
+    R t = d[i];
+    int k = i - 1;
+    while (k >= 0 && d[k] > t) {
+      d[k + 1] = d[k];
+      k--;
+    }
+    d[k + 1] = t;
+  }
+  R prev = 0;
+  for (int j = 0; j < N; j++) {
+    ax[3 * N + j] = d[j] * scale;
+    R s = d[j];
+    if (j > 0) {
+      const R pert = R(10) * eps * fabs(s);
+      if (s - prev < pert) s = prev + pert;
+    }
+    ax[4 * N + j] = s;
+    prev = s;
+  }
+  ax[5 * N + 1] = onenrm;
+  if (st) status[zl] |= st;
+}
+
+// strided per-thread view of a shared array: element i at [i * kT64]
+template <typename R>
+struct SArr {
+  R* p;
+  __device__ __forceinline__ R& operator[](int i) const { return p[i * kT64]; }
+};
+
+// The same for N <= kNV64 in FP64 with d and e in shared memory (element i of thread t at
+// [i * kT64 + t]) instead of per-thread local arrays, which the L1 cannot hold for a full SM
+// of threads: identical arithmetic in the same order, so the same eigenvalues bit for bit.
+__global__ void __launch_bounds__(kT64)
+    k_eig_values_fp64s(int N, int32_t nzc, double* __restrict__ aux,
+                       const int32_t* __restrict__ nobs, int32_t* __restrict__ status) {
+  using R = double;
+  __shared__ R sd[kNV64 * kT64], se[kNV64 * kT64];
+  const int32_t zl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (zl >= nzc || nobs[zl] == 0) return;  // no barrier below
+  const R eps = Prec<R>::eps();
+  R* ax = aux + (int64_t)zl * aux_stride(N);
+  SArr<R> d{sd + threadIdx.x}, e{se + threadIdx.x};
   R onenrm = 0;
   for (int i = 0; i < N; i++) {
     d[i] = ax[i];
@@ -518,8 +635,6 @@ __global__ void __launch_bounds__(128)
 // consecutive threads, consecutive words) and its second superdiagonal as one bit per row (it
 // is the tridiagonal's next off-diagonal entry where rows were swapped, else 0). 32 KB a
 // block: seven warps per SM.
-constexpr int kT64 = 32;
-constexpr int kNV64 = 64;
 
 // 1/p by two Newton steps from the FP32 reciprocal (relative error below 2^-52, not always
 // correctly rounded). The IEEE FP64 division is a called routine whose call keeps the live
@@ -692,7 +807,9 @@ __global__ void __launch_bounds__(kThreads)
   R* t1 = t0 + N;       // [N]
   R* vv = t1 + N;       // [N]
   R* qs = vv + N;       // [N] lambda^(1/4)        (evaluated in FP64)
-  int* cst = reinterpret_cast<int*>(qs + N);  // [N] cluster start of each eigenvector
+  R* cf = qs + N;       // [4][N] back-transform coefficients of four reflectors
+  R* pc = cf + 4 * N;   // [3][N] reflector couplings p_s[k] = v_k . v_(k-s), s = 1, 2, 3
+  int* cst = reinterpret_cast<int*>(pc + 3 * N);  // [N] cluster start of each eigenvector
   __shared__ R red[kWarps];
   __shared__ int32_t s_zone;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -818,8 +935,59 @@ __global__ void __launch_bounds__(kThreads)
       for (int i = tid; i < N; i += kThreads) U[i * ld + j] *= sc;
       __syncthreads();
     }
-    // U = Q_h Z = H_0 H_1 ... H_{N-3} Z: apply H_k for k = N-3 .. 0
-    for (int k = N - 3; k >= 0; k--) {
+    // U = Q_h Z = H_0 H_1 ... H_{N-3} Z, H_k = I - b_k v_k v_k^T (v_k below the diagonal of
+    // column k of A): four reflectors at a time, k, k-1, k-2, k-3 in that order. The four dots
+    // d_r = v_(k-r) . u_j of the unchanged column u_j are independent (one thread each, all
+    // 4 x N of them at once); the coefficients follow from c_r = b_(k-r) (d_r - sum_(r'<r) c_r'
+    // v_(k-r) . v_(k-r')), and one pass subtracts sum_r c_r v_(k-r): three barriers per four
+    // reflectors instead of eight, the same products as one reflector at a time.
+    for (int kk = tid; kk < N - 2; kk += kThreads) {
+#pragma unroll
+      for (int sft = 1; sft <= 3; sft++) {
+        R sp = 0;
+        if (kk >= sft)  // v_kk and v_(kk-s) overlap on rows kk + 1 .. N - 1
+          for (int i = kk + 1; i < N; i++) sp = fma(Aw[i * la + kk], Aw[i * la + kk - sft], sp);
+        pc[(sft - 1) * N + kk] = sp;
+      }
+    }
+    __syncthreads();
+    int kb = N - 3;
+    for (; kb >= 3; kb -= 4) {
+      for (int it = tid; it < 4 * N; it += kThreads) {
+        const int r = it / N, j = it - r * N, kr = kb - r;
+        R sd = 0;
+        for (int i = kr + 1; i < N; i++) sd = fma(Aw[i * la + kr], U[i * ld + j], sd);
+        cf[r * N + j] = sd;
+      }
+      __syncthreads();
+      for (int j = tid; j < N; j += kThreads) {
+        const R d0 = cf[j], d1 = cf[N + j], d2 = cf[2 * N + j], d3 = cf[3 * N + j];
+        const R c0 = beta[kb] * d0;
+        const R c1 = beta[kb - 1] * fma(-c0, pc[kb], d1);
+        const R c2 = beta[kb - 2] * fma(-c1, pc[kb - 1], fma(-c0, pc[N + kb], d2));
+        const R c3 = beta[kb - 3] *
+                     fma(-c2, pc[kb - 2], fma(-c1, pc[N + kb - 1], fma(-c0, pc[2 * N + kb], d3)));
+        cf[j] = c0;
+        cf[N + j] = c1;
+        cf[2 * N + j] = c2;
+        cf[3 * N + j] = c3;
+      }
+      __syncthreads();
+      // rows kb - 2 .. N - 1 (v_(kb-3) starts at row kb - 2; the others vanish there first)
+      const int r0 = kb - 2, L = N - r0;
+      for (int idx = tid; idx < L * N; idx += kThreads) {
+        const int i = r0 + idx / N, j = idx - (idx / N) * N;
+        const R v0 = (i > kb) ? Aw[i * la + kb] : R(0);
+        const R v1 = (i > kb - 1) ? Aw[i * la + kb - 1] : R(0);
+        const R v2 = (i > kb - 2) ? Aw[i * la + kb - 2] : R(0);
+        const R v3 = Aw[i * la + kb - 3];
+        R* u = U + i * ld + j;
+        *u = fma(-cf[3 * N + j], v3,
+                 fma(-cf[2 * N + j], v2, fma(-cf[N + j], v1, fma(-cf[j], v0, *u))));
+      }
+      __syncthreads();
+    }
+    for (int k = kb; k >= 0; k--) {  // the remaining reflectors one at a time
       const R bk = beta[k];
       if (bk == R(0)) continue;  // uniform across the block
       const int L = N - k - 1;
@@ -976,10 +1144,10 @@ cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z,
                       const int32_t* d_nobs, int rotate, R* d_ampl, int32_t* d_status,
                       int32_t* d_work, cudaStream_t st) {
   // two N x N matrices in shared memory when they fit (227 KB a block), else one (A in GT)
-  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
+  size_t smem3 = (size_t)(2 * N * (N + 1) + 16 * N) * sizeof(R) + (size_t)N * sizeof(int);
   int a_global = 0;
   if (smem3 > (size_t)227 * 1024) {
-    smem3 = (size_t)(N * (N + 1) + 9 * N) * sizeof(R) + (size_t)N * sizeof(int);
+    smem3 = (size_t)(N * (N + 1) + 16 * N) * sizeof(R) + (size_t)N * sizeof(int);
     a_global = 1;
   }
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<R>,
@@ -1021,7 +1189,7 @@ cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux
   if (N <= eig128_max_n())
     return eig128_transform(N, nzc, d_GT, d_aux, const_cast<float*>(d_Z), d_g, d_nobs, rotate,
                             d_ampl, d_status, st);
-  size_t smem3 = (size_t)(2 * N * (N + 1) + 9 * N) * sizeof(float) + (size_t)N * sizeof(int);
+  size_t smem3 = (size_t)(2 * N * (N + 1) + 16 * N) * sizeof(float) + (size_t)N * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
   if (e != cudaSuccess) return e;
@@ -1038,6 +1206,9 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
     k_eig_values_multisect<R><<<dim3((unsigned)N, (unsigned)nzc), 32, 0, st>>>(N, nzc, d_aux,
                                                                                d_nobs);
     k_eig_shifts<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs);
+  } else if (sizeof(R) == sizeof(double) && N <= kNV64) {
+    k_eig_values_fp64s<<<(nzc + kT64 - 1) / kT64, kT64, 0, st>>>(
+        N, nzc, reinterpret_cast<double*>(d_aux), d_nobs, d_status);
   } else {
     k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   }
@@ -1060,7 +1231,7 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
 template <>
 cudaError_t launch_e2<float>(int N, int32_t nzc, float* d_aux, float* d_Z, const int32_t* d_nobs,
                              int32_t* d_status, cudaStream_t st) {
-  if (N <= eig128_max_n()) {  // shared-memory E2a / E2b of zone_eig32.cu
+  if (N <= eig32_max_n()) {  // shared-memory E2a / E2b of zone_eig32.cu
     cudaError_t e = eig32_values(N, nzc, d_aux, d_nobs, d_status, st);
     if (e != cudaSuccess) return e;
     return eig32_vectors(N, nzc, d_aux, d_Z, d_nobs, st);

@@ -855,102 +855,8 @@ __global__ void __launch_bounds__(kT2)
   if (st) status[zl] |= st;
 }
 
-// E2a for 65..128 members: one block of NB2 threads per zone, thread j bisects eigenvalue j
-// (the j-th smallest) of Tri. count(x) = the number of negative pivots of the LDL^T of Tri - x I
-// (Sturm; the ratio form q_i = d_i - x - e_(i-1)^2 / q_(i-1), a pivot below pivmin in magnitude
-// taken as -pivmin, as LAPACK's bisection does) is the number of eigenvalues below x. Starting
-// from the Gershgorin interval, the step halves the interval until its width is below
-// 2 eps max(|lo|, |hi|) or eps ||Tri||_1 / 64 (at most kBisectSteps steps), so the eigenvalues
-// come sorted and as accurate as the QR sweeps' (whose deflation floor is eps ||Tri||_1). Every
-// thread is busy: the thread-per-zone QR sweeps leave most lanes idle at these sizes. Outputs
-// are those of k_eig_values32 (eigenvalues, inverse-iteration shifts, ||Tri||_1).
-constexpr int kBisectSteps = 40;
-
-__global__ void __launch_bounds__(128)
-    k_eig_values_bisect(int N, int32_t nzc, float* __restrict__ aux,
-                        const int32_t* __restrict__ nobs) {
-  __shared__ float sd[128], se2[128], sl[128];
-  __shared__ float red[3][4];
-  const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
-  const int32_t zl = blockIdx.x;
-  if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
-  const float eps = 5.9604645e-8f;
-  float* ax = aux + (int64_t)zl * aux_stride32(N);
-  const float dj = (j < N) ? ax[j] : 0.f;
-  const float ej = (j < N - 1) ? ax[N + j] : 0.f;
-  const float ejm = (j > 0 && j < N) ? ax[N + j - 1] : 0.f;
-  sd[j] = dj;
-  se2[j] = ej * ej;
-  // ||Tri||_1, the Gershgorin interval and max e^2 (block reductions)
-  const float rad = fabsf(ej) + fabsf(ejm);
-  float nrm = (j < N) ? fabsf(dj) + rad : 0.f;
-  float glo = (j < N) ? dj - rad : INFINITY;
-  float ghi = (j < N) ? dj + rad : -INFINITY;
-  for (int o = 16; o > 0; o >>= 1) {
-    nrm = fmaxf(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
-    glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
-    ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
-  }
-  if (lane == 0) {
-    red[0][warp] = nrm;
-    red[1][warp] = glo;
-    red[2][warp] = ghi;
-  }
-  __syncthreads();
-  const float onenrm = fmaxf(fmaxf(red[0][0], red[0][1]), fmaxf(red[0][2], red[0][3]));
-  float lo = fminf(fminf(red[1][0], red[1][1]), fminf(red[1][2], red[1][3]));
-  float hi = fmaxf(fmaxf(red[2][0], red[2][1]), fmaxf(red[2][2], red[2][3]));
-  const float pad = 2.f * eps * onenrm * (float)N + 1e-30f;
-  lo -= pad;
-  hi += pad;
-  float e2max = 0.f;
-  for (int i = 0; i < N - 1; i++) e2max = fmaxf(e2max, se2[i]);
-  const float pivmin = 1.17549435e-38f * fmaxf(1.f, e2max);
-  const float abs_w = eps * onenrm * (1.f / 64.f);
-  if (j < N) {
-#pragma unroll 1
-    for (int it = 0; it < kBisectSteps; it++) {
-      const float w = hi - lo;
-      if (!(w > fmaxf(abs_w, 2.f * eps * fmaxf(fabsf(lo), fabsf(hi))))) break;
-      const float x = 0.5f * (lo + hi);
-      float q = sd[0] - x;
-      if (fabsf(q) < pivmin) q = -pivmin;
-      int cnt = (q < 0.f);
-      for (int i = 1; i < N; i++) {
-        q = (sd[i] - x) - __fdividef(se2[i - 1], q);
-        if (fabsf(q) < pivmin) q = -pivmin;
-        cnt += (q < 0.f);
-      }
-      if (cnt > j)
-        hi = x;
-      else
-        lo = x;
-    }
-    sl[j] = 0.5f * (lo + hi);
-  }
-  __syncthreads();
-  const float scale = ax[5 * N];
-  if (j < N) ax[3 * N + j] = sl[j] * scale;
-  if (j == 0) {
-    // inverse-iteration shifts: separated by 10 eps |lambda| (as k_eig_values32)
-    float prev = 0.f;
-    for (int i = 0; i < N; i++) {
-      float sh = sl[i];
-      if (i > 0) {
-        const float pert = 10.f * eps * fabsf(sh);
-        if (sh - prev < pert) sh = prev + pert;
-      }
-      ax[4 * N + i] = sh;
-      prev = sh;
-    }
-    ax[5 * N + 1] = onenrm;
-  }
-}
-
 // ------------------------------------------------------------------------------------ E2b
-// One block of 64 threads per zone and 64 eigenpairs (a second block, blockIdx.y = 1, for
-// eigenpairs 64..127 of the 65..128-member ensembles), thread j = eigenpair j: inverse
-// iteration on Tri - shift_j I
+// One block of 64 threads per zone, thread j = eigenpair j: inverse iteration on Tri - shift_j I
 // (two solves from a fixed pseudo-random start, as the generic E2b). The partial-pivoting LU
 // is recomputed in each forward sweep (fused with the elimination), its upper factor kept in
 // shared memory: the first super-diagonal and the pivot reciprocals, while the second
@@ -1644,31 +1550,19 @@ int eig32_max_n() { return NB; }
 
 cudaError_t eig32_values(int N, int32_t nzc, float* d_aux, const int32_t* d_nobs,
                          int32_t* d_status, cudaStream_t st) {
-  if (N < 2 || N > NB2) return cudaErrorInvalidValue;
-  if (N <= NB)
-    k_eig_values32<<<(nzc + kT2 - 1) / kT2, kT2, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
-  else
-    k_eig_values_bisect<<<nzc > 0 ? nzc : 1, 128, 0, st>>>(N, nzc, d_aux, d_nobs);
+  if (N < 2 || N > NB) return cudaErrorInvalidValue;
+  k_eig_values32<<<(nzc + kT2 - 1) / kT2, kT2, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   return cudaGetLastError();
 }
 
 cudaError_t eig32_vectors(int N, int32_t nzc, const float* d_aux, float* d_Z,
                           const int32_t* d_nobs, cudaStream_t st) {
-  if (N < 2 || N > NB2) return cudaErrorInvalidValue;
-  const unsigned nz = nzc > 0 ? nzc : 1;
-  if (N <= NB) {
-    const size_t smem = (size_t)2 * NB * kT2 * sizeof(float);  // >= NB x (kT2 + 1): transpose
-    cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_eig_vectors32<NB><<<dim3(nz, 1), kT2, smem, st>>>(N, nzc, d_aux, d_Z, d_nobs);
-  } else {
-    const size_t smem = (size_t)2 * NB2 * kT2 * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB2>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_eig_vectors32<NB2><<<dim3(nz, 2), kT2, smem, st>>>(N, nzc, d_aux, d_Z, d_nobs);
-  }
+  if (N < 2 || N > NB) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)2 * NB * kT2 * sizeof(float);  // >= NB x (kT2 + 1): transpose
+  cudaError_t e = cudaFuncSetAttribute(k_eig_vectors32<NB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_eig_vectors32<NB><<<dim3(nzc > 0 ? nzc : 1, 1), kT2, smem, st>>>(N, nzc, d_aux, d_Z, d_nobs);
   return cudaGetLastError();
 }
 

@@ -76,7 +76,7 @@ constexpr size_t kDynSmem = 1024 + 2 * (size_t)kBufBytes + kSliceBytes +
 struct OzShared {
   int32_t ring_q[kRing];
   double ring_s[kRing];  // |w| / sqrt(r_q)
-  double ring_y[kRing];  // |w| / sqrt(r_q) (yo - Hxf)_q
+  double ring_t[kRing];  // w^2 / r_q (yo - Hxf)_q
   unsigned long long mbar[2];
   int32_t warp_cnt[kThreads / 32];
   int32_t E[NB];         // column exponents
@@ -160,26 +160,44 @@ __device__ __forceinline__ uint32_t tile_off(int row, int chunk) {
   return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
-// round(x 2^(54 - E)) from the FP64 bit pattern (|x| <= 2^E); *bad set for a non-finite x or
-// one above the bound
-__device__ __forceinline__ long long fixed54(double x, int E, int& bad) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  const int ex = (int)((bits >> 52) & 0x7FFu);
-  if (ex == 0) return 0;  // zero or subnormal (below 2^-1022: far under the column scale)
-  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-  const int sh = ex - 1021 - E;  // x 2^(54 - E) = mant 2^sh
-  long long F;
-  if (sh >= 0) {
-    if (sh > 1) {
-      bad = 1;
-      return 0;
-    }
-    F = (long long)(mant << sh);
-  } else {
-    const int r = -sh;
-    F = (r >= 62) ? 0 : (long long)((mant + (1ull << (r - 1))) >> r);
+// round(s h 2^(54 - E)) for s >= 0 (|s h| <= 2^E), from the FP64 bit patterns with integer
+// arithmetic: the product of the two 53-bit significands is exact in 128 bits and rounded once
+// (half away from zero) at the fixed-point position; no FP64 operation. *bad is set for a
+// non-finite factor or a product above the bound.
+__device__ __forceinline__ long long fixed_prod(double s, double h, int E, int& bad) {
+  const unsigned long long sb = (unsigned long long)__double_as_longlong(s);
+  const unsigned long long hb = (unsigned long long)__double_as_longlong(h);
+  const int es = (int)((sb >> 52) & 0x7FFu), eh = (int)((hb >> 52) & 0x7FFu);
+  if (es == 0x7FF || eh == 0x7FF) {
+    bad = 1;
+    return 0;
   }
-  return (bits >> 63) ? -F : F;
+  if (es == 0 || eh == 0) return 0;  // a zero or subnormal factor (far under the column scale)
+  const unsigned long long ms = (sb & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const unsigned long long mh = (hb & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  // s h 2^(54 - E) = ms mh 2^(es + eh - 2150 + 54 - E) = P 2^-r, P = ms mh < 2^106
+  const int r = 2096 + E - es - eh;
+  if (r >= 107) return 0;  // below half a unit of the fixed point
+  if (r < 50) {            // at least 2^54: above the bound
+    bad = 1;
+    return 0;
+  }
+  unsigned long long lo = ms * mh, hi = __umul64hi(ms, mh);
+  // P + 2^(r-1), then >> r
+  if (r - 1 < 64) {
+    const unsigned long long add = 1ull << (r - 1);
+    const unsigned long long lo2 = lo + add;
+    hi += (lo2 < lo) ? 1ull : 0ull;
+    lo = lo2;
+  } else {
+    hi += 1ull << (r - 1 - 64);
+  }
+  const unsigned long long F = (r < 64) ? ((hi << (64 - r)) | (lo >> r)) : (hi >> (r - 64));
+  if (F > (1ull << 54)) {
+    bad = 1;
+    return 0;
+  }
+  return (hb >> 63) ? -(long long)F : (long long)F;
 }
 
 // BF16 bits of the digit (byte - 128), exact: the FP32 value has at most 8 significant bits
@@ -194,8 +212,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_zone_gram_oz(CellGrid g, SortedObs so, int N, LocParams lp, int32_t z0, int32_t nzc,
                    const double* __restrict__ zone_xyzt, const double* __restrict__ corr_len,
                    const double* __restrict__ max_len, const int32_t* __restrict__ col_exp,
-                   double* __restrict__ G, double* __restrict__ gv, int32_t* __restrict__ nobs,
-                   int brute, int32_t* __restrict__ work, int32_t* __restrict__ err,
+                   const double* __restrict__ isr, double* __restrict__ G,
+                   double* __restrict__ gv, int32_t* __restrict__ nobs, int brute, int32_t* __restrict__ work, int32_t* __restrict__ err,
                    const int32_t* __restrict__ order) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   __shared__ __align__(16) OzShared ts;
@@ -355,9 +373,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (k < rows && a < N) {
               const int idx = (head + k) & (kRing - 1);
               const int32_t q = ts.ring_q[idx];
-              const double X = ts.ring_s[idx] * so.HSt[(int64_t)q * N + a];
-              gsum = fma(X, ts.ring_y[idx], gsum);
-              F = fixed54(X, Ea, bad);
+              const double h = so.HSt[(int64_t)q * N + a];
+              gsum = fma(h, ts.ring_t[idx], gsum);
+              F = fixed_prod(ts.ring_s[idx], h, Ea, bad);
             }
             const unsigned long long U = (unsigned long long)F + kDigitBias;
             lo2[u] = (uint32_t)U;
@@ -458,8 +476,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int32_t qb = q_lo; qb < q_hi && !abort; qb += kThreads) {
           const int32_t q = qb + tid;
           int sel = 0, rel = 0;
-          double w64 = 0.0;
-          bool have_w = false;
           if (q < q_hi) {
             // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
             bool done = false;
@@ -494,28 +510,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                 d = fabs(__dsub_rn(so.u[q], zu));
               if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
                 rel = (d <= Rmax);
-                const double t = d / L;
-                w64 = (rel || !lp.localise) ? exp(-(t * t)) : 0.0;
               } else {
-                w64 = sel::locfun(d / L);
-                rel = (d <= Rmax) && (w64 != 0.0);
+                rel = (d <= Rmax) && (sel::locfun(d / L) != 0.0);
               }
-              have_w = true;
             }
             sel = rel || !lp.localise;
-            if (sel && !have_w) {  // the plain form's FP64 weight (zone_gram.cu)
-              double d;
-              if (lp.loctype == 1)
-                d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
-              else
-                d = fabs(__dsub_rn(so.u[q], zu));
-              if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-                const double t = d / L;
-                w64 = exp(-(t * t));
-              } else {
-                w64 = sel::locfun(d / L);
-              }
-            }
           }
           nrel_local += rel;
           const unsigned ball = __ballot_sync(0xffffffffu, sel);
@@ -529,14 +528,32 @@ __global__ void __launch_bounds__(kThreads, 1)
             total += cnt;
           }
           if (sel) {
-            // c = w (w / r) (DCDCovar, covariance.F90:612-619); sqrt(c) = |w| / sqrt(r)
-            const double sc = fabs(w64) * rsqrt(so.r[q]);
             const int slot = (tail + before + __popc(ball & ((1u << lane) - 1u))) & (kRing - 1);
             ts.ring_q[slot] = q;
-            ts.ring_s[slot] = sc;
-            ts.ring_y[slot] = sc * so.innov[q];
           }
           __syncthreads();
+          // the plain form's FP64 weights of the new entries (zone_gram.cu), one thread an
+          // entry, so that the FP64 work runs with full warps: sqrt(c) = |w| / sqrt(r)
+          // (c = w (w / r), DCDCovar, covariance.F90:612-619) and c (yo - Hxf)
+          if (tid < total) {
+            const int slot = (tail + tid) & (kRing - 1);
+            const int32_t qs = ts.ring_q[slot];
+            double d;
+            if (lp.loctype == 1)
+              d = sel::distance(so.u[qs], so.v[qs], zu, zv, lp.metric);
+            else
+              d = fabs(__dsub_rn(so.u[qs], zu));
+            double w64;
+            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+              const double t = d / L;
+              w64 = exp(-(t * t));
+            } else {
+              w64 = sel::locfun(d / L);
+            }
+            const double sc = fabs(w64) * isr[qs];
+            ts.ring_s[slot] = sc;
+            ts.ring_t[slot] = sc * sc * so.innov[qs];
+          }
           tail += total;
           while (tail - head >= KT && !abort) do_tile(KT);
         }
@@ -597,14 +614,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                  "r"(kTmemCols));
 }
 
-// column exponents: E_a with max_q |HS_qa| r_q^-1/2 (1 + 2^-20) <= 2^E_a (|w| <= 1, so every
-// |X_qa| of every zone is below it). The maxima of non-negative FP64 values are taken on their
-// bit patterns (ordered like the values). Non-finite values and r <= 0 are left out: the zones
-// that select such an observation get a non-finite weight or element, which marks their G as
-// NaN (as the CUDA-core products would propagate it); the other zones keep the scale of the
-// finite data.
+// isr_q = r_q^-1/2 and the column exponents: E_a with max_q |HS_qa| isr_q (1 + 2^-20) <= 2^E_a
+// (|w| <= 1, so every |X_qa| of every zone is below it). The maxima of non-negative FP64
+// values are taken on their bit patterns (ordered like the values). Non-finite values and
+// r <= 0 are left out: the zones that select such an observation get a non-finite weight or
+// element, which marks their G as NaN (as the CUDA-core products would propagate it); the
+// other zones keep the scale of the finite data.
 __global__ void k_oz_colmax(int64_t m, int N, const double* __restrict__ HSt,
-                            const double* __restrict__ r, unsigned long long* __restrict__ mx) {
+                            const double* __restrict__ r, unsigned long long* __restrict__ mx,
+                            double* __restrict__ isr) {
   __shared__ unsigned long long smax[NB];
   if (threadIdx.x < NB) smax[threadIdx.x] = 0ull;
   __syncthreads();
@@ -614,8 +632,10 @@ __global__ void k_oz_colmax(int64_t m, int N, const double* __restrict__ HSt,
     for (int64_t q = blockIdx.x * (int64_t)(blockDim.x / NB) + threadIdx.x / NB; q < m;
          q += (int64_t)gridDim.x * (blockDim.x / NB)) {
       const double rq = r[q];
+      const double iq = rsqrt(rq);
+      if (a == 0) isr[q] = iq;
       if (!(rq > 0.0) || !(rq < INFINITY)) continue;
-      const double v = fabs(HSt[q * N + a]) * rsqrt(rq);
+      const double v = fabs(HSt[q * N + a]) * iq;
       const unsigned long long vb = (unsigned long long)__double_as_longlong(v);
       if (vb < 0x7FF0000000000000ull) loc = vb > loc ? vb : loc;
     }
@@ -650,7 +670,9 @@ __global__ void k_oz_exponents(int N, const unsigned long long* __restrict__ mx,
 
 int gram_oz_max_n() { return NB; }
 
-size_t gram_oz_scratch_bytes() { return NB * sizeof(unsigned long long) + NB * sizeof(int32_t); }
+size_t gram_oz_scratch_bytes(int64_t m) {
+  return NB * sizeof(unsigned long long) + NB * sizeof(int32_t) + (size_t)m * sizeof(double);
+}
 
 cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int N, LocParams lp,
                          int32_t z0, int32_t nzc, const double* zone_xyzt, const double* corr_len,
@@ -660,6 +682,7 @@ cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int 
   if (N < 1 || N > NB || !so.HSt || !so.r || !d_scratch) return cudaErrorInvalidValue;
   unsigned long long* mx = reinterpret_cast<unsigned long long*>(d_scratch);
   int32_t* E = reinterpret_cast<int32_t*>(mx + NB);
+  double* isr = reinterpret_cast<double*>(E + NB);  // 8-byte aligned: NB int32 = 256 bytes
   cudaError_t e = cudaMemsetAsync(mx, 0, NB * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
@@ -669,7 +692,7 @@ cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int 
     const int64_t per = kThreads / NB;
     int64_t blocks = (m + per - 1) / per;
     if (blocks > 4 * (int64_t)sms) blocks = 4 * (int64_t)sms;
-    k_oz_colmax<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, 0, st>>>(m, N, so.HSt, so.r, mx);
+    k_oz_colmax<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, 0, st>>>(m, N, so.HSt, so.r, mx, isr);
     count_launches(1);
   }
   k_oz_exponents<<<1, NB, 0, st>>>(N, mx, E);
@@ -686,8 +709,8 @@ cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int 
   e = cudaMemsetAsync(d_work, 0, sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
   k_zone_gram_oz<<<grid, kThreads, kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
-                                                   max_len, E, d_G, d_g, d_nobs, brute, d_work,
-                                                   d_err, order);
+                                                   max_len, E, isr, d_G, d_g, d_nobs, brute,
+                                                   d_work, d_err, order);
   count_launches(1);
   return cudaGetLastError();
 }
