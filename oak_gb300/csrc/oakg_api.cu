@@ -76,7 +76,7 @@ enum BufId {
   B_C_AMPL, B_C_ZERO, B_C_INC, B_C_UX, B_C_UHX, B_C_R2, B_C_BF, B_C_BA, B_SMWB, B_HSTA, B_GAUG,
   B_GVAUG, B_GLOB, B_L_PART, B_L_WORK, B_L_ZS, B_L_ZI, B_L_INV, B_L_X, B_L_Y, B_L_IDX, B_L_MASK,
   B_L_SEA, B_L_COORD, B_L_POS, B_L_OIDX, B_L_OW, B_L_SIMP, B_HXF64, B_YO64, B_R64, B_G0, B_SREF,
-  B_OZSCR, B_COUNT_
+  B_OZSCR, B_SCU, B_SRUV, B_COUNT_
 };
 
 struct Ctx {
@@ -570,9 +570,14 @@ int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH,
     if ((rc = scratch(c, B_SINNOV, (size_t)m, &d_sinnov, "obs"))) return rc;
     if ((rc = scratch(c, B_SR, (size_t)m, &d_sr, "obs"))) return rc;
     if ((rc = scratch(c, B_HST, (size_t)m * N, &d_hst, "obs rows"))) return rc;
+    int32_t* d_scu;
+    float* d_sruv;
+    if ((rc = scratch(c, B_SCU, (size_t)m, &d_scu, "obs cells")) ||
+        (rc = scratch(c, B_SRUV, (size_t)2 * m, &d_sruv, "obs cell offsets")))
+      return rc;
     e = obs_bin_and_sort(g, m, N, P->u, P->v, P->yo, P->Hxf, P->r, P->HSf, P->HSf32, ldH,
-                         d_cell, d_count,
-                         d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr, d_hst, st);
+                         d_cell, d_count, d_cstart, d_pos, d_perm, d_su, d_sv, d_sinnov, d_sr,
+                         d_hst, d_scu, d_sruv, d_sruv + m, st);
     if (e != cudaSuccess) return cuda_fail(e, "observation binning");
     so.u = d_su;
     so.v = d_sv;
@@ -582,6 +587,9 @@ int bin_observations(Ctx* c, const oakg_loc* loc, int64_t m, int N, int64_t ldH,
     so.cell_start = d_cstart;
     so.perm = d_perm;
     so.m = m;
+    so.cu = d_scu;
+    so.ru = d_sruv;
+    so.rv = d_sruv + m;
     if (loc->precision != OAKG_PREC_FP64) {
       float* d_hst32;
       if ((rc = scratch(c, B_HST32, (size_t)m * N, &d_hst32, "obs rows (FP32)"))) return rc;

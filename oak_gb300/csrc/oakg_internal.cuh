@@ -38,6 +38,11 @@ struct SortedObs {
   const int32_t* cell_start;  // [ncells + 1]
   const int32_t* perm;  // sorted position -> original index                [m]
   int64_t m;            // number of observations
+  // cell-relative coordinates: u cell index of the observation (its v cell is the row its cell
+  // lies in) and the FP32 offsets u - (u0 + cu csu), v - (v0 + cv csv) inside the cell  [m]
+  const int32_t* cu;
+  const float* ru;
+  const float* rv;
 };
 
 struct LocParams {
@@ -55,7 +60,8 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
                              int64_t ldH, int32_t* d_cell, int32_t* d_count,
                              int32_t* d_cell_start, int32_t* d_pos, int32_t* d_perm,
                              double* d_u, double* d_v, double* d_innov, double* d_r,
-                             double* d_HSt, cudaStream_t st);
+                             double* d_HSt, int32_t* d_cu, float* d_ru, float* d_rv,
+                             cudaStream_t st);
 cudaError_t zone_offsets(const int32_t* zone_size, int32_t Z, int64_t* d_zone_start,
                          int32_t* d_zone_max, cudaStream_t st);
 

@@ -209,21 +209,31 @@ __global__ void k_cell_sort_large(int32_t ncells, const int32_t* __restrict__ ce
   }
 }
 
-__global__ void k_gather_scalars(int64_t m, const int32_t* __restrict__ perm,
+__global__ void k_gather_scalars(CellGrid g, int64_t m, const int32_t* __restrict__ perm,
                                  const double* __restrict__ u_src,
                                  const double* __restrict__ v_src,
                                  const double* __restrict__ yo, const double* __restrict__ Hxf,
                                  const double* __restrict__ r, int32_t* __restrict__ pos,
                                  double* __restrict__ u, double* __restrict__ v,
-                                 double* __restrict__ innov, double* __restrict__ rs) {
+                                 double* __restrict__ innov, double* __restrict__ rs,
+                                 int32_t* __restrict__ cu, float* __restrict__ ru,
+                                 float* __restrict__ rv) {
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < m;
        q += (int64_t)gridDim.x * blockDim.x) {
     int32_t j = perm[q];
     pos[j] = (int32_t)q;
-    u[q] = u_src[j];
-    v[q] = v_src ? v_src[j] : 0.0;
+    const double uj = u_src[j], vj = v_src ? v_src[j] : 0.0;
+    u[q] = uj;
+    v[q] = vj;
     innov[q] = yo[j] - Hxf[j];
     rs[q] = r[j];
+    // the cell the observation was binned into and its offsets inside it
+    const int32_t c = cell_of(g, uj, vj);
+    const int32_t ci = c % g.nu, cj = c / g.nu;
+    const double uw = g.periodic_u ? uj - 360.0 * floor(uj / 360.0) : uj;  // as cell_of
+    cu[q] = ci;
+    ru[q] = (float)(uw - (g.u0 + ci * g.csu));
+    rv[q] = (float)(vj - (g.v0 + cj * g.csv));
   }
 }
 
@@ -271,7 +281,8 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
                              int64_t ldH, int32_t* d_cell, int32_t* d_count,
                              int32_t* d_cell_start, int32_t* d_pos, int32_t* d_perm,
                              double* d_u, double* d_v, double* d_innov, double* d_r,
-                             double* d_HSt, cudaStream_t st) {
+                             double* d_HSt, int32_t* d_cu, float* d_ru, float* d_rv,
+                             cudaStream_t st) {
   const int64_t ncells = (int64_t)g.nu * g.nv;
   cudaError_t e = cudaMemsetAsync(d_count, 0, (ncells + 1) * sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
@@ -289,8 +300,9 @@ cudaError_t obs_bin_and_sort(const CellGrid& g, int64_t m, int N, const double* 
         (int32_t)ncells, d_cell_start, d_perm, d_count + ncells);
     k_cell_sort_large<<<grid_for(ncells, 128), 128, 0, st>>>((int32_t)ncells, d_cell_start,
                                                              d_perm);
-    k_gather_scalars<<<grid_for(m, 256), 256, 0, st>>>(m, d_perm, u_src, v_src, yo, Hxf, r,
-                                                       d_pos, d_u, d_v, d_innov, d_r);
+    k_gather_scalars<<<grid_for(m, 256), 256, 0, st>>>(g, m, d_perm, u_src, v_src, yo, Hxf, r,
+                                                       d_pos, d_u, d_v, d_innov, d_r, d_cu,
+                                                       d_ru, d_rv);
     dim3 tb(32, 8), tg((unsigned)((m + 31) / 32), (unsigned)((N + 31) / 32));
     if (HSf32)
       k_transpose_rows<float><<<tg, tb, 0, st>>>(m, N, HSf32, ldH, d_pos, d_HSt);

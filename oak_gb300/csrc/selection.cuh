@@ -59,6 +59,46 @@ static __device__ __forceinline__ double distance(double x0, double y0, double x
   }
 }
 
+// Cell-relative FP32 coordinates of a zone for the Cartesian and 1-D distances: its cell indices
+// along u and v (not clamped) and its FP32 offsets inside that cell. The distance to an
+// observation of cell indices (cq, cvq) and offsets (rq, rvq) is then, per axis,
+// (cq - cu) csu + (rq - ru) in FP32: every term is below maxLength + 2 csu in magnitude, so
+// with cell edges of at most 2 maxLength its relative error at d = maxLength stays below
+// 1e-6 (about 12 roundings of 2^-24), whatever the magnitude of the coordinates, and no FP64
+// operation is spent on a candidate. ok is false for periodic grids and wider cells.
+struct ZoneCell32 {
+  int cu, cv;
+  float ru, rv, csu, csv;
+  bool ok;
+};
+
+static __device__ __forceinline__ ZoneCell32 zone_cell32(const CellGrid& g, double zu, double zv,
+                                                         double Rmax) {
+  ZoneCell32 z;
+  const double fu = floor((zu - g.u0) / g.csu), fv = floor((zv - g.v0) / g.csv);
+  z.ok = !g.periodic_u && g.csu <= 2.0 * Rmax && g.csv <= 2.0 * Rmax && fabs(fu) < 1e8 &&
+         fabs(fv) < 1e8;
+  z.cu = z.ok ? (int)fu : 0;
+  z.cv = z.ok ? (int)fv : 0;
+  z.ru = (float)(zu - (g.u0 + z.cu * g.csu));
+  z.rv = (float)(zv - (g.v0 + z.cv * g.csv));
+  z.csu = (float)g.csu;
+  z.csv = (float)g.csv;
+  return z;
+}
+
+// FP32 distance between the zone and observation q of cell row cv (see ZoneCell32)
+static __device__ __forceinline__ float cell_distance32(const ZoneCell32& z, const SortedObs& so,
+                                                        int32_t q, int cv, bool two_d) {
+  const float du = fmaf((float)(so.cu[q] - z.cu), z.csu, so.ru[q] - z.ru);
+  float D2 = du * du;
+  if (two_d) {
+    const float dv = fmaf((float)(cv - z.cv), z.csv, so.rv[q] - z.rv);
+    D2 = fmaf(dv, dv, D2);
+  }
+  return sqrtf(D2);
+}
+
 // Cell-index ranges a zone has to visit. Rows are v cells [cv0, cv1]; in each row the u cells
 // [cu0, cu1] (unclamped for a periodic axis; iterate modulo nu). all_u: visit every u cell.
 struct ScanRange {

@@ -316,118 +316,6 @@ __global__ void __launch_bounds__(128)
   if (st) status[zl] |= st;
 }
 
-// strided per-thread view of a shared array: element i at [i * kT64]
-template <typename R>
-struct SArr {
-  R* p;
-  __device__ __forceinline__ R& operator[](int i) const { return p[i * kT64]; }
-};
-
-// The same for N <= kNV64 in FP64 with d and e in shared memory (element i of thread t at
-// [i * kT64 + t]) instead of per-thread local arrays, which the L1 cannot hold for a full SM
-// of threads: identical arithmetic in the same order, so the same eigenvalues bit for bit.
-__global__ void __launch_bounds__(kT64)
-    k_eig_values_fp64s(int N, int32_t nzc, double* __restrict__ aux,
-                       const int32_t* __restrict__ nobs, int32_t* __restrict__ status) {
-  using R = double;
-  __shared__ R sd[kNV64 * kT64], se[kNV64 * kT64];
-  const int32_t zl = blockIdx.x * blockDim.x + threadIdx.x;
-  if (zl >= nzc || nobs[zl] == 0) return;  // no barrier below
-  const R eps = Prec<R>::eps();
-  R* ax = aux + (int64_t)zl * aux_stride(N);
-  SArr<R> d{sd + threadIdx.x}, e{se + threadIdx.x};
-  R onenrm = 0;
-  for (int i = 0; i < N; i++) {
-    d[i] = ax[i];
-    e[i] = (i < N - 1) ? ax[N + i] : R(0);
-  }
-  for (int i = 0; i < N; i++) {
-    R s = fabs(d[i]) + fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : R(0));
-    onenrm = fmax(onenrm, s);
-  }
-  const R scale = ax[5 * N];
-  int st = 0;
-  int hi = N - 1, sweeps = 0;
-  const int max_sweeps = kMaxSweepsPerN * N;
-  const R abs_tol = eps * onenrm;  // deflation floor: the rounding level of Tri
-  while (hi > 0) {
-    while (hi > 0) {
-      R t = fabs(e[hi - 1]);
-      if (t <= eps * (fabs(d[hi - 1]) + fabs(d[hi])) || t <= abs_tol) {
-        e[hi - 1] = 0;
-        hi--;
-      } else {
-        break;
-      }
-    }
-    if (hi == 0) break;
-    int lo = hi - 1;
-    while (lo > 0) {
-      R t = fabs(e[lo - 1]);
-      if (t <= eps * (fabs(d[lo - 1]) + fabs(d[lo])) || t <= abs_tol) {
-        e[lo - 1] = 0;
-        break;
-      }
-      lo--;
-    }
-    if (++sweeps > max_sweeps) {
-      st |= ZST_EIG;
-      break;
-    }
-    const R a = d[hi - 1], b = d[hi], f = e[hi - 1];
-    const R del = R(0.5) * (a - b);
-    const R den = del + copysign(Prec<R>::sqrt_(del * del + f * f), del == R(0) ? R(1) : del);
-    const R mu = (den == R(0)) ? b : b - f * f / den;
-    R x = d[lo] - mu, z = e[lo], bulge = 0;
-    for (int k = lo; k < hi; k++) {
-      if (k > lo) {
-        x = e[k - 1];
-        z = bulge;
-      }
-      const R r2 = x * x + z * z;
-      R c = 1, s = 0, r = 0;
-      if (r2 > R(0)) {
-        const R ri = Prec<R>::rsqrt_(r2);
-        c = x * ri;
-        s = z * ri;
-        r = r2 * ri;
-      }
-      if (k > lo) e[k - 1] = r;
-      const R dk = d[k], dk1 = d[k + 1], ek = e[k];
-      const R ek1 = (k + 1 < hi) ? e[k + 1] : R(0);
-      const R cc = c * c, ss = s * s, cs = c * s;
-      d[k] = cc * dk + R(2) * cs * ek + ss * dk1;
-      d[k + 1] = ss * dk - R(2) * cs * ek + cc * dk1;
-      e[k] = cs * (dk1 - dk) + (cc - ss) * ek;
-      if (k + 1 < hi) e[k + 1] = c * ek1;
-      bulge = s * ek1;
-    }
-  }
-  // ascending order (insertion sort)
-  for (int i = 1; i < N; i++) {
-    R t = d[i];
-    int k = i - 1;
-    while (k >= 0 && d[k] > t) {
-      d[k + 1] = d[k];
-      k--;
-    }
-    d[k + 1] = t;
-  }
-  R prev = 0;
-  for (int j = 0; j < N; j++) {
-    ax[3 * N + j] = d[j] * scale;
-    R s = d[j];
-    if (j > 0) {
-      const R pert = R(10) * eps * fabs(s);
-      if (s - prev < pert) s = prev + pert;
-    }
-    ax[4 * N + j] = s;
-    prev = s;
-  }
-  ax[5 * N + 1] = onenrm;
-  if (st) status[zl] |= st;
-}
-
 // E2a for few zones (fewer than the GPU has SMs, e.g. the one-zone global analysis), where the
 // thread-per-zone QR above leaves the GPU idle and its latency is the whole stage: one warp per
 // eigenvalue (grid N x zones), so that the zone's eigenvalues spread over the SMs. Eigenvalue
@@ -1206,9 +1094,6 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
     k_eig_values_multisect<R><<<dim3((unsigned)N, (unsigned)nzc), 32, 0, st>>>(N, nzc, d_aux,
                                                                                d_nobs);
     k_eig_shifts<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs);
-  } else if (sizeof(R) == sizeof(double) && N <= kNV64) {
-    k_eig_values_fp64s<<<(nzc + kT64 - 1) / kT64, kT64, 0, st>>>(
-        N, nzc, reinterpret_cast<double*>(d_aux), d_nobs, d_status);
   } else {
     k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   }

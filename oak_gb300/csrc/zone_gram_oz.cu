@@ -36,9 +36,10 @@
 // The innovation projection g = X^T (sqrt(c) d) (rrsqrt.F90:142) is accumulated in FP64 by the
 // staging threads (one FMA per staged element).
 //
-// Pipeline per CTA (one zone at a time, one CTA per SM: its shared memory and the 512
-// tensor-memory columns admit no second one): candidates are tested 256 at a time; selected
-// observations go to a ring of (index, |w| / sqrt(r), |w| / sqrt(r) d); every full K-tile is
+// Pipeline per CTA (one zone at a time, one CTA of 512 threads per SM: its shared memory and
+// the 512 tensor-memory columns admit no second one): candidates are tested 512 at a time;
+// selected observations go to a ring, their FP64 weights are computed one thread an entry
+// (|w| / sqrt(r) and w^2 / r (yo - Hxf)); every full K-tile is
 // staged into one of two shared buffers (7 slices) and handed to the tensor core by one thread
 // (44 MMAs and a commit to the buffer's mbarrier), so staging of the next tile overlaps the
 // MMAs. Every mbarrier wait is bounded; on expiry the kernel records ZST_TIMEOUT, stops taking
@@ -53,11 +54,11 @@ namespace oakg {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int NB = 64;                 // padded ensemble width
 constexpr int KT = 64;                 // observations per K-tile (128 bytes of BF16 a row)
 constexpr int kDigits = 7;
-constexpr int kRing = 512;             // selected-observation ring (power of two)
+constexpr int kRing = 1024;            // selected-observation ring (power of two)
 constexpr uint32_t kSliceBytes = 64u * 128u;         // one digit slice of a K-tile
 constexpr uint32_t kBufBytes = kDigits * kSliceBytes;  // one K-tile buffer
 constexpr uint32_t kTmemCols = 512;
@@ -65,13 +66,14 @@ constexpr int kWaitPolls = 1 << 22;
 constexpr int kFlushTiles = 4;         // K-tiles between accumulator reads (256 observations)
 constexpr int kTri = NB * (NB + 1) / 2;
 constexpr int kLevelsExact = 4;        // levels held as 64-bit integer sums
+constexpr int kStageGroups = kThreads / NB;  // threads a member in the staging (8-obs chunks)
 constexpr unsigned long long kDigitBias = 0x80808080808080ull;
 // dynamic shared memory: alignment slack, two K-tile buffers, the slice past the second buffer
 // (rows 64-127 of the A operand of the last digit: read by the MMA, never read back), the
 // integer and FP32 level sums (lower triangle) and the FP64 innovation partials
 constexpr size_t kDynSmem = 1024 + 2 * (size_t)kBufBytes + kSliceBytes +
                             (size_t)kLevelsExact * kTri * sizeof(long long) +
-                            (size_t)kTri * sizeof(float) + 4 * NB * sizeof(double);
+                            (size_t)kTri * sizeof(float) + kStageGroups * NB * sizeof(double);
 
 struct OzShared {
   int32_t ring_q[kRing];
@@ -223,10 +225,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tile_addr = raw_addr + pad;
   long long* acc64 = reinterpret_cast<long long*>(tiles + 2 * kBufBytes + kSliceBytes);
   float* accf = reinterpret_cast<float*>(acc64 + kLevelsExact * kTri);
-  double* gpart = reinterpret_cast<double*>(accf + kTri);  // [4][NB]
+  double* gpart = reinterpret_cast<double*>(accf + kTri);  // [kStageGroups][NB]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // staging: member a, 8-observation chunks kq and kq + 4 of a K-tile
+  // staging: member a, 8-observation chunk kq of a K-tile
   const int a = tid & (NB - 1), kq = tid >> 6;
   const uint32_t mbar0 = smem_u32(&ts.mbar[0]);
 
@@ -277,18 +279,19 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   // add the accumulators into the level sums (all MMAs complete and published by a barrier).
   // Warp w reads lanes 32 (w % 4) .. + 31, i.e. rows j of the lower (D_p) half for w % 4 < 2;
-  // warps 0-3 take levels 0..3, warps 4-7 levels 4..6; row j keeps columns c <= j.
+  // warp group h = w / 4 takes levels 2h, 2h + 1 (h < 2) or 4..6 (h = 2); row j keeps columns
+  // c <= j.
   auto flush = [&]() {
     fence_after();
     const int q = warp & 3, h = warp >> 2;
-    if (q < 2) {
+    if (q < 2 && h < 3) {
       const int j = 32 * q + lane;
       const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16);
       const int ncol = 32 * (q + 1);  // warp-uniform bound of the row's lower triangle
       const int tj = tri(j);
-      if (h == 0) {
+      if (h < 2) {
 #pragma unroll
-        for (int L = 0; L < kLevelsExact; L++) {
+        for (int L = 2 * h; L < 2 * h + 2; L++) {
           long long* accL = acc64 + L * kTri + tj;
           for (int c0 = 0; c0 < ncol; c0 += 8) {
             float v[8];
@@ -328,7 +331,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double zv = (lp.loctype == 1) ? zy : 0.0;
     const double L = corr_len[z], Rmax = max_len[z];
     const float iL32 = (float)(1.0 / L);
-    const float r_lo = (float)Rmax * (1.f - 1e-6f), r_hi = (float)Rmax * (1.f + 1e-6f);
+    // the FP32 distance (relative error < 1e-6, sel::ZoneCell32) decides outside a 3e-6 band
+    const float r_lo = (float)Rmax * (1.f - 3e-6f), r_hi = (float)Rmax * (1.f + 3e-6f);
+    const sel::ZoneCell32 zc = sel::zone_cell32(g, zu, zv, Rmax);
+    const bool fastz = fast && zc.ok && !brute;  // brute force: one cell, no local offsets
     if (tid == 0) {
       ts.nrel = 0;
       ts.bad = 0;
@@ -360,8 +366,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       unsigned char* tb = tiles + b * kBufBytes;
 #pragma unroll 1
-      for (int pass = 0; pass < 2; pass++) {
-        const int chunk = kq + 4 * pass;
+      for (int pass = 0; pass < KT / 8 / kStageGroups; pass++) {
+        const int chunk = kq + kStageGroups * pass;
         uint32_t pk[kDigits][4];
 #pragma unroll
         for (int i = 0; i < 8; i += 2) {
@@ -479,14 +485,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (q < q_hi) {
             // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
             bool done = false;
-            if (fast) {
-              const double du = so.u[q] - zu;
-              double D2 = du * du;
-              if (lp.loctype == 1) {
-                const double dv = so.v[q] - zv;
-                D2 = fma(dv, dv, D2);
-              }
-              const float d32 = sqrtf((float)D2);  // relative error < 2e-7
+            if (fastz) {
+              const float d32 = sel::cell_distance32(zc, so, q, cv, lp.loctype == 1);
               const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
               if (inside >= 0) {
                 const float r32 = d32 * iL32;
@@ -596,9 +596,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         Gz[j * N + c] = val;
         Gz[c * N + j] = val;
       }
-      if (tid < N)
-        gv[(int64_t)zl * N + tid] =
-            ((gpart[tid] + gpart[NB + tid]) + gpart[2 * NB + tid]) + gpart[3 * NB + tid];
+      if (tid < N) {
+        double gs = 0.0;
+#pragma unroll
+        for (int p = 0; p < kStageGroups; p++) gs += gpart[p * NB + tid];
+        gv[(int64_t)zl * N + tid] = gs;
+      }
     }
     __syncthreads();  // G staging and partials consumed before the next zone's tiles
   }

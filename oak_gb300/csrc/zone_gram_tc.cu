@@ -2,8 +2,9 @@
 //
 // Selection makes the decisions of zone_gram.cu (assimilation.F90:3683-3771): d <= maxLength
 // and, for Gaspari-Cohn, locfun(d/L) /= 0. For Cartesian and 1-D distances they are taken from
-// an FP32 distance (relative error < 2e-7, from an FP64 squared distance) when it is farther
-// than a relative 1e-6 from maxLength and r = d/L is below 2 - 1e-3 or above 2 + 1e-5; inside
+// an FP32 distance (relative error < 1e-6, from cell-relative FP32 coordinates: no FP64
+// operation a candidate) when it is farther than a relative 3e-6 from maxLength and r = d/L is
+// below 2 - 1e-3 or above 2 + 1e-5; inside
 // those margins the reference's FP64 distance and locfun with IEEE rounding decide, as they do
 // for the spherical metrics. The selected set is therefore identical to the plain form's. The
 // weights themselves are FP32 (locfun or exp of the FP32 ratio). The Gram matrix
@@ -92,6 +93,7 @@ struct TcShared {
   int32_t zone;
   int32_t nrel;
   int32_t flag;
+  sel::ZoneCell32 zc;  // the zone's cell-relative FP32 coordinates (read by broadcast)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -313,8 +315,14 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
     const double zv = (lp.loctype == 1) ? zy : 0.0;
     const double L = corr_len[z], Rmax = max_len[z];
     const float iL32 = (float)(1.0 / L);
-    const float r_lo = (float)Rmax * (1.f - 1e-6f), r_hi = (float)Rmax * (1.f + 1e-6f);
-    if (tid == 0) ts.nrel = 0;
+    // the FP32 distance (relative error < 1e-6, sel::ZoneCell32) decides outside a 3e-6 band
+    const float r_lo = (float)Rmax * (1.f - 3e-6f), r_hi = (float)Rmax * (1.f + 3e-6f);
+    if (tid == 0) {
+      ts.nrel = 0;
+      ts.zc = sel::zone_cell32(g, zu, zv, Rmax);
+    }
+    __syncthreads();  // ts.zc published (no thread reads it before this zone's scan)
+    const bool fastz = fast && ts.zc.ok && !brute;  // brute force: one cell, no local offsets
     for (int e = tid; e < C::kTri; e += kThreads) gacc[e] = 0.f;
     int head = 0, tail = 0, ntile = 0, ctile = 0, nrel_local = 0;
     float gsum = 0.f, gcmp = 0.f;
@@ -442,14 +450,8 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
           if (q < q_hi) {
             // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
             bool done = false;
-            if (fast) {
-              const double du = so.u[q] - zu;
-              double D2 = du * du;
-              if (lp.loctype == 1) {
-                const double dv = so.v[q] - zv;
-                D2 = fma(dv, dv, D2);
-              }
-              const float d32 = sqrtf((float)D2);  // relative error < 2e-7
+            if (fastz) {
+              const float d32 = sel::cell_distance32(ts.zc, so, q, cv, lp.loctype == 1);
               const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
               if (inside >= 0) {
                 const float r32 = d32 * iL32;
