@@ -577,7 +577,7 @@ def main():
         return
     per_step = {k: v / args.steps for k, v in stage_ms.items()}
     dom = max(("gram", "eig", "update"), key=lambda k: per_step[k])
-    kernel = {"gram": "k_zone_gram_fp64", "eig": "k_zone_eig_fp64",
+    kernel = {"gram": "k_zone_gram_oz", "eig": "k_zone_eig_fp64",
               "update": "k_zone_update_fp64"}[dom]
     work = algorithmic_work(c, nobs, dom)
     achieved = work / (per_step[dom] / 1e3) / 1e12

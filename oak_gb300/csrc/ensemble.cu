@@ -149,10 +149,8 @@ __global__ void __launch_bounds__(kThreads)
 // sqrt2ens with Theta = I: Om = sqrt(N-1) perpSpace(w) has rows sqrt(N-1) (e_i + a w^2 1) for
 // i < N-1 and sqrt(N-1) a (w + 1) w 1 for the last (a = -1 / (w + 1), w = 1/sqrt(N)), so
 //   E(:, i) = mean + sqrt(N-1) (S(:, i) + a w^2 rs),  E(:, N-1) = mean + sqrt(N-1) a (w+1) w rs,
-// rs the row sums of S: one read of S and one write of E, with no N x N-1 product. Rows with
-// K <= 64 anomaly columns keep them in registers; longer rows read S twice.
-constexpr int kRegMembers = 64;
-template <bool kReg>
+// rs the row sums of S: no N x N-1 product. A thread takes a row in two passes over S (the
+// second from L2) with few registers, and one FMA an element: the FP64 pipe bounds the loop.
 __global__ void __launch_bounds__(kThreads)
     k_sqrt2ens_identity(int64_t rows, int N, const double* __restrict__ mean,
                         const double* __restrict__ S, int64_t ldS, double* __restrict__ E,
@@ -163,27 +161,13 @@ __global__ void __launch_bounds__(kThreads)
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double mu = mean[i];
-    if (kReg) {
-      double v[kRegMembers];
-#pragma unroll
-      for (int k = 0; k < kRegMembers; k++) v[k] = (k < K) ? S[i + (int64_t)k * ldS] : 0.0;
-      double rs = 0.0;
-#pragma unroll
-      for (int k = 0; k < kRegMembers; k++)
-        if (k < K) rs += v[k];
-      // mean + sqrt(N-1) (S + a w^2 rs) as one FMA an element (the FP64 pipe bounds the loop)
-      const double base = fma(sc * cw, rs, mu);
-#pragma unroll
-      for (int k = 0; k < kRegMembers; k++)
-        if (k < K) E[i + (int64_t)k * ldE] = fma(sc, v[k], base);
-      E[i + (int64_t)K * ldE] = fma(cl, rs, mu);
-    } else {
-      double rs = 0.0;
-      for (int k = 0; k < K; k++) rs += S[i + (int64_t)k * ldS];
-      const double base = fma(sc * cw, rs, mu);
-      for (int k = 0; k < K; k++) E[i + (int64_t)k * ldE] = fma(sc, S[i + (int64_t)k * ldS], base);
-      E[i + (int64_t)K * ldE] = fma(cl, rs, mu);
-    }
+    double rs = 0.0;
+#pragma unroll 8
+    for (int k = 0; k < K; k++) rs += S[i + (int64_t)k * ldS];
+    const double base = fma(sc * cw, rs, mu);
+#pragma unroll 8
+    for (int k = 0; k < K; k++) E[i + (int64_t)k * ldE] = fma(sc, S[i + (int64_t)k * ldS], base);
+    E[i + (int64_t)K * ldE] = fma(cl, rs, mu);
   }
 }
 
@@ -242,10 +226,7 @@ cudaError_t ensemble_sqrt2ens(int64_t n, int N, const double* mean, const double
 
 cudaError_t ensemble_sqrt2ens_identity(int64_t n, int N, const double* mean, const double* S,
                                        int64_t ldS, double* E, int64_t ldE, cudaStream_t st) {
-  if (N - 1 <= kRegMembers)
-    k_sqrt2ens_identity<true><<<grid_for(n), kThreads, 0, st>>>(n, N, mean, S, ldS, E, ldE);
-  else
-    k_sqrt2ens_identity<false><<<grid_for(n), kThreads, 0, st>>>(n, N, mean, S, ldS, E, ldE);
+  k_sqrt2ens_identity<<<grid_for(n), kThreads, 0, st>>>(n, N, mean, S, ldS, E, ldE);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -35,6 +35,21 @@ static __device__ __forceinline__ double locfun(double r) {
   return 0.0;
 }
 
+// locfun's value with FMA and reciprocal constants (one division): for weight values, where an
+// ulp or two of difference from the reference's rounding does not matter; relevance decisions
+// use locfun above
+static __device__ __forceinline__ double locfun_value(double r) {
+  if (r <= 1.0) {
+    const double t = fma(fma(fma(-0.25, r, 0.5), r, 0.625), r, -5.0 / 3.0);
+    return fma(t, r * r, 1.0);
+  }
+  if (r <= 2.0) {
+    const double t = fma(fma(fma(fma(r, 1.0 / 12.0, -0.5), r, 0.625), r, 5.0 / 3.0), r, -5.0);
+    return fma(t, r, 4.0) - (2.0 / 3.0) / r;
+  }
+  return 0.0;
+}
+
 // distance(p0 = observation, p1 = zone) (assimilation.F90:3635-3672). Products and sums are
 // rounded one by one (no FMA contraction), so the Cartesian value is the correctly rounded
 // result of the reference expression and the d <= maxLength test matches a CPU evaluation.

@@ -87,6 +87,9 @@ struct OzShared {
   int32_t nrel;
   int32_t flag;
   int32_t bad;
+  sel::ZoneCell32 zc;  // the zone's cell-relative FP32 coordinates (read by broadcast)
+  sel::ScanRange sr;   // the zone's cell range
+  double iL;           // 1 / L
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -330,19 +333,33 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
     const double zv = (lp.loctype == 1) ? zy : 0.0;
     const double L = corr_len[z], Rmax = max_len[z];
-    const float iL32 = (float)(1.0 / L);
     // the FP32 distance (relative error < 1e-6, sel::ZoneCell32) decides outside a 3e-6 band
     const float r_lo = (float)Rmax * (1.f - 3e-6f), r_hi = (float)Rmax * (1.f + 3e-6f);
-    const sel::ZoneCell32 zc = sel::zone_cell32(g, zu, zv, Rmax);
-    const bool fastz = fast && zc.ok && !brute;  // brute force: one cell, no local offsets
+    // the zone's FP64 set-up (divisions, floors) once, by one thread
     if (tid == 0) {
       ts.nrel = 0;
       ts.bad = 0;
+      ts.zc = sel::zone_cell32(g, zu, zv, Rmax);
+      ts.iL = 1.0 / L;
+      if (full_scan) {
+        ts.sr.cu0 = 0;
+        ts.sr.cu1 = g.nu - 1;
+        ts.sr.cv0 = 0;
+        ts.sr.cv1 = g.nv - 1;
+        ts.sr.all_u = 1;
+      } else {
+        ts.sr = sel::zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
+      }
     }
+    __syncthreads();  // ts.zc, ts.sr, ts.iL published (read only in this zone's scan)
+    const sel::ZoneCell32 zc = ts.zc;
+    const bool fastz = fast && zc.ok && !brute;  // brute force: one cell, no local offsets
+    const double iL = ts.iL, iL2 = iL * iL;
+    const float iL32 = (float)iL;
     for (int e = tid; e < kLevelsExact * kTri; e += kThreads) acc64[e] = 0;
     for (int e = tid; e < kTri; e += kThreads) accf[e] = 0.f;
     int head = 0, tail = 0, ntile = 0, ctile = 0, nrel_local = 0, bad = 0;
-    double gsum = 0.0;
+    double gsum = 0.0, gsum1 = 0.0;
 
     // stage ring entries [head, head + rows) as one K-tile and issue its MMAs
     auto do_tile = [&](int rows) {
@@ -369,20 +386,30 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int pass = 0; pass < KT / 8 / kStageGroups; pass++) {
         const int chunk = kq + kStageGroups * pass;
         uint32_t pk[kDigits][4];
+        // the chunk's 8 elements loaded first (independent loads in flight together)
+        double hv[8], sv[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int k = 8 * chunk + i;
+          hv[i] = 0.0;
+          sv[i] = 0.0;
+          if (k < rows && a < N) {
+            const int idx = (head + k) & (kRing - 1);
+            hv[i] = so.HSt[(int64_t)ts.ring_q[idx] * N + a];
+            sv[i] = ts.ring_s[idx];
+            // two accumulators (even / odd observations): shorter FMA chains
+            if (i & 1)
+              gsum1 = fma(hv[i], ts.ring_t[idx], gsum1);
+            else
+              gsum = fma(hv[i], ts.ring_t[idx], gsum);
+          }
+        }
 #pragma unroll
         for (int i = 0; i < 8; i += 2) {
           uint32_t lo2[2], hi2[2];
 #pragma unroll
           for (int u = 0; u < 2; u++) {
-            const int k = 8 * chunk + i + u;
-            long long F = 0;
-            if (k < rows && a < N) {
-              const int idx = (head + k) & (kRing - 1);
-              const int32_t q = ts.ring_q[idx];
-              const double h = so.HSt[(int64_t)q * N + a];
-              gsum = fma(h, ts.ring_t[idx], gsum);
-              F = fixed_prod(ts.ring_s[idx], h, Ea, bad);
-            }
+            const long long F = fixed_prod(sv[i + u], hv[i + u], Ea, bad);
             const unsigned long long U = (unsigned long long)F + kDigitBias;
             lo2[u] = (uint32_t)U;
             hi2[u] = (uint32_t)(U >> 32);
@@ -440,16 +467,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       head += rows;
     };
 
-    sel::ScanRange sr;
-    if (full_scan) {
-      sr.cu0 = 0;
-      sr.cu1 = g.nu - 1;
-      sr.cv0 = 0;
-      sr.cv1 = g.nv - 1;
-      sr.all_u = 1;
-    } else {
-      sr = sel::zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
-    }
+    const sel::ScanRange sr = ts.sr;
     for (int cv = sr.cv0; cv <= sr.cv1 && !abort; cv++) {
       for (int part = 0; part < 2 && !abort; part++) {
         int cu_a, cu_b;
@@ -534,21 +552,35 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncthreads();
           // the plain form's FP64 weights of the new entries (zone_gram.cu), one thread an
           // entry, so that the FP64 work runs with full warps: sqrt(c) = |w| / sqrt(r)
-          // (c = w (w / r), DCDCovar, covariance.F90:612-619) and c (yo - Hxf)
+          // (c = w (w / r), DCDCovar, covariance.F90:612-619) and c (yo - Hxf). The values
+          // (not the decisions, made above with the reference's rounding) are evaluated with
+          // fewer FP64 operations for the Cartesian and 1-D distances: exp(-d^2 / L^2) needs
+          // no square root or division, locfun(sqrt(d^2) / L) takes 1/L once a zone.
           if (tid < total) {
             const int slot = (tail + tid) & (kRing - 1);
             const int32_t qs = ts.ring_q[slot];
-            double d;
-            if (lp.loctype == 1)
-              d = sel::distance(so.u[qs], so.v[qs], zu, zv, lp.metric);
-            else
-              d = fabs(__dsub_rn(so.u[qs], zu));
             double w64;
-            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-              const double t = d / L;
-              w64 = exp(-(t * t));
+            if (fast) {
+              const double du = so.u[qs] - zu;
+              double D2 = du * du;
+              if (lp.loctype == 1) {
+                const double dv = so.v[qs] - zv;
+                D2 = fma(dv, dv, D2);
+              }
+              w64 = (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) ? exp(-(D2 * iL2))
+                                                            : sel::locfun_value(sqrt(D2) * iL);
             } else {
-              w64 = sel::locfun(d / L);
+              double d;
+              if (lp.loctype == 1)
+                d = sel::distance(so.u[qs], so.v[qs], zu, zv, lp.metric);
+              else
+                d = fabs(__dsub_rn(so.u[qs], zu));
+              if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+                const double t = d / L;
+                w64 = exp(-(t * t));
+              } else {
+                w64 = sel::locfun(d / L);
+              }
             }
             const double sc = fabs(w64) * isr[qs];
             ts.ring_s[slot] = sc;
@@ -565,7 +597,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int o = 16; o > 0; o >>= 1) nrel_local += __shfl_xor_sync(0xffffffffu, nrel_local, o);
     if (lane == 0) atomicAdd(&ts.nrel, nrel_local);
     if (bad) atomicOr(&ts.bad, 1);
-    gpart[kq * NB + a] = gsum;
+    gpart[kq * NB + a] = gsum + gsum1;
     if (ntile > 0) {
       if (pend0) drain(0);
       if (pend1) drain(1);

@@ -94,6 +94,8 @@ struct TcShared {
   int32_t nrel;
   int32_t flag;
   sel::ZoneCell32 zc;  // the zone's cell-relative FP32 coordinates (read by broadcast)
+  sel::ScanRange sr;   // the zone's cell range
+  float iL32;          // 1 / L
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -314,14 +316,25 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
     const double zu = (lp.loctype == 1) ? zx : (lp.loctype == 2 ? zzc : ztc);
     const double zv = (lp.loctype == 1) ? zy : 0.0;
     const double L = corr_len[z], Rmax = max_len[z];
-    const float iL32 = (float)(1.0 / L);
     // the FP32 distance (relative error < 1e-6, sel::ZoneCell32) decides outside a 3e-6 band
     const float r_lo = (float)Rmax * (1.f - 3e-6f), r_hi = (float)Rmax * (1.f + 3e-6f);
+    // the zone's FP64 set-up (divisions, floors) once, by one thread: evaluated by every thread
+    // it kept the FP64 pipe half busy
     if (tid == 0) {
       ts.nrel = 0;
       ts.zc = sel::zone_cell32(g, zu, zv, Rmax);
+      ts.iL32 = (float)(1.0 / L);
+      if (full_scan) {
+        ts.sr.cu0 = 0;
+        ts.sr.cu1 = g.nu - 1;
+        ts.sr.cv0 = 0;
+        ts.sr.cv1 = g.nv - 1;
+        ts.sr.all_u = 1;
+      } else {
+        ts.sr = sel::zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
+      }
     }
-    __syncthreads();  // ts.zc published (no thread reads it before this zone's scan)
+    __syncthreads();  // ts.zc, ts.sr, ts.iL32 published (read only in this zone's scan)
     const bool fastz = fast && ts.zc.ok && !brute;  // brute force: one cell, no local offsets
     for (int e = tid; e < C::kTri; e += kThreads) gacc[e] = 0.f;
     int head = 0, tail = 0, ntile = 0, ctile = 0, nrel_local = 0;
@@ -404,16 +417,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
       head += rows;
     };
 
-    sel::ScanRange sr;
-    if (full_scan) {
-      sr.cu0 = 0;
-      sr.cu1 = g.nu - 1;
-      sr.cv0 = 0;
-      sr.cv1 = g.nv - 1;
-      sr.all_u = 1;
-    } else {
-      sr = sel::zone_scan_range(g, lp.metric, lp.loctype, zu, zv, Rmax);
-    }
+    const sel::ScanRange& sr = ts.sr;  // read from shared memory (register pressure)
     for (int cv = sr.cv0; cv <= sr.cv1 && !abort; cv++) {
       for (int part = 0; part < 2 && !abort; part++) {
         int cu_a, cu_b;
@@ -454,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, TcCfg<NB>::kCtas)
               const float d32 = sel::cell_distance32(ts.zc, so, q, cv, lp.loctype == 1);
               const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
               if (inside >= 0) {
-                const float r32 = d32 * iL32;
+                const float r32 = d32 * ts.iL32;
                 if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
                   rel = inside;
                   w32 = (rel || !lp.localise) ? expf(-(r32 * r32)) : 0.f;

@@ -103,9 +103,9 @@ def test_ens2sqrt_sqrt2ens_match_oracle(oakg, device):
 
 @pytest.mark.parametrize("N", [2, 33, 65, 100])
 def test_sqrt2ens_identity_and_general_theta(oakg, N):
-    """Theta = I takes the closed form (registers up to 64 anomaly columns, two reads of S
-    beyond), a general Theta the library GEMM; both against the oracle's N x (N-1) product, on
-    device arrays with padded leading dimensions; ens2sqrt gives back the mean and S S^T."""
+    """Theta = I takes the closed form (row sums of S, one FMA an element), a general Theta the
+    library GEMM; both against the oracle's N x (N-1) product, on device arrays with padded
+    leading dimensions; ens2sqrt gives back the mean and S S^T."""
     import torch
     rng = np.random.default_rng(200 + N)
     n = 2500
