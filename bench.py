@@ -74,7 +74,10 @@ def dist_env():
 def workload_config(c, scale):
     return {"workload": c.name, "zones": int(c.Z), "n": int(c.n), "N": int(c.N), "m": int(c.m),
             "localisation": "Gaspari-Cohn locfun(d/6), maxLength 12 cells",
-            "precision": "fp64 (plain form)", "horizontal_scale": scale,
+            "precision": "fp64 (plain form: FP64 selection, weights, eigensolve and update; "
+                         "the Gram as exact integer products of 8-bit slices on the BF16 "
+                         "tensor cores)",
+            "horizontal_scale": scale,
             "l2": "inputs larger than L2 (Sf and Sa 664 MB each at full scale)"}
 
 

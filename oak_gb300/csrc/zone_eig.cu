@@ -741,9 +741,15 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
     __syncthreads();
-    // FP64: two classical Gram-Schmidt passes of column j against its cluster [cst[j], j).
-    // FP32 (larger relative rounding, gaps between clusters less reliable): every column
-    // against all columns of larger eigenvalue, largest first.
+    // FP64: classical Gram-Schmidt of column j against its cluster [cst[j], j). FP32 (larger
+    // relative rounding, gaps between clusters less reliable): every column against all columns
+    // of larger eigenvalue, largest first. Column j is a unit vector and the earlier columns
+    // are orthonormal: if one pass leaves it at least half its squared norm, it is orthogonal to
+    // them to working precision ("twice is enough", Kahan-Parlett; Parlett, The Symmetric
+    // Eigenvalue Problem, 6-9) and accepted after that pass. A vector that keeps less is
+    // collapsed (replaced below); it still gets the second pass, since later columns of the
+    // cluster are projected against its (normalised) residual, which must then be orthogonal
+    // to the earlier columns.
     const bool full = sizeof(R) < sizeof(double);
     for (int jj = 1; jj < N; jj++) {
       const int j = full ? N - 1 - jj : jj;
@@ -763,19 +769,21 @@ __global__ void __launch_bounds__(kThreads)
           U[i * ld + j] = s;
         }
         __syncthreads();
-      }
-      if (warp == 0) {
-        R s = 0;
-        for (int i = lane; i < N; i += 32) s = fma(U[i * ld + j], U[i * ld + j], s);
-        s = warp_sum(s);
-        // a unit vector that kept less than half its norm lay (almost) in the span of the
-        // cluster's earlier vectors: mark it for the complement fill below
-        if (lane == 0) {
-          red[0] = (s > R(0)) ? Prec<R>::rsqrt_(s) : R(0);
-          if (s < R(0.5)) cst[j] = -1;
+        if (warp == 0) {
+          R s = 0;
+          for (int i = lane; i < N; i += 32) s = fma(U[i * ld + j], U[i * ld + j], s);
+          s = warp_sum(s);
+          // a unit vector that kept less than half its norm lay (almost) in the span of the
+          // cluster's earlier vectors: mark it for the complement fill below
+          if (lane == 0) {
+            red[0] = (s > R(0)) ? Prec<R>::rsqrt_(s) : R(0);
+            red[1] = (s < R(0.5)) ? R(1) : R(0);
+            if (pass == 1 && s < R(0.5)) cst[j] = -1;
+          }
         }
+        __syncthreads();
+        if (red[1] == R(0)) break;  // uniform: accepted after this pass
       }
-      __syncthreads();
       const R sc = red[0];
       for (int i = tid; i < N; i += kThreads) U[i * ld + j] *= sc;
       __syncthreads();
