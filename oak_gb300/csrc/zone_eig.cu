@@ -519,10 +519,10 @@ __global__ void __launch_bounds__(128)
 // kernel live in local memory, and with thousands of threads per SM they go to DRAM (most of
 // the eigensolve's traffic); here the partial-pivoting LU is recomputed in each forward sweep
 // (fused with the elimination), the iterate is kept in registers (loops unrolled to 64), the
-// factor's first superdiagonal and pivot reciprocals in shared memory ([i][j] layout:
-// consecutive threads, consecutive words) and its second superdiagonal as one bit per row (it
-// is the tridiagonal's next off-diagonal entry where rows were swapped, else 0). 32 KB a
-// block: seven warps per SM.
+// factor's first superdiagonal, pivot reciprocals and multipliers in shared memory ([i][j]
+// layout: consecutive threads, consecutive words) and its second superdiagonal as one bit per
+// row (it is the tridiagonal's next off-diagonal entry where rows were swapped, else 0); the
+// second solve applies the stored factors instead of refactoring. 48 KB a block.
 
 // 1/p by two Newton steps from the FP32 reciprocal (relative error below 2^-52, not always
 // correctly rounded). The IEEE FP64 division is a called routine whose call keeps the live
@@ -556,10 +556,11 @@ __global__ void __launch_bounds__(kT64)
     k_eig_vectors_fp64(int N, int32_t nzc, const double* __restrict__ aux,
                        double* __restrict__ Zg, const int32_t* __restrict__ nobs) {
   constexpr int NV = kNV64;
-  extern __shared__ __align__(16) double sfac64[];  // u1, 1/pivot: [i][jl] each
+  extern __shared__ __align__(16) double sfac64[];  // u1, 1/pivot, multiplier: [i][jl] each
   __shared__ double sd[NV], se[NV + 1];
   double* su1 = sfac64;
   double* sui = sfac64 + NV * kT64;
+  double* sli = sfac64 + 2 * NV * kT64;
   const int jl = threadIdx.x, j = kT64 * blockIdx.y + jl;  // eigenpair j
   const int32_t zl = blockIdx.x;
   if (zl >= nzc || nobs[zl] == 0) return;  // block-uniform
@@ -592,27 +593,43 @@ __global__ void __launch_bounds__(kT64)
 #pragma unroll 1
     for (int it = 0; it < 2; it++) {
       double cd = sd[0] - l, csup = (N > 1) ? se[0] : 0.0;
+      if (it == 0) {
+        // the factorisation, fused with the elimination of the first right-hand side
 #pragma unroll
-      for (int i = 0; i < NV - 1; i++) {
-        if (i < N - 1) {
-          const double sub = se[i], dg = sd[i + 1] - l, sp = se[i + 1];  // se[i + 1] = 0 past N - 2
-          const bool swap = fabs(cd) < fabs(sub);
-          double pivot = swap ? sub : cd;
-          if (!swap && fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
-          const double ui = rcp_newton(pivot);
-          const double li = (swap ? cd : sub) * ui;
-          if (it == 0) {
+        for (int i = 0; i < NV - 1; i++) {
+          if (i < N - 1) {
+            const double sub = se[i], dg = sd[i + 1] - l, sp = se[i + 1];  // 0 past N - 2
+            const bool swap = fabs(cd) < fabs(sub);
+            double pivot = swap ? sub : cd;
+            if (!swap && fabs(pivot) < tiny) pivot = copysign(tiny, pivot);
+            const double ui = rcp_newton(pivot);
+            const double li = (swap ? cd : sub) * ui;
             su1[i * kT64 + jl] = swap ? dg : csup;
             sui[i * kT64 + jl] = ui;
+            sli[i * kT64 + jl] = li;
             if (swap) piv |= 1ull << i;
+            const double aa = swap ? csup : dg, bb = swap ? dg : csup;
+            cd = fma(-li, bb, aa);
+            const double nls = -li * sp;
+            csup = swap ? nls : sp;
+            const double xi = swap ? x[i + 1] : x[i], xn = swap ? x[i] : x[i + 1];
+            x[i] = xi;
+            x[i + 1] = fma(-li, xi, xn);
           }
-          const double aa = swap ? csup : dg, bb = swap ? dg : csup;
-          cd = fma(-li, bb, aa);
-          const double nls = -li * sp;
-          csup = swap ? nls : sp;
-          const double xi = swap ? x[i + 1] : x[i], xn = swap ? x[i] : x[i + 1];
-          x[i] = xi;
-          x[i + 1] = fma(-li, xi, xn);
+        }
+      } else {
+        // the second solve has the same factors (same Tri, same shift): apply the stored
+        // interchanges and multipliers only (the same values the factorisation produced, so
+        // the result is the one a recomputation would give, bit for bit)
+#pragma unroll
+        for (int i = 0; i < NV - 1; i++) {
+          if (i < N - 1) {
+            const bool swap = (piv >> i) & 1ull;
+            const double li = sli[i * kT64 + jl];
+            const double xi = swap ? x[i + 1] : x[i], xn = swap ? x[i] : x[i + 1];
+            x[i] = xi;
+            x[i + 1] = fma(-li, xi, xn);
+          }
         }
       }
       if (it == 0) {
@@ -1106,7 +1123,7 @@ cudaError_t launch_e2(int N, int32_t nzc, R* d_aux, R* d_Z, const int32_t* d_nob
     k_eig_tridiag_values<R><<<(nzc + 127) / 128, 128, 0, st>>>(N, nzc, d_aux, d_nobs, d_status);
   }
   if (sizeof(R) == sizeof(double) && N <= kNV64) {
-    const size_t smem = (size_t)2 * kNV64 * kT64 * sizeof(double);
+    const size_t smem = (size_t)3 * kNV64 * kT64 * sizeof(double);
     cudaError_t e = cudaFuncSetAttribute(k_eig_vectors_fp64,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
