@@ -90,7 +90,8 @@ extern "C" {
                                     FMA) instead of the tensor cores (3xTF32, used when the
                                     longest zone has at least 48 elements); both give
                                     FP32-level products                                    */
-#define OAKG_FLAG_SIMT_GRAM 8    /* plain form: the Gram products on the FP64 CUDA cores
+#define OAKG_FLAG_SIMT_GRAM 8    /* plain form: the Gram and square-root-transform
+                                    (U (I+L)^-1/2 U^T) products on the FP64 CUDA cores
                                     instead of the tensor cores (exact 8-bit slice products,
                                     used for N <= 64); both give FP64-level products       */
 

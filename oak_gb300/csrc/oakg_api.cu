@@ -227,8 +227,13 @@ struct ZoneKernels<double> {
     return zone_gram_fp64(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
                           st, order);
   }
-  template <typename... A>
-  static cudaError_t eig(A... a) { return zone_eig_fp64(a...); }
+  // T_sym on the tensor cores as the Gram (unless OAKG_FLAG_SIMT_GRAM)
+  static cudaError_t eig(int N, int32_t nzc, double* GT, const double* g, const int32_t* nobs,
+                         int rotate, double* ampl, int32_t* status, double* aux, double* Z,
+                         int32_t* work, cudaStream_t st, int32_t flags) {
+    return zone_eig_fp64(N, nzc, GT, g, nobs, rotate, ampl, status, aux, Z, work, st,
+                         (flags & OAKG_FLAG_SIMT_GRAM) ? 0 : 1);
+  }
   template <typename... A>
   static cudaError_t update(A... a) { return zone_update_fp64(a...); }
   template <typename... A>
@@ -248,8 +253,11 @@ struct ZoneKernels<float> {
     return zone_gram_fp32(g, so, N, lp, z0, nzc, zxyzt, corr, maxl, d_G, d_g, nobs, brute, work,
                           st, order);
   }
-  template <typename... A>
-  static cudaError_t eig(A... a) { return zone_eig_fp32(a...); }
+  static cudaError_t eig(int N, int32_t nzc, float* GT, const float* g, const int32_t* nobs,
+                         int rotate, float* ampl, int32_t* status, float* aux, float* Z,
+                         int32_t* work, cudaStream_t st, int32_t /*flags*/) {
+    return zone_eig_fp32(N, nzc, GT, g, nobs, rotate, ampl, status, aux, Z, work, st);
+  }
   template <typename... A>
   static cudaError_t update(A... a) { return zone_update_fp32(a...); }
   template <typename... A>
@@ -448,10 +456,10 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
                                   d_Sref, st);
       else
         e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate,
-                   d_za, d_status, d_aux, d_zvec, d_work + 4, st);
+                   d_za, d_status, d_aux, d_zvec, d_work + 4, st, a.lp.flags);
     } else {
       e = K::eig(N, nzc, d_G, (const R*)d_gv, (const int32_t*)(a.nobs + z0), a.lp.rotate, d_za,
-                 d_status, d_aux, d_zvec, d_work + 4, st);
+                 d_status, d_aux, d_zvec, d_work + 4, st, a.lp.flags);
     }
     if (e != cudaSuccess) return cuda_fail(e, "eigensolve kernel");
     if (timed) cudaEventRecord(c->ev[4], st);

@@ -96,6 +96,15 @@ cudaError_t zone_gram_tc(const CellGrid& g, const SortedObs& so, int N, LocParam
 // ZST_TIMEOUT (OR) if a bounded device wait expired.
 int gram_oz_max_n();
 size_t gram_oz_scratch_bytes(int64_t m);
+// The FP64 square-root transform of zones [0, nzc) on the tensor cores, N <= gram_oz_max_n():
+// T_sym = X^T X with X_ka = q_k U_ak (q_k = (1 + lambda_k)^-1/4) as exact 8-bit slice products,
+// then T = T_sym Omega (rotate) in FP64, written to d_GT (N x N a zone). Inputs left by the
+// eigensolve's transform stage: the eigenvectors vector-major in d_Z (d_Z[k N + a] = U_ak),
+// q_k at d_aux[4N + k] and v at d_aux[k] of each zone (zone_eig_aux(N) elements a zone).
+// A bounded wait that expires sets ZST_TIMEOUT in the zone's d_status.
+cudaError_t zone_tsym_oz(int N, int32_t nzc, double* d_GT, const double* d_aux,
+                         const double* d_Z, const int32_t* d_nobs, int rotate,
+                         int32_t* d_status, cudaStream_t st);
 cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int N, LocParams lp,
                          int32_t z0, int32_t nzc, const double* zone_xyzt, const double* corr_len,
                          const double* max_len, double* d_G, double* d_g, int32_t* d_nobs,
@@ -178,10 +187,12 @@ cudaError_t global_gram_fp64(int64_t m, int N, const double* HSf, int64_t ldH,
 // zone), T = U (I+L)^-1/2 U^T Omega written over G, ampl (N per zone), status per zone.
 // d_nobs/d_ampl/d_status are chunk-relative.
 // d_aux holds zone_eig_aux(N) elements per zone, d_Z N*N elements per zone;
-// d_work two counters.
+// d_work two counters. FP64 with tc_products and N <= gram_oz_max_n(): T_sym = U (I+L)^-1/2 U^T
+// as exact slice products on the tensor cores (zone_tsym_oz), else on the FP64 CUDA cores.
 cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
                           const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
-                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st);
+                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st,
+                          int tc_products = 1);
 cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,
                           const int32_t* d_nobs, int rotate, float* d_ampl, int32_t* d_status,
                           float* d_aux, float* d_Z, int32_t* d_work, cudaStream_t st);

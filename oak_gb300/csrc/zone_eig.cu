@@ -692,10 +692,11 @@ __global__ void __launch_bounds__(kT64)
 // ------------------------------------------------------------------------------------ E3
 template <typename R>
 __global__ void __launch_bounds__(kThreads)
-    k_eig_transform(int N, int32_t nzc, R* __restrict__ GT, const R* __restrict__ aux,
-                    const R* __restrict__ Zg, const R* __restrict__ gv,
+    k_eig_transform(int N, int32_t nzc, R* __restrict__ GT, R* __restrict__ aux,
+                    R* __restrict__ Zg, const R* __restrict__ gv,
                     const int32_t* __restrict__ nobs, int rotate, R* __restrict__ ampl_out,
-                    int32_t* __restrict__ status, int32_t* __restrict__ work, int a_global) {
+                    int32_t* __restrict__ status, int32_t* __restrict__ work, int a_global,
+                    int tc_out) {
   extern __shared__ __align__(16) unsigned char dyn_raw[];
   R* dyn = reinterpret_cast<R*>(dyn_raw);
   const int ld = N + 1;
@@ -728,8 +729,8 @@ __global__ void __launch_bounds__(kThreads)
       continue;
     }
     R* Gz = GT + (int64_t)zl * N * N;
-    const R* ax = aux + (int64_t)zl * aux_stride(N);
-    const R* Z = Zg + (int64_t)zl * N * N;
+    R* ax = aux + (int64_t)zl * aux_stride(N);
+    R* Z = Zg + (int64_t)zl * N * N;
     R* Aw = a_global ? Gz : A;
     const int la = a_global ? N : ld;
     for (int idx = tid; idx < N * N; idx += kThreads) {
@@ -956,6 +957,22 @@ __global__ void __launch_bounds__(kThreads)
       const R inv = red[0];
       for (int r = tid; r < N; r += kThreads) vv[r] *= inv;
     }
+    if (tc_out) {
+      // T_sym and T are formed on the tensor cores (zone_tsym_oz): the eigenvectors go to the
+      // zone's Z slot vector-major (Z[k N + i] = U_ik; Z was read above), (1 + lambda)^-1/4 to
+      // the shift slots and v to the d slots of aux (neither is read after this stage)
+      for (int idx = tid; idx < N * N; idx += kThreads) {
+        const int k = idx / N, i = idx - k * N;
+        Z[idx] = U[i * ld + k];
+      }
+      for (int i = tid; i < N; i += kThreads) {  // vv[i] was scaled by this thread
+        ax[4 * N + i] = qs[i];
+        ax[i] = rotate ? vv[i] : R(0);
+      }
+      if (tid == 0 && nan_flag) status[zl] |= ZST_NAN;
+      __syncthreads();
+      continue;
+    }
     // T_sym = U diag(sqrt(lambda)) U^T: U's columns scaled by lambda^(1/4), then U U^T
     for (int idx = tid; idx < N * N; idx += kThreads) {
       int r = idx / N, i = idx - r * N;
@@ -1053,9 +1070,9 @@ cudaError_t launch_e1(int N, int32_t nzc, R* d_GT, R* d_aux, const int32_t* d_no
 }
 
 template <typename R>
-cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z, const R* d_g,
+cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, R* d_aux, R* d_Z, const R* d_g,
                       const int32_t* d_nobs, int rotate, R* d_ampl, int32_t* d_status,
-                      int32_t* d_work, cudaStream_t st) {
+                      int32_t* d_work, cudaStream_t st, int tc_out = 0) {
   // two N x N matrices in shared memory when they fit (227 KB a block), else one (A in GT)
   size_t smem3 = (size_t)(2 * N * (N + 1) + 16 * N) * sizeof(R) + (size_t)N * sizeof(int);
   int a_global = 0;
@@ -1068,7 +1085,7 @@ cudaError_t launch_e3(int N, int32_t nzc, R* d_GT, const R* d_aux, const R* d_Z,
   if (e != cudaSuccess) return e;
   k_eig_transform<R><<<grid_for_smem((const void*)k_eig_transform<R>, smem3, nzc), kThreads,
                        smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl,
-                                    d_status, d_work, a_global);
+                                    d_status, d_work, a_global, tc_out);
   return cudaSuccess;
 }
 
@@ -1091,24 +1108,23 @@ cudaError_t launch_e1<float>(int N, int32_t nzc, float* d_GT, float* d_aux,
 }
 
 template <>
-cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, const float* d_aux,
-                             const float* d_Z, const float* d_g, const int32_t* d_nobs,
-                             int rotate, float* d_ampl, int32_t* d_status, int32_t* d_work,
-                             cudaStream_t st) {
+cudaError_t launch_e3<float>(int N, int32_t nzc, float* d_GT, float* d_aux, float* d_Z,
+                             const float* d_g, const int32_t* d_nobs, int rotate, float* d_ampl,
+                             int32_t* d_status, int32_t* d_work, cudaStream_t st,
+                             int /*tc_out*/) {
   // mode 0 does not write Z
   if (N <= eig32_max_n())
-    return eig32_transform(N, nzc, d_GT, d_aux, const_cast<float*>(d_Z), d_g, d_nobs, rotate,
-                           d_ampl, d_status, st);
+    return eig32_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, st);
   if (N <= eig128_max_n())
-    return eig128_transform(N, nzc, d_GT, d_aux, const_cast<float*>(d_Z), d_g, d_nobs, rotate,
-                            d_ampl, d_status, st);
+    return eig128_transform(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status,
+                            st);
   size_t smem3 = (size_t)(2 * N * (N + 1) + 16 * N) * sizeof(float) + (size_t)N * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(k_eig_transform<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
   if (e != cudaSuccess) return e;
   k_eig_transform<float><<<grid_for_smem((const void*)k_eig_transform<float>, smem3, nzc),
                            kThreads, smem3, st>>>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate,
-                                                  d_ampl, d_status, d_work, 0);
+                                                  d_ampl, d_status, d_work, 0, 0);
   return cudaSuccess;
 }
 
@@ -1156,7 +1172,7 @@ cudaError_t launch_e2<float>(int N, int32_t nzc, float* d_aux, float* d_Z, const
 template <typename R>
 cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32_t* d_nobs,
                           int rotate, R* d_ampl, int32_t* d_status, R* d_aux, R* d_Z,
-                          int32_t* d_work, cudaStream_t st) {
+                          int32_t* d_work, cudaStream_t st, int tc_products = 0) {
   if (N < 2 || N > kNMax) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int32_t) * (nzc > 0 ? nzc : 1), st);
   if (e != cudaSuccess) return e;
@@ -1167,10 +1183,18 @@ cudaError_t zone_eig_impl(int N, int32_t nzc, R* d_GT, const R* d_g, const int32
   // E2a, E2b
   e = launch_e2<R>(N, nzc, d_aux, d_Z, d_nobs, d_status, st);
   if (e != cudaSuccess) return e;
+  // T_sym on the tensor cores (FP64 only): E3 hands over U, (1 + lambda)^-1/4 and v
+  const int tc = (sizeof(R) == sizeof(double) && tc_products && N <= gram_oz_max_n()) ? 1 : 0;
   e = launch_e3<R>(N, nzc, d_GT, d_aux, d_Z, d_g, d_nobs, rotate, d_ampl, d_status, d_work + 1,
-                   st);
+                   st, tc);
   if (e != cudaSuccess) return e;
   count_launches(4);
+  if (tc) {
+    e = zone_tsym_oz(N, nzc, reinterpret_cast<double*>(d_GT),
+                     reinterpret_cast<const double*>(d_aux), reinterpret_cast<const double*>(d_Z),
+                     d_nobs, rotate, d_status, st);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 
@@ -1180,9 +1204,10 @@ size_t zone_eig_aux(int N) { return (size_t)aux_stride(N); }
 
 cudaError_t zone_eig_fp64(int N, int32_t nzc, double* d_GT, const double* d_g,
                           const int32_t* d_nobs, int rotate, double* d_ampl, int32_t* d_status,
-                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st) {
+                          double* d_aux, double* d_Z, int32_t* d_work, cudaStream_t st,
+                          int tc_products) {
   return zone_eig_impl<double>(N, nzc, d_GT, d_g, d_nobs, rotate, d_ampl, d_status, d_aux, d_Z,
-                               d_work, st);
+                               d_work, st, tc_products);
 }
 
 cudaError_t zone_eig_fp32(int N, int32_t nzc, float* d_GT, const float* d_g,

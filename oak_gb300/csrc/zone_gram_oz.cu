@@ -701,6 +701,272 @@ __global__ void k_oz_exponents(int N, const unsigned long long* __restrict__ mx,
   E[a] = e;
 }
 
+// ------------------------------------------------------------------ square-root transform
+// The plain form's T_sym = U diag((1 + lambda)^-1/2) U^T (rrsqrt.F90:162-169) as the Gram X^T X
+// of X_ka = q_k U_ak, q_k = (1 + lambda_k)^-1/4: row k of X is eigenvector k scaled, so a zone
+// is one K-tile of 64 rows and the slice products of k_zone_gram_oz apply unchanged. With one
+// K-tile every level (at most 7 x 64 x 2^14 < 2^23 in magnitude) is exact in its FP32
+// accumulator, and one read of the tensor memory gives T_sym = 2^(E_a + E_b - 36) (v + V456 /
+// 256), recombined here as the integer v 2^16 + round(256 V456) (below 2^62) with one
+// conversion to FP64. Column exponents come from the exponent fields: a normal x lies below
+// 2^(e(x) - 1022) (e the biased exponent), so E_a = max_k (e(q_k) + e(U_ak)) - 2044 bounds
+// |X_ka| (at most two bits above the column's maximum) and every product fits the fixed point.
+//
+// T = T_sym Omega (rrsqrt.F90:171-185) follows in FP64. Omega = P_v P_w + (1 - s_v s_w) v w^T
+// with P_x = I - u_x u_x^T / c_x, u_x = x + s_x e_N, c_x = 1 + |x_N| (matoper.F90:509-535;
+// w = N^-1/2 1, s_w = 1), so T = T_sym - a u_v^T - g u_w^T + b w^T is a rank-three update
+// with a = T_sym u_v / c_v, g = (T_sym u_w - (u_v . u_w) a) / c_w and b = (1 - s_v) T_sym v.
+// T_sym v and the row sums (T_sym u_w = w rowsum + T_sym e_N) are accumulated while T_sym is
+// formed; the update is then one FMA and one add an element.
+// One CTA of 512 threads per SM (persistent, zones strided); the shared-memory request is
+// sized so that no second CTA (which would wait for the tensor memory) shares an SM.
+constexpr int kTsLd = NB + 1;
+constexpr size_t kTsData = 1024 + (size_t)kBufBytes + kSliceBytes +
+                           (size_t)NB * kTsLd * sizeof(double) + 14 * NB * sizeof(double);
+constexpr size_t kTsDynSmem = (size_t)116 * 1024;
+static_assert(kTsData <= kTsDynSmem, "square-root transform shared memory");
+
+struct TsShared {
+  unsigned long long mbar;
+  uint32_t tmem_base;
+  int32_t emax[NB];  // max_k e(q_k) + e(U_ak) of the zone
+  int32_t E[NB];     // column exponents
+  int32_t flag;
+  int32_t bad;
+  double uvuw;       // u_v . u_w
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_zone_tsym_oz(int N, int32_t nzc, double* __restrict__ GT, const double* __restrict__ aux,
+                   const double* __restrict__ Zg, const int32_t* __restrict__ nobs, int rotate,
+                   int32_t* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char dyn_raw[];
+  __shared__ __align__(16) TsShared ts;
+  const uint32_t raw_addr = smem_u32(dyn_raw);
+  const uint32_t pad = ((raw_addr + 1023u) & ~1023u) - raw_addr;
+  unsigned char* tile = dyn_raw + pad;  // the 7 slices and the zero slice past them
+  const uint32_t tile_addr = raw_addr + pad;
+  double* Ts = reinterpret_cast<double*>(tile + kBufBytes + kSliceBytes);  // [NB][kTsLd]
+  double* vv = Ts + NB * kTsLd;  // v
+  double* uv = vv + NB;          // u_v
+  double* pv = uv + NB;          // [4][NB] partial T_sym v (column groups)
+  double* ps = pv + 4 * NB;      // [4][NB] partial row sums
+  double* ar = ps + 4 * NB;      // a
+  double* cr = ar + NB;          // (b - g) w
+  double* gr = cr + NB;          // g
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int a = tid & (NB - 1), kq = tid >> 6;  // member a; rows 8 kq .. 8 kq + 7 of X
+  const uint32_t mbar = smem_u32(&ts.mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    ts.flag = 0;
+  }
+  if (tid < NB) ts.emax[tid] = 0;
+  // rows 64-127 of the last digit's A operand: read by the MMA, never read back
+  for (uint32_t i = tid; i < kSliceBytes / 16; i += kThreads)
+    reinterpret_cast<uint4*>(tile + kBufBytes)[i] = make_uint4(0, 0, 0, 0);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ts.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = ts.tmem_base;
+  const double wv = 1.0 / sqrt((double)N);
+  const double cw = 1.0 + wv, icw = 1.0 / cw;
+  uint32_t ph = 0;
+  bool pending = false;  // an MMA group whose completion was not observed (timeout)
+  for (int32_t zl = blockIdx.x; zl < nzc; zl += gridDim.x) {
+    if (nobs[zl] == 0) continue;  // block-uniform
+    const double* ax = aux + (int64_t)zl * (5 * N + 2);
+    const double* Uz = Zg + (int64_t)zl * N * N;
+    // this thread's 8 elements of X (q_k, U_ak for k = 8 kq + i) and their exponent bound
+    double hv[8], sv[8];
+    int em = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int k = 8 * kq + i;
+      hv[i] = (a < N && k < N) ? Uz[k * N + a] : 0.0;
+      sv[i] = (k < N) ? ax[4 * N + k] : 0.0;
+      const int es = (int)(((unsigned long long)__double_as_longlong(sv[i]) >> 52) & 0x7FFu);
+      const int eh = (int)(((unsigned long long)__double_as_longlong(hv[i]) >> 52) & 0x7FFu);
+      if (es != 0 && eh != 0 && es != 0x7FF && eh != 0x7FF) em = max(em, es + eh);
+    }
+    if (em > 0) atomicMax(&ts.emax[a], em);
+    if (tid == 0) ts.bad = 0;
+    if (rotate && tid < NB) vv[tid] = (tid < N) ? ax[tid] : 0.0;
+    __syncthreads();  // emax and v complete
+    const double sgv = signbit(vv[N - 1]) ? -1.0 : 1.0;  // s_v (rotate only)
+    const int ema = ts.emax[a];
+    const int Ea = (ema > 0) ? ema - 2044 : 0;
+    if (tid < NB) {  // a == tid
+      ts.E[tid] = Ea;
+      if (rotate) uv[tid] = vv[tid] + ((tid == N - 1) ? sgv : 0.0);
+    }
+    int bad = 0;
+    uint32_t pk[kDigits][4];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+      uint32_t lo2[2], hi2[2];
+#pragma unroll
+      for (int u = 0; u < 2; u++) {
+        const long long F = fixed_prod(sv[i + u], hv[i + u], Ea, bad);
+        const unsigned long long Ub = (unsigned long long)F + kDigitBias;
+        lo2[u] = (uint32_t)Ub;
+        hi2[u] = (uint32_t)(Ub >> 32);
+      }
+      const int wd = i >> 1;
+#pragma unroll
+      for (int p = 0; p < kDigits; p++) {
+        const int byte = 6 - p;
+        const uint32_t b0 = (byte >= 4) ? (hi2[0] >> (8 * (byte - 4))) & 255u
+                                        : (lo2[0] >> (8 * byte)) & 255u;
+        const uint32_t b1 = (byte >= 4) ? (hi2[1] >> (8 * (byte - 4))) & 255u
+                                        : (lo2[1] >> (8 * byte)) & 255u;
+        pk[p][wd] = __byte_perm(digit_bits(b0), digit_bits(b1), 0x7632);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < kDigits; p++)
+      *reinterpret_cast<uint4*>(tile + p * kSliceBytes + tile_off(a, kq)) =
+          make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
+    if (bad) atomicOr(&ts.bad, 1);
+    if (rotate && warp == 1) {  // u_v . u_w, u_w = w 1 + e_N
+      double sdot = 0.0;
+      for (int j = lane; j < N; j += 32) {
+        const double uj = vv[j] + ((j == N - 1) ? sgv : 0.0);
+        sdot = fma(uj, wv + ((j == N - 1) ? 1.0 : 0.0), sdot);
+      }
+      for (int o = 16; o > 0; o >>= 1) sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
+      if (lane == 0) ts.uvuw = sdot;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();  // tile staged; every emax read done; E, u_v, u_v . u_w published
+    if (tid < NB) ts.emax[tid] = 0;
+    if (tid == 0) {
+      fence_after();
+#pragma unroll 1
+      for (int kk = 0; kk < KT / 16; kk++) {
+        const uint32_t ko = kk * 32;
+        const uint32_t acc0 = kk > 0 ? 1u : 0u;
+        // levels 0..3 in columns 64 L: A = [D_p ; D_p+1], B = D_0 .. D_(3-p)
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+          mma_bf16(tmem + 64 * p, make_desc(tile_addr + p * kSliceBytes + ko),
+                   make_desc(tile_addr + ko), idesc_bf16(64u * (4 - p)), p == 0 ? acc0 : 1u);
+        // levels 4..6 in columns 256 + 64 (L - 4): B = D_qlo .. D_qhi, q = L - p
+#pragma unroll
+        for (int p = 0; p < kDigits; p++) {
+          const int qlo = (4 - p > 0) ? 4 - p : 0;
+          const int qhi = (6 - p < kDigits - 1) ? 6 - p : kDigits - 1;
+          const int off = qlo - (4 - p);
+          mma_bf16(tmem + 256 + 64 * off, make_desc(tile_addr + p * kSliceBytes + ko),
+                   make_desc(tile_addr + qlo * kSliceBytes + ko),
+                   idesc_bf16(64u * (qhi - qlo + 1)), p == 0 ? acc0 : 1u);
+        }
+      }
+      mma_commit(mbar);
+      if (!mbar_wait(mbar, ph)) ts.flag = 1;
+    }
+    ph ^= 1u;
+    __syncthreads();  // MMA completion (or the timeout) published
+    if (ts.flag) {
+      pending = true;
+      if (tid == 0) atomicOr(&status[zl], ZST_TIMEOUT);
+      break;
+    }
+    fence_after();
+    // T_sym from the accumulators: lanes 0-63 (rows j) are read by warps 0, 1, 4, 5, 8, 9,
+    // 12, 13; warp group cg takes columns 16 cg .. 16 cg + 15 of all seven levels, and its
+    // partial sums of T_sym v and of the row
+    if ((warp & 3) < 2) {
+      const int qd = warp & 3, cg = warp >> 2;
+      const int j = 32 * qd + lane;
+      const uint32_t ta = tmem + ((uint32_t)(32 * qd) << 16);
+      const bool zbad = ts.bad != 0;
+      const int Ej = ts.E[j];
+      double sv_part = 0.0, sr_part = 0.0;
+#pragma unroll 1
+      for (int h8 = 0; h8 < 2; h8++) {
+        const int c0 = 16 * cg + 8 * h8;
+        float l0[8], l1[8], l2[8], l3[8], l4[8], l5[8], l6[8];
+        tmem_ld8(ta + c0, l0);
+        tmem_ld8(ta + 64 + c0, l1);
+        tmem_ld8(ta + 128 + c0, l2);
+        tmem_ld8(ta + 192 + c0, l3);
+        tmem_ld8(ta + 256 + c0, l4);
+        tmem_ld8(ta + 320 + c0, l5);
+        tmem_ld8(ta + 384 + c0, l6);
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+          const int c = c0 + t;
+          const long long v =
+              (((long long)__float2int_rn(l0[t]) * 256 + __float2int_rn(l1[t])) * 256 +
+               __float2int_rn(l2[t])) * 256 +
+              __float2int_rn(l3[t]);
+          // 256 V456 is below 2^31 in magnitude (level 4 below 5 x 64 x 2^14)
+          const float f456 = fmaf(l6[t], 1.f / 65536.f, fmaf(l5[t], 1.f / 256.f, l4[t]));
+          const long long vt = v * 65536 + (long long)__float2int_rn(f456 * 256.f);
+          int ex = Ej + ts.E[c] - 52 + 1023;
+          ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+          double val = (double)vt * __longlong_as_double((long long)ex << 52);
+          if (zbad) val = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input
+          Ts[j * kTsLd + c] = val;
+          if (rotate) {
+            sv_part = fma(val, vv[c], sv_part);
+            sr_part += (c < N) ? val : 0.0;
+          }
+        }
+      }
+      if (rotate) {
+        pv[cg * NB + j] = sv_part;
+        ps[cg * NB + j] = sr_part;
+      }
+    }
+    fence_before();
+    __syncthreads();  // T_sym and the partial sums complete; tensor memory read
+    double* Gz = GT + (int64_t)zl * N * N;
+    if (rotate) {
+      if (tid < N) {
+        const int i = tid;
+        const double tvi = (pv[i] + pv[NB + i]) + (pv[2 * NB + i] + pv[3 * NB + i]);  // T_sym v
+        const double rsi = (ps[i] + ps[NB + i]) + (ps[2 * NB + i] + ps[3 * NB + i]);
+        const double tlast = Ts[i * kTsLd + N - 1];
+        const double ai = fma(sgv, tlast, tvi) / (1.0 + fabs(vv[N - 1]));  // T_sym u_v / c_v
+        const double gi = fma(-ts.uvuw, ai, fma(wv, rsi, tlast)) * icw;
+        ar[i] = ai;
+        gr[i] = gi;
+        cr[i] = ((1.0 - sgv) * tvi - gi) * wv;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < N * N; idx += kThreads) {
+        const int i = idx / N, j = idx - i * N;
+        double t = fma(-ar[i], uv[j], Ts[i * kTsLd + j]) + cr[i];
+        if (j == N - 1) t -= gr[i];
+        Gz[idx] = t;
+      }
+    } else {
+      for (int idx = tid; idx < N * N; idx += kThreads) {
+        const int i = idx / N, j = idx - i * N;
+        Gz[idx] = Ts[i * kTsLd + j];
+      }
+    }
+    __syncthreads();  // T_sym, the sums and the coefficients consumed before the next zone
+  }
+  // teardown: no MMA may still write tensor memory when it is freed
+  if (pending && tid == 0) mbar_wait(mbar, ph ^ 1u);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols));
+}
+
 }  // namespace
 
 int gram_oz_max_n() { return NB; }
@@ -746,6 +1012,27 @@ cudaError_t zone_gram_oz(const CellGrid& g, const SortedObs& so, int64_t m, int 
   k_zone_gram_oz<<<grid, kThreads, kDynSmem, st>>>(g, so, N, lp, z0, nzc, zone_xyzt, corr_len,
                                                    max_len, E, isr, d_G, d_g, d_nobs, brute,
                                                    d_work, d_err, order);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t zone_tsym_oz(int N, int32_t nzc, double* d_GT, const double* d_aux,
+                         const double* d_Z, const int32_t* d_nobs, int rotate,
+                         int32_t* d_status, cudaStream_t st) {
+  if (N < 1 || N > NB) return cudaErrorInvalidValue;
+  if (nzc <= 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_zone_tsym_oz, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kTsDynSmem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_zone_tsym_oz, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = sms < nzc ? sms : nzc;
+  k_zone_tsym_oz<<<grid, kThreads, kTsDynSmem, st>>>(N, nzc, d_GT, d_aux, d_Z, d_nobs, rotate,
+                                                     d_status);
   count_launches(1);
   return cudaGetLastError();
 }
