@@ -359,8 +359,8 @@ def loc_analysis(zone_size, xf, Hxf, yo, Sf, HSf, r_diag, zone_pos, obs_pos, cor
     eigenpairs refined to FP64 accuracy). ``smw_B`` (m x k): the observation error
     covariance R = diag(r_diag) + B B^T (SMWCovar, covariance.F90:464-570; FP64 form).
     ``simt_update``: the mixed form's ensemble update on the CUDA cores instead of the tensor
-    cores. ``simt_gram``: the plain form's Gram products on the FP64 CUDA cores instead of the
-    tensor cores (exact 8-bit slice products, N <= 64).
+    cores. ``simt_gram``: the plain form's Gram and square-root-transform products on the FP64
+    CUDA cores instead of the tensor cores (exact 8-bit slice products, N <= 64).
 
     A float32 ``Sf`` selects FP32 storage at the boundary (oakg_locanalysis_f32): xf, Hxf, yo,
     HSf, r_diag are then taken, and xa, Sa, amplitudes returned, in float32; the geometry

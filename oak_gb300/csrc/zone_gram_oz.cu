@@ -81,6 +81,10 @@ struct OzShared {
   double ring_t[kRing];  // w^2 / r_q (yo - Hxf)_q
   unsigned long long mbar[2];
   int32_t warp_cnt[kThreads / 32];
+  int32_t rlo[kThreads];   // first observation of each candidate range of a block of ranges
+  int32_t roff[kThreads];  // exclusive prefix of the ranges' lengths
+  int32_t wpre[kThreads / 32];
+  int32_t rtotal;
   int32_t E[NB];         // column exponents
   uint32_t tmem_base;
   int32_t zone;
@@ -468,128 +472,180 @@ __global__ void __launch_bounds__(kThreads, 1)
     };
 
     const sel::ScanRange sr = ts.sr;
-    for (int cv = sr.cv0; cv <= sr.cv1 && !abort; cv++) {
-      for (int part = 0; part < 2 && !abort; part++) {
-        int cu_a, cu_b;
-        if (sr.all_u) {
-          if (part) break;
-          cu_a = 0;
-          cu_b = g.nu - 1;
-        } else if (!g.periodic_u) {
-          if (part) break;
-          cu_a = sr.cu0;
-          cu_b = sr.cu1;
-        } else {
-          const int a0 = sr.cu0, b0 = sr.cu1;
-          if (a0 < 0) {
-            cu_a = part ? 0 : a0 + g.nu;
-            cu_b = part ? b0 : g.nu - 1;
-          } else if (b0 >= g.nu) {
-            cu_a = part ? 0 : a0;
-            cu_b = part ? b0 - g.nu : g.nu - 1;
+    // The zone's candidates are the observations of cell rows cv0..cv1, each row one or (a
+    // periodic u axis wrapping) two contiguous ranges of the cell-sorted order. Range ri is
+    // (row cv0 + ri / 2, part ri % 2); blocks of kThreads ranges are flattened into one index
+    // space (exclusive prefix of their lengths), so that a pass of kThreads threads takes
+    // kThreads candidates across rows in the order of the rows. The order, and so the ring
+    // and the selection, are those of a row-by-row scan.
+    const int nranges = 2 * (sr.cv1 - sr.cv0 + 1);
+    for (int rbase = 0; rbase < nranges && !abort; rbase += kThreads) {
+      {
+        const int ri = rbase + tid;
+        int32_t rq0 = 0, rlen = 0;
+        if (ri < nranges) {
+          const int cv = sr.cv0 + (ri >> 1), part = ri & 1;
+          int cu_a = 0, cu_b = -1;
+          if (sr.all_u) {
+            if (!part) cu_b = g.nu - 1;
+          } else if (!g.periodic_u) {
+            if (!part) {
+              cu_a = sr.cu0;
+              cu_b = sr.cu1;
+            }
           } else {
-            if (part) break;
-            cu_a = a0;
-            cu_b = b0;
+            const int a0 = sr.cu0, b0 = sr.cu1;
+            if (a0 < 0) {
+              cu_a = part ? 0 : a0 + g.nu;
+              cu_b = part ? b0 : g.nu - 1;
+            } else if (b0 >= g.nu) {
+              cu_a = part ? 0 : a0;
+              cu_b = part ? b0 - g.nu : g.nu - 1;
+            } else if (!part) {
+              cu_a = a0;
+              cu_b = b0;
+            }
+          }
+          const int64_t c_lo = (int64_t)cu_a + (int64_t)g.nu * cv;
+          const int64_t c_hi = (int64_t)cu_b + (int64_t)g.nu * cv;
+          if (c_lo <= c_hi && c_lo >= 0 && c_hi < ncells) {
+            rq0 = so.cell_start[c_lo];
+            rlen = so.cell_start[c_hi + 1] - rq0;
           }
         }
-        const int64_t c_lo = (int64_t)cu_a + (int64_t)g.nu * cv;
-        const int64_t c_hi = (int64_t)cu_b + (int64_t)g.nu * cv;
-        if (c_lo > c_hi || c_lo < 0 || c_hi >= ncells) continue;
-        const int32_t q_lo = so.cell_start[c_lo], q_hi = so.cell_start[c_hi + 1];
-        for (int32_t qb = q_lo; qb < q_hi && !abort; qb += kThreads) {
-          const int32_t q = qb + tid;
-          int sel = 0, rel = 0;
-          if (q < q_hi) {
-            // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
-            bool done = false;
-            if (fastz) {
-              const float d32 = sel::cell_distance32(zc, so, q, cv, lp.loctype == 1);
-              const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
-              if (inside >= 0) {
-                const float r32 = d32 * iL32;
-                if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-                  rel = inside;
-                  done = true;
-                } else if (r32 >= 2.f + 1e-5f) {  // locfun = 0
-                  rel = 0;
-                  done = true;
-                } else if (r32 <= 2.f - 1e-3f) {  // locfun > 3e-13, far above its FP64 rounding
-                  rel = inside;
-                  done = true;
-                }
-              }
-            }
-            if (!done) {
-              double d;
-              if (lp.loctype == 1)
-                d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
-              else
-                d = fabs(__dsub_rn(so.u[q], zu));
-              if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-                rel = (d <= Rmax);
-              } else {
-                rel = (d <= Rmax) && (sel::locfun(d / L) != 0.0);
-              }
-            }
-            sel = rel || !lp.localise;
-          }
-          nrel_local += rel;
-          const unsigned ball = __ballot_sync(0xffffffffu, sel);
-          if (lane == 0) ts.warp_cnt[warp] = __popc(ball);
-          __syncthreads();
-          int before = 0, total = 0;
+        int incl = rlen;
 #pragma unroll
-          for (int w2 = 0; w2 < kThreads / 32; w2++) {
-            const int cnt = ts.warp_cnt[w2];
-            before += (w2 < warp) ? cnt : 0;
-            total += cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (lane == 31) ts.warp_cnt[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+          const int wsum = (lane < kThreads / 32) ? ts.warp_cnt[lane] : 0;
+          int winc = wsum;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, winc, o);
+            if (lane >= o) winc += t;
           }
-          if (sel) {
-            const int slot = (tail + before + __popc(ball & ((1u << lane) - 1u))) & (kRing - 1);
-            ts.ring_q[slot] = q;
+          if (lane < kThreads / 32) ts.wpre[lane] = winc - wsum;
+          if (lane == 31) ts.rtotal = winc;
+        }
+        __syncthreads();
+        ts.rlo[tid] = rq0;
+        ts.roff[tid] = ts.wpre[warp] + incl - rlen;
+        __syncthreads();
+      }
+      const int32_t ncand = ts.rtotal;
+      const int nr = min(kThreads, nranges - rbase);
+      for (int32_t gb = 0; gb < ncand && !abort; gb += kThreads) {
+        const int32_t gi = gb + tid;
+        int32_t q = 0;
+        int cv = sr.cv0;
+        const bool valid = gi < ncand;
+        if (valid) {
+          // the last range starting at or before gi (empty ranges share the next one's start)
+          int lo_i = 0, hi_i = nr - 1;
+          while (lo_i < hi_i) {
+            const int mid = (lo_i + hi_i + 1) >> 1;
+            if (ts.roff[mid] <= gi) lo_i = mid;
+            else hi_i = mid - 1;
           }
-          __syncthreads();
-          // the plain form's FP64 weights of the new entries (zone_gram.cu), one thread an
-          // entry, so that the FP64 work runs with full warps: sqrt(c) = |w| / sqrt(r)
-          // (c = w (w / r), DCDCovar, covariance.F90:612-619) and c (yo - Hxf). The values
-          // (not the decisions, made above with the reference's rounding) are evaluated with
-          // fewer FP64 operations for the Cartesian and 1-D distances: exp(-d^2 / L^2) needs
-          // no square root or division, locfun(sqrt(d^2) / L) takes 1/L once a zone.
-          if (tid < total) {
-            const int slot = (tail + tid) & (kRing - 1);
-            const int32_t qs = ts.ring_q[slot];
-            double w64;
-            if (fast) {
-              const double du = so.u[qs] - zu;
-              double D2 = du * du;
-              if (lp.loctype == 1) {
-                const double dv = so.v[qs] - zv;
-                D2 = fma(dv, dv, D2);
-              }
-              w64 = (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) ? exp(-(D2 * iL2))
-                                                            : sel::locfun_value(sqrt(D2) * iL);
-            } else {
-              double d;
-              if (lp.loctype == 1)
-                d = sel::distance(so.u[qs], so.v[qs], zu, zv, lp.metric);
-              else
-                d = fabs(__dsub_rn(so.u[qs], zu));
+          q = ts.rlo[lo_i] + (gi - ts.roff[lo_i]);
+          cv = sr.cv0 + ((rbase + lo_i) >> 1);
+        }
+        int sel = 0, rel = 0;
+        if (valid) {
+          // FP32 decisions away from the thresholds, the reference's FP64 evaluation near them
+          bool done = false;
+          if (fastz) {
+            const float d32 = sel::cell_distance32(zc, so, q, cv, lp.loctype == 1);
+            const int inside = (d32 <= r_lo) ? 1 : ((d32 >= r_hi) ? 0 : -1);
+            if (inside >= 0) {
+              const float r32 = d32 * iL32;
               if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
-                const double t = d / L;
-                w64 = exp(-(t * t));
-              } else {
-                w64 = sel::locfun(d / L);
+                rel = inside;
+                done = true;
+              } else if (r32 >= 2.f + 1e-5f) {  // locfun = 0
+                rel = 0;
+                done = true;
+              } else if (r32 <= 2.f - 1e-3f) {  // locfun > 3e-13, far above its FP64 rounding
+                rel = inside;
+                done = true;
               }
             }
-            const double sc = fabs(w64) * isr[qs];
-            ts.ring_s[slot] = sc;
-            ts.ring_t[slot] = sc * sc * so.innov[qs];
           }
-          tail += total;
-          while (tail - head >= KT && !abort) do_tile(KT);
+          if (!done) {
+            double d;
+            if (lp.loctype == 1)
+              d = sel::distance(so.u[q], so.v[q], zu, zv, lp.metric);
+            else
+              d = fabs(__dsub_rn(so.u[q], zu));
+            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+              rel = (d <= Rmax);
+            } else {
+              rel = (d <= Rmax) && (sel::locfun(d / L) != 0.0);
+            }
+          }
+          sel = rel || !lp.localise;
         }
+        nrel_local += rel;
+        const unsigned ball = __ballot_sync(0xffffffffu, sel);
+        if (lane == 0) ts.warp_cnt[warp] = __popc(ball);
+        __syncthreads();
+        int before = 0, total = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < kThreads / 32; w2++) {
+          const int cnt = ts.warp_cnt[w2];
+          before += (w2 < warp) ? cnt : 0;
+          total += cnt;
+        }
+        if (sel) {
+          const int slot = (tail + before + __popc(ball & ((1u << lane) - 1u))) & (kRing - 1);
+          ts.ring_q[slot] = q;
+        }
+        __syncthreads();
+        // the plain form's FP64 weights of the new entries (zone_gram.cu), one thread an
+        // entry, so that the FP64 work runs with full warps: sqrt(c) = |w| / sqrt(r)
+        // (c = w (w / r), DCDCovar, covariance.F90:612-619) and c (yo - Hxf). The values
+        // (not the decisions, made above with the reference's rounding) are evaluated with
+        // fewer FP64 operations for the Cartesian and 1-D distances: exp(-d^2 / L^2) needs
+        // no square root or division, locfun(sqrt(d^2) / L) takes 1/L once a zone.
+        if (tid < total) {
+          const int slot = (tail + tid) & (kRing - 1);
+          const int32_t qs = ts.ring_q[slot];
+          double w64;
+          if (fast) {
+            const double du = so.u[qs] - zu;
+            double D2 = du * du;
+            if (lp.loctype == 1) {
+              const double dv = so.v[qs] - zv;
+              D2 = fma(dv, dv, D2);
+            }
+            w64 = (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) ? exp(-(D2 * iL2))
+                                                          : sel::locfun_value(sqrt(D2) * iL);
+          } else {
+            double d;
+            if (lp.loctype == 1)
+              d = sel::distance(so.u[qs], so.v[qs], zu, zv, lp.metric);
+            else
+              d = fabs(__dsub_rn(so.u[qs], zu));
+            if (lp.weight == OAKG_WEIGHT_GAUSS_CUTOFF) {
+              const double t = d / L;
+              w64 = exp(-(t * t));
+            } else {
+              w64 = sel::locfun(d / L);
+            }
+          }
+          const double sc = fabs(w64) * isr[qs];
+          ts.ring_s[slot] = sc;
+          ts.ring_t[slot] = sc * sc * so.innov[qs];
+        }
+        tail += total;
+        while (tail - head >= KT && !abort) do_tile(KT);
       }
+      __syncthreads();  // the block's ranges consumed before the next block overwrites them
     }
     if (!abort && tail > head) do_tile(tail - head);
     if (abort) break;
