@@ -75,8 +75,8 @@ def workload_config(c, scale):
     return {"workload": c.name, "zones": int(c.Z), "n": int(c.n), "N": int(c.N), "m": int(c.m),
             "localisation": "Gaspari-Cohn locfun(d/6), maxLength 12 cells",
             "precision": "fp64 (plain form: FP64 selection, weights, eigensolve and update; "
-                         "the Gram as exact integer products of 8-bit slices on the BF16 "
-                         "tensor cores)",
+                         "the Gram and the square-root transform's U (I+L)^-1/2 U^T as exact "
+                         "integer products of 8-bit slices on the BF16 tensor cores)",
             "horizontal_scale": scale,
             "l2": "inputs larger than L2 (Sf and Sa 664 MB each at full scale)"}
 
@@ -229,7 +229,9 @@ class ClockSampler:
 def algorithmic_work(c, nobs, stage):
     """Algorithmic FP64 flops of one launch of a stage (per-zone counts x zones):
     gram: p N (N+1) + 2 p N   (lower-triangular HS^T diag(c) HS plus HS^T diag(c) d)
-    eig:  9 N^3 (Householder tridiagonalisation + QR with vectors) + 2 N^3 + 4 N^2 (T, ampl)
+    eig:  9 N^3 (Householder tridiagonalisation + QR with vectors) + 2 N^3 + 4 N^2 (T, ampl),
+          less T_sym's N^2 (N+1) where it runs on the tensor cores (N <= 64): the count is
+          the FP64-pipe work, set against the FP64 peak
     update: 2 nz N^2 + 2 nz N (Sf T and Sf ampl), zones with observations."""
     N = c.N
     act = nobs > 0
@@ -238,7 +240,8 @@ def algorithmic_work(c, nobs, stage):
     if stage == "gram":
         return float(np.sum(p * N * (N + 1) + 2 * p * N))
     if stage == "eig":
-        return float(act.sum() * (11.0 * N ** 3 + 4.0 * N ** 2))
+        tsym_tc = float(N * N * (N + 1)) if N <= 64 else 0.0
+        return float(act.sum() * (11.0 * N ** 3 + 4.0 * N ** 2 - tsym_tc))
     return float(np.sum(2 * nz * N * N + 2 * nz * N))
 
 
@@ -607,6 +610,9 @@ def main():
         "roofline": {"kernel": kernel, "bound": "fp64", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak if peak > 0 else None,
                      "peak_source": "measured FP64 FMA loop (oakg_fp64_peak) on this GPU",
+                     "kernels": ("E1-E4: k_eig_tridiag, k_eig_tridiag_values, "
+                                 "k_eig_vectors_fp64, k_eig_transform, k_zone_tsym_oz"
+                                 if kernel == "k_zone_eig_fp64" else kernel),
                      "traffic": traffic,
                      "algorithmic_flops_per_launch": work},
         "cpu_baseline": cpu,
