@@ -48,8 +48,6 @@ static_assert(2 * kNoAllocMaxN * kNoAllocMaxN * 8 + 7 * kNoAllocMaxN * 8 + 16 + 
                   kScratchBytes,
               "scratch array too small for the largest ensemble size");
 
-unsigned char* g_scratch_dev[64] = {};
-
 __global__ void k_noalloc_init(int64_t* zone_start, int64_t n, int32_t* nobs, int32_t has_obs) {
   zone_start[0] = 0;
   zone_start[1] = n;
@@ -92,19 +90,15 @@ extern "C" int oakg_analysis_noalloc(const oakg_dims* dims, const double* xf, co
   if (m > 0 && (!Hxf || !yo || !HSf || !r_diag))
     return fail(OAKG_ERR_ARGS, "Hxf, yo, HSf and r_diag are required when m > 0");
 
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (dev < 0 || dev >= 64) return fail(OAKG_ERR_CUDA, "device index out of range");
-  if (!g_scratch_dev[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
-    g_scratch_dev[dev] = static_cast<unsigned char*>(p);
-  }
+  cudaError_t e;
+  // the scratch's address, looked up on every call (a host call): a cached address would go
+  // stale if the context were reset and the module reloaded
+  void* scratch_p = nullptr;
+  e = cudaGetSymbolAddress(&scratch_p, g_noalloc_scratch);
+  if (e != cudaSuccess || !scratch_p) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-  double* base = reinterpret_cast<double*>(g_scratch_dev[dev]);
+  double* base = reinterpret_cast<double*>(scratch_p);
   double* d_G = base;
   double* d_Z = d_G + (size_t)N * N;
   double* d_aux = d_Z + (size_t)N * N;
