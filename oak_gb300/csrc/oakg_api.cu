@@ -334,9 +334,14 @@ int run_chunks(Ctx* c, const ChunkArgs& a, int32_t** status_all, double* t_gram,
   int64_t chunk = c->chunk_override > 0 ? c->chunk_override
                                         : (int64_t)(chunk_budget_bytes() / per_zone);
   // host-memory calls: the Sf rows of every chunk go in while the selection, Gram and
-  // eigensolve stages run (they do not read Sf); the zones are not split further for it, as
-  // smaller chunks leave SMs idle in the per-zone stages
+  // eigensolve stages run (they do not read Sf). The Sa / xa rows of a chunk go out while the
+  // next chunk computes, so large calls are split into kPipeChunks chunks (of at least
+  // kPipeMinZones zones, which keep every SM busy in the per-zone stages): only the last
+  // chunk's output copy is left behind the kernels
   const bool pipe = a.sf_host != nullptr && mode == RunMode::kTimed;
+  constexpr int64_t kPipeChunks = 4, kPipeMinZones = 4096;
+  if (pipe && c->chunk_override <= 0 && a.Z >= kPipeChunks * kPipeMinZones)
+    chunk = std::min<int64_t>(chunk, (a.Z + kPipeChunks - 1) / kPipeChunks);
   if (chunk < 1) chunk = 1;
   if (chunk > a.Z) chunk = a.Z;
   R *d_G, *d_gv, *d_za, *d_aux, *d_zvec;
