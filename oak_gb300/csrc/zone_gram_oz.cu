@@ -17,8 +17,10 @@
 //   d_0 in [-64, 64] and d_1..d_6 in [-128, 127] (the bytes of F + 0x80808080808080 minus 128);
 //   every digit is exact in BF16.
 //   Then G_ab = 2^(E_a + E_b - 12) sum_L 256^-L level_L(a, b), level_L = sum_{p+q=L} D_p^T D_q
-//   (D_p the digit-p matrix of the zone's rows), for levels 0..6; the levels from 7 on weigh
-//   below 2^-56 of the column scale and are left out. A K-tile of 64 observations is staged as
+//   (D_p the digit-p matrix of the zone's rows), for levels 0..6. Levels 7..12 are left out:
+//   a row adds at most 6 x 2^14 x 256^5 = 1.5 x 2^56 to level 7 against 2^108 = F_a F_b at the
+//   column bounds, so they weigh at most ~2^-51.4 of 2^(E_a + E_b) a row when every digit sits
+//   at its bound with one sign (far less for data). A K-tile of 64 observations is staged as
 //   7 digit slices (64 members x 64 observations of BF16, K-major, 128-byte swizzle) and each
 //   K-step of 16 observations issues tcgen05.mma kind::f16 (BF16 x BF16 -> FP32) with
 //   A = [D_p ; D_(p+1)] (M = 128; only rows 0-63 are read back) and B = the run of slices whose
@@ -27,11 +29,13 @@
 //   Exactness: a digit product is at most 2^14 (2^13 with d_0), so the FP32 sums of levels 0..3
 //   stay exact integers below 2^24 over 256 observations; the accumulators are read every 4
 //   K-tiles and added into 64-bit integer sums (levels 0..3) and an FP32 sum of
-//   level_4 + level_5 / 256 + level_6 / 65536 (whose rounding weighs below 2^-56 of the column
-//   scale). At the end of the zone G = 2^(E_a + E_b - 36) (v + V456 / 256) with
-//   v = ((L0 256 + L1) 256 + L2) 256 + L3 as a 64-bit integer, converted once to FP64.
-//   The error of G is therefore the truncation of X to 54 bits below its column scale (and the
-//   dropped levels), not the length of the sums: about 2^-53 of max|X_a| max|X_b| per term.
+//   level_4 + level_5 / 256 + level_6 / 65536 (its FP32 rounding, about an ulp of level 4 per
+//   read, weighs ~2^-52 of 2^(E_a + E_b) per 256 observations). At the end of the zone
+//   G = 2^(E_a + E_b - 36) (v + V456 / 256) with v = ((L0 256 + L1) 256 + L2) 256 + L3 as a
+//   64-bit integer, converted once to FP64. The error of G is therefore the rounding of X to
+//   the fixed point (2^-54 of its column scale) and the dropped levels, not the length of the
+//   sums: at most ~2^-51 of 2^(E_a + E_b) per term, typically near 2^-53 (the CPU model of
+//   these steps, tests/test_slice_products_model.py, checks the bound and the budgets).
 //
 // The innovation projection g = X^T (sqrt(c) d) (rrsqrt.F90:142) is accumulated in FP64 by the
 // staging threads (one FMA per staged element).
