@@ -778,23 +778,79 @@ __global__ void k_oz_exponents(int N, const unsigned long long* __restrict__ mx,
 // with a = T_sym u_v / c_v, g = (T_sym u_w - (u_v . u_w) a) / c_w and b = (1 - s_v) T_sym v.
 // T_sym v and the row sums (T_sym u_w = w rowsum + T_sym e_N) are accumulated while T_sym is
 // formed; the update is then one FMA and one add an element.
-// One CTA of 512 threads per SM (persistent, zones strided); the shared-memory request is
-// sized so that no second CTA (which would wait for the tensor memory) shares an SM.
+// Pipeline per CTA (one of 512 threads per SM, zones strided): while zone i's MMAs run, zone
+// i + 1's U and scalings are copied into shared memory (cp.async); after zone i's accumulator
+// read, zone i + 1 is split and its MMAs issued, and zone i's rotation and T write run beside
+// them. The levels are recombined into FP64 by integer operations (the FP64 pipe carries only
+// the rotation's sums and update). The shared-memory request keeps a second CTA (which would
+// wait for the tensor memory) off the SM.
 constexpr int kTsLd = NB + 1;
 constexpr size_t kTsData = 1024 + (size_t)kBufBytes + kSliceBytes +
-                           (size_t)NB * kTsLd * sizeof(double) + 14 * NB * sizeof(double);
-constexpr size_t kTsDynSmem = (size_t)116 * 1024;
+                           (size_t)NB * kTsLd * sizeof(double) + (size_t)NB * NB * sizeof(double) +
+                           18 * NB * sizeof(double);
+constexpr size_t kTsDynSmem = (size_t)148 * 1024;
 static_assert(kTsData <= kTsDynSmem, "square-root transform shared memory");
 
 struct TsShared {
   unsigned long long mbar;
   uint32_t tmem_base;
-  int32_t emax[NB];  // max_k e(q_k) + e(U_ak) of the zone
-  int32_t E[NB];     // column exponents
+  int32_t emax[NB];  // max_k e(q_k) + e(U_ak) of the zone being split
+  int32_t E[NB];     // column exponents of the zone in the accumulators
   int32_t flag;
-  int32_t bad;
-  double uvuw;       // u_v . u_w
+  int32_t bad[2];    // non-finite input, by zone parity
+  double uvuw;       // u_v . u_w of the current zone
 };
+
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// vt 2^e2 rounded to nearest even, by integer operations (the conversion and scaling FP64
+// instructions avoided); |vt| < 2^63. Outside FP64's normal range the FP64 operations decide.
+__device__ __forceinline__ double scaled_i64(long long vt, int e2) {
+  if (vt == 0) return 0.0;
+  const unsigned long long sgn = vt < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long m = vt < 0 ? (unsigned long long)(-vt) : (unsigned long long)vt;
+  const int lz = __clzll((long long)m);
+  const int be = 63 - lz + e2 + 1023;
+  if (be < 1 || be > 2045) {
+    int ex = e2 + 1023;
+    ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
+    return (double)vt * __longlong_as_double((long long)ex << 52);
+  }
+  const unsigned long long mm = m << lz;  // leading one at bit 63
+  const unsigned long long mant = (mm >> 11) & 0xFFFFFFFFFFFFFull;
+  const unsigned long long rem = mm & 0x7FFull;
+  const unsigned long long up = (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  return __longlong_as_double((long long)(sgn | (((unsigned long long)be << 52) + mant + up)));
+}
+
+// the seven levels' 8 columns at c0 of this warp's 32 lanes: seven loads, one wait; the empty
+// asm statements tie the registers' uses to the wait
+__device__ __forceinline__ void tmem_ld7x8(uint32_t ta, int c0, uint32_t (&r)[56]) {
+  const uint32_t cols[7] = {0u, 64u, 128u, 192u, 256u, 320u, 384u};
+#pragma unroll
+  for (int L = 0; L < 7; L++)
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r[8 * L]), "=r"(r[8 * L + 1]), "=r"(r[8 * L + 2]), "=r"(r[8 * L + 3]),
+          "=r"(r[8 * L + 4]), "=r"(r[8 * L + 5]), "=r"(r[8 * L + 6]), "=r"(r[8 * L + 7])
+        : "r"(ta + cols[L] + (uint32_t)c0));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 56; q += 14)
+    asm volatile(""
+                 : "+r"(r[q]), "+r"(r[q + 1]), "+r"(r[q + 2]), "+r"(r[q + 3]), "+r"(r[q + 4]),
+                   "+r"(r[q + 5]), "+r"(r[q + 6]), "+r"(r[q + 7]), "+r"(r[q + 8]),
+                   "+r"(r[q + 9]), "+r"(r[q + 10]), "+r"(r[q + 11]), "+r"(r[q + 12]),
+                   "+r"(r[q + 13])
+                 :
+                 : "memory");
+}
 
 __global__ void __launch_bounds__(kThreads, 1)
     k_zone_tsym_oz(int N, int32_t nzc, double* __restrict__ GT, const double* __restrict__ aux,
@@ -807,13 +863,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* tile = dyn_raw + pad;  // the 7 slices and the zero slice past them
   const uint32_t tile_addr = raw_addr + pad;
   double* Ts = reinterpret_cast<double*>(tile + kBufBytes + kSliceBytes);  // [NB][kTsLd]
-  double* vv = Ts + NB * kTsLd;  // v
-  double* uv = vv + NB;          // u_v
-  double* pv = uv + NB;          // [4][NB] partial T_sym v (column groups)
-  double* ps = pv + 4 * NB;      // [4][NB] partial row sums
-  double* ar = ps + 4 * NB;      // a
-  double* cr = ar + NB;          // (b - g) w
-  double* gr = cr + NB;          // g
+  double* Upre = Ts + NB * kTsLd;  // next zone's U slot, as stored (U_ak at k N + a)
+  double* qpre = Upre + NB * NB;   // next zone's (1 + lambda)^-1/4
+  double* vpre = qpre + NB;        // next zone's v
+  double* vvb = vpre + NB;         // [2][NB] v by zone parity
+  double* uv = vvb + 2 * NB;       // u_v of the current zone
+  double* pv = uv + NB;            // [4][NB] partial T_sym v (column groups)
+  double* ps = pv + 4 * NB;        // [4][NB] partial row sums
+  double* ar = ps + 4 * NB;        // a
+  double* cr = ar + NB;            // (b - g) w
+  double* gr = cr + NB;            // g
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int a = tid & (NB - 1), kq = tid >> 6;  // member a; rows 8 kq .. 8 kq + 7 of X
   const uint32_t mbar = smem_u32(&ts.mbar);
@@ -838,35 +897,42 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = ts.tmem_base;
   const double wv = 1.0 / sqrt((double)N);
   const double cw = 1.0 + wv, icw = 1.0 / cw;
+  const int nmine = (nzc - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
   uint32_t ph = 0;
   bool pending = false;  // an MMA group whose completion was not observed (timeout)
-  for (int32_t zl = blockIdx.x; zl < nzc; zl += gridDim.x) {
-    if (nobs[zl] == 0) continue;  // block-uniform
-    const double* ax = aux + (int64_t)zl * (5 * N + 2);
-    const double* Uz = Zg + (int64_t)zl * N * N;
-    // this thread's 8 elements of X (q_k, U_ak for k = 8 kq + i) and their exponent bound
+
+  // zone number i of this CTA's share into Upre / qpre / vpre (asynchronous copies)
+  auto prefetch = [&](int i) {
+    const int32_t zn = (int32_t)blockIdx.x + i * (int32_t)gridDim.x;
+    const double* src = Zg + (int64_t)zn * N * N;
+    for (int idx = tid; idx < N * N; idx += kThreads) cp_async8(Upre + idx, src + idx);
+    const double* axn = aux + (int64_t)zn * (5 * N + 2);
+    if (tid < N) {
+      cp_async8(qpre + tid, axn + 4 * N + tid);
+      cp_async8(vpre + tid, axn + tid);
+    }
+  };
+  // split the prefetched zone (parity par) into the slices and issue its MMAs; its copies
+  // have landed and are visible (a barrier since this thread's cp_async_wait_all)
+  auto stage_issue = [&](int par) {
     double hv[8], sv[8];
     int em = 0;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
       const int k = 8 * kq + i;
-      hv[i] = (a < N && k < N) ? Uz[k * N + a] : 0.0;
-      sv[i] = (k < N) ? ax[4 * N + k] : 0.0;
+      hv[i] = (a < N && k < N) ? Upre[k * N + a] : 0.0;
+      sv[i] = (k < N) ? qpre[k] : 0.0;
       const int es = (int)(((unsigned long long)__double_as_longlong(sv[i]) >> 52) & 0x7FFu);
       const int eh = (int)(((unsigned long long)__double_as_longlong(hv[i]) >> 52) & 0x7FFu);
       if (es != 0 && eh != 0 && es != 0x7FF && eh != 0x7FF) em = max(em, es + eh);
     }
     if (em > 0) atomicMax(&ts.emax[a], em);
-    if (tid == 0) ts.bad = 0;
-    if (rotate && tid < NB) vv[tid] = (tid < N) ? ax[tid] : 0.0;
-    __syncthreads();  // emax and v complete
-    const double sgv = signbit(vv[N - 1]) ? -1.0 : 1.0;  // s_v (rotate only)
+    if (tid == 0) ts.bad[par] = 0;
+    if (tid < NB) vvb[par * NB + tid] = (rotate && tid < N) ? vpre[tid] : 0.0;
+    __syncthreads();  // maxima complete; the previous zone's exponents no longer read
     const int ema = ts.emax[a];
     const int Ea = (ema > 0) ? ema - 2044 : 0;
-    if (tid < NB) {  // a == tid
-      ts.E[tid] = Ea;
-      if (rotate) uv[tid] = vv[tid] + ((tid == N - 1) ? sgv : 0.0);
-    }
+    if (tid < NB) ts.E[tid] = Ea;  // a == tid
     int bad = 0;
     uint32_t pk[kDigits][4];
 #pragma unroll
@@ -894,18 +960,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int p = 0; p < kDigits; p++)
       *reinterpret_cast<uint4*>(tile + p * kSliceBytes + tile_off(a, kq)) =
           make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
-    if (bad) atomicOr(&ts.bad, 1);
-    if (rotate && warp == 1) {  // u_v . u_w, u_w = w 1 + e_N
-      double sdot = 0.0;
-      for (int j = lane; j < N; j += 32) {
-        const double uj = vv[j] + ((j == N - 1) ? sgv : 0.0);
-        sdot = fma(uj, wv + ((j == N - 1) ? 1.0 : 0.0), sdot);
-      }
-      for (int o = 16; o > 0; o >>= 1) sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
-      if (lane == 0) ts.uvuw = sdot;
-    }
+    if (bad) atomicOr(&ts.bad[par], 1);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();  // tile staged; every emax read done; E, u_v, u_v . u_w published
+    __syncthreads();  // slices staged; Upre, qpre, vpre and the maxima read
     if (tid < NB) ts.emax[tid] = 0;
     if (tid == 0) {
       fence_after();
@@ -930,8 +987,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       mma_commit(mbar);
-      if (!mbar_wait(mbar, ph)) ts.flag = 1;
     }
+  };
+
+  if (nmine > 0) {
+    prefetch(0);
+    cp_async_wait_all();
+    __syncthreads();
+    stage_issue(0);
+    if (nmine > 1) prefetch(1);
+  }
+  for (int i = 0; i < nmine; i++) {
+    const int par = i & 1;
+    const int32_t zl = (int32_t)blockIdx.x + i * (int32_t)gridDim.x;
+    if (tid == 0 && !mbar_wait(mbar, ph)) ts.flag = 1;
     ph ^= 1u;
     __syncthreads();  // MMA completion (or the timeout) published
     if (ts.flag) {
@@ -940,40 +1009,36 @@ __global__ void __launch_bounds__(kThreads, 1)
       break;
     }
     fence_after();
+    const double* vv = vvb + par * NB;
     // T_sym from the accumulators: lanes 0-63 (rows j) are read by warps 0, 1, 4, 5, 8, 9,
     // 12, 13; warp group cg takes columns 16 cg .. 16 cg + 15 of all seven levels, and its
-    // partial sums of T_sym v and of the row
+    // partial sums of T_sym v and of the row. Warp 2 forms u_v and u_v . u_w meanwhile.
     if ((warp & 3) < 2) {
       const int qd = warp & 3, cg = warp >> 2;
       const int j = 32 * qd + lane;
       const uint32_t ta = tmem + ((uint32_t)(32 * qd) << 16);
-      const bool zbad = ts.bad != 0;
+      const bool zbad = ts.bad[par] != 0;
       const int Ej = ts.E[j];
       double sv_part = 0.0, sr_part = 0.0;
 #pragma unroll 1
       for (int h8 = 0; h8 < 2; h8++) {
         const int c0 = 16 * cg + 8 * h8;
-        float l0[8], l1[8], l2[8], l3[8], l4[8], l5[8], l6[8];
-        tmem_ld8(ta + c0, l0);
-        tmem_ld8(ta + 64 + c0, l1);
-        tmem_ld8(ta + 128 + c0, l2);
-        tmem_ld8(ta + 192 + c0, l3);
-        tmem_ld8(ta + 256 + c0, l4);
-        tmem_ld8(ta + 320 + c0, l5);
-        tmem_ld8(ta + 384 + c0, l6);
+        uint32_t r[56];
+        tmem_ld7x8(ta, c0, r);
 #pragma unroll
         for (int t = 0; t < 8; t++) {
           const int c = c0 + t;
           const long long v =
-              (((long long)__float2int_rn(l0[t]) * 256 + __float2int_rn(l1[t])) * 256 +
-               __float2int_rn(l2[t])) * 256 +
-              __float2int_rn(l3[t]);
+              (((long long)__float2int_rn(__uint_as_float(r[t])) * 256 +
+                __float2int_rn(__uint_as_float(r[8 + t]))) * 256 +
+               __float2int_rn(__uint_as_float(r[16 + t]))) * 256 +
+              __float2int_rn(__uint_as_float(r[24 + t]));
           // 256 V456 is below 2^31 in magnitude (level 4 below 5 x 64 x 2^14)
-          const float f456 = fmaf(l6[t], 1.f / 65536.f, fmaf(l5[t], 1.f / 256.f, l4[t]));
+          const float f456 = fmaf(__uint_as_float(r[48 + t]), 1.f / 65536.f,
+                                  fmaf(__uint_as_float(r[40 + t]), 1.f / 256.f,
+                                       __uint_as_float(r[32 + t])));
           const long long vt = v * 65536 + (long long)__float2int_rn(f456 * 256.f);
-          int ex = Ej + ts.E[c] - 52 + 1023;
-          ex = ex < 1 ? 1 : (ex > 2046 ? 2046 : ex);
-          double val = (double)vt * __longlong_as_double((long long)ex << 52);
+          double val = scaled_i64(vt, Ej + ts.E[c] - 52);
           if (zbad) val = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input
           Ts[j * kTsLd + c] = val;
           if (rotate) {
@@ -986,38 +1051,55 @@ __global__ void __launch_bounds__(kThreads, 1)
         pv[cg * NB + j] = sv_part;
         ps[cg * NB + j] = sr_part;
       }
+    } else if (warp == 2 && rotate) {  // u_v and u_v . u_w, u_w = w 1 + e_N
+      const double sgv = signbit(vv[N - 1]) ? -1.0 : 1.0;
+      double sdot = 0.0;
+      for (int jj = lane; jj < NB; jj += 32) {
+        const double u = (jj < N) ? vv[jj] + ((jj == N - 1) ? sgv : 0.0) : 0.0;
+        uv[jj] = u;
+        sdot = fma(u, wv + ((jj == N - 1) ? 1.0 : 0.0), sdot);
+      }
+      for (int o = 16; o > 0; o >>= 1) sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
+      if (lane == 0) ts.uvuw = sdot;
     }
+    if (i + 1 < nmine) cp_async_wait_all();  // the next zone's copies (this thread's)
     fence_before();
-    __syncthreads();  // T_sym and the partial sums complete; tensor memory read
+    __syncthreads();  // T_sym, sums, u_v published; tensor memory read; next zone landed
+    if (i + 1 < nmine) {
+      stage_issue(par ^ 1);  // the next zone's MMAs run beside this zone's rotation
+      if (i + 2 < nmine) prefetch(i + 2);
+    }
+    if (nobs[zl] == 0) continue;  // block-uniform: no T for a zone without observations
     double* Gz = GT + (int64_t)zl * N * N;
     if (rotate) {
+      const double sgv = signbit(vv[N - 1]) ? -1.0 : 1.0;
       if (tid < N) {
-        const int i = tid;
-        const double tvi = (pv[i] + pv[NB + i]) + (pv[2 * NB + i] + pv[3 * NB + i]);  // T_sym v
-        const double rsi = (ps[i] + ps[NB + i]) + (ps[2 * NB + i] + ps[3 * NB + i]);
-        const double tlast = Ts[i * kTsLd + N - 1];
+        const int r = tid;
+        const double tvi = (pv[r] + pv[NB + r]) + (pv[2 * NB + r] + pv[3 * NB + r]);  // T_sym v
+        const double rsi = (ps[r] + ps[NB + r]) + (ps[2 * NB + r] + ps[3 * NB + r]);
+        const double tlast = Ts[r * kTsLd + N - 1];
         const double ai = fma(sgv, tlast, tvi) / (1.0 + fabs(vv[N - 1]));  // T_sym u_v / c_v
         const double gi = fma(-ts.uvuw, ai, fma(wv, rsi, tlast)) * icw;
-        ar[i] = ai;
-        gr[i] = gi;
-        cr[i] = ((1.0 - sgv) * tvi - gi) * wv;
+        ar[r] = ai;
+        gr[r] = gi;
+        cr[r] = ((1.0 - sgv) * tvi - gi) * wv;
       }
       __syncthreads();
       for (int idx = tid; idx < N * N; idx += kThreads) {
-        const int i = idx / N, j = idx - i * N;
-        double t = fma(-ar[i], uv[j], Ts[i * kTsLd + j]) + cr[i];
-        if (j == N - 1) t -= gr[i];
+        const int r = idx / N, c = idx - r * N;
+        double t = fma(-ar[r], uv[c], Ts[r * kTsLd + c]) + cr[r];
+        if (c == N - 1) t -= gr[r];
         Gz[idx] = t;
       }
     } else {
       for (int idx = tid; idx < N * N; idx += kThreads) {
-        const int i = idx / N, j = idx - i * N;
-        Gz[idx] = Ts[i * kTsLd + j];
+        const int r = idx / N, c = idx - r * N;
+        Gz[idx] = Ts[r * kTsLd + c];
       }
     }
-    __syncthreads();  // T_sym, the sums and the coefficients consumed before the next zone
   }
-  // teardown: no MMA may still write tensor memory when it is freed
+  // teardown: no MMA may still write tensor memory when it is freed, no copy still land
+  cp_async_wait_all();
   if (pending && tid == 0) mbar_wait(mbar, ph ^ 1u);
   fence_before();
   __syncthreads();
