@@ -1,4 +1,6 @@
-// K1 + K2 of the plain (FP64) form on the tensor cores, ensembles of up to 64 members.
+// The plain (FP64) form's products on the tensor cores, ensembles of up to 64 members: K1 + K2
+// (selection and the Gram, k_zone_gram_oz) and E4 of the eigensolve (the square-root transform
+// T = U (I+L)^-1/2 U^T Omega, k_zone_tsym_oz, further below).
 //
 // Selection and weights are those of zone_gram.cu (assimilation.F90:3683-3771): the relevance
 // decisions of the tensor-core mixed kernel (FP32 distances away from the thresholds, the
@@ -41,7 +43,8 @@
 // staging threads (one FMA per staged element).
 //
 // Pipeline per CTA (one zone at a time, one CTA of 512 threads per SM: its shared memory and
-// the 512 tensor-memory columns admit no second one): candidates are tested 512 at a time;
+// the 512 tensor-memory columns admit no second one): candidates are tested 512 at a time
+// (a zone's cell-row ranges flattened into one index space);
 // selected observations go to a ring, their FP64 weights are computed one thread an entry
 // (|w| / sqrt(r) and w^2 / r (yo - Hxf)); every full K-tile is
 // staged into one of two shared buffers (7 slices) and handed to the tensor core by one thread
